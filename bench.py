@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 tuning engine: candidates/s on the 8-state, 65,536-candidate workload.
+
+A step is one full evaluation of 65,536 candidate gain sets on the 8-state
+nonlinear plant (10,000 simulation steps, 400 sweep frequencies): simulation,
+LIN_A + FP64 eigensolve, modal fit, modal solve, nominal closed-loop check and
+margin sweep, producing the INFO cost rows.
+
+* value -- candidates/s with gains and INFO rows resident in HBM (ce_evaluate_device);
+* e2e   -- candidates/s through the C ABI with pinned host buffers (ce_evaluate:
+           H2D gains + INFO rows, the pipeline, D2H INFO rows, every step);
+* roofline -- the dominant kernel, timed live with CUDA events on its stream;
+* cpu_baseline -- the CPU oracle (a C port of the reference method, OpenMP) on a
+           bounded sample of the same workload on this host's cores;
+* fp64_form -- the same pipeline with every stage in FP64 (the plain FP64 form).
+
+`--impl reference` times the reference method on the host cores instead: the
+reference's Eigen host path does not build here (Eigen is not vendored), so the
+C port of its method in oracle/ stands in for it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "tuning candidates/s (8-state, 64K batch)"
+UNIT = "candidates/s"
+
+
+def workload_args(a):
+    return dict(n=a.candidates, time=a.time, freq=a.freq)
+
+
+def sim_ops_per_step(ns, nd, nw, n_instr):
+    """FP32 operations of one simulation step (FMA, add and mul each count 1)."""
+    dots = 4 * ns + 2                      # K.(hi,lo), C.(hi,lo), D u, u_raw
+    observer = ns * (2 * ns + 2)           # (A-I)(hi,lo), B u, L yerr
+    plant = nd * (2 * nd + nw + 1)         # (Ad-I)(hi,lo), Bw W, Bu u
+    dfadd = 11 * (ns + nd)                 # double-float accumulation
+    return dots + observer + plant + dfadd + 5 + n_instr
+
+
+class ClockSampler:
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms",
+                                       "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self, gpu_index=0):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[0] == str(gpu_index):
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(problem, seconds: float, threads: int):
+    from oracle import oracle as O
+    orc = O.Oracle(problem.config_text, problem.plant, threads=threads)
+    n_total = problem.cuda_mx.shape[0]
+    probe = min(64, n_total)
+    t0 = time.perf_counter()
+    orc.evaluate(problem.cuda_mx[:probe], problem.info_mx[:probe])
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    n_s = int(min(n_total, max(probe, rate * seconds)))
+    t0 = time.perf_counter()
+    orc.evaluate(problem.cuda_mx[:n_s], problem.info_mx[:n_s])
+    dt = time.perf_counter() - t0
+    return {"value": n_s / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n_s} of the {n_total} candidates, full horizon, oracle C port with OpenMP ({dt:.1f} s)"}
+
+
+def run_reference(a, rank, world):
+    from controllerengine_gb300 import synth
+    if rank != 0:
+        return
+    problem = synth.eight_state(**workload_args(a))
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    orc = O.Oracle(problem.config_text, problem.plant, threads=threads)
+    probe = 64
+    t0 = time.perf_counter()
+    orc.evaluate(problem.cuda_mx[:probe], problem.info_mx[:probe])
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    n_s = int(min(problem.cuda_mx.shape[0], max(probe, rate * a.ref_step_seconds)))
+    for _ in range(a.warmup):
+        orc.evaluate(problem.cuda_mx[:min(n_s, 256)], problem.info_mx[:min(n_s, 256)])
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        sl = slice((k * n_s) % (problem.cuda_mx.shape[0] - n_s + 1), None)
+        g = problem.cuda_mx[sl][:n_s]
+        orc.evaluate(g, problem.info_mx[sl][:g.shape[0]])
+    dt = time.perf_counter() - t0
+    value = n_s * a.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 eigensolve)", "data": "synthetic (seeded eight_state workload)", "impl": "reference",
+            "config": {"workload": "eight_state: 65536 candidates, 8-state plant, 4 nonlinear terms, 10000 steps, "
+                                   "400 sweep points; each step a bounded sample",
+                       "candidates_per_step": n_s, "time": a.time, "freq": a.freq},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n_s} candidates per step, full horizon; the reference's Eigen host "
+                                       "path is not buildable here (Eigen not vendored), its method is timed "
+                                       "through the C port in oracle/"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--candidates", type=int, default=65536)
+    ap.add_argument("--time", type=int, default=10000)
+    ap.add_argument("--freq", type=int, default=400)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from controllerengine_gb300 import build, synth
+    build.build()
+    import controllerengine_gb300 as ce
+    from controllerengine_gb300.engine import measure_fma_rate
+
+    problem = synth.eight_state(seed=2 + rank, **workload_args(a))  # each rank its own candidates (weak scaling)
+    n = problem.cuda_mx.shape[0]
+    cfg = ce.EngineConfig.parse(problem.config_text)
+    sess = ce.Session(cfg, problem.plant)
+
+    dev = torch.device("cuda", local)
+    g = torch.from_numpy(problem.cuda_mx).to(dev)
+    info_in = torch.from_numpy(problem.info_mx).to(dev)
+    info_out = torch.empty_like(info_in)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+
+    def step():
+        sess.evaluate_device(n, g.data_ptr(), info_in.data_ptr(), info_out.data_ptr(), stream=stream.cuda_stream)
+
+    for _ in range(a.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    sess.set_profiling(True)
+    l0 = sess.kernel_launches
+    clocks = ClockSampler()
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        flush.zero_()  # L2 flush between timed iterations, outside the events
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop(local)
+    launches = sess.kernel_launches - l0
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    stages = sess.stage_times()
+    sess.set_profiling(False)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / a.steps
+    value = world * n * a.steps / (ms * 1e-3)
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    pin_g = torch.from_numpy(problem.cuda_mx).pin_memory().numpy()
+    pin_i = torch.from_numpy(problem.info_mx).pin_memory().numpy()
+    pin_o = torch.empty(problem.info_mx.shape, dtype=torch.float32).pin_memory().numpy()
+    lib = ce.load_library()
+    import ctypes as C
+    from controllerengine_gb300 import _ffi
+    fp = lambda arr: arr.ctypes.data_as(_ffi._FP)
+    lib.ce_evaluate(sess._h, 0, n, fp(pin_g), fp(pin_i), fp(pin_o))  # warm
+    e2e_steps = max(2, min(a.steps, 3))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = lib.ce_evaluate(sess._h, 0, n, fp(pin_g), fp(pin_i), fp(pin_o))
+        assert rc == 0, _ffi.last_error(lib)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n * e2e_steps / e2e_s
+    h2d = n * (cfg.cuda_mx_width + cfg.info_mx_width) * 4
+    d2h = n * cfg.info_mx_width * 4
+
+    # ---- FP64 form ----
+    fp64 = None
+    if a.fp64_steps > 0:
+        sess.set_precision("fp64")
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.fp64_steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        f_ms = e0.elapsed_time(e1) / a.fp64_steps
+        fp64 = {"value": world * n / (f_ms * 1e-3), "unit": UNIT, "ms_per_step": f_ms,
+                "speedup_of_mixed": (world * n / (ms_per_step * 1e-3)) / (world * n / (f_ms * 1e-3))}
+        sess.set_precision("mixed")
+
+    # ---- roofline of the dominant kernel ----
+    per_launch = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
+    dom = max(per_launch, key=per_launch.get)
+    fp32_rate = measure_fma_rate(False)
+    fp64_rate = measure_fma_rate(True)
+    n_instr = 1 + 1 + 10  # DC, U and the NL instructions of this workload
+    roof = None
+    if dom == "sim":
+        work = sim_ops_per_step(8, 8, 4, n_instr) * a.time * n
+        ach = work / (per_launch[dom] * 1e-3) / 1e12
+        peak = fp32_rate / 1e12
+        roof = {"kernel": "k_sim_mixed<8,8>", "bound": "fp32", "achieved": ach, "peak": peak, "unit": "Tops/s",
+                "frac": ach / peak, "traffic": None,
+                "work_per_launch": f"{sim_ops_per_step(8, 8, 4, n_instr)} FP32 ops/step x {a.time} steps x {n}",
+                "peak_source": "measured FP32 FFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"}
+    else:
+        roof = {"kernel": dom, "bound": "fp32", "achieved": None, "peak": fp32_rate / 1e12, "unit": "Tops/s",
+                "frac": None, "traffic": None}
+    peaks_file = ROOT / "MEASURED_PEAKS.json"
+    hbm_peak = json.loads(peaks_file.read_text())["hbm_gbs"] if peaks_file.exists() else 6800.0
+    win_bytes = n * cfg.fit_steps * 4 * 2  # fit window written by k_sim and read by k_fit
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 eigensolve)", "data": "synthetic (seeded eight_state workload, random-draw plant)",
+        "config": {"workload": "eight_state: 65536 candidates, 8-state plant, 4 nonlinear terms, 10000 steps, "
+                               "400 sweep points", "candidates_per_gpu": n, "time": a.time, "freq": a.freq,
+                   "l2": "256 MB buffer written between timed steps (outside the events)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "stages_ms_per_launch": per_launch,
+        "fit_window_hbm": {"bytes_per_step": win_bytes, "gbs_if_overlapped": win_bytes / (ms_per_step * 1e-3) / 1e9,
+                           "peak_gbs": hbm_peak},
+        "peaks_measured": {"fp32_tops": fp32_rate / 1e12, "fp64_tops": fp64_rate / 1e12},
+        "fp64_form": fp64,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sess.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+// ce_device.cuh -- device arithmetic shared by the kernels.
+//
+// Rounding discipline: every operation whose result must equal the
+// reference's is written with an explicit round-to-nearest intrinsic
+// (__fadd_rn, __fmul_rn, __fmaf_rn, ...), so the compiler can neither
+// contract a multiply-add the reference keeps separate nor split one it
+// fuses.  The reference's device code uses __fmaf_rn / __fadd_rn explicitly
+// in the simulation (ref: src/main.cu:122-155, src/discrete_solves.cu); its
+// host stages (Eigen on x86) never fuse.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include "ce_internal.h"
+
+namespace ce {
+
+// ---- scalar ops in a type-generic, contraction-proof form -------------------
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <typename R> __device__ __forceinline__ R rnan();
+template <> __device__ __forceinline__ float rnan<float>() { return CUDART_NAN_F; }
+template <> __device__ __forceinline__ double rnan<double>() { return CUDART_NAN; }
+
+// ---- double-float accumulation (ref: src/main.cu:129-155) --------------------
+// TwoSum of a and b.
+__device__ __forceinline__ void df_two_sum(float a, float b, float& hi, float& lo) {
+    hi = __fadd_rn(a, b);
+    const float b0 = __fsub_rn(hi, a);
+    lo = __fadd_rn(__fsub_rn(a, __fsub_rn(hi, b0)), __fsub_rn(b, b0));
+}
+// (HI,LO) += (hi,lo): TwoSum of the high parts, low parts folded in, renormalised.
+__device__ __forceinline__ void df_add(float& HI, float& LO, float hi, float lo) {
+    float sh, sl;
+    df_two_sum(HI, hi, sh, sl);
+    const float v = __fadd_rn(__fadd_rn(LO, lo), sl);
+    HI = __fadd_rn(sh, v);
+    LO = __fsub_rn(v, __fsub_rn(HI, sh));
+}
+
+// ---- the instruction interpreter (ref: src/main.cu:260-291) ------------------
+// Evaluates one SKIP-free chain of `n` instructions.  `src` holds the NSRC
+// source values addressed by the instruction column; column `ycol` (if >= 0)
+// addresses `yval` instead (the NL chains' plant-output slot).  The first
+// instruction's running value is the seed when HAS_SEED and the seed is not NaN,
+// else the state under its column; later ones use the running result.
+template <typename R, int NSRC, int MAXC, bool HAS_SEED>
+__device__ __forceinline__ R run_chain(const Instr* __restrict__ ins, int n, const R* src, int ycol, R yval, R seed) {
+    R result = R(0);
+#pragma unroll
+    for (int r = 0; r < MAXC; ++r) {
+        if (r >= n) break;
+        const int op = ins[r].op, col = ins[r].col, ak = ins[r].akind, bk = ins[r].bkind;
+        R pos = R(0);
+#pragma unroll
+        for (int c = 0; c < NSRC; ++c)
+            if (col == c) pos = src[c];
+        if (col == ycol) pos = yval;
+        R prev;
+        if (r == 0) prev = (HAS_SEED && !isnan(seed)) ? seed : pos;
+        else prev = result;
+        const R a = ak == CE_OPERAND_CONST ? R(ins[r].aval) : (ak == CE_OPERAND_STATE ? pos : prev);
+        const R b = bk == CE_OPERAND_CONST ? R(ins[r].bval) : (bk == CE_OPERAND_STATE ? pos : prev);
+        switch (op) {
+            case 1: result = radd(a, b); break;
+            case 2: result = rsub(a, b); break;
+            case 3: result = rmul(a, b); break;
+            case 4: result = rdiv(a, b); break;
+            case 5: result = fmin(fmax(prev, a), b); break;
+            case 6: result = R((R(0) < a) - (a < R(0))); break;
+            default: break;  // op outside 1..6: no change, but the chain counts as started
+        }
+    }
+    return result;
+}
+
+// ---- complex arithmetic in a fixed operation order ---------------------------
+template <typename R>
+struct cplx {
+    R re, im;
+};
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
+    return {rsub(rmul(a.re, b.re), rmul(a.im, b.im)), radd(rmul(a.re, b.im), rmul(a.im, b.re))};
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> csub(cplx<R> a, cplx<R> b) {
+    return {rsub(a.re, b.re), rsub(a.im, b.im)};
+}
+// a / b as a*conj(b) / |b|^2, each part divided by |b|^2.
+template <typename R>
+__device__ __forceinline__ cplx<R> cdiv(cplx<R> a, cplx<R> b) {
+    const R d = radd(rmul(b.re, b.re), rmul(b.im, b.im));
+    const R nr = radd(rmul(a.re, b.re), rmul(a.im, b.im));
+    const R ni = rsub(rmul(a.im, b.re), rmul(a.re, b.im));
+    return {rdiv(nr, d), rdiv(ni, d)};
+}
+__device__ __forceinline__ float cabs_(cplx<float> a) { return hypotf(a.re, a.im); }
+__device__ __forceinline__ double cabs_(cplx<double> a) { return hypot(a.re, a.im); }
+__device__ __forceinline__ float carg_(cplx<float> a) { return atan2f(a.im, a.re); }
+__device__ __forceinline__ double carg_(cplx<double> a) { return atan2(a.im, a.re); }
+// squared modulus; orders pivots like the modulus does, without a libm call
+template <typename R>
+__device__ __forceinline__ R cnorm2(cplx<R> a) {
+    return radd(rmul(a.re, a.re), rmul(a.im, a.im));
+}
+template <typename R>
+__device__ __forceinline__ bool cfinite(cplx<R> a) {
+    return isfinite(a.re) && isfinite(a.im);
+}
+
+// Solve (z I - A) x = b for an NS x NS real A (row stride NS) by complex LU
+// with partial pivoting (largest modulus, compared as re^2+im^2; first on ties), unit-lower forward
+// and column-oriented backward substitution.  Restates the partialPivLu().solve
+// call sites of the reference (ref: src/allmargin.cu:24-29, 37, 103-104).
+// A is read as A[(i*NS + j) * astride].  An exactly zero pivot is left in
+// place, so the solve then produces non-finite values.
+template <typename R, int NS>
+__device__ __forceinline__ void lu_solve_shifted(cplx<R> z, const R* A, int astride, const R* b, cplx<R>* x) {
+    cplx<R> M[NS][NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i)
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+            // z*I - A, with z*I formed as z times (1,0) / (0,0)
+            const cplx<R> zi = (i == j) ? cplx<R>{rsub(rmul(z.re, R(1)), rmul(z.im, R(0))), radd(rmul(z.re, R(0)), rmul(z.im, R(1)))}
+                                        : cplx<R>{rsub(rmul(z.re, R(0)), rmul(z.im, R(0))), radd(rmul(z.re, R(0)), rmul(z.im, R(0)))};
+            M[i][j] = csub(zi, cplx<R>{A[(i * NS + j) * astride], R(0)});
+        }
+    int perm[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        // pivot: largest |M(i,k)|, i >= k, first maximum wins
+        int p = k;
+        R best = cnorm2(M[k][k]);
+#pragma unroll
+        for (int i = k + 1; i < NS; ++i) {
+            const R s = cnorm2(M[i][k]);
+            if (s > best) { best = s; p = i; }
+        }
+        perm[k] = p;
+        if (best != R(0)) {
+            if (p != k) {
+#pragma unroll
+                for (int i = k + 1; i < NS; ++i)
+                    if (i == p) {
+#pragma unroll
+                        for (int j = 0; j < NS; ++j) {
+                            const cplx<R> t = M[k][j];
+                            M[k][j] = M[i][j];
+                            M[i][j] = t;
+                        }
+                    }
+            }
+#pragma unroll
+            for (int i = k + 1; i < NS; ++i) M[i][k] = cdiv(M[i][k], M[k][k]);
+        }
+#pragma unroll
+        for (int i = k + 1; i < NS; ++i)
+#pragma unroll
+            for (int j = k + 1; j < NS; ++j) M[i][j] = csub(M[i][j], cmul(M[i][k], M[k][j]));
+    }
+    // x = P b
+#pragma unroll
+    for (int i = 0; i < NS; ++i) x[i] = cplx<R>{b[i], R(0)};
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        const int p = perm[k];
+#pragma unroll
+        for (int i = k + 1; i < NS; ++i)
+            if (i == p) {
+                const cplx<R> t = x[k];
+                x[k] = x[i];
+                x[i] = t;
+            }
+    }
+    // unit lower, column oriented
+#pragma unroll
+    for (int i = 0; i < NS; ++i)
+#pragma unroll
+        for (int s = i + 1; s < NS; ++s) x[s] = csub(x[s], cmul(x[i], M[s][i]));
+    // upper, column oriented
+#pragma unroll
+    for (int i = NS - 1; i >= 0; --i) {
+        x[i] = cdiv(x[i], M[i][i]);
+#pragma unroll
+        for (int s = 0; s < i; ++s) x[s] = csub(x[s], cmul(x[i], M[s][i]));
+    }
+}
+
+}  // namespace ce

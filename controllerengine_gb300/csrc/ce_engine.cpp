@@ -1,0 +1,794 @@
+// ce_engine.cpp -- sessions, the stage pipeline, the C ABI and RunControllerEngine.
+//
+// The reference's orchestrator (ref: src/main.cu:385-582) runs every stage
+// synchronously, bouncing LIN_A, eigenvalues and AtA/Atb through host memory
+// for the Eigen stages.  Here a session keeps the decoded plant tables and the
+// plant's frequency response on the host (they travel to the kernels in the
+// launch parameters) and a grow-only set of device scratch buffers; one
+// evaluation is six kernel launches on one stream, with the FP64 eigensolve
+// forked onto a second stream so it overlaps the FP32 simulation:
+//
+//   fork ─┬─ k_lina_eig (FP64 pipe) ──┐
+//         └─ k_sim      (FP32 pipe) ──┴─ join ─ k_fit ─ k_modal ─ k_nominal ─ k_sweep
+//
+// Only gains in and cost rows out cross the host boundary.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <memory>
+#include <sstream>
+#include <vector>
+
+#include "ce_host.h"
+
+namespace ce {
+
+thread_local std::string g_last_error;
+
+namespace {
+
+constexpr float PI = 0x1.921fb6p+1f;
+
+// ---- host complex LU: the same algorithm as the device lu_solve_shifted -----
+template <typename R>
+struct hc {
+    R re, im;
+};
+template <typename R>
+hc<R> hmul(hc<R> a, hc<R> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename R>
+hc<R> hsub(hc<R> a, hc<R> b) {
+    return {a.re - b.re, a.im - b.im};
+}
+template <typename R>
+hc<R> hdiv(hc<R> a, hc<R> b) {
+    const R d = b.re * b.re + b.im * b.im;
+    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+
+// x = (z I - A)^{-1} b, A n x n row-major.  Returns false if x is not finite.
+template <typename R>
+bool host_lu_solve(hc<R> z, const R* A, const R* b, int n, hc<R>* x) {
+    hc<R> M[8][8];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const hc<R> zi = (i == j) ? hc<R>{z.re * R(1) - z.im * R(0), z.re * R(0) + z.im * R(1)}
+                                      : hc<R>{z.re * R(0) - z.im * R(0), z.re * R(0) + z.im * R(0)};
+            M[i][j] = hsub(zi, hc<R>{A[i * n + j], R(0)});
+        }
+    int perm[8];
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        R best = M[k][k].re * M[k][k].re + M[k][k].im * M[k][k].im;
+        for (int i = k + 1; i < n; ++i) {
+            const R s = M[i][k].re * M[i][k].re + M[i][k].im * M[i][k].im;
+            if (s > best) {
+                best = s;
+                p = i;
+            }
+        }
+        perm[k] = p;
+        if (best != R(0)) {
+            if (p != k)
+                for (int j = 0; j < n; ++j) std::swap(M[k][j], M[p][j]);
+            for (int i = k + 1; i < n; ++i) M[i][k] = hdiv(M[i][k], M[k][k]);
+        }
+        for (int i = k + 1; i < n; ++i)
+            for (int j = k + 1; j < n; ++j) M[i][j] = hsub(M[i][j], hmul(M[i][k], M[k][j]));
+    }
+    for (int i = 0; i < n; ++i) x[i] = hc<R>{b[i], R(0)};
+    for (int k = 0; k < n; ++k) std::swap(x[k], x[perm[k]]);
+    for (int i = 0; i < n; ++i)
+        for (int s = i + 1; s < n; ++s) x[s] = hsub(x[s], hmul(x[i], M[s][i]));
+    for (int i = n - 1; i >= 0; --i) {
+        x[i] = hdiv(x[i], M[i][i]);
+        for (int s = 0; s < i; ++s) x[s] = hsub(x[s], hmul(x[i], M[s][i]));
+    }
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(x[i].re) || !std::isfinite(x[i].im)) return false;
+    return true;
+}
+
+// C^T x + D
+template <typename R>
+hc<R> host_ctx(const R* C, const hc<R>* x, int n, R D) {
+    hc<R> acc{R(0), R(0)};
+    for (int i = 0; i < n; ++i) {
+        const hc<R> t = hmul(hc<R>{C[i], R(0)}, x[i]);
+        acc = hc<R>{acc.re + t.re, acc.im + t.im};
+    }
+    return hc<R>{acc.re + D, acc.im};
+}
+
+float habs(hc<float> a) { return std::hypot(a.re, a.im); }
+double habs(hc<double> a) { return std::hypot(a.re, a.im); }
+
+}  // namespace
+
+struct Buffers {
+    int64_t cap = 0;
+    int nt = 0, time = 0, pitch = 0, precision = -1;
+    float* gains = nullptr;
+    float* info = nullptr;
+    float* lina = nullptr;
+    void* eig = nullptr;
+    void* ywin = nullptr;
+    void* summ = nullptr;
+    void* ata = nullptr;
+    void* atb = nullptr;
+    int* nominal = nullptr;
+    float* traj = nullptr;
+    int64_t traj_cap = 0;
+    void release() {
+        for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal, (void*)traj})
+            if (p) cudaFree(p);
+        gains = info = lina = traj = nullptr;
+        eig = ywin = summ = ata = atb = nullptr;
+        nominal = nullptr;
+        cap = traj_cap = 0;
+    }
+};
+
+}  // namespace ce
+
+struct ce_session {
+    ce_config cfg{};
+    int n_plants = 0;
+    int precision = CE_PRECISION_MIXED;
+    std::vector<ce::Plant> plants;
+    std::vector<std::string> plant_err;
+    std::vector<float> alpha32;
+    std::vector<double> alpha64;
+    std::vector<float> fgrid32;   // n_plants * freq * 8
+    std::vector<double> fgrid64;
+    float* d_fgrid32 = nullptr;
+    double* d_fgrid64 = nullptr;
+    ce::Buffers buf;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int64_t launches = 0;
+    int device = 0;
+    // stage timing (ce_session_set_profiling)
+    bool profiling = false;
+    struct Pending {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[CE_NUM_STAGES] = {};
+    int64_t stage_n[CE_NUM_STAGES] = {};
+    cudaEvent_t take_event() {
+        if (!event_pool.empty()) {
+            cudaEvent_t e = event_pool.back();
+            event_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        CE_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+};
+
+namespace ce {
+
+namespace {
+
+void set_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return 1;
+    } catch (...) {
+        set_error("unknown error");
+        return 1;
+    }
+}
+
+int fit_pitch(int steps) { return ((steps + 7) / 8) * 8; }
+
+template <typename T>
+void dev_alloc(T*& p, size_t count) {
+    if (count == 0) count = 1;
+    CE_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+}
+
+void ensure_buffers(ce_session* s, int64_t n, bool traj) {
+    Buffers& b = s->buf;
+    const ce_config& c = s->cfg;
+    const int nt = c.total_dim, pitch = fit_pitch(c.fit_steps);
+    const size_t rsz = s->precision == CE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    if (n > b.cap || b.precision != s->precision || b.nt != nt || b.pitch != pitch) {
+        b.release();
+        const int64_t cap = n;
+        dev_alloc(b.gains, (size_t)cap * c.cuda_mx_width);
+        dev_alloc(b.info, (size_t)cap * c.info_mx_width);
+        dev_alloc(b.lina, (size_t)cap * nt * nt);
+        CE_CUDA(cudaMalloc(&b.eig, (size_t)cap * 2 * nt * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.ywin, (size_t)cap * pitch * rsz + 64));
+        CE_CUDA(cudaMalloc(&b.summ, (size_t)cap * 4 * rsz + 64));
+        CE_CUDA(cudaMalloc(&b.ata, (size_t)cap * 4 * nt * nt * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.atb, (size_t)cap * 2 * nt * rsz + 16));
+        dev_alloc(b.nominal, (size_t)cap);
+        b.cap = cap;
+        b.nt = nt;
+        b.pitch = pitch;
+        b.precision = s->precision;
+    }
+    if (traj && n > b.traj_cap) {
+        if (b.traj) cudaFree(b.traj);
+        b.traj = nullptr;
+        dev_alloc(b.traj, (size_t)n * c.time);
+        b.traj_cap = n;
+    }
+}
+
+Run make_run(const ce_session* s, int plant, int64_t n) {
+    const ce_config& c = s->cfg;
+    Run r{};
+    r.n = n;
+    r.ns = c.statespace_dim;
+    r.nd = c.discrete_dim;
+    r.nt = c.total_dim;
+    r.nw = c.nonlin_dim;
+    r.time = c.time;
+    r.fit_start_id = c.fit_start_id;
+    r.fit_steps = c.fit_steps;
+    r.fit_pitch = fit_pitch(c.fit_steps);
+    r.steady_start_id = c.steady_start_id;
+    r.ref_step_id = c.ref_step_id;
+    r.cuda_w = c.cuda_mx_width;
+    r.info_w = c.info_mx_width;
+    r.info_scoring = c.info_scoring;
+    r.info_freqresp = c.info_freqresp;
+    r.info_allmargin = c.info_allmargin;
+    r.info_modal = c.info_modal;
+    r.freq = c.freq;
+    r.ts = c.ts;
+    r.ref_amp = c.ref_amplitude;
+    r.fit_t0 = c.fit_t0;
+    r.fit_t1 = c.fit_t1;
+    r.unstable_err = c.unstable_err;
+    r.eig_fail_err = c.eig_fail_err;
+    r.bandwidth = c.bandwidth;
+    r.damping = c.damping;
+    r.overshoot = c.overshoot;
+    r.sse = c.steady_state_error;
+    r.target_gm = c.target_gm;
+    r.target_pm = c.target_pm;
+    r.target_b = c.target_b;
+    r.alpha = s->alpha32[plant];
+    r.alpha64 = s->alpha64[plant];
+    r.store_traj = 0;
+    return r;
+}
+
+// One evaluation: gains and info rows already on the device in d_gains / d_info.
+void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
+                  bool traj) {
+    if (!s->plant_err[plant].empty()) throw std::runtime_error(s->plant_err[plant]);
+    ensure_buffers(s, n, traj);
+    Buffers& b = s->buf;
+    Run r = make_run(s, plant, n);
+    r.store_traj = traj ? 1 : 0;
+    const Plant& P = s->plants[plant];
+    const int prec = s->precision;
+    const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + (size_t)plant * s->cfg.freq * 8)
+                                                  : (const void*)(s->d_fgrid32 + (size_t)plant * s->cfg.freq * 8);
+    // each launch optionally bracketed by events on the stream it runs on
+    auto timed = [&](int stage, cudaStream_t on, auto&& launch) {
+        if (!s->profiling) {
+            launch();
+            return;
+        }
+        ce_session::Pending pd{stage, s->take_event(), s->take_event()};
+        CE_CUDA(cudaEventRecord(pd.a, on));
+        launch();
+        CE_CUDA(cudaEventRecord(pd.b, on));
+        s->pending.push_back(pd);
+    };
+    CE_CUDA(cudaEventRecord(s->ev_fork, st));
+    CE_CUDA(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    timed(0, s->side, [&] { launch_lina_eig(r, P, prec, d_gains, b.lina, b.eig, s->side); });
+    CE_CUDA(cudaEventRecord(s->ev_join, s->side));
+    timed(1, st, [&] { launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st); });
+    CE_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
+    timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, st); });
+    timed(3, st, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, st); });
+    timed(4, st, [&] { launch_nominal(r, P, prec, d_gains, b.lina, d_info, b.nominal, st); });
+    timed(5, st, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, st); });
+    s->launches += 6;
+}
+
+std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {
+    std::vector<Instr> out;
+    for (const auto& r : rows)
+        if (r.op != 0) out.push_back(Instr{r.op, r.col, r.akind, r.bkind, r.aval, r.bval});
+    return out;
+}
+
+// Build the padded plant of round `p` (ref: src/main.cu:341-383, 390-397).
+void build_plant(const ce_config& c, const ce_plant& in, int p, Plant& P) {
+    std::memset(&P, 0, sizeof(P));
+    const int ns = c.statespace_dim, nd = c.discrete_dim, nw = c.nonlin_dim;
+    for (int i = 0; i < ns; ++i) {
+        for (int j = 0; j < ns; ++j) {
+            P.ss_a[i * MAXS + j] = in.statespace_a[i * ns + j];
+            P.ss_ai[i * MAXS + j] = in.statespace_a_i[i * ns + j];
+        }
+        P.ss_b[i] = in.statespace_b[i];
+        P.ss_c[i] = in.statespace_c[i];
+    }
+    P.ss_d = in.statespace_d[0];
+    const size_t oa = (size_t)p * nd * nd, ov = (size_t)p * nd, ow = (size_t)p * nd * nw;
+    for (int i = 0; i < nd; ++i) {
+        for (int j = 0; j < nd; ++j) {
+            P.d_a[i * MAXD + j] = in.discrete_a[oa + i * nd + j];
+            P.d_ai[i * MAXD + j] = in.discrete_a_i[oa + i * nd + j];
+        }
+        P.d_bu[i] = in.discrete_bu[ov + i];
+        for (int k = 0; k < nw; ++k) P.d_bw[i * MAXW + k] = in.discrete_bw[ow + i * nw + k];
+        P.d_c[i] = in.discrete_c[ov + i];
+    }
+    // margin plant: observer model (batch) or the true linear plant (serial)
+    if (c.serial) {
+        for (int i = 0; i < nd; ++i) {
+            for (int j = 0; j < nd; ++j) P.m_a[i * MAXS + j] = P.d_a[i * MAXD + j];
+            P.m_b[i] = P.d_bu[i];
+            P.m_c[i] = P.d_c[i];
+        }
+        P.m_d = 0.0f;
+    } else {
+        for (int i = 0; i < ns; ++i) {
+            for (int j = 0; j < ns; ++j) P.m_a[i * MAXS + j] = P.ss_a[i * MAXS + j];
+            P.m_b[i] = P.ss_b[i];
+            P.m_c[i] = P.ss_c[i];
+        }
+        P.m_d = P.ss_d;
+    }
+    // instruction tables, decoded with this round's BASE_PARAMS
+    const float* bp = in.base_params + (size_t)p * c.n_params;
+    std::vector<ce_instruction> rows;
+    rows.resize(std::max(c.dc_instructions, 1));
+    decode_instructions(in.dc_info, c.dc_dim, c.dc_instructions, bp, c.n_params, rows.data());
+    rows.resize(c.dc_instructions);
+    auto dc = compact(rows);
+    rows.assign(std::max(c.u_instructions, 1), ce_instruction{});
+    decode_instructions(in.u_info, c.u_dim, c.u_instructions, bp, c.n_params, rows.data());
+    rows.resize(c.u_instructions);
+    auto u = compact(rows);
+    P.n_dc = (int)dc.size();
+    P.n_u = (int)u.size();
+    for (int i = 0; i < P.n_dc; ++i) P.dc[i] = dc[i];
+    for (int i = 0; i < P.n_u; ++i) P.u[i] = u[i];
+    int row = 0;
+    for (int i = 0; i < c.nonlin_dim; ++i) {
+        const int cnt = c.nl_instructions[i];
+        rows.assign(std::max(cnt, 1), ce_instruction{});
+        decode_instructions(in.nl_info + (size_t)row * c.nl_dim, c.nl_dim, cnt, bp, c.n_params, rows.data());
+        rows.resize(cnt);
+        for (auto& r : rows)
+            if (r.col == c.discrete_dim) r.col = MAXD;  // plant output slot (ref: src/main.cu:377)
+        auto nl = compact(rows);
+        P.n_nl[i] = (int)nl.size();
+        for (int k = 0; k < P.n_nl[i]; ++k) P.nl[i][k] = nl[k];
+        row += cnt;
+    }
+}
+
+// Sweep grid and plant response of one plant, float and double forms
+// (ref: src/main.cu:421-428, src/allmargin.cu:11-41).
+void build_fgrid(ce_session* s, int p) {
+    const ce_config& c = s->cfg;
+    const Plant& P = s->plants[p];
+    const int n = c.serial ? c.discrete_dim : c.statespace_dim;
+    const int F = c.freq;
+    float A32[64], B32[8], C32[8];
+    double A64[64], B64[8], C64[8];
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            A32[i * n + j] = P.m_a[i * MAXS + j];
+            A64[i * n + j] = P.m_a[i * MAXS + j];
+        }
+        B32[i] = P.m_b[i];
+        C32[i] = P.m_c[i];
+        B64[i] = P.m_b[i];
+        C64[i] = P.m_c[i];
+    }
+    float* g32 = s->fgrid32.data() + (size_t)p * F * 8;
+    double* g64 = s->fgrid64.data() + (size_t)p * F * 8;
+    const float inc = (logf(c.freq_max) - logf(c.freq_min)) / (float)(F - 1);
+    const double inc64 = (std::log((double)c.freq_max) - std::log((double)c.freq_min)) / (double)(F - 1);
+    for (int w = 0; w < F; ++w) {
+        const float th = expf(logf(c.freq_min) + inc * (float)w) * c.ts;
+        const hc<float> z{cosf(th), sinf(th)};
+        hc<float> x[8];
+        const bool ok = host_lu_solve<float>(z, A32, B32, n, x);
+        const hc<float> Pr = ok ? host_ctx<float>(C32, x, n, P.m_d) : hc<float>{0.0f, 0.0f};
+        float* g = g32 + 8 * w;
+        g[0] = z.re; g[1] = z.im; g[2] = std::atan2(z.im, z.re);
+        g[3] = Pr.re; g[4] = Pr.im; g[5] = habs(Pr); g[6] = ok ? 1.0f : 0.0f; g[7] = 0.0f;
+
+        const double th64 = std::exp(std::log((double)c.freq_min) + inc64 * (double)w) * (double)c.ts;
+        const hc<double> z64{std::cos(th64), std::sin(th64)};
+        hc<double> x64[8];
+        const bool ok64 = host_lu_solve<double>(z64, A64, B64, n, x64);
+        const hc<double> Pr64 = ok64 ? host_ctx<double>(C64, x64, n, (double)P.m_d) : hc<double>{0.0, 0.0};
+        double* h = g64 + 8 * w;
+        h[0] = z64.re; h[1] = z64.im; h[2] = std::atan2(z64.im, z64.re);
+        h[3] = Pr64.re; h[4] = Pr64.im; h[5] = habs(Pr64); h[6] = ok64 ? 1.0 : 0.0; h[7] = 0.0;
+    }
+    // plant scaling at the spec crossover
+    {
+        const float th = c.crossover * c.ts;
+        const hc<float> zc{1.0f * cosf(th), 1.0f * sinf(th)};
+        hc<float> x[8];
+        const bool ok = host_lu_solve<float>(zc, A32, B32, n, x);
+        const float pmag = habs(host_ctx<float>(C32, x, n, P.m_d));
+        if (!ok || !(pmag > 0.0f) || !std::isfinite(pmag))
+            s->plant_err[p] = std::format("allmargin: plant has no finite nonzero gain at crossover = {} rad/s", c.crossover);
+        s->alpha32[p] = 1.0f / pmag;
+        const double th64 = (double)c.crossover * (double)c.ts;
+        const hc<double> zc64{std::cos(th64), std::sin(th64)};
+        hc<double> x64[8];
+        host_lu_solve<double>(zc64, A64, B64, n, x64);
+        s->alpha64[p] = 1.0 / habs(host_ctx<double>(C64, x64, n, (double)P.m_d));
+    }
+}
+
+void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants, ce_session** out) {
+    if (!cfg_in || !plant || !out) fail("ce_session_create: null argument");
+    if (n_plants < 1) fail("ce_session_create: n_plants must be >= 1, got {}", n_plants);
+    auto s = std::make_unique<ce_session>();
+    s->cfg = *cfg_in;
+    const ce_config& c = s->cfg;
+    if (c.statespace_dim < 1 || c.statespace_dim > MAXS || c.discrete_dim < 1 || c.discrete_dim > MAXD ||
+        c.nonlin_dim < 0 || c.nonlin_dim > MAXW || c.total_dim != c.statespace_dim + c.discrete_dim)
+        fail("ce_session_create: config dimensions are out of range or not derived");
+    s->n_plants = n_plants;
+    s->plants.resize(n_plants);
+    s->plant_err.assign(n_plants, std::string());
+    s->alpha32.assign(n_plants, 0.0f);
+    s->alpha64.assign(n_plants, 0.0);
+    s->fgrid32.assign((size_t)n_plants * c.freq * 8, 0.0f);
+    s->fgrid64.assign((size_t)n_plants * c.freq * 8, 0.0);
+    for (int p = 0; p < n_plants; ++p) {
+        build_plant(c, *plant, p, s->plants[p]);
+        build_fgrid(s.get(), p);
+    }
+    CE_CUDA(cudaGetDevice(&s->device));
+    CE_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    CE_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    CE_CUDA(cudaMalloc((void**)&s->d_fgrid32, s->fgrid32.size() * sizeof(float)));
+    CE_CUDA(cudaMalloc((void**)&s->d_fgrid64, s->fgrid64.size() * sizeof(double)));
+    CE_CUDA(cudaMemcpy(s->d_fgrid32, s->fgrid32.data(), s->fgrid32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CE_CUDA(cudaMemcpy(s->d_fgrid64, s->fgrid64.data(), s->fgrid64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    *out = s.release();
+}
+
+void collect_stage_times(ce_session* s) {
+    for (auto& pd : s->pending) {
+        CE_CUDA(cudaEventSynchronize(pd.b));
+        float ms = 0.0f;
+        CE_CUDA(cudaEventElapsedTime(&ms, pd.a, pd.b));
+        s->stage_ms[pd.stage] += ms;
+        s->stage_n[pd.stage] += 1;
+        s->event_pool.push_back(pd.a);
+        s->event_pool.push_back(pd.b);
+    }
+    s->pending.clear();
+}
+
+void destroy_session(ce_session* s) {
+    if (!s) return;
+    for (auto& pd : s->pending) {
+        cudaEventDestroy(pd.a);
+        cudaEventDestroy(pd.b);
+    }
+    for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+    s->buf.release();
+    if (s->d_fgrid32) cudaFree(s->d_fgrid32);
+    if (s->d_fgrid64) cudaFree(s->d_fgrid64);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->side) cudaStreamDestroy(s->side);
+    delete s;
+}
+
+void check_eval(ce_session* s, int plant, int64_t n) {
+    if (!s) fail("null session");
+    if (plant < 0 || plant >= s->n_plants) fail("plant index {} out of range [0, {})", plant, s->n_plants);
+    if (n < 0) fail("candidate count {} is negative", n);
+}
+
+void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, const float* info_in, float* info_out,
+                   const ce_diagnostics* diag) {
+    check_eval(s, plant, n);
+    if (n == 0) return;
+    const ce_config& c = s->cfg;
+    const bool traj = diag && diag->yplant;
+    ensure_buffers(s, n, traj);
+    Buffers& b = s->buf;
+    cudaStream_t st = s->stream;
+    CE_CUDA(cudaMemcpyAsync(b.gains, cuda_mx, (size_t)n * c.cuda_mx_width * sizeof(float), cudaMemcpyHostToDevice, st));
+    CE_CUDA(cudaMemcpyAsync(b.info, info_in, (size_t)n * c.info_mx_width * sizeof(float), cudaMemcpyHostToDevice, st));
+    run_pipeline(s, plant, n, b.gains, b.info, st, traj);
+    CE_CUDA(cudaMemcpyAsync(info_out, b.info, (size_t)n * c.info_mx_width * sizeof(float), cudaMemcpyDeviceToHost, st));
+    const int nt = c.total_dim;
+    const bool f64 = s->precision == CE_PRECISION_FP64;
+    std::vector<double> tmp;
+    if (diag) {
+        if (diag->yplant)
+            CE_CUDA(cudaMemcpyAsync(diag->yplant, b.traj, (size_t)n * c.time * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (diag->lina)
+            CE_CUDA(cudaMemcpyAsync(diag->lina, b.lina, (size_t)n * nt * nt * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    CE_CUDA(cudaStreamSynchronize(st));
+    if (diag) {
+        auto pull = [&](float* dst, const void* src, size_t count) {
+            if (!dst) return;
+            if (!f64) {
+                CE_CUDA(cudaMemcpy(dst, src, count * sizeof(float), cudaMemcpyDeviceToHost));
+            } else {
+                tmp.resize(count);
+                CE_CUDA(cudaMemcpy(tmp.data(), src, count * sizeof(double), cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < count; ++i) dst[i] = (float)tmp[i];
+            }
+        };
+        pull(diag->eigen, b.eig, (size_t)n * 2 * nt);
+        pull(diag->ata, b.ata, (size_t)n * 4 * nt * nt);
+        pull(diag->atb, b.atb, (size_t)n * 2 * nt);
+    }
+}
+
+// ---- file boundary ----------------------------------------------------------
+std::string read_text(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail("Cannot open {}", path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+// ref: src/main.cu:294-302 -- exact size check over `slices` stacked copies
+template <typename T>
+std::vector<T> readbin(size_t count, const std::string& filename, int slices = 1) {
+    const size_t nbytes = count * sizeof(T);
+    std::ifstream file(filename, std::ios::binary);
+    if (!file) fail("Cannot open {}", filename);
+    file.seekg(0, std::ios::end);
+    const size_t expected = nbytes * slices;
+    const std::streamoff actual = file.tellg();
+    if (actual != static_cast<std::streamoff>(expected))
+        fail("{} is {} bytes, expected {} ({} x {})", filename, (long long)actual, expected, slices, nbytes);
+    file.seekg(0, std::ios::beg);
+    std::vector<T> v(count * slices);
+    if (!v.empty()) {
+        file.read(reinterpret_cast<char*>(v.data()), expected);
+        if (!file) fail("Cannot read {} (intended {}-byte allocation)", filename, nbytes);
+    }
+    return v;
+}
+
+void write_bin(const std::string& name, const void* p, size_t bytes) {
+    std::ofstream f(name, std::ios::binary);
+    if (!f) fail("Cannot open {}", name);
+    f.write(reinterpret_cast<const char*>(p), (std::streamsize)bytes);
+}
+
+void run_files() {
+    ce_config c;
+    parse_config(read_text("ControllerEngine.config"), "ControllerEngine.config", c);
+    const int ns = c.statespace_dim, nd = c.discrete_dim;
+    const int slices = c.serial ? c.n_rounds : 1;
+    // same read order as init64KB / upload_plant (ref: src/main.cu:341-399)
+    auto ssa = readbin<float>((size_t)ns * ns, "STATESPACE_A.bin");
+    auto ssai = readbin<float>((size_t)ns * ns, "STATESPACE_A_I.bin");
+    auto ssb = readbin<float>((size_t)ns, "STATESPACE_B.bin");
+    auto ssc = readbin<float>((size_t)ns, "STATESPACE_C.bin");
+    auto ssd = readbin<float>(1, "STATESPACE_D.bin");
+    auto da = readbin<float>((size_t)nd * nd, "DISCRETE_A.bin", slices);
+    auto dbu = readbin<float>((size_t)nd, "DISCRETE_BU.bin", slices);
+    auto dbw = readbin<float>((size_t)nd * c.nonlin_dim, "DISCRETE_BW.bin", slices);
+    auto dc = readbin<float>((size_t)nd, "DISCRETE_C.bin", slices);
+    auto dai = readbin<float>((size_t)nd * nd, "DISCRETE_A_I.bin", slices);
+    auto bp = readbin<float>((size_t)c.n_params, "BASE_PARAMS.bin", slices);
+    auto dci = readbin<int32_t>((size_t)c.dc_dim * c.dc_instructions, "DC_INFO.bin");
+    auto ui = readbin<int32_t>((size_t)c.u_dim * c.u_instructions, "U_INFO.bin");
+    auto nli = readbin<int32_t>((size_t)c.nl_dim * c.nl_instructions_total, "NL_INFO.bin");
+    ce_plant pl{ssa.data(), ssai.data(), ssb.data(), ssc.data(), ssd.data(), da.data(), dai.data(), dbu.data(),
+                dbw.data(), dc.data(), bp.data(), dci.data(), ui.data(), nli.data()};
+    ce_session* raw = nullptr;
+    create_session(&c, &pl, slices, &raw);
+    std::unique_ptr<ce_session, void (*)(ce_session*)> s(raw, destroy_session);
+
+    {
+        std::ofstream plog("params.log");
+        plog << std::scientific << std::setprecision(9);
+        for (int i = 0; i < c.n_params; i++) plog << "BASE_PARAMS_HOST[" << i << "] = " << bp[i] << "\n";
+        plog << "ref amplitude = " << c.ref_amplitude << "\n";
+    }
+    const size_t nthr = (size_t)c.n_threads;
+    const size_t cw = c.cuda_mx_width, iw = c.info_mx_width;
+    std::ifstream cudamx("CUDA_MX.bin", std::ios::binary);
+    if (!cudamx) fail("Cannot open CUDA_MX.bin");
+    cudamx.seekg(0, std::ios::end);
+    const std::streamoff cexp = (std::streamoff)((size_t)c.n_rounds * nthr * cw * sizeof(float));
+    if (cudamx.tellg() != cexp)
+        fail("CUDA_MX.bin is {} bytes, expected {} ({} rounds x {} candidates)", (long long)cudamx.tellg(),
+             (long long)cexp, c.n_rounds, c.n_threads);
+    cudamx.seekg(0, std::ios::beg);
+    std::ifstream infomx("INFO_MX.bin", std::ios::binary);
+    if (!infomx) fail("Cannot open INFO_MX.bin");
+    infomx.seekg(0, std::ios::end);
+    const std::streamoff iexp = (std::streamoff)((size_t)c.n_rounds * nthr * iw * sizeof(float));
+    if (infomx.tellg() != iexp)
+        fail("INFO_MX.bin is {} bytes, expected {} ({} rounds x {} candidates)", (long long)infomx.tellg(),
+             (long long)iexp, c.n_rounds, c.n_threads);
+    infomx.seekg(0, std::ios::beg);
+    std::ofstream infoout("INFO_MX_OUT.bin", std::ios::binary);
+    if (!infoout) fail("Cannot open INFO_MX_OUT.bin");
+
+    float *hc_mx = nullptr, *hinfo = nullptr;
+    CE_CUDA(cudaMallocHost((void**)&hc_mx, nthr * cw * sizeof(float)));
+    CE_CUDA(cudaMallocHost((void**)&hinfo, nthr * iw * sizeof(float)));
+    std::unique_ptr<float, cudaError_t (*)(void*)> g1(hc_mx, cudaFreeHost), g2(hinfo, cudaFreeHost);
+    const int nt = c.total_dim;
+    std::vector<float> dy, dl, de, da2, db;
+    ce_diagnostics dg{};
+    if (c.dump_diagnostics) {
+        dy.resize(nthr * c.time);
+        dl.resize(nthr * nt * nt);
+        de.resize(nthr * 2 * nt);
+        da2.resize(nthr * 4 * nt * nt);
+        db.resize(nthr * 2 * nt);
+        dg = ce_diagnostics{dy.data(), dl.data(), de.data(), da2.data(), db.data()};
+    }
+    for (int round = 0; round < c.n_rounds; round++) {
+        cudamx.read(reinterpret_cast<char*>(hc_mx), nthr * cw * sizeof(float));
+        if (!cudamx) fail("Cannot read CUDA_MX.bin round {} (intended {}-byte allocation)", round, nthr * cw * sizeof(float));
+        infomx.read(reinterpret_cast<char*>(hinfo), nthr * iw * sizeof(float));
+        if (!infomx) fail("Cannot read INFO_MX.bin round {} (intended {}-byte allocation)", round, nthr * iw * sizeof(float));
+        evaluate_host(s.get(), c.serial ? round : 0, (int64_t)nthr, hc_mx, hinfo, hinfo,
+                      c.dump_diagnostics ? &dg : nullptr);
+        if (c.dump_diagnostics) {
+            write_bin("YPLANT_OUT.bin", dy.data(), dy.size() * sizeof(float));
+            write_bin("LINA_MX_OUT.bin", dl.data(), dl.size() * sizeof(float));
+            write_bin("EIGEN_MX_OUT.bin", de.data(), de.size() * sizeof(float));
+            write_bin("ATA_MX_OUT.bin", da2.data(), da2.size() * sizeof(float));
+            write_bin("ATB_MX_OUT.bin", db.data(), db.size() * sizeof(float));
+        }
+        infoout.write(reinterpret_cast<char*>(hinfo), nthr * iw * sizeof(float));
+    }
+}
+
+}  // namespace
+}  // namespace ce
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using namespace ce;
+
+extern "C" {
+
+CE_EXPORT const char* ce_last_error(void) { return g_last_error.c_str(); }
+
+CE_EXPORT const char* ce_version(void) { return "controllerengine-gb300 0.1 (sm_103a)"; }
+
+CE_EXPORT int ce_parse_config(const char* text, const char* filename, ce_config* out) {
+    return guarded([&] {
+        if (!text || !out) fail("ce_parse_config: null argument");
+        parse_config(text, filename ? filename : "ControllerEngine.config", *out);
+    });
+}
+
+CE_EXPORT int ce_decode_instructions(const int32_t* info, int32_t dim, int32_t count, const float* base_params,
+                                     int32_t n_params, ce_instruction* out) {
+    return guarded([&] {
+        if (count > 0 && (!info || !out || !base_params)) fail("ce_decode_instructions: null argument");
+        decode_instructions(info, dim, count, base_params, n_params, out);
+    });
+}
+
+CE_EXPORT int ce_session_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants, ce_session** out) {
+    return guarded([&] { create_session(cfg, plant, n_plants, out); });
+}
+
+CE_EXPORT void ce_session_destroy(ce_session* s) { destroy_session(s); }
+
+CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64) fail("unknown precision {}", precision);
+        s->precision = precision;
+    });
+}
+
+CE_EXPORT int ce_session_get_config(const ce_session* s, ce_config* out) {
+    return guarded([&] {
+        if (!s || !out) fail("null argument");
+        *out = s->cfg;
+    });
+}
+
+CE_EXPORT int ce_evaluate(ce_session* s, int32_t plant_index, int64_t n, const float* cuda_mx, const float* info_in,
+                          float* info_out) {
+    return guarded([&] { evaluate_host(s, plant_index, n, cuda_mx, info_in, info_out, nullptr); });
+}
+
+CE_EXPORT int ce_evaluate_diagnostics(ce_session* s, int32_t plant_index, int64_t n, const float* cuda_mx,
+                                      const float* info_in, float* info_out, const ce_diagnostics* diag) {
+    return guarded([&] { evaluate_host(s, plant_index, n, cuda_mx, info_in, info_out, diag); });
+}
+
+CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
+                                 const float* d_info_in, float* d_info_out, void* stream) {
+    return guarded([&] {
+        check_eval(s, plant_index, n);
+        if (n == 0) return;
+        cudaStream_t st = (cudaStream_t)stream;
+        if (d_info_out != d_info_in)
+            CE_CUDA(cudaMemcpyAsync(d_info_out, d_info_in, (size_t)n * s->cfg.info_mx_width * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, st));
+        run_pipeline(s, plant_index, n, d_cuda_mx, d_info_out, st, false);
+    });
+}
+
+CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s) { return s ? s->launches : 0; }
+
+CE_EXPORT int ce_session_set_profiling(ce_session* s, int32_t on) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        collect_stage_times(s);
+        s->profiling = on != 0;
+        for (int i = 0; i < CE_NUM_STAGES; ++i) {
+            s->stage_ms[i] = 0.0;
+            s->stage_n[i] = 0;
+        }
+    });
+}
+
+CE_EXPORT int ce_session_stage_times(ce_session* s, double* ms, int64_t* launches) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        collect_stage_times(s);
+        for (int i = 0; i < CE_NUM_STAGES; ++i) {
+            if (ms) ms[i] = s->stage_ms[i];
+            if (launches) launches[i] = s->stage_n[i];
+        }
+    });
+}
+
+CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second) {
+    return guarded([&] {
+        if (!ops_per_second) fail("null argument");
+        *ops_per_second = measure_fma_rate(fp64 != 0);
+    });
+}
+
+CE_EXPORT int RunControllerEngine(void) {
+    try {
+        run_files();
+        return 0;
+    } catch (const std::exception& e) {
+        std::ofstream elog("error.log", std::ios::app);
+        elog << "ControllerEngine error: " << e.what() << std::endl;
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+}  // extern "C"

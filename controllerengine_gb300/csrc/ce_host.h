@@ -1,0 +1,48 @@
+// ce_host.h -- host-side declarations of the engine library (C++20).
+#pragma once
+
+#include <format>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/controller_engine.h"
+#include "ce_internal.h"
+
+namespace ce {
+
+// Every failure is an exception carrying the message; the C ABI catches it,
+// stores it for ce_last_error() and returns nonzero (ref: src/main.cu:22-33).
+template <typename... Args>
+[[noreturn]] void fail(std::format_string<Args...> fmt, Args&&... args) {
+    throw std::runtime_error(std::format(fmt, std::forward<Args>(args)...));
+}
+
+#define CE_CUDA(x)                                                                                  \
+    do {                                                                                            \
+        cudaError_t err_ = (x);                                                                     \
+        if (err_ != cudaSuccess) ::ce::fail("CUDA error {} at {}:{}", cudaGetErrorString(err_), __FILE__, __LINE__); \
+    } while (0)
+
+void derive(ce_config& c);
+void parse_config(const std::string& text, const std::string& filename, ce_config& out);
+void decode_instructions(const int32_t* info, int dim, int count, const float* base_params, int n_params,
+                         ce_instruction* out);
+
+// Kernel launchers (ce_k_*.cu); all enqueue on `st`.
+void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
+                cudaStream_t st);
+void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+                     cudaStream_t st);
+void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+                    const float* info, int* nominal, cudaStream_t st);
+void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
+                void* atb, float* info, cudaStream_t st);
+void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
+                  cudaStream_t st);
+void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
+                  const void* fgrid, float* info, cudaStream_t st);
+
+double measure_fma_rate(bool fp64);
+
+}  // namespace ce

@@ -1,0 +1,71 @@
+// ce_internal.h -- layouts shared by the host orchestrator and the kernels.
+//
+// The plant, observer model and decoded instruction tables of one plant are
+// passed to every kernel BY VALUE as a __grid_constant__ parameter, so they sit
+// in the launch's constant bank: warp-uniform operands that FFMA reads straight
+// from the constant cache, and a per-launch copy, so sessions with different
+// plants can run concurrently on different streams (the reference keeps one
+// global __constant__ copy, ref: src/main.cu:56-87, which makes it non-reentrant).
+#pragma once
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "../../include/controller_engine.h"
+
+namespace ce {
+
+constexpr int MAXS = CE_MAX_STATESPACE_DIM;   // 8
+constexpr int MAXD = CE_MAX_DISCRETE_DIM;     // 8
+constexpr int MAXW = CE_MAX_NONLIN_DIM;       // 4
+constexpr int MAXT = CE_MAX_TOTAL_DIM;        // 16
+constexpr int MAXNC = 2 * CE_MAX_TOTAL_DIM;   // 32: modal basis columns
+constexpr int MAX_DC = CE_MAX_DC_INSTRUCTIONS;
+constexpr int MAX_U = CE_MAX_U_INSTRUCTIONS;
+constexpr int MAX_NL = CE_MAX_NL_INSTRUCTIONS;
+
+// One decoded, SKIP-free instruction.  Removing the SKIP rows of a chain
+// changes nothing: the reference interpreter passes over them without touching
+// `started` or `result` (ref: src/main.cu:266-268).
+struct Instr {
+    int op, col, akind, bkind;
+    float aval, bval;
+};
+
+// Plant + observer model of one round, zero-padded to the MAX dims with row
+// stride 8 (the reference's padded __constant__ layout, ref: src/main.cu:304-315).
+struct Plant {
+    float ss_a[MAXS * MAXS], ss_ai[MAXS * MAXS], ss_b[MAXS], ss_c[MAXS], ss_d;
+    float d_a[MAXD * MAXD], d_ai[MAXD * MAXD], d_bu[MAXD], d_bw[MAXD * MAXW], d_c[MAXD];
+    // margin plant: observer model in batch mode, true linear plant in serial
+    // mode (ref: src/allmargin.cu:11-15); compact ns x ns (row stride MAXS).
+    float m_a[MAXS * MAXS], m_b[MAXS], m_c[MAXS], m_d;
+    int n_dc, n_u, n_nl[MAXW];
+    Instr dc[MAX_DC];
+    Instr u[MAX_U];
+    Instr nl[MAXW][MAX_NL];  // NL columns: 0..nd-1 plant states, MAXD = plant output y
+};
+
+// Sizes and scalars of one evaluation (the slice of the config the kernels read,
+// cf. EngineParams, ref: src/config.cu:84-104).
+struct Run {
+    int64_t n;  // candidates
+    int ns, nd, nt, nw;
+    int time, fit_start_id, fit_steps, fit_pitch, steady_start_id, ref_step_id;
+    int cuda_w, info_w, info_scoring, info_freqresp, info_allmargin, info_modal;
+    int freq;
+    float ts, ref_amp, fit_t0, fit_t1, unstable_err, eig_fail_err;
+    float bandwidth, damping, overshoot, sse, target_gm, target_pm, target_b, alpha;
+    double alpha64;  // alpha of the FP64 form
+    int store_traj;  // also write the full trajectory (diagnostics)
+};
+
+// Per-candidate simulation summary (the parts of the trajectory that modalsetup
+// reads besides the fit window).
+struct SimSummary {
+    float ysum;  // plain float sum of y over [steady_start_id, time), in t order
+    float ymax;  // NaN-ignoring max of y over [0, time)
+    float ymin;  // NaN-ignoring min of y over [0, time)
+    float pad;
+};
+
+}  // namespace ce

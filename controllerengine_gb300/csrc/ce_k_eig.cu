@@ -1,0 +1,510 @@
+// ce_k_eig.cu -- linearised closed loop and the FP64 eigensolves.
+//
+// k_lina_eig: builds LIN_A (ref: src/eigensetup.cu:1-57) in float with the
+// reference's roundings, then computes its eigenvalues in FP64 and stores them
+// as float (re, im) pairs (ref: src/eigensolve.cu:1-19).
+// k_nominal: for candidates still in the running after the modal stage, the
+// FP64 eigenvalues of the nominal closed loop Acl_nom of the margin check
+// (ref: src/allmargin.cu:61-87): stable iff the solve succeeds and every
+// |lambda| < 1.
+//
+// The eigensolver restates the algorithm of the reference's dependency, Eigen's
+// EigenSolver<double> with computeEigenvectors=false (Eigen 3.3/3.4; the
+// submodule commit is not recorded): scale by max|a_ij|, Householder reduction
+// to upper Hessenberg form, Francis double-shift QR with Wilkinson's ad-hoc
+// shift at iteration 10 and the MATLAB-style shift at iteration 30 of an
+// eigenvalue, at most 40*n iterations, deflation when
+// |h(i,i-1)| <= max(eps*(|h(i-1,i-1)|+|h(i,i)|), max(norm*eps^2, DBL_MIN)),
+// 2x2 blocks with real eigenvalues split by a Givens rotation; eigenvalues read
+// off the quasi-triangular T in diagonal order, a complex pair as
+// (t + p, +z), (t + p, -z).  (EISPACK hqr / JAMA hqr2 are the published forms of
+// the same iteration.)  Sums are accumulated in index order without fused
+// multiply-adds.  Failure (no convergence, or a non-finite eigenvalue) yields
+// NaN for the unset eigenvalues; the reference reads unset storage there.
+//
+// GB300 layout: FP64 is a low-rate pipe on this part, so each matrix is owned by
+// one thread (every lane does useful FP64 work; no idle lanes in shuffles) and
+// lives in shared memory as [element][thread], conflict-free across the warp.
+#include <cfloat>
+
+#include "ce_device.cuh"
+#include "ce_host.h"
+
+namespace ce {
+
+constexpr int EIG_BLOCK = 32;
+constexpr double DEPS = 2.220446049250313080847e-16;
+constexpr double DMIN_ = 2.2250738585072013831e-308;
+
+struct SMat {
+    double* p;  // element (i,j) at p[(i*n + j) * B]
+    int n, B;
+    __device__ __forceinline__ double& operator()(int i, int j) const { return p[(i * n + j) * B]; }
+};
+
+// Householder of the column segment T(r0 .. r0+m-1, col): essential part
+// written back into T(r0+1 .., col), returns tau and beta.
+__device__ __forceinline__ void house_inplace(const SMat& T, int r0, int m, int col, double& tau, double& beta) {
+    const double c0 = T(r0, col);
+    double tail = 0.0;
+    for (int k = r0 + 1; k < r0 + m; ++k) tail = __dadd_rn(tail, __dmul_rn(T(k, col), T(k, col)));
+    if (m == 1) tail = 0.0;
+    if (tail <= DMIN_) {
+        tau = 0.0;
+        beta = c0;
+        for (int k = r0 + 1; k < r0 + m; ++k) T(k, col) = 0.0;
+    } else {
+        beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+        if (c0 >= 0.0) beta = -beta;
+        const double d = __dsub_rn(c0, beta);
+        for (int k = r0 + 1; k < r0 + m; ++k) T(k, col) = __ddiv_rn(T(k, col), d);
+        tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+    }
+}
+
+// Householder of a short register vector v[0..m-1] (m = 2 or 3).
+__device__ __forceinline__ void house_vec(const double* v, int m, double* ess, double& tau, double& beta) {
+    const double c0 = v[0];
+    double tail = __dmul_rn(v[1], v[1]);
+    if (m == 3) tail = __dadd_rn(tail, __dmul_rn(v[2], v[2]));
+    if (tail <= DMIN_) {
+        tau = 0.0;
+        beta = c0;
+        ess[0] = 0.0;
+        ess[1] = 0.0;
+    } else {
+        beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+        if (c0 >= 0.0) beta = -beta;
+        const double d = __dsub_rn(c0, beta);
+        ess[0] = __ddiv_rn(v[1], d);
+        ess[1] = m == 3 ? __ddiv_rn(v[2], d) : 0.0;
+        tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+    }
+}
+
+// H = I - tau [1;ess][1;ess]^T applied from the left to rows r0..r0+m-1,
+// columns c0..c1-1.  ess_at(k) gives essential element k (k < m-1).
+template <typename E>
+__device__ __forceinline__ void house_left(const SMat& T, int r0, int m, int c0, int c1, E ess_at, double tau) {
+    if (m == 1) {
+        const double f = __dsub_rn(1.0, tau);
+        for (int j = c0; j < c1; ++j) T(r0, j) = __dmul_rn(T(r0, j), f);
+        return;
+    }
+    if (tau == 0.0) return;
+    for (int j = c0; j < c1; ++j) {
+        double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
+        for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
+        tmp = __dadd_rn(tmp, T(r0, j));
+        T(r0, j) = __dsub_rn(T(r0, j), __dmul_rn(tau, tmp));
+        for (int k = 0; k < m - 1; ++k) T(r0 + 1 + k, j) = __dsub_rn(T(r0 + 1 + k, j), __dmul_rn(tmp, __dmul_rn(tau, ess_at(k))));
+    }
+}
+
+// H applied from the right to rows r0..r1-1, columns c0..c0+m-1.
+template <typename E>
+__device__ __forceinline__ void house_right(const SMat& T, int r0, int r1, int c0, int m, E ess_at, double tau) {
+    if (m == 1) {
+        const double f = __dsub_rn(1.0, tau);
+        for (int i = r0; i < r1; ++i) T(i, c0) = __dmul_rn(T(i, c0), f);
+        return;
+    }
+    if (tau == 0.0) return;
+    for (int i = r0; i < r1; ++i) {
+        double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
+        for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
+        tmp = __dadd_rn(tmp, T(i, c0));
+        T(i, c0) = __dsub_rn(T(i, c0), __dmul_rn(tau, tmp));
+        const double tt = __dmul_rn(tau, tmp);
+        for (int k = 0; k < m - 1; ++k) T(i, c0 + 1 + k) = __dsub_rn(T(i, c0 + 1 + k), __dmul_rn(ess_at(k), tt));
+    }
+}
+
+// Givens rotation (c, s) with [c -s; s c] [p; q] = [r; 0].
+__device__ __forceinline__ void make_givens(double p, double q, double& c, double& s) {
+    if (q == 0.0) {
+        c = p < 0.0 ? -1.0 : 1.0;
+        s = 0.0;
+    } else if (p == 0.0) {
+        c = 0.0;
+        s = q < 0.0 ? 1.0 : -1.0;
+    } else if (fabs(p) > fabs(q)) {
+        const double t = __ddiv_rn(q, p);
+        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+        if (p < 0.0) u = -u;
+        c = __ddiv_rn(1.0, u);
+        s = __dmul_rn(-t, c);
+    } else {
+        const double t = __ddiv_rn(p, q);
+        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+        if (q < 0.0) u = -u;
+        s = __ddiv_rn(-1.0, u);
+        c = __dmul_rn(-t, s);
+    }
+}
+
+// x' = c x - s y, y' = s x + c y (the rotation's adjoint applied to the pair).
+__device__ __forceinline__ void rot_pair(double& x, double& y, double c, double s) {
+    const double xi = x, yi = y;
+    x = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
+    y = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+}
+
+// Eigenvalues of the n x n matrix in T (overwritten).  emit(i, re, im) is called
+// for i = 0..n-1 in Schur order; returns true on success.
+template <typename Emit>
+__device__ bool eig_real(const SMat& T, int n, Emit emit) {
+    // scale
+    double scale = 0.0;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) scale = fmax(scale, fabs(T(i, j)));
+    bool ok = true;
+    if (scale < DMIN_) {
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) T(i, j) = 0.0;
+    } else {
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) T(i, j) = __ddiv_rn(T(i, j), scale);
+        // Hessenberg reduction
+        for (int i = 0; i < n - 1; ++i) {
+            const int rs = n - i - 1;
+            double tau, beta;
+            house_inplace(T, i + 1, rs, i, tau, beta);
+            T(i + 1, i) = beta;
+            auto ess = [&](int k) { return T(i + 2 + k, i); };
+            house_left(T, i + 1, rs, i + 1, n, ess, tau);
+            house_right(T, 0, n, i + 1, rs, ess, tau);
+        }
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j + 1 < i; ++j) T(i, j) = 0.0;
+        // Francis double-shift QR
+        double norm = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const int last = min(j + 1, n - 1);
+            for (int i = 0; i <= last; ++i) norm = __dadd_rn(norm, fabs(T(i, j)));
+        }
+        const double zero_tol = fmax(__dmul_rn(norm, __dmul_rn(DEPS, DEPS)), DMIN_);
+        int iu = n - 1, iter = 0, total = 0;
+        const int max_iter = 40 * n;
+        double exshift = 0.0;
+        if (norm != 0.0) {
+            while (iu >= 0) {
+                int il = iu;
+                while (il > 0) {
+                    double s = __dadd_rn(fabs(T(il - 1, il - 1)), fabs(T(il, il)));
+                    s = fmax(__dmul_rn(s, DEPS), zero_tol);
+                    if (fabs(T(il, il - 1)) <= s) break;
+                    il--;
+                }
+                if (il == iu) {
+                    T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
+                    if (iu > 0) T(iu, iu - 1) = 0.0;
+                    iu--;
+                    iter = 0;
+                } else if (il == iu - 1) {
+                    const double p = __dmul_rn(0.5, __dsub_rn(T(iu - 1, iu - 1), T(iu, iu)));
+                    const double q = __dadd_rn(__dmul_rn(p, p), __dmul_rn(T(iu, iu - 1), T(iu - 1, iu)));
+                    T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
+                    T(iu - 1, iu - 1) = __dadd_rn(T(iu - 1, iu - 1), exshift);
+                    if (q >= 0.0) {
+                        const double z = sqrt(fabs(q));
+                        double c, s;
+                        make_givens(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), T(iu, iu - 1), c, s);
+                        if (!(c == 1.0 && s == 0.0)) {
+                            for (int j = iu - 1; j < n; ++j) {
+                                double x = T(iu - 1, j), y = T(iu, j);
+                                rot_pair(x, y, c, s);
+                                T(iu - 1, j) = x;
+                                T(iu, j) = y;
+                            }
+                            for (int i = 0; i <= iu; ++i) {
+                                double x = T(i, iu - 1), y = T(i, iu);
+                                rot_pair(x, y, c, s);
+                                T(i, iu - 1) = x;
+                                T(i, iu) = y;
+                            }
+                        }
+                        T(iu, iu - 1) = 0.0;
+                    }
+                    if (iu > 1) T(iu - 1, iu - 2) = 0.0;
+                    iu -= 2;
+                    iter = 0;
+                } else {
+                    // shift
+                    double sh0 = T(iu, iu), sh1 = T(iu - 1, iu - 1), sh2 = __dmul_rn(T(iu, iu - 1), T(iu - 1, iu));
+                    if (iter == 10) {
+                        exshift = __dadd_rn(exshift, sh0);
+                        for (int i = 0; i <= iu; ++i) T(i, i) = __dsub_rn(T(i, i), sh0);
+                        const double s = __dadd_rn(fabs(T(iu, iu - 1)), fabs(T(iu - 1, iu - 2)));
+                        sh0 = __dmul_rn(0.75, s);
+                        sh1 = __dmul_rn(0.75, s);
+                        sh2 = __dmul_rn(__dmul_rn(-0.4375, s), s);
+                    }
+                    if (iter == 30) {
+                        double s = __ddiv_rn(__dsub_rn(sh1, sh0), 2.0);
+                        s = __dadd_rn(__dmul_rn(s, s), sh2);
+                        if (s > 0.0) {
+                            s = sqrt(s);
+                            if (sh1 < sh0) s = -s;
+                            s = __dadd_rn(s, __ddiv_rn(__dsub_rn(sh1, sh0), 2.0));
+                            s = __dsub_rn(sh0, __ddiv_rn(sh2, s));
+                            exshift = __dadd_rn(exshift, s);
+                            for (int i = 0; i <= iu; ++i) T(i, i) = __dsub_rn(T(i, i), s);
+                            sh0 = sh1 = sh2 = 0.964;
+                        }
+                    }
+                    iter++;
+                    total++;
+                    if (total > max_iter) break;
+                    // first Householder vector
+                    double v[3];
+                    int im;
+                    for (im = iu - 2; im >= il; --im) {
+                        const double Tmm = T(im, im);
+                        const double r = __dsub_rn(sh0, Tmm);
+                        const double s = __dsub_rn(sh1, Tmm);
+                        v[0] = __dadd_rn(__ddiv_rn(__dsub_rn(__dmul_rn(r, s), sh2), T(im + 1, im)), T(im, im + 1));
+                        v[1] = __dsub_rn(__dsub_rn(__dsub_rn(T(im + 1, im + 1), Tmm), r), s);
+                        v[2] = T(im + 2, im + 1);
+                        if (im == il) break;
+                        const double lhs = __dmul_rn(T(im, im - 1), __dadd_rn(fabs(v[1]), fabs(v[2])));
+                        const double rhs = __dmul_rn(
+                            v[0], __dadd_rn(__dadd_rn(fabs(T(im - 1, im - 1)), fabs(Tmm)), fabs(T(im + 1, im + 1))));
+                        if (fabs(lhs) < __dmul_rn(DEPS, rhs)) break;
+                    }
+                    // the QR step
+                    for (int k = im; k <= iu - 2; ++k) {
+                        const bool first = (k == im);
+                        double w[3];
+                        if (first) {
+                            w[0] = v[0]; w[1] = v[1]; w[2] = v[2];
+                        } else {
+                            w[0] = T(k, k - 1); w[1] = T(k + 1, k - 1); w[2] = T(k + 2, k - 1);
+                        }
+                        double ess[2], tau, beta;
+                        house_vec(w, 3, ess, tau, beta);
+                        if (beta != 0.0) {
+                            if (first && k > il) T(k, k - 1) = -T(k, k - 1);
+                            else if (!first) T(k, k - 1) = beta;
+                            auto e = [&](int q) { return ess[q]; };
+                            house_left(T, k, 3, k, n, e, tau);
+                            house_right(T, 0, min(iu, k + 3) + 1, k, 3, e, tau);
+                        }
+                    }
+                    {
+                        double w[2] = {T(iu - 1, iu - 2), T(iu, iu - 2)};
+                        double ess[2], tau, beta;
+                        house_vec(w, 2, ess, tau, beta);
+                        if (beta != 0.0) {
+                            T(iu - 1, iu - 2) = beta;
+                            auto e = [&](int q) { return ess[q]; };
+                            house_left(T, iu - 1, 2, iu - 1, n, e, tau);
+                            house_right(T, 0, iu + 1, iu - 1, 2, e, tau);
+                        }
+                    }
+                    for (int i = im + 2; i <= iu; ++i) {
+                        T(i, i - 2) = 0.0;
+                        if (i > im + 2) T(i, i - 3) = 0.0;
+                    }
+                }
+            }
+        }
+        ok = total <= max_iter;
+        if (ok)
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) T(i, j) = __dmul_rn(T(i, j), scale);
+    }
+    if (!ok) {
+        for (int i = 0; i < n; ++i) emit(i, CUDART_NAN, CUDART_NAN);
+        return false;
+    }
+    int i = 0;
+    while (i < n) {
+        if (i == n - 1 || T(i + 1, i) == 0.0) {
+            const double re = T(i, i);
+            if (!isfinite(re)) {
+                for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
+                return false;
+            }
+            emit(i, re, 0.0);
+            ++i;
+        } else {
+            const double p = __dmul_rn(0.5, __dsub_rn(T(i, i), T(i + 1, i + 1)));
+            double t0 = T(i + 1, i), t1 = T(i, i + 1);
+            const double maxval = fmax(fabs(p), fmax(fabs(t0), fabs(t1)));
+            t0 = __ddiv_rn(t0, maxval);
+            t1 = __ddiv_rn(t1, maxval);
+            const double p0 = __ddiv_rn(p, maxval);
+            const double z = __dmul_rn(maxval, sqrt(fabs(__dadd_rn(__dmul_rn(p0, p0), __dmul_rn(t0, t1)))));
+            const double re = __dadd_rn(T(i + 1, i + 1), p);
+            if (!(isfinite(re) && isfinite(z))) {
+                for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
+                return false;
+            }
+            emit(i, re, z);
+            emit(i + 1, re, -z);
+            i += 2;
+        }
+    }
+    return true;
+}
+
+// LIN_A = [A - B K - L (C - D K),  L Cd ;  -Bu K,  Ad]   (ref: src/eigensetup.cu:19-42)
+__device__ __forceinline__ float lina_entry(const Plant& P, const float* K, const float* L, int ns, int i, int j) {
+    if (i < ns && j < ns) {
+        const float pbk = __fmaf_rn(P.ss_b[i], K[j], 0.0f);
+        const float pdk = __fmaf_rn(P.ss_d, K[j], 0.0f);
+        const float pcpd = __fsub_rn(P.ss_c[j], pdk);
+        const float lpc = __fmaf_rn(L[i], pcpd, 0.0f);
+        return __fsub_rn(__fsub_rn(P.ss_a[i * MAXS + j], pbk), lpc);
+    }
+    if (i < ns) return __fmaf_rn(L[i], P.d_c[j - ns], 0.0f);
+    if (j < ns) return -__fmaf_rn(P.d_bu[i - ns], K[j], 0.0f);
+    return P.d_a[(i - ns) * MAXD + (j - ns)];
+}
+
+__global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __grid_constant__ Plant P,
+                                                        const float* __restrict__ gains, float* __restrict__ lina,
+                                                        float* __restrict__ eig32, double* __restrict__ eig64) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
+    if (c >= run.n) return;
+    const int ns = run.ns, nt = run.nt;
+    const float* row = gains + c * run.cuda_w;
+    float K[MAXS], L[MAXS];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        K[i] = i < ns ? row[i] : 0.0f;
+        L[i] = i < ns ? row[ns + i] : 0.0f;
+    }
+    SMat T{smem + tid, nt, EIG_BLOCK};
+    float* lrow = lina + c * (int64_t)(nt * nt);
+    for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nt; ++j) {
+            const float v = lina_entry(P, K, L, ns, i, j);
+            lrow[i * nt + j] = v;
+            T(i, j) = (double)v;
+        }
+    if (eig64) {
+        double* out = eig64 + c * (int64_t)(2 * nt);
+        eig_real(T, nt, [&](int i, double re, double im) {
+            out[2 * i] = re;
+            out[2 * i + 1] = im;
+        });
+    } else {
+        float* out = eig32 + c * (int64_t)(2 * nt);
+        eig_real(T, nt, [&](int i, double re, double im) {
+            out[2 * i] = (float)re;
+            out[2 * i + 1] = (float)im;
+        });
+    }
+}
+
+// FP64-form LIN_A: the same blocks formed in double from the float inputs.
+__global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
+                                                          const float* __restrict__ gains, float* __restrict__ lina,
+                                                          double* __restrict__ eig64) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
+    if (c >= run.n) return;
+    const int ns = run.ns, nt = run.nt;
+    const float* row = gains + c * run.cuda_w;
+    SMat T{smem + tid, nt, EIG_BLOCK};
+    float* lrow = lina + c * (int64_t)(nt * nt);
+    for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nt; ++j) {
+            double v;
+            if (i < ns && j < ns) {
+                const double Kj = row[j], Li = row[ns + i];
+                v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
+            } else if (i < ns) {
+                v = (double)row[ns + i] * (double)P.d_c[j - ns];
+            } else if (j < ns) {
+                v = -(double)P.d_bu[i - ns] * (double)row[j];
+            } else {
+                v = P.d_a[(i - ns) * MAXD + (j - ns)];
+            }
+            lrow[i * nt + j] = (float)v;
+            T(i, j) = v;
+        }
+    double* out = eig64 + c * (int64_t)(2 * nt);
+    eig_real(T, nt, [&](int i, double re, double im) {
+        out[2 * i] = re;
+        out[2 * i + 1] = im;
+    });
+}
+
+// Nominal closed loop of the margin check (ref: src/allmargin.cu:50-87):
+// Acl_nom = [OPEN_A - (D L) K^T, -L C^T; B K^T, A] with OPEN_A = LIN_A[:ns,:ns]
+// and (A, B, C, D) the margin plant.  Only candidates with sc0 < unstable_err
+// are solved; nominal[c] = 1 if stable, 0 if not, -1 if not needed.
+__global__ void __launch_bounds__(EIG_BLOCK) k_nominal(const Run run, const __grid_constant__ Plant P,
+                                                       const float* __restrict__ gains, const float* __restrict__ lina,
+                                                       const float* __restrict__ info, int* __restrict__ nominal,
+                                                       int fp64_form) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
+    if (c >= run.n) return;
+    const float sc0 = info[c * (int64_t)run.info_w + run.info_scoring];
+    if (sc0 >= run.unstable_err) {
+        nominal[c] = -1;
+        return;
+    }
+    const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
+    const float* row = gains + c * run.cuda_w;
+    const float* la = lina + c * (int64_t)(nt * nt);
+    SMat T{smem + tid, n2, EIG_BLOCK};
+    for (int i = 0; i < ns; ++i) {
+        const float Li = row[ns + i];
+        for (int j = 0; j < ns; ++j) {
+            const float Kj = row[j];
+            if (fp64_form) {
+                T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
+                T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
+                T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
+            } else {
+                T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
+                T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
+                T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
+            }
+            T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
+        }
+    }
+    bool stable = true;
+    const bool ok = eig_real(T, n2, [&](int, double re, double im) {
+        if (hypot(re, im) >= 1.0) stable = false;
+    });
+    nominal[c] = (ok && stable) ? 1 : 0;
+}
+
+static void set_smem(const void* fn, size_t bytes) {
+    CE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+                     cudaStream_t st) {
+    const int grid = (int)((run.n + EIG_BLOCK - 1) / EIG_BLOCK);
+    const size_t smem = (size_t)run.nt * run.nt * EIG_BLOCK * sizeof(double);
+    if (precision == CE_PRECISION_FP64) {
+        set_smem((const void*)k_lina_eig64, smem);
+        k_lina_eig64<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, (double*)eig);
+    } else {
+        set_smem((const void*)k_lina_eig, smem);
+        k_lina_eig<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, (float*)eig, nullptr);
+    }
+    CE_CUDA(cudaGetLastError());
+}
+
+void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+                    const float* info, int* nominal, cudaStream_t st) {
+    const int grid = (int)((run.n + EIG_BLOCK - 1) / EIG_BLOCK);
+    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * EIG_BLOCK * sizeof(double);
+    set_smem((const void*)k_nominal, smem);
+    k_nominal<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, info, nominal, precision == CE_PRECISION_FP64);
+    CE_CUDA(cudaGetLastError());
+}
+
+}  // namespace ce

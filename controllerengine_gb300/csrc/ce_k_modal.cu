@@ -1,0 +1,476 @@
+// ce_k_modal.cu -- modal fit of the step response and the behaviour score.
+//
+// k_fit restates modalsetup (ref: src/modalsetup.cu:1-97): eigenvalues -> s
+// plane, instability flag, dedupe of consecutive eigenvalues, yss, overshoot,
+// and the normal equations AtA/Atb of the least-squares fit of
+// y - yss to e^{sigma t - shift} cos/sin(omega t) over the fit window, with the
+// reference's float roundings (the same expf/cosf/sinf arguments, the same
+// fused multiply-adds, the same sequential order in t), so AtA/Atb equal the
+// reference kernel's.
+//
+// GB300 layout: the reference keeps the 32x32 AtA in a per-thread local array
+// (4.6 KB stack, ref: src/modalsetup.cu:67).  Here 16 lanes own one candidate:
+// lane l computes the basis pair of mode l (one expf + one sin/cos pair per
+// mode per step, no duplication), the 32 basis values are exchanged through
+// shared memory, and lane l accumulates rows l and 31-l of the lower triangle
+// (33 entries per lane, balanced) in registers.  The fit window is read as 64
+// contiguous bytes per 16 steps and broadcast by shuffle.
+//
+// k_modal restates modalsolve (ref: src/modalsolve.cu:1-108): diagonal
+// scaling, LDLT with symmetric pivoting of the 2nt x 2nt system, per-mode
+// energies, energy-weighted wn/zeta of the oscillatory modes and the behaviour
+// error.  One warp per candidate, lane i owning row i of the factorisation.
+#include <cfloat>
+
+#include "ce_device.cuh"
+#include "ce_host.h"
+
+namespace ce {
+
+constexpr float TINY_E6 = 0x1.0c6f7ap-20f;   // ~1e-6, the reference's threshold constant
+constexpr float SENT = 0x1.2a05f2p+33f;      // 1e10 sentinel of the dedupe scan
+constexpr float LOGFLOOR = 0x1.a484cp-100f;  // ~1e-30 floor of |lambda| before the log
+constexpr float PI_F = 0x1.921fb6p+1f;
+
+__device__ __forceinline__ float rexp(float x) { return expf(x); }
+__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__device__ __forceinline__ float rcos(float x) { return cosf(x); }
+__device__ __forceinline__ double rcos(double x) { return cos(x); }
+__device__ __forceinline__ float rsin(float x) { return sinf(x); }
+__device__ __forceinline__ double rsin(double x) { return sin(x); }
+__device__ __forceinline__ float rlog(float x) { return logf(x); }
+__device__ __forceinline__ double rlog(double x) { return log(x); }
+__device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float rhypot(float a, float b) { return hypotf(a, b); }
+__device__ __forceinline__ double rhypot(double a, double b) { return hypot(a, b); }
+__device__ __forceinline__ float ratan2(float a, float b) { return atan2f(a, b); }
+__device__ __forceinline__ double ratan2(double a, double b) { return atan2(a, b); }
+
+// Modes of one candidate from its eigenvalues (ref: src/modalsetup.cu:8-50,
+// src/modalsolve.cu:114-148).  Every lane computes the same values.
+template <typename R>
+struct Modes {
+    R Re[MAXT], Im[MAXT];
+    bool dup[MAXT];
+    R max_mag;
+    int unique;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_modes(const R* eig, int nt, R ts, Modes<R>& m) {
+    m.max_mag = R(0);
+#pragma unroll
+    for (int i = 0; i < MAXT; ++i) {
+        m.Re[i] = R(0);
+        m.Im[i] = R(0);
+        m.dup[i] = false;
+        if (i < nt) {
+            const R re = eig[2 * i], im = eig[2 * i + 1];
+            const R mag = rhypot(re, im);
+            m.max_mag = fmax(m.max_mag, mag);
+            m.Re[i] = rdiv(rlog(fmax(mag, R(LOGFLOOR))), ts);
+            m.Im[i] = rdiv(ratan2(im, re), ts);
+        }
+    }
+    R pre = R(SENT), pim = R(SENT);
+    int unique = nt;
+#pragma unroll
+    for (int i = 0; i < MAXT; ++i) {
+        if (i < nt) {
+            if (fabs(rsub(m.Re[i], pre)) < R(TINY_E6) && fabs(rsub(fabs(m.Im[i]), fabs(pim))) < R(TINY_E6)) {
+                m.dup[i] = true;
+                unique--;
+            }
+            pre = m.Re[i];
+            pim = m.Im[i];
+        }
+    }
+    m.unique = unique;
+}
+
+// sigma and |omega| of unique mode number `e`.
+template <typename R>
+__device__ __forceinline__ void mode_of(const Modes<R>& m, int nt, int e, R& sigma, R& omega) {
+    sigma = R(0);
+    omega = R(0);
+    int slot = 0;
+#pragma unroll
+    for (int i = 0; i < MAXT; ++i) {
+        if (i < nt && !m.dup[i]) {
+            if (slot == e) {
+                sigma = m.Re[i];
+                omega = fabs(m.Im[i]);
+            }
+            slot++;
+        }
+    }
+}
+
+constexpr int FIT_BLOCK = 128;            // 8 candidates per block
+constexpr int FIT_CPB = FIT_BLOCK / 16;
+
+template <typename R, typename Sum>
+__global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __restrict__ eig, const R* __restrict__ ywin,
+                                                   const Sum* __restrict__ summ, R* __restrict__ ata,
+                                                   R* __restrict__ atb, float* __restrict__ info) {
+    __shared__ R csm[FIT_CPB][2][MAXNC];
+    const int lane = threadIdx.x & 15;
+    const int g = threadIdx.x >> 4;
+    const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
+    const int64_t c = (int64_t)blockIdx.x * FIT_CPB + g;
+    if (c >= run.n) return;  // the whole half-warp leaves together
+    const int nt = run.nt;
+    const R ts = R(run.ts);
+
+    Modes<R> m;
+    load_modes<R>(eig + c * (int64_t)(2 * nt), nt, ts, m);
+    float* out = info + c * (int64_t)run.info_w;
+    const int n2 = 2 * nt;
+    R* arow = ata + c * (int64_t)(n2 * n2);
+    if (m.max_mag > R(1)) {
+        if (lane == 0) {
+            const float v = (float)radd(R(run.unstable_err), rdiv(rlog(m.max_mag), ts));
+            out[run.info_scoring] = v;
+            out[run.info_scoring + 1] = v;
+        }
+        // AtA/Atb stay zero, as after the reference's memset (ref: src/main.cu:520-521)
+        for (int r = lane; r < n2; r += 16) {
+            for (int j = 0; j < n2; ++j) arow[r * n2 + j] = R(0);
+            atb[c * (int64_t)n2 + r] = R(0);
+        }
+        return;
+    }
+    const int unique = m.unique, nc = 2 * unique;
+    R sig, om, shift = R(0);
+    mode_of<R>(m, nt, lane, sig, om);
+    shift = fmax(rmul(sig, R(run.fit_t0)), rmul(sig, R(run.fit_t1)));
+
+    // steady-state value and overshoot (ref: src/modalsetup.cu:52-62); the
+    // running max of y*yss equals max(y)*yss (yss >= 0) or min(y)*yss (yss < 0)
+    // because rounding is monotone; NaN samples are ignored either way.
+    R ysum, ymax, ymin;
+    if constexpr (sizeof(R) == 4) {
+        ysum = summ[c].ysum; ymax = summ[c].ymax; ymin = summ[c].ymin;
+    } else {
+        ysum = summ[4 * c]; ymax = summ[4 * c + 1]; ymin = summ[4 * c + 2];
+    }
+    const R yss = rdiv(ysum, R(run.time - run.steady_start_id));
+    if (lane == 0) {
+        const R pk = fmax(R(0), yss >= R(0) ? rmul(ymax, yss) : rmul(ymin, yss));
+        out[run.info_freqresp + 2] = (float)rsub(rdiv(pk, fmax(rmul(yss, yss), R(TINY_E6))), R(1));
+        out[run.info_freqresp + 3] = (float)yss;
+    }
+
+    // normal equations
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        csm[g][b][lane] = R(0);
+        csm[g][b][lane + 16] = R(0);
+    }
+    __syncwarp(hmask);
+    R A1[16], A2[32], B1 = R(0), B2 = R(0);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) A1[j] = R(0);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) A2[j] = R(0);
+    const int r1 = lane, r2 = 31 - lane;
+    const R* wrow = ywin + c * (int64_t)run.fit_pitch;
+    const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
+    const int steps = run.fit_steps;
+    R ybuf = R(0);
+    for (int w = 0; w < steps; ++w) {
+        if ((w & 15) == 0) {
+            const int idx = w + lane;
+            ybuf = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
+        }
+        const R yw = __shfl_sync(hmask, ybuf, w & 15, 16);
+        const int b = w & 1;
+        const R tval = rmul(R(run.fit_start_id + w), ts);
+        if (lane < unique) {
+            const R decay = rexp(rfma(sig, tval, -shift));
+            const R arg = rmul(om, tval);
+            csm[g][b][2 * lane] = rmul(decay, rcos(arg));
+            csm[g][b][2 * lane + 1] = rmul(decay, rsin(arg));
+        }
+        __syncwarp(hmask);
+        const R y = rsub(yw, yss);
+        const R c1 = csm[g][b][r1];
+        const R c2 = csm[g][b][r2];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const R cj = csm[g][b][j];
+            if (j <= r1) A1[j] = rfma(c1, cj, A1[j]);
+            A2[j] = rfma(c2, cj, A2[j]);
+        }
+        if (nc > 16) {
+#pragma unroll
+            for (int j = 16; j < 32; ++j) {
+                const R cj = csm[g][b][j];
+                if (j <= r2) A2[j] = rfma(c2, cj, A2[j]);
+            }
+        }
+        B1 = rfma(c1, y, B1);
+        B2 = rfma(c2, y, B2);
+    }
+
+    // AtA is 2nt x 2nt, row stride 2nt; only j <= i < nc is ever accumulated
+    // (ref: src/modalsetup.cu:86-90), the rest is zero.
+    if (r1 < n2) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < n2) arow[r1 * n2 + j] = (r1 < nc && j <= r1 && j < 16) ? A1[j & 15] : R(0);
+        atb[c * (int64_t)n2 + r1] = r1 < nc ? B1 : R(0);
+    }
+    if (r2 < n2) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < n2) arow[r2 * n2 + j] = (r2 < nc && j <= r2) ? A2[j] : R(0);
+        atb[c * (int64_t)n2 + r2] = r2 < nc ? B2 : R(0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+constexpr int MODAL_WARPS = 4;
+
+template <typename R>
+__device__ __forceinline__ R rmin_normal();
+template <>
+__device__ __forceinline__ float rmin_normal<float>() { return FLT_MIN; }
+template <>
+__device__ __forceinline__ double rmin_normal<double>() { return DBL_MIN; }
+
+template <typename R>
+__global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const R* __restrict__ eig,
+                                                            const R* __restrict__ ata, const R* __restrict__ atb,
+                                                            float* __restrict__ info) {
+    __shared__ R Ms[MODAL_WARPS][MAXNC][MAXNC + 1];
+    __shared__ R xs[MODAL_WARPS][MAXNC];
+    __shared__ R cs[MODAL_WARPS][MAXNC];
+    __shared__ int trans[MODAL_WARPS][MAXNC];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const int64_t c = (int64_t)blockIdx.x * MODAL_WARPS + wi;
+    if (c >= run.n) return;  // whole warp
+    float* out = info + c * (int64_t)run.info_w;
+    float* sc = out + run.info_scoring;
+    float* fr = out + run.info_freqresp;
+    float* md = out + run.info_modal;
+    if (sc[0] != 0.0f) return;  // pre-flagged or unstable (ref: src/modalsolve.cu:112)
+    const int nt = run.nt, n = 2 * nt;
+    const R ts = R(run.ts);
+    Modes<R> m;
+    load_modes<R>(eig + c * (int64_t)(2 * nt), nt, ts, m);
+    if (m.max_mag > R(1)) {
+        if (lane == 0) {
+            const float v = (float)radd(R(run.unstable_err), rdiv(rlog(m.max_mag), ts));
+            sc[0] = v;
+            sc[1] = v;
+        }
+        return;
+    }
+    R (*M)[MAXNC + 1] = Ms[wi];
+    const R* A = ata + c * (int64_t)(n * n);
+    // full symmetric copy of the lower triangle, then D^-1 A D^-1 with
+    // D = diag(sqrt(a_ii) or 1) (ref: src/modalsolve.cu:154-162)
+    if (lane < n)
+        for (int j = 0; j < n; ++j) M[lane][j] = j <= lane ? A[lane * n + j] : A[j * n + lane];
+    __syncwarp();
+    if (lane < n) {
+        const R s = rsqrt_(M[lane][lane]);
+        cs[wi][lane] = s > R(TINY_E6) ? s : R(1);
+    }
+    __syncwarp();
+    if (lane < n) {
+        const R inv_i = rdiv(R(1), cs[wi][lane]);
+        for (int j = 0; j < n; ++j) M[lane][j] = rmul(rmul(inv_i, M[lane][j]), rdiv(R(1), cs[wi][j]));
+        xs[wi][lane] = rdiv(atb[c * (int64_t)n + lane], cs[wi][lane]);
+    }
+    __syncwarp();
+
+    // LDLT with symmetric pivoting, left-looking, lower triangle
+    // (Eigen's LDLT<Lower> algorithm: pivot = largest remaining |diagonal|)
+    bool stop = false;
+    for (int k = 0; k < n && !stop; ++k) {
+        // pivot: first index of the largest |M(i,i)|, i >= k (a NaN never wins
+        // unless it sits at k, like a sequential `if (v > best)` scan)
+        R v = (lane >= k && lane < n) ? fabs(M[lane][lane]) : -rnan<R>();
+        if (lane == k && isnan(v)) v = CUDART_INF;
+        if (isnan(v)) v = -CUDART_INF;
+        int idx = (lane >= k && lane < n) ? lane : 1 << 20;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const R ov = __shfl_down_sync(0xffffffffu, v, off);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, off);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        const int p = __shfl_sync(0xffffffffu, idx, 0);
+        if (lane == 0) trans[wi][k] = p;
+        if (p != k) {
+            if (lane < k) {
+                const R t = M[k][lane];
+                M[k][lane] = M[p][lane];
+                M[p][lane] = t;
+            }
+            if (lane > p && lane < n) {
+                const R t = M[lane][k];
+                M[lane][k] = M[lane][p];
+                M[lane][p] = t;
+            }
+            if (lane > k && lane < p) {
+                const R t = M[lane][k];
+                M[lane][k] = M[p][lane];
+                M[p][lane] = t;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const R t = M[k][k];
+                M[k][k] = M[p][p];
+                M[p][p] = t;
+            }
+        }
+        __syncwarp();
+        if (k > 0) {
+            // temp_j = d_j * l_kj; a_kk -= sum_j l_kj temp_j; a_ik -= sum_j l_ij temp_j
+            R tk = R(0);
+            if (lane == k) {
+                R acc = R(0);
+                for (int j = 0; j < k; ++j) acc = radd(acc, rmul(M[k][j], rmul(M[j][j], M[k][j])));
+                tk = acc;
+            }
+            R ti = R(0);
+            const bool below = lane > k && lane < n;
+            if (below) {
+                R acc = R(0);
+                for (int j = 0; j < k; ++j) acc = radd(acc, rmul(M[lane][j], rmul(M[j][j], M[k][j])));
+                ti = acc;
+            }
+            __syncwarp();
+            if (lane == k) M[k][k] = rsub(M[k][k], tk);
+            if (below) M[lane][k] = rsub(M[lane][k], ti);
+            __syncwarp();
+        }
+        const R akk = M[k][k];
+        const bool valid = fabs(akk) > R(0);
+        if (k == 0 && !valid) {
+            if (lane < n) trans[wi][lane] = lane;
+            stop = true;  // all-zero diagonal: nothing left to factor, the solve yields 0
+        } else if (valid && lane > k && lane < n) {
+            M[lane][k] = rdiv(M[lane][k], akk);
+        }
+        __syncwarp();
+    }
+
+    // solve: P, L, D^+, L^T, P^T
+    if (lane == 0)
+        for (int k = 0; k < n; ++k) {
+            const int p = trans[wi][k];
+            const R t = xs[wi][k];
+            xs[wi][k] = xs[wi][p];
+            xs[wi][p] = t;
+        }
+    __syncwarp();
+    for (int i = 0; i < n; ++i) {
+        const R xi = xs[wi][i];
+        if (lane > i && lane < n) xs[wi][lane] = rsub(xs[wi][lane], rmul(xi, M[lane][i]));
+        __syncwarp();
+    }
+    if (lane < n) {
+        const R d = M[lane][lane];
+        xs[wi][lane] = fabs(d) > rmin_normal<R>() ? rdiv(xs[wi][lane], d) : R(0);
+    }
+    __syncwarp();
+    for (int i = n - 1; i >= 0; --i) {
+        const R xi = xs[wi][i];
+        if (lane < i) xs[wi][lane] = rsub(xs[wi][lane], rmul(M[i][lane], xi));
+        __syncwarp();
+    }
+    if (lane == 0)
+        for (int k = n - 1; k >= 0; --k) {
+            const int p = trans[wi][k];
+            const R t = xs[wi][k];
+            xs[wi][k] = xs[wi][p];
+            xs[wi][p] = t;
+        }
+    __syncwarp();
+    if (lane < n) xs[wi][lane] = rdiv(xs[wi][lane], cs[wi][lane]);
+    __syncwarp();
+
+    // energies and the behaviour error (ref: src/modalsolve.cu:167-203)
+    if (lane == 0) {
+        R esum = R(0), logwn = R(0), zw = R(0);
+        int e = 0;
+        for (int i = 0; i < nt; ++i) {
+            if (m.dup[i]) continue;
+            const int id = 2 * e;
+            const R c0 = xs[wi][id], c1 = xs[wi][id + 1];
+            const R g00 = A[id * n + id], g01 = A[(id + 1) * n + id], g11 = A[(id + 1) * n + id + 1];
+            const R energy = radd(radd(rmul(rmul(c0, c0), g00), rmul(rmul(rmul(R(2), c0), c1), g01)), rmul(rmul(c1, c1), g11));
+            const R re = m.Re[i], im = fabs(m.Im[i]);
+            const R wn_e = fmax(rsqrt_(radd(rmul(re, re), rmul(im, im))), R(TINY_E6));
+            const R ze = rdiv(-re, wn_e);
+            md[id] = (float)wn_e;
+            md[id + 1] = (float)ze;
+            md[2 * nt + e] = (float)energy;
+            e++;
+            if (im < R(TINY_E6)) continue;
+            esum = radd(esum, energy);
+            logwn = radd(logwn, rmul(energy, rlog(wn_e)));
+            zw = radd(zw, rmul(energy, ze));
+        }
+        md[3 * nt] = (float)m.unique;
+        R wn, zeta;
+        if (esum <= R(TINY_E6)) {
+            wn = R(TINY_E6);
+            zeta = R(0);
+        } else {
+            wn = rexp(rdiv(logwn, esum));
+            zeta = rdiv(zw, esum);
+        }
+        const R D = R(run.damping), d2 = rmul(D, D);
+        const R targetwn = rdiv(rmul(rmul(R(2), R(PI_F)), R(run.bandwidth)),
+                                rsqrt_(radd(rsub(R(1), rmul(R(2), d2)),
+                                            rsqrt_(radd(rsub(rmul(rmul(R(4), d2), d2), rmul(R(4), d2)), R(2))))));
+        const R lw = rlog(rdiv(wn, targetwn));
+        const R dz = rsub(zeta, D);
+        R berr = radd(rmul(lw, lw), rdiv(rdiv(rmul(dz, dz), D), D));
+        const R OS = R(run.overshoot), SSE = R(run.sse);
+        const R eos = rdiv(fmax(R(0), rsub(R(fr[2]), OS)), OS);
+        berr = radd(berr, rmul(eos, eos));
+        const R ess = rdiv(fmax(R(0), rsub(fabs(rsub(rdiv(R(fr[3]), R(run.ref_amp)), R(1))), SSE)), SSE);
+        berr = radd(berr, rmul(ess, ess));
+        const float b32 = (float)berr;
+        sc[0] = isfinite(b32) ? b32 : run.eig_fail_err;
+        sc[1] = sc[0];
+        fr[0] = (float)wn;
+        fr[1] = (float)zeta;
+    }
+}
+
+void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
+                void* atb, float* info, cudaStream_t st) {
+    const int grid = (int)((run.n + FIT_CPB - 1) / FIT_CPB);
+    if (precision == CE_PRECISION_FP64)
+        k_fit<double, double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin,
+                                                         (const double*)summ, (double*)ata, (double*)atb, info);
+    else
+        k_fit<float, SimSummary><<<grid, FIT_BLOCK, 0, st>>>(run, (const float*)eig, (const float*)ywin,
+                                                            (const SimSummary*)summ, (float*)ata, (float*)atb, info);
+    CE_CUDA(cudaGetLastError());
+}
+
+void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
+                  cudaStream_t st) {
+    const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
+    if (precision == CE_PRECISION_FP64)
+        k_modal<double><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
+                                                          (const double*)atb, info);
+    else
+        k_modal<float><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const float*)eig, (const float*)ata,
+                                                         (const float*)atb, info);
+    CE_CUDA(cudaGetLastError());
+}
+
+}  // namespace ce

@@ -1,0 +1,285 @@
+// ce_k_sim.cu -- closed-loop simulation of every candidate (the hot loop).
+//
+// Restates discrete_solve<Luenberger> (ref: src/discrete_solves.cu:12-79):
+// per step t
+//   y      = DC(xp_hi)                                   plant output chain
+//   u      = U(xh_hi, seed = N*ref[t] - K.(xh_hi,xh_lo)) controller output chain
+//   yhat   = C.(xh_hi,xh_lo) + D*u
+//   xh    += (A-I)xh + B*u + L*(y - yhat)                double-float add
+//   W      = NL_k([xp_hi, y]), k < 4                     nonlinear terms
+//   xp    += (Ad-I)xp + Bu*u + Bw*W                      double-float add
+// with the reference's operation order and roundings, so trajectories are
+// bit-identical to the reference kernel's.
+//
+// GB300 layout: one thread per candidate with all state in registers; the
+// plant and the decoded instruction tables come from the launch's constant
+// bank (uniform operands of FFMA); instead of the reference's full
+// candidate-major trajectory written with a 4*time-byte stride per lane
+// (32 sectors per warp store), only the fit window is stored, staged 8 samples
+// at a time in shared memory and written as two 16-byte vectors per lane, i.e.
+// one full 32-byte sector per lane; yss and the overshoot extremes are reduced
+// in registers.
+//
+// Padding: the reference always loops to the MAX dims (8/8/4) with zero
+// padding.  Here loops run to a dimension class NSC/NDC >= the actual dims
+// (classes 4 and 8; padding inside the class is real, zero-filled state).  The
+// padding between the class and 8 is virtual: a zero-coefficient term adds
+// +0 (which turns a -0 accumulator into +0) or, once the padded state has
+// become NaN, NaN.  `padS`/`padD` hold that value, and the poison flags
+// reproduce when the reference's padded states turn NaN (a zero coefficient
+// times a non-finite operand).
+#include "ce_device.cuh"
+#include "ce_host.h"
+
+namespace ce {
+
+constexpr int SIM_BLOCK = 64;
+
+template <int NSC, int NDC>
+__global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __grid_constant__ Plant P,
+                                                         const float* __restrict__ gains, float* __restrict__ ywin,
+                                                         SimSummary* __restrict__ summ, float* __restrict__ traj) {
+    __shared__ float stage[8][SIM_BLOCK];
+    const int tid = threadIdx.x;
+    const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
+    if (c >= run.n) return;  // each thread only touches its own column of `stage`
+
+    const int ns = run.ns;
+    const float* row = gains + c * run.cuda_w;
+    float K[NSC], L[NSC];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) {
+        K[i] = i < ns ? row[i] : 0.0f;
+        L[i] = i < ns ? row[ns + i] : 0.0f;
+    }
+    const float N = row[2 * ns];
+
+    float xh_hi[NSC], xh_lo[NSC], xp_hi[NDC], xp_lo[NDC];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) xh_hi[i] = xh_lo[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NDC; ++i) xp_hi[i] = xp_lo[i] = 0.0f;
+    bool poisS = false, poisD = false;
+
+    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float* wrow = ywin + c * (int64_t)run.fit_pitch;
+    const int T = run.time;
+
+    for (int t = 0; t < T; ++t) {
+        const float padS = poisS ? CUDART_NAN_F : 0.0f;
+        const float padD = poisD ? CUDART_NAN_F : 0.0f;
+
+        // plant output
+        const float y = run_chain<float, NDC, MAX_DC, false>(P.dc, P.n_dc, xp_hi, -1, 0.0f, 0.0f);
+
+        // outputs: fit window, steady-state sum, extremes, optional full trajectory
+        {
+            const int w = t - run.fit_start_id;
+            if (w >= 0 && w < run.fit_steps) {
+                stage[w & 7][tid] = y;
+                if ((w & 7) == 7 || w == run.fit_steps - 1 || t == T - 1) {
+                    float4 a, b;
+                    a.x = stage[0][tid]; a.y = stage[1][tid]; a.z = stage[2][tid]; a.w = stage[3][tid];
+                    b.x = stage[4][tid]; b.y = stage[5][tid]; b.z = stage[6][tid]; b.w = stage[7][tid];
+                    float4* dst = reinterpret_cast<float4*>(wrow + (w & ~7));
+                    dst[0] = a;
+                    dst[1] = b;
+                }
+            }
+            if (t >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            ymax = fmaxf(ymax, y);
+            ymin = fminf(ymin, y);
+            if (run.store_traj) traj[c * (int64_t)T + t] = y;
+        }
+
+        // controller output
+        float kx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) kx = __fmaf_rn(K[i], xh_hi[i], kx);
+        if (NSC < MAXS) kx = __fadd_rn(kx, padS);
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) kx = __fmaf_rn(K[i], xh_lo[i], kx);
+        if (NSC < MAXS) kx = __fadd_rn(kx, padS);
+        const float ref = t < run.ref_step_id ? 0.0f : run.ref_amp;
+        const float u_raw = __fmaf_rn(N, ref, -kx);
+        const float u = run_chain<float, NSC, MAX_U, true>(P.u, P.n_u, xh_hi, -1, 0.0f, u_raw);
+
+        // observer output error
+        float yh = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_hi[i], yh);
+        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_lo[i], yh);
+        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
+        yh = __fmaf_rn(P.ss_d, u, yh);
+        const float yerr = __fsub_rn(y, yh);
+
+        // observer increment (A-I)xh + B u + L yerr, then double-float add
+        float dh[NSC], dl[NSC];
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) {
+            float h = __fmaf_rn(L[i], yerr, __fmul_rn(P.ss_b[i], u));
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) h = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) l = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_lo[j], l);
+            if (NSC < MAXS) {
+                h = __fadd_rn(h, padS);
+                l = __fadd_rn(l, padS);
+            }
+            dh[i] = h;
+            dl[i] = l;
+        }
+        if (NSC < MAXS) {
+            bool bad = !isfinite(yerr) || !isfinite(u);
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) bad = bad || !isfinite(xh_hi[j]) || !isfinite(xh_lo[j]);
+            poisS = poisS || bad;
+        }
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) df_add(xh_hi[i], xh_lo[i], dh[i], dl[i]);
+
+        // nonlinear terms over [xp_hi, y]
+        float W[MAXW];
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k)
+            W[k] = run_chain<float, NDC, MAX_NL, false>(P.nl[k], P.n_nl[k], xp_hi, MAXD, y, 0.0f);
+
+        // plant increment (Ad-I)xp + Bu u + Bw W, then double-float add
+        float ph[NDC], pl[NDC];
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) {
+            float h = __fmul_rn(P.d_bu[i], u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(P.d_bw[i * MAXW + k], W[k], h);
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) h = __fmaf_rn(P.d_ai[i * MAXD + j], xp_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) l = __fmaf_rn(P.d_ai[i * MAXD + j], xp_lo[j], l);
+            if (NDC < MAXD) {
+                h = __fadd_rn(h, padD);
+                l = __fadd_rn(l, padD);
+            }
+            ph[i] = h;
+            pl[i] = l;
+        }
+        if (NDC < MAXD) {
+            bool bad = !isfinite(u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) bad = bad || !isfinite(W[k]);
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) bad = bad || !isfinite(xp_hi[j]) || !isfinite(xp_lo[j]);
+            poisD = poisD || bad;
+        }
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) df_add(xp_hi[i], xp_lo[i], ph[i], pl[i]);
+    }
+
+    SimSummary s;
+    s.ysum = ysum;
+    s.ymax = ymax;
+    s.ymin = ymin;
+    s.pad = 0.0f;
+    summ[c] = s;
+}
+
+// The plain FP64 form of the same recurrence: double state, no hi/lo split.
+template <int NSC, int NDC>
+__global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __grid_constant__ Plant P,
+                                                        const float* __restrict__ gains, double* __restrict__ ywin,
+                                                        double* __restrict__ summ) {
+    const int tid = threadIdx.x;
+    const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
+    if (c >= run.n) return;
+    const int ns = run.ns;
+    const float* row = gains + c * run.cuda_w;
+    double K[NSC], L[NSC];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) {
+        K[i] = i < ns ? (double)row[i] : 0.0;
+        L[i] = i < ns ? (double)row[ns + i] : 0.0;
+    }
+    const double N = row[2 * ns];
+    double xh[NSC], xp[NDC];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) xh[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NDC; ++i) xp[i] = 0.0;
+    double ysum = 0.0, ymax = -CUDART_INF, ymin = CUDART_INF;
+    double* wrow = ywin + c * (int64_t)run.fit_pitch;
+    const int T = run.time;
+    for (int t = 0; t < T; ++t) {
+        const double y = run_chain<double, NDC, MAX_DC, false>(P.dc, P.n_dc, xp, -1, 0.0, 0.0);
+        const int w = t - run.fit_start_id;
+        if (w >= 0 && w < run.fit_steps) wrow[w] = y;
+        if (t >= run.steady_start_id) ysum = __dadd_rn(ysum, y);
+        ymax = fmax(ymax, y);
+        ymin = fmin(ymin, y);
+        double kx = 0.0;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) kx = __fma_rn(K[i], xh[i], kx);
+        const double ref = t < run.ref_step_id ? 0.0 : (double)run.ref_amp;
+        const double u = run_chain<double, NSC, MAX_U, true>(P.u, P.n_u, xh, -1, 0.0, __fma_rn(N, ref, -kx));
+        double yh = 0.0;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) yh = __fma_rn((double)P.ss_c[i], xh[i], yh);
+        yh = __fma_rn((double)P.ss_d, u, yh);
+        const double yerr = __dsub_rn(y, yh);
+        double dh[NSC];
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) {
+            double h = __fma_rn(L[i], yerr, __dmul_rn((double)P.ss_b[i], u));
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) h = __fma_rn((double)P.ss_ai[i * MAXS + j], xh[j], h);
+            dh[i] = h;
+        }
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) xh[i] = __dadd_rn(xh[i], dh[i]);
+        double W[MAXW];
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k) W[k] = run_chain<double, NDC, MAX_NL, false>(P.nl[k], P.n_nl[k], xp, MAXD, y, 0.0);
+        double ph[NDC];
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) {
+            double h = __dmul_rn((double)P.d_bu[i], u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) h = __fma_rn((double)P.d_bw[i * MAXW + k], W[k], h);
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) h = __fma_rn((double)P.d_ai[i * MAXD + j], xp[j], h);
+            ph[i] = h;
+        }
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) xp[i] = __dadd_rn(xp[i], ph[i]);
+    }
+    summ[4 * c + 0] = ysum;
+    summ[4 * c + 1] = ymax;
+    summ[4 * c + 2] = ymin;
+    summ[4 * c + 3] = 0.0;
+}
+
+static int dim_class(int d) { return d <= 4 ? 4 : 8; }
+
+template <int NSC, int NDC>
+static void sim_launch(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ,
+                       float* traj, cudaStream_t st) {
+    const int grid = (int)((run.n + SIM_BLOCK - 1) / SIM_BLOCK);
+    if (precision == CE_PRECISION_FP64)
+        k_sim_fp64<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
+    else
+        k_sim_mixed<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
+}
+
+void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
+                cudaStream_t st) {
+    const int cs = dim_class(run.ns), cd = dim_class(run.nd);
+    if (cs == 4 && cd == 4) sim_launch<4, 4>(run, P, precision, gains, ywin, summ, traj, st);
+    else if (cs == 4 && cd == 8) sim_launch<4, 8>(run, P, precision, gains, ywin, summ, traj, st);
+    else if (cs == 8 && cd == 4) sim_launch<8, 4>(run, P, precision, gains, ywin, summ, traj, st);
+    else sim_launch<8, 8>(run, P, precision, gains, ywin, summ, traj, st);
+    CE_CUDA(cudaGetLastError());
+}
+
+}  // namespace ce

@@ -1,0 +1,257 @@
+"""Python mirror of the reference's interface, on top of the C ABI.
+
+The reference is driven through files (ControllerEngine.config + *.bin) and one
+call, RunControllerEngine() (ref: src/main.cu:592-602).  This module offers:
+
+* ``run_controller_engine(workdir)`` -- that call, unchanged, in a directory;
+* ``EngineConfig.parse(text)`` -- the reference's config parser (same keys,
+  defaults and error messages, ref: src/config.cu:106-244) with the derived sizes;
+* ``decode_instructions(...)`` -- the base-36 instruction decoder
+  (ref: src/main.cu:317-337);
+* ``PlantFiles`` -- the .bin file set as numpy arrays (read/write);
+* ``Session`` -- a device-resident plant with ``evaluate`` (host arrays),
+  ``evaluate_diagnostics`` and ``evaluate_device`` (device pointers), the
+  in-memory form of one RunControllerEngine round.
+
+Errors raise ``ControllerEngineError`` carrying the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import _ffi
+
+F32 = np.float32
+I32 = np.int32
+
+
+class ControllerEngineError(RuntimeError):
+    pass
+
+
+def _lib():
+    return _ffi.load_library()
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise ControllerEngineError(_ffi.last_error(_lib()))
+
+
+def _fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == F32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ffi._FP)
+
+
+def _iptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == I32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ffi._IP)
+
+
+class EngineConfig:
+    """A parsed ControllerEngine.config with its derived sizes."""
+
+    def __init__(self, raw: _ffi.ce_config):
+        self.raw = raw
+
+    @classmethod
+    def parse(cls, text: str, filename: str = "ControllerEngine.config") -> "EngineConfig":
+        raw = _ffi.ce_config()
+        _check(_lib().ce_parse_config(text.encode(), filename.encode(), C.byref(raw)))
+        return cls(raw)
+
+    def __getattr__(self, name):
+        raw = self.__dict__["raw"]
+        v = getattr(raw, name)
+        if name == "nl_instructions":
+            return list(v)
+        return v
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in _ffi.ce_config._fields_:
+            v = getattr(self.raw, name)
+            out[name] = list(v) if name == "nl_instructions" else v
+        return out
+
+
+def decode_instructions(info: np.ndarray, dim: int, count: int, base_params: np.ndarray) -> np.ndarray:
+    """Decode `count` rows of width `dim`; returns a structured array (op, col, akind, bkind, aval, bval)."""
+    info = np.ascontiguousarray(info, dtype=I32).reshape(-1)
+    bp = np.ascontiguousarray(base_params, dtype=F32).reshape(-1)
+    out = (_ffi.ce_instruction * max(count, 1))()
+    _check(_lib().ce_decode_instructions(_iptr(info) if info.size else None, dim, count,
+                                         _fptr(bp) if bp.size else None, int(bp.size), out))
+    dt = np.dtype([("op", I32), ("col", I32), ("akind", I32), ("bkind", I32), ("aval", F32), ("bval", F32)])
+    arr = np.frombuffer(bytes(out), dtype=dt)[:count].copy()
+    return arr
+
+
+PLANT_FILES = (
+    ("statespace_a", "STATESPACE_A.bin", F32), ("statespace_a_i", "STATESPACE_A_I.bin", F32),
+    ("statespace_b", "STATESPACE_B.bin", F32), ("statespace_c", "STATESPACE_C.bin", F32),
+    ("statespace_d", "STATESPACE_D.bin", F32),
+    ("discrete_a", "DISCRETE_A.bin", F32), ("discrete_a_i", "DISCRETE_A_I.bin", F32),
+    ("discrete_bu", "DISCRETE_BU.bin", F32), ("discrete_bw", "DISCRETE_BW.bin", F32),
+    ("discrete_c", "DISCRETE_C.bin", F32), ("base_params", "BASE_PARAMS.bin", F32),
+    ("dc_info", "DC_INFO.bin", I32), ("u_info", "U_INFO.bin", I32), ("nl_info", "NL_INFO.bin", I32),
+)
+
+
+@dataclass
+class PlantFiles:
+    """The reference's plant/observer/instruction .bin set (compact row-major, flattened)."""
+
+    statespace_a: np.ndarray
+    statespace_a_i: np.ndarray
+    statespace_b: np.ndarray
+    statespace_c: np.ndarray
+    statespace_d: np.ndarray
+    discrete_a: np.ndarray
+    discrete_a_i: np.ndarray
+    discrete_bu: np.ndarray
+    discrete_bw: np.ndarray
+    discrete_c: np.ndarray
+    base_params: np.ndarray
+    dc_info: np.ndarray
+    u_info: np.ndarray
+    nl_info: np.ndarray
+
+    def __post_init__(self):
+        for name, _, dt in PLANT_FILES:
+            setattr(self, name, np.ascontiguousarray(getattr(self, name), dtype=dt).reshape(-1))
+
+    def write(self, directory: str | os.PathLike):
+        d = Path(directory)
+        for name, fname, _ in PLANT_FILES:
+            getattr(self, name).tofile(d / fname)
+
+    @classmethod
+    def read(cls, directory: str | os.PathLike) -> "PlantFiles":
+        d = Path(directory)
+        return cls(**{name: np.fromfile(d / fname, dtype=dt) for name, fname, dt in PLANT_FILES})
+
+    def round_slice(self, cfg: EngineConfig, r: int) -> "PlantFiles":
+        """The plant of round r of a serial (stacked) file set."""
+        nd, nw, npar = cfg.discrete_dim, cfg.nonlin_dim, cfg.n_params
+        kw = {name: getattr(self, name) for name, _, _ in PLANT_FILES}
+        for name, size in (("discrete_a", nd * nd), ("discrete_a_i", nd * nd), ("discrete_bu", nd),
+                           ("discrete_bw", nd * nw), ("discrete_c", nd), ("base_params", npar)):
+            kw[name] = getattr(self, name)[r * size:(r + 1) * size]
+        return PlantFiles(**kw)
+
+    def ce_plant(self) -> _ffi.ce_plant:
+        p = _ffi.ce_plant()
+        for name, _, dt in PLANT_FILES:
+            a = getattr(self, name)
+            setattr(p, name, _iptr(a) if dt == I32 else _fptr(a))
+        return p
+
+
+class Session:
+    """Plant + config resident on the current CUDA device (ce_session_create)."""
+
+    def __init__(self, config: EngineConfig, plant: PlantFiles, n_plants: int = 1, precision: str = "mixed"):
+        self.config = config
+        self._plant = plant  # keeps the arrays alive for the call
+        self._h = C.c_void_p()
+        raw = config.raw
+        _check(_lib().ce_session_create(C.byref(raw), C.byref(plant.ce_plant()), n_plants, C.byref(self._h)))
+        self.set_precision(precision)
+
+    def set_precision(self, precision: str):
+        code = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64}[precision]
+        _check(_lib().ce_session_set_precision(self._h, code))
+        self.precision = precision
+
+    def close(self):
+        if self._h:
+            _lib().ce_session_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(_lib().ce_session_kernel_launches(self._h))
+
+    def set_profiling(self, on: bool):
+        _check(_lib().ce_session_set_profiling(self._h, 1 if on else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (milliseconds summed, launches)} since profiling was switched on."""
+        ms = (C.c_double * _ffi.NUM_STAGES)()
+        n = (C.c_int64 * _ffi.NUM_STAGES)()
+        _check(_lib().ce_session_stage_times(self._h, ms, n))
+        return {name: (ms[i], n[i]) for i, name in enumerate(_ffi.STAGE_NAMES)}
+
+    def _rows(self, cuda_mx, info_in):
+        c = self.config
+        g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
+        n = g.shape[0]
+        if info_in is None:
+            info_in = np.zeros((n, c.info_mx_width), F32)
+        i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
+        return g, i, n
+
+    def evaluate(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, plant_index: int = 0) -> np.ndarray:
+        """One round: gains rows [K, L, N] -> INFO rows (input columns passed through)."""
+        g, i, n = self._rows(cuda_mx, info_in)
+        out = np.empty_like(i)
+        _check(_lib().ce_evaluate(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out)))
+        return out
+
+    def evaluate_diagnostics(self, cuda_mx, info_in=None, plant_index: int = 0, want=("yplant", "lina", "eigen",
+                                                                                      "ata", "atb")):
+        g, i, n = self._rows(cuda_mx, info_in)
+        c = self.config
+        nt = c.total_dim
+        shapes = {"yplant": (n, c.time), "lina": (n, nt * nt), "eigen": (n, 2 * nt), "ata": (n, 4 * nt * nt),
+                  "atb": (n, 2 * nt)}
+        arrs = {k: np.empty(shapes[k], F32) for k in want}
+        d = _ffi.ce_diagnostics(*[_fptr(arrs.get(k)) for k in ("yplant", "lina", "eigen", "ata", "atb")])
+        out = np.empty_like(i)
+        _check(_lib().ce_evaluate_diagnostics(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(d)))
+        return out, arrs
+
+    def evaluate_device(self, n: int, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0,
+                        plant_index: int = 0):
+        """Enqueue on `stream`: device pointers (ints), no synchronisation."""
+        _check(_lib().ce_evaluate_device(self._h, plant_index, n, C.c_void_p(d_cuda_mx), C.c_void_p(d_info_in),
+                                         C.c_void_p(d_info_out), C.c_void_p(stream)))
+
+
+def measure_fma_rate(fp64: bool = False) -> float:
+    """FMA-issue throughput of the current device, operations per second."""
+    v = C.c_double()
+    _check(_lib().ce_measure_fma_rate(1 if fp64 else 0, C.byref(v)))
+    return v.value
+
+
+def run_controller_engine(workdir: str | os.PathLike) -> int:
+    """Call RunControllerEngine() with `workdir` as the current directory."""
+    old = os.getcwd()
+    os.chdir(workdir)
+    try:
+        return int(_lib().RunControllerEngine())
+    finally:
+        os.chdir(old)

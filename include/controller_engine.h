@@ -1,0 +1,222 @@
+/*
+ * controller_engine.h -- C ABI of the GB300 batch controller-tuning engine.
+ *
+ * Drop-in boundary.  The reference exports exactly one symbol,
+ *   int RunControllerEngine(void)             (ref: src/main.cu:592, src/ControllerEngine.h:11)
+ * which reads ControllerEngine.config and the *.bin plant/gain files from the
+ * current directory and writes INFO_MX_OUT.bin.  This library exports the same
+ * symbol with the same file semantics, and adds an in-memory session API on
+ * which RunControllerEngine is built.  Every entry point takes plain pointers
+ * and sizes; none takes a C++ or torch type.
+ *
+ * Error convention (ref: src/main.cu:22-33, 592-602): entry points return 0 on
+ * success and nonzero on failure; the message of the last failure on the
+ * calling thread is returned by ce_last_error().  RunControllerEngine also
+ * appends "ControllerEngine error: <message>" to error.log, as the reference does.
+ * Candidate-level numeric failures are not errors: they become the unstable /
+ * eig-fail penalties in the cost vector, exactly as in the reference.
+ */
+#ifndef CONTROLLER_ENGINE_H
+#define CONTROLLER_ENGINE_H
+
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define CE_EXPORT __declspec(dllexport)
+#else
+#define CE_EXPORT __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shape envelope, identical to the reference's compile-time limits (ref: src/main.cu:44-52). */
+#define CE_MAX_STATESPACE_DIM 8
+#define CE_MAX_DISCRETE_DIM 8
+#define CE_MAX_NONLIN_DIM 4
+#define CE_MAX_TOTAL_DIM 16
+#define CE_MAX_NL_DIM 9
+#define CE_MAX_DC_INSTRUCTIONS 4
+#define CE_MAX_U_INSTRUCTIONS 4
+#define CE_MAX_NL_INSTRUCTIONS 8
+#define CE_MAX_PARAMS 34
+
+/* Operand kinds of a decoded instruction (ref: src/main.cu:73). */
+#define CE_OPERAND_CONST 0
+#define CE_OPERAND_STATE 1
+#define CE_OPERAND_PREV 2
+
+/* Arithmetic of a session. */
+#define CE_PRECISION_MIXED 0 /* reference arithmetic: FP32 double-float simulation, FP32 fit and sweep, FP64 eigensolves */
+#define CE_PRECISION_FP64 1  /* the plain FP64 form of the same method: every stage in FP64 */
+
+/*
+ * Parsed ControllerEngine.config plus the sizes derived from it.
+ * Fields and derivations follow EngineConfig (ref: src/config.cu:5-79) and
+ * make_engine_params (ref: src/config.cu:93-104).
+ */
+typedef struct ce_config {
+    /* sizing */
+    int32_t statespace_dim, discrete_dim, nonlin_dim, n_params, input_size;
+    int32_t dc_instructions, u_instructions;
+    int32_t nl_instructions[CE_MAX_NONLIN_DIM];
+    /* launch */
+    int32_t n_cores, n_rounds, serial;
+    /* simulation */
+    int32_t time;
+    float duration;
+    double ref_step_time;
+    float ref_amplitude;
+    /* scoring / fit */
+    float fit_start, fit_end, steady_start;
+    float bandwidth, damping, overshoot, steady_state_error, crossover_coeff, target_gm, target_pm, target_b;
+    float eig_fail_err, unstable_err;
+    int32_t freq;
+    float freq_min;
+    int32_t dump_diagnostics;
+    /* extension: upper end of the frequency sweep in rad/s; 0 = Nyquist (the reference's only choice) */
+    float freq_max_key;
+    /* derived (ref: src/config.cu:40-78, 99-100) */
+    int32_t n_threads;
+    float freq_max;
+    int32_t total_dim, dc_dim, u_dim, nl_dim, nl_instructions_total;
+    int32_t cuda_mx_width, info_scoring, info_freqresp, info_allmargin, info_modal, info_mx_width;
+    int32_t eigen_mx_width, lina_mx_width, ata_mx_width, atb_mx_width;
+    float ts, fit_t0, fit_t1, damping2, damping4, crossover;
+    int32_t fit_start_id, steady_start_id;
+    int32_t fit_steps;   /* number of fit samples: #{t >= 0 : (float)t < (fit_end-fit_start)*time} (ref: src/modalsetup.cu:75-76) */
+    int32_t ref_step_id; /* first t with !(t < ref_step_time*time) (ref: src/main.cu:414) */
+} ce_config;
+
+/* A decoded instruction (ref: src/main.cu:75-82). */
+typedef struct ce_instruction {
+    int32_t op;    /* 0 SKIP, 1 ADD, 2 SUB, 3 MUL, 4 DIV, 5 SAT, 6 SGN; other values: no-op that still starts the chain */
+    int32_t col;   /* column of the row's last nonzero entry */
+    int32_t akind; /* CE_OPERAND_* */
+    int32_t bkind;
+    float aval;    /* BASE_PARAMS value when akind == CE_OPERAND_CONST */
+    float bval;
+} ce_instruction;
+
+/*
+ * Plant, observer model and instruction tables, in the compact row-major
+ * layouts of the reference's .bin files (ref: src/main.cu:341-383, 385-400).
+ * For n_plants > 1 (mode = serial: one plant per round; or one plant per
+ * candidate), discrete_* and base_params hold n_plants stacked copies, as the
+ * stacked .bin files do (ref: src/main.cu:294-302, 343-354).
+ */
+typedef struct ce_plant {
+    const float* statespace_a;   /* ns*ns   STATESPACE_A.bin   */
+    const float* statespace_a_i; /* ns*ns   STATESPACE_A_I.bin */
+    const float* statespace_b;   /* ns      STATESPACE_B.bin   */
+    const float* statespace_c;   /* ns      STATESPACE_C.bin   */
+    const float* statespace_d;   /* 1       STATESPACE_D.bin   */
+    const float* discrete_a;     /* nd*nd   DISCRETE_A.bin     (x n_plants) */
+    const float* discrete_a_i;   /* nd*nd   DISCRETE_A_I.bin   (x n_plants) */
+    const float* discrete_bu;    /* nd      DISCRETE_BU.bin    (x n_plants) */
+    const float* discrete_bw;    /* nd*nw   DISCRETE_BW.bin    (x n_plants) */
+    const float* discrete_c;     /* nd      DISCRETE_C.bin     (x n_plants) */
+    const float* base_params;    /* n_params BASE_PARAMS.bin   (x n_plants) */
+    const int32_t* dc_info;      /* dc_instructions*nd          DC_INFO.bin */
+    const int32_t* u_info;       /* u_instructions*ns           U_INFO.bin  */
+    const int32_t* nl_info;      /* sum(nl_instructions)*(nd+1) NL_INFO.bin */
+} ce_plant;
+
+/* Optional per-candidate intermediates (the reference's dump_diagnostics set,
+ * ref: src/main.cu:483-548).  Each pointer may be NULL.  Host memory. */
+typedef struct ce_diagnostics {
+    float* yplant; /* n * time          candidate-major trajectory   (YPLANT_OUT.bin)   */
+    float* lina;   /* n * nt*nt         linearised closed loop      (LINA_MX_OUT.bin)  */
+    float* eigen;  /* n * 2nt           eigenvalues (re,im) as float (EIGEN_MX_OUT.bin) */
+    float* ata;    /* n * (2nt)^2       modal normal matrix         (ATA_MX_OUT.bin)   */
+    float* atb;    /* n * 2nt           modal right-hand side       (ATB_MX_OUT.bin)   */
+} ce_diagnostics;
+
+typedef struct ce_session ce_session;
+
+/* Message of the last failed call on this thread ("" if none). */
+CE_EXPORT const char* ce_last_error(void);
+
+/* Library version string. */
+CE_EXPORT const char* ce_version(void);
+
+/* Parse ControllerEngine.config text with the reference's keys, defaults,
+ * validation and error messages, then derive the sizes.
+ * Replaces load_config + EngineConfig::derive (ref: src/config.cu:106-244, 40-78).
+ * `filename` is only used in error messages. */
+CE_EXPORT int ce_parse_config(const char* text, const char* filename, ce_config* out);
+
+/* Decode `count` base-36 instruction rows of width `dim`: the last nonzero
+ * entry of a row is the instruction, digits 0 / 35 / 1..34 select state /
+ * running value / BASE_PARAMS[d-1].  Replaces decode_instructions
+ * (ref: src/main.cu:317-337).  NL chains additionally remap col == discrete_dim
+ * to CE_MAX_DISCRETE_DIM (the plant output slot); that remap is done by
+ * ce_session_create (ref: src/main.cu:374-378), not here. */
+CE_EXPORT int ce_decode_instructions(const int32_t* info, int32_t dim, int32_t count,
+                                     const float* base_params, int32_t n_params, ce_instruction* out);
+
+/* Create a session: validates the plant, decodes the instruction tables of
+ * every plant, uploads everything to the current CUDA device and computes the
+ * plant's frequency response on the sweep grid.  Replaces init64KB /
+ * upload_plant and the plant half of allmargin (ref: src/main.cu:341-400,
+ * src/allmargin.cu:11-41).  n_plants = 1 for mode = batch, n_rounds for
+ * mode = serial. */
+CE_EXPORT int ce_session_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants, ce_session** out);
+CE_EXPORT void ce_session_destroy(ce_session* s);
+CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision);
+CE_EXPORT int ce_session_get_config(const ce_session* s, ce_config* out);
+
+/* Evaluate n candidates against plant `plant_index` (the round in mode =
+ * serial).  cuda_mx: n rows of cuda_mx_width floats [K(ns), L(ns), N];
+ * info_in / info_out: n rows of info_mx_width floats (info_out may alias
+ * info_in).  Host memory; synchronous.  One call = one round of
+ * orchestrate_sims (ref: src/main.cu:467-559). */
+CE_EXPORT int ce_evaluate(ce_session* s, int32_t plant_index, int64_t n,
+                          const float* cuda_mx, const float* info_in, float* info_out);
+
+/* As ce_evaluate, and also returns the intermediates requested in `diag`. */
+CE_EXPORT int ce_evaluate_diagnostics(ce_session* s, int32_t plant_index, int64_t n,
+                                      const float* cuda_mx, const float* info_in, float* info_out,
+                                      const ce_diagnostics* diag);
+
+/* Device-memory variant: pointers are device pointers, work is enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) and the call returns
+ * without synchronising.  The session owns its scratch; calls on one session
+ * must not overlap. */
+CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n,
+                                 const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
+                                 void* stream);
+
+/* Launches of this library's kernels since the session was created. */
+CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s);
+
+/* Measurement hooks (no counterpart in the reference).  With profiling on,
+ * every stage launch is bracketed by CUDA events on the stream it runs on;
+ * ce_session_stage_times waits for them and returns, per stage, the summed
+ * milliseconds and the launch count since profiling was switched on.
+ * Stages, in order: 0 lina+eigensolve, 1 simulation, 2 modal fit,
+ * 3 modal solve, 4 nominal closed loop, 5 margin sweep. */
+#define CE_NUM_STAGES 6
+CE_EXPORT int ce_session_set_profiling(ce_session* s, int32_t on);
+CE_EXPORT int ce_session_stage_times(ce_session* s, double* ms, int64_t* launches);
+
+/* FMA-issue throughput of the current device in operations per second,
+ * measured with a register-resident dependent-chain kernel (fp64 = 0: FP32
+ * FFMA, 1: FP64 DFMA).  Used as the roofline denominator for the FP32/FP64
+ * pipes, which the HBM/tensor peak file does not cover. */
+CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second);
+
+/* The drop-in entry point (ref: src/main.cu:592-602, src/ControllerEngine.h:11):
+ * reads ControllerEngine.config and the .bin files from the current
+ * directory, streams n_rounds rounds of n_threads candidates, writes
+ * INFO_MX_OUT.bin and params.log (and the *_OUT.bin diagnostics when
+ * dump_diagnostics is set).  Returns 0, or 1 after appending the message to
+ * error.log. */
+CE_EXPORT int RunControllerEngine(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONTROLLER_ENGINE_H */

@@ -1,0 +1,42 @@
+"""The C-ABI library loads and exports every entry point include/controller_engine.h declares.  CPU only."""
+import re
+import subprocess
+from pathlib import Path
+
+import controllerengine_gb300 as ce
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    syms = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        for m in re.finditer(r"CE_EXPORT\s+[\w\s\*]+?\b(\w+)\s*\(", h.read_text()):
+            syms.append(m.group(1))
+    return syms
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert "RunControllerEngine" in syms and len(syms) >= 10
+    out = subprocess.run(["nm", "-D", "--defined-only", str(ce.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    for s in syms:
+        assert hasattr(lib, s)
+
+
+def test_no_stray_exports(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(ce.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert exported <= set(declared_symbols()), sorted(exported - set(declared_symbols()))
+
+
+def test_version_and_error_channel(lib):
+    assert b"sm_103a" in lib.ce_version()
+    import pytest
+    with pytest.raises(ce.ControllerEngineError, match="missing `statespace_dim`"):
+        ce.EngineConfig.parse("time = 5\n")

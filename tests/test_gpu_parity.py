@@ -1,0 +1,169 @@
+"""GPU parity against the CPU oracle, stage by stage and end to end.
+
+Bit-exact: trajectories (FP32 double-float recurrence), LIN_A, the FP64
+eigenvalues (as float), yss / overshoot, and every candidate classification
+(modal-unstable, nominal-unstable, eig-fail, pre-flag pass-through).
+To a tolerance (the stages call expf/cosf/sinf/logf/atan2f/hypotf, whose CUDA
+and glibc implementations differ in the last ulp): AtA/Atb (2e-5 of the row
+scale), behaviour / margin / total scores (1e-4 relative), gain and phase
+margins (1e-3 dB / deg absolute, the tolerance this port states for margins).
+"""
+import numpy as np
+import pytest
+
+import controllerengine_gb300 as ce
+
+pytestmark = pytest.mark.gpu
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def _mismatch(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    bad = ~((a == b) | (np.isnan(a) & np.isnan(b)))
+    return int(bad.sum())
+
+
+def _cols(cfg):
+    s = cfg.info_scoring
+    return dict(sc=slice(s, s + 3), fr=slice(s + 3, s + 7), am=slice(s + 7, s + 12),
+                md=slice(s + 12, s + 12 + 3 * cfg.total_dim + 1))
+
+
+def _classes(info, cfg):
+    c = _cols(cfg)
+    sc, am = info[:, c["sc"]], info[:, c["am"]]
+    return np.stack([sc[:, 1] >= cfg.unstable_err, sc[:, 2] == np.float32(cfg.unstable_err),
+                     sc[:, 2] == np.float32(cfg.eig_fail_err), am[:, 3]], axis=1)
+
+
+def _close(a, b, rtol, atol=0.0):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    ok = both_nan | (np.abs(a - b) <= atol + rtol * np.abs(b)) | (a == b)
+    return ok
+
+
+def _stagewise(problem, oracle_mod):
+    cfg = ce.EngineConfig.parse(problem.config_text)
+    with ce.Session(cfg, problem.plant) as s:
+        info, d = s.evaluate_diagnostics(problem.cuda_mx, problem.info_mx)
+        launches = s.kernel_launches
+    assert launches == 6
+    orc = oracle_mod.Oracle(problem.config_text, problem.plant)
+    g = problem.cuda_mx
+
+    y_o = orc.sim(g)
+    assert _eq(d["yplant"], y_o), f"trajectory mismatches: {_mismatch(d['yplant'], y_o)}"
+    lina_o = orc.lina(g)
+    assert _eq(d["lina"], lina_o), f"LIN_A mismatches: {_mismatch(d['lina'], lina_o)}"
+    eig_o = orc.eigensolve(d["lina"])
+    assert _eq(d["eigen"], eig_o), f"eigenvalue mismatches: {_mismatch(d['eigen'], eig_o)}"
+
+    ata_o, atb_o, info1 = orc.modalsetup(d["yplant"], d["eigen"], problem.info_mx)
+    c = _cols(cfg)
+    fr = c["fr"]
+    # yss and overshoot involve no libm call: bit-exact
+    assert _eq(info[:, fr][:, 2:4], info1[:, fr][:, 2:4])
+    scale = np.maximum(np.abs(ata_o).max(axis=1, keepdims=True), 1e-30)
+    assert np.all(_close(d["ata"], ata_o, 0, 2e-5 * scale)), "AtA"
+    bscale = np.maximum(np.abs(atb_o).max(axis=1, keepdims=True), 1e-30)
+    assert np.all(_close(d["atb"], atb_o, 0, 2e-5 * bscale)), "Atb"
+
+    # modal solve + margins in the oracle on the engine's own intermediates
+    info2 = orc.modalsolve(d["ata"], d["atb"], d["eigen"], info1)
+    info3 = orc.allmargin(d["lina"], g, info2)
+    assert _eq(_classes(info, cfg), _classes(info3, cfg)), "classification differs"
+    sc, am, md = c["sc"], c["am"], c["md"]
+    assert np.all(_close(info[:, sc], info3[:, sc], 1e-4, 1e-6)), "scores"
+    assert np.all(_close(info[:, fr][:, :2], info3[:, fr][:, :2], 1e-4, 1e-6)), "wn, zeta"
+    assert np.all(_close(info[:, md], info3[:, md], 1e-4, 1e-6)), "modal columns"
+    a, b = info[:, am], info3[:, am]
+    assert np.all(_close(a[:, 0], b[:, 0], 0, 1e-3)), "gain margin (dB)"
+    assert np.all(_close(a[:, 1], b[:, 1], 0, 1e-3)), "phase margin (deg)"
+    assert np.all(_close(a[:, 2], b[:, 2], 1e-4, 1e-6)), "delay margin"
+    assert _eq(a[:, 3], b[:, 3])
+    assert np.all(_close(a[:, 4], b[:, 4], 1e-5, 1e-7)), "b_PC"
+    # the user columns pass through untouched
+    assert _eq(info[:, :cfg.input_size], problem.info_mx[:, :cfg.input_size])
+    return cfg, info
+
+
+def test_stagewise_mass_spring(lib, oracle_mod, mass_spring):
+    cfg, info = _stagewise(mass_spring, oracle_mod)
+    cls = _classes(info, cfg)
+    # the workload exercises every branch
+    assert cls[:, 0].sum() > 0 and cls[:, 3].sum() > 0
+    s = cfg.info_scoring
+    assert info[5, s] == np.float32(2.0e6) and info[5, s + 2] == np.float32(2.0e6)   # pre-flag above unstable_err
+    assert info[3, s + 1] == np.float32(5.0)                                          # pre-flag below: kept in sc1
+
+
+def test_stagewise_eight_state(lib, oracle_mod, eight_state_small):
+    _stagewise(eight_state_small, oracle_mod)
+
+
+def test_end_to_end_against_independent_oracle(lib, oracle_mod, mass_spring, eight_state_small):
+    for p in (mass_spring, eight_state_small):
+        cfg = ce.EngineConfig.parse(p.config_text)
+        with ce.Session(cfg, p.plant) as s:
+            info = s.evaluate(p.cuda_mx, p.info_mx)
+        ref = oracle_mod.Oracle(p.config_text, p.plant).evaluate(p.cuda_mx, p.info_mx)
+        cls_a, cls_b = _classes(info, cfg), _classes(ref, cfg)
+        assert _eq(cls_a, cls_b), f"classification mismatches: {int((cls_a != cls_b).any(axis=1).sum())}"
+        c = _cols(cfg)
+        am = c["am"]
+        assert np.all(_close(info[:, am][:, 0], ref[:, am][:, 0], 0, 1e-3))
+        assert np.all(_close(info[:, am][:, 1], ref[:, am][:, 1], 0, 1e-3))
+        # total score: identical classification; values within 1e-3 relative for all but
+        # ill-conditioned modal fits, which must stay under 0.5% of the candidates
+        sa, sb = info[:, c["sc"]][:, 0], ref[:, c["sc"]][:, 0]
+        bad = ~_close(sa, sb, 1e-3, 1e-5)
+        assert bad.mean() < 0.005, (bad.sum(), np.where(bad)[0][:10])
+
+
+def test_device_api_matches_host_api(lib, mass_spring):
+    import torch
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        host = s.evaluate(p.cuda_mx, p.info_mx)
+        g = torch.from_numpy(p.cuda_mx).cuda()
+        i = torch.from_numpy(p.info_mx).cuda()
+        o = torch.empty_like(i)
+        st = torch.cuda.current_stream()
+        s.evaluate_device(g.shape[0], g.data_ptr(), i.data_ptr(), o.data_ptr(), stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        dev = o.cpu().numpy()
+        # in-place (info_out aliasing info_in)
+        s.evaluate_device(g.shape[0], g.data_ptr(), i.data_ptr(), i.data_ptr(), stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        inplace = i.cpu().numpy()
+    assert _eq(host, dev) and _eq(host, inplace)
+
+
+def test_batch_size_independence(lib, eight_state_small):
+    """A candidate's row does not depend on the batch it is evaluated in."""
+    p = eight_state_small
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        full = s.evaluate(p.cuda_mx, p.info_mx)
+        part = np.vstack([s.evaluate(p.cuda_mx[a:a + 37], p.info_mx[a:a + 37]) for a in range(0, 512, 37)])
+        one = s.evaluate(p.cuda_mx[100:101], p.info_mx[100:101])
+    assert _eq(full, part) and _eq(full[100:101], one)
+
+
+def test_fp64_form_runs_and_agrees_on_classification(lib, eight_state_small):
+    p = eight_state_small
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, precision="fp64") as s:
+        f64 = s.evaluate(p.cuda_mx, p.info_mx)
+    with ce.Session(cfg, p.plant) as s:
+        mix = s.evaluate(p.cuda_mx, p.info_mx)
+    ca, cb = _classes(mix, cfg), _classes(f64, cfg)
+    assert (ca != cb).any(axis=1).mean() < 0.01
+    c = _cols(cfg)
+    ok = ~(ca != cb).any(axis=1) & (mix[:, c["am"]][:, 3] == 1)
+    np.testing.assert_allclose(mix[ok][:, c["am"]][:, 4], f64[ok][:, c["am"]][:, 4], rtol=1e-3)

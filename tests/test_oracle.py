@@ -1,0 +1,84 @@
+"""Pins of the CPU oracle itself: the FP64 eigensolver against LAPACK and closed
+forms, the simulation against an independent float64 recurrence, and the
+workload generator's invariants.  CPU only."""
+import numpy as np
+import pytest
+from scipy.linalg import expm
+
+
+def test_eig_matches_lapack(oracle_mod):
+    rng = np.random.default_rng(3)
+    for n in list(range(1, 17)) * 4:
+        A = rng.standard_normal((n, n))
+        if rng.random() < 0.3:
+            A = A @ np.diag(rng.uniform(0.01, 10.0, n))
+        ok, ev = oracle_mod.eig_matrix(A)
+        assert ok
+        ref = np.linalg.eigvals(A)
+        # same multiset of eigenvalues
+        key = lambda z: (round(z.real, 6), round(abs(z.imag), 6), np.sign(z.imag))
+        a = sorted(ev, key=key)
+        b = sorted(ref, key=key)
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * max(1.0, np.abs(ref).max()))
+
+
+def test_eig_pair_convention(oracle_mod):
+    # complex pairs are adjacent with the positive imaginary part first (Schur-diagonal order)
+    rng = np.random.default_rng(4)
+    for _ in range(50):
+        A = rng.standard_normal((8, 8))
+        ok, ev = oracle_mod.eig_matrix(A)
+        i = 0
+        while i < 8:
+            if ev[i].imag != 0:
+                assert ev[i].imag > 0 and ev[i + 1] == np.conj(ev[i])
+                i += 2
+            else:
+                i += 1
+
+
+def test_eig_zoh_closed_form(oracle_mod):
+    # ZOH of a damped oscillator: eigenvalues exp(s dt), s = -zeta wn +- i wn sqrt(1-zeta^2)
+    Ac = np.array([[0.0, 1.0], [-4.0, -0.4]])
+    Ad = expm(Ac * 1e-3)
+    ok, ev = oracle_mod.eig_matrix(Ad)
+    s = np.roots([1.0, 0.4, 4.0])
+    np.testing.assert_allclose(sorted(ev, key=lambda z: z.imag), sorted(np.exp(s * 1e-3), key=lambda z: z.imag),
+                               rtol=1e-13)
+
+
+def test_eig_zero_and_triangular(oracle_mod):
+    ok, ev = oracle_mod.eig_matrix(np.zeros((4, 4)))
+    assert ok and np.all(ev == 0)
+    T = np.triu(np.arange(1.0, 17.0).reshape(4, 4))
+    ok, ev = oracle_mod.eig_matrix(T)
+    assert ok and sorted(ev.real) == [1.0, 6.0, 11.0, 16.0]
+
+
+def test_sim_linear_matches_float64(oracle_mod):
+    """No nonlinearity, K = L = 0: y is the plant's step response to u = N r."""
+    from controllerengine_gb300 import synth
+    p = synth.mass_spring(1536)
+    p.plant.nl_info[:] = 0
+    g = np.zeros((1, 7), np.float32)
+    g[0, 6] = 2.0
+    y = oracle_mod.Oracle(p.config_text, p.plant).sim(g)[0]
+    A = p.plant.discrete_a.reshape(2, 2).astype(np.float64)
+    B = p.plant.discrete_bu.astype(np.float64)
+    x = np.zeros(2)
+    ref = np.empty(2000)
+    for t in range(2000):
+        ref[t] = x[0]
+        u = 0.0 if t < 100 else 2.0
+        x = A @ x + B * u
+    np.testing.assert_allclose(y, ref, rtol=1e-5, atol=1e-9)
+
+
+def test_generator_invariants():
+    from controllerengine_gb300 import synth
+    p = synth.eight_state(n=64, time=500, freq=50)
+    A = p.plant.discrete_a.reshape(8, 8).astype(np.float64)
+    r = np.abs(np.linalg.eigvals(A))
+    assert np.all((r > 0.899) & (r < 0.9951))
+    np.testing.assert_array_equal(p.plant.discrete_a_i, p.plant.discrete_a - np.eye(8, dtype=np.float32).reshape(-1))
+    assert p.cuda_mx.shape == (64, 17) and np.all(np.isfinite(p.cuda_mx))
