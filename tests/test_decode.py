@@ -75,3 +75,27 @@ def test_matches_oracle_on_random_tables(lib, oracle_mod):
         got = [(int(m["op"]), int(m["col"]), int(m["akind"]), int(m["bkind"]), np.float32(m["aval"]),
                 np.float32(m["bval"])) for m in mine]
         assert got == [(a, b, c, d, np.float32(e), np.float32(f)) for a, b, c, d, e, f in ref]
+
+
+def test_matches_reference_decoder_golden(lib):
+    """tests/golden/decode_golden.json: the reference's own decode_instructions
+    (src/main.cu:317-337, built by `make -C oracle ref`; generator
+    tests/golden/make_decode_golden.py) on 120 seeded tables.  Bit-exact,
+    error texts included."""
+    import json
+    from pathlib import Path
+    cases = json.loads((Path(__file__).parent / "golden" / "decode_golden.json").read_text())
+    for t in cases:
+        rows = np.array(t["rows"], np.int32).reshape(-1, t["dim"]) if t["count"] else np.zeros((0, t["dim"]), np.int32)
+        bp = np.array(t["base_params"], np.float32)[:t["n_params"]]
+        if "error" in t:
+            with pytest.raises(ce.ControllerEngineError) as e:
+                ce.decode_instructions(rows, t["dim"], t["count"], bp)
+            assert str(e.value) == t["error"]
+            continue
+        mine = ce.decode_instructions(rows, t["dim"], t["count"], bp)
+        assert len(mine) == len(t["decoded"])
+        for m, ref in zip(mine, t["decoded"]):
+            assert [int(m["op"]), int(m["col"]), int(m["akind"]), int(m["bkind"])] == ref[:4]
+            if ref[4] is not None:
+                assert float(m["aval"]).hex() == ref[4] and float(m["bval"]).hex() == ref[5]
