@@ -24,7 +24,8 @@ EXPORTED_SYMBOLS = (
     "ce_last_error", "ce_version", "ce_parse_config", "ce_decode_instructions",
     "ce_session_create", "ce_session_destroy", "ce_session_set_precision", "ce_session_get_config",
     "ce_evaluate", "ce_evaluate_diagnostics", "ce_evaluate_device", "ce_session_kernel_launches",
-    "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "RunControllerEngine",
+    "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
+    "RunControllerEngine",
 )
 NUM_STAGES = 6
 STAGE_NAMES = ("lina_eig", "sim", "fit", "modal", "nominal", "sweep")
@@ -110,6 +111,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_session_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.ce_session_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.ce_measure_fma_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]
+    lib.ce_modal_fit_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int64] + [C.c_void_p] * 6
     lib.RunControllerEngine.restype = C.c_int
     if path is None:
         _lib = lib

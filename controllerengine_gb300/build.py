@@ -25,7 +25,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ce_k_sim.cu", "ce_k_eig.cu", "ce_k_modal.cu", "ce_k_sweep.cu", "ce_k_calib.cu"]
+CU_SOURCES = ["ce_k_sim.cu", "ce_k_eig.cu", "ce_k_modal.cu", "ce_k_sweep.cu", "ce_k_calib.cu", "ce_noalloc.cu"]
 CPP_SOURCES = ["ce_config.cpp", "ce_engine.cpp"]
 
 

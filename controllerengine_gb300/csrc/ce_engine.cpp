@@ -677,6 +677,15 @@ void run_files() {
 }  // namespace
 }  // namespace ce
 
+namespace ce {
+// Read-only views of a session for other translation units of the library.
+const Plant* session_plant(const ce_session* s, int plant) { return &s->plants[plant]; }
+const ce_config* session_config(const ce_session* s) { return &s->cfg; }
+int session_plants(const ce_session* s) { return s->n_plants; }
+Run session_run(const ce_session* s, int plant, int64_t n) { return make_run(s, plant, n); }
+void session_count_launches(ce_session* s, int k) { s->launches += k; }
+}  // namespace ce
+
 // ============================================================================
 // C ABI
 // ============================================================================

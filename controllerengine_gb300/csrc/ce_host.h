@@ -11,6 +11,8 @@
 
 namespace ce {
 
+extern thread_local std::string g_last_error;
+
 // Every failure is an exception carrying the message; the C ABI catches it,
 // stores it for ce_last_error() and returns nonzero (ref: src/main.cu:22-33).
 template <typename... Args>
@@ -44,5 +46,11 @@ void launch_sweep(const Run& run, int precision, const float* gains, const float
                   const void* fgrid, float* info, cudaStream_t st);
 
 double measure_fma_rate(bool fp64);
+
+const Plant* session_plant(const ce_session* s, int plant);
+const ce_config* session_config(const ce_session* s);
+int session_plants(const ce_session* s);
+Run session_run(const ce_session* s, int plant, int64_t n);
+void session_count_launches(ce_session* s, int k);
 
 }  // namespace ce

@@ -207,6 +207,29 @@ CE_EXPORT int ce_session_stage_times(ce_session* s, double* ms, int64_t* launche
  * pipes, which the HBM/tensor peak file does not cover. */
 CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second);
 
+/* Allocation-free variant of the modal-fit path.  No counterpart in the
+ * reference.  For callers that must not allocate device memory when they
+ * evaluate: a real-time tuning loop that cannot afford cudaMalloc's latency,
+ * work issued inside a stream capture, or a host application whose device
+ * memory belongs to its own allocator.  It runs the simulation and the modal
+ * setup (the same kernels as the session pipeline) for n candidates of plant
+ * `plant_index`: d_cuda_mx (n x cuda_mx_width gains) and d_eigen (n x 2nt float
+ * eigenvalues, e.g. from a previous evaluation) in; d_ata (n x (2nt)^2), d_atb
+ * (n x 2nt) out; d_info (n x info_mx_width) in/out, receiving the steady-state
+ * value, the overshoot and the unstable penalty.  Device pointers, enqueued on
+ * `stream`, no synchronisation.
+ * Its only scratch, the fit window and trajectory summaries, is a static
+ * device array of CE_NOALLOC_SCRATCH_FLOATS floats (32 MiB, held by every
+ * device that loads the library until exit); a call needs
+ * n * (round_up(fit_steps, 8) + 4) floats and is rejected with an error if that
+ * is more.  It calls no cudaMalloc/cudaFree.  The first call on a device looks
+ * up the array's address (cudaGetSymbolAddress, with that device current):
+ * make it before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU race; serialise them. */
+#define CE_NOALLOC_SCRATCH_FLOATS (8 * 1024 * 1024)
+CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
+                                   const float* d_eigen, float* d_ata, float* d_atb, float* d_info, void* stream);
+
 /* The drop-in entry point (ref: src/main.cu:592-602, src/ControllerEngine.h:11):
  * reads ControllerEngine.config and the .bin files from the current
  * directory, streams n_rounds rounds of n_threads candidates, writes
