@@ -22,9 +22,12 @@
 // multiply-adds.  Failure (no convergence, or a non-finite eigenvalue) yields
 // NaN for the unset eigenvalues; the reference reads unset storage there.
 //
-// GB300 layout: FP64 is a low-rate pipe on this part, so each matrix is owned by
-// one thread (every lane does useful FP64 work; no idle lanes in shuffles) and
-// lives in shared memory as [element][thread], conflict-free across the warp.
+// GB300 layout: FP64 is a low-rate pipe on this part and the iteration is a long
+// chain of small dependent updates, so latency dominates.  Each matrix lives in
+// shared memory ([element][matrix], padded stride) and is owned by a quad of 4
+// lanes that split every row / column loop, which quadruples the warps in flight
+// per SM at the same shared-memory footprint; every element is still updated by
+// exactly one lane in the sequential order, so results do not depend on the split.
 #include <cfloat>
 
 #include "ce_device.cuh"
@@ -32,7 +35,10 @@
 
 namespace ce {
 
-constexpr int EIG_BLOCK = 32;
+constexpr int EIG_BLOCK = 128;              // 32 matrices per block, 4 lanes (a quad) per matrix
+constexpr int EIG_Q = 4;
+constexpr int EIG_M = EIG_BLOCK / EIG_Q;     // matrices per block
+constexpr int EIG_STRIDE = EIG_M + 1;        // padded so the 4 lanes of a quad hit different banks
 constexpr double DEPS = 2.220446049250313080847e-16;
 constexpr double DMIN_ = 2.2250738585072013831e-308;
 
@@ -42,9 +48,23 @@ struct SMat {
     __device__ __forceinline__ double& operator()(int i, int j) const { return p[(i * n + j) * B]; }
 };
 
-// Householder of the column segment T(r0 .. r0+m-1, col): essential part
-// written back into T(r0+1 .., col), returns tau and beta.
-__device__ __forceinline__ void house_inplace(const SMat& T, int r0, int m, int col, double& tau, double& beta) {
+// A quad of lanes owns one matrix: loops over rows / columns are split by 4,
+// scalar decisions are computed redundantly by all four lanes (they read the
+// same values after each __syncwarp), and single-element writes are made by
+// lane 0 of the quad.  Every element is updated by exactly one lane with the
+// same operation sequence as a sequential code, so the results do not depend
+// on the split.
+struct Quad {
+    int q;          // 0..3
+    unsigned mask;  // the quad's lanes
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ bool lead() const { return q == 0; }
+};
+
+// Householder of the column segment T(r0 .. r0+m-1, col): returns tau and beta
+// (read phase only; the caller writes the essential part).
+__device__ __forceinline__ void house_coeffs(const SMat& T, int r0, int m, int col, double& tau, double& beta,
+                                             double& d) {
     const double c0 = T(r0, col);
     double tail = 0.0;
     for (int k = r0 + 1; k < r0 + m; ++k) tail = __dadd_rn(tail, __dmul_rn(T(k, col), T(k, col)));
@@ -52,12 +72,11 @@ __device__ __forceinline__ void house_inplace(const SMat& T, int r0, int m, int 
     if (tail <= DMIN_) {
         tau = 0.0;
         beta = c0;
-        for (int k = r0 + 1; k < r0 + m; ++k) T(k, col) = 0.0;
+        d = 0.0;
     } else {
         beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
         if (c0 >= 0.0) beta = -beta;
-        const double d = __dsub_rn(c0, beta);
-        for (int k = r0 + 1; k < r0 + m; ++k) T(k, col) = __ddiv_rn(T(k, col), d);
+        d = __dsub_rn(c0, beta);
         tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
     }
 }
@@ -82,17 +101,18 @@ __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, d
     }
 }
 
-// H = I - tau [1;ess][1;ess]^T applied from the left to rows r0..r0+m-1,
-// columns c0..c1-1.  ess_at(k) gives essential element k (k < m-1).
+// H = I - tau [1;ess][1;ess]^T from the left on rows r0..r0+m-1, columns
+// c0..c1-1 (columns split over the quad).
 template <typename E>
-__device__ __forceinline__ void house_left(const SMat& T, int r0, int m, int c0, int c1, E ess_at, double tau) {
+__device__ __forceinline__ void house_left(const SMat& T, const Quad& Q, int r0, int m, int c0, int c1, E ess_at,
+                                           double tau) {
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int j = c0; j < c1; ++j) T(r0, j) = __dmul_rn(T(r0, j), f);
+        for (int j = c0 + Q.q; j < c1; j += EIG_Q) T(r0, j) = __dmul_rn(T(r0, j), f);
         return;
     }
     if (tau == 0.0) return;
-    for (int j = c0; j < c1; ++j) {
+    for (int j = c0 + Q.q; j < c1; j += EIG_Q) {
         double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
         tmp = __dadd_rn(tmp, T(r0, j));
@@ -101,16 +121,17 @@ __device__ __forceinline__ void house_left(const SMat& T, int r0, int m, int c0,
     }
 }
 
-// H applied from the right to rows r0..r1-1, columns c0..c0+m-1.
+// H from the right on rows r0..r1-1 (split over the quad), columns c0..c0+m-1.
 template <typename E>
-__device__ __forceinline__ void house_right(const SMat& T, int r0, int r1, int c0, int m, E ess_at, double tau) {
+__device__ __forceinline__ void house_right(const SMat& T, const Quad& Q, int r0, int r1, int c0, int m, E ess_at,
+                                            double tau) {
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int i = r0; i < r1; ++i) T(i, c0) = __dmul_rn(T(i, c0), f);
+        for (int i = r0 + Q.q; i < r1; i += EIG_Q) T(i, c0) = __dmul_rn(T(i, c0), f);
         return;
     }
     if (tau == 0.0) return;
-    for (int i = r0; i < r1; ++i) {
+    for (int i = r0 + Q.q; i < r1; i += EIG_Q) {
         double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
         tmp = __dadd_rn(tmp, T(i, c0));
@@ -150,33 +171,40 @@ __device__ __forceinline__ void rot_pair(double& x, double& y, double c, double 
     y = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
 }
 
-// Eigenvalues of the n x n matrix in T (overwritten).  emit(i, re, im) is called
-// for i = 0..n-1 in Schur order; returns true on success.
+// Eigenvalues of the n x n matrix in T (overwritten), computed by a quad.
+// emit(i, re, im) is called by the quad's lane 0 for i = 0..n-1 in Schur
+// order; returns true on success (the same value in every lane).
 template <typename Emit>
-__device__ bool eig_real(const SMat& T, int n, Emit emit) {
-    // scale
+__device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
+    const int nn = n * n;
     double scale = 0.0;
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) scale = fmax(scale, fabs(T(i, j)));
+    for (int e = 0; e < nn; ++e) scale = fmax(scale, fabs(T(e / n, e % n)));
+    Q.sync();
     bool ok = true;
     if (scale < DMIN_) {
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) T(i, j) = 0.0;
+        for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = 0.0;
+        Q.sync();
     } else {
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) T(i, j) = __ddiv_rn(T(i, j), scale);
+        for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = __ddiv_rn(T(e / n, e % n), scale);
+        Q.sync();
         // Hessenberg reduction
         for (int i = 0; i < n - 1; ++i) {
             const int rs = n - i - 1;
-            double tau, beta;
-            house_inplace(T, i + 1, rs, i, tau, beta);
-            T(i + 1, i) = beta;
+            double tau, beta, d;
+            house_coeffs(T, i + 1, rs, i, tau, beta, d);
+            Q.sync();
+            for (int k = i + 2 + Q.q; k < n; k += EIG_Q) T(k, i) = d == 0.0 ? 0.0 : __ddiv_rn(T(k, i), d);
+            if (Q.lead()) T(i + 1, i) = beta;
+            Q.sync();
             auto ess = [&](int k) { return T(i + 2 + k, i); };
-            house_left(T, i + 1, rs, i + 1, n, ess, tau);
-            house_right(T, 0, n, i + 1, rs, ess, tau);
+            house_left(T, Q, i + 1, rs, i + 1, n, ess, tau);
+            Q.sync();
+            house_right(T, Q, 0, n, i + 1, rs, ess, tau);
+            Q.sync();
         }
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j + 1 < i; ++j) T(i, j) = 0.0;
+        for (int e = Q.q; e < nn; e += EIG_Q)
+            if (e % n + 1 < e / n) T(e / n, e % n) = 0.0;
+        Q.sync();
         // Francis double-shift QR
         double norm = 0.0;
         for (int j = 0; j < n; ++j) {
@@ -196,45 +224,58 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
                     if (fabs(T(il, il - 1)) <= s) break;
                     il--;
                 }
+                Q.sync();
                 if (il == iu) {
-                    T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
-                    if (iu > 0) T(iu, iu - 1) = 0.0;
+                    if (Q.lead()) {
+                        T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
+                        if (iu > 0) T(iu, iu - 1) = 0.0;
+                    }
+                    Q.sync();
                     iu--;
                     iter = 0;
                 } else if (il == iu - 1) {
                     const double p = __dmul_rn(0.5, __dsub_rn(T(iu - 1, iu - 1), T(iu, iu)));
                     const double q = __dadd_rn(__dmul_rn(p, p), __dmul_rn(T(iu, iu - 1), T(iu - 1, iu)));
-                    T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
-                    T(iu - 1, iu - 1) = __dadd_rn(T(iu - 1, iu - 1), exshift);
+                    const double sub = T(iu, iu - 1);
+                    Q.sync();
+                    if (Q.lead()) {
+                        T(iu, iu) = __dadd_rn(T(iu, iu), exshift);
+                        T(iu - 1, iu - 1) = __dadd_rn(T(iu - 1, iu - 1), exshift);
+                    }
+                    Q.sync();
                     if (q >= 0.0) {
                         const double z = sqrt(fabs(q));
                         double c, s;
-                        make_givens(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), T(iu, iu - 1), c, s);
+                        make_givens(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), sub, c, s);
                         if (!(c == 1.0 && s == 0.0)) {
-                            for (int j = iu - 1; j < n; ++j) {
+                            for (int j = iu - 1 + Q.q; j < n; j += EIG_Q) {
                                 double x = T(iu - 1, j), y = T(iu, j);
                                 rot_pair(x, y, c, s);
                                 T(iu - 1, j) = x;
                                 T(iu, j) = y;
                             }
-                            for (int i = 0; i <= iu; ++i) {
+                            Q.sync();
+                            for (int i = Q.q; i <= iu; i += EIG_Q) {
                                 double x = T(i, iu - 1), y = T(i, iu);
                                 rot_pair(x, y, c, s);
                                 T(i, iu - 1) = x;
                                 T(i, iu) = y;
                             }
+                            Q.sync();
                         }
-                        T(iu, iu - 1) = 0.0;
+                        if (Q.lead()) T(iu, iu - 1) = 0.0;
                     }
-                    if (iu > 1) T(iu - 1, iu - 2) = 0.0;
+                    if (Q.lead() && iu > 1) T(iu - 1, iu - 2) = 0.0;
+                    Q.sync();
                     iu -= 2;
                     iter = 0;
                 } else {
-                    // shift
                     double sh0 = T(iu, iu), sh1 = T(iu - 1, iu - 1), sh2 = __dmul_rn(T(iu, iu - 1), T(iu - 1, iu));
+                    Q.sync();
                     if (iter == 10) {
                         exshift = __dadd_rn(exshift, sh0);
-                        for (int i = 0; i <= iu; ++i) T(i, i) = __dsub_rn(T(i, i), sh0);
+                        for (int i = Q.q; i <= iu; i += EIG_Q) T(i, i) = __dsub_rn(T(i, i), sh0);
+                        Q.sync();
                         const double s = __dadd_rn(fabs(T(iu, iu - 1)), fabs(T(iu - 1, iu - 2)));
                         sh0 = __dmul_rn(0.75, s);
                         sh1 = __dmul_rn(0.75, s);
@@ -249,7 +290,8 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
                             s = __dadd_rn(s, __ddiv_rn(__dsub_rn(sh1, sh0), 2.0));
                             s = __dsub_rn(sh0, __ddiv_rn(sh2, s));
                             exshift = __dadd_rn(exshift, s);
-                            for (int i = 0; i <= iu; ++i) T(i, i) = __dsub_rn(T(i, i), s);
+                            for (int i = Q.q; i <= iu; i += EIG_Q) T(i, i) = __dsub_rn(T(i, i), s);
+                            Q.sync();
                             sh0 = sh1 = sh2 = 0.964;
                         }
                     }
@@ -257,7 +299,7 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
                     total++;
                     if (total > max_iter) break;
                     // first Householder vector
-                    double v[3];
+                    double v[3] = {0.0, 0.0, 0.0};
                     int im;
                     for (im = iu - 2; im >= il; --im) {
                         const double Tmm = T(im, im);
@@ -283,39 +325,50 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
                         }
                         double ess[2], tau, beta;
                         house_vec(w, 3, ess, tau, beta);
+                        Q.sync();
                         if (beta != 0.0) {
-                            if (first && k > il) T(k, k - 1) = -T(k, k - 1);
-                            else if (!first) T(k, k - 1) = beta;
-                            auto e = [&](int q) { return ess[q]; };
-                            house_left(T, k, 3, k, n, e, tau);
-                            house_right(T, 0, min(iu, k + 3) + 1, k, 3, e, tau);
+                            if (Q.lead()) {
+                                if (first && k > il) T(k, k - 1) = -T(k, k - 1);
+                                else if (!first) T(k, k - 1) = beta;
+                            }
+                            auto e = [&](int qq) { return ess[qq]; };
+                            house_left(T, Q, k, 3, k, n, e, tau);
+                            Q.sync();
+                            house_right(T, Q, 0, min(iu, k + 3) + 1, k, 3, e, tau);
+                            Q.sync();
                         }
                     }
                     {
                         double w[2] = {T(iu - 1, iu - 2), T(iu, iu - 2)};
                         double ess[2], tau, beta;
                         house_vec(w, 2, ess, tau, beta);
+                        Q.sync();
                         if (beta != 0.0) {
-                            T(iu - 1, iu - 2) = beta;
-                            auto e = [&](int q) { return ess[q]; };
-                            house_left(T, iu - 1, 2, iu - 1, n, e, tau);
-                            house_right(T, 0, iu + 1, iu - 1, 2, e, tau);
+                            if (Q.lead()) T(iu - 1, iu - 2) = beta;
+                            auto e = [&](int qq) { return ess[qq]; };
+                            house_left(T, Q, iu - 1, 2, iu - 1, n, e, tau);
+                            Q.sync();
+                            house_right(T, Q, 0, iu + 1, iu - 1, 2, e, tau);
+                            Q.sync();
                         }
                     }
-                    for (int i = im + 2; i <= iu; ++i) {
+                    for (int i = im + 2 + Q.q; i <= iu; i += EIG_Q) {
                         T(i, i - 2) = 0.0;
                         if (i > im + 2) T(i, i - 3) = 0.0;
                     }
+                    Q.sync();
                 }
             }
         }
         ok = total <= max_iter;
-        if (ok)
-            for (int i = 0; i < n; ++i)
-                for (int j = 0; j < n; ++j) T(i, j) = __dmul_rn(T(i, j), scale);
+        if (ok) {
+            for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = __dmul_rn(T(e / n, e % n), scale);
+            Q.sync();
+        }
     }
     if (!ok) {
-        for (int i = 0; i < n; ++i) emit(i, CUDART_NAN, CUDART_NAN);
+        if (Q.lead())
+            for (int i = 0; i < n; ++i) emit(i, CUDART_NAN, CUDART_NAN);
         return false;
     }
     int i = 0;
@@ -323,10 +376,11 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
         if (i == n - 1 || T(i + 1, i) == 0.0) {
             const double re = T(i, i);
             if (!isfinite(re)) {
-                for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
+                if (Q.lead())
+                    for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
                 return false;
             }
-            emit(i, re, 0.0);
+            if (Q.lead()) emit(i, re, 0.0);
             ++i;
         } else {
             const double p = __dmul_rn(0.5, __dsub_rn(T(i, i), T(i + 1, i + 1)));
@@ -338,11 +392,14 @@ __device__ bool eig_real(const SMat& T, int n, Emit emit) {
             const double z = __dmul_rn(maxval, sqrt(fabs(__dadd_rn(__dmul_rn(p0, p0), __dmul_rn(t0, t1)))));
             const double re = __dadd_rn(T(i + 1, i + 1), p);
             if (!(isfinite(re) && isfinite(z))) {
-                for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
+                if (Q.lead())
+                    for (int k = i; k < n; ++k) emit(k, CUDART_NAN, CUDART_NAN);
                 return false;
             }
-            emit(i, re, z);
-            emit(i + 1, re, -z);
+            if (Q.lead()) {
+                emit(i, re, z);
+                emit(i + 1, re, -z);
+            }
             i += 2;
         }
     }
@@ -363,13 +420,19 @@ __device__ __forceinline__ float lina_entry(const Plant& P, const float* K, cons
     return P.d_a[(i - ns) * MAXD + (j - ns)];
 }
 
+__device__ __forceinline__ Quad make_quad() {
+    const int lane = threadIdx.x & 31;
+    return Quad{lane & 3, 0xFu << (lane & ~3)};
+}
+
 __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int tid = threadIdx.x;
-    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
-    if (c >= run.n) return;
+    const int m = threadIdx.x >> 2;
+    const Quad Q = make_quad();
+    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
+    if (c >= run.n) return;  // the whole quad leaves together
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
     float K[MAXS], L[MAXS];
@@ -378,23 +441,24 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __g
         K[i] = i < ns ? row[i] : 0.0f;
         L[i] = i < ns ? row[ns + i] : 0.0f;
     }
-    SMat T{smem + tid, nt, EIG_BLOCK};
+    SMat T{smem + m, nt, EIG_STRIDE};
     float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int i = 0; i < nt; ++i)
-        for (int j = 0; j < nt; ++j) {
-            const float v = lina_entry(P, K, L, ns, i, j);
-            lrow[i * nt + j] = v;
-            T(i, j) = (double)v;
-        }
+    for (int e = Q.q; e < nt * nt; e += EIG_Q) {
+        const int i = e / nt, j = e % nt;
+        const float v = lina_entry(P, K, L, ns, i, j);
+        lrow[e] = v;
+        T(i, j) = (double)v;
+    }
+    Q.sync();
     if (eig64) {
         double* out = eig64 + c * (int64_t)(2 * nt);
-        eig_real(T, nt, [&](int i, double re, double im) {
+        eig_real(T, Q, nt, [&](int i, double re, double im) {
             out[2 * i] = re;
             out[2 * i + 1] = im;
         });
     } else {
         float* out = eig32 + c * (int64_t)(2 * nt);
-        eig_real(T, nt, [&](int i, double re, double im) {
+        eig_real(T, Q, nt, [&](int i, double re, double im) {
             out[2 * i] = (float)re;
             out[2 * i + 1] = (float)im;
         });
@@ -406,31 +470,33 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const _
                                                           const float* __restrict__ gains, float* __restrict__ lina,
                                                           double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int tid = threadIdx.x;
-    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
+    const int m = threadIdx.x >> 2;
+    const Quad Q = make_quad();
+    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
     if (c >= run.n) return;
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
-    SMat T{smem + tid, nt, EIG_BLOCK};
+    SMat T{smem + m, nt, EIG_STRIDE};
     float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int i = 0; i < nt; ++i)
-        for (int j = 0; j < nt; ++j) {
-            double v;
-            if (i < ns && j < ns) {
-                const double Kj = row[j], Li = row[ns + i];
-                v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
-            } else if (i < ns) {
-                v = (double)row[ns + i] * (double)P.d_c[j - ns];
-            } else if (j < ns) {
-                v = -(double)P.d_bu[i - ns] * (double)row[j];
-            } else {
-                v = P.d_a[(i - ns) * MAXD + (j - ns)];
-            }
-            lrow[i * nt + j] = (float)v;
-            T(i, j) = v;
+    for (int e = Q.q; e < nt * nt; e += EIG_Q) {
+        const int i = e / nt, j = e % nt;
+        double v;
+        if (i < ns && j < ns) {
+            const double Kj = row[j], Li = row[ns + i];
+            v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
+        } else if (i < ns) {
+            v = (double)row[ns + i] * (double)P.d_c[j - ns];
+        } else if (j < ns) {
+            v = -(double)P.d_bu[i - ns] * (double)row[j];
+        } else {
+            v = P.d_a[(i - ns) * MAXD + (j - ns)];
         }
+        lrow[e] = (float)v;
+        T(i, j) = v;
+    }
+    Q.sync();
     double* out = eig64 + c * (int64_t)(2 * nt);
-    eig_real(T, nt, [&](int i, double re, double im) {
+    eig_real(T, Q, nt, [&](int i, double re, double im) {
         out[2 * i] = re;
         out[2 * i + 1] = im;
     });
@@ -445,39 +511,40 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_nominal(const Run run, const __gr
                                                        const float* __restrict__ info, int* __restrict__ nominal,
                                                        int fp64_form) {
     extern __shared__ double smem[];
-    const int tid = threadIdx.x;
-    const int64_t c = (int64_t)blockIdx.x * EIG_BLOCK + tid;
+    const int m = threadIdx.x >> 2;
+    const Quad Q = make_quad();
+    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
     if (c >= run.n) return;
     const float sc0 = info[c * (int64_t)run.info_w + run.info_scoring];
     if (sc0 >= run.unstable_err) {
-        nominal[c] = -1;
+        if (Q.lead()) nominal[c] = -1;
         return;
     }
     const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
     const float* row = gains + c * run.cuda_w;
     const float* la = lina + c * (int64_t)(nt * nt);
-    SMat T{smem + tid, n2, EIG_BLOCK};
-    for (int i = 0; i < ns; ++i) {
+    SMat T{smem + m, n2, EIG_STRIDE};
+    for (int e = Q.q; e < ns * ns; e += EIG_Q) {
+        const int i = e / ns, j = e % ns;
         const float Li = row[ns + i];
-        for (int j = 0; j < ns; ++j) {
-            const float Kj = row[j];
-            if (fp64_form) {
-                T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
-                T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
-                T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
-            } else {
-                T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
-                T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
-                T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
-            }
-            T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
+        const float Kj = row[j];
+        if (fp64_form) {
+            T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
+            T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
+            T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
+        } else {
+            T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
+            T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
+            T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
         }
+        T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
     }
+    Q.sync();
     bool stable = true;
-    const bool ok = eig_real(T, n2, [&](int, double re, double im) {
+    const bool ok = eig_real(T, Q, n2, [&](int, double re, double im) {
         if (hypot(re, im) >= 1.0) stable = false;
     });
-    nominal[c] = (ok && stable) ? 1 : 0;
+    if (Q.lead()) nominal[c] = (ok && stable) ? 1 : 0;
 }
 
 static void set_smem(const void* fn, size_t bytes) {
@@ -486,8 +553,8 @@ static void set_smem(const void* fn, size_t bytes) {
 
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                      cudaStream_t st) {
-    const int grid = (int)((run.n + EIG_BLOCK - 1) / EIG_BLOCK);
-    const size_t smem = (size_t)run.nt * run.nt * EIG_BLOCK * sizeof(double);
+    const int grid = (int)((run.n + EIG_M - 1) / EIG_M);
+    const size_t smem = (size_t)run.nt * run.nt * EIG_STRIDE * sizeof(double);
     if (precision == CE_PRECISION_FP64) {
         set_smem((const void*)k_lina_eig64, smem);
         k_lina_eig64<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, (double*)eig);
@@ -500,8 +567,8 @@ void launch_lina_eig(const Run& run, const Plant& P, int precision, const float*
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const float* info, int* nominal, cudaStream_t st) {
-    const int grid = (int)((run.n + EIG_BLOCK - 1) / EIG_BLOCK);
-    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * EIG_BLOCK * sizeof(double);
+    const int grid = (int)((run.n + EIG_M - 1) / EIG_M);
+    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * EIG_STRIDE * sizeof(double);
     set_smem((const void*)k_nominal, smem);
     k_nominal<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, info, nominal, precision == CE_PRECISION_FP64);
     CE_CUDA(cudaGetLastError());

@@ -110,11 +110,16 @@ __device__ __forceinline__ void mode_of(const Modes<R>& m, int nt, int e, R& sig
 constexpr int FIT_BLOCK = 128;            // 8 candidates per block
 constexpr int FIT_CPB = FIT_BLOCK / 16;
 
+// 16-byte vector of basis values (4 floats or 2 doubles)
+template <typename R> struct vec4_t;
+template <> struct vec4_t<float> { using type = float4; static constexpr int N = 4; };
+template <> struct vec4_t<double> { using type = double2; static constexpr int N = 2; };
+
 template <typename R, typename Sum>
 __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __restrict__ eig, const R* __restrict__ ywin,
                                                    const Sum* __restrict__ summ, R* __restrict__ ata,
                                                    R* __restrict__ atb, float* __restrict__ info) {
-    __shared__ R csm[FIT_CPB][2][MAXNC];
+    __shared__ __align__(16) R csm[FIT_CPB][2][MAXNC];
     const int lane = threadIdx.x & 15;
     const int g = threadIdx.x >> 4;
     const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
@@ -197,21 +202,41 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
         const R y = rsub(yw, yss);
         const R c1 = csm[g][b][r1];
         const R c2 = csm[g][b][r2];
+        // basis values as 16-byte broadcast loads (every lane of the half-warp reads the same address)
+        using V = typename vec4_t<R>::type;
+        constexpr int VN = vec4_t<R>::N;
+        const V* cv = reinterpret_cast<const V*>(&csm[g][b][0]);
+        R cj[32];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const R cj = csm[g][b][j];
-            if (j <= r1) A1[j] = rfma(c1, cj, A1[j]);
-            A2[j] = rfma(c2, cj, A2[j]);
-        }
-        if (nc > 16) {
-#pragma unroll
-            for (int j = 16; j < 32; ++j) {
-                const R cj = csm[g][b][j];
-                if (j <= r2) A2[j] = rfma(c2, cj, A2[j]);
+        for (int q = 0; q < 16 / VN; ++q) {
+            const V v = cv[q];
+            if constexpr (VN == 4) {
+                cj[4 * q] = v.x; cj[4 * q + 1] = v.y; cj[4 * q + 2] = v.z; cj[4 * q + 3] = v.w;
+            } else {
+                cj[2 * q] = v.x; cj[2 * q + 1] = v.y;
             }
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (j <= r1) A1[j] = rfma(c1, cj[j], A1[j]);
+        if (nc > 16) {  // rows 16..31 exist only when nc > 16
+#pragma unroll
+            for (int q = 16 / VN; q < 32 / VN; ++q) {
+                const V v = cv[q];
+                if constexpr (VN == 4) {
+                    cj[4 * q] = v.x; cj[4 * q + 1] = v.y; cj[4 * q + 2] = v.z; cj[4 * q + 3] = v.w;
+                } else {
+                    cj[2 * q] = v.x; cj[2 * q + 1] = v.y;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) A2[j] = rfma(c2, cj[j], A2[j]);
+#pragma unroll
+            for (int j = 16; j < 32; ++j)
+                if (j <= r2) A2[j] = rfma(c2, cj[j], A2[j]);
+            B2 = rfma(c2, y, B2);
+        }
         B1 = rfma(c1, y, B1);
-        B2 = rfma(c2, y, B2);
     }
 
     // AtA is 2nt x 2nt, row stride 2nt; only j <= i < nc is ever accumulated
