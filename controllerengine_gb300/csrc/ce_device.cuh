@@ -83,6 +83,36 @@ __device__ __forceinline__ R run_chain(const Instr* __restrict__ ins, int n, con
     return result;
 }
 
+// The same chain with its sources in shared memory: source column c of this
+// thread is src[c * stride].  The column is warp-uniform, so each interpreted
+// instruction reads its state with one load instead of a select over every
+// column; the loads do not depend on the chain and issue ahead of it.
+template <typename R, int MAXC, bool HAS_SEED>
+__device__ __forceinline__ R run_chain_sm(const Instr* __restrict__ ins, int n, const R* src, int stride, R seed) {
+    R result = R(0);
+#pragma unroll
+    for (int r = 0; r < MAXC; ++r) {
+        if (r >= n) break;
+        const int op = ins[r].op, ak = ins[r].akind, bk = ins[r].bkind;
+        const R pos = src[ins[r].col * stride];
+        R prev;
+        if (r == 0) prev = (HAS_SEED && !isnan(seed)) ? seed : pos;
+        else prev = result;
+        const R a = ak == CE_OPERAND_CONST ? R(ins[r].aval) : (ak == CE_OPERAND_STATE ? pos : prev);
+        const R b = bk == CE_OPERAND_CONST ? R(ins[r].bval) : (bk == CE_OPERAND_STATE ? pos : prev);
+        switch (op) {
+            case 1: result = radd(a, b); break;
+            case 2: result = rsub(a, b); break;
+            case 3: result = rmul(a, b); break;
+            case 4: result = rdiv(a, b); break;
+            case 5: result = fmin(fmax(prev, a), b); break;
+            case 6: result = R((R(0) < a) - (a < R(0))); break;
+            default: break;
+        }
+    }
+    return result;
+}
+
 // ---- complex arithmetic in a fixed operation order ---------------------------
 template <typename R>
 struct cplx {

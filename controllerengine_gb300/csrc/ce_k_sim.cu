@@ -40,6 +40,8 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __
                                                          const float* __restrict__ gains, float* __restrict__ ywin,
                                                          SimSummary* __restrict__ summ, float* __restrict__ traj) {
     __shared__ float stage[8][SIM_BLOCK];
+    __shared__ float srcP[MAXD + 1][SIM_BLOCK];  // plant states, then y in row MAXD (DC / NL sources)
+    __shared__ float srcH[MAXS][SIM_BLOCK];      // observer states (U source)
     const int tid = threadIdx.x;
     const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
     if (c >= run.n) return;  // each thread only touches its own column of `stage`
@@ -69,8 +71,15 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __
         const float padS = poisS ? CUDART_NAN_F : 0.0f;
         const float padD = poisD ? CUDART_NAN_F : 0.0f;
 
+        // chain sources of this step
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) srcP[i][tid] = xp_hi[i];
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) srcH[i][tid] = xh_hi[i];
+
         // plant output
-        const float y = run_chain<float, NDC, MAX_DC, false>(P.dc, P.n_dc, xp_hi, -1, 0.0f, 0.0f);
+        const float y = run_chain_sm<float, MAX_DC, false>(P.dc, P.n_dc, &srcP[0][tid], SIM_BLOCK, 0.0f);
+        srcP[MAXD][tid] = y;
 
         // outputs: fit window, steady-state sum, extremes, optional full trajectory
         {
@@ -102,7 +111,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __
         if (NSC < MAXS) kx = __fadd_rn(kx, padS);
         const float ref = t < run.ref_step_id ? 0.0f : run.ref_amp;
         const float u_raw = __fmaf_rn(N, ref, -kx);
-        const float u = run_chain<float, NSC, MAX_U, true>(P.u, P.n_u, xh_hi, -1, 0.0f, u_raw);
+        const float u = run_chain_sm<float, MAX_U, true>(P.u, P.n_u, &srcH[0][tid], SIM_BLOCK, u_raw);
 
         // observer output error
         float yh = 0.0f;
@@ -145,7 +154,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __
         float W[MAXW];
 #pragma unroll
         for (int k = 0; k < MAXW; ++k)
-            W[k] = run_chain<float, NDC, MAX_NL, false>(P.nl[k], P.n_nl[k], xp_hi, MAXD, y, 0.0f);
+            W[k] = run_chain_sm<float, MAX_NL, false>(P.nl[k], P.n_nl[k], &srcP[0][tid], SIM_BLOCK, 0.0f);
 
         // plant increment (Ad-I)xp + Bu u + Bw W, then double-float add
         float ph[NDC], pl[NDC];
