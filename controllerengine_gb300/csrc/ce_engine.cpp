@@ -5,11 +5,11 @@
 // for the Eigen stages.  Here a session keeps the decoded plant tables and the
 // plant's frequency response on the host (they travel to the kernels in the
 // launch parameters) and a grow-only set of device scratch buffers; one
-// evaluation is six kernel launches on one stream, with the FP64 eigensolve
-// forked onto a second stream so it overlaps the FP32 simulation:
+// evaluation is six kernel launches, the two FP64 eigensolves on a second
+// stream so they overlap the FP32 simulation and modal fit:
 //
-//   fork ─┬─ k_lina_eig (FP64 pipe) ──┐
-//         └─ k_sim      (FP32 pipe) ──┴─ join ─ k_fit ─ k_modal ─ k_nominal ─ k_sweep
+//   fork ─┬─ k_lina_eig (FP64) ──┬── k_nominal (FP64) ──────────┐
+//         └─ k_sim      (FP32) ──┴─ k_fit ─ k_modal (FP32) ──────┴─ k_sweep
 //
 // Only gains in and cost rows out cross the host boundary.
 #include <cmath>
@@ -149,7 +149,7 @@ struct ce_session {
     double* d_fgrid64 = nullptr;
     ce::Buffers buf;
     cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_eig = nullptr, ev_join = nullptr;
     int64_t launches = 0;
     int device = 0;
     // stage timing (ce_session_set_profiling)
@@ -298,13 +298,17 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     };
     CE_CUDA(cudaEventRecord(s->ev_fork, st));
     CE_CUDA(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    // side stream: the FP64 eigensolves (LIN_A, then the nominal closed loop of
+    // every candidate LIN_A does not flag) run under the FP32 simulation and fit
     timed(0, s->side, [&] { launch_lina_eig(r, P, prec, d_gains, b.lina, b.eig, s->side); });
+    CE_CUDA(cudaEventRecord(s->ev_eig, s->side));
+    timed(4, s->side, [&] { launch_nominal(r, P, prec, d_gains, b.lina, b.eig, b.nominal, s->side); });
     CE_CUDA(cudaEventRecord(s->ev_join, s->side));
     timed(1, st, [&] { launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st); });
-    CE_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
+    CE_CUDA(cudaStreamWaitEvent(st, s->ev_eig, 0));
     timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, st); });
     timed(3, st, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, st); });
-    timed(4, st, [&] { launch_nominal(r, P, prec, d_gains, b.lina, d_info, b.nominal, st); });
+    CE_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
     timed(5, st, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, st); });
     s->launches += 6;
 }
@@ -469,6 +473,7 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     CE_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     CE_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
     CE_CUDA(cudaMalloc((void**)&s->d_fgrid32, s->fgrid32.size() * sizeof(float)));
     CE_CUDA(cudaMalloc((void**)&s->d_fgrid64, s->fgrid64.size() * sizeof(double)));
@@ -501,6 +506,7 @@ void destroy_session(ce_session* s) {
     if (s->d_fgrid32) cudaFree(s->d_fgrid32);
     if (s->d_fgrid64) cudaFree(s->d_fgrid64);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_eig) cudaEventDestroy(s->ev_eig);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->side) cudaStreamDestroy(s->side);

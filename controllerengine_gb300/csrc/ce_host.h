@@ -37,7 +37,7 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                      cudaStream_t st);
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
-                    const float* info, int* nominal, cudaStream_t st);
+                    const void* eig, int* nominal, cudaStream_t st);
 void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
                 void* atb, float* info, cudaStream_t st);
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,

@@ -22,12 +22,14 @@
 // multiply-adds.  Failure (no convergence, or a non-finite eigenvalue) yields
 // NaN for the unset eigenvalues; the reference reads unset storage there.
 //
-// GB300 layout: FP64 is a low-rate pipe on this part and the iteration is a long
-// chain of small dependent updates, so latency dominates.  Each matrix lives in
-// shared memory ([element][matrix], padded stride) and is owned by a quad of 4
-// lanes that split every row / column loop, which quadruples the warps in flight
-// per SM at the same shared-memory footprint; every element is still updated by
-// exactly one lane in the sequential order, so results do not depend on the split.
+// GB300 layout: FP64 is a low-rate pipe on this part (1/64 of FP32) and these
+// kernels are FP64-issue bound (ncu: FP64 pipe ~80% busy).  Each matrix lives in
+// shared memory as [element][matrix] and is owned by EIG_Q lanes that split the
+// row / column loops (every element is still updated by exactly one lane in the
+// sequential order, so results do not depend on EIG_Q).  EIG_Q = 1 -- one lane
+// per matrix -- issues the fewest FP64 instructions per matrix: with 4 lanes the
+// scalar parts (Householder vectors, shifts, deflation tests) cost a warp
+// instruction per 8 matrices instead of per 32.
 #include <cfloat>
 
 #include "ce_device.cuh"
@@ -35,8 +37,8 @@
 
 namespace ce {
 
-constexpr int EIG_BLOCK = 128;              // 32 matrices per block, 4 lanes (a quad) per matrix
-constexpr int EIG_Q = 4;
+constexpr int EIG_Q = 1;                     // lanes per matrix (see the note on the layout above)
+constexpr int EIG_BLOCK = 32 * EIG_Q;        // 32 matrices per block
 constexpr int EIG_M = EIG_BLOCK / EIG_Q;     // matrices per block
 constexpr int EIG_STRIDE = EIG_M + 1;        // padded so the 4 lanes of a quad hit different banks
 constexpr double DEPS = 2.220446049250313080847e-16;
@@ -422,14 +424,15 @@ __device__ __forceinline__ float lina_entry(const Plant& P, const float* K, cons
 
 __device__ __forceinline__ Quad make_quad() {
     const int lane = threadIdx.x & 31;
-    return Quad{lane & 3, 0xFu << (lane & ~3)};
+    const int q = lane % EIG_Q;
+    return Quad{q, ((EIG_Q == 32) ? 0xFFFFFFFFu : ((1u << EIG_Q) - 1u)) << (lane - q)};
 }
 
 __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x >> 2;
+    const int m = threadIdx.x / EIG_Q;
     const Quad Q = make_quad();
     const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
     if (c >= run.n) return;  // the whole quad leaves together
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const _
                                                           const float* __restrict__ gains, float* __restrict__ lina,
                                                           double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x >> 2;
+    const int m = threadIdx.x / EIG_Q;
     const Quad Q = make_quad();
     const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
     if (c >= run.n) return;
@@ -504,21 +507,37 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const _
 
 // Nominal closed loop of the margin check (ref: src/allmargin.cu:50-87):
 // Acl_nom = [OPEN_A - (D L) K^T, -L C^T; B K^T, A] with OPEN_A = LIN_A[:ns,:ns]
-// and (A, B, C, D) the margin plant.  Only candidates with sc0 < unstable_err
-// are solved; nominal[c] = 1 if stable, 0 if not, -1 if not needed.
+// and (A, B, C, D) the margin plant.  nominal[c] = 1 if stable, 0 if not, -1
+// if the candidate is modal-unstable (the sweep never reads it then).
 __global__ void __launch_bounds__(EIG_BLOCK) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
-                                                       const float* __restrict__ info, int* __restrict__ nominal,
+                                                       const void* __restrict__ eig, int* __restrict__ nominal,
                                                        int fp64_form) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x >> 2;
+    const int m = threadIdx.x / EIG_Q;
     const Quad Q = make_quad();
     const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
     if (c >= run.n) return;
-    const float sc0 = info[c * (int64_t)run.info_w + run.info_scoring];
-    if (sc0 >= run.unstable_err) {
-        if (Q.lead()) nominal[c] = -1;
-        return;
+    // Candidates the modal stage will flag unstable (max |lambda(LIN_A)| > 1, the
+    // same float test) never reach the sweep; everything else is solved here,
+    // independent of the modal stage, so this kernel can run concurrently with it.
+    {
+        bool unstable;
+        if (fp64_form) {
+            double mx = 0.0;
+            const double* e = static_cast<const double*>(eig) + c * (int64_t)(2 * run.nt);
+            for (int i = 0; i < run.nt; ++i) mx = fmax(mx, hypot(e[2 * i], e[2 * i + 1]));
+            unstable = mx > 1.0;
+        } else {
+            float mx = 0.0f;
+            const float* e = static_cast<const float*>(eig) + c * (int64_t)(2 * run.nt);
+            for (int i = 0; i < run.nt; ++i) mx = fmaxf(mx, hypotf(e[2 * i], e[2 * i + 1]));
+            unstable = mx > 1.0f;
+        }
+        if (unstable) {
+            if (Q.lead()) nominal[c] = -1;
+            return;
+        }
     }
     const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
     const float* row = gains + c * run.cuda_w;
@@ -566,11 +585,11 @@ void launch_lina_eig(const Run& run, const Plant& P, int precision, const float*
 }
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
-                    const float* info, int* nominal, cudaStream_t st) {
+                    const void* eig, int* nominal, cudaStream_t st) {
     const int grid = (int)((run.n + EIG_M - 1) / EIG_M);
     const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * EIG_STRIDE * sizeof(double);
     set_smem((const void*)k_nominal, smem);
-    k_nominal<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, info, nominal, precision == CE_PRECISION_FP64);
+    k_nominal<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, eig, nominal, precision == CE_PRECISION_FP64);
     CE_CUDA(cudaGetLastError());
 }
 

@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
                 cj[2 * q] = v.x; cj[2 * q + 1] = v.y;
             }
         }
+        // all 16 / 32 slots accumulate: slots j > row hold values that are never
+        // stored (only j <= row is written out), and skipping the predicates keeps
+        // the integer pipe free
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            if (j <= r1) A1[j] = rfma(c1, cj[j], A1[j]);
+        for (int j = 0; j < 16; ++j) A1[j] = rfma(c1, cj[j], A1[j]);
         if (nc > 16) {  // rows 16..31 exist only when nc > 16
 #pragma unroll
             for (int q = 16 / VN; q < 32 / VN; ++q) {
@@ -230,10 +232,7 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
                 }
             }
 #pragma unroll
-            for (int j = 0; j < 16; ++j) A2[j] = rfma(c2, cj[j], A2[j]);
-#pragma unroll
-            for (int j = 16; j < 32; ++j)
-                if (j <= r2) A2[j] = rfma(c2, cj[j], A2[j]);
+            for (int j = 0; j < 32; ++j) A2[j] = rfma(c2, cj[j], A2[j]);
             B2 = rfma(c2, y, B2);
         }
         B1 = rfma(c1, y, B1);
