@@ -159,6 +159,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -183,6 +184,8 @@ def main():
     n = problem.cuda_mx.shape[0]
     cfg = ce.EngineConfig.parse(problem.config_text)
     sess = ce.Session(cfg, problem.plant)
+    if sess.sim_kernel != a.sim_kernel:
+        sess.set_sim_kernel(a.sim_kernel)  # raises with the compiler's log if specialising fails
 
     dev = torch.device("cuda", local)
     g = torch.from_numpy(problem.cuda_mx).to(dev)
@@ -299,7 +302,8 @@ def main():
         "dtype": "f32 (f64 eigensolve)", "data": "synthetic (seeded eight_state workload, random-draw plant)",
         "config": {"workload": "eight_state: 65536 candidates, 8-state plant, 4 nonlinear terms, 10000 steps, "
                                "400 sweep points", "candidates_per_gpu": n, "time": a.time, "freq": a.freq,
-                   "l2": "256 MB buffer written between timed steps (outside the events)"},
+                   "l2": "256 MB buffer written between timed steps (outside the events)",
+                   "sim_kernel": sess.sim_kernel},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": roof,

@@ -25,8 +25,10 @@ EXPORTED_SYMBOLS = (
     "ce_session_create", "ce_session_destroy", "ce_session_set_precision", "ce_session_get_config",
     "ce_evaluate", "ce_evaluate_diagnostics", "ce_evaluate_device", "ce_session_kernel_launches",
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
+    "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
     "RunControllerEngine",
 )
+SIM_TABLE, SIM_SPECIALISED = 0, 1
 NUM_STAGES = 6
 STAGE_NAMES = ("lina_eig", "sim", "fit", "modal", "nominal", "sweep")
 
@@ -108,6 +110,12 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
                                        C.c_void_p]
     lib.ce_session_kernel_launches.argtypes = [C.c_void_p]
     lib.ce_session_kernel_launches.restype = C.c_int64
+    lib.ce_session_set_sim_kernel.argtypes = [C.c_void_p, C.c_int32]
+    lib.ce_session_sim_kernel.argtypes = [C.c_void_p]
+    lib.ce_session_sim_kernel.restype = C.c_int32
+    lib.ce_session_sim_log.argtypes = [C.c_void_p]
+    lib.ce_session_sim_log.restype = C.c_char_p
+    lib.ce_sim_specialised_source.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]
     lib.ce_session_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.ce_session_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.ce_measure_fma_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]

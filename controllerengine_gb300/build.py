@@ -26,7 +26,10 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ce_k_sim.cu", "ce_k_eig.cu", "ce_k_modal.cu", "ce_k_sweep.cu", "ce_k_calib.cu", "ce_noalloc.cu"]
-CPP_SOURCES = ["ce_config.cpp", "ce_engine.cpp"]
+CPP_SOURCES = ["ce_config.cpp", "ce_engine.cpp", "ce_jit.cpp"]
+# headers the run-time specialiser (ce_jit.cpp) hands to NVRTC, by the name they are #included under
+JIT_HEADERS = [("ce_sim_body.cuh", "ce_sim_body.cuh"), ("ce_device.cuh", "ce_device.cuh"),
+               ("ce_internal.h", "ce_internal.h"), ("../../include/controller_engine.h", None)]
 
 
 def _run(cmd: list[str]) -> str:
@@ -47,6 +50,19 @@ def _digest() -> str:
     return h.hexdigest()[:16]
 
 
+def _write_jit_headers(path: Path):
+    parts = ["// generated by controllerengine_gb300/build.py: headers compiled by NVRTC at run time",
+             "struct JitHeader { const char* name; const char* text; };",
+             "const JitHeader kJitHeaders[] = {"]
+    for name, rel in JIT_HEADERS:
+        src = (CSRC / rel) if rel else (ROOT / "include" / "controller_engine.h")
+        text = src.read_text()
+        assert ")CE_SRC\"" not in text
+        parts.append(f'    {{"{name}", R"CE_SRC({text})CE_SRC"}},')
+    parts.append("};")
+    path.write_text("\n".join(parts) + "\n")
+
+
 def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> Path:
     """Compile and link the library; returns its path.  Skips work if sources are unchanged."""
     OUT.mkdir(exist_ok=True)
@@ -58,7 +74,10 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     if objdir.exists():
         shutil.rmtree(objdir)
     objdir.mkdir()
-    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
+    gen = OUT / "gen"
+    gen.mkdir(exist_ok=True)
+    _write_jit_headers(gen / "ce_jit_src.inc")
+    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC), "-I", str(gen)]
     jobs = []
     for src in CU_SOURCES:
         obj = objdir / (src + ".o")
@@ -70,6 +89,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     for src in CPP_SOURCES:
         obj = objdir / (src + ".o")
         cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden",
+               f'-DCE_CUDA_INCLUDE="{CUDA_HOME / "include"}"',
                "-I", str(CUDA_HOME / "include"), *inc, "-c", str(CSRC / src), "-o", str(obj)]
         jobs.append(cmd)
     logs = []
@@ -78,7 +98,9 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
             logs.append(out)
     objs = [str(objdir / (s + ".o")) for s in CU_SOURCES + CPP_SOURCES]
     tmp = OUT / (LIB.name + ".tmp")
-    _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"])
+    _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs,
+          "-L", str(CUDA_HOME / "lib64"), "-lnvrtc", f"-Xlinker=-rpath,{CUDA_HOME / 'lib64'}",
+          "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)
     stamp.write_text(dig)
     if verbose or ptxas_info:

@@ -9,7 +9,9 @@
 // host stages (Eigen on x86) never fuse.
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
+#endif
 #include <math_constants.h>
 #include "ce_internal.h"
 

@@ -141,6 +141,11 @@ struct ce_session {
     int precision = CE_PRECISION_MIXED;
     std::vector<ce::Plant> plants;
     std::vector<std::string> plant_err;
+    // simulation kernel of each plant in mixed precision: compiled for its
+    // instruction program (ce_jit.cpp), or null for the table-driven kernel
+    int sim_kind = CE_SIM_SPECIALISED;
+    std::vector<const void*> sim_kernel;
+    std::string sim_log;
     std::vector<float> alpha32;
     std::vector<double> alpha64;
     std::vector<float> fgrid32;   // n_plants * freq * 8
@@ -304,7 +309,11 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     CE_CUDA(cudaEventRecord(s->ev_eig, s->side));
     timed(4, s->side, [&] { launch_nominal(r, P, prec, d_gains, b.lina, b.eig, b.nominal, s->side); });
     CE_CUDA(cudaEventRecord(s->ev_join, s->side));
-    timed(1, st, [&] { launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st); });
+    const void* sk = prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
+    timed(1, st, [&] {
+        if (sk) launch_sim_specialised(sk, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, traj ? b.traj : nullptr, st);
+        else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st);
+    });
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_eig, 0));
     timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, st); });
     timed(3, st, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, st); });
@@ -449,6 +458,23 @@ void build_fgrid(ce_session* s, int p) {
     }
 }
 
+// Select the simulation kernel of every plant.  CE_SIM_SPECIALISED compiles
+// each distinct instruction program once per process (NVRTC); a failure throws
+// with the compiler's log and leaves the session's kernels unchanged.
+void select_sim_kernel(ce_session* s, int kind) {
+    std::vector<const void*> ks(s->n_plants, nullptr);
+    if (kind == CE_SIM_SPECIALISED) {
+        for (int p = 0; p < s->n_plants; ++p) {
+            std::string log;
+            ks[p] = specialise_sim(s->plants[p], s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                   s->cfg.discrete_dim <= 4 ? 4 : 8, log);
+            if (!ks[p]) fail("specialising the simulation kernel of plant {} failed: {}", p, log);
+        }
+    }
+    s->sim_kernel = ks;
+    s->sim_kind = kind;
+}
+
 void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants, ce_session** out) {
     if (!cfg_in || !plant || !out) fail("ce_session_create: null argument");
     if (n_plants < 1) fail("ce_session_create: n_plants must be >= 1, got {}", n_plants);
@@ -458,6 +484,8 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     if (c.statespace_dim < 1 || c.statespace_dim > MAXS || c.discrete_dim < 1 || c.discrete_dim > MAXD ||
         c.nonlin_dim < 0 || c.nonlin_dim > MAXW || c.total_dim != c.statespace_dim + c.discrete_dim)
         fail("ce_session_create: config dimensions are out of range or not derived");
+    if (c.dc_dim != c.discrete_dim || c.u_dim != c.statespace_dim || c.nl_dim != c.discrete_dim + 1)
+        fail("ce_session_create: instruction table widths are not derived from the dimensions");
     s->n_plants = n_plants;
     s->plants.resize(n_plants);
     s->plant_err.assign(n_plants, std::string());
@@ -479,6 +507,19 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     CE_CUDA(cudaMalloc((void**)&s->d_fgrid64, s->fgrid64.size() * sizeof(double)));
     CE_CUDA(cudaMemcpy(s->d_fgrid32, s->fgrid32.data(), s->fgrid32.size() * sizeof(float), cudaMemcpyHostToDevice));
     CE_CUDA(cudaMemcpy(s->d_fgrid64, s->fgrid64.data(), s->fgrid64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // Default: the specialised kernel.  CE_SIM_KERNEL=table in the environment
+    // selects the table-driven one; if compiling fails the session keeps the
+    // table-driven kernel and ce_session_sim_kernel reports which one runs.
+    s->sim_kernel.assign(n_plants, nullptr);
+    s->sim_kind = CE_SIM_TABLE;
+    const char* env = std::getenv("CE_SIM_KERNEL");
+    if (!(env && std::string(env) == "table")) {
+        try {
+            select_sim_kernel(s.get(), CE_SIM_SPECIALISED);
+        } catch (const std::exception& e) {
+            s->sim_log = e.what();
+        }
+    }
     *out = s.release();
 }
 
@@ -763,6 +804,35 @@ CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n, 
 }
 
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s) { return s ? s->launches : 0; }
+
+CE_EXPORT int ce_session_set_sim_kernel(ce_session* s, int32_t kind) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        if (kind != CE_SIM_TABLE && kind != CE_SIM_SPECIALISED) fail("unknown simulation kernel kind {}", kind);
+        select_sim_kernel(s, kind);
+    });
+}
+
+CE_EXPORT int32_t ce_session_sim_kernel(const ce_session* s) { return s ? s->sim_kind : -1; }
+
+CE_EXPORT const char* ce_session_sim_log(const ce_session* s) { return s ? s->sim_log.c_str() : ""; }
+
+CE_EXPORT int ce_sim_specialised_source(const ce_session* s, int32_t plant_index, char* buf, int64_t cap,
+                                        int64_t* size) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        if (plant_index < 0 || plant_index >= s->n_plants)
+            fail("plant index {} out of range [0, {})", plant_index, s->n_plants);
+        const std::string src = specialised_source(s->plants[plant_index], s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                                   s->cfg.discrete_dim <= 4 ? 4 : 8);
+        if (size) *size = (int64_t)src.size() + 1;
+        if (buf && cap > 0) {
+            const size_t k = std::min<size_t>(src.size(), (size_t)cap - 1);
+            std::memcpy(buf, src.data(), k);
+            buf[k] = '\0';
+        }
+    });
+}
 
 CE_EXPORT int ce_session_set_profiling(ce_session* s, int32_t on) {
     return guarded([&] {

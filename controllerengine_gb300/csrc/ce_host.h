@@ -47,6 +47,13 @@ void launch_sweep(const Run& run, int precision, const float* gains, const float
 
 double measure_fma_rate(bool fp64);
 
+// Simulation kernel specialised to a plant's instruction program (ce_jit.cpp):
+// returns the compiled kernel (cached per program), or nullptr with `log` set.
+const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log);
+std::string specialised_source(const Plant& P, int ns, int nd);
+void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
+                            SimSummary* summ, float* traj, cudaStream_t st);
+
 const Plant* session_plant(const ce_session* s, int plant);
 const ce_config* session_config(const ce_session* s);
 int session_plants(const ce_session* s);

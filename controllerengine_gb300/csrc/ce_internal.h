@@ -8,11 +8,18 @@
 // global __constant__ copy, ref: src/main.cu:56-87, which makes it non-reentrant).
 #pragma once
 
+#ifdef __CUDACC_RTC__
+typedef int int32_t;
+typedef long long int64_t;
+#else
 #include <stdint.h>
 #include <cuda_runtime.h>
+#endif
 #include "../../include/controller_engine.h"
 
 namespace ce {
+
+constexpr int SIM_BLOCK = 64;  // threads per simulation block (one candidate per thread)
 
 constexpr int MAXS = CE_MAX_STATESPACE_DIM;   // 8
 constexpr int MAXD = CE_MAX_DISCRETE_DIM;     // 8

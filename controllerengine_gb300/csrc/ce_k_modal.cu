@@ -38,6 +38,8 @@ __device__ __forceinline__ float rcos(float x) { return cosf(x); }
 __device__ __forceinline__ double rcos(double x) { return cos(x); }
 __device__ __forceinline__ float rsin(float x) { return sinf(x); }
 __device__ __forceinline__ double rsin(double x) { return sin(x); }
+__device__ __forceinline__ void rsincos(float x, float& s, float& c) { sincosf(x, &s, &c); }
+__device__ __forceinline__ void rsincos(double x, double& s, double& c) { sincos(x, &s, &c); }
 __device__ __forceinline__ float rlog(float x) { return logf(x); }
 __device__ __forceinline__ double rlog(double x) { return log(x); }
 __device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
@@ -195,8 +197,10 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
         if (lane < unique) {
             const R decay = rexp(rfma(sig, tval, -shift));
             const R arg = rmul(om, tval);
-            csm[g][b][2 * lane] = rmul(decay, rcos(arg));
-            csm[g][b][2 * lane + 1] = rmul(decay, rsin(arg));
+            R sn, cs;
+            rsincos(arg, sn, cs);  // one argument reduction for both
+            csm[g][b][2 * lane] = rmul(decay, cs);
+            csm[g][b][2 * lane + 1] = rmul(decay, sn);
         }
         __syncwarp(hmask);
         const R y = rsub(yw, yss);

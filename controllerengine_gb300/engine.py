@@ -194,6 +194,27 @@ class Session:
     def kernel_launches(self) -> int:
         return int(_lib().ce_session_kernel_launches(self._h))
 
+    @property
+    def sim_kernel(self) -> str:
+        """"specialised" (compiled for the plant's instruction program) or "table"."""
+        k = int(_lib().ce_session_sim_kernel(self._h))
+        return {_ffi.SIM_TABLE: "table", _ffi.SIM_SPECIALISED: "specialised"}[k]
+
+    def set_sim_kernel(self, kind: str):
+        k = {"table": _ffi.SIM_TABLE, "specialised": _ffi.SIM_SPECIALISED}[kind]
+        _check(_lib().ce_session_set_sim_kernel(self._h, k))
+
+    @property
+    def sim_log(self) -> str:
+        return _lib().ce_session_sim_log(self._h).decode()
+
+    def specialised_source(self, plant: int = 0) -> str:
+        size = C.c_int64(0)
+        _check(_lib().ce_sim_specialised_source(self._h, plant, None, 0, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        _check(_lib().ce_sim_specialised_source(self._h, plant, buf, size.value, C.byref(size)))
+        return buf.value.decode()
+
     def set_profiling(self, on: bool):
         _check(_lib().ce_session_set_profiling(self._h, 1 if on else 0))
 

@@ -19,7 +19,9 @@
 #ifndef CONTROLLER_ENGINE_H
 #define CONTROLLER_ENGINE_H
 
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#endif
 
 #if defined(_WIN32)
 #define CE_EXPORT __declspec(dllexport)
@@ -135,6 +137,10 @@ typedef struct ce_diagnostics {
 
 typedef struct ce_session ce_session;
 
+/* The functions are host API; device code compiled at run time (NVRTC) sees
+ * only the constants and structures above. */
+#ifndef __CUDACC_RTC__
+
 /* Message of the last failed call on this thread ("" if none). */
 CE_EXPORT const char* ce_last_error(void);
 
@@ -191,6 +197,26 @@ CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n,
 /* Launches of this library's kernels since the session was created. */
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s);
 
+/* Simulation kernel selection (no counterpart in the reference, whose kernel
+ * always interprets the decoded instruction tables).
+ * CE_SIM_SPECIALISED: the plant's DC/U/NL programs are compiled at session
+ * creation (NVRTC, once per distinct program per process) into straight-line
+ * code; results are bit-identical to the table-driven kernel's.
+ * CE_SIM_TABLE: the table-driven kernel, which needs no compile step.
+ * Sessions start specialised unless the environment sets
+ * CE_SIM_KERNEL=table or compiling fails (then ce_session_sim_log holds the
+ * reason).  ce_session_set_sim_kernel fails, leaving the selection unchanged,
+ * if compiling fails.  FP64 precision always uses its own table-driven kernel. */
+#define CE_SIM_TABLE 0
+#define CE_SIM_SPECIALISED 1
+CE_EXPORT int ce_session_set_sim_kernel(ce_session* s, int32_t kind);
+CE_EXPORT int32_t ce_session_sim_kernel(const ce_session* s);
+CE_EXPORT const char* ce_session_sim_log(const ce_session* s);
+/* The CUDA source generated for one plant's program (NUL-terminated; *size
+ * receives the length including the NUL).  Copies at most cap-1 characters. */
+CE_EXPORT int ce_sim_specialised_source(const ce_session* s, int32_t plant_index, char* buf, int64_t cap,
+                                        int64_t* size);
+
 /* Measurement hooks (no counterpart in the reference).  With profiling on,
  * every stage launch is bracketed by CUDA events on the stream it runs on;
  * ce_session_stage_times waits for them and returns, per stage, the summed
@@ -237,6 +263,8 @@ CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index, int64_t n
  * dump_diagnostics is set).  Returns 0, or 1 after appending the message to
  * error.log. */
 CE_EXPORT int RunControllerEngine(void);
+
+#endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }
