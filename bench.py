@@ -42,6 +42,21 @@ def workload_args(a):
     return dict(n=a.candidates, time=a.time, freq=a.freq)
 
 
+def fit_ops(eigen, steps):
+    """FP32 operations of the modal fit over one batch: for each stable candidate,
+    per window step, the normal-equation FMAs nc(nc+1)/2 + nc and 5 operations per
+    mode for the basis arguments and products (expf and sin/cos counted as 0).
+    `eigen` is (n, nt, 2); a mode equal in (re, |im|) to its predecessor is a
+    conjugate duplicate and does not enter the basis."""
+    re, im = eigen[..., 0].astype(np.float64), eigen[..., 1].astype(np.float64)
+    dup = np.zeros(re.shape, bool)
+    dup[:, 1:] = (re[:, 1:] == re[:, :-1]) & (np.abs(im[:, 1:]) == np.abs(im[:, :-1]))
+    unique = re.shape[1] - dup.sum(1)
+    stable = np.hypot(re, im).max(1) <= 1.0
+    nc = 2 * unique[stable]
+    return float(steps * (nc * (nc + 1) // 2 + nc + 5 * unique[stable]).sum())
+
+
 def sim_ops_per_step(ns, nd, nw, n_instr):
     """FP32 operations of one simulation step (FMA, add and mul each count 1)."""
     dots = 4 * ns + 2                      # K.(hi,lo), C.(hi,lo), D u, u_raw
@@ -197,6 +212,11 @@ def main():
     def step():
         sess.evaluate_device(n, g.data_ptr(), info_in.data_ptr(), info_out.data_ptr(), stream=stream.cuda_stream)
 
+    # eigenvalues of every candidate (untimed): the fit's work depends on the mode count
+    _, diag = sess.evaluate_diagnostics(problem.cuda_mx, problem.info_mx, want=("eigen",))
+    fit_work = fit_ops(diag["eigen"].reshape(n, cfg.total_dim, 2), cfg.fit_steps)
+    del diag
+
     for _ in range(a.warmup):
         flush.zero_()
         step()
@@ -281,18 +301,22 @@ def main():
     fp32_rate = measure_fma_rate(False)
     fp64_rate = measure_fma_rate(True)
     n_instr = 1 + 1 + 10  # DC, U and the NL instructions of this workload
-    roof = None
-    if dom == "sim":
-        work = sim_ops_per_step(8, 8, 4, n_instr) * a.time * n
-        ach = work / (per_launch[dom] * 1e-3) / 1e12
-        peak = fp32_rate / 1e12
-        roof = {"kernel": "k_sim_mixed<8,8>", "bound": "fp32", "achieved": ach, "peak": peak, "unit": "Tops/s",
-                "frac": ach / peak, "traffic": None,
-                "work_per_launch": f"{sim_ops_per_step(8, 8, 4, n_instr)} FP32 ops/step x {a.time} steps x {n}",
-                "peak_source": "measured FP32 FFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"}
-    else:
-        roof = {"kernel": dom, "bound": "fp32", "achieved": None, "peak": fp32_rate / 1e12, "unit": "Tops/s",
-                "frac": None, "traffic": None}
+    peak = fp32_rate / 1e12
+    src = "measured FP32 FFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"
+    sim_name = "ce_sim_specialised (8,8)" if sess.sim_kernel == "specialised" else "k_sim_mixed<8,8>"
+    work = {"sim": (sim_name, sim_ops_per_step(8, 8, 4, n_instr) * a.time * n,
+                    f"{sim_ops_per_step(8, 8, 4, n_instr)} FP32 ops/step x {a.time} steps x {n} candidates"),
+            "fit": ("k_fit<float>", fit_work,
+                    f"normal-equation FMAs + 5 basis ops per mode-step, {cfg.fit_steps} window steps, "
+                    f"summed over the stable candidates ({fit_work / 1e9:.2f} G ops)")}
+    rooflines = {}
+    for st, (kname, ops, desc) in work.items():
+        ach = ops / (per_launch[st] * 1e-3) / 1e12 if per_launch.get(st) else None
+        rooflines[st] = {"kernel": kname, "bound": "fp32", "achieved": ach, "peak": peak, "unit": "Tops/s",
+                         "frac": ach / peak if ach else None, "traffic": None, "work_per_launch": desc,
+                         "peak_source": src}
+    roof = rooflines.get(dom) or {"kernel": dom, "bound": "fp64" if dom in ("lina_eig", "nominal") else "fp32",
+                                  "achieved": None, "peak": None, "unit": "Tops/s", "frac": None, "traffic": None}
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text())["hbm_gbs"] if peaks_file.exists() else 6800.0
     win_bytes = n * cfg.fit_steps * 4 * 2  # fit window written by k_sim and read by k_fit
@@ -307,6 +331,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": roof,
+        "rooflines_by_stage": rooflines,
         "stages_ms_per_launch": per_launch,
         "fit_window_hbm": {"bytes_per_step": win_bytes, "gbs_if_overlapped": win_bytes / (ms_per_step * 1e-3) / 1e9,
                            "peak_gbs": hbm_peak},

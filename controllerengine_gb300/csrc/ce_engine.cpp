@@ -121,14 +121,17 @@ struct Buffers {
     void* ata = nullptr;
     void* atb = nullptr;
     int* nominal = nullptr;
+    int* fit_counts = nullptr;
+    int* fit_order = nullptr;
     float* traj = nullptr;
     int64_t traj_cap = 0;
     void release() {
-        for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal, (void*)traj})
+        for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
+                        (void*)fit_counts, (void*)fit_order, (void*)traj})
             if (p) cudaFree(p);
         gains = info = lina = traj = nullptr;
         eig = ywin = summ = ata = atb = nullptr;
-        nominal = nullptr;
+        nominal = fit_counts = fit_order = nullptr;
         cap = traj_cap = 0;
     }
 };
@@ -224,6 +227,8 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         CE_CUDA(cudaMalloc(&b.ata, (size_t)cap * 4 * nt * nt * rsz + 16));
         CE_CUDA(cudaMalloc(&b.atb, (size_t)cap * 2 * nt * rsz + 16));
         dev_alloc(b.nominal, (size_t)cap);
+        dev_alloc(b.fit_counts, (size_t)(MAXT + 1));
+        dev_alloc(b.fit_order, (size_t)(MAXT + 1) * cap);
         b.cap = cap;
         b.nt = nt;
         b.pitch = pitch;
@@ -315,11 +320,11 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st);
     });
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_eig, 0));
-    timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, st); });
+    timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, b.fit_counts, b.fit_order, st); });
     timed(3, st, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, st); });
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
     timed(5, st, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, st); });
-    s->launches += 6;
+    s->launches += 7;
 }
 
 std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {

@@ -38,8 +38,10 @@ void launch_lina_eig(const Run& run, const Plant& P, int precision, const float*
                      cudaStream_t st);
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const void* eig, int* nominal, cudaStream_t st);
+// counts (MAXT + 1 ints) and order ((MAXT + 1) * n ints) bucket the candidates
+// by fit class before the fit; both null: candidates in index order.
 void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
-                void* atb, float* info, cudaStream_t st);
+                void* atb, float* info, int* counts, int* order, cudaStream_t st);
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st);
 void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,

@@ -22,25 +22,38 @@
 // multiply-adds.  Failure (no convergence, or a non-finite eigenvalue) yields
 // NaN for the unset eigenvalues; the reference reads unset storage there.
 //
-// GB300 layout: FP64 is a low-rate pipe on this part (1/64 of FP32) and these
-// kernels are FP64-issue bound (ncu: FP64 pipe ~80% busy).  Each matrix lives in
-// shared memory as [element][matrix] and is owned by EIG_Q lanes that split the
-// row / column loops (every element is still updated by exactly one lane in the
-// sequential order, so results do not depend on EIG_Q).  EIG_Q = 1 -- one lane
-// per matrix -- issues the fewest FP64 instructions per matrix: with 4 lanes the
-// scalar parts (Householder vectors, shifts, deflation tests) cost a warp
-// instruction per 8 matrices instead of per 32.
+// Only the eigenvalues are wanted, so the updates of the Schur form are limited
+// to the active window [il, iu]: the reference's full-width updates also
+// transform the rows above il and the columns right of iu, but no later step
+// that determines an eigenvalue reads those entries (every entry the window's
+// steps read lies inside the window, a deflated block is never touched again,
+// and the final extraction reads the diagonal band), so the eigenvalues are
+// bit-identical with less than the reference's work.  The exceptional shifts
+// still update the whole diagonal 0..iu, as in the reference.
+//
+// GB300 layout: FP64 is a low-rate pipe on this part (2 lanes per clock per
+// SM, 1/64 of FP32).  Each matrix lives in shared memory as [element][matrix]
+// and is owned by EQ lanes that split the row / column loops (every element is
+// still updated by exactly one lane in the sequential order, so results do not
+// depend on EQ).  A 16x16 matrix takes 2 KB, so shared memory bounds the
+// matrices resident per SM (about 100) and with them the warps that keep the
+// FP64 pipe fed: EQ = 1 issues the fewest FP64 instructions per matrix but
+// leaves 3 warps per SM; EQ = 2 or 4 gives 6 or 12 warps at the price of
+// computing the scalar steps (Householder vectors, shifts, deflation tests)
+// redundantly in every lane of the group.
 #include <cfloat>
+#include <cstdlib>
 
 #include "ce_device.cuh"
 #include "ce_host.h"
 
 namespace ce {
 
-constexpr int EIG_Q = 1;                     // lanes per matrix (see the note on the layout above)
-constexpr int EIG_BLOCK = 32 * EIG_Q;        // 32 matrices per block
-constexpr int EIG_M = EIG_BLOCK / EIG_Q;     // matrices per block
-constexpr int EIG_STRIDE = EIG_M + 1;        // padded so the 4 lanes of a quad hit different banks
+// One warp per block; EQ lanes per matrix, so 32 / EQ matrices per block,
+// interleaved in shared memory with a stride of 32 / EQ + 1 doubles.
+constexpr int EIG_LANES_DEFAULT = 2;
+template <int EQ> constexpr int eig_mats() { return 32 / EQ; }
+template <int EQ> constexpr int eig_stride() { return 32 / EQ + 1; }
 constexpr double DEPS = 2.220446049250313080847e-16;
 constexpr double DMIN_ = 2.2250738585072013831e-308;
 
@@ -56,9 +69,11 @@ struct SMat {
 // lane 0 of the quad.  Every element is updated by exactly one lane with the
 // same operation sequence as a sequential code, so the results do not depend
 // on the split.
+template <int EQ>
 struct Quad {
-    int q;          // 0..3
-    unsigned mask;  // the quad's lanes
+    static constexpr int N = EQ;  // lanes per matrix
+    int q;                        // 0..EQ-1
+    unsigned mask;                // the group's lanes
     __device__ __forceinline__ void sync() const { __syncwarp(mask); }
     __device__ __forceinline__ bool lead() const { return q == 0; }
 };
@@ -104,17 +119,40 @@ __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, d
 }
 
 // H = I - tau [1;ess][1;ess]^T from the left on rows r0..r0+m-1, columns
-// c0..c1-1 (columns split over the quad).
-template <typename E>
-__device__ __forceinline__ void house_left(const SMat& T, const Quad& Q, int r0, int m, int c0, int c1, E ess_at,
+// c0..c1-1 (columns split over the group).  Per column: tmp = ess.T(r0+1..) +
+// T(r0), T(r0) -= tau tmp, T(r0+k+1) -= tmp (tau ess_k).  Two columns are
+// processed per iteration so that their independent chains overlap; each
+// column's operations and their order are unchanged.
+template <class Qd, typename E>
+__device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, int m, int c0, int c1, E ess_at,
                                            double tau) {
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int j = c0 + Q.q; j < c1; j += EIG_Q) T(r0, j) = __dmul_rn(T(r0, j), f);
+        for (int j = c0 + Q.q; j < c1; j += Qd::N) T(r0, j) = __dmul_rn(T(r0, j), f);
         return;
     }
     if (tau == 0.0) return;
-    for (int j = c0 + Q.q; j < c1; j += EIG_Q) {
+    int j = c0 + Q.q;
+    for (; j + Qd::N < c1; j += 2 * Qd::N) {
+        const int j2 = j + Qd::N;
+        const double e = ess_at(0);
+        double ta = __dmul_rn(e, T(r0 + 1, j)), tb = __dmul_rn(e, T(r0 + 1, j2));
+        for (int k = 1; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+            ta = __dadd_rn(ta, __dmul_rn(ek, T(r0 + 1 + k, j)));
+            tb = __dadd_rn(tb, __dmul_rn(ek, T(r0 + 1 + k, j2)));
+        }
+        ta = __dadd_rn(ta, T(r0, j));
+        tb = __dadd_rn(tb, T(r0, j2));
+        T(r0, j) = __dsub_rn(T(r0, j), __dmul_rn(tau, ta));
+        T(r0, j2) = __dsub_rn(T(r0, j2), __dmul_rn(tau, tb));
+        for (int k = 0; k < m - 1; ++k) {
+            const double te = __dmul_rn(tau, ess_at(k));
+            T(r0 + 1 + k, j) = __dsub_rn(T(r0 + 1 + k, j), __dmul_rn(ta, te));
+            T(r0 + 1 + k, j2) = __dsub_rn(T(r0 + 1 + k, j2), __dmul_rn(tb, te));
+        }
+    }
+    if (j < c1) {
         double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
         tmp = __dadd_rn(tmp, T(r0, j));
@@ -123,23 +161,123 @@ __device__ __forceinline__ void house_left(const SMat& T, const Quad& Q, int r0,
     }
 }
 
-// H from the right on rows r0..r1-1 (split over the quad), columns c0..c0+m-1.
-template <typename E>
-__device__ __forceinline__ void house_right(const SMat& T, const Quad& Q, int r0, int r1, int c0, int m, E ess_at,
+// H from the right on rows r0..r1-1 (split over the group), columns
+// c0..c0+m-1.  Per row: tmp = T(i,c0+1..).ess + T(i,c0), T(i,c0) -= tau tmp,
+// T(i,c0+k+1) -= ess_k (tau tmp).  Two rows per iteration.
+template <class Qd, typename E>
+__device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, int r1, int c0, int m, E ess_at,
                                             double tau) {
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int i = r0 + Q.q; i < r1; i += EIG_Q) T(i, c0) = __dmul_rn(T(i, c0), f);
+        for (int i = r0 + Q.q; i < r1; i += Qd::N) T(i, c0) = __dmul_rn(T(i, c0), f);
         return;
     }
     if (tau == 0.0) return;
-    for (int i = r0 + Q.q; i < r1; i += EIG_Q) {
+    int i = r0 + Q.q;
+    for (; i + Qd::N < r1; i += 2 * Qd::N) {
+        const int i2 = i + Qd::N;
+        const double e = ess_at(0);
+        double ta = __dmul_rn(T(i, c0 + 1), e), tb = __dmul_rn(T(i2, c0 + 1), e);
+        for (int k = 1; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+            ta = __dadd_rn(ta, __dmul_rn(T(i, c0 + 1 + k), ek));
+            tb = __dadd_rn(tb, __dmul_rn(T(i2, c0 + 1 + k), ek));
+        }
+        ta = __dadd_rn(ta, T(i, c0));
+        tb = __dadd_rn(tb, T(i2, c0));
+        T(i, c0) = __dsub_rn(T(i, c0), __dmul_rn(tau, ta));
+        T(i2, c0) = __dsub_rn(T(i2, c0), __dmul_rn(tau, tb));
+        const double tta = __dmul_rn(tau, ta), ttb = __dmul_rn(tau, tb);
+        for (int k = 0; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+            T(i, c0 + 1 + k) = __dsub_rn(T(i, c0 + 1 + k), __dmul_rn(ek, tta));
+            T(i2, c0 + 1 + k) = __dsub_rn(T(i2, c0 + 1 + k), __dmul_rn(ek, ttb));
+        }
+    }
+    if (i < r1) {
         double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
         tmp = __dadd_rn(tmp, T(i, c0));
         T(i, c0) = __dsub_rn(T(i, c0), __dmul_rn(tau, tmp));
         const double tt = __dmul_rn(tau, tmp);
         for (int k = 0; k < m - 1; ++k) T(i, c0 + 1 + k) = __dsub_rn(T(i, c0 + 1 + k), __dmul_rn(ess_at(k), tt));
+    }
+}
+
+// The Francis-step reflectors (m = 3, and m = 2 for the last one) with the
+// essential part in registers; same per-column / per-row operations as above.
+template <class Qd, int M>
+__device__ __forceinline__ void house_left_small(const SMat& T, const Qd& Q, int r0, int c0, int c1, double e0,
+                                                 double e1, double tau) {
+    if (tau == 0.0) return;
+    const double te0 = __dmul_rn(tau, e0), te1 = __dmul_rn(tau, e1);
+    int j = c0 + Q.q;
+    for (; j + Qd::N < c1; j += 2 * Qd::N) {
+        const int j2 = j + Qd::N;
+        const double a0 = T(r0, j), a1 = T(r0 + 1, j), b0 = T(r0, j2), b1 = T(r0 + 1, j2);
+        const double a2 = M == 3 ? T(r0 + 2, j) : 0.0, b2 = M == 3 ? T(r0 + 2, j2) : 0.0;
+        double ta = __dmul_rn(e0, a1), tb = __dmul_rn(e0, b1);
+        if (M == 3) {
+            ta = __dadd_rn(ta, __dmul_rn(e1, a2));
+            tb = __dadd_rn(tb, __dmul_rn(e1, b2));
+        }
+        ta = __dadd_rn(ta, a0);
+        tb = __dadd_rn(tb, b0);
+        T(r0, j) = __dsub_rn(a0, __dmul_rn(tau, ta));
+        T(r0, j2) = __dsub_rn(b0, __dmul_rn(tau, tb));
+        T(r0 + 1, j) = __dsub_rn(a1, __dmul_rn(ta, te0));
+        T(r0 + 1, j2) = __dsub_rn(b1, __dmul_rn(tb, te0));
+        if (M == 3) {
+            T(r0 + 2, j) = __dsub_rn(a2, __dmul_rn(ta, te1));
+            T(r0 + 2, j2) = __dsub_rn(b2, __dmul_rn(tb, te1));
+        }
+    }
+    if (j < c1) {
+        const double a0 = T(r0, j), a1 = T(r0 + 1, j), a2 = M == 3 ? T(r0 + 2, j) : 0.0;
+        double ta = __dmul_rn(e0, a1);
+        if (M == 3) ta = __dadd_rn(ta, __dmul_rn(e1, a2));
+        ta = __dadd_rn(ta, a0);
+        T(r0, j) = __dsub_rn(a0, __dmul_rn(tau, ta));
+        T(r0 + 1, j) = __dsub_rn(a1, __dmul_rn(ta, te0));
+        if (M == 3) T(r0 + 2, j) = __dsub_rn(a2, __dmul_rn(ta, te1));
+    }
+}
+
+template <class Qd, int M>
+__device__ __forceinline__ void house_right_small(const SMat& T, const Qd& Q, int r0, int r1, int c0, double e0,
+                                                  double e1, double tau) {
+    if (tau == 0.0) return;
+    int i = r0 + Q.q;
+    for (; i + Qd::N < r1; i += 2 * Qd::N) {
+        const int i2 = i + Qd::N;
+        const double a0 = T(i, c0), a1 = T(i, c0 + 1), b0 = T(i2, c0), b1 = T(i2, c0 + 1);
+        const double a2 = M == 3 ? T(i, c0 + 2) : 0.0, b2 = M == 3 ? T(i2, c0 + 2) : 0.0;
+        double ta = __dmul_rn(a1, e0), tb = __dmul_rn(b1, e0);
+        if (M == 3) {
+            ta = __dadd_rn(ta, __dmul_rn(a2, e1));
+            tb = __dadd_rn(tb, __dmul_rn(b2, e1));
+        }
+        ta = __dadd_rn(ta, a0);
+        tb = __dadd_rn(tb, b0);
+        T(i, c0) = __dsub_rn(a0, __dmul_rn(tau, ta));
+        T(i2, c0) = __dsub_rn(b0, __dmul_rn(tau, tb));
+        const double tta = __dmul_rn(tau, ta), ttb = __dmul_rn(tau, tb);
+        T(i, c0 + 1) = __dsub_rn(a1, __dmul_rn(e0, tta));
+        T(i2, c0 + 1) = __dsub_rn(b1, __dmul_rn(e0, ttb));
+        if (M == 3) {
+            T(i, c0 + 2) = __dsub_rn(a2, __dmul_rn(e1, tta));
+            T(i2, c0 + 2) = __dsub_rn(b2, __dmul_rn(e1, ttb));
+        }
+    }
+    if (i < r1) {
+        const double a0 = T(i, c0), a1 = T(i, c0 + 1), a2 = M == 3 ? T(i, c0 + 2) : 0.0;
+        double ta = __dmul_rn(a1, e0);
+        if (M == 3) ta = __dadd_rn(ta, __dmul_rn(a2, e1));
+        ta = __dadd_rn(ta, a0);
+        T(i, c0) = __dsub_rn(a0, __dmul_rn(tau, ta));
+        const double tta = __dmul_rn(tau, ta);
+        T(i, c0 + 1) = __dsub_rn(a1, __dmul_rn(e0, tta));
+        if (M == 3) T(i, c0 + 2) = __dsub_rn(a2, __dmul_rn(e1, tta));
     }
 }
 
@@ -176,18 +314,18 @@ __device__ __forceinline__ void rot_pair(double& x, double& y, double c, double 
 // Eigenvalues of the n x n matrix in T (overwritten), computed by a quad.
 // emit(i, re, im) is called by the quad's lane 0 for i = 0..n-1 in Schur
 // order; returns true on success (the same value in every lane).
-template <typename Emit>
-__device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
+template <class Qd, typename Emit>
+__device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
     const int nn = n * n;
     double scale = 0.0;
     for (int e = 0; e < nn; ++e) scale = fmax(scale, fabs(T(e / n, e % n)));
     Q.sync();
     bool ok = true;
     if (scale < DMIN_) {
-        for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = 0.0;
+        for (int e = Q.q; e < nn; e += Qd::N) T(e / n, e % n) = 0.0;
         Q.sync();
     } else {
-        for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = __ddiv_rn(T(e / n, e % n), scale);
+        for (int e = Q.q; e < nn; e += Qd::N) T(e / n, e % n) = __ddiv_rn(T(e / n, e % n), scale);
         Q.sync();
         // Hessenberg reduction
         for (int i = 0; i < n - 1; ++i) {
@@ -195,7 +333,7 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
             double tau, beta, d;
             house_coeffs(T, i + 1, rs, i, tau, beta, d);
             Q.sync();
-            for (int k = i + 2 + Q.q; k < n; k += EIG_Q) T(k, i) = d == 0.0 ? 0.0 : __ddiv_rn(T(k, i), d);
+            for (int k = i + 2 + Q.q; k < n; k += Qd::N) T(k, i) = d == 0.0 ? 0.0 : __ddiv_rn(T(k, i), d);
             if (Q.lead()) T(i + 1, i) = beta;
             Q.sync();
             auto ess = [&](int k) { return T(i + 2 + k, i); };
@@ -204,7 +342,7 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
             house_right(T, Q, 0, n, i + 1, rs, ess, tau);
             Q.sync();
         }
-        for (int e = Q.q; e < nn; e += EIG_Q)
+        for (int e = Q.q; e < nn; e += Qd::N)
             if (e % n + 1 < e / n) T(e / n, e % n) = 0.0;
         Q.sync();
         // Francis double-shift QR
@@ -250,14 +388,14 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
                         double c, s;
                         make_givens(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), sub, c, s);
                         if (!(c == 1.0 && s == 0.0)) {
-                            for (int j = iu - 1 + Q.q; j < n; j += EIG_Q) {
+                            for (int j = iu - 1 + Q.q; j <= iu; j += Qd::N) {
                                 double x = T(iu - 1, j), y = T(iu, j);
                                 rot_pair(x, y, c, s);
                                 T(iu - 1, j) = x;
                                 T(iu, j) = y;
                             }
                             Q.sync();
-                            for (int i = Q.q; i <= iu; i += EIG_Q) {
+                            for (int i = iu - 1 + Q.q; i <= iu; i += Qd::N) {
                                 double x = T(i, iu - 1), y = T(i, iu);
                                 rot_pair(x, y, c, s);
                                 T(i, iu - 1) = x;
@@ -276,7 +414,7 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
                     Q.sync();
                     if (iter == 10) {
                         exshift = __dadd_rn(exshift, sh0);
-                        for (int i = Q.q; i <= iu; i += EIG_Q) T(i, i) = __dsub_rn(T(i, i), sh0);
+                        for (int i = Q.q; i <= iu; i += Qd::N) T(i, i) = __dsub_rn(T(i, i), sh0);
                         Q.sync();
                         const double s = __dadd_rn(fabs(T(iu, iu - 1)), fabs(T(iu - 1, iu - 2)));
                         sh0 = __dmul_rn(0.75, s);
@@ -292,7 +430,7 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
                             s = __dadd_rn(s, __ddiv_rn(__dsub_rn(sh1, sh0), 2.0));
                             s = __dsub_rn(sh0, __ddiv_rn(sh2, s));
                             exshift = __dadd_rn(exshift, s);
-                            for (int i = Q.q; i <= iu; i += EIG_Q) T(i, i) = __dsub_rn(T(i, i), s);
+                            for (int i = Q.q; i <= iu; i += Qd::N) T(i, i) = __dsub_rn(T(i, i), s);
                             Q.sync();
                             sh0 = sh1 = sh2 = 0.964;
                         }
@@ -333,10 +471,9 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
                                 if (first && k > il) T(k, k - 1) = -T(k, k - 1);
                                 else if (!first) T(k, k - 1) = beta;
                             }
-                            auto e = [&](int qq) { return ess[qq]; };
-                            house_left(T, Q, k, 3, k, n, e, tau);
+                            house_left_small<Qd, 3>(T, Q, k, k, iu + 1, ess[0], ess[1], tau);
                             Q.sync();
-                            house_right(T, Q, 0, min(iu, k + 3) + 1, k, 3, e, tau);
+                            house_right_small<Qd, 3>(T, Q, il, min(iu, k + 3) + 1, k, ess[0], ess[1], tau);
                             Q.sync();
                         }
                     }
@@ -347,14 +484,13 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
                         Q.sync();
                         if (beta != 0.0) {
                             if (Q.lead()) T(iu - 1, iu - 2) = beta;
-                            auto e = [&](int qq) { return ess[qq]; };
-                            house_left(T, Q, iu - 1, 2, iu - 1, n, e, tau);
+                            house_left_small<Qd, 2>(T, Q, iu - 1, iu - 1, iu + 1, ess[0], 0.0, tau);
                             Q.sync();
-                            house_right(T, Q, 0, iu + 1, iu - 1, 2, e, tau);
+                            house_right_small<Qd, 2>(T, Q, il, iu + 1, iu - 1, ess[0], 0.0, tau);
                             Q.sync();
                         }
                     }
-                    for (int i = im + 2 + Q.q; i <= iu; i += EIG_Q) {
+                    for (int i = im + 2 + Q.q; i <= iu; i += Qd::N) {
                         T(i, i - 2) = 0.0;
                         if (i > im + 2) T(i, i - 3) = 0.0;
                     }
@@ -364,7 +500,14 @@ __device__ bool eig_real(const SMat& T, const Quad& Q, int n, Emit emit) {
         }
         ok = total <= max_iter;
         if (ok) {
-            for (int e = Q.q; e < nn; e += EIG_Q) T(e / n, e % n) = __dmul_rn(T(e / n, e % n), scale);
+            // the extraction below reads the diagonal band only
+            for (int i = Q.q; i < n; i += Qd::N) {
+                T(i, i) = __dmul_rn(T(i, i), scale);
+                if (i + 1 < n) {
+                    T(i + 1, i) = __dmul_rn(T(i + 1, i), scale);
+                    T(i, i + 1) = __dmul_rn(T(i, i + 1), scale);
+                }
+            }
             Q.sync();
         }
     }
@@ -422,19 +565,20 @@ __device__ __forceinline__ float lina_entry(const Plant& P, const float* K, cons
     return P.d_a[(i - ns) * MAXD + (j - ns)];
 }
 
-__device__ __forceinline__ Quad make_quad() {
+template <int EQ>
+__device__ __forceinline__ Quad<EQ> make_quad() {
     const int lane = threadIdx.x & 31;
-    const int q = lane % EIG_Q;
-    return Quad{q, ((EIG_Q == 32) ? 0xFFFFFFFFu : ((1u << EIG_Q) - 1u)) << (lane - q)};
+    const int q = lane % EQ;
+    return Quad<EQ>{q, ((EQ == 32) ? 0xFFFFFFFFu : ((1u << EQ) - 1u)) << (lane - q)};
 }
-
-__global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __grid_constant__ Plant P,
+template <int EQ>
+__global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EIG_Q;
-    const Quad Q = make_quad();
-    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
+    const int m = threadIdx.x / EQ;
+    const auto Q = make_quad<EQ>();
+    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
     if (c >= run.n) return;  // the whole quad leaves together
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
@@ -444,9 +588,9 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __g
         K[i] = i < ns ? row[i] : 0.0f;
         L[i] = i < ns ? row[ns + i] : 0.0f;
     }
-    SMat T{smem + m, nt, EIG_STRIDE};
+    SMat T{smem + m, nt, eig_stride<EQ>()};
     float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int e = Q.q; e < nt * nt; e += EIG_Q) {
+    for (int e = Q.q; e < nt * nt; e += EQ) {
         const int i = e / nt, j = e % nt;
         const float v = lina_entry(P, K, L, ns, i, j);
         lrow[e] = v;
@@ -469,19 +613,20 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig(const Run run, const __g
 }
 
 // FP64-form LIN_A: the same blocks formed in double from the float inputs.
-__global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
+template <int EQ>
+__global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
                                                           const float* __restrict__ gains, float* __restrict__ lina,
                                                           double* __restrict__ eig64) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EIG_Q;
-    const Quad Q = make_quad();
-    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
+    const int m = threadIdx.x / EQ;
+    const auto Q = make_quad<EQ>();
+    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
     if (c >= run.n) return;
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
-    SMat T{smem + m, nt, EIG_STRIDE};
+    SMat T{smem + m, nt, eig_stride<EQ>()};
     float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int e = Q.q; e < nt * nt; e += EIG_Q) {
+    for (int e = Q.q; e < nt * nt; e += EQ) {
         const int i = e / nt, j = e % nt;
         double v;
         if (i < ns && j < ns) {
@@ -509,14 +654,15 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_lina_eig64(const Run run, const _
 // Acl_nom = [OPEN_A - (D L) K^T, -L C^T; B K^T, A] with OPEN_A = LIN_A[:ns,:ns]
 // and (A, B, C, D) the margin plant.  nominal[c] = 1 if stable, 0 if not, -1
 // if the candidate is modal-unstable (the sweep never reads it then).
-__global__ void __launch_bounds__(EIG_BLOCK) k_nominal(const Run run, const __grid_constant__ Plant P,
+template <int EQ>
+__global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
                                                        const void* __restrict__ eig, int* __restrict__ nominal,
                                                        int fp64_form) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EIG_Q;
-    const Quad Q = make_quad();
-    const int64_t c = (int64_t)blockIdx.x * EIG_M + m;
+    const int m = threadIdx.x / EQ;
+    const auto Q = make_quad<EQ>();
+    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
     if (c >= run.n) return;
     // Candidates the modal stage will flag unstable (max |lambda(LIN_A)| > 1, the
     // same float test) never reach the sweep; everything else is solved here,
@@ -542,8 +688,8 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_nominal(const Run run, const __gr
     const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
     const float* row = gains + c * run.cuda_w;
     const float* la = lina + c * (int64_t)(nt * nt);
-    SMat T{smem + m, n2, EIG_STRIDE};
-    for (int e = Q.q; e < ns * ns; e += EIG_Q) {
+    SMat T{smem + m, n2, eig_stride<EQ>()};
+    for (int e = Q.q; e < ns * ns; e += EQ) {
         const int i = e / ns, j = e % ns;
         const float Li = row[ns + i];
         const float Kj = row[j];
@@ -570,26 +716,61 @@ static void set_smem(const void* fn, size_t bytes) {
     CE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
+// Lanes per matrix of the FP64 eigensolves.  One lane per matrix issues the
+// fewest FP64 instructions; more lanes per matrix put more warps on each SM
+// (the matrices of a warp share its shared-memory footprint), at the price of
+// computing the scalar steps redundantly.  Two lanes measured fastest on the
+// eight-state workload (LIN_A eigensolve of 65,536 16x16 matrices: 21.9 ms with
+// one lane, 18.4 ms with two).  CE_EIG_LANES=1|2|4 overrides.
+static int eig_lanes() {
+    static const int v = [] {
+        const char* e = std::getenv("CE_EIG_LANES");
+        const int k = e ? std::atoi(e) : 0;
+        return (k == 1 || k == 2 || k == 4) ? k : EIG_LANES_DEFAULT;
+    }();
+    return v;
+}
+
+template <int EQ>
+static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+                       cudaStream_t st) {
+    const int grid = (int)((run.n + eig_mats<EQ>() - 1) / eig_mats<EQ>());
+    const size_t smem = (size_t)run.nt * run.nt * eig_stride<EQ>() * sizeof(double);
+    if (precision == CE_PRECISION_FP64) {
+        set_smem((const void*)k_lina_eig64<EQ>, smem);
+        k_lina_eig64<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig);
+    } else {
+        set_smem((const void*)k_lina_eig<EQ>, smem);
+        k_lina_eig<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nullptr);
+    }
+}
+
+template <int EQ>
+static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+                      const void* eig, int* nominal, cudaStream_t st) {
+    const int grid = (int)((run.n + eig_mats<EQ>() - 1) / eig_mats<EQ>());
+    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
+    set_smem((const void*)k_nominal<EQ>, smem);
+    k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, eig, nominal, precision == CE_PRECISION_FP64);
+}
+
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                      cudaStream_t st) {
-    const int grid = (int)((run.n + EIG_M - 1) / EIG_M);
-    const size_t smem = (size_t)run.nt * run.nt * EIG_STRIDE * sizeof(double);
-    if (precision == CE_PRECISION_FP64) {
-        set_smem((const void*)k_lina_eig64, smem);
-        k_lina_eig64<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, (double*)eig);
-    } else {
-        set_smem((const void*)k_lina_eig, smem);
-        k_lina_eig<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, (float*)eig, nullptr);
+    switch (eig_lanes()) {
+        case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, st); break;
+        case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, st); break;
+        default: lina_eig_q<4>(run, P, precision, gains, lina, eig, st); break;
     }
     CE_CUDA(cudaGetLastError());
 }
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const void* eig, int* nominal, cudaStream_t st) {
-    const int grid = (int)((run.n + EIG_M - 1) / EIG_M);
-    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * EIG_STRIDE * sizeof(double);
-    set_smem((const void*)k_nominal, smem);
-    k_nominal<<<grid, EIG_BLOCK, smem, st>>>(run, P, gains, lina, eig, nominal, precision == CE_PRECISION_FP64);
+    switch (eig_lanes()) {
+        case 1: nominal_q<1>(run, P, precision, gains, lina, eig, nominal, st); break;
+        case 2: nominal_q<2>(run, P, precision, gains, lina, eig, nominal, st); break;
+        default: nominal_q<4>(run, P, precision, gains, lina, eig, nominal, st); break;
+    }
     CE_CUDA(cudaGetLastError());
 }
 

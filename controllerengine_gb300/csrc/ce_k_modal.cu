@@ -9,13 +9,14 @@
 // reference kernel's.
 //
 // GB300 layout: the reference keeps the 32x32 AtA in a per-thread local array
-// (4.6 KB stack, ref: src/modalsetup.cu:67).  Here 16 lanes own one candidate:
-// lane l computes the basis pair of mode l (one expf + one sin/cos pair per
-// mode per step, no duplication), the 32 basis values are exchanged through
-// shared memory, and lane l accumulates rows l and 31-l of the lower triangle
-// (33 entries per lane, balanced) in registers.  The fit window is read as 64
-// contiguous bytes per 16 steps and broadcast by shuffle.
-//
+// (4.6 KB stack, ref: src/modalsetup.cu:67).  Here 16 lanes own one candidate
+// and work through the window in chunks of 16 steps: first the chunk's
+// 16 x unique basis pairs (one expf + one sin/cos pair each) are spread evenly
+// over the lanes and written to shared memory, then every lane accumulates its
+// 4x4 tiles of the lower triangle over the 16 steps with two 16-byte shared
+// loads and 16 fused multiply-adds per tile and step.  The fit window is read
+// as 64 contiguous bytes per chunk.
+
 // k_modal restates modalsolve (ref: src/modalsolve.cu:1-108): diagonal
 // scaling, LDLT with symmetric pivoting of the 2nt x 2nt system, per-mode
 // energies, energy-weighted wn/zeta of the oscillatory modes and the behaviour
@@ -111,22 +112,66 @@ __device__ __forceinline__ void mode_of(const Modes<R>& m, int nt, int e, R& sig
 
 constexpr int FIT_BLOCK = 128;            // 8 candidates per block
 constexpr int FIT_CPB = FIT_BLOCK / 16;
+constexpr int FIT_CHUNK = 16;             // window steps per chunk (= lanes per candidate)
+constexpr int FIT_PITCH = 36;             // basis row: nc values, y at index nc, zeros up to 4*ceil((nc+1)/4)
+constexpr int FIT_ROUNDS = 2;             // 4x4 tiles per lane and pass (32 tiles: nc <= 27 in one pass)
+constexpr int FIT_CLASSES = MAXT + 1;     // 0: modal-unstable, u = 1..MAXT: stable with u unique modes
 
-// 16-byte vector of basis values (4 floats or 2 doubles)
-template <typename R> struct vec4_t;
-template <> struct vec4_t<float> { using type = float4; static constexpr int N = 4; };
-template <> struct vec4_t<double> { using type = double2; static constexpr int N = 2; };
+// four consecutive basis values (16-byte aligned) from shared memory
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+// Fit classes: the work of a candidate's fit is set by its unique-mode count,
+// and a modal-unstable candidate only writes its penalty.  Candidates are
+// bucketed by class (counts[cls], order[cls * n + slot]) so that the two
+// candidates sharing a warp in k_fit run the same loop trip counts.  The slot
+// order inside a class is whatever the atomics give; every candidate's result
+// is computed by one half-warp alone, so it does not depend on that order.
+template <typename R>
+__global__ void __launch_bounds__(128) k_fit_classify(const Run run, const R* __restrict__ eig, int* __restrict__ counts,
+                                                      int* __restrict__ order) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (c >= run.n) return;
+    Modes<R> m;
+    load_modes<R>(eig + c * (int64_t)(2 * run.nt), run.nt, R(run.ts), m);
+    const int cls = m.max_mag > R(1) ? 0 : m.unique;
+    const int slot = atomicAdd(&counts[cls], 1);
+    order[(int64_t)cls * run.n + slot] = (int)c;
+}
+
+// Candidate of half-warp h: classes in order of decreasing work (MAXT unique
+// modes first, the unstable class last), identity order without a class table.
+__device__ __forceinline__ int64_t fit_candidate(const Run& run, const int* counts, const int* order, int64_t h) {
+    if (!counts) return h;
+    int64_t start = 0;
+    for (int cls = MAXT; cls >= 0; --cls) {
+        const int k = counts[cls];
+        if (h < start + k) return order[(int64_t)cls * run.n + (h - start)];
+        start += k;
+    }
+    return run.n;
+}
 
 template <typename R, typename Sum>
 __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __restrict__ eig, const R* __restrict__ ywin,
                                                    const Sum* __restrict__ summ, R* __restrict__ ata,
-                                                   R* __restrict__ atb, float* __restrict__ info) {
-    __shared__ __align__(16) R csm[FIT_CPB][2][MAXNC];
+                                                   R* __restrict__ atb, float* __restrict__ info,
+                                                   const int* __restrict__ counts, const int* __restrict__ order) {
+    __shared__ __align__(16) R cb[FIT_CPB][FIT_CHUNK][FIT_PITCH];
+    __shared__ __align__(16) R mp[FIT_CPB][MAXT][4];
     const int lane = threadIdx.x & 15;
     const int g = threadIdx.x >> 4;
     const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
-    const int64_t c = (int64_t)blockIdx.x * FIT_CPB + g;
-    if (c >= run.n) return;  // the whole half-warp leaves together
+    const int64_t h = (int64_t)blockIdx.x * FIT_CPB + g;
+    if (h >= run.n) return;  // the whole half-warp leaves together
+    const int64_t c = fit_candidate(run, counts, order, h);
+    if (c >= run.n) return;
     const int nt = run.nt;
     const R ts = R(run.ts);
 
@@ -135,23 +180,28 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
     float* out = info + c * (int64_t)run.info_w;
     const int n2 = 2 * nt;
     R* arow = ata + c * (int64_t)(n2 * n2);
+    R* brow = atb + c * (int64_t)n2;
+    // AtA is 2nt x 2nt with row stride 2nt; entries outside j <= i < nc stay
+    // zero, as after the reference's memset (ref: src/main.cu:520-521)
+    for (int e = lane; e < n2 * n2; e += 16) arow[e] = R(0);
+    for (int e = lane; e < n2; e += 16) brow[e] = R(0);
     if (m.max_mag > R(1)) {
         if (lane == 0) {
             const float v = (float)radd(R(run.unstable_err), rdiv(rlog(m.max_mag), ts));
             out[run.info_scoring] = v;
             out[run.info_scoring + 1] = v;
         }
-        // AtA/Atb stay zero, as after the reference's memset (ref: src/main.cu:520-521)
-        for (int r = lane; r < n2; r += 16) {
-            for (int j = 0; j < n2; ++j) arow[r * n2 + j] = R(0);
-            atb[c * (int64_t)n2 + r] = R(0);
-        }
         return;
     }
     const int unique = m.unique, nc = 2 * unique;
-    R sig, om, shift = R(0);
-    mode_of<R>(m, nt, lane, sig, om);
-    shift = fmax(rmul(sig, R(run.fit_t0)), rmul(sig, R(run.fit_t1)));
+    {
+        R sig, om;
+        mode_of<R>(m, nt, lane, sig, om);
+        mp[g][lane][0] = sig;
+        mp[g][lane][1] = om;
+        mp[g][lane][2] = fmax(rmul(sig, R(run.fit_t0)), rmul(sig, R(run.fit_t1)));
+        mp[g][lane][3] = R(0);
+    }
 
     // steady-state value and overshoot (ref: src/modalsetup.cu:52-62); the
     // running max of y*yss equals max(y)*yss (yss >= 0) or min(y)*yss (yss < 0)
@@ -169,92 +219,104 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
         out[run.info_freqresp + 3] = (float)yss;
     }
 
-    // normal equations
-#pragma unroll
-    for (int b = 0; b < 2; ++b) {
-        csm[g][b][lane] = R(0);
-        csm[g][b][lane + 16] = R(0);
-    }
-    __syncwarp(hmask);
-    R A1[16], A2[32], B1 = R(0), B2 = R(0);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) A1[j] = R(0);
-#pragma unroll
-    for (int j = 0; j < 32; ++j) A2[j] = R(0);
-    const int r1 = lane, r2 = 31 - lane;
+    // Normal equations (ref: src/modalsetup.cu:64-94).  The basis vector of a
+    // step is extended by the sample y at index nc, so AtA (j <= i < nc) and
+    // Atb (row nc) are the lower triangle of one rank-1 accumulation of size
+    // N = nc + 1, tiled into 4x4 blocks spread over the 16 lanes.  Each entry
+    // is still one fused multiply-add per step in the order of t.
+    for (int e = lane; e < FIT_CHUNK * FIT_PITCH; e += 16) (&cb[g][0][0])[e] = R(0);
+    const int N = nc + 1, NB = (N + 3) >> 2, nblk = NB * (NB + 1) / 2;
+    // basis work item k = (step k / unique, mode k % unique); lane l takes k = l, l + 16, ...
+    const int s0 = lane / unique, m0 = lane - s0 * unique;
+    const int ds = FIT_CHUNK / unique, dm = FIT_CHUNK - ds * unique;
     const R* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
     const int steps = run.fit_steps;
-    R ybuf = R(0);
-    for (int w = 0; w < steps; ++w) {
-        if ((w & 15) == 0) {
-            const int idx = w + lane;
-            ybuf = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
-        }
-        const R yw = __shfl_sync(hmask, ybuf, w & 15, 16);
-        const int b = w & 1;
-        const R tval = rmul(R(run.fit_start_id + w), ts);
-        if (lane < unique) {
-            const R decay = rexp(rfma(sig, tval, -shift));
-            const R arg = rmul(om, tval);
-            R sn, cs;
-            rsincos(arg, sn, cs);  // one argument reduction for both
-            csm[g][b][2 * lane] = rmul(decay, cs);
-            csm[g][b][2 * lane + 1] = rmul(decay, sn);
-        }
-        __syncwarp(hmask);
-        const R y = rsub(yw, yss);
-        const R c1 = csm[g][b][r1];
-        const R c2 = csm[g][b][r2];
-        // basis values as 16-byte broadcast loads (every lane of the half-warp reads the same address)
-        using V = typename vec4_t<R>::type;
-        constexpr int VN = vec4_t<R>::N;
-        const V* cv = reinterpret_cast<const V*>(&csm[g][b][0]);
-        R cj[32];
+    __syncwarp(hmask);
+    // one pass over the window per 32 tiles (a second pass only when nc > 27)
+    for (int t0 = 0; t0 < nblk; t0 += 16 * FIT_ROUNDS) {
+        int bi[FIT_ROUNDS], bj[FIT_ROUNDS];
 #pragma unroll
-        for (int q = 0; q < 16 / VN; ++q) {
-            const V v = cv[q];
-            if constexpr (VN == 4) {
-                cj[4 * q] = v.x; cj[4 * q + 1] = v.y; cj[4 * q + 2] = v.z; cj[4 * q + 3] = v.w;
-            } else {
-                cj[2 * q] = v.x; cj[2 * q + 1] = v.y;
+        for (int r = 0; r < FIT_ROUNDS; ++r) {
+            const int blk = t0 + lane + 16 * r;
+            int i = 0;
+            while ((i + 1) * (i + 2) / 2 <= blk) ++i;
+            bi[r] = 4 * i;
+            bj[r] = 4 * (blk - i * (i + 1) / 2);
+        }
+        const bool act0 = t0 + lane < nblk, act1 = t0 + lane + 16 < nblk;
+        const bool any1 = t0 + 16 < nblk;  // the same in every lane of the half-warp
+        R acc[FIT_ROUNDS][16];
+#pragma unroll
+        for (int r = 0; r < FIT_ROUNDS; ++r)
+#pragma unroll
+            for (int k = 0; k < 16; ++k) acc[r][k] = R(0);
+        for (int w0 = 0; w0 < steps; w0 += FIT_CHUNK) {
+            {
+                const int idx = w0 + lane;
+                const R yw = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
+                cb[g][lane][nc] = rsub(yw, yss);
             }
-        }
-        // all 16 / 32 slots accumulate: slots j > row hold values that are never
-        // stored (only j <= row is written out), and skipping the predicates keeps
-        // the integer pipe free
-#pragma unroll
-        for (int j = 0; j < 16; ++j) A1[j] = rfma(c1, cj[j], A1[j]);
-        if (nc > 16) {  // rows 16..31 exist only when nc > 16
-#pragma unroll
-            for (int q = 16 / VN; q < 32 / VN; ++q) {
-                const V v = cv[q];
-                if constexpr (VN == 4) {
-                    cj[4 * q] = v.x; cj[4 * q + 1] = v.y; cj[4 * q + 2] = v.z; cj[4 * q + 3] = v.w;
-                } else {
-                    cj[2 * q] = v.x; cj[2 * q + 1] = v.y;
+            int s = s0, md = m0;
+            for (int it = 0; it < unique; ++it) {
+                const int w = w0 + s;
+                if (w < steps) {
+                    const R sig = mp[g][md][0], om = mp[g][md][1], shift = mp[g][md][2];
+                    const R tval = rmul(R(run.fit_start_id + w), ts);
+                    const R decay = rexp(rfma(sig, tval, -shift));
+                    R sn, cs;
+                    rsincos(rmul(om, tval), sn, cs);  // one argument reduction for both
+                    cb[g][s][2 * md] = rmul(decay, cs);
+                    cb[g][s][2 * md + 1] = rmul(decay, sn);
+                }
+                s += ds;
+                md += dm;
+                if (md >= unique) {
+                    md -= unique;
+                    ++s;
                 }
             }
+            __syncwarp(hmask);
+            const int cnt = min(FIT_CHUNK, steps - w0);
+            for (int st = 0; st < cnt; ++st) {
+                const R* row = &cb[g][st][0];
+                if (act0) {
+                    R a[4], b[4];
+                    ld4(row + bi[0], a);
+                    ld4(row + bj[0], b);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) A2[j] = rfma(c2, cj[j], A2[j]);
-            B2 = rfma(c2, y, B2);
+                    for (int p = 0; p < 4; ++p)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[0][4 * p + q] = rfma(a[p], b[q], acc[0][4 * p + q]);
+                }
+                if (any1 && act1) {
+                    R a[4], b[4];
+                    ld4(row + bi[1], a);
+                    ld4(row + bj[1], b);
+#pragma unroll
+                    for (int p = 0; p < 4; ++p)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[1][4 * p + q] = rfma(a[p], b[q], acc[1][4 * p + q]);
+                }
+            }
+            __syncwarp(hmask);
         }
-        B1 = rfma(c1, y, B1);
-    }
-
-    // AtA is 2nt x 2nt, row stride 2nt; only j <= i < nc is ever accumulated
-    // (ref: src/modalsetup.cu:86-90), the rest is zero.
-    if (r1 < n2) {
+        // owners write their entries over the zeros
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if (j < n2) arow[r1 * n2 + j] = (r1 < nc && j <= r1 && j < 16) ? A1[j & 15] : R(0);
-        atb[c * (int64_t)n2 + r1] = r1 < nc ? B1 : R(0);
-    }
-    if (r2 < n2) {
+        for (int r = 0; r < FIT_ROUNDS; ++r) {
+            if (t0 + lane + 16 * r < nblk) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if (j < n2) arow[r2 * n2 + j] = (r2 < nc && j <= r2) ? A2[j] : R(0);
-        atb[c * (int64_t)n2 + r2] = r2 < nc ? B2 : R(0);
+                for (int p = 0; p < 4; ++p)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int i = bi[r] + p, j = bj[r] + q;
+                        if (j < nc && j <= i) {
+                            if (i < nc) arow[i * n2 + j] = acc[r][4 * p + q];
+                            else if (i == nc) brow[j] = acc[r][4 * p + q];
+                        }
+                    }
+            }
+        }
     }
 }
 
@@ -478,14 +540,25 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const
 }
 
 void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
-                void* atb, float* info, cudaStream_t st) {
+                void* atb, float* info, int* counts, int* order, cudaStream_t st) {
     const int grid = (int)((run.n + FIT_CPB - 1) / FIT_CPB);
+    if (counts) {
+        CE_CUDA(cudaMemsetAsync(counts, 0, FIT_CLASSES * sizeof(int), st));
+        const int cgrid = (int)((run.n + 127) / 128);
+        if (precision == CE_PRECISION_FP64)
+            k_fit_classify<double><<<cgrid, 128, 0, st>>>(run, (const double*)eig, counts, order);
+        else
+            k_fit_classify<float><<<cgrid, 128, 0, st>>>(run, (const float*)eig, counts, order);
+        CE_CUDA(cudaGetLastError());
+    }
     if (precision == CE_PRECISION_FP64)
         k_fit<double, double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin,
-                                                         (const double*)summ, (double*)ata, (double*)atb, info);
+                                                         (const double*)summ, (double*)ata, (double*)atb, info,
+                                                         counts, order);
     else
         k_fit<float, SimSummary><<<grid, FIT_BLOCK, 0, st>>>(run, (const float*)eig, (const float*)ywin,
-                                                            (const SimSummary*)summ, (float*)ata, (float*)atb, info);
+                                                            (const SimSummary*)summ, (float*)ata, (float*)atb, info,
+                                                            counts, order);
     CE_CUDA(cudaGetLastError());
 }
 

@@ -81,7 +81,7 @@ extern "C" CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index
         cudaStream_t st = (cudaStream_t)stream;
         r.store_traj = 0;
         launch_sim(r, *session_plant(s, plant_index), CE_PRECISION_MIXED, d_cuda_mx, ywin, summ, nullptr, st);
-        launch_fit(r, CE_PRECISION_MIXED, d_eigen, ywin, summ, d_ata, d_atb, d_info, st);
+        launch_fit(r, CE_PRECISION_MIXED, d_eigen, ywin, summ, d_ata, d_atb, d_info, nullptr, nullptr, st);
         session_count_launches(s, 2);
         return 0;
     } catch (const std::exception& e) {
