@@ -156,6 +156,14 @@ __device__ __forceinline__ bool cfinite(cplx<R> a) {
 // call sites of the reference (ref: src/allmargin.cu:24-29, 37, 103-104).
 // A is read as A[(i*NS + j) * astride].  An exactly zero pivot is left in
 // place, so the solve then produces non-finite values.
+//
+// The forward substitution is carried along with the elimination: at step k
+// the right-hand side takes the row interchange and then x[i] -= x[k] l_ik for
+// i > k.  Every element of x receives the same operations in the same order
+// as in "x = P b, then column-oriented forward substitution" (interchanges do
+// not change values, and x[k] is final when it is used), so the results are
+// identical; the multipliers are dead after their step, which keeps the
+// factorisation in registers.
 template <typename R, int NS>
 __device__ __forceinline__ void lu_solve_shifted(cplx<R> z, const R* A, int astride, const R* b, cplx<R>* x) {
     cplx<R> M[NS][NS];
@@ -168,7 +176,8 @@ __device__ __forceinline__ void lu_solve_shifted(cplx<R> z, const R* A, int astr
                                         : cplx<R>{rsub(rmul(z.re, R(0)), rmul(z.im, R(0))), radd(rmul(z.re, R(0)), rmul(z.im, R(0)))};
             M[i][j] = csub(zi, cplx<R>{A[(i * NS + j) * astride], R(0)});
         }
-    int perm[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) x[i] = cplx<R>{b[i], R(0)};
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
         // pivot: largest |M(i,k)|, i >= k, first maximum wins
@@ -179,47 +188,35 @@ __device__ __forceinline__ void lu_solve_shifted(cplx<R> z, const R* A, int astr
             const R s = cnorm2(M[i][k]);
             if (s > best) { best = s; p = i; }
         }
-        perm[k] = p;
-        if (best != R(0)) {
-            if (p != k) {
+        // row interchange (the multiplier columns j < k are not used again),
+        // as selects over the candidate rows so that M stays in registers
 #pragma unroll
-                for (int i = k + 1; i < NS; ++i)
-                    if (i == p) {
+        for (int j = k; j <= NS; ++j) {
+            cplx<R>& top = j < NS ? M[k][j] : x[k];
+            cplx<R> piv = top;
 #pragma unroll
-                        for (int j = 0; j < NS; ++j) {
-                            const cplx<R> t = M[k][j];
-                            M[k][j] = M[i][j];
-                            M[i][j] = t;
-                        }
-                    }
+            for (int i = k + 1; i < NS; ++i) {
+                cplx<R>& e = j < NS ? M[i][j] : x[i];
+                const bool hit = i == p;
+                const cplx<R> old = e;
+                e.re = hit ? top.re : e.re;
+                e.im = hit ? top.im : e.im;
+                piv.re = hit ? old.re : piv.re;
+                piv.im = hit ? old.im : piv.im;
             }
+            top = piv;
+        }
+        if (best != R(0)) {
 #pragma unroll
             for (int i = k + 1; i < NS; ++i) M[i][k] = cdiv(M[i][k], M[k][k]);
         }
 #pragma unroll
-        for (int i = k + 1; i < NS; ++i)
+        for (int i = k + 1; i < NS; ++i) {
 #pragma unroll
             for (int j = k + 1; j < NS; ++j) M[i][j] = csub(M[i][j], cmul(M[i][k], M[k][j]));
+            x[i] = csub(x[i], cmul(x[k], M[i][k]));
+        }
     }
-    // x = P b
-#pragma unroll
-    for (int i = 0; i < NS; ++i) x[i] = cplx<R>{b[i], R(0)};
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-        const int p = perm[k];
-#pragma unroll
-        for (int i = k + 1; i < NS; ++i)
-            if (i == p) {
-                const cplx<R> t = x[k];
-                x[k] = x[i];
-                x[i] = t;
-            }
-    }
-    // unit lower, column oriented
-#pragma unroll
-    for (int i = 0; i < NS; ++i)
-#pragma unroll
-        for (int s = i + 1; s < NS; ++s) x[s] = csub(x[s], cmul(x[i], M[s][i]));
     // upper, column oriented
 #pragma unroll
     for (int i = NS - 1; i >= 0; --i) {
