@@ -123,15 +123,17 @@ struct Buffers {
     int* nominal = nullptr;
     int* fit_counts = nullptr;
     int* fit_order = nullptr;
+    int* nominal_list = nullptr;
+    int* nominal_count = nullptr;
     float* traj = nullptr;
     int64_t traj_cap = 0;
     void release() {
         for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
-                        (void*)fit_counts, (void*)fit_order, (void*)traj})
+                        (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count, (void*)traj})
             if (p) cudaFree(p);
         gains = info = lina = traj = nullptr;
         eig = ywin = summ = ata = atb = nullptr;
-        nominal = fit_counts = fit_order = nullptr;
+        nominal = fit_counts = fit_order = nominal_list = nominal_count = nullptr;
         cap = traj_cap = 0;
     }
 };
@@ -156,8 +158,10 @@ struct ce_session {
     float* d_fgrid32 = nullptr;
     double* d_fgrid64 = nullptr;
     ce::Buffers buf;
-    cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_eig = nullptr, ev_join = nullptr;
+    // stream: host-buffer evaluations; fast: the FP32 stages (lowest
+    // priority); side: the FP64 eigensolves (highest priority)
+    cudaStream_t stream = nullptr, fast = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_eig = nullptr, ev_join = nullptr, ev_done = nullptr;
     int64_t launches = 0;
     int device = 0;
     // stage timing (ce_session_set_profiling)
@@ -229,6 +233,8 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         dev_alloc(b.nominal, (size_t)cap);
         dev_alloc(b.fit_counts, (size_t)(MAXT + 1));
         dev_alloc(b.fit_order, (size_t)(MAXT + 1) * cap);
+        dev_alloc(b.nominal_list, (size_t)cap);
+        dev_alloc(b.nominal_count, (size_t)3);  // listed count, then the work counters of the two FP64 kernels
         b.cap = cap;
         b.nt = nt;
         b.pitch = pitch;
@@ -306,24 +312,33 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         CE_CUDA(cudaEventRecord(pd.b, on));
         s->pending.push_back(pd);
     };
-    CE_CUDA(cudaEventRecord(s->ev_fork, st));
-    CE_CUDA(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
-    // side stream: the FP64 eigensolves (LIN_A, then the nominal closed loop of
-    // every candidate LIN_A does not flag) run under the FP32 simulation and fit
-    timed(0, s->side, [&] { launch_lina_eig(r, P, prec, d_gains, b.lina, b.eig, s->side); });
-    CE_CUDA(cudaEventRecord(s->ev_eig, s->side));
-    timed(4, s->side, [&] { launch_nominal(r, P, prec, d_gains, b.lina, b.eig, b.nominal, s->side); });
-    CE_CUDA(cudaEventRecord(s->ev_join, s->side));
+    // Fork from the caller's stream onto the session's two streams and join
+    // back.  The FP64 eigensolves are persistent kernels with a fixed number
+    // of blocks per SM, launched first on a high-priority stream so that every
+    // SM takes its share of them; the FP32 stages on the other stream fill the
+    // rest of each SM and run alongside.
     const void* sk = prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
-    timed(1, st, [&] {
-        if (sk) launch_sim_specialised(sk, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, traj ? b.traj : nullptr, st);
-        else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, st);
+    cudaStream_t fs = s->fast, ss = s->side;
+    CE_CUDA(cudaEventRecord(s->ev_fork, st));
+    CE_CUDA(cudaStreamWaitEvent(fs, s->ev_fork, 0));
+    CE_CUDA(cudaStreamWaitEvent(ss, s->ev_fork, 0));
+    timed(0, ss, [&] {
+        launch_lina_eig(r, P, prec, d_gains, b.lina, b.eig, b.nominal, b.nominal_list, b.nominal_count, ss);
     });
-    CE_CUDA(cudaStreamWaitEvent(st, s->ev_eig, 0));
-    timed(2, st, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, b.fit_counts, b.fit_order, st); });
-    timed(3, st, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, st); });
-    CE_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
-    timed(5, st, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, st); });
+    timed(1, fs, [&] {
+        if (sk) launch_sim_specialised(sk, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, traj ? b.traj : nullptr, fs);
+        else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, fs);
+    });
+    CE_CUDA(cudaEventRecord(s->ev_eig, ss));
+    timed(4, ss, [&] { launch_nominal(r, P, prec, d_gains, b.lina, b.nominal_list, b.nominal_count, b.nominal, ss); });
+    CE_CUDA(cudaEventRecord(s->ev_join, ss));
+    CE_CUDA(cudaStreamWaitEvent(fs, s->ev_eig, 0));
+    timed(2, fs, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, b.fit_counts, b.fit_order, fs); });
+    timed(3, fs, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, fs); });
+    CE_CUDA(cudaStreamWaitEvent(fs, s->ev_join, 0));
+    timed(5, fs, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, fs); });
+    CE_CUDA(cudaEventRecord(s->ev_done, fs));
+    CE_CUDA(cudaStreamWaitEvent(st, s->ev_done, 0));
     s->launches += 7;
 }
 
@@ -504,7 +519,11 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     }
     CE_CUDA(cudaGetDevice(&s->device));
     CE_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-    CE_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    int prio_least = 0, prio_greatest = 0;
+    CE_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    CE_CUDA(cudaStreamCreateWithPriority(&s->fast, cudaStreamNonBlocking, prio_least));
+    CE_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_greatest));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
@@ -556,6 +575,8 @@ void destroy_session(ce_session* s) {
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->side) cudaStreamDestroy(s->side);
+    if (s->fast) cudaStreamDestroy(s->fast);
+    if (s->ev_done) cudaEventDestroy(s->ev_done);
     delete s;
 }
 

@@ -26,6 +26,17 @@ template <typename... Args>
         if (err_ != cudaSuccess) ::ce::fail("CUDA error {} at {}:{}", cudaGetErrorString(err_), __FILE__, __LINE__); \
     } while (0)
 
+// Every kernel of the pipeline asks for the largest shared-memory carveout.
+// An SM holds blocks of several kernels at once only under one L1/shared
+// split; with the default (per-kernel) preference the small-footprint FP32
+// kernels get SMs configured for little shared memory, on which the FP64
+// eigensolves' blocks (35 KB each) cannot be placed, and the two streams
+// serialise instead of sharing the SMs.
+inline void prefer_shared(const void* fn) {
+    CE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+}
+
 void derive(ce_config& c);
 void parse_config(const std::string& text, const std::string& filename, ce_config& out);
 void decode_instructions(const int32_t* info, int dim, int count, const float* base_params, int n_params,
@@ -34,10 +45,14 @@ void decode_instructions(const int32_t* info, int dim, int count, const float* b
 // Kernel launchers (ce_k_*.cu); all enqueue on `st`.
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
                 cudaStream_t st);
+// LIN_A and its FP64 eigenvalues; candidates that pass the modal stability
+// test are appended to list, the others get nominal = -1.  count holds three
+// ints (reset here): the listed count and the work counters of both kernels.
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                     cudaStream_t st);
+                     int* nominal, int* list, int* count, cudaStream_t st);
+// Nominal closed-loop stability (nominal = 1 / 0) of the listed candidates.
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
-                    const void* eig, int* nominal, cudaStream_t st);
+                    const int* list, const int* count, int* nominal, cudaStream_t st);
 // counts (MAXT + 1 ints) and order ((MAXT + 1) * n ints) bucket the candidates
 // by fit class before the fit; both null: candidates in index order.
 void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,

@@ -141,6 +141,12 @@ const void* compile(const std::string& src, std::string& log) {
         log = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
         return nullptr;
     }
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k), cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) {
+        log = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
     return reinterpret_cast<const void*>(k);
 }
 

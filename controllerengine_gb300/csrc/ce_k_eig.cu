@@ -42,6 +42,7 @@
 // computing the scalar steps (Householder vectors, shifts, deflation tests)
 // redundantly in every lane of the group.
 #include <cfloat>
+#include <algorithm>
 #include <cstdlib>
 
 #include "ce_device.cuh"
@@ -52,6 +53,7 @@ namespace ce {
 // One warp per block; EQ lanes per matrix, so 32 / EQ matrices per block,
 // interleaved in shared memory with a stride of 32 / EQ + 1 doubles.
 constexpr int EIG_LANES_DEFAULT = 2;
+constexpr int EIG_BLOCKS_PER_SM_DEFAULT = 5;
 template <int EQ> constexpr int eig_mats() { return 32 / EQ; }
 template <int EQ> constexpr int eig_stride() { return 32 / EQ + 1; }
 constexpr double DEPS = 2.220446049250313080847e-16;
@@ -571,44 +573,73 @@ __device__ __forceinline__ Quad<EQ> make_quad() {
     const int q = lane % EQ;
     return Quad<EQ>{q, ((EQ == 32) ? 0xFFFFFFFFu : ((1u << EQ) - 1u)) << (lane - q)};
 }
+// First index of the next 32 / EQ matrices for the calling warp (one-warp
+// blocks); called by all 32 lanes together, so the loop around it decides to
+// stop for the whole warp at once.
+template <int EQ>
+__device__ __forceinline__ int64_t take_work(int* next) {
+    int base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(next, eig_mats<EQ>());
+    return (int64_t)__shfl_sync(0xFFFFFFFFu, base, 0);
+}
+
+// Candidates whose LIN_A eigenvalues pass the modal stability test (no
+// |lambda| > 1, the test k_fit and k_modal apply) go on the list that k_nominal
+// works through; the others get nominal = -1 (the sweep never reads it).
+__device__ __forceinline__ void list_if_stable(bool unstable, int64_t c, int* nominal, int* list, int* count) {
+    if (unstable) {
+        nominal[c] = -1;
+    } else {
+        list[atomicAdd(count, 1)] = (int)c;
+    }
+}
+
 template <int EQ>
 __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
-                                                        float* __restrict__ eig32, double* __restrict__ eig64) {
+                                                        float* __restrict__ eig32, int* __restrict__ nominal,
+                                                        int* __restrict__ list, int* __restrict__ count,
+                                                        int* __restrict__ next) {
     extern __shared__ double smem[];
     const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
-    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
-    if (c >= run.n) return;  // the whole quad leaves together
-    const int ns = run.ns, nt = run.nt;
-    const float* row = gains + c * run.cuda_w;
-    float K[MAXS], L[MAXS];
+    // persistent: the grid covers a fixed number of blocks per SM; each warp
+    // takes the next 32 / EQ matrices from a counter when it is done (the
+    // iteration count varies a lot between matrices, a static split would
+    // leave the slowest warp's share as the tail)
+    for (;;) {
+        const int64_t base = take_work<EQ>(next);  // the same in every lane
+        if (base >= run.n) break;
+        const int64_t c = base + m;
+        if (c < run.n) {
+            const int ns = run.ns, nt = run.nt;
+            const float* row = gains + c * run.cuda_w;
+            float K[MAXS], L[MAXS];
 #pragma unroll
-    for (int i = 0; i < MAXS; ++i) {
-        K[i] = i < ns ? row[i] : 0.0f;
-        L[i] = i < ns ? row[ns + i] : 0.0f;
-    }
-    SMat T{smem + m, nt, eig_stride<EQ>()};
-    float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int e = Q.q; e < nt * nt; e += EQ) {
-        const int i = e / nt, j = e % nt;
-        const float v = lina_entry(P, K, L, ns, i, j);
-        lrow[e] = v;
-        T(i, j) = (double)v;
-    }
-    Q.sync();
-    if (eig64) {
-        double* out = eig64 + c * (int64_t)(2 * nt);
-        eig_real(T, Q, nt, [&](int i, double re, double im) {
-            out[2 * i] = re;
-            out[2 * i + 1] = im;
-        });
-    } else {
-        float* out = eig32 + c * (int64_t)(2 * nt);
-        eig_real(T, Q, nt, [&](int i, double re, double im) {
-            out[2 * i] = (float)re;
-            out[2 * i + 1] = (float)im;
-        });
+            for (int i = 0; i < MAXS; ++i) {
+                K[i] = i < ns ? row[i] : 0.0f;
+                L[i] = i < ns ? row[ns + i] : 0.0f;
+            }
+            SMat T{smem + m, nt, eig_stride<EQ>()};
+            float* lrow = lina + c * (int64_t)(nt * nt);
+            for (int e = Q.q; e < nt * nt; e += EQ) {
+                const int i = e / nt, j = e % nt;
+                const float v = lina_entry(P, K, L, ns, i, j);
+                lrow[e] = v;
+                T(i, j) = (double)v;
+            }
+            Q.sync();
+            float* out = eig32 + c * (int64_t)(2 * nt);
+            float mx = 0.0f;
+            eig_real(T, Q, nt, [&](int i, double re, double im) {
+                const float fr = (float)re, fi = (float)im;
+                out[2 * i] = fr;
+                out[2 * i + 1] = fi;
+                mx = fmaxf(mx, hypotf(fr, fi));
+            });
+            if (Q.lead()) list_if_stable(mx > 1.0f, c, nominal, list, count);
+        }
+        __syncwarp();  // the slots are rewritten for the next matrices
     }
 }
 
@@ -616,104 +647,106 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
 template <int EQ>
 __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
                                                           const float* __restrict__ gains, float* __restrict__ lina,
-                                                          double* __restrict__ eig64) {
+                                                          double* __restrict__ eig64, int* __restrict__ nominal,
+                                                          int* __restrict__ list, int* __restrict__ count,
+                                                          int* __restrict__ next) {
     extern __shared__ double smem[];
     const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
-    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
-    if (c >= run.n) return;
-    const int ns = run.ns, nt = run.nt;
-    const float* row = gains + c * run.cuda_w;
-    SMat T{smem + m, nt, eig_stride<EQ>()};
-    float* lrow = lina + c * (int64_t)(nt * nt);
-    for (int e = Q.q; e < nt * nt; e += EQ) {
-        const int i = e / nt, j = e % nt;
-        double v;
-        if (i < ns && j < ns) {
-            const double Kj = row[j], Li = row[ns + i];
-            v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
-        } else if (i < ns) {
-            v = (double)row[ns + i] * (double)P.d_c[j - ns];
-        } else if (j < ns) {
-            v = -(double)P.d_bu[i - ns] * (double)row[j];
-        } else {
-            v = P.d_a[(i - ns) * MAXD + (j - ns)];
+    for (;;) {
+        const int64_t base = take_work<EQ>(next);
+        if (base >= run.n) break;
+        const int64_t c = base + m;
+        if (c < run.n) {
+            const int ns = run.ns, nt = run.nt;
+            const float* row = gains + c * run.cuda_w;
+            SMat T{smem + m, nt, eig_stride<EQ>()};
+            float* lrow = lina + c * (int64_t)(nt * nt);
+            for (int e = Q.q; e < nt * nt; e += EQ) {
+                const int i = e / nt, j = e % nt;
+                double v;
+                if (i < ns && j < ns) {
+                    const double Kj = row[j], Li = row[ns + i];
+                    v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
+                } else if (i < ns) {
+                    v = (double)row[ns + i] * (double)P.d_c[j - ns];
+                } else if (j < ns) {
+                    v = -(double)P.d_bu[i - ns] * (double)row[j];
+                } else {
+                    v = P.d_a[(i - ns) * MAXD + (j - ns)];
+                }
+                lrow[e] = (float)v;
+                T(i, j) = v;
+            }
+            Q.sync();
+            double* out = eig64 + c * (int64_t)(2 * nt);
+            double mx = 0.0;
+            eig_real(T, Q, nt, [&](int i, double re, double im) {
+                out[2 * i] = re;
+                out[2 * i + 1] = im;
+                mx = fmax(mx, hypot(re, im));
+            });
+            if (Q.lead()) list_if_stable(mx > 1.0, c, nominal, list, count);
         }
-        lrow[e] = (float)v;
-        T(i, j) = v;
+        __syncwarp();
     }
-    Q.sync();
-    double* out = eig64 + c * (int64_t)(2 * nt);
-    eig_real(T, Q, nt, [&](int i, double re, double im) {
-        out[2 * i] = re;
-        out[2 * i + 1] = im;
-    });
 }
 
 // Nominal closed loop of the margin check (ref: src/allmargin.cu:50-87):
 // Acl_nom = [OPEN_A - (D L) K^T, -L C^T; B K^T, A] with OPEN_A = LIN_A[:ns,:ns]
-// and (A, B, C, D) the margin plant.  nominal[c] = 1 if stable, 0 if not, -1
-// if the candidate is modal-unstable (the sweep never reads it then).
+// and (A, B, C, D) the margin plant.  nominal[c] = 1 if stable, 0 if not.
+// Only the candidates k_lina_eig listed (those the modal stage does not flag
+// unstable, so the only ones the sweep reads) are solved, packed into full
+// warps; the work is independent of the modal stage, so this kernel runs
+// concurrently with it.
 template <int EQ>
 __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
-                                                       const void* __restrict__ eig, int* __restrict__ nominal,
-                                                       int fp64_form) {
+                                                       const int* __restrict__ list, const int* __restrict__ count,
+                                                       int* __restrict__ nominal, int fp64_form, int* __restrict__ next) {
     extern __shared__ double smem[];
     const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
-    const int64_t c = (int64_t)blockIdx.x * eig_mats<EQ>() + m;
-    if (c >= run.n) return;
-    // Candidates the modal stage will flag unstable (max |lambda(LIN_A)| > 1, the
-    // same float test) never reach the sweep; everything else is solved here,
-    // independent of the modal stage, so this kernel can run concurrently with it.
-    {
-        bool unstable;
-        if (fp64_form) {
-            double mx = 0.0;
-            const double* e = static_cast<const double*>(eig) + c * (int64_t)(2 * run.nt);
-            for (int i = 0; i < run.nt; ++i) mx = fmax(mx, hypot(e[2 * i], e[2 * i + 1]));
-            unstable = mx > 1.0;
-        } else {
-            float mx = 0.0f;
-            const float* e = static_cast<const float*>(eig) + c * (int64_t)(2 * run.nt);
-            for (int i = 0; i < run.nt; ++i) mx = fmaxf(mx, hypotf(e[2 * i], e[2 * i + 1]));
-            unstable = mx > 1.0f;
+    const int64_t listed = *count;
+    for (;;) {
+        const int64_t base = take_work<EQ>(next);
+        if (base >= listed) break;
+        const int64_t idx = base + m;
+        if (idx < listed) {
+            const int64_t c = list[idx];
+            const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
+            const float* row = gains + c * run.cuda_w;
+            const float* la = lina + c * (int64_t)(nt * nt);
+            SMat T{smem + m, n2, eig_stride<EQ>()};
+            for (int e = Q.q; e < ns * ns; e += EQ) {
+                const int i = e / ns, j = e % ns;
+                const float Li = row[ns + i];
+                const float Kj = row[j];
+                if (fp64_form) {
+                    T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
+                    T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
+                    T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
+                } else {
+                    T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
+                    T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
+                    T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
+                }
+                T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
+            }
+            Q.sync();
+            bool stable = true;
+            const bool ok = eig_real(T, Q, n2, [&](int, double re, double im) {
+                if (hypot(re, im) >= 1.0) stable = false;
+            });
+            if (Q.lead()) nominal[c] = (ok && stable) ? 1 : 0;
         }
-        if (unstable) {
-            if (Q.lead()) nominal[c] = -1;
-            return;
-        }
+        __syncwarp();
     }
-    const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
-    const float* row = gains + c * run.cuda_w;
-    const float* la = lina + c * (int64_t)(nt * nt);
-    SMat T{smem + m, n2, eig_stride<EQ>()};
-    for (int e = Q.q; e < ns * ns; e += EQ) {
-        const int i = e / ns, j = e % ns;
-        const float Li = row[ns + i];
-        const float Kj = row[j];
-        if (fp64_form) {
-            T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
-            T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
-            T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
-        } else {
-            T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
-            T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
-            T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
-        }
-        T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
-    }
-    Q.sync();
-    bool stable = true;
-    const bool ok = eig_real(T, Q, n2, [&](int, double re, double im) {
-        if (hypot(re, im) >= 1.0) stable = false;
-    });
-    if (Q.lead()) nominal[c] = (ok && stable) ? 1 : 0;
 }
 
 static void set_smem(const void* fn, size_t bytes) {
     CE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    prefer_shared(fn);
 }
 
 // Lanes per matrix of the FP64 eigensolves.  One lane per matrix issues the
@@ -731,45 +764,65 @@ static int eig_lanes() {
     return v;
 }
 
+// Blocks (one warp each) per SM of the persistent FP64 kernels.  Their
+// footprint is mostly shared memory (16 matrices x 2 KB per warp with two
+// lanes per matrix); a fixed number per SM keeps the FP64 pipe of every SM
+// fed while leaving the rest of the SM to the FP32 stages that run alongside
+// on the other stream.  CE_EIG_BLOCKS_PER_SM overrides.
+static int eig_grid(int64_t work, int mats) {
+    static const int per_sm = [] {
+        const char* e = std::getenv("CE_EIG_BLOCKS_PER_SM");
+        const int k = e ? std::atoi(e) : 0;
+        return (k >= 1 && k <= 32) ? k : EIG_BLOCKS_PER_SM_DEFAULT;
+    }();
+    int dev = 0, sms = 0;
+    CE_CUDA(cudaGetDevice(&dev));
+    CE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t need = (work + mats - 1) / mats;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)per_sm * sms));
+}
+
 template <int EQ>
 static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                       cudaStream_t st) {
-    const int grid = (int)((run.n + eig_mats<EQ>() - 1) / eig_mats<EQ>());
+                       int* nominal, int* list, int* count, cudaStream_t st) {
+    const int grid = eig_grid(run.n, eig_mats<EQ>());
     const size_t smem = (size_t)run.nt * run.nt * eig_stride<EQ>() * sizeof(double);
     if (precision == CE_PRECISION_FP64) {
         set_smem((const void*)k_lina_eig64<EQ>, smem);
-        k_lina_eig64<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig);
+        k_lina_eig64<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig, nominal, list, count, count + 1);
     } else {
         set_smem((const void*)k_lina_eig<EQ>, smem);
-        k_lina_eig<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nullptr);
+        k_lina_eig<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count, count + 1);
     }
 }
 
 template <int EQ>
 static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
-                      const void* eig, int* nominal, cudaStream_t st) {
-    const int grid = (int)((run.n + eig_mats<EQ>() - 1) / eig_mats<EQ>());
+                      const int* list, const int* count, int* nominal, cudaStream_t st) {
+    const int grid = eig_grid(run.n, eig_mats<EQ>());  // the listed count is only known on the device
     const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
     set_smem((const void*)k_nominal<EQ>, smem);
-    k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, eig, nominal, precision == CE_PRECISION_FP64);
+    k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, precision == CE_PRECISION_FP64,
+                                          const_cast<int*>(count) + 2);
 }
 
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                     cudaStream_t st) {
+                     int* nominal, int* list, int* count, cudaStream_t st) {
+    CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
     switch (eig_lanes()) {
-        case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, st); break;
-        case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, st); break;
-        default: lina_eig_q<4>(run, P, precision, gains, lina, eig, st); break;
+        case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
+        case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
+        default: lina_eig_q<4>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
     }
     CE_CUDA(cudaGetLastError());
 }
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
-                    const void* eig, int* nominal, cudaStream_t st) {
+                    const int* list, const int* count, int* nominal, cudaStream_t st) {
     switch (eig_lanes()) {
-        case 1: nominal_q<1>(run, P, precision, gains, lina, eig, nominal, st); break;
-        case 2: nominal_q<2>(run, P, precision, gains, lina, eig, nominal, st); break;
-        default: nominal_q<4>(run, P, precision, gains, lina, eig, nominal, st); break;
+        case 1: nominal_q<1>(run, P, precision, gains, lina, list, count, nominal, st); break;
+        case 2: nominal_q<2>(run, P, precision, gains, lina, list, count, nominal, st); break;
+        default: nominal_q<4>(run, P, precision, gains, lina, list, count, nominal, st); break;
     }
     CE_CUDA(cudaGetLastError());
 }

@@ -10,12 +10,14 @@
 //
 // GB300 layout: the reference keeps the 32x32 AtA in a per-thread local array
 // (4.6 KB stack, ref: src/modalsetup.cu:67).  Here 16 lanes own one candidate
-// and work through the window in chunks of 16 steps: first the chunk's
-// 16 x unique basis pairs (one expf + one sin/cos pair each) are spread evenly
+// and work through the window in chunks of 8 steps: first the chunk's
+// 8 x unique basis pairs (one expf + one sin/cos pair each) are spread evenly
 // over the lanes and written to shared memory, then every lane accumulates its
-// 4x4 tiles of the lower triangle over the 16 steps with two 16-byte shared
+// 4x4 tiles of the lower triangle over the 8 steps with two 16-byte shared
 // loads and 16 fused multiply-adds per tile and step.  The fit window is read
-// as 64 contiguous bytes per chunk.
+// as 32 contiguous bytes per chunk.  The small chunk keeps the shared-memory
+// footprint (1.2 KB per candidate) low enough for the FP64 eigensolves that
+// run alongside on the same SMs.
 
 // k_modal restates modalsolve (ref: src/modalsolve.cu:1-108): diagonal
 // scaling, LDLT with symmetric pivoting of the 2nt x 2nt system, per-mode
@@ -112,7 +114,7 @@ __device__ __forceinline__ void mode_of(const Modes<R>& m, int nt, int e, R& sig
 
 constexpr int FIT_BLOCK = 128;            // 8 candidates per block
 constexpr int FIT_CPB = FIT_BLOCK / 16;
-constexpr int FIT_CHUNK = 16;             // window steps per chunk (= lanes per candidate)
+constexpr int FIT_CHUNK = 8;              // window steps per chunk (shared memory: 1.2 KB per candidate)
 constexpr int FIT_PITCH = 36;             // basis row: nc values, y at index nc, zeros up to 4*ceil((nc+1)/4)
 constexpr int FIT_ROUNDS = 2;             // 4x4 tiles per lane and pass (32 tiles: nc <= 27 in one pass)
 constexpr int FIT_CLASSES = MAXT + 1;     // 0: modal-unstable, u = 1..MAXT: stable with u unique modes
@@ -226,9 +228,11 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
     // is still one fused multiply-add per step in the order of t.
     for (int e = lane; e < FIT_CHUNK * FIT_PITCH; e += 16) (&cb[g][0][0])[e] = R(0);
     const int N = nc + 1, NB = (N + 3) >> 2, nblk = NB * (NB + 1) / 2;
-    // basis work item k = (step k / unique, mode k % unique); lane l takes k = l, l + 16, ...
+    // basis work item k = (step k / unique, mode k % unique) of a chunk; lane l
+    // takes k = l, l + 16, ... < FIT_CHUNK * unique
     const int s0 = lane / unique, m0 = lane - s0 * unique;
-    const int ds = FIT_CHUNK / unique, dm = FIT_CHUNK - ds * unique;
+    const int ds = 16 / unique, dm = 16 - ds * unique;
+    const int items = FIT_CHUNK * unique;
     const R* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
     const int steps = run.fit_steps;
@@ -252,13 +256,13 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
 #pragma unroll
             for (int k = 0; k < 16; ++k) acc[r][k] = R(0);
         for (int w0 = 0; w0 < steps; w0 += FIT_CHUNK) {
-            {
+            if (lane < FIT_CHUNK) {
                 const int idx = w0 + lane;
                 const R yw = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
                 cb[g][lane][nc] = rsub(yw, yss);
             }
             int s = s0, md = m0;
-            for (int it = 0; it < unique; ++it) {
+            for (int k = lane; k < items; k += 16) {
                 const int w = w0 + s;
                 if (w < steps) {
                     const R sig = mp[g][md][0], om = mp[g][md][1], shift = mp[g][md][2];
@@ -545,12 +549,17 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
     if (counts) {
         CE_CUDA(cudaMemsetAsync(counts, 0, FIT_CLASSES * sizeof(int), st));
         const int cgrid = (int)((run.n + 127) / 128);
-        if (precision == CE_PRECISION_FP64)
+        if (precision == CE_PRECISION_FP64) {
+            prefer_shared((const void*)k_fit_classify<double>);
             k_fit_classify<double><<<cgrid, 128, 0, st>>>(run, (const double*)eig, counts, order);
-        else
+        } else {
+            prefer_shared((const void*)k_fit_classify<float>);
             k_fit_classify<float><<<cgrid, 128, 0, st>>>(run, (const float*)eig, counts, order);
+        }
         CE_CUDA(cudaGetLastError());
     }
+    prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_fit<double, double>
+                                                 : (const void*)k_fit<float, SimSummary>);
     if (precision == CE_PRECISION_FP64)
         k_fit<double, double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin,
                                                          (const double*)summ, (double*)ata, (double*)atb, info,
@@ -565,6 +574,7 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st) {
     const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
+    prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_modal<double> : (const void*)k_modal<float>);
     if (precision == CE_PRECISION_FP64)
         k_modal<double><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
                                                           (const double*)atb, info);

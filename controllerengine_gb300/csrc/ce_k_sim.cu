@@ -97,10 +97,13 @@ template <int NSC, int NDC>
 static void sim_launch(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ,
                        float* traj, cudaStream_t st) {
     const int grid = (int)((run.n + SIM_BLOCK - 1) / SIM_BLOCK);
-    if (precision == CE_PRECISION_FP64)
+    if (precision == CE_PRECISION_FP64) {
+        prefer_shared((const void*)k_sim_fp64<NSC, NDC>);
         k_sim_fp64<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
-    else
+    } else {
+        prefer_shared((const void*)k_sim_mixed<NSC, NDC>);
         k_sim_mixed<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
+    }
 }
 
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,

@@ -180,9 +180,16 @@ template <typename R>
 static void sweep_dispatch(const Run& run, const float* gains, const float* lina, const int* nominal, const R* fgrid,
                            float* info, cudaStream_t st) {
     const int grid = (int)((run.n + SWEEP_BLOCK - 1) / SWEEP_BLOCK);
-    if (run.ns <= 2) k_sweep<R, 2><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
-    else if (run.ns <= 4) k_sweep<R, 4><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
-    else k_sweep<R, 8><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+    if (run.ns <= 2) {
+        prefer_shared((const void*)k_sweep<R, 2>);
+        k_sweep<R, 2><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+    } else if (run.ns <= 4) {
+        prefer_shared((const void*)k_sweep<R, 4>);
+        k_sweep<R, 4><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+    } else {
+        prefer_shared((const void*)k_sweep<R, 8>);
+        k_sweep<R, 8><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+    }
 }
 
 void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
