@@ -12,7 +12,9 @@
 //         └─ k_sim      (FP32) ──┴─ k_fit ─ k_modal (FP32) ──────┴─ k_sweep
 //
 // Only gains in and cost rows out cross the host boundary.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -161,7 +163,8 @@ struct ce_session {
     // stream: host-buffer evaluations; fast: the FP32 stages (lowest
     // priority); side: the FP64 eigensolves (highest priority)
     cudaStream_t stream = nullptr, fast = nullptr, side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_eig = nullptr, ev_join = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_eig[ce::MAX_CHUNKS] = {}, ev_nom[ce::MAX_CHUNKS] = {};
     int64_t launches = 0;
     int device = 0;
     // stage timing (ce_session_set_profiling)
@@ -231,10 +234,11 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         CE_CUDA(cudaMalloc(&b.ata, (size_t)cap * 4 * nt * nt * rsz + 16));
         CE_CUDA(cudaMalloc(&b.atb, (size_t)cap * 2 * nt * rsz + 16));
         dev_alloc(b.nominal, (size_t)cap);
-        dev_alloc(b.fit_counts, (size_t)(MAXT + 1));
+        dev_alloc(b.fit_counts, (size_t)(MAXT + 1) * MAX_CHUNKS);
         dev_alloc(b.fit_order, (size_t)(MAXT + 1) * cap);
         dev_alloc(b.nominal_list, (size_t)cap);
-        dev_alloc(b.nominal_count, (size_t)3);  // listed count, then the work counters of the two FP64 kernels
+        // per chunk: listed count, then the work counters of the two FP64 kernels
+        dev_alloc(b.nominal_count, (size_t)3 * MAX_CHUNKS);
         b.cap = cap;
         b.nt = nt;
         b.pitch = pitch;
@@ -288,6 +292,19 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
     return r;
 }
 
+// Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
+// CE_CHUNKS (default 4).
+int n_chunks(int64_t n) {
+    static const int want = [] {
+        const char* e = std::getenv("CE_CHUNKS");
+        const int k = e ? std::atoi(e) : 0;
+        return (k >= 1 && k <= MAX_CHUNKS) ? k : 4;
+    }();
+    int k = want;
+    while (k > 1 && n / k < 16384) --k;
+    return k;
+}
+
 // One evaluation: gains and info rows already on the device in d_gains / d_info.
 void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
                   bool traj) {
@@ -316,30 +333,76 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // back.  The FP64 eigensolves are persistent kernels with a fixed number
     // of blocks per SM, launched first on a high-priority stream so that every
     // SM takes its share of them; the FP32 stages on the other stream fill the
-    // rest of each SM and run alongside.
+    // rest of each SM and run alongside.  Large batches are cut into chunks so
+    // that the fit of a chunk starts as soon as its eigenvalues are known, while
+    // the eigensolves of the next chunks continue.
     const void* sk = prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
     cudaStream_t fs = s->fast, ss = s->side;
+    const int nch = n_chunks(n);
+    const int64_t per = (n + nch - 1) / nch;
+    const size_t rsz = prec == CE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    const int nt = r.nt, cw = r.cuda_w, iw = r.info_w;
+    auto chunk = [&](int k, Run& rc, int64_t& off) {
+        off = k * per;
+        rc = r;
+        rc.n = std::min<int64_t>(per, n - off);
+    };
+    auto at = [](const void* p, int64_t off, size_t bytes) {
+        return (void*)((const char*)p + (size_t)off * bytes);
+    };
     CE_CUDA(cudaEventRecord(s->ev_fork, st));
     CE_CUDA(cudaStreamWaitEvent(fs, s->ev_fork, 0));
     CE_CUDA(cudaStreamWaitEvent(ss, s->ev_fork, 0));
-    timed(0, ss, [&] {
-        launch_lina_eig(r, P, prec, d_gains, b.lina, b.eig, b.nominal, b.nominal_list, b.nominal_count, ss);
-    });
+    for (int k = 0; k < nch; ++k) {
+        Run rc;
+        int64_t off;
+        chunk(k, rc, off);
+        timed(0, ss, [&] {
+            launch_lina_eig(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt, at(b.eig, off, 2 * nt * rsz),
+                            b.nominal + off, b.nominal_list + off, b.nominal_count + 3 * k, ss);
+        });
+        CE_CUDA(cudaEventRecord(s->ev_eig[k], ss));
+    }
+    for (int k = 0; k < nch; ++k) {
+        Run rc;
+        int64_t off;
+        chunk(k, rc, off);
+        timed(4, ss, [&] {
+            launch_nominal(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal_list + off,
+                           b.nominal_count + 3 * k, b.nominal + off, ss);
+        });
+        CE_CUDA(cudaEventRecord(s->ev_nom[k], ss));
+    }
     timed(1, fs, [&] {
         if (sk) launch_sim_specialised(sk, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, traj ? b.traj : nullptr, fs);
         else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, fs);
     });
-    CE_CUDA(cudaEventRecord(s->ev_eig, ss));
-    timed(4, ss, [&] { launch_nominal(r, P, prec, d_gains, b.lina, b.nominal_list, b.nominal_count, b.nominal, ss); });
-    CE_CUDA(cudaEventRecord(s->ev_join, ss));
-    CE_CUDA(cudaStreamWaitEvent(fs, s->ev_eig, 0));
-    timed(2, fs, [&] { launch_fit(r, prec, b.eig, b.ywin, b.summ, b.ata, b.atb, d_info, b.fit_counts, b.fit_order, fs); });
-    timed(3, fs, [&] { launch_modal(r, prec, b.eig, b.ata, b.atb, d_info, fs); });
-    CE_CUDA(cudaStreamWaitEvent(fs, s->ev_join, 0));
-    timed(5, fs, [&] { launch_sweep(r, prec, d_gains, b.lina, b.nominal, fgrid, d_info, fs); });
+    for (int k = 0; k < nch; ++k) {
+        Run rc;
+        int64_t off;
+        chunk(k, rc, off);
+        CE_CUDA(cudaStreamWaitEvent(fs, s->ev_eig[k], 0));
+        const void* eig = at(b.eig, off, 2 * nt * rsz);
+        void* ata = at(b.ata, off, 4 * nt * nt * rsz);
+        void* atb = at(b.atb, off, 2 * nt * rsz);
+        timed(2, fs, [&] {
+            launch_fit(rc, prec, eig, at(b.ywin, off, (size_t)r.fit_pitch * rsz), at(b.summ, off, 4 * rsz), ata, atb,
+                       d_info + off * iw, b.fit_counts + (MAXT + 1) * k, b.fit_order + (MAXT + 1) * off, fs);
+        });
+        timed(3, fs, [&] { launch_modal(rc, prec, eig, ata, atb, d_info + off * iw, fs); });
+    }
+    for (int k = 0; k < nch; ++k) {
+        Run rc;
+        int64_t off;
+        chunk(k, rc, off);
+        CE_CUDA(cudaStreamWaitEvent(fs, s->ev_nom[k], 0));
+        timed(5, fs, [&] {
+            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, fgrid, d_info + off * iw, fs);
+        });
+    }
     CE_CUDA(cudaEventRecord(s->ev_done, fs));
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_done, 0));
-    s->launches += 7;
+    s->launches += 1 + 6 * nch;
 }
 
 std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {
@@ -525,8 +588,10 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     CE_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_greatest));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
-    CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig, cudaEventDisableTiming));
-    CE_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    for (int k = 0; k < MAX_CHUNKS; ++k) {
+        CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig[k], cudaEventDisableTiming));
+        CE_CUDA(cudaEventCreateWithFlags(&s->ev_nom[k], cudaEventDisableTiming));
+    }
     CE_CUDA(cudaMalloc((void**)&s->d_fgrid32, s->fgrid32.size() * sizeof(float)));
     CE_CUDA(cudaMalloc((void**)&s->d_fgrid64, s->fgrid64.size() * sizeof(double)));
     CE_CUDA(cudaMemcpy(s->d_fgrid32, s->fgrid32.data(), s->fgrid32.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -571,8 +636,10 @@ void destroy_session(ce_session* s) {
     if (s->d_fgrid32) cudaFree(s->d_fgrid32);
     if (s->d_fgrid64) cudaFree(s->d_fgrid64);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
-    if (s->ev_eig) cudaEventDestroy(s->ev_eig);
-    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    for (int k = 0; k < MAX_CHUNKS; ++k) {
+        if (s->ev_eig[k]) cudaEventDestroy(s->ev_eig[k]);
+        if (s->ev_nom[k]) cudaEventDestroy(s->ev_nom[k]);
+    }
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->fast) cudaStreamDestroy(s->fast);

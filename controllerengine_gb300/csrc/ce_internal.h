@@ -19,7 +19,8 @@ typedef long long int64_t;
 
 namespace ce {
 
-constexpr int SIM_BLOCK = 64;  // threads per simulation block (one candidate per thread)
+constexpr int SIM_BLOCK = 64;
+constexpr int MAX_CHUNKS = 8;  // largest number of chunks one evaluation is cut into  // threads per simulation block (one candidate per thread)
 
 constexpr int MAXS = CE_MAX_STATESPACE_DIM;   // 8
 constexpr int MAXD = CE_MAX_DISCRETE_DIM;     // 8
