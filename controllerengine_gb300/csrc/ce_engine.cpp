@@ -293,12 +293,13 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
 }
 
 // Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
-// CE_CHUNKS (default 4).
+// CE_CHUNKS (default 2: of 1, 2 and 4 chunks, 2 measured fastest on the
+// eight-state workload of 65,536 candidates).
 int n_chunks(int64_t n) {
     static const int want = [] {
         const char* e = std::getenv("CE_CHUNKS");
         const int k = e ? std::atoi(e) : 0;
-        return (k >= 1 && k <= MAX_CHUNKS) ? k : 4;
+        return (k >= 1 && k <= MAX_CHUNKS) ? k : 2;
     }();
     int k = want;
     while (k > 1 && n / k < 16384) --k;
