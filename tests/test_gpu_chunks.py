@@ -1,7 +1,8 @@
 """A large batch is evaluated in chunks (eigensolves of later chunks overlap the
 fit of earlier ones).  Every candidate is computed independently, so the INFO
-rows must not depend on how the batch is cut: one 49,152-candidate call (three
-chunks) must equal three 16,384-candidate calls (one chunk each), bit for bit.
+rows must not depend on how the batch is cut: one 49,152-candidate call (cut
+into chunks) must equal three 16,384-candidate calls (one chunk each), bit for
+bit.
 """
 import numpy as np
 import pytest
