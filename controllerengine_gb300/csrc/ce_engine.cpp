@@ -127,15 +127,21 @@ struct Buffers {
     int* fit_order = nullptr;
     int* nominal_list = nullptr;
     int* nominal_count = nullptr;
+    int* sweep_list = nullptr;
+    int* sweep_count = nullptr;
+    SweepScratch sweep{};
     float* traj = nullptr;
     int64_t traj_cap = 0;
     void release() {
         for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
-                        (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count, (void*)traj})
+                        (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count,
+                        (void*)sweep_list, (void*)sweep_count, sweep.mag, sweep.arg, sweep.bpc, (void*)sweep.fail,
+                        (void*)traj})
             if (p) cudaFree(p);
         gains = info = lina = traj = nullptr;
         eig = ywin = summ = ata = atb = nullptr;
-        nominal = fit_counts = fit_order = nominal_list = nominal_count = nullptr;
+        nominal = fit_counts = fit_order = nominal_list = nominal_count = sweep_list = sweep_count = nullptr;
+        sweep = SweepScratch{};
         cap = traj_cap = 0;
     }
 };
@@ -239,6 +245,14 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         dev_alloc(b.nominal_list, (size_t)cap);
         // per chunk: listed count, then the work counters of the two FP64 kernels
         dev_alloc(b.nominal_count, (size_t)3 * MAX_CHUNKS);
+        dev_alloc(b.sweep_list, (size_t)cap);
+        dev_alloc(b.sweep_count, (size_t)MAX_CHUNKS);
+        // shared by the chunks, which the sweep processes one after the other
+        const size_t groups = (size_t)(c.freq + SWEEP_FG - 1) / SWEEP_FG;
+        CE_CUDA(cudaMalloc(&b.sweep.mag, (size_t)cap * c.freq * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.sweep.arg, (size_t)cap * c.freq * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.sweep.bpc, (size_t)cap * groups * rsz + 16));
+        dev_alloc(b.sweep.fail, (size_t)cap * groups);
         b.cap = cap;
         b.nt = nt;
         b.pitch = pitch;
@@ -398,12 +412,13 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         CE_CUDA(cudaStreamWaitEvent(fs, s->ev_nom[k], 0));
         timed(5, fs, [&] {
-            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, fgrid, d_info + off * iw, fs);
+            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, fgrid, d_info + off * iw,
+                         b.sweep_list + off, b.sweep_count + k, b.sweep, fs);
         });
     }
     CE_CUDA(cudaEventRecord(s->ev_done, fs));
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_done, 0));
-    s->launches += 1 + 6 * nch;
+    s->launches += 1 + 8 * nch;
 }
 
 std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {

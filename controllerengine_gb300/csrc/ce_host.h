@@ -59,8 +59,19 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
                 void* atb, float* info, int* counts, int* order, cudaStream_t st);
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st);
+// Scratch of the margin sweep for up to `cap` listed candidates: |PG| and
+// arg(PG) per frequency (freq x cap values each, float or double as the
+// precision), and per frequency group the b(w) minimum and the first failure.
+struct SweepScratch {
+    void* mag;
+    void* arg;
+    void* bpc;
+    int* fail;
+};
+// The margin sweep; list (n ints) and count (1 int) are scratch for the
+// candidates that run the frequency loop.
 void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
-                  const void* fgrid, float* info, cudaStream_t st);
+                  const void* fgrid, float* info, int* list, int* count, const SweepScratch& sw, cudaStream_t st);
 
 double measure_fma_rate(bool fp64);
 

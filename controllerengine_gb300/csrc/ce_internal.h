@@ -20,7 +20,8 @@ typedef long long int64_t;
 namespace ce {
 
 constexpr int SIM_BLOCK = 64;
-constexpr int MAX_CHUNKS = 8;  // largest number of chunks one evaluation is cut into  // threads per simulation block (one candidate per thread)
+constexpr int MAX_CHUNKS = 8;  // largest number of chunks one evaluation is cut into
+constexpr int SWEEP_FG = 16;   // frequencies per thread in the LU pass of the margin sweep  // threads per simulation block (one candidate per thread)
 
 constexpr int MAXS = CE_MAX_STATESPACE_DIM;   // 8
 constexpr int MAXD = CE_MAX_DISCRETE_DIM;     // 8

@@ -122,39 +122,43 @@ __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, d
 
 // H = I - tau [1;ess][1;ess]^T from the left on rows r0..r0+m-1, columns
 // c0..c1-1 (columns split over the group).  Per column: tmp = ess.T(r0+1..) +
-// T(r0), T(r0) -= tau tmp, T(r0+k+1) -= tmp (tau ess_k).  Two columns are
+// T(r0), T(r0) -= tau tmp, T(r0+k+1) -= tmp (tau ess_k).  Four columns are
 // processed per iteration so that their independent chains overlap; each
 // column's operations and their order are unchanged.
 template <class Qd, typename E>
 __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, int m, int c0, int c1, E ess_at,
                                            double tau) {
+    constexpr int S = Qd::N;
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int j = c0 + Q.q; j < c1; j += Qd::N) T(r0, j) = __dmul_rn(T(r0, j), f);
+        for (int j = c0 + Q.q; j < c1; j += S) T(r0, j) = __dmul_rn(T(r0, j), f);
         return;
     }
     if (tau == 0.0) return;
     int j = c0 + Q.q;
-    for (; j + Qd::N < c1; j += 2 * Qd::N) {
-        const int j2 = j + Qd::N;
+    for (; j + 3 * S < c1; j += 4 * S) {
+        double t[4];
         const double e = ess_at(0);
-        double ta = __dmul_rn(e, T(r0 + 1, j)), tb = __dmul_rn(e, T(r0 + 1, j2));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] = __dmul_rn(e, T(r0 + 1, j + u * S));
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
-            ta = __dadd_rn(ta, __dmul_rn(ek, T(r0 + 1 + k, j)));
-            tb = __dadd_rn(tb, __dmul_rn(ek, T(r0 + 1 + k, j2)));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(ek, T(r0 + 1 + k, j + u * S)));
         }
-        ta = __dadd_rn(ta, T(r0, j));
-        tb = __dadd_rn(tb, T(r0, j2));
-        T(r0, j) = __dsub_rn(T(r0, j), __dmul_rn(tau, ta));
-        T(r0, j2) = __dsub_rn(T(r0, j2), __dmul_rn(tau, tb));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            t[u] = __dadd_rn(t[u], T(r0, j + u * S));
+            T(r0, j + u * S) = __dsub_rn(T(r0, j + u * S), __dmul_rn(tau, t[u]));
+        }
         for (int k = 0; k < m - 1; ++k) {
             const double te = __dmul_rn(tau, ess_at(k));
-            T(r0 + 1 + k, j) = __dsub_rn(T(r0 + 1 + k, j), __dmul_rn(ta, te));
-            T(r0 + 1 + k, j2) = __dsub_rn(T(r0 + 1 + k, j2), __dmul_rn(tb, te));
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                T(r0 + 1 + k, j + u * S) = __dsub_rn(T(r0 + 1 + k, j + u * S), __dmul_rn(t[u], te));
         }
     }
-    if (j < c1) {
+    for (; j < c1; j += S) {
         double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
         tmp = __dadd_rn(tmp, T(r0, j));
@@ -165,38 +169,43 @@ __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, i
 
 // H from the right on rows r0..r1-1 (split over the group), columns
 // c0..c0+m-1.  Per row: tmp = T(i,c0+1..).ess + T(i,c0), T(i,c0) -= tau tmp,
-// T(i,c0+k+1) -= ess_k (tau tmp).  Two rows per iteration.
+// T(i,c0+k+1) -= ess_k (tau tmp).  Four rows per iteration.
 template <class Qd, typename E>
 __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, int r1, int c0, int m, E ess_at,
                                             double tau) {
+    constexpr int S = Qd::N;
     if (m == 1) {
         const double f = __dsub_rn(1.0, tau);
-        for (int i = r0 + Q.q; i < r1; i += Qd::N) T(i, c0) = __dmul_rn(T(i, c0), f);
+        for (int i = r0 + Q.q; i < r1; i += S) T(i, c0) = __dmul_rn(T(i, c0), f);
         return;
     }
     if (tau == 0.0) return;
     int i = r0 + Q.q;
-    for (; i + Qd::N < r1; i += 2 * Qd::N) {
-        const int i2 = i + Qd::N;
+    for (; i + 3 * S < r1; i += 4 * S) {
+        double t[4];
         const double e = ess_at(0);
-        double ta = __dmul_rn(T(i, c0 + 1), e), tb = __dmul_rn(T(i2, c0 + 1), e);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] = __dmul_rn(T(i + u * S, c0 + 1), e);
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
-            ta = __dadd_rn(ta, __dmul_rn(T(i, c0 + 1 + k), ek));
-            tb = __dadd_rn(tb, __dmul_rn(T(i2, c0 + 1 + k), ek));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(T(i + u * S, c0 + 1 + k), ek));
         }
-        ta = __dadd_rn(ta, T(i, c0));
-        tb = __dadd_rn(tb, T(i2, c0));
-        T(i, c0) = __dsub_rn(T(i, c0), __dmul_rn(tau, ta));
-        T(i2, c0) = __dsub_rn(T(i2, c0), __dmul_rn(tau, tb));
-        const double tta = __dmul_rn(tau, ta), ttb = __dmul_rn(tau, tb);
+        double tt[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            t[u] = __dadd_rn(t[u], T(i + u * S, c0));
+            T(i + u * S, c0) = __dsub_rn(T(i + u * S, c0), __dmul_rn(tau, t[u]));
+            tt[u] = __dmul_rn(tau, t[u]);
+        }
         for (int k = 0; k < m - 1; ++k) {
             const double ek = ess_at(k);
-            T(i, c0 + 1 + k) = __dsub_rn(T(i, c0 + 1 + k), __dmul_rn(ek, tta));
-            T(i2, c0 + 1 + k) = __dsub_rn(T(i2, c0 + 1 + k), __dmul_rn(ek, ttb));
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                T(i + u * S, c0 + 1 + k) = __dsub_rn(T(i + u * S, c0 + 1 + k), __dmul_rn(ek, tt[u]));
         }
     }
-    if (i < r1) {
+    for (; i < r1; i += S) {
         double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
         tmp = __dadd_rn(tmp, T(i, c0));
@@ -208,40 +217,61 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
 
 // The Francis-step reflectors (m = 3, and m = 2 for the last one) with the
 // essential part in registers; same per-column / per-row operations as above.
+// Four columns (rows) per iteration: the work per element is a short chain of
+// dependent FP64 operations, and four independent chains per lane hide most
+// of their latency.
+template <int M>
+__device__ __forceinline__ void left_col(double& a0, double& a1, double& a2, double e0, double e1, double tau,
+                                         double te0, double te1) {
+    double t = __dmul_rn(e0, a1);
+    if (M == 3) t = __dadd_rn(t, __dmul_rn(e1, a2));
+    t = __dadd_rn(t, a0);
+    a0 = __dsub_rn(a0, __dmul_rn(tau, t));
+    a1 = __dsub_rn(a1, __dmul_rn(t, te0));
+    if (M == 3) a2 = __dsub_rn(a2, __dmul_rn(t, te1));
+}
+
+template <int M>
+__device__ __forceinline__ void right_row(double& a0, double& a1, double& a2, double e0, double e1, double tau) {
+    double t = __dmul_rn(a1, e0);
+    if (M == 3) t = __dadd_rn(t, __dmul_rn(a2, e1));
+    t = __dadd_rn(t, a0);
+    a0 = __dsub_rn(a0, __dmul_rn(tau, t));
+    const double tt = __dmul_rn(tau, t);
+    a1 = __dsub_rn(a1, __dmul_rn(e0, tt));
+    if (M == 3) a2 = __dsub_rn(a2, __dmul_rn(e1, tt));
+}
+
 template <class Qd, int M>
 __device__ __forceinline__ void house_left_small(const SMat& T, const Qd& Q, int r0, int c0, int c1, double e0,
                                                  double e1, double tau) {
     if (tau == 0.0) return;
     const double te0 = __dmul_rn(tau, e0), te1 = __dmul_rn(tau, e1);
+    constexpr int S = Qd::N;
     int j = c0 + Q.q;
-    for (; j + Qd::N < c1; j += 2 * Qd::N) {
-        const int j2 = j + Qd::N;
-        const double a0 = T(r0, j), a1 = T(r0 + 1, j), b0 = T(r0, j2), b1 = T(r0 + 1, j2);
-        const double a2 = M == 3 ? T(r0 + 2, j) : 0.0, b2 = M == 3 ? T(r0 + 2, j2) : 0.0;
-        double ta = __dmul_rn(e0, a1), tb = __dmul_rn(e0, b1);
-        if (M == 3) {
-            ta = __dadd_rn(ta, __dmul_rn(e1, a2));
-            tb = __dadd_rn(tb, __dmul_rn(e1, b2));
+    for (; j + 3 * S < c1; j += 4 * S) {
+        double a[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u][0] = T(r0, j + u * S);
+            a[u][1] = T(r0 + 1, j + u * S);
+            a[u][2] = M == 3 ? T(r0 + 2, j + u * S) : 0.0;
         }
-        ta = __dadd_rn(ta, a0);
-        tb = __dadd_rn(tb, b0);
-        T(r0, j) = __dsub_rn(a0, __dmul_rn(tau, ta));
-        T(r0, j2) = __dsub_rn(b0, __dmul_rn(tau, tb));
-        T(r0 + 1, j) = __dsub_rn(a1, __dmul_rn(ta, te0));
-        T(r0 + 1, j2) = __dsub_rn(b1, __dmul_rn(tb, te0));
-        if (M == 3) {
-            T(r0 + 2, j) = __dsub_rn(a2, __dmul_rn(ta, te1));
-            T(r0 + 2, j2) = __dsub_rn(b2, __dmul_rn(tb, te1));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) left_col<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau, te0, te1);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            T(r0, j + u * S) = a[u][0];
+            T(r0 + 1, j + u * S) = a[u][1];
+            if (M == 3) T(r0 + 2, j + u * S) = a[u][2];
         }
     }
-    if (j < c1) {
-        const double a0 = T(r0, j), a1 = T(r0 + 1, j), a2 = M == 3 ? T(r0 + 2, j) : 0.0;
-        double ta = __dmul_rn(e0, a1);
-        if (M == 3) ta = __dadd_rn(ta, __dmul_rn(e1, a2));
-        ta = __dadd_rn(ta, a0);
-        T(r0, j) = __dsub_rn(a0, __dmul_rn(tau, ta));
-        T(r0 + 1, j) = __dsub_rn(a1, __dmul_rn(ta, te0));
-        if (M == 3) T(r0 + 2, j) = __dsub_rn(a2, __dmul_rn(ta, te1));
+    for (; j < c1; j += S) {
+        double a0 = T(r0, j), a1 = T(r0 + 1, j), a2 = M == 3 ? T(r0 + 2, j) : 0.0;
+        left_col<M>(a0, a1, a2, e0, e1, tau, te0, te1);
+        T(r0, j) = a0;
+        T(r0 + 1, j) = a1;
+        if (M == 3) T(r0 + 2, j) = a2;
     }
 }
 
@@ -249,37 +279,31 @@ template <class Qd, int M>
 __device__ __forceinline__ void house_right_small(const SMat& T, const Qd& Q, int r0, int r1, int c0, double e0,
                                                   double e1, double tau) {
     if (tau == 0.0) return;
+    constexpr int S = Qd::N;
     int i = r0 + Q.q;
-    for (; i + Qd::N < r1; i += 2 * Qd::N) {
-        const int i2 = i + Qd::N;
-        const double a0 = T(i, c0), a1 = T(i, c0 + 1), b0 = T(i2, c0), b1 = T(i2, c0 + 1);
-        const double a2 = M == 3 ? T(i, c0 + 2) : 0.0, b2 = M == 3 ? T(i2, c0 + 2) : 0.0;
-        double ta = __dmul_rn(a1, e0), tb = __dmul_rn(b1, e0);
-        if (M == 3) {
-            ta = __dadd_rn(ta, __dmul_rn(a2, e1));
-            tb = __dadd_rn(tb, __dmul_rn(b2, e1));
+    for (; i + 3 * S < r1; i += 4 * S) {
+        double a[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u][0] = T(i + u * S, c0);
+            a[u][1] = T(i + u * S, c0 + 1);
+            a[u][2] = M == 3 ? T(i + u * S, c0 + 2) : 0.0;
         }
-        ta = __dadd_rn(ta, a0);
-        tb = __dadd_rn(tb, b0);
-        T(i, c0) = __dsub_rn(a0, __dmul_rn(tau, ta));
-        T(i2, c0) = __dsub_rn(b0, __dmul_rn(tau, tb));
-        const double tta = __dmul_rn(tau, ta), ttb = __dmul_rn(tau, tb);
-        T(i, c0 + 1) = __dsub_rn(a1, __dmul_rn(e0, tta));
-        T(i2, c0 + 1) = __dsub_rn(b1, __dmul_rn(e0, ttb));
-        if (M == 3) {
-            T(i, c0 + 2) = __dsub_rn(a2, __dmul_rn(e1, tta));
-            T(i2, c0 + 2) = __dsub_rn(b2, __dmul_rn(e1, ttb));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) right_row<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            T(i + u * S, c0) = a[u][0];
+            T(i + u * S, c0 + 1) = a[u][1];
+            if (M == 3) T(i + u * S, c0 + 2) = a[u][2];
         }
     }
-    if (i < r1) {
-        const double a0 = T(i, c0), a1 = T(i, c0 + 1), a2 = M == 3 ? T(i, c0 + 2) : 0.0;
-        double ta = __dmul_rn(a1, e0);
-        if (M == 3) ta = __dadd_rn(ta, __dmul_rn(a2, e1));
-        ta = __dadd_rn(ta, a0);
-        T(i, c0) = __dsub_rn(a0, __dmul_rn(tau, ta));
-        const double tta = __dmul_rn(tau, ta);
-        T(i, c0 + 1) = __dsub_rn(a1, __dmul_rn(e0, tta));
-        if (M == 3) T(i, c0 + 2) = __dsub_rn(a2, __dmul_rn(e1, tta));
+    for (; i < r1; i += S) {
+        double a0 = T(i, c0), a1 = T(i, c0 + 1), a2 = M == 3 ? T(i, c0 + 2) : 0.0;
+        right_row<M>(a0, a1, a2, e0, e1, tau);
+        T(i, c0) = a0;
+        T(i, c0 + 1) = a1;
+        if (M == 3) T(i, c0 + 2) = a2;
     }
 }
 

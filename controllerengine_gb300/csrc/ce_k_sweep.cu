@@ -17,6 +17,7 @@
 // size (zero padding inside the class is exact: padded rows are decoupled
 // z*I rows whose right-hand side is zero).
 #include <cfloat>
+#include <climits>
 
 #include "ce_device.cuh"
 #include "ce_host.h"
@@ -37,14 +38,14 @@ __device__ __forceinline__ double rlogf_(double x) { return log(x); }
 __device__ __forceinline__ float rsqrtf_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double rsqrtf_(double x) { return sqrt(x); }
 
-// fgrid row per frequency: z.re, z.im, arg z, P.re, P.im, |P|, ok, 0
-template <typename R, int NSC>
-__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const float* __restrict__ gains,
-                                                       const float* __restrict__ lina, const int* __restrict__ nominal,
-                                                       const R* __restrict__ fgrid, float* __restrict__ info) {
-    __shared__ R As[NSC * NSC][SWEEP_BLOCK];
-    const int tid = threadIdx.x;
-    const int64_t c = (int64_t)blockIdx.x * SWEEP_BLOCK + tid;
+// Candidates that skip the sweep get their outputs here: flagged by the
+// modal stage (zero margins), or a nominal closed loop that is not stable
+// (the unstable penalty).  The rest are listed for k_sweep, so its warps hold
+// only candidates that run the frequency loop.
+__global__ void __launch_bounds__(128) k_sweep_select(const Run run, const int* __restrict__ nominal,
+                                                      float* __restrict__ info, int* __restrict__ list,
+                                                      int* __restrict__ count) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
     if (c >= run.n) return;
     float* out = info + c * (int64_t)run.info_w;
     float* sc = out + run.info_scoring;
@@ -65,6 +66,37 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
         sc[0] = isfinite(total) ? total : EIGF;
         return;
     }
+    list[atomicAdd(count, 1)] = (int)c;
+}
+
+// The sweep in two passes.  k_sweep_resp: one thread per (listed candidate,
+// group of SWEEP_FG frequencies) solves the complex LU of every frequency of
+// its group and stores |P G| and arg(P G) (layout [w][candidate]), the
+// minimum of the b(w) terms and the first frequency that fails (no plant
+// response or a non-finite solve).  k_sweep_scan: one thread per listed
+// candidate walks the frequencies in order for the phase unwrap, the
+// crossovers and the margins (ref: src/allmargin.cu:100-181).  Each value is
+// computed with the same operations as in one sequential loop; the minimum
+// is exact in any order, and the frequencies after the first failure, which
+// the sequential loop never reaches, only feed values that the failure path
+// discards.
+
+// fgrid row per frequency: z.re, z.im, arg z, P.re, P.im, |P|, ok, 0
+template <typename R, int NSC>
+__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const float* __restrict__ gains,
+                                                            const float* __restrict__ lina,
+                                                            const int* __restrict__ list, const int* __restrict__ count,
+                                                            const R* __restrict__ fgrid, R* __restrict__ mag,
+                                                            R* __restrict__ arg, R* __restrict__ bpc,
+                                                            int* __restrict__ fail) {
+    __shared__ R As[NSC * NSC][SWEEP_BLOCK];
+    const int tid = threadIdx.x;
+    const int64_t idx = (int64_t)blockIdx.x * SWEEP_BLOCK + tid;
+    const int64_t listed = *count;
+    if (idx >= listed) return;
+    const int g = blockIdx.y;
+    const int w0 = g * SWEEP_FG, w1 = min(run.freq, w0 + SWEEP_FG);
+    const int64_t c = list[idx];
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
     const float* la = lina + c * (int64_t)(nt * nt);
@@ -76,16 +108,13 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
 #pragma unroll
         for (int j = 0; j < NSC; ++j) As[i * NSC + j][tid] = (i < ns && j < ns) ? R(la[i * nt + j]) : R(0);
     }
-    const R PI = pi_<R>(), TWO_PI = rmul(R(2), PI), R2D = rdiv(R(180), PI), D2R = rdiv(PI, R(180));
-    const R TS = R(run.ts);
     const R ALPHA = sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64);
-    R PM = R(FLT_MAX), GM = R(FLT_MAX), DM = R(FLT_MAX), BPC = R(1);
-    bool gain_crossed = false, ok = true;
-    R prevMag = R(0), prevPhase = R(0), prevRaw = R(0), prevTheta = R(0);
-    for (int w = 0; w < run.freq; ++w) {
+    R bmin = R(1);
+    int first_bad = INT_MAX;
+    for (int w = w0; w < w1; ++w) {
         const R* fg = fgrid + 8 * (int64_t)w;
         if (fg[6] == R(0)) {
-            ok = false;
+            first_bad = w;
             break;
         }
         const cplx<R> z{fg[0], fg[1]};
@@ -95,7 +124,7 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
 #pragma unroll
         for (int i = 0; i < NSC; ++i) fin = fin && cfinite(x[i]);
         if (!fin) {
-            ok = false;
+            first_bad = w;
             break;
         }
         cplx<R> G{R(0), R(0)};
@@ -107,15 +136,55 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
         G.re = radd(G.re, R(0));
         const cplx<R> P{fg[3], fg[4]};
         const cplx<R> resp = cmul(P, G);
-        const R m = cabs_(resp);
-        const R raw = carg_(resp);
-        const R theta = fg[2];
-        {
-            const R Ps = rmul(ALPHA, fg[5]), Cs = rdiv(cabs_(G), ALPHA);
-            const R num = cabs_(cplx<R>{radd(R(1), resp.re), resp.im});
-            const R den = rmul(rsqrtf_(radd(R(1), rmul(Ps, Ps))), rsqrtf_(radd(R(1), rmul(Cs, Cs))));
-            BPC = fmin(BPC, rdiv(num, den));
-        }
+        mag[(int64_t)w * listed + idx] = cabs_(resp);
+        arg[(int64_t)w * listed + idx] = carg_(resp);
+        const R Ps = rmul(ALPHA, fg[5]), Cs = rdiv(cabs_(G), ALPHA);
+        const R num = cabs_(cplx<R>{radd(R(1), resp.re), resp.im});
+        const R den = rmul(rsqrtf_(radd(R(1), rmul(Ps, Ps))), rsqrtf_(radd(R(1), rmul(Cs, Cs))));
+        bmin = fmin(bmin, rdiv(num, den));
+    }
+    bpc[(int64_t)g * listed + idx] = bmin;
+    fail[(int64_t)g * listed + idx] = first_bad;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_sweep_scan(const Run run, const int* __restrict__ list,
+                                                    const int* __restrict__ count, const R* __restrict__ fgrid,
+                                                    const R* __restrict__ mag, const R* __restrict__ arg,
+                                                    const R* __restrict__ bpc, const int* __restrict__ fail,
+                                                    float* __restrict__ info) {
+    const int64_t idx = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    const int64_t listed = *count;
+    if (idx >= listed) return;
+    const int64_t c = list[idx];
+    float* out = info + c * (int64_t)run.info_w;
+    float* sc = out + run.info_scoring;
+    float* am = out + run.info_allmargin;
+    const float sc0 = sc[0];
+    const float EIGF = run.eig_fail_err;
+    const int groups = (run.freq + SWEEP_FG - 1) / SWEEP_FG;
+    int first_bad = INT_MAX;
+    R BPC = R(1);
+    for (int g = 0; g < groups; ++g) {
+        first_bad = min(first_bad, fail[(int64_t)g * listed + idx]);
+        BPC = fmin(BPC, bpc[(int64_t)g * listed + idx]);
+    }
+    if (first_bad < run.freq) {
+        sc[1] = sc0;
+        sc[2] = EIGF;
+        sc[0] = EIGF;
+        am[0] = 0.0f; am[1] = 0.0f; am[2] = 0.0f; am[3] = 1.0f; am[4] = 0.0f;
+        return;
+    }
+    const R PI = pi_<R>(), TWO_PI = rmul(R(2), PI), R2D = rdiv(R(180), PI), D2R = rdiv(PI, R(180));
+    const R TS = R(run.ts);
+    R PM = R(FLT_MAX), GM = R(FLT_MAX), DM = R(FLT_MAX);
+    bool gain_crossed = false;
+    R prevMag = R(0), prevPhase = R(0), prevRaw = R(0), prevTheta = R(0);
+    for (int w = 0; w < run.freq; ++w) {
+        const R m = mag[(int64_t)w * listed + idx];
+        const R raw = arg[(int64_t)w * listed + idx];
+        const R theta = fgrid[8 * (int64_t)w + 2];
         if (w > 0) {
             R delta = rsub(raw, prevRaw);
             if (delta > PI) delta = rsub(delta, TWO_PI);
@@ -152,13 +221,6 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
         prevRaw = raw;
         prevTheta = theta;
     }
-    if (!ok) {
-        sc[1] = sc0;
-        sc[2] = EIGF;
-        sc[0] = EIGF;
-        am[0] = 0.0f; am[1] = 0.0f; am[2] = 0.0f; am[3] = 1.0f; am[4] = 0.0f;
-        return;
-    }
     const R TGM = R(run.target_gm), TPM = R(run.target_pm), TB = R(run.target_b);
     const R egm = rdiv(fmax(R(0), rsub(TGM, GM)), TGM);
     const R epm = gain_crossed ? rdiv(fmax(R(0), rsub(TPM, PM)), TPM) : R(0);
@@ -177,27 +239,37 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep(const Run run, const floa
 }
 
 template <typename R>
-static void sweep_dispatch(const Run& run, const float* gains, const float* lina, const int* nominal, const R* fgrid,
-                           float* info, cudaStream_t st) {
-    const int grid = (int)((run.n + SWEEP_BLOCK - 1) / SWEEP_BLOCK);
+static void sweep_dispatch(const Run& run, const float* gains, const float* lina, const int* list, const int* count,
+                           const R* fgrid, float* info, const SweepScratch& sw, cudaStream_t st) {
+    // the listed count is only known on the device: grids cover all n
+    const dim3 grid((unsigned)((run.n + SWEEP_BLOCK - 1) / SWEEP_BLOCK), (unsigned)((run.freq + SWEEP_FG - 1) / SWEEP_FG));
+    R* mag = (R*)sw.mag;
+    R* arg = (R*)sw.arg;
+    R* bpc = (R*)sw.bpc;
     if (run.ns <= 2) {
-        prefer_shared((const void*)k_sweep<R, 2>);
-        k_sweep<R, 2><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+        prefer_shared((const void*)k_sweep_resp<R, 2>);
+        k_sweep_resp<R, 2><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, list, count, fgrid, mag, arg, bpc, sw.fail);
     } else if (run.ns <= 4) {
-        prefer_shared((const void*)k_sweep<R, 4>);
-        k_sweep<R, 4><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+        prefer_shared((const void*)k_sweep_resp<R, 4>);
+        k_sweep_resp<R, 4><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, list, count, fgrid, mag, arg, bpc, sw.fail);
     } else {
-        prefer_shared((const void*)k_sweep<R, 8>);
-        k_sweep<R, 8><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, nominal, fgrid, info);
+        prefer_shared((const void*)k_sweep_resp<R, 8>);
+        k_sweep_resp<R, 8><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, list, count, fgrid, mag, arg, bpc, sw.fail);
     }
+    prefer_shared((const void*)k_sweep_scan<R>);
+    k_sweep_scan<R><<<(unsigned)((run.n + 127) / 128), 128, 0, st>>>(run, list, count, fgrid, mag, arg, bpc, sw.fail,
+                                                                     info);
 }
 
 void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
-                  const void* fgrid, float* info, cudaStream_t st) {
+                  const void* fgrid, float* info, int* list, int* count, const SweepScratch& sw, cudaStream_t st) {
+    CE_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
+    prefer_shared((const void*)k_sweep_select);
+    k_sweep_select<<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, nominal, info, list, count);
     if (precision == CE_PRECISION_FP64)
-        sweep_dispatch<double>(run, gains, lina, nominal, (const double*)fgrid, info, st);
+        sweep_dispatch<double>(run, gains, lina, list, count, (const double*)fgrid, info, sw, st);
     else
-        sweep_dispatch<float>(run, gains, lina, nominal, (const float*)fgrid, info, st);
+        sweep_dispatch<float>(run, gains, lina, list, count, (const float*)fgrid, info, sw, st);
     CE_CUDA(cudaGetLastError());
 }
 

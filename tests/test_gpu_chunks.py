@@ -18,7 +18,7 @@ def test_chunked_batch_equals_separate_calls():
     with Session(cfg, prob.plant) as s:
         l0 = s.kernel_launches
         whole = s.evaluate(prob.cuda_mx, prob.info_mx)
-        assert s.kernel_launches - l0 > 7  # the batch was cut into chunks
+        assert s.kernel_launches - l0 > 9  # the batch was cut into chunks
         parts = [s.evaluate(prob.cuda_mx[k:k + 16384], prob.info_mx[k:k + 16384]) for k in range(0, 49152, 16384)]
     sep = np.vstack(parts)
     bad = np.flatnonzero(whole.view(np.uint32) != sep.view(np.uint32))

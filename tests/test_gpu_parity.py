@@ -54,7 +54,7 @@ def _stagewise(problem, oracle_mod):
     with ce.Session(cfg, problem.plant) as s:
         info, d = s.evaluate_diagnostics(problem.cuda_mx, problem.info_mx)
         launches = s.kernel_launches
-    assert launches == 7  # lina+eig, sim, fit classes, fit, modal, nominal, sweep
+    assert launches == 9  # lina+eig, sim, fit classes, fit, modal, nominal, sweep selection, LU pass, scan
     orc = oracle_mod.Oracle(problem.config_text, problem.plant)
     g = problem.cuda_mx
 
