@@ -158,6 +158,29 @@ __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, i
                 T(r0 + 1 + k, j + u * S) = __dsub_rn(T(r0 + 1 + k, j + u * S), __dmul_rn(t[u], te));
         }
     }
+    if (j + S < c1) {
+        double t[2];
+        const double e = ess_at(0);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) t[u] = __dmul_rn(e, T(r0 + 1, j + u * S));
+        for (int k = 1; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(ek, T(r0 + 1 + k, j + u * S)));
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            t[u] = __dadd_rn(t[u], T(r0, j + u * S));
+            T(r0, j + u * S) = __dsub_rn(T(r0, j + u * S), __dmul_rn(tau, t[u]));
+        }
+        for (int k = 0; k < m - 1; ++k) {
+            const double te = __dmul_rn(tau, ess_at(k));
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                T(r0 + 1 + k, j + u * S) = __dsub_rn(T(r0 + 1 + k, j + u * S), __dmul_rn(t[u], te));
+        }
+        j += 2 * S;
+    }
     for (; j < c1; j += S) {
         double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
@@ -205,6 +228,31 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
                 T(i + u * S, c0 + 1 + k) = __dsub_rn(T(i + u * S, c0 + 1 + k), __dmul_rn(ek, tt[u]));
         }
     }
+    if (i + S < r1) {
+        double t[2];
+        const double e = ess_at(0);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) t[u] = __dmul_rn(T(i + u * S, c0 + 1), e);
+        for (int k = 1; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(T(i + u * S, c0 + 1 + k), ek));
+        }
+        double tt[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            t[u] = __dadd_rn(t[u], T(i + u * S, c0));
+            T(i + u * S, c0) = __dsub_rn(T(i + u * S, c0), __dmul_rn(tau, t[u]));
+            tt[u] = __dmul_rn(tau, t[u]);
+        }
+        for (int k = 0; k < m - 1; ++k) {
+            const double ek = ess_at(k);
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                T(i + u * S, c0 + 1 + k) = __dsub_rn(T(i + u * S, c0 + 1 + k), __dmul_rn(ek, tt[u]));
+        }
+        i += 2 * S;
+    }
     for (; i < r1; i += S) {
         double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
         for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
@@ -217,9 +265,9 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
 
 // The Francis-step reflectors (m = 3, and m = 2 for the last one) with the
 // essential part in registers; same per-column / per-row operations as above.
-// Four columns (rows) per iteration: the work per element is a short chain of
-// dependent FP64 operations, and four independent chains per lane hide most
-// of their latency.
+// Several columns (rows) per step: the work per element is a short chain of
+// dependent FP64 operations, and independent chains per lane hide most of
+// their latency.
 template <int M>
 __device__ __forceinline__ void left_col(double& a0, double& a1, double& a2, double e0, double e1, double tau,
                                          double te0, double te1) {
@@ -242,6 +290,48 @@ __device__ __forceinline__ void right_row(double& a0, double& a1, double& a2, do
     if (M == 3) a2 = __dsub_rn(a2, __dmul_rn(e1, tt));
 }
 
+// U columns j, j+S, .., j+(U-1)S of the left reflector.
+template <int M, int U, int S>
+__device__ __forceinline__ void left_cols(const SMat& T, int r0, int j, double e0, double e1, double tau, double te0,
+                                          double te1) {
+    double a[U][3];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        a[u][0] = T(r0, j + u * S);
+        a[u][1] = T(r0 + 1, j + u * S);
+        a[u][2] = M == 3 ? T(r0 + 2, j + u * S) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) left_col<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau, te0, te1);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        T(r0, j + u * S) = a[u][0];
+        T(r0 + 1, j + u * S) = a[u][1];
+        if (M == 3) T(r0 + 2, j + u * S) = a[u][2];
+    }
+}
+
+// U rows i, i+S, .., i+(U-1)S of the right reflector.
+template <int M, int U, int S>
+__device__ __forceinline__ void right_rows(const SMat& T, int i, int c0, double e0, double e1, double tau) {
+    double a[U][3];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        a[u][0] = T(i + u * S, c0);
+        a[u][1] = T(i + u * S, c0 + 1);
+        a[u][2] = M == 3 ? T(i + u * S, c0 + 2) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) right_row<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        T(i + u * S, c0) = a[u][0];
+        T(i + u * S, c0 + 1) = a[u][1];
+        if (M == 3) T(i + u * S, c0 + 2) = a[u][2];
+    }
+}
+
+// Columns (rows) go four at a time, then a pair, then one.
 template <class Qd, int M>
 __device__ __forceinline__ void house_left_small(const SMat& T, const Qd& Q, int r0, int c0, int c1, double e0,
                                                  double e1, double tau) {
@@ -249,30 +339,12 @@ __device__ __forceinline__ void house_left_small(const SMat& T, const Qd& Q, int
     const double te0 = __dmul_rn(tau, e0), te1 = __dmul_rn(tau, e1);
     constexpr int S = Qd::N;
     int j = c0 + Q.q;
-    for (; j + 3 * S < c1; j += 4 * S) {
-        double a[4][3];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            a[u][0] = T(r0, j + u * S);
-            a[u][1] = T(r0 + 1, j + u * S);
-            a[u][2] = M == 3 ? T(r0 + 2, j + u * S) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) left_col<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau, te0, te1);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            T(r0, j + u * S) = a[u][0];
-            T(r0 + 1, j + u * S) = a[u][1];
-            if (M == 3) T(r0 + 2, j + u * S) = a[u][2];
-        }
+    for (; j + 3 * S < c1; j += 4 * S) left_cols<M, 4, S>(T, r0, j, e0, e1, tau, te0, te1);
+    if (j + S < c1) {
+        left_cols<M, 2, S>(T, r0, j, e0, e1, tau, te0, te1);
+        j += 2 * S;
     }
-    for (; j < c1; j += S) {
-        double a0 = T(r0, j), a1 = T(r0 + 1, j), a2 = M == 3 ? T(r0 + 2, j) : 0.0;
-        left_col<M>(a0, a1, a2, e0, e1, tau, te0, te1);
-        T(r0, j) = a0;
-        T(r0 + 1, j) = a1;
-        if (M == 3) T(r0 + 2, j) = a2;
-    }
+    if (j < c1) left_cols<M, 1, S>(T, r0, j, e0, e1, tau, te0, te1);
 }
 
 template <class Qd, int M>
@@ -281,30 +353,12 @@ __device__ __forceinline__ void house_right_small(const SMat& T, const Qd& Q, in
     if (tau == 0.0) return;
     constexpr int S = Qd::N;
     int i = r0 + Q.q;
-    for (; i + 3 * S < r1; i += 4 * S) {
-        double a[4][3];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            a[u][0] = T(i + u * S, c0);
-            a[u][1] = T(i + u * S, c0 + 1);
-            a[u][2] = M == 3 ? T(i + u * S, c0 + 2) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) right_row<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            T(i + u * S, c0) = a[u][0];
-            T(i + u * S, c0 + 1) = a[u][1];
-            if (M == 3) T(i + u * S, c0 + 2) = a[u][2];
-        }
+    for (; i + 3 * S < r1; i += 4 * S) right_rows<M, 4, S>(T, i, c0, e0, e1, tau);
+    if (i + S < r1) {
+        right_rows<M, 2, S>(T, i, c0, e0, e1, tau);
+        i += 2 * S;
     }
-    for (; i < r1; i += S) {
-        double a0 = T(i, c0), a1 = T(i, c0 + 1), a2 = M == 3 ? T(i, c0 + 2) : 0.0;
-        right_row<M>(a0, a1, a2, e0, e1, tau);
-        T(i, c0) = a0;
-        T(i, c0 + 1) = a1;
-        if (M == 3) T(i, c0 + 2) = a2;
-    }
+    if (i < r1) right_rows<M, 1, S>(T, i, c0, e0, e1, tau);
 }
 
 // Givens rotation (c, s) with [c -s; s c] [p; q] = [r; 0].
