@@ -52,9 +52,22 @@ def fit_ops(eigen, steps):
     dup = np.zeros(re.shape, bool)
     dup[:, 1:] = (re[:, 1:] == re[:, :-1]) & (np.abs(im[:, 1:]) == np.abs(im[:, :-1]))
     unique = re.shape[1] - dup.sum(1)
-    stable = np.hypot(re, im).max(1) <= 1.0
+    stable = modal_stable(eigen)
     nc = 2 * unique[stable]
     return float(steps * (nc * (nc + 1) // 2 + nc + 5 * unique[stable]).sum())
+
+
+def modal_stable(eigen):
+    """Candidates whose LIN_A eigenvalues all satisfy |lambda| <= 1 (the ones the fit
+    models and the nominal closed loop is solved for)."""
+    return np.hypot(eigen[..., 0].astype(np.float64), eigen[..., 1].astype(np.float64)).max(1) <= 1.0
+
+
+def eig_flops(n):
+    """Eigenvalues of a real n x n matrix by Householder-Hessenberg reduction and
+    Francis double-shift QR: 10 n^3 flops (Golub and Van Loan, Matrix
+    Computations, 4th ed., table 7.5.2)."""
+    return 10 * n ** 3
 
 
 def sim_ops_per_step(ns, nd, nw, n_instr):
@@ -214,8 +227,10 @@ def main():
 
     # eigenvalues of every candidate (untimed): the fit's work depends on the mode count
     _, diag = sess.evaluate_diagnostics(problem.cuda_mx, problem.info_mx, want=("eigen",))
-    fit_work = fit_ops(diag["eigen"].reshape(n, cfg.total_dim, 2), cfg.fit_steps)
-    del diag
+    eig_all = diag["eigen"].reshape(n, cfg.total_dim, 2)
+    fit_work = fit_ops(eig_all, cfg.fit_steps)
+    n_listed = int(modal_stable(eig_all).sum())
+    del diag, eig_all
 
     for _ in range(a.warmup):
         flush.zero_()
@@ -311,14 +326,21 @@ def main():
             "fit": ("k_fit<float>", fit_work,
                     f"normal-equation FMAs + 5 basis ops per mode-step, {cfg.fit_steps} window steps, "
                     f"summed over the stable candidates ({fit_work / 1e9:.2f} G ops)")}
+    nt, n2 = cfg.total_dim, 2 * cfg.statespace_dim
+    work64 = {"lina_eig": ("k_lina_eig<2>", eig_flops(nt) * n,
+                           f"10 n^3 flops of a {nt}x{nt} real eigensolve x {n} candidates"),
+              "nominal": ("k_nominal<2>", eig_flops(n2) * n_listed,
+                          f"10 n^3 flops of a {n2}x{n2} real eigensolve x {n_listed} listed candidates")}
+    src64 = "measured FP64 DFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"
     rooflines = {}
-    for st, (kname, ops, desc) in work.items():
-        ach = ops / (per_step[st] * 1e-3) / 1e12 if per_step.get(st) else None
-        rooflines[st] = {"kernel": kname, "bound": "fp32", "achieved": ach, "peak": peak, "unit": "Tops/s",
-                         "frac": ach / peak if ach else None, "traffic": None, "work_per_launch": desc,
-                         "peak_source": src}
-    roof = rooflines.get(dom) or {"kernel": dom, "bound": "fp64" if dom in ("lina_eig", "nominal") else "fp32",
-                                  "achieved": None, "peak": None, "unit": "Tops/s", "frac": None, "traffic": None}
+    for group, bound, pk, sname in ((work, "fp32", peak, src), (work64, "fp64", fp64_rate / 1e12, src64)):
+        for st, (kname, ops, desc) in group.items():
+            ach = ops / (per_step[st] * 1e-3) / 1e12 if per_step.get(st) else None
+            rooflines[st] = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "Tops/s",
+                             "frac": ach / pk if ach else None, "traffic": None, "work_per_launch": desc,
+                             "peak_source": sname}
+    roof = rooflines.get(dom) or {"kernel": dom, "bound": "fp32", "achieved": None, "peak": None, "unit": "Tops/s",
+                                  "frac": None, "traffic": None}
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text())["hbm_gbs"] if peaks_file.exists() else 6800.0
     win_bytes = n * cfg.fit_steps * 4 * 2  # fit window written by k_sim and read by k_fit
