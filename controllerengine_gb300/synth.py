@@ -225,3 +225,96 @@ def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 40
         crossover_coeff=1.0, target_gm=9.0, target_pm=55.0, target_b=0.2, eig_fail_err=1.0e18, unstable_err=1.0e6,
         freq=freq, freq_min=0.1)
     return Problem("eight_state", text, plant, gains, info)
+
+
+def stable_matrix(rng, n: int, rmin=0.85, rmax=0.995, thmin=0.01, thmax=0.5) -> np.ndarray:
+    """Real n x n matrix with floor(n/2) complex pole pairs and, for odd n, one real pole, all of
+    modulus in [rmin, rmax], in a Haar-random orthogonal basis."""
+    blocks = np.zeros((n, n))
+    for p in range(n // 2):
+        r, th = rng.uniform(rmin, rmax), rng.uniform(thmin, thmax)
+        blocks[2 * p:2 * p + 2, 2 * p:2 * p + 2] = r * np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+    if n % 2:
+        blocks[n - 1, n - 1] = rng.uniform(rmin, rmax)
+    Q, R = np.linalg.qr(rng.standard_normal((n, n)))
+    Q = Q * np.sign(np.diag(R))
+    return Q @ blocks @ Q.T
+
+
+def random_shape(seed: int, n: int = 256, time: int | None = None, freq: int | None = None) -> Problem:
+    """One instance of the uneven-shape workload: statespace and discrete dimensions U{2..8},
+    0-4 nonlinear terms with 1-8 instructions each (no-op and SKIP rows included), horizon
+    log-uniform in [1e3, 2e4] steps and 50-400 sweep points unless given.  The observer model
+    (ns states) is a separately drawn stable system with y = z_0; the plant (nd states) is drawn
+    the same way; K is an LQR gain and L a steady-state Kalman predictor gain of the model, both
+    from seeded weights and scaled per candidate, so the batch holds stable and unstable loops."""
+    rng = np.random.default_rng(seed)
+    ns, nd, nw = int(rng.integers(2, 9)), int(rng.integers(2, 9)), int(rng.integers(0, 5))
+    if time is None:
+        time = int(np.exp(rng.uniform(np.log(1e3), np.log(2e4))))
+    if freq is None:
+        freq = int(rng.integers(50, 401))
+    ts = 1e-3
+    # observer model in output-first coordinates
+    Am, Bm, Cm = output_first_basis(stable_matrix(rng, ns), rng.standard_normal((ns, 1)), rng.standard_normal(ns))
+    e0s = np.zeros(ns)
+    e0s[0] = 1.0
+    Ap, Bp, _ = output_first_basis(stable_matrix(rng, nd), rng.standard_normal((nd, 1)), rng.standard_normal(nd))
+    e0d = np.zeros(nd)
+    e0d[0] = 1.0
+    Bw = 1e-3 * rng.standard_normal((nd, nw))
+    # BASE_PARAMS: 1 one, 2 small coefficient, 3 -r, 4 r, 5 umin, 6 umax, 7 second coefficient
+    c1, c2, r = rng.uniform(0.01, 0.5), rng.uniform(-0.5, 0.5), rng.uniform(0.2, 2.0)
+    bp = np.array([1.0, c1, -r, r, -5.0, 5.0, c2], F32)
+    dc_chain = [(MUL, 0, STATE, 1)]
+    if rng.random() < 0.5:
+        dc_chain.append((7, 0, STATE, STATE))  # an op outside 1..6: no change
+    u_chain = [(SAT, 0, 5, 6)]
+    nl_rows, nl_counts = [], []
+    for _ in range(nw):
+        i, j = int(rng.integers(0, nd)), int(rng.integers(0, nd + 1))  # j == nd reads the plant output
+        kind = int(rng.integers(0, 4))
+        if kind == 0:
+            ch = [(MUL, i, STATE, STATE), (MUL, i, PREV, STATE), (MUL, i, PREV, 2)]
+        elif kind == 1:
+            ch = [(SGN, j, STATE, STATE), (MUL, j, PREV, 2)]
+        elif kind == 2:
+            ch = [(SAT, i, 3, 4), (SUB, i, PREV, STATE)]
+        else:
+            ch = [(MUL, j, STATE, 7), (ADD, i, PREV, STATE), (DIV, i, PREV, 1)]
+        while len(ch) < 8 and rng.random() < 0.3:
+            ch.insert(int(rng.integers(0, len(ch) + 1)), (0, int(rng.integers(0, nd + 1)), 0, 0))  # SKIP row
+        rows = instr_rows(ch, nd + 1)
+        nl_rows.append(rows)
+        nl_counts.append(len(ch))
+    nl = np.vstack(nl_rows) if nl_rows else np.zeros((0, nd + 1), np.int32)
+    Amf, Bmf, Apf, Bpf = Am.astype(F32), Bm[:, 0].astype(F32), Ap.astype(F32), Bp[:, 0].astype(F32)
+    plant = PlantFiles(
+        statespace_a=Amf, statespace_a_i=Amf - np.eye(ns, dtype=F32), statespace_b=Bmf,
+        statespace_c=e0s.astype(F32), statespace_d=np.zeros(1, F32), discrete_a=Apf,
+        discrete_a_i=Apf - np.eye(nd, dtype=F32), discrete_bu=Bpf, discrete_bw=Bw.astype(F32),
+        discrete_c=e0d.astype(F32), base_params=bp, dc_info=instr_rows(dc_chain, nd),
+        u_info=instr_rows(u_chain, ns), nl_info=nl)
+    Qk = np.diag(np.exp(rng.uniform(np.log(1e-2), np.log(1e1), ns)))
+    Rk = np.array([[np.exp(rng.uniform(np.log(1e-1), np.log(1e1)))]])
+    P = solve_discrete_are(Am, Bm, Qk, Rk)
+    K0 = np.linalg.solve(Rk + Bm.T @ P @ Bm, Bm.T @ P @ Am).reshape(ns)
+    Qo = np.diag(np.exp(rng.uniform(np.log(1e-3), np.log(1e0), ns)))
+    S = solve_discrete_are(Am.T, e0s.reshape(ns, 1), Qo, np.array([[0.1]]))
+    L0 = (Am @ S @ e0s / (e0s @ S @ e0s + 0.1)).reshape(ns)
+    K = K0[None] * np.exp(rng.uniform(np.log(0.2), np.log(5.0), (n, 1)))
+    L = L0[None] * np.exp(rng.uniform(np.log(0.5), np.log(2.0), (n, 1)))
+    Nn = np.exp(rng.uniform(np.log(0.5), np.log(2.0), (n, 1)))
+    gains = np.hstack([K, L, Nn]).astype(F32)
+    input_size = 2 * ns + 1
+    info = np.zeros((n, info_width(ns, nd, input_size)), F32)
+    info[:, :input_size] = gains
+    text = _config_text(
+        statespace_dim=ns, discrete_dim=nd, nonlin_dim=nw, n_params=len(bp), input_size=input_size,
+        dc_instructions=len(dc_chain), u_instructions=len(u_chain), nl_instructions=nl_counts,
+        n_cores=128 * max(1, -(-n // 1536)), n_rounds=1, mode="batch", time=time, duration=time * ts,
+        ref_step_time=0.05, ref_amplitude=1.0, fit_start=0.05, fit_end=0.75, steady_start=0.75,
+        bandwidth=float(np.exp(rng.uniform(np.log(0.5), np.log(20.0)))), damping=0.6, overshoot=0.10,
+        steady_state_error=0.05, crossover_coeff=1.0, target_gm=6.0, target_pm=45.0, target_b=0.2,
+        eig_fail_err=1.0e18, unstable_err=1.0e6, freq=freq, freq_min=0.1)
+    return Problem(f"random_shape_{seed}", text, plant, gains, info)
