@@ -26,8 +26,10 @@ EXPORTED_SYMBOLS = (
     "ce_evaluate", "ce_evaluate_diagnostics", "ce_evaluate_device", "ce_session_kernel_launches",
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
-    "RunControllerEngine",
+    "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
+    "ce_server_reset_stats", "RunControllerEngine",
 )
+PENDING = 2
 SIM_TABLE, SIM_SPECIALISED = 0, 1
 NUM_STAGES = 6
 STAGE_NAMES = ("lina_eig", "sim", "fit", "modal", "nominal", "sweep")
@@ -81,6 +83,17 @@ class ce_diagnostics(C.Structure):
     _fields_ = [(n, _FP) for n in ("yplant", "lina", "eigen", "ata", "atb")]
 
 
+class ce_server_options(C.Structure):
+    _fields_ = [("max_batch", C.c_int32), ("lanes", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+                ("max_wait_us", C.c_int32)]
+
+
+class ce_server_stats(C.Structure):
+    _fields_ = [("capacity", C.c_int64), ("lanes", C.c_int32), ("completed", C.c_int64), ("batches", C.c_int64),
+                ("batched_candidates", C.c_int64), ("queued", C.c_int64), ("latency_p50_ms", C.c_double),
+                ("latency_p99_ms", C.c_double), ("latency_max_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -116,6 +129,15 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_session_sim_log.argtypes = [C.c_void_p]
     lib.ce_session_sim_log.restype = C.c_char_p
     lib.ce_sim_specialised_source.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]
+    lib.ce_server_create.argtypes = [C.POINTER(ce_config), C.POINTER(ce_plant), C.c_int32,
+                                     C.POINTER(ce_server_options), C.POINTER(C.c_void_p)]
+    lib.ce_server_destroy.argtypes = [C.c_void_p]
+    lib.ce_server_destroy.restype = None
+    lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_int64)]
+    lib.ce_server_wait.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
+    lib.ce_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ce_server_stats)]
+    lib.ce_server_reset_stats.argtypes = [C.c_void_p]
     lib.ce_session_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.ce_session_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.ce_measure_fma_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]

@@ -1,0 +1,409 @@
+// ce_server.cpp -- the serving front end: requests of any size, continuous
+// batching onto a few concurrent evaluations, HBM-footprint admission.
+//
+// The reference serves one caller at a time: RunControllerEngine reads a
+// fixed-size round from files, runs it synchronously and returns
+// (ref: src/main.cu:467-582, 592-602).  A server here keeps `lanes` sessions of
+// the same configuration (each with its own device scratch and streams) and a
+// scheduler thread.  Requests (gains and INFO rows in host memory) queue in
+// arrival order; when a lane is free the scheduler packs the oldest request's
+// plant with the requests behind it that use the same plant, up to the lane's
+// capacity (a request larger than that is served in pieces), copies their
+// rows into the lane's pinned staging buffers, and enqueues H2D, the
+// evaluation and D2H on the lane's stream.  While one lane's batch is on the
+// GPU the next is staged, and batches of different lanes run concurrently.
+// Each candidate's row is computed independently of the batch it lands in, so
+// a request's result does not depend on what it was batched with.
+//
+// Admission: the lane capacity (candidates per batch) is the largest that
+// fits `lanes` x (session scratch + batch buffers) into the HBM budget; the
+// per-candidate footprint is derived from the configuration.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "ce_host.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    int64_t id = 0;
+    int plant = 0;
+    int64_t n = 0;
+    const float* gains = nullptr;
+    const float* info_in = nullptr;
+    float* info_out = nullptr;
+    int64_t next = 0;      // first row not yet dispatched
+    int64_t finished = 0;  // rows completed
+    bool done = false;
+    std::string error;
+    Clock::time_point t_submit, t_done;
+};
+
+struct Piece {
+    std::shared_ptr<Request> req;
+    int64_t row0, rows, off;  // request rows [row0, row0+rows) at batch offset `off`
+};
+
+struct Lane {
+    ce_session* sess = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    float* d_gains = nullptr;
+    float* d_info = nullptr;
+    float* h_gains = nullptr;  // pinned
+    float* h_info = nullptr;   // pinned
+    bool busy = false;
+    std::vector<Piece> pieces;
+};
+
+}  // namespace
+
+struct ce_server {
+    ce_config cfg{};
+    int n_plants = 0;
+    int64_t capacity = 0;  // candidates per batch (per lane)
+    int max_wait_us = 0;
+    std::vector<Lane> lanes;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::unordered_map<int64_t, std::shared_ptr<Request>> live;
+    int64_t next_id = 1;
+    bool stop = false;
+    std::thread worker;
+    // statistics
+    int64_t batches = 0, batched_rows = 0, completed = 0;
+    std::vector<double> latency_ms;  // completed requests, in completion order
+    std::string fatal;
+};
+
+namespace ce {
+
+namespace {
+
+// Device bytes one evaluation needs per candidate (session scratch + the
+// lane's batch buffers), from the sizes the session allocates.
+int64_t bytes_per_candidate(const ce_config& c) {
+    const int64_t nt = c.total_dim, pitch = ((c.fit_steps + 7) / 8) * 8;
+    const int64_t groups = (c.freq + SWEEP_FG - 1) / SWEEP_FG;
+    int64_t f = 0;
+    f += 2 * (int64_t)c.cuda_mx_width + 2 * (int64_t)c.info_mx_width;  // gains + INFO, session and lane
+    f += nt * nt;                                                      // LIN_A
+    f += 2 * nt + pitch + 4;                                           // eigenvalues, fit window, summary
+    f += 4 * nt * nt + 2 * nt;                                         // AtA, Atb
+    f += 1 + (MAXT + 1) + 1 + 1;                                       // nominal, fit order, lists
+    f += 2 * (int64_t)c.freq + 2 * groups;                             // sweep scratch
+    return 4 * f;
+}
+
+void complete_lane(ce_server* s, Lane& L) {
+    const int64_t iw = s->cfg.info_mx_width;
+    // each piece's rows go to a disjoint slice of its request's output
+    for (const Piece& p : L.pieces)
+        std::memcpy(p.req->info_out + p.row0 * iw, L.h_info + p.off * iw, (size_t)p.rows * iw * sizeof(float));
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> g(s->mu);
+    for (const Piece& p : L.pieces) {
+        p.req->finished += p.rows;
+        if (p.req->finished == p.req->n && !p.req->done) {
+            p.req->done = true;
+            p.req->t_done = now;
+            s->completed++;
+            s->latency_ms.push_back(std::chrono::duration<double, std::milli>(now - p.req->t_submit).count());
+        }
+    }
+    L.pieces.clear();
+    L.busy = false;
+    s->cv_done.notify_all();
+}
+
+void fail_pieces(ce_server* s, Lane& L, const std::string& msg) {
+    std::lock_guard<std::mutex> g(s->mu);
+    for (const Piece& p : L.pieces) {
+        p.req->error = msg;
+        p.req->done = true;
+        p.req->t_done = Clock::now();
+    }
+    L.pieces.clear();
+    L.busy = false;
+    s->cv_done.notify_all();
+}
+
+// Take rows for one batch from the queue (caller holds the lock).
+std::vector<Piece> form_batch(ce_server* s, int& plant) {
+    std::vector<Piece> out;
+    if (s->queue.empty()) return out;
+    plant = s->queue.front()->plant;
+    int64_t room = s->capacity, off = 0;
+    for (auto it = s->queue.begin(); it != s->queue.end() && room > 0;) {
+        Request& r = **it;
+        if (r.plant != plant) {
+            ++it;
+            continue;
+        }
+        const int64_t take = std::min(room, r.n - r.next);
+        out.push_back(Piece{*it, r.next, take, off});
+        r.next += take;
+        off += take;
+        room -= take;
+        if (r.next == r.n) it = s->queue.erase(it);
+        else ++it;
+    }
+    return out;
+}
+
+void dispatch(ce_server* s, Lane& L, int plant) {
+    const int64_t cw = s->cfg.cuda_mx_width, iw = s->cfg.info_mx_width;
+    int64_t n = 0;
+    for (const Piece& p : L.pieces) {
+        std::memcpy(L.h_gains + p.off * cw, p.req->gains + p.row0 * cw, (size_t)p.rows * cw * sizeof(float));
+        std::memcpy(L.h_info + p.off * iw, p.req->info_in + p.row0 * iw, (size_t)p.rows * iw * sizeof(float));
+        n = std::max(n, p.off + p.rows);
+    }
+    CE_CUDA(cudaMemcpyAsync(L.d_gains, L.h_gains, (size_t)n * cw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
+    CE_CUDA(cudaMemcpyAsync(L.d_info, L.h_info, (size_t)n * iw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
+    if (ce_evaluate_device(L.sess, plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0)
+        throw std::runtime_error(ce_last_error());
+    CE_CUDA(cudaMemcpyAsync(L.h_info, L.d_info, (size_t)n * iw * sizeof(float), cudaMemcpyDeviceToHost, L.stream));
+    CE_CUDA(cudaEventRecord(L.done, L.stream));
+    std::lock_guard<std::mutex> g(s->mu);
+    s->batches++;
+    s->batched_rows += n;
+}
+
+void worker_loop(ce_server* s, int device) {
+    cudaSetDevice(device);
+    for (;;) {
+        // retire finished batches
+        for (Lane& L : s->lanes) {
+            if (!L.busy) continue;
+            const cudaError_t q = cudaEventQuery(L.done);
+            if (q == cudaSuccess) complete_lane(s, L);
+            else if (q != cudaErrorNotReady) fail_pieces(s, L, std::string("CUDA error: ") + cudaGetErrorString(q));
+        }
+        Lane* freeL = nullptr;
+        for (Lane& L : s->lanes)
+            if (!L.busy) {
+                freeL = &L;
+                break;
+            }
+        bool any_busy = false;
+        for (Lane& L : s->lanes) any_busy = any_busy || L.busy;
+        int plant = 0;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->stop && s->queue.empty() && !any_busy) return;
+            if (!freeL || s->queue.empty()) {
+                // nothing to dispatch: wait for a request, or poll the busy lanes
+                s->cv_work.wait_for(lk, std::chrono::microseconds(any_busy ? 50 : 2000));
+                continue;
+            }
+            // continuous batching: a partial batch may wait briefly for more rows
+            if (s->max_wait_us > 0) {
+                int64_t rows = 0;
+                for (auto& r : s->queue) rows += r->n - r->next;
+                const auto age = Clock::now() - s->queue.front()->t_submit;
+                if (rows < s->capacity && age < std::chrono::microseconds(s->max_wait_us) && !s->stop) {
+                    s->cv_work.wait_for(lk, std::chrono::microseconds(50));
+                    continue;
+                }
+            }
+            freeL->pieces = form_batch(s, plant);
+            freeL->busy = !freeL->pieces.empty();
+        }
+        if (freeL->busy) {
+            try {
+                dispatch(s, *freeL, plant);
+            } catch (const std::exception& e) {
+                cudaStreamSynchronize(freeL->stream);  // nothing of the batch may still be in flight
+                fail_pieces(s, *freeL, e.what());
+            }
+        }
+    }
+}
+
+void destroy_server(ce_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    for (Lane& L : s->lanes) {
+        if (L.stream) cudaStreamSynchronize(L.stream);
+        if (L.sess) ce_session_destroy(L.sess);
+        if (L.done) cudaEventDestroy(L.done);
+        if (L.stream) cudaStreamDestroy(L.stream);
+        if (L.d_gains) cudaFree(L.d_gains);
+        if (L.d_info) cudaFree(L.d_info);
+        if (L.h_gains) cudaFreeHost(L.h_gains);
+        if (L.h_info) cudaFreeHost(L.h_info);
+    }
+    delete s;
+}
+
+void create_server(const ce_config* cfg, const ce_plant* plant, int n_plants, const ce_server_options* opt,
+                   ce_server** out) {
+    if (!cfg || !plant || !out) fail("ce_server_create: null argument");
+    ce_server_options o{};
+    if (opt) o = *opt;
+    const int lanes = o.lanes > 0 ? o.lanes : 2;
+    if (lanes > 8) fail("ce_server_create: at most 8 lanes, got {}", lanes);
+    int64_t cap = o.max_batch > 0 ? o.max_batch : 65536;
+    const int64_t per = bytes_per_candidate(*cfg);
+    if (o.hbm_budget_bytes > 0) {
+        const int64_t fit = o.hbm_budget_bytes / ((int64_t)lanes * per);
+        if (fit < 1)
+            fail("ce_server_create: an HBM budget of {} bytes does not hold one candidate per lane ({} bytes each, {} lanes)",
+                 o.hbm_budget_bytes, per, lanes);
+        cap = std::min(cap, fit);
+    }
+    auto s = std::unique_ptr<ce_server, void (*)(ce_server*)>(new ce_server, destroy_server);
+    s->cfg = *cfg;
+    s->n_plants = n_plants;
+    s->capacity = cap;
+    s->max_wait_us = std::max(0, o.max_wait_us);
+    s->lanes.resize(lanes);
+    int device = 0;
+    CE_CUDA(cudaGetDevice(&device));
+    for (Lane& L : s->lanes) {
+        if (ce_session_create(cfg, plant, n_plants, &L.sess) != 0) throw std::runtime_error(ce_last_error());
+        CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+        CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+        CE_CUDA(cudaMalloc((void**)&L.d_gains, (size_t)cap * cfg->cuda_mx_width * sizeof(float)));
+        CE_CUDA(cudaMalloc((void**)&L.d_info, (size_t)cap * cfg->info_mx_width * sizeof(float)));
+        CE_CUDA(cudaHostAlloc((void**)&L.h_gains, (size_t)cap * cfg->cuda_mx_width * sizeof(float), cudaHostAllocDefault));
+        CE_CUDA(cudaHostAlloc((void**)&L.h_info, (size_t)cap * cfg->info_mx_width * sizeof(float), cudaHostAllocDefault));
+    }
+    s->worker = std::thread(worker_loop, s.get(), device);
+    *out = s.release();
+}
+
+}  // namespace
+}  // namespace ce
+
+using namespace ce;
+
+extern "C" {
+
+CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants,
+                               const ce_server_options* opt, ce_server** out) {
+    try {
+        create_server(cfg, plant, n_plants, opt, out);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT void ce_server_destroy(ce_server* s) { destroy_server(s); }
+
+CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, const float* cuda_mx, const float* info_in,
+                               float* info_out, int64_t* request_id) {
+    try {
+        if (!s || !request_id) fail("ce_server_submit: null argument");
+        if (plant_index < 0 || plant_index >= s->n_plants)
+            fail("plant index {} out of range [0, {})", plant_index, s->n_plants);
+        if (n < 0) fail("candidate count {} is negative", n);
+        if (n > 0 && (!cuda_mx || !info_in || !info_out)) fail("ce_server_submit: null buffer");
+        auto r = std::make_shared<Request>();
+        r->plant = plant_index;
+        r->n = n;
+        r->gains = cuda_mx;
+        r->info_in = info_in;
+        r->info_out = info_out;
+        r->t_submit = Clock::now();
+        {
+            std::lock_guard<std::mutex> g(s->mu);
+            if (s->stop) fail("ce_server_submit: server is shutting down");
+            r->id = s->next_id++;
+            s->live.emplace(r->id, r);
+            if (n == 0) {
+                r->done = true;
+                r->t_done = r->t_submit;
+            } else {
+                s->queue.push_back(r);
+            }
+            *request_id = r->id;
+        }
+        s->cv_work.notify_one();
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT int ce_server_wait(ce_server* s, int64_t request_id, int32_t timeout_ms) {
+    try {
+        if (!s) fail("null server");
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->live.find(request_id);
+        if (it == s->live.end()) fail("unknown request id {}", request_id);
+        std::shared_ptr<Request> r = it->second;
+        auto ready = [&] { return r->done; };
+        if (timeout_ms < 0) s->cv_done.wait(lk, ready);
+        else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return CE_PENDING;
+        s->live.erase(request_id);
+        if (!r->error.empty()) fail("request {} failed: {}", request_id, r->error);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT int ce_server_get_stats(ce_server* s, ce_server_stats* out) {
+    try {
+        if (!s || !out) fail("null argument");
+        std::lock_guard<std::mutex> g(s->mu);
+        ce_server_stats st{};
+        st.capacity = s->capacity;
+        st.lanes = (int32_t)s->lanes.size();
+        st.completed = s->completed;
+        st.batches = s->batches;
+        st.batched_candidates = s->batched_rows;
+        st.queued = (int64_t)s->queue.size();
+        std::vector<double> v = s->latency_ms;
+        if (!v.empty()) {
+            std::sort(v.begin(), v.end());
+            auto pct = [&](double p) {
+                const size_t k = std::min(v.size() - 1, (size_t)std::ceil(p * (double)v.size()) - 1);
+                return v[k];
+            };
+            st.latency_p50_ms = pct(0.50);
+            st.latency_p99_ms = pct(0.99);
+            st.latency_max_ms = v.back();
+        }
+        *out = st;
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT int ce_server_reset_stats(ce_server* s) {
+    if (!s) return 1;
+    std::lock_guard<std::mutex> g(s->mu);
+    s->latency_ms.clear();
+    s->completed = s->batches = s->batched_rows = 0;
+    return 0;
+}
+
+}  // extern "C"

@@ -261,6 +261,75 @@ class Session:
                                          C.c_void_p(d_info_out), C.c_void_p(stream)))
 
 
+class Request:
+    """One submitted request: its buffers stay referenced until `wait` returns."""
+
+    def __init__(self, server: "Server", rid: int, cuda_mx: np.ndarray, info_in: np.ndarray, out: np.ndarray):
+        self._server, self.id = server, rid
+        self._keep = (cuda_mx, info_in)
+        self.out = out
+
+    def wait(self, timeout_ms: int = -1) -> np.ndarray | None:
+        """INFO rows of the request, or None if `timeout_ms` passed first."""
+        rc = _lib().ce_server_wait(self._server._h, self.id, timeout_ms)
+        if rc == _ffi.PENDING:
+            return None
+        _check(rc)
+        self._keep = None
+        return self.out
+
+
+class Server:
+    """Continuous-batching front end (ce_server_*): requests of any size, packed per plant into batches of up
+    to `max_batch` candidates, `lanes` batches in flight on the GPU."""
+
+    def __init__(self, config: EngineConfig, plant: PlantFiles, n_plants: int = 1, max_batch: int = 0,
+                 lanes: int = 0, hbm_budget_bytes: int = 0, max_wait_us: int = 0):
+        self.config = config
+        self._plant = plant
+        self._h = C.c_void_p()
+        opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us)
+        _check(_lib().ce_server_create(C.byref(config.raw), C.byref(plant.ce_plant()), n_plants, C.byref(opt),
+                                       C.byref(self._h)))
+
+    def submit(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, plant_index: int = 0) -> Request:
+        c = self.config
+        g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
+        n = g.shape[0]
+        if info_in is None:
+            info_in = np.zeros((n, c.info_mx_width), F32)
+        i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
+        out = np.empty_like(i)
+        rid = C.c_int64()
+        _check(_lib().ce_server_submit(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(rid)))
+        return Request(self, rid.value, g, i, out)
+
+    def stats(self) -> dict:
+        st = _ffi.ce_server_stats()
+        _check(_lib().ce_server_get_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def reset_stats(self):
+        _check(_lib().ce_server_reset_stats(self._h))
+
+    def close(self):
+        if self._h:
+            _lib().ce_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def measure_fma_rate(fp64: bool = False) -> float:
     """FMA-issue throughput of the current device, operations per second."""
     v = C.c_double()

@@ -256,6 +256,47 @@ CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second);
 CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
                                    const float* d_eigen, float* d_ata, float* d_atb, float* d_info, void* stream);
 
+/* ---- Serving (no counterpart in the reference, which serves one synchronous
+ * file round per call, ref: src/main.cu:467-582) ----------------------------
+ * A server holds `lanes` sessions of one configuration and a scheduler thread.
+ * Requests of any size queue in arrival order; the scheduler packs the oldest
+ * request's plant with the queued requests of the same plant into a batch of
+ * up to `capacity` candidates (a larger request is served in pieces) and runs
+ * it on a free lane; lanes run concurrently on the GPU.  A request's rows do
+ * not depend on the batch they are packed into.  The caller's buffers must
+ * stay valid until ce_server_wait reports the request done; every request must
+ * be waited for once. */
+typedef struct ce_server ce_server;
+
+typedef struct ce_server_options {
+    int32_t max_batch;        /* candidates per batch (0: 65,536) */
+    int32_t lanes;            /* concurrent batches (0: 2, at most 8) */
+    int64_t hbm_budget_bytes; /* device memory for all lanes (0: no limit); capacity shrinks to fit */
+    int32_t max_wait_us;      /* a partial batch waits up to this long for more requests (0: none) */
+} ce_server_options;
+
+typedef struct ce_server_stats {
+    int64_t capacity;           /* candidates per batch after admission */
+    int32_t lanes;
+    int64_t completed;          /* requests completed since creation / the last reset */
+    int64_t batches;            /* batches dispatched */
+    int64_t batched_candidates; /* candidates in those batches */
+    int64_t queued;             /* requests waiting for dispatch */
+    double latency_p50_ms, latency_p99_ms, latency_max_ms; /* submit -> results in the caller's buffer */
+} ce_server_stats;
+
+#define CE_PENDING 2 /* ce_server_wait: the timeout passed first */
+
+CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants,
+                               const ce_server_options* options, ce_server** out);
+CE_EXPORT void ce_server_destroy(ce_server* s); /* serves what is queued, then stops */
+CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, const float* cuda_mx,
+                               const float* info_in, float* info_out, int64_t* request_id);
+/* 0: done (info_out filled); CE_PENDING: timeout (timeout_ms < 0 waits forever); 1: error. */
+CE_EXPORT int ce_server_wait(ce_server* s, int64_t request_id, int32_t timeout_ms);
+CE_EXPORT int ce_server_get_stats(ce_server* s, ce_server_stats* out);
+CE_EXPORT int ce_server_reset_stats(ce_server* s);
+
 /* The drop-in entry point (ref: src/main.cu:592-602, src/ControllerEngine.h:11):
  * reads ControllerEngine.config and the .bin files from the current
  * directory, streams n_rounds rounds of n_threads candidates, writes

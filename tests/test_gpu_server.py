@@ -1,0 +1,121 @@
+"""The serving front end (ce_server_*): requests of assorted sizes are packed into
+batches per plant, split when larger than a batch, and run on concurrent lanes;
+every request's rows must equal the rows of the same candidates evaluated alone,
+bit for bit.  Also: several plants in one server, submissions from several
+threads, HBM-budget admission and the latency statistics."""
+import dataclasses
+import threading
+
+import numpy as np
+import pytest
+
+import controllerengine_gb300 as ce
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def _alone(prob, plant_files=None, n_plants=1, plant_index=0, rows=slice(None)):
+    cfg = ce.EngineConfig.parse(prob.config_text)
+    with ce.Session(cfg, plant_files or prob.plant, n_plants=n_plants) as s:
+        return s.evaluate(prob.cuda_mx[rows], prob.info_mx[rows], plant_index=plant_index)
+
+
+def test_mixed_sizes_equal_alone(eight_state_small):
+    p = eight_state_small
+    cfg = ce.EngineConfig.parse(p.config_text)
+    ref = _alone(p)
+    cuts = [0, 37, 237, 242, 512]  # 37, 200, 5 and 270 candidates; batches hold 300
+    with ce.Server(cfg, p.plant, max_batch=300, lanes=2) as srv:
+        reqs = [srv.submit(p.cuda_mx[a:b], p.info_mx[a:b]) for a, b in zip(cuts, cuts[1:])]
+        outs = [r.wait() for r in reqs]
+        st = srv.stats()
+    got = np.vstack(outs)
+    assert np.array_equal(_bits(got), _bits(ref))
+    assert st["completed"] == 4 and st["capacity"] == 300
+    assert st["batched_candidates"] == 512 and st["batches"] >= 2  # the 270-candidate request is split
+    assert 0 < st["latency_p50_ms"] <= st["latency_p99_ms"] <= st["latency_max_ms"]
+
+
+def test_request_larger_than_a_batch_is_split(mass_spring):
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    ref = _alone(p)
+    with ce.Server(cfg, p.plant, max_batch=256, lanes=3) as srv:
+        out = srv.submit(p.cuda_mx, p.info_mx).wait()
+        st = srv.stats()
+    assert np.array_equal(_bits(out), _bits(ref))
+    assert st["batches"] == 6  # 1536 candidates in batches of 256
+
+
+def _two_plants(p):
+    """The mass-spring plant twice, the second copy with another cubic stiffness (BASE_PARAMS[0])."""
+    pl = p.plant
+    bp2 = pl.base_params.copy()
+    bp2[0] *= 3.0
+    stack = lambda a: np.concatenate([a.ravel(), a.ravel()])
+    return dataclasses.replace(pl, discrete_a=stack(pl.discrete_a), discrete_a_i=stack(pl.discrete_a_i),
+                               discrete_bu=stack(pl.discrete_bu), discrete_bw=stack(pl.discrete_bw),
+                               discrete_c=stack(pl.discrete_c), base_params=np.concatenate([pl.base_params, bp2]))
+
+
+def test_two_plants_in_one_server(mass_spring):
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    pl2 = _two_plants(p)
+    refs = [_alone(p, pl2, 2, k) for k in range(2)]
+    assert not np.array_equal(refs[0], refs[1])  # the plants differ
+    with ce.Server(cfg, pl2, n_plants=2, max_batch=512, lanes=2) as srv:
+        reqs = [(k, a, srv.submit(p.cuda_mx[a:a + 192], p.info_mx[a:a + 192], plant_index=k))
+                for a in range(0, 1536, 192) for k in range(2)]
+        for k, a, r in reqs:
+            assert np.array_equal(_bits(r.wait()), _bits(refs[k][a:a + 192]))
+
+
+def test_concurrent_submitters(eight_state_small):
+    p = eight_state_small
+    cfg = ce.EngineConfig.parse(p.config_text)
+    ref = _alone(p)
+    results, errors = {}, []
+    with ce.Server(cfg, p.plant, max_batch=200, lanes=2) as srv:
+        def client(t):
+            try:
+                for a in range(t * 64, 512, 4 * 64):
+                    results[a] = srv.submit(p.cuda_mx[a:a + 64], p.info_mx[a:a + 64]).wait()
+            except Exception as e:  # reported below
+                errors.append(e)
+        th = [threading.Thread(target=client, args=(t,)) for t in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    assert not errors
+    got = np.vstack([results[a] for a in sorted(results)])
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
+def test_hbm_budget_admission(eight_state_small):
+    p = eight_state_small
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Server(cfg, p.plant, max_batch=65536, lanes=2, hbm_budget_bytes=64 << 20) as srv:
+        cap = srv.stats()["capacity"]
+        assert 0 < cap < 65536
+        out = srv.submit(p.cuda_mx, p.info_mx).wait()
+    assert np.array_equal(_bits(out), _bits(_alone(p)))
+    with pytest.raises(ce.ControllerEngineError, match="HBM budget"):
+        ce.Server(cfg, p.plant, lanes=2, hbm_budget_bytes=1024)
+
+
+def test_timeout_and_empty_request(mass_spring):
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Server(cfg, p.plant, max_batch=1536) as srv:
+        empty = srv.submit(p.cuda_mx[:0], p.info_mx[:0])
+        assert empty.wait(0).shape == (0, cfg.info_mx_width)
+        r = srv.submit(p.cuda_mx, p.info_mx)
+        first = r.wait(0)  # usually still running; either way no error
+        out = first if first is not None else r.wait()
+    assert np.array_equal(_bits(out), _bits(_alone(p)))
