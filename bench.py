@@ -174,6 +174,58 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int = 65536, seed: int = 7):
+    """Request serving (ce_server_*): requests of U[256, 16384] candidates of the bench plant.
+    Saturation: 48 requests submitted at once, candidates/s until all are done.  Latency:
+    Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of submit -> results in the
+    caller's buffer (measured by the server)."""
+    import controllerengine_gb300 as ce
+    rng = np.random.default_rng(seed)
+    n_all = problem.cuda_mx.shape[0]
+
+    def draw():
+        m = int(rng.integers(256, 16385))
+        a = int(rng.integers(0, n_all - m + 1))
+        return problem.cuda_mx[a:a + m], problem.info_mx[a:a + m]
+
+    with ce.Server(cfg, problem.plant, max_batch=max_batch, lanes=lanes) as srv:
+        # warm-up: every lane sizes its scratch for a full batch
+        for r in [srv.submit(problem.cuda_mx, problem.info_mx) for _ in range(lanes)]:
+            r.wait()
+        reqs = [draw() for _ in range(48)]
+        total = sum(g.shape[0] for g, _ in reqs)
+        t0 = time.perf_counter()
+        hs = [srv.submit(g, i) for g, i in reqs]
+        for h in hs:
+            h.wait()
+        sat = total / (time.perf_counter() - t0)
+        mean_size = (256 + 16384) / 2
+        rate = 0.7 * sat / mean_size  # requests/s
+        srv.reset_stats()
+        hs, offered = [], 0
+        t0 = time.perf_counter()
+        t_next = t0
+        while t_next - t0 < seconds:
+            now = time.perf_counter()
+            if now < t_next:
+                time.sleep(t_next - now)
+            g, i = draw()
+            offered += g.shape[0]
+            hs.append(srv.submit(g, i))
+            t_next += rng.exponential(1.0 / rate)
+        for h in hs:
+            h.wait()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    return {"request_sizes": "U[256, 16384] candidates of the bench plant (T = 10,000, F = 400)",
+            "lanes": lanes, "max_batch": st["capacity"], "saturation_candidates_per_s": sat,
+            "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
+            "requests": st["completed"], "achieved_candidates_per_s": offered / wall,
+            "batches": st["batches"], "mean_batch": st["batched_candidates"] / max(1, st["batches"]),
+            "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
+            "latency_max_ms": st["latency_max_ms"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,6 +240,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
+    ap.add_argument("--serve-seconds", type=float, default=6.0, help="Poisson serving run (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -365,6 +418,8 @@ def main():
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    if rank == 0 and a.serve_seconds > 0:
+        line["serving"] = serving_bench(problem, cfg, a.serve_seconds)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
