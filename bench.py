@@ -174,7 +174,7 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int = 65536, seed: int = 7):
+def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int = 16384, seed: int = 7):
     """Request serving (ce_server_*): requests of U[256, 16384] candidates of the bench plant.
     Saturation: 48 requests submitted at once, candidates/s until all are done.  Latency:
     Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of submit -> results in the
