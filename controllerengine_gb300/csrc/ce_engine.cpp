@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <iomanip>
 #include <memory>
 #include <sstream>
@@ -744,6 +745,62 @@ void write_bin(const std::string& name, const void* p, size_t bytes) {
     f.write(reinterpret_cast<const char*>(p), (std::streamsize)bytes);
 }
 
+// The rounds of a file run without diagnostics, double-buffered: while round
+// r is on the GPU (H2D, the pipeline and D2H enqueued on the session stream),
+// the host writes round r-1's rows to INFO_MX_OUT.bin and reads round r+1 from
+// CUDA_MX.bin / INFO_MX.bin into the other pinned slot.  Rounds are written in
+// order; a read failure of round r+1 surfaces after round r has been written,
+// as in a sequential run.
+template <typename Read>
+void stream_rounds(ce_session* s, const ce_config& c, Read&& read_round, std::ofstream& out) {
+    const size_t nthr = (size_t)c.n_threads, cw = c.cuda_mx_width, iw = c.info_mx_width;
+    struct Slot {
+        float *hg = nullptr, *hi = nullptr, *dg = nullptr, *di = nullptr;
+        cudaEvent_t done = nullptr;
+    } slot[2];
+    auto release = [&] {
+        for (Slot& k : slot) {
+            if (k.hg) cudaFreeHost(k.hg);
+            if (k.hi) cudaFreeHost(k.hi);
+            if (k.dg) cudaFree(k.dg);
+            if (k.di) cudaFree(k.di);
+            if (k.done) cudaEventDestroy(k.done);
+        }
+    };
+    std::unique_ptr<Slot, std::function<void(Slot*)>> guard(slot, [&](Slot*) {
+        cudaStreamSynchronize(s->stream);
+        release();
+    });
+    for (Slot& k : slot) {
+        CE_CUDA(cudaMallocHost((void**)&k.hg, nthr * cw * sizeof(float)));
+        CE_CUDA(cudaMallocHost((void**)&k.hi, nthr * iw * sizeof(float)));
+        CE_CUDA(cudaMalloc((void**)&k.dg, nthr * cw * sizeof(float)));
+        CE_CUDA(cudaMalloc((void**)&k.di, nthr * iw * sizeof(float)));
+        CE_CUDA(cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming));
+    }
+    cudaStream_t st = s->stream;
+    auto write_round = [&](Slot& k) {
+        CE_CUDA(cudaEventSynchronize(k.done));
+        out.write(reinterpret_cast<char*>(k.hi), nthr * iw * sizeof(float));
+    };
+    read_round(0, slot[0].hg, slot[0].hi);
+    for (int round = 0; round < c.n_rounds; round++) {
+        Slot& k = slot[round & 1];
+        CE_CUDA(cudaMemcpyAsync(k.dg, k.hg, nthr * cw * sizeof(float), cudaMemcpyHostToDevice, st));
+        CE_CUDA(cudaMemcpyAsync(k.di, k.hi, nthr * iw * sizeof(float), cudaMemcpyHostToDevice, st));
+        run_pipeline(s, c.serial ? round : 0, (int64_t)nthr, k.dg, k.di, st, false);
+        CE_CUDA(cudaMemcpyAsync(k.hi, k.di, nthr * iw * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CE_CUDA(cudaEventRecord(k.done, st));
+        if (round + 1 < c.n_rounds) {
+            Slot& other = slot[(round + 1) & 1];
+            if (round >= 1) write_round(other);  // round - 1
+            read_round(round + 1, other.hg, other.hi);
+        }
+    }
+    if (c.n_rounds >= 2) write_round(slot[(c.n_rounds - 2) & 1]);
+    if (c.n_rounds >= 1) write_round(slot[(c.n_rounds - 1) & 1]);
+}
+
 void run_files() {
     ce_config c;
     parse_config(read_text("ControllerEngine.config"), "ControllerEngine.config", c);
@@ -812,11 +869,18 @@ void run_files() {
         db.resize(nthr * 2 * nt);
         dg = ce_diagnostics{dy.data(), dl.data(), de.data(), da2.data(), db.data()};
     }
-    for (int round = 0; round < c.n_rounds; round++) {
-        cudamx.read(reinterpret_cast<char*>(hc_mx), nthr * cw * sizeof(float));
+    auto read_round = [&](int round, float* g, float* info) {
+        cudamx.read(reinterpret_cast<char*>(g), nthr * cw * sizeof(float));
         if (!cudamx) fail("Cannot read CUDA_MX.bin round {} (intended {}-byte allocation)", round, nthr * cw * sizeof(float));
-        infomx.read(reinterpret_cast<char*>(hinfo), nthr * iw * sizeof(float));
+        infomx.read(reinterpret_cast<char*>(info), nthr * iw * sizeof(float));
         if (!infomx) fail("Cannot read INFO_MX.bin round {} (intended {}-byte allocation)", round, nthr * iw * sizeof(float));
+    };
+    if (!c.dump_diagnostics) {
+        stream_rounds(s.get(), c, read_round, infoout);
+        return;
+    }
+    for (int round = 0; round < c.n_rounds; round++) {
+        read_round(round, hc_mx, hinfo);
         evaluate_host(s.get(), c.serial ? round : 0, (int64_t)nthr, hc_mx, hinfo, hinfo,
                       c.dump_diagnostics ? &dg : nullptr);
         if (c.dump_diagnostics) {

@@ -59,3 +59,35 @@ def test_errors_go_to_error_log(lib, mass_spring, tmp_path, breakage, msg):
     assert ce.run_controller_engine(tmp_path) == 1
     lines = (tmp_path / "error.log").read_text().splitlines()
     assert lines[-1].startswith(msg), lines[-1]
+
+
+def test_streamed_rounds_match_sessions(lib, tmp_path):
+    """Three rounds without diagnostics go through the double-buffered path; in
+    mode = serial every round has its own plant (stacked DISCRETE_* and
+    BASE_PARAMS, ref: src/main.cu:341-354).  Each round's rows must equal a
+    session evaluation of that round's plant."""
+    import dataclasses
+    p = synth.eight_state(n=1536, time=2000, freq=100)
+    pl = p.plant
+    rounds = 3
+    bps = [pl.base_params.copy() for _ in range(rounds)]
+    for r in range(rounds):
+        bps[r][1] *= 1.0 + 0.5 * r  # Coulomb friction coefficient differs per round
+    stack = lambda a: np.concatenate([np.asarray(a).ravel()] * rounds)
+    pl3 = dataclasses.replace(pl, discrete_a=stack(pl.discrete_a), discrete_a_i=stack(pl.discrete_a_i),
+                              discrete_bu=stack(pl.discrete_bu), discrete_bw=stack(pl.discrete_bw),
+                              discrete_c=stack(pl.discrete_c), base_params=np.concatenate(bps))
+    text = p.config_text.replace("n_rounds = 1", f"n_rounds = {rounds}").replace("mode = batch", "mode = serial")
+    rng = np.random.default_rng(5)
+    perms = [rng.permutation(1536) for _ in range(rounds)]
+    g = np.vstack([p.cuda_mx[q] for q in perms])
+    info = np.vstack([p.info_mx[q] for q in perms])
+    synth.Problem("serial_rounds", text, pl3, g, info).write(tmp_path)
+    assert ce.run_controller_engine(tmp_path) == 0
+    cfg = ce.EngineConfig.parse(text)
+    out = np.fromfile(tmp_path / "INFO_MX_OUT.bin", np.float32).reshape(rounds, 1536, cfg.info_mx_width)
+    with ce.Session(cfg, pl3, n_plants=rounds) as s:
+        for r in range(rounds):
+            ref = s.evaluate(g[r * 1536:(r + 1) * 1536], info[r * 1536:(r + 1) * 1536], plant_index=r)
+            assert np.array_equal(out[r], ref, equal_nan=True), f"round {r}"
+    assert not np.array_equal(out[0], out[1], equal_nan=True)  # the plants differ
