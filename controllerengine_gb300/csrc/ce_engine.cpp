@@ -34,82 +34,6 @@ namespace {
 
 constexpr float PI = 0x1.921fb6p+1f;
 
-// ---- host complex LU: the same algorithm as the device lu_solve_shifted -----
-template <typename R>
-struct hc {
-    R re, im;
-};
-template <typename R>
-hc<R> hmul(hc<R> a, hc<R> b) {
-    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
-template <typename R>
-hc<R> hsub(hc<R> a, hc<R> b) {
-    return {a.re - b.re, a.im - b.im};
-}
-template <typename R>
-hc<R> hdiv(hc<R> a, hc<R> b) {
-    const R d = b.re * b.re + b.im * b.im;
-    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
-}
-
-// x = (z I - A)^{-1} b, A n x n row-major.  Returns false if x is not finite.
-template <typename R>
-bool host_lu_solve(hc<R> z, const R* A, const R* b, int n, hc<R>* x) {
-    hc<R> M[8][8];
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) {
-            const hc<R> zi = (i == j) ? hc<R>{z.re * R(1) - z.im * R(0), z.re * R(0) + z.im * R(1)}
-                                      : hc<R>{z.re * R(0) - z.im * R(0), z.re * R(0) + z.im * R(0)};
-            M[i][j] = hsub(zi, hc<R>{A[i * n + j], R(0)});
-        }
-    int perm[8];
-    for (int k = 0; k < n; ++k) {
-        int p = k;
-        R best = M[k][k].re * M[k][k].re + M[k][k].im * M[k][k].im;
-        for (int i = k + 1; i < n; ++i) {
-            const R s = M[i][k].re * M[i][k].re + M[i][k].im * M[i][k].im;
-            if (s > best) {
-                best = s;
-                p = i;
-            }
-        }
-        perm[k] = p;
-        if (best != R(0)) {
-            if (p != k)
-                for (int j = 0; j < n; ++j) std::swap(M[k][j], M[p][j]);
-            for (int i = k + 1; i < n; ++i) M[i][k] = hdiv(M[i][k], M[k][k]);
-        }
-        for (int i = k + 1; i < n; ++i)
-            for (int j = k + 1; j < n; ++j) M[i][j] = hsub(M[i][j], hmul(M[i][k], M[k][j]));
-    }
-    for (int i = 0; i < n; ++i) x[i] = hc<R>{b[i], R(0)};
-    for (int k = 0; k < n; ++k) std::swap(x[k], x[perm[k]]);
-    for (int i = 0; i < n; ++i)
-        for (int s = i + 1; s < n; ++s) x[s] = hsub(x[s], hmul(x[i], M[s][i]));
-    for (int i = n - 1; i >= 0; --i) {
-        x[i] = hdiv(x[i], M[i][i]);
-        for (int s = 0; s < i; ++s) x[s] = hsub(x[s], hmul(x[i], M[s][i]));
-    }
-    for (int i = 0; i < n; ++i)
-        if (!std::isfinite(x[i].re) || !std::isfinite(x[i].im)) return false;
-    return true;
-}
-
-// C^T x + D
-template <typename R>
-hc<R> host_ctx(const R* C, const hc<R>* x, int n, R D) {
-    hc<R> acc{R(0), R(0)};
-    for (int i = 0; i < n; ++i) {
-        const hc<R> t = hmul(hc<R>{C[i], R(0)}, x[i]);
-        acc = hc<R>{acc.re + t.re, acc.im + t.im};
-    }
-    return hc<R>{acc.re + D, acc.im};
-}
-
-float habs(hc<float> a) { return std::hypot(a.re, a.im); }
-double habs(hc<double> a) { return std::hypot(a.re, a.im); }
-
 }  // namespace
 
 struct Buffers {
@@ -160,12 +84,15 @@ struct ce_session {
     int sim_kind = CE_SIM_SPECIALISED;
     std::vector<const void*> sim_kernel;
     std::string sim_log;
-    std::vector<float> alpha32;
+    // margin plants and their sweep grids: one per plant in serial mode, the
+    // observer model shared by all plants in batch mode (ref: src/allmargin.cu:11-15)
+    int grid_np = 1;
+    int grid_of(int plant) const { return cfg.serial ? plant : 0; }
+    std::vector<float> alpha32;   // per margin plant
     std::vector<double> alpha64;
-    std::vector<float> fgrid32;   // n_plants * freq * 8
-    std::vector<double> fgrid64;
-    float* d_fgrid32 = nullptr;
-    double* d_fgrid64 = nullptr;
+    float* d_mplant = nullptr;    // grid_np x margin_plant_stride() floats
+    float* d_fgrid32 = nullptr;   // grid_np x freq x 8
+    double* d_fgrid64 = nullptr;  // built on the first FP64 evaluation
     ce::Buffers buf;
     // stream: host-buffer evaluations; fast: the FP32 stages (lowest
     // priority); side: the FP64 eigensolves (highest priority)
@@ -301,11 +228,13 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
     r.target_gm = c.target_gm;
     r.target_pm = c.target_pm;
     r.target_b = c.target_b;
-    r.alpha = s->alpha32[plant];
-    r.alpha64 = s->alpha64[plant];
+    r.alpha = s->alpha32[s->grid_of(plant)];
+    r.alpha64 = s->alpha64.empty() ? 0.0 : s->alpha64[s->grid_of(plant)];
     r.store_traj = 0;
     return r;
 }
+
+void build_grids(ce_session* s, int precision);
 
 // Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
 // CE_CHUNKS (default 2: of 1, 2 and 4 chunks, 2 measured fastest on the
@@ -325,14 +254,15 @@ int n_chunks(int64_t n) {
 void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
                   bool traj) {
     if (!s->plant_err[plant].empty()) throw std::runtime_error(s->plant_err[plant]);
+    const int prec = s->precision;
+    if (prec == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
     ensure_buffers(s, n, traj);
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
     r.store_traj = traj ? 1 : 0;
     const Plant& P = s->plants[plant];
-    const int prec = s->precision;
-    const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + (size_t)plant * s->cfg.freq * 8)
-                                                  : (const void*)(s->d_fgrid32 + (size_t)plant * s->cfg.freq * 8);
+    const size_t goff = (size_t)s->grid_of(plant) * s->cfg.freq * 8;
+    const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + goff) : (const void*)(s->d_fgrid32 + goff);
     // each launch optionally bracketed by events on the stream it runs on
     auto timed = [&](int stage, cudaStream_t on, auto&& launch) {
         if (!s->profiling) {
@@ -498,64 +428,81 @@ void build_plant(const ce_config& c, const ce_plant& in, int p, Plant& P) {
     }
 }
 
-// Sweep grid and plant response of one plant, float and double forms
-// (ref: src/main.cu:421-428, src/allmargin.cu:11-41).
-void build_fgrid(ce_session* s, int p) {
+// The sweep grid and the margin plants' response on it, with the plant scaling
+// at the crossover (ref: src/main.cu:421-428, src/allmargin.cu:20-41).  The z
+// grid is formed here with host float libm, as in the reference; P(z_w) and
+// alpha run on the device for all margin plants at once (k_plant_grid).  A
+// margin plant without a finite nonzero gain at the crossover makes its
+// evaluations fail with the reference's message.
+void build_grids(ce_session* s, int precision) {
     const ce_config& c = s->cfg;
-    const Plant& P = s->plants[p];
-    const int n = c.serial ? c.discrete_dim : c.statespace_dim;
-    const int F = c.freq;
-    float A32[64], B32[8], C32[8];
-    double A64[64], B64[8], C64[8];
-    for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) {
-            A32[i * n + j] = P.m_a[i * MAXS + j];
-            A64[i * n + j] = P.m_a[i * MAXS + j];
-        }
-        B32[i] = P.m_b[i];
-        C32[i] = P.m_c[i];
-        B64[i] = P.m_b[i];
-        C64[i] = P.m_c[i];
-    }
-    float* g32 = s->fgrid32.data() + (size_t)p * F * 8;
-    double* g64 = s->fgrid64.data() + (size_t)p * F * 8;
+    const int F = c.freq, n = c.serial ? c.discrete_dim : c.statespace_dim, np = s->grid_np;
+    const bool f64 = precision == CE_PRECISION_FP64;
+    const size_t rsz = f64 ? sizeof(double) : sizeof(float);
+    std::vector<double> z64((size_t)(F + 1) * 4, 0.0);
+    std::vector<float> z32((size_t)(F + 1) * 4, 0.0f);
     const float inc = (logf(c.freq_max) - logf(c.freq_min)) / (float)(F - 1);
     const double inc64 = (std::log((double)c.freq_max) - std::log((double)c.freq_min)) / (double)(F - 1);
     for (int w = 0; w < F; ++w) {
         const float th = expf(logf(c.freq_min) + inc * (float)w) * c.ts;
-        const hc<float> z{cosf(th), sinf(th)};
-        hc<float> x[8];
-        const bool ok = host_lu_solve<float>(z, A32, B32, n, x);
-        const hc<float> Pr = ok ? host_ctx<float>(C32, x, n, P.m_d) : hc<float>{0.0f, 0.0f};
-        float* g = g32 + 8 * w;
-        g[0] = z.re; g[1] = z.im; g[2] = std::atan2(z.im, z.re);
-        g[3] = Pr.re; g[4] = Pr.im; g[5] = habs(Pr); g[6] = ok ? 1.0f : 0.0f; g[7] = 0.0f;
-
+        z32[4 * w] = cosf(th);
+        z32[4 * w + 1] = sinf(th);
+        z32[4 * w + 2] = std::atan2(z32[4 * w + 1], z32[4 * w]);
         const double th64 = std::exp(std::log((double)c.freq_min) + inc64 * (double)w) * (double)c.ts;
-        const hc<double> z64{std::cos(th64), std::sin(th64)};
-        hc<double> x64[8];
-        const bool ok64 = host_lu_solve<double>(z64, A64, B64, n, x64);
-        const hc<double> Pr64 = ok64 ? host_ctx<double>(C64, x64, n, (double)P.m_d) : hc<double>{0.0, 0.0};
-        double* h = g64 + 8 * w;
-        h[0] = z64.re; h[1] = z64.im; h[2] = std::atan2(z64.im, z64.re);
-        h[3] = Pr64.re; h[4] = Pr64.im; h[5] = habs(Pr64); h[6] = ok64 ? 1.0 : 0.0; h[7] = 0.0;
+        z64[4 * w] = std::cos(th64);
+        z64[4 * w + 1] = std::sin(th64);
+        z64[4 * w + 2] = std::atan2(z64[4 * w + 1], z64[4 * w]);
     }
-    // plant scaling at the spec crossover
     {
         const float th = c.crossover * c.ts;
-        const hc<float> zc{1.0f * cosf(th), 1.0f * sinf(th)};
-        hc<float> x[8];
-        const bool ok = host_lu_solve<float>(zc, A32, B32, n, x);
-        const float pmag = habs(host_ctx<float>(C32, x, n, P.m_d));
-        if (!ok || !(pmag > 0.0f) || !std::isfinite(pmag))
-            s->plant_err[p] = std::format("allmargin: plant has no finite nonzero gain at crossover = {} rad/s", c.crossover);
-        s->alpha32[p] = 1.0f / pmag;
+        z32[4 * F] = 1.0f * cosf(th);
+        z32[4 * F + 1] = 1.0f * sinf(th);
         const double th64 = (double)c.crossover * (double)c.ts;
-        const hc<double> zc64{std::cos(th64), std::sin(th64)};
-        hc<double> x64[8];
-        host_lu_solve<double>(zc64, A64, B64, n, x64);
-        s->alpha64[p] = 1.0 / habs(host_ctx<double>(C64, x64, n, (double)P.m_d));
+        z64[4 * F] = std::cos(th64);
+        z64[4 * F + 1] = std::sin(th64);
     }
+    const int ms = margin_plant_stride();
+    if (!s->d_mplant) {
+        std::vector<float> mp((size_t)np * ms, 0.0f);
+        for (int p = 0; p < np; ++p) {
+            const Plant& P = s->plants[p];
+            float* m = mp.data() + (size_t)p * ms;
+            std::memcpy(m, P.m_a, sizeof(P.m_a));
+            std::memcpy(m + MAXS * MAXS, P.m_b, sizeof(P.m_b));
+            std::memcpy(m + MAXS * MAXS + MAXS, P.m_c, sizeof(P.m_c));
+            m[MAXS * MAXS + 2 * MAXS] = P.m_d;
+        }
+        CE_CUDA(cudaMalloc((void**)&s->d_mplant, mp.size() * sizeof(float)));
+        CE_CUDA(cudaMemcpy(s->d_mplant, mp.data(), mp.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    void* zg = nullptr;
+    void* alpha = nullptr;
+    int* bad = nullptr;
+    void* grid = nullptr;
+    CE_CUDA(cudaMalloc(&zg, (size_t)(F + 1) * 4 * rsz));
+    CE_CUDA(cudaMalloc(&alpha, (size_t)np * rsz));
+    CE_CUDA(cudaMalloc((void**)&bad, (size_t)np * sizeof(int)));
+    CE_CUDA(cudaMalloc(&grid, (size_t)np * F * 8 * rsz));
+    std::unique_ptr<void, cudaError_t (*)(void*)> g1(zg, cudaFree), g2(alpha, cudaFree), g3(bad, cudaFree);
+    if (f64) CE_CUDA(cudaMemcpy(zg, z64.data(), z64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    else CE_CUDA(cudaMemcpy(zg, z32.data(), z32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    launch_plant_grid(precision, np, n, F, s->d_mplant, zg, grid, alpha, bad, s->stream);
+    std::vector<int> hbad(np);
+    CE_CUDA(cudaMemcpyAsync(hbad.data(), bad, (size_t)np * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (f64) {
+        s->alpha64.resize(np);
+        CE_CUDA(cudaMemcpyAsync(s->alpha64.data(), alpha, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        s->d_fgrid64 = (double*)grid;
+    } else {
+        s->alpha32.resize(np);
+        CE_CUDA(cudaMemcpyAsync(s->alpha32.data(), alpha, (size_t)np * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        s->d_fgrid32 = (float*)grid;
+    }
+    CE_CUDA(cudaStreamSynchronize(s->stream));
+    if (!f64)
+        for (int p = 0; p < s->n_plants; ++p)
+            if (hbad[s->grid_of(p)])
+                s->plant_err[p] = std::format("allmargin: plant has no finite nonzero gain at crossover = {} rad/s", c.crossover);
 }
 
 // Select the simulation kernel of every plant.  CE_SIM_SPECIALISED compiles
@@ -589,14 +536,8 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     s->n_plants = n_plants;
     s->plants.resize(n_plants);
     s->plant_err.assign(n_plants, std::string());
-    s->alpha32.assign(n_plants, 0.0f);
-    s->alpha64.assign(n_plants, 0.0);
-    s->fgrid32.assign((size_t)n_plants * c.freq * 8, 0.0f);
-    s->fgrid64.assign((size_t)n_plants * c.freq * 8, 0.0);
-    for (int p = 0; p < n_plants; ++p) {
-        build_plant(c, *plant, p, s->plants[p]);
-        build_fgrid(s.get(), p);
-    }
+    s->grid_np = c.serial ? n_plants : 1;
+    for (int p = 0; p < n_plants; ++p) build_plant(c, *plant, p, s->plants[p]);
     CE_CUDA(cudaGetDevice(&s->device));
     CE_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     int prio_least = 0, prio_greatest = 0;
@@ -609,10 +550,7 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig[k], cudaEventDisableTiming));
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_nom[k], cudaEventDisableTiming));
     }
-    CE_CUDA(cudaMalloc((void**)&s->d_fgrid32, s->fgrid32.size() * sizeof(float)));
-    CE_CUDA(cudaMalloc((void**)&s->d_fgrid64, s->fgrid64.size() * sizeof(double)));
-    CE_CUDA(cudaMemcpy(s->d_fgrid32, s->fgrid32.data(), s->fgrid32.size() * sizeof(float), cudaMemcpyHostToDevice));
-    CE_CUDA(cudaMemcpy(s->d_fgrid64, s->fgrid64.data(), s->fgrid64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    build_grids(s.get(), CE_PRECISION_MIXED);
     // Default: the specialised kernel.  CE_SIM_KERNEL=table in the environment
     // selects the table-driven one; if compiling fails the session keeps the
     // table-driven kernel and ce_session_sim_kernel reports which one runs.
@@ -652,6 +590,7 @@ void destroy_session(ce_session* s) {
     s->buf.release();
     if (s->d_fgrid32) cudaFree(s->d_fgrid32);
     if (s->d_fgrid64) cudaFree(s->d_fgrid64);
+    if (s->d_mplant) cudaFree(s->d_mplant);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     for (int k = 0; k < MAX_CHUNKS; ++k) {
         if (s->ev_eig[k]) cudaEventDestroy(s->ev_eig[k]);

@@ -42,6 +42,14 @@ void parse_config(const std::string& text, const std::string& filename, ce_confi
 void decode_instructions(const int32_t* info, int dim, int count, const float* base_params, int n_params,
                          ce_instruction* out);
 
+// Response of `np` margin plants (margin_plant_stride() floats each: m_a,
+// m_b, m_c, m_d) on the z grid zg ((F + 1) x 4: z, arg z; row F the crossover)
+// -> grid (np x F x 8 rows), alpha = 1/|P(crossover)| and bad (no finite
+// nonzero gain there), all in the session precision.
+void launch_plant_grid(int precision, int np, int n, int F, const float* mp, const void* zg, void* grid, void* alpha,
+                       int* bad, cudaStream_t st);
+int margin_plant_stride();
+
 // Kernel launchers (ce_k_*.cu); all enqueue on `st`.
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
                 cudaStream_t st);
