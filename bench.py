@@ -226,6 +226,44 @@ def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int =
             "latency_max_ms": st["latency_max_ms"]}
 
 
+def monte_carlo_bench(n_plants: int, steps: int, warmup: int):
+    """Monte Carlo over plants (one plant per candidate, serial-mode margins): candidates/s of
+    ce_evaluate_plants_device over n_plants plants, inputs resident, CUDA events."""
+    import torch
+    import controllerengine_gb300 as ce
+    from controllerengine_gb300 import synth
+    t0 = time.perf_counter()
+    p = synth.monte_carlo(n_plants=n_plants)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    sess = ce.Session(cfg, p.plant, n_plants=n_plants)
+    setup = time.perf_counter() - t0
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = torch.from_numpy(p.cuda_mx).to(dev)
+    info = torch.from_numpy(p.info_mx).to(dev)
+    out = torch.empty_like(info)
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        sess.evaluate_plants_device(n_plants, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+    torch.cuda.synchronize()
+    ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sess.evaluate_plants_device(n_plants, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    o = out.cpu().numpy()
+    sess.close()
+    sc = o[:, cfg.info_scoring]
+    return {"workload": f"{n_plants} plants: eight-state A, B_u x (1 + 0.1 N(0,1)), BASE_PARAMS x U[0.8, 1.2], "
+                        f"one gain set, T = {cfg.time}, F = {cfg.freq}, serial-mode margins",
+            "candidates_per_s": n_plants * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps,
+            "session_setup_s": setup, "scored_fraction": float(np.mean(sc < cfg.unstable_err))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -241,6 +279,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="Poisson serving run (0: skip)")
+    ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -418,6 +457,8 @@ def main():
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    if rank == 0 and a.mc_plants > 0:
+        line["monte_carlo"] = monte_carlo_bench(a.mc_plants, 2, 1)
     if rank == 0 and a.serve_seconds > 0:
         line["serving"] = serving_bench(problem, cfg, a.serve_seconds)
     if rank == 0 and not a.no_cpu:

@@ -27,7 +27,7 @@ EXPORTED_SYMBOLS = (
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
     "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
-    "ce_server_reset_stats", "RunControllerEngine",
+    "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "RunControllerEngine",
 )
 PENDING = 2
 SIM_TABLE, SIM_SPECIALISED = 0, 1
@@ -138,6 +138,9 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_server_wait.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
     lib.ce_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ce_server_stats)]
     lib.ce_server_reset_stats.argtypes = [C.c_void_p]
+    lib.ce_evaluate_plants.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.ce_evaluate_plants_device.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p]
     lib.ce_session_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.ce_session_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.ce_measure_fma_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]

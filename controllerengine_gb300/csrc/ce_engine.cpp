@@ -91,6 +91,12 @@ struct ce_session {
     std::vector<float> alpha32;   // per margin plant
     std::vector<double> alpha64;
     float* d_mplant = nullptr;    // grid_np x margin_plant_stride() floats
+    void* d_alpha32 = nullptr;    // per margin plant, on the device (per-candidate plants)
+    void* d_alpha64 = nullptr;
+    // per-candidate plants: the plant table (MC_FIELDS x n_plants) and the
+    // simulation kernel compiled for it, built on first use
+    float* d_mc_tab = nullptr;
+    const void* sim_kernel_mc = nullptr;
     float* d_fgrid32 = nullptr;   // grid_np x freq x 8
     double* d_fgrid64 = nullptr;  // built on the first FP64 evaluation
     ce::Buffers buf;
@@ -236,6 +242,44 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
 
 void build_grids(ce_session* s, int precision);
 
+// The per-candidate plant table (MC_FIELDS x n_plants, field-major) and the
+// simulation kernel compiled for it, built on first use.
+void ensure_plant_table(ce_session* s) {
+    if (!s->sim_kernel_mc) {
+        std::string log;
+        s->sim_kernel_mc = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                          s->cfg.discrete_dim <= 4 ? 4 : 8, log, true);
+        if (!s->sim_kernel_mc) fail("per-candidate plants need the specialised simulation kernel: {}", log);
+    }
+    if (s->d_mc_tab) return;
+    const int64_t np = s->n_plants;
+    std::vector<float> t((size_t)MC_FIELDS * np, 0.0f);
+    auto put = [&](int field, int64_t p, float v) { t[(size_t)field * np + p] = v; };
+    for (int64_t p = 0; p < np; ++p) {
+        const Plant& P = s->plants[p];
+        for (int e = 0; e < MAXD * MAXD; ++e) {
+            put(MC_AI + e, p, P.d_ai[e]);
+            put(MC_A + e, p, P.d_a[e]);
+        }
+        for (int i = 0; i < MAXD; ++i) {
+            put(MC_BU + i, p, P.d_bu[i]);
+            put(MC_C + i, p, P.d_c[i]);
+        }
+        for (int e = 0; e < MAXD * MAXW; ++e) put(MC_BW + e, p, P.d_bw[e]);
+        auto consts = [&](const Instr* ins, int cnt, int slot0) {
+            for (int k = 0; k < cnt; ++k) {
+                put(MC_CST + 2 * (slot0 + k), p, ins[k].aval);
+                put(MC_CST + 2 * (slot0 + k) + 1, p, ins[k].bval);
+            }
+        };
+        consts(P.dc, P.n_dc, 0);
+        consts(P.u, P.n_u, MAX_DC);
+        for (int w = 0; w < MAXW; ++w) consts(P.nl[w], P.n_nl[w], MAX_DC + MAX_U + w * MAX_NL);
+    }
+    CE_CUDA(cudaMalloc((void**)&s->d_mc_tab, t.size() * sizeof(float)));
+    CE_CUDA(cudaMemcpy(s->d_mc_tab, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
 // Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
 // CE_CHUNKS (default 2: of 1, 2 and 4 chunks, 2 measured fastest on the
 // eight-state workload of 65,536 candidates).
@@ -251,18 +295,35 @@ int n_chunks(int64_t n) {
 }
 
 // One evaluation: gains and info rows already on the device in d_gains / d_info.
+// With per_candidate, candidate c uses plant `plant + c` (its values from the
+// plant table; the instruction structure and the observer model are shared).
 void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
-                  bool traj) {
-    if (!s->plant_err[plant].empty()) throw std::runtime_error(s->plant_err[plant]);
+                  bool traj, bool per_candidate = false) {
+    const int64_t np_used = per_candidate ? n : 1;
+    for (int64_t q = 0; q < np_used; ++q)
+        if (!s->plant_err[plant + q].empty()) throw std::runtime_error(s->plant_err[plant + q]);
     const int prec = s->precision;
     if (prec == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
+    if (per_candidate) {
+        if (prec != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
+        ensure_plant_table(s);
+    }
     ensure_buffers(s, n, traj);
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
     r.store_traj = traj ? 1 : 0;
+    if (per_candidate) {
+        r.mc.tab = s->d_mc_tab;
+        r.mc.np = s->n_plants;
+        r.mc.first = plant;
+        r.mc.grid_stride = s->cfg.serial ? (int64_t)s->cfg.freq * 8 : 0;
+        r.mc.alpha = s->d_alpha32;
+        r.mc.margin = s->cfg.serial ? 1 : 0;
+    }
     const Plant& P = s->plants[plant];
     const size_t goff = (size_t)s->grid_of(plant) * s->cfg.freq * 8;
     const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + goff) : (const void*)(s->d_fgrid32 + goff);
+    const size_t gstep = (size_t)(per_candidate ? r.mc.grid_stride : 0) * (prec == CE_PRECISION_FP64 ? 8 : 4);
     // each launch optionally bracketed by events on the stream it runs on
     auto timed = [&](int stage, cudaStream_t on, auto&& launch) {
         if (!s->profiling) {
@@ -282,7 +343,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // rest of each SM and run alongside.  Large batches are cut into chunks so
     // that the fit of a chunk starts as soon as its eigenvalues are known, while
     // the eigensolves of the next chunks continue.
-    const void* sk = prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
+    const void* sk = per_candidate ? s->sim_kernel_mc : prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
     cudaStream_t fs = s->fast, ss = s->side;
     const int nch = n_chunks(n);
     const int64_t per = (n + nch - 1) / nch;
@@ -292,6 +353,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         off = k * per;
         rc = r;
         rc.n = std::min<int64_t>(per, n - off);
+        rc.mc.first = r.mc.first + off;
     };
     auto at = [](const void* p, int64_t off, size_t bytes) {
         return (void*)((const char*)p + (size_t)off * bytes);
@@ -343,8 +405,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         CE_CUDA(cudaStreamWaitEvent(fs, s->ev_nom[k], 0));
         timed(5, fs, [&] {
-            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, fgrid, d_info + off * iw,
-                         b.sweep_list + off, b.sweep_count + k, b.sweep, fs);
+            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, at(fgrid, off, gstep),
+                         d_info + off * iw, b.sweep_list + off, b.sweep_count + k, b.sweep, fs);
         });
     }
     CE_CUDA(cudaEventRecord(s->ev_done, fs));
@@ -483,7 +545,8 @@ void build_grids(ce_session* s, int precision) {
     CE_CUDA(cudaMalloc(&alpha, (size_t)np * rsz));
     CE_CUDA(cudaMalloc((void**)&bad, (size_t)np * sizeof(int)));
     CE_CUDA(cudaMalloc(&grid, (size_t)np * F * 8 * rsz));
-    std::unique_ptr<void, cudaError_t (*)(void*)> g1(zg, cudaFree), g2(alpha, cudaFree), g3(bad, cudaFree);
+    std::unique_ptr<void, cudaError_t (*)(void*)> g1(zg, cudaFree), g3(bad, cudaFree);
+    (f64 ? s->d_alpha64 : s->d_alpha32) = alpha;
     if (f64) CE_CUDA(cudaMemcpy(zg, z64.data(), z64.size() * sizeof(double), cudaMemcpyHostToDevice));
     else CE_CUDA(cudaMemcpy(zg, z32.data(), z32.size() * sizeof(float), cudaMemcpyHostToDevice));
     launch_plant_grid(precision, np, n, F, s->d_mplant, zg, grid, alpha, bad, s->stream);
@@ -511,12 +574,13 @@ void build_grids(ce_session* s, int precision) {
 void select_sim_kernel(ce_session* s, int kind) {
     std::vector<const void*> ks(s->n_plants, nullptr);
     if (kind == CE_SIM_SPECIALISED) {
-        for (int p = 0; p < s->n_plants; ++p) {
-            std::string log;
-            ks[p] = specialise_sim(s->plants[p], s->cfg.statespace_dim <= 4 ? 4 : 8,
-                                   s->cfg.discrete_dim <= 4 ? 4 : 8, log);
-            if (!ks[p]) fail("specialising the simulation kernel of plant {} failed: {}", p, log);
-        }
+        // the plants of a session share the DC/U/NL tables, so the programs'
+        // structure is the same for all of them: one compiled kernel serves all
+        std::string log;
+        const void* k = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                       s->cfg.discrete_dim <= 4 ? 4 : 8, log);
+        if (!k) fail("specialising the simulation kernel failed: {}", log);
+        ks.assign(s->n_plants, k);
     }
     s->sim_kernel = ks;
     s->sim_kind = kind;
@@ -591,6 +655,9 @@ void destroy_session(ce_session* s) {
     if (s->d_fgrid32) cudaFree(s->d_fgrid32);
     if (s->d_fgrid64) cudaFree(s->d_fgrid64);
     if (s->d_mplant) cudaFree(s->d_mplant);
+    if (s->d_alpha32) cudaFree(s->d_alpha32);
+    if (s->d_alpha64) cudaFree(s->d_alpha64);
+    if (s->d_mc_tab) cudaFree(s->d_mc_tab);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     for (int k = 0; k < MAX_CHUNKS; ++k) {
         if (s->ev_eig[k]) cudaEventDestroy(s->ev_eig[k]);
@@ -609,9 +676,16 @@ void check_eval(ce_session* s, int plant, int64_t n) {
     if (n < 0) fail("candidate count {} is negative", n);
 }
 
+void check_plants(ce_session* s, int first, int64_t n) {
+    check_eval(s, first, n);
+    if (first + n > s->n_plants)
+        fail("plants [{}, {}) exceed the session's {} plants (one plant per candidate)", first, first + n, s->n_plants);
+}
+
 void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, const float* info_in, float* info_out,
-                   const ce_diagnostics* diag) {
-    check_eval(s, plant, n);
+                   const ce_diagnostics* diag, bool per_candidate = false) {
+    if (per_candidate) check_plants(s, plant, n);
+    else check_eval(s, plant, n);
     if (n == 0) return;
     const ce_config& c = s->cfg;
     const bool traj = diag && diag->yplant;
@@ -620,7 +694,7 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
     cudaStream_t st = s->stream;
     CE_CUDA(cudaMemcpyAsync(b.gains, cuda_mx, (size_t)n * c.cuda_mx_width * sizeof(float), cudaMemcpyHostToDevice, st));
     CE_CUDA(cudaMemcpyAsync(b.info, info_in, (size_t)n * c.info_mx_width * sizeof(float), cudaMemcpyHostToDevice, st));
-    run_pipeline(s, plant, n, b.gains, b.info, st, traj);
+    run_pipeline(s, plant, n, b.gains, b.info, st, traj, per_candidate);
     CE_CUDA(cudaMemcpyAsync(info_out, b.info, (size_t)n * c.info_mx_width * sizeof(float), cudaMemcpyDeviceToHost, st));
     const int nt = c.total_dim;
     const bool f64 = s->precision == CE_PRECISION_FP64;
@@ -912,6 +986,24 @@ CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n, 
             CE_CUDA(cudaMemcpyAsync(d_info_out, d_info_in, (size_t)n * s->cfg.info_mx_width * sizeof(float),
                                     cudaMemcpyDeviceToDevice, st));
         run_pipeline(s, plant_index, n, d_cuda_mx, d_info_out, st, false);
+    });
+}
+
+CE_EXPORT int ce_evaluate_plants(ce_session* s, int32_t first_plant, int64_t n, const float* cuda_mx,
+                                 const float* info_in, float* info_out) {
+    return guarded([&] { evaluate_host(s, first_plant, n, cuda_mx, info_in, info_out, nullptr, true); });
+}
+
+CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int64_t n, const float* d_cuda_mx,
+                                        const float* d_info_in, float* d_info_out, void* stream) {
+    return guarded([&] {
+        check_plants(s, first_plant, n);
+        if (n == 0) return;
+        cudaStream_t st = (cudaStream_t)stream;
+        if (d_info_out != d_info_in)
+            CE_CUDA(cudaMemcpyAsync(d_info_out, d_info_in, (size_t)n * s->cfg.info_mx_width * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, st));
+        run_pipeline(s, first_plant, n, d_cuda_mx, d_info_out, st, false, true);
     });
 }
 

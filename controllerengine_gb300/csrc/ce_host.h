@@ -85,7 +85,7 @@ double measure_fma_rate(bool fp64);
 
 // Simulation kernel specialised to a plant's instruction program (ce_jit.cpp):
 // returns the compiled kernel (cached per program), or nullptr with `log` set.
-const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log);
+const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc = false);
 std::string specialised_source(const Plant& P, int ns, int nd);
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
                             SimSummary* summ, float* traj, cudaStream_t st);

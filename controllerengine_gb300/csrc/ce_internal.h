@@ -19,9 +19,9 @@ typedef long long int64_t;
 
 namespace ce {
 
-constexpr int SIM_BLOCK = 64;
+constexpr int SIM_BLOCK = 64;   // threads per simulation block (one candidate per thread)
 constexpr int MAX_CHUNKS = 8;  // largest number of chunks one evaluation is cut into
-constexpr int SWEEP_FG = 16;   // frequencies per thread in the LU pass of the margin sweep  // threads per simulation block (one candidate per thread)
+constexpr int SWEEP_FG = 16;   // frequencies per thread in the LU pass of the margin sweep
 
 constexpr int MAXS = CE_MAX_STATESPACE_DIM;   // 8
 constexpr int MAXD = CE_MAX_DISCRETE_DIM;     // 8
@@ -54,6 +54,30 @@ struct Plant {
     Instr nl[MAXW][MAX_NL];  // NL columns: 0..nd-1 plant states, MAXD = plant output y
 };
 
+// One plant per candidate (Monte Carlo over plants, or the serial mode's
+// per-round plants evaluated in one launch).  The plants' values live on the
+// device as a structure of arrays -- field f of plant p at tab[f * np + p] --
+// so consecutive candidates read consecutive words; the instruction structure
+// (ops, columns, operand kinds) and the observer model are the launch Plant's,
+// shared by all plants.  Candidate c of an evaluation uses plant first + c.
+constexpr int MC_AI = 0;                      // d_a - I, row stride MAXD
+constexpr int MC_A = MC_AI + MAXD * MAXD;     // d_a
+constexpr int MC_BU = MC_A + MAXD * MAXD;     // d_bu
+constexpr int MC_BW = MC_BU + MAXD;           // d_bw, row stride MAXW
+constexpr int MC_C = MC_BW + MAXD * MAXW;     // d_c
+constexpr int MC_CST = MC_C + MAXD;           // instruction constants, (a, b) per slot
+constexpr int MC_SLOTS = MAX_DC + MAX_U + MAXW * MAX_NL;  // DC k: k; U k: MAX_DC + k; NL w, k: MAX_DC + MAX_U + w MAX_NL + k
+constexpr int MC_FIELDS = MC_CST + 2 * MC_SLOTS;
+
+struct McPlants {
+    const float* tab;    // null: every candidate uses the launch's Plant
+    int64_t np;          // plants in the table (the field stride)
+    int64_t first;       // plant of candidate 0
+    int64_t grid_stride; // elements between consecutive plants' sweep grids (0: one grid for all)
+    const void* alpha;   // per sweep grid: the plant scaling (float or double as the precision)
+    int margin;          // 1: the margin plant is the candidate's plant (serial mode), 0: the Plant's
+};
+
 // Sizes and scalars of one evaluation (the slice of the config the kernels read,
 // cf. EngineParams, ref: src/config.cu:84-104).
 struct Run {
@@ -66,6 +90,7 @@ struct Run {
     float bandwidth, damping, overshoot, sse, target_gm, target_pm, target_b, alpha;
     double alpha64;  // alpha of the FP64 form
     int store_traj;  // also write the full trajectory (diagnostics)
+    McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
 };
 
 // Per-candidate simulation summary (the parts of the trajectory that modalsetup

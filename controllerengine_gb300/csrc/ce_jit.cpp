@@ -8,7 +8,9 @@
 // with the shared step loop (ce_sim_body.cuh) for the exact plant dimensions.
 // The instruction *structure* (op, column, operand kinds) is compiled in; the
 // constant operands stay in the launch parameters, so every round of a serial
-// run (same program, different BASE_PARAMS) shares one compiled kernel.  Each
+// run (same program, different BASE_PARAMS) shares one compiled kernel.  The
+// per-candidate-plant form (`mc`) reads the constants and the plant matrices
+// from the candidate's row of the plant table instead.  Each
 // generated instruction performs exactly the operations of the interpreter
 // (ref: src/main.cu:260-291) with the same roundings, so results are
 // bit-identical to the table-driven kernel's.  Compiled kernels are cached per
@@ -36,10 +38,14 @@ namespace {
 std::mutex g_jit_mu;
 std::map<std::string, const void*> g_jit_cache;  // source -> cudaKernel_t
 
-std::string fmt_chain(const char* fname, const Instr* ins, int n, bool seed, bool nl, const char* table) {
+// One chain as straight-line code.  Constant operands come from the launch's
+// Plant, or with `mc` from the candidate's plant-table row (slot numbering of
+// MC_CST: `slot0` is the chain's first slot).
+std::string fmt_chain(const char* fname, const Instr* ins, int n, bool seed, bool nl, const char* table, int slot0,
+                      bool mc) {
     std::ostringstream o;
-    o << "template <int NSRC>\n__device__ __forceinline__ float " << fname
-      << "(const ce::Plant& P, const float (&xs)[NSRC], float y, float seed) {\n    float r = 0.0f;\n";
+    o << "template <int NSRC, class Lc>\n__device__ __forceinline__ float " << fname
+      << "(const ce::Plant& P, const Lc& L, const float (&xs)[NSRC], float y, float seed) {\n    float r = 0.0f;\n";
     for (int k = 0; k < n; ++k) {
         const Instr& I = ins[k];
         o << "    {  // op " << I.op << " col " << I.col << " kinds " << I.akind << "," << I.bkind << "\n";
@@ -49,7 +55,8 @@ std::string fmt_chain(const char* fname, const Instr* ins, int n, bool seed, boo
         else o << "        const float prev = r;\n";
         auto operand = [&](int kind, const char* field) {
             std::ostringstream e;
-            if (kind == CE_OPERAND_CONST) e << "P." << table << "[" << k << "]." << field;
+            if (kind == CE_OPERAND_CONST && mc) e << "L.c(" << 2 * (slot0 + k) + (field[0] == 'b' ? 1 : 0) << ")";
+            else if (kind == CE_OPERAND_CONST) e << "P." << table << "[" << k << "]." << field;
             else if (kind == CE_OPERAND_STATE) e << "pos";
             else e << "prev";
             return e.str();
@@ -66,32 +73,35 @@ std::string fmt_chain(const char* fname, const Instr* ins, int n, bool seed, boo
         }
         o << "        (void)pos;\n    }\n";
     }
-    o << "    (void)seed; (void)y; (void)xs; (void)P;\n    return r;\n}\n\n";
+    o << "    (void)seed; (void)y; (void)xs; (void)P; (void)L;\n    return r;\n}\n\n";
     return o.str();
 }
 
-std::string jit_source(const Plant& P, int ns, int nd) {
+std::string jit_source(const Plant& P, int ns, int nd, bool mc) {
     std::ostringstream o;
     o << "#include \"ce_sim_body.cuh\"\n\nnamespace cejit {\n\n";
-    o << fmt_chain("dc", P.dc, P.n_dc, false, false, "dc");
-    o << fmt_chain("u", P.u, P.n_u, true, false, "u");
+    o << fmt_chain("dc", P.dc, P.n_dc, false, false, "dc", 0, mc);
+    o << fmt_chain("u", P.u, P.n_u, true, false, "u", MAX_DC, mc);
     for (int k = 0; k < MAXW; ++k) {
         const std::string fn = "nl" + std::to_string(k), tab = "nl[" + std::to_string(k) + "]";
-        o << fmt_chain(fn.c_str(), P.nl[k], P.n_nl[k], false, true, tab.c_str());
+        o << fmt_chain(fn.c_str(), P.nl[k], P.n_nl[k], false, true, tab.c_str(), MAX_DC + MAX_U + k * MAX_NL, mc);
     }
     o << "struct Chains {\n"
          "    static constexpr bool kSmem = false;\n"
          "    template <int NDC>\n"
-         "    __device__ static __forceinline__ float dc(const ce::Plant& P, const float (&xp)[NDC], const float*) {\n"
-         "        return cejit::dc(P, xp, 0.0f, 0.0f);\n    }\n"
-         "    template <int NSC>\n"
-         "    __device__ static __forceinline__ float u(const ce::Plant& P, const float (&xh)[NSC], const float*, float seed) {\n"
-         "        return cejit::u(P, xh, 0.0f, seed);\n    }\n"
-         "    template <int NDC>\n"
-         "    __device__ static __forceinline__ void nl(const ce::Plant& P, const float (&xp)[NDC], float y, const float*,\n"
-         "                                              float (&W)[ce::MAXW]) {\n"
-         "        W[0] = cejit::nl0(P, xp, y, 0.0f);\n        W[1] = cejit::nl1(P, xp, y, 0.0f);\n"
-         "        W[2] = cejit::nl2(P, xp, y, 0.0f);\n        W[3] = cejit::nl3(P, xp, y, 0.0f);\n    }\n};\n\n"
+      << (mc ? "    using Local = ce::McLocal<NDC>;\n" : "    using Local = ce::BankLocal<NDC>;\n")
+      << "    template <int NDC, class Lc>\n"
+         "    __device__ static __forceinline__ float dc(const ce::Plant& P, const Lc& L, const float (&xp)[NDC], const float*) {\n"
+         "        return cejit::dc(P, L, xp, 0.0f, 0.0f);\n    }\n"
+         "    template <int NSC, class Lc>\n"
+         "    __device__ static __forceinline__ float u(const ce::Plant& P, const Lc& L, const float (&xh)[NSC], const float*,\n"
+         "                                              float seed) {\n"
+         "        return cejit::u(P, L, xh, 0.0f, seed);\n    }\n"
+         "    template <int NDC, class Lc>\n"
+         "    __device__ static __forceinline__ void nl(const ce::Plant& P, const Lc& L, const float (&xp)[NDC], float y,\n"
+         "                                              const float*, float (&W)[ce::MAXW]) {\n"
+         "        W[0] = cejit::nl0(P, L, xp, y, 0.0f);\n        W[1] = cejit::nl1(P, L, xp, y, 0.0f);\n"
+         "        W[2] = cejit::nl2(P, L, xp, y, 0.0f);\n        W[3] = cejit::nl3(P, L, xp, y, 0.0f);\n    }\n};\n\n"
          "}  // namespace cejit\n\n";
     o << "extern \"C\" __global__ void __launch_bounds__(ce::SIM_BLOCK) ce_sim_specialised(\n"
          "    const ce::Run run, const __grid_constant__ ce::Plant P, const float* __restrict__ gains,\n"
@@ -152,8 +162,8 @@ const void* compile(const std::string& src, std::string& log) {
 
 }  // namespace
 
-const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log) {
-    const std::string src = jit_source(P, ns, nd);
+const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc) {
+    const std::string src = jit_source(P, ns, nd, mc);
     std::lock_guard<std::mutex> g(g_jit_mu);
     auto it = g_jit_cache.find(src);
     if (it != g_jit_cache.end()) return it->second;
@@ -162,7 +172,7 @@ const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log) {
     return k;
 }
 
-std::string specialised_source(const Plant& P, int ns, int nd) { return jit_source(P, ns, nd); }
+std::string specialised_source(const Plant& P, int ns, int nd) { return jit_source(P, ns, nd, false); }
 
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
                             SimSummary* summ, float* traj, cudaStream_t st) {

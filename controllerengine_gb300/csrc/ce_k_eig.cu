@@ -631,8 +631,27 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
     return true;
 }
 
+// Plant values (discrete A, B_u, C) of a candidate: the launch's Plant, or the
+// candidate's row of the per-candidate plant table.
+struct BankPlantValues {
+    const Plant& P;
+    __device__ __forceinline__ float a(int i, int j) const { return P.d_a[i * MAXD + j]; }
+    __device__ __forceinline__ float bu(int i) const { return P.d_bu[i]; }
+    __device__ __forceinline__ float c(int j) const { return P.d_c[j]; }
+};
+struct TablePlantValues {
+    const float* t;
+    int64_t np, p;
+    __device__ __forceinline__ float f(int field) const { return t[(int64_t)field * np + p]; }
+    __device__ __forceinline__ float a(int i, int j) const { return f(MC_A + i * MAXD + j); }
+    __device__ __forceinline__ float bu(int i) const { return f(MC_BU + i); }
+    __device__ __forceinline__ float c(int j) const { return f(MC_C + j); }
+};
+
 // LIN_A = [A - B K - L (C - D K),  L Cd ;  -Bu K,  Ad]   (ref: src/eigensetup.cu:19-42)
-__device__ __forceinline__ float lina_entry(const Plant& P, const float* K, const float* L, int ns, int i, int j) {
+template <class PV>
+__device__ __forceinline__ float lina_entry(const Plant& P, const PV& pv, const float* K, const float* L, int ns,
+                                            int i, int j) {
     if (i < ns && j < ns) {
         const float pbk = __fmaf_rn(P.ss_b[i], K[j], 0.0f);
         const float pdk = __fmaf_rn(P.ss_d, K[j], 0.0f);
@@ -640,9 +659,9 @@ __device__ __forceinline__ float lina_entry(const Plant& P, const float* K, cons
         const float lpc = __fmaf_rn(L[i], pcpd, 0.0f);
         return __fsub_rn(__fsub_rn(P.ss_a[i * MAXS + j], pbk), lpc);
     }
-    if (i < ns) return __fmaf_rn(L[i], P.d_c[j - ns], 0.0f);
-    if (j < ns) return -__fmaf_rn(P.d_bu[i - ns], K[j], 0.0f);
-    return P.d_a[(i - ns) * MAXD + (j - ns)];
+    if (i < ns) return __fmaf_rn(L[i], pv.c(j - ns), 0.0f);
+    if (j < ns) return -__fmaf_rn(pv.bu(i - ns), K[j], 0.0f);
+    return pv.a(i - ns, j - ns);
 }
 
 template <int EQ>
@@ -700,12 +719,16 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
             }
             SMat T{smem + m, nt, eig_stride<EQ>()};
             float* lrow = lina + c * (int64_t)(nt * nt);
-            for (int e = Q.q; e < nt * nt; e += EQ) {
-                const int i = e / nt, j = e % nt;
-                const float v = lina_entry(P, K, L, ns, i, j);
-                lrow[e] = v;
-                T(i, j) = (double)v;
-            }
+            auto fill = [&](const auto& pv) {
+                for (int e = Q.q; e < nt * nt; e += EQ) {
+                    const int i = e / nt, j = e % nt;
+                    const float v = lina_entry(P, pv, K, L, ns, i, j);
+                    lrow[e] = v;
+                    T(i, j) = (double)v;
+                }
+            };
+            if (run.mc.tab) fill(TablePlantValues{run.mc.tab, run.mc.np, run.mc.first + c});
+            else fill(BankPlantValues{P});
             Q.sync();
             float* out = eig32 + c * (int64_t)(2 * nt);
             float mx = 0.0f;
@@ -796,20 +819,26 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
             const float* row = gains + c * run.cuda_w;
             const float* la = lina + c * (int64_t)(nt * nt);
             SMat T{smem + m, n2, eig_stride<EQ>()};
+            // margin plant: the Plant's (observer model in batch mode, the round's plant in
+            // serial mode), or in serial mode with per-candidate plants the candidate's own
+            const TablePlantValues tv{run.mc.tab, run.mc.np, run.mc.first + c};
+            const bool own = run.mc.tab && run.mc.margin;
             for (int e = Q.q; e < ns * ns; e += EQ) {
                 const int i = e / ns, j = e % ns;
                 const float Li = row[ns + i];
                 const float Kj = row[j];
+                const float md = own ? 0.0f : P.m_d, mcj = own ? tv.c(j) : P.m_c[j], mbi = own ? tv.bu(i) : P.m_b[i];
+                const float maij = own ? tv.a(i, j) : P.m_a[i * MAXS + j];
                 if (fp64_form) {
-                    T(i, j) = (double)la[i * nt + j] - (double)P.m_d * (double)Li * (double)Kj;
-                    T(i, ns + j) = -((double)Li * (double)P.m_c[j]);
-                    T(ns + i, j) = (double)P.m_b[i] * (double)Kj;
+                    T(i, j) = (double)la[i * nt + j] - (double)md * (double)Li * (double)Kj;
+                    T(i, ns + j) = -((double)Li * (double)mcj);
+                    T(ns + i, j) = (double)mbi * (double)Kj;
                 } else {
-                    T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(P.m_d, Li), Kj));
-                    T(i, ns + j) = (double)(-__fmul_rn(Li, P.m_c[j]));
-                    T(ns + i, j) = (double)__fmul_rn(P.m_b[i], Kj);
+                    T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(md, Li), Kj));
+                    T(i, ns + j) = (double)(-__fmul_rn(Li, mcj));
+                    T(ns + i, j) = (double)__fmul_rn(mbi, Kj);
                 }
-                T(ns + i, ns + j) = (double)P.m_a[i * MAXS + j];
+                T(ns + i, ns + j) = (double)maij;
             }
             Q.sync();
             bool stable = true;

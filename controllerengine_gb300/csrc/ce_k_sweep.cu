@@ -108,11 +108,15 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const
 #pragma unroll
         for (int j = 0; j < NSC; ++j) As[i * NSC + j][tid] = (i < ns && j < ns) ? R(la[i * nt + j]) : R(0);
     }
-    const R ALPHA = sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64);
+    // per-candidate plants in serial mode: the candidate's own grid and scaling
+    const bool own = run.mc.tab && run.mc.grid_stride;
+    const R ALPHA = own ? ((const R*)run.mc.alpha)[run.mc.first + c]
+                        : (sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64));
+    const R* fgc = fgrid + (own ? c * run.mc.grid_stride : 0);
     R bmin = R(1);
     int first_bad = INT_MAX;
     for (int w = w0; w < w1; ++w) {
-        const R* fg = fgrid + 8 * (int64_t)w;
+        const R* fg = fgc + 8 * (int64_t)w;
         if (fg[6] == R(0)) {
             first_bad = w;
             break;

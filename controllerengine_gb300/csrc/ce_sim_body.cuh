@@ -29,11 +29,49 @@
 //
 // Chains policy: Chains::kSmem says whether the chains read their sources from
 // the per-thread shared-memory rows srcP (plant states, y in row MAXD) and srcH
-// (observer states); dc / u / nl evaluate the DC, U and NL_k chains.
+// (observer states); dc / u / nl evaluate the DC, U and NL_k chains;
+// Chains::Local<NDC> supplies the candidate's plant values (BankLocal: the
+// launch's Plant; McLocal: the candidate's row of the per-candidate plant table).
 #pragma once
 #include "ce_device.cuh"
 
 namespace ce {
+
+// The plant values of one candidate: the launch's Plant (the constant bank)...
+template <int NDC>
+struct BankLocal {
+    const Plant& P;
+    __device__ __forceinline__ BankLocal(const Run&, const Plant& p, int64_t) : P(p) {}
+    __device__ __forceinline__ float ai(int i, int j) const { return P.d_ai[i * MAXD + j]; }
+    __device__ __forceinline__ float bu(int i) const { return P.d_bu[i]; }
+    __device__ __forceinline__ float bw(int i, int k) const { return P.d_bw[i * MAXW + k]; }
+};
+
+// ...or the candidate's own plant from the per-candidate plant table, loaded
+// into registers once per candidate (instruction constants that the program
+// never uses are never loaded).
+template <int NDC>
+struct McLocal {
+    float ai_[NDC * NDC], bu_[NDC], bw_[NDC * MAXW], cst_[2 * MC_SLOTS];
+    __device__ __forceinline__ McLocal(const Run& run, const Plant&, int64_t c) {
+        const float* __restrict__ t = run.mc.tab;
+        const int64_t np = run.mc.np, p = run.mc.first + c;
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) {
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) ai_[i * NDC + j] = t[(int64_t)(MC_AI + i * MAXD + j) * np + p];
+            bu_[i] = t[(int64_t)(MC_BU + i) * np + p];
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) bw_[i * MAXW + k] = t[(int64_t)(MC_BW + i * MAXW + k) * np + p];
+        }
+#pragma unroll
+        for (int k = 0; k < 2 * MC_SLOTS; ++k) cst_[k] = t[(int64_t)(MC_CST + k) * np + p];
+    }
+    __device__ __forceinline__ float ai(int i, int j) const { return ai_[i * NDC + j]; }
+    __device__ __forceinline__ float bu(int i) const { return bu_[i]; }
+    __device__ __forceinline__ float bw(int i, int k) const { return bw_[i * MAXW + k]; }
+    __device__ __forceinline__ float c(int k) const { return cst_[k]; }
+};
 
 template <int NSC, int NDC, class Chains>
 __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const float* __restrict__ gains,
@@ -45,6 +83,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
     const int tid = threadIdx.x;
     const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
     if (c >= run.n) return;  // each thread only touches its own column of the shared rows
+    const typename Chains::template Local<NDC> Lc(run, P, c);
 
     const int ns = run.ns;
     const float* row = gains + c * run.cuda_w;
@@ -79,7 +118,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
         }
 
         // plant output
-        const float y = Chains::dc(P, xp_hi, &srcP[0][tid]);
+        const float y = Chains::dc(P, Lc, xp_hi, &srcP[0][tid]);
         if constexpr (Chains::kSmem) srcP[Chains::kSmem ? MAXD : 0][tid] = y;
 
         // outputs: fit window, steady-state sum, extremes, optional full trajectory
@@ -112,7 +151,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
         if (NSC < MAXS) kx = __fadd_rn(kx, padS);
         const float ref = t < run.ref_step_id ? 0.0f : run.ref_amp;
         const float u_raw = __fmaf_rn(N, ref, -kx);
-        const float u = Chains::u(P, xh_hi, &srcH[0][tid], u_raw);
+        const float u = Chains::u(P, Lc, xh_hi, &srcH[0][tid], u_raw);
 
         // observer output error
         float yh = 0.0f;
@@ -153,20 +192,20 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
 
         // nonlinear terms over [xp_hi, y]
         float W[MAXW];
-        Chains::nl(P, xp_hi, y, &srcP[0][tid], W);
+        Chains::nl(P, Lc, xp_hi, y, &srcP[0][tid], W);
 
         // plant increment (Ad-I)xp + Bu u + Bw W, then double-float add
         float ph[NDC], pl[NDC];
 #pragma unroll
         for (int i = 0; i < NDC; ++i) {
-            float h = __fmul_rn(P.d_bu[i], u);
+            float h = __fmul_rn(Lc.bu(i), u);
 #pragma unroll
-            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(P.d_bw[i * MAXW + k], W[k], h);
+            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(Lc.bw(i, k), W[k], h);
             float l = 0.0f;
 #pragma unroll
-            for (int j = 0; j < NDC; ++j) h = __fmaf_rn(P.d_ai[i * MAXD + j], xp_hi[j], h);
+            for (int j = 0; j < NDC; ++j) h = __fmaf_rn(Lc.ai(i, j), xp_hi[j], h);
 #pragma unroll
-            for (int j = 0; j < NDC; ++j) l = __fmaf_rn(P.d_ai[i * MAXD + j], xp_lo[j], l);
+            for (int j = 0; j < NDC; ++j) l = __fmaf_rn(Lc.ai(i, j), xp_lo[j], l);
             if (NDC < MAXD) {
                 h = __fadd_rn(h, padD);
                 l = __fadd_rn(l, padD);
@@ -198,15 +237,18 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
 struct TableChains {
     static constexpr bool kSmem = true;
     template <int NDC>
-    __device__ static __forceinline__ float dc(const Plant& P, const float (&)[NDC], const float* sp) {
+    using Local = BankLocal<NDC>;
+    template <int NDC, class Lc>
+    __device__ static __forceinline__ float dc(const Plant& P, const Lc&, const float (&)[NDC], const float* sp) {
         return run_chain_sm<float, MAX_DC, false>(P.dc, P.n_dc, sp, SIM_BLOCK, 0.0f);
     }
-    template <int NSC>
-    __device__ static __forceinline__ float u(const Plant& P, const float (&)[NSC], const float* sh, float seed) {
+    template <int NSC, class Lc>
+    __device__ static __forceinline__ float u(const Plant& P, const Lc&, const float (&)[NSC], const float* sh,
+                                              float seed) {
         return run_chain_sm<float, MAX_U, true>(P.u, P.n_u, sh, SIM_BLOCK, seed);
     }
-    template <int NDC>
-    __device__ static __forceinline__ void nl(const Plant& P, const float (&)[NDC], float, const float* sp,
+    template <int NDC, class Lc>
+    __device__ static __forceinline__ void nl(const Plant& P, const Lc&, const float (&)[NDC], float, const float* sp,
                                               float (&W)[MAXW]) {
 #pragma unroll
         for (int k = 0; k < MAXW; ++k) W[k] = run_chain_sm<float, MAX_NL, false>(P.nl[k], P.n_nl[k], sp, SIM_BLOCK, 0.0f);

@@ -254,6 +254,18 @@ class Session:
         _check(_lib().ce_evaluate_diagnostics(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(d)))
         return out, arrs
 
+    def evaluate_plants(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, first_plant: int = 0) -> np.ndarray:
+        """One plant per candidate: row c uses plant first_plant + c (ce_evaluate_plants)."""
+        g, i, n = self._rows(cuda_mx, info_in)
+        out = np.empty_like(i)
+        _check(_lib().ce_evaluate_plants(self._h, first_plant, n, _fptr(g), _fptr(i), _fptr(out)))
+        return out
+
+    def evaluate_plants_device(self, n: int, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0,
+                               first_plant: int = 0):
+        _check(_lib().ce_evaluate_plants_device(self._h, first_plant, n, C.c_void_p(d_cuda_mx), C.c_void_p(d_info_in),
+                                                C.c_void_p(d_info_out), C.c_void_p(stream)))
+
     def evaluate_device(self, n: int, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0,
                         plant_index: int = 0):
         """Enqueue on `stream`: device pointers (ints), no synchronisation."""

@@ -194,6 +194,21 @@ CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n,
                                  const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
                                  void* stream);
 
+/* One plant per candidate (no counterpart in the reference, whose mode =
+ * serial runs one plant per round, ref: src/main.cu:341-383, 467-559):
+ * candidate c of the batch uses plant first_plant + c of the session
+ * (first_plant + n <= n_plants).  The plants share the instruction structure
+ * and the observer model; their discrete matrices and BASE_PARAMS differ.  In
+ * mode = serial the margin check and the sweep use each candidate's own plant,
+ * as a serial round would.  Rows are bit-identical to evaluating each
+ * candidate with ce_evaluate(s, first_plant + c, 1, ...).  Mixed precision and
+ * the specialised simulation kernel (compiled for the plant table on first
+ * use) only. */
+CE_EXPORT int ce_evaluate_plants(ce_session* s, int32_t first_plant, int64_t n, const float* cuda_mx,
+                                 const float* info_in, float* info_out);
+CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int64_t n, const float* d_cuda_mx,
+                                        const float* d_info_in, float* d_info_out, void* stream);
+
 /* Launches of this library's kernels since the session was created. */
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s);
 
