@@ -2,16 +2,17 @@
 //
 // The reference's orchestrator (ref: src/main.cu:385-582) runs every stage
 // synchronously, bouncing LIN_A, eigenvalues and AtA/Atb through host memory
-// for the Eigen stages.  Here a session keeps the decoded plant tables and the
-// plant's frequency response on the host (they travel to the kernels in the
-// launch parameters) and a grow-only set of device scratch buffers; one
-// evaluation is six kernel launches, the two FP64 eigensolves on a second
-// stream so they overlap the FP32 simulation and modal fit:
+// for the Eigen stages.  Here a session keeps the decoded plant tables on the
+// host (they travel to the kernels in the launch parameters), the margin
+// plants' sweep grids on the device and a grow-only set of device scratch
+// buffers.  One evaluation forks the caller's stream onto two session streams:
 //
-//   fork ─┬─ k_lina_eig (FP64) ──┬── k_nominal (FP64) ──────────┐
-//         └─ k_sim      (FP32) ──┴─ k_fit ─ k_modal (FP32) ──────┴─ k_sweep
+//   high priority:  k_lina_eig (FP64, persistent) ── k_nominal (FP64, persistent)
+//   low priority:   k_sim ─ [eig ready] k_fit_classify ─ k_fit ─ k_modal ─ [nominal ready] k_sweep_*
 //
-// Only gains in and cost rows out cross the host boundary.
+// and joins back; batches of >= 32,768 candidates run the per-candidate stages
+// in two chunks so the fit of the first starts while the second's eigensolve
+// runs.  Only gains in and cost rows out cross the host boundary.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>

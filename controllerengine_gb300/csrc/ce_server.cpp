@@ -87,7 +87,6 @@ struct ce_server {
     // statistics
     int64_t batches = 0, batched_rows = 0, completed = 0;
     std::vector<double> latency_ms;  // completed requests, in completion order
-    std::string fatal;
 };
 
 namespace ce {
