@@ -174,28 +174,46 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int = 16384, seed: int = 7):
-    """Request serving (ce_server_*): requests of U[256, 16384] candidates of the bench plant.
-    Saturation: 48 requests submitted at once, candidates/s until all are done.  Latency:
-    Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of submit -> results in the
-    caller's buffer (measured by the server)."""
+def serving_models(k: int = 16, seed: int = 5):
+    """The serving mix: k plants drawn as in the uneven-shape workload (dimensions 2..8, 0-4
+    nonlinear terms, 50-400 sweep points) with horizons log-uniform in [1e3, 1e4] steps, each
+    with 16,384 candidate rows."""
+    from controllerengine_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(k):
+        T = int(np.exp(rng.uniform(np.log(1e3), np.log(1e4))))
+        out.append(synth.random_shape(1000 + m, n=16384, time=T, freq=int(rng.integers(50, 401))))
+    return out
+
+
+def serving_bench(problems, seconds: float, lanes: int = 2, max_batch: int = 16384, seed: int = 7):
+    """Request serving (ce_server_*): requests of U[256, 16384] candidates on a model drawn
+    uniformly from `problems`.  Saturation: 48 requests submitted at once, candidates/s until
+    all are done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of
+    submit -> results in the caller's buffer (measured by the server)."""
     import controllerengine_gb300 as ce
     rng = np.random.default_rng(seed)
-    n_all = problem.cuda_mx.shape[0]
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in problems]
 
     def draw():
+        k = int(rng.integers(0, len(problems)))
+        p = problems[k]
         m = int(rng.integers(256, 16385))
-        a = int(rng.integers(0, n_all - m + 1))
-        return problem.cuda_mx[a:a + m], problem.info_mx[a:a + m]
+        a = int(rng.integers(0, p.cuda_mx.shape[0] - m + 1))
+        return k, p.cuda_mx[a:a + m], p.info_mx[a:a + m]
 
-    with ce.Server(cfg, problem.plant, max_batch=max_batch, lanes=lanes) as srv:
-        # warm-up: every lane sizes its scratch for a full batch
-        for r in [srv.submit(problem.cuda_mx, problem.info_mx) for _ in range(lanes)]:
-            r.wait()
+    models = [(c, p.plant, 1) for c, p in zip(cfgs, problems)]
+    with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes) as srv:
+        # warm-up: every lane sizes its scratch for a full batch of every model
+        for _ in range(lanes):
+            for r in [srv.submit(p.cuda_mx[:max_batch], p.info_mx[:max_batch], model=k)
+                      for k, p in enumerate(problems)]:
+                r.wait()
         reqs = [draw() for _ in range(48)]
-        total = sum(g.shape[0] for g, _ in reqs)
+        total = sum(g.shape[0] for _, g, _ in reqs)
         t0 = time.perf_counter()
-        hs = [srv.submit(g, i) for g, i in reqs]
+        hs = [srv.submit(g, i, model=k) for k, g, i in reqs]
         for h in hs:
             h.wait()
         sat = total / (time.perf_counter() - t0)
@@ -209,15 +227,18 @@ def serving_bench(problem, cfg, seconds: float, lanes: int = 2, max_batch: int =
             now = time.perf_counter()
             if now < t_next:
                 time.sleep(t_next - now)
-            g, i = draw()
+            k, g, i = draw()
             offered += g.shape[0]
-            hs.append(srv.submit(g, i))
+            hs.append(srv.submit(g, i, model=k))
             t_next += rng.exponential(1.0 / rate)
         for h in hs:
             h.wait()
         wall = time.perf_counter() - t0
         st = srv.stats()
-    return {"request_sizes": "U[256, 16384] candidates of the bench plant (T = 10,000, F = 400)",
+    shapes = sorted({(c.statespace_dim, c.discrete_dim, c.time, c.freq) for c in cfgs})
+    return {"request_mix": f"U[256, 16384] candidates on one of {len(problems)} plants of the uneven-shape "
+                           "workload (dims 2..8, horizons 1e3..1e4, 50..400 sweep points)",
+            "models": [list(x) for x in shapes],
             "lanes": lanes, "max_batch": st["capacity"], "saturation_candidates_per_s": sat,
             "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
             "requests": st["completed"], "achieved_candidates_per_s": offered / wall,
@@ -460,7 +481,7 @@ def main():
     if rank == 0 and a.mc_plants > 0:
         line["monte_carlo"] = monte_carlo_bench(a.mc_plants, 2, 1)
     if rank == 0 and a.serve_seconds > 0:
-        line["serving"] = serving_bench(problem, cfg, a.serve_seconds)
+        line["serving"] = serving_bench(serving_models(), a.serve_seconds)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

@@ -27,7 +27,8 @@ EXPORTED_SYMBOLS = (
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
     "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
-    "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "RunControllerEngine",
+    "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
+    "ce_server_submit_model", "RunControllerEngine",
 )
 PENDING = 2
 SIM_TABLE, SIM_SPECIALISED = 0, 1
@@ -131,6 +132,10 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_sim_specialised_source.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]
     lib.ce_server_create.argtypes = [C.POINTER(ce_config), C.POINTER(ce_plant), C.c_int32,
                                      C.POINTER(ce_server_options), C.POINTER(C.c_void_p)]
+    lib.ce_server_create_models.argtypes = [C.POINTER(ce_config), C.POINTER(ce_plant), C.POINTER(C.c_int32), C.c_int32,
+                                            C.POINTER(ce_server_options), C.POINTER(C.c_void_p)]
+    lib.ce_server_submit_model.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.POINTER(C.c_int64)]
     lib.ce_server_destroy.argtypes = [C.c_void_p]
     lib.ce_server_destroy.restype = None
     lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,

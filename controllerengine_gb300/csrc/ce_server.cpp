@@ -40,6 +40,7 @@ using Clock = std::chrono::steady_clock;
 
 struct Request {
     int64_t id = 0;
+    int model = 0;
     int plant = 0;
     int64_t n = 0;
     const float* gains = nullptr;
@@ -58,7 +59,7 @@ struct Piece {
 };
 
 struct Lane {
-    ce_session* sess = nullptr;
+    std::vector<ce_session*> sess;  // one per model
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     float* d_gains = nullptr;
@@ -72,9 +73,9 @@ struct Lane {
 }  // namespace
 
 struct ce_server {
-    ce_config cfg{};
-    int n_plants = 0;
-    int64_t capacity = 0;  // candidates per batch (per lane)
+    std::vector<ce_config> cfg;  // per model
+    std::vector<int> n_plants;   // per model
+    int64_t capacity = 0;        // candidates per batch (per lane)
     int max_wait_us = 0;
     std::vector<Lane> lanes;
     std::mutex mu;
@@ -109,10 +110,11 @@ int64_t bytes_per_candidate(const ce_config& c) {
 }
 
 void complete_lane(ce_server* s, Lane& L) {
-    const int64_t iw = s->cfg.info_mx_width;
     // each piece's rows go to a disjoint slice of its request's output
-    for (const Piece& p : L.pieces)
+    for (const Piece& p : L.pieces) {
+        const int64_t iw = s->cfg[p.req->model].info_mx_width;
         std::memcpy(p.req->info_out + p.row0 * iw, L.h_info + p.off * iw, (size_t)p.rows * iw * sizeof(float));
+    }
     const auto now = Clock::now();
     std::lock_guard<std::mutex> g(s->mu);
     for (const Piece& p : L.pieces) {
@@ -141,15 +143,18 @@ void fail_pieces(ce_server* s, Lane& L, const std::string& msg) {
     s->cv_done.notify_all();
 }
 
-// Take rows for one batch from the queue (caller holds the lock).
-std::vector<Piece> form_batch(ce_server* s, int& plant) {
+// Take rows for one batch from the queue (caller holds the lock): the oldest
+// request's model and plant, then the queued requests of the same model and
+// plant in arrival order.
+std::vector<Piece> form_batch(ce_server* s, int& model, int& plant) {
     std::vector<Piece> out;
     if (s->queue.empty()) return out;
+    model = s->queue.front()->model;
     plant = s->queue.front()->plant;
     int64_t room = s->capacity, off = 0;
     for (auto it = s->queue.begin(); it != s->queue.end() && room > 0;) {
         Request& r = **it;
-        if (r.plant != plant) {
+        if (r.model != model || r.plant != plant) {
             ++it;
             continue;
         }
@@ -164,8 +169,8 @@ std::vector<Piece> form_batch(ce_server* s, int& plant) {
     return out;
 }
 
-void dispatch(ce_server* s, Lane& L, int plant) {
-    const int64_t cw = s->cfg.cuda_mx_width, iw = s->cfg.info_mx_width;
+void dispatch(ce_server* s, Lane& L, int model, int plant) {
+    const int64_t cw = s->cfg[model].cuda_mx_width, iw = s->cfg[model].info_mx_width;
     int64_t n = 0;
     for (const Piece& p : L.pieces) {
         std::memcpy(L.h_gains + p.off * cw, p.req->gains + p.row0 * cw, (size_t)p.rows * cw * sizeof(float));
@@ -174,7 +179,7 @@ void dispatch(ce_server* s, Lane& L, int plant) {
     }
     CE_CUDA(cudaMemcpyAsync(L.d_gains, L.h_gains, (size_t)n * cw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
     CE_CUDA(cudaMemcpyAsync(L.d_info, L.h_info, (size_t)n * iw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
-    if (ce_evaluate_device(L.sess, plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0)
+    if (ce_evaluate_device(L.sess[model], plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0)
         throw std::runtime_error(ce_last_error());
     CE_CUDA(cudaMemcpyAsync(L.h_info, L.d_info, (size_t)n * iw * sizeof(float), cudaMemcpyDeviceToHost, L.stream));
     CE_CUDA(cudaEventRecord(L.done, L.stream));
@@ -201,7 +206,7 @@ void worker_loop(ce_server* s, int device) {
             }
         bool any_busy = false;
         for (Lane& L : s->lanes) any_busy = any_busy || L.busy;
-        int plant = 0;
+        int model = 0, plant = 0;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             if (s->stop && s->queue.empty() && !any_busy) return;
@@ -220,12 +225,12 @@ void worker_loop(ce_server* s, int device) {
                     continue;
                 }
             }
-            freeL->pieces = form_batch(s, plant);
+            freeL->pieces = form_batch(s, model, plant);
             freeL->busy = !freeL->pieces.empty();
         }
         if (freeL->busy) {
             try {
-                dispatch(s, *freeL, plant);
+                dispatch(s, *freeL, model, plant);
             } catch (const std::exception& e) {
                 cudaStreamSynchronize(freeL->stream);  // nothing of the batch may still be in flight
                 fail_pieces(s, *freeL, e.what());
@@ -244,7 +249,8 @@ void destroy_server(ce_server* s) {
     if (s->worker.joinable()) s->worker.join();
     for (Lane& L : s->lanes) {
         if (L.stream) cudaStreamSynchronize(L.stream);
-        if (L.sess) ce_session_destroy(L.sess);
+        for (ce_session* x : L.sess)
+            if (x) ce_session_destroy(x);
         if (L.done) cudaEventDestroy(L.done);
         if (L.stream) cudaStreamDestroy(L.stream);
         if (L.d_gains) cudaFree(L.d_gains);
@@ -255,15 +261,22 @@ void destroy_server(ce_server* s) {
     delete s;
 }
 
-void create_server(const ce_config* cfg, const ce_plant* plant, int n_plants, const ce_server_options* opt,
-                   ce_server** out) {
-    if (!cfg || !plant || !out) fail("ce_server_create: null argument");
+void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n_plants, int n_models,
+                   const ce_server_options* opt, ce_server** out) {
+    if (!cfg || !plant || !n_plants || !out) fail("ce_server_create: null argument");
+    if (n_models < 1) fail("ce_server_create: n_models must be >= 1, got {}", n_models);
     ce_server_options o{};
     if (opt) o = *opt;
     const int lanes = o.lanes > 0 ? o.lanes : 2;
     if (lanes > 8) fail("ce_server_create: at most 8 lanes, got {}", lanes);
     int64_t cap = o.max_batch > 0 ? o.max_batch : 65536;
-    const int64_t per = bytes_per_candidate(*cfg);
+    // every lane may hold a full batch's scratch for every model
+    int64_t per = 0, cw = 0, iw = 0;
+    for (int m = 0; m < n_models; ++m) {
+        per += bytes_per_candidate(cfg[m]);
+        cw = std::max<int64_t>(cw, cfg[m].cuda_mx_width);
+        iw = std::max<int64_t>(iw, cfg[m].info_mx_width);
+    }
     if (o.hbm_budget_bytes > 0) {
         const int64_t fit = o.hbm_budget_bytes / ((int64_t)lanes * per);
         if (fit < 1)
@@ -272,21 +285,24 @@ void create_server(const ce_config* cfg, const ce_plant* plant, int n_plants, co
         cap = std::min(cap, fit);
     }
     auto s = std::unique_ptr<ce_server, void (*)(ce_server*)>(new ce_server, destroy_server);
-    s->cfg = *cfg;
-    s->n_plants = n_plants;
+    s->cfg.assign(cfg, cfg + n_models);
+    s->n_plants.assign(n_plants, n_plants + n_models);
     s->capacity = cap;
     s->max_wait_us = std::max(0, o.max_wait_us);
     s->lanes.resize(lanes);
     int device = 0;
     CE_CUDA(cudaGetDevice(&device));
     for (Lane& L : s->lanes) {
-        if (ce_session_create(cfg, plant, n_plants, &L.sess) != 0) throw std::runtime_error(ce_last_error());
+        L.sess.assign(n_models, nullptr);
+        for (int m = 0; m < n_models; ++m)
+            if (ce_session_create(&cfg[m], &plant[m], n_plants[m], &L.sess[m]) != 0)
+                throw std::runtime_error(ce_last_error());
         CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
         CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
-        CE_CUDA(cudaMalloc((void**)&L.d_gains, (size_t)cap * cfg->cuda_mx_width * sizeof(float)));
-        CE_CUDA(cudaMalloc((void**)&L.d_info, (size_t)cap * cfg->info_mx_width * sizeof(float)));
-        CE_CUDA(cudaHostAlloc((void**)&L.h_gains, (size_t)cap * cfg->cuda_mx_width * sizeof(float), cudaHostAllocDefault));
-        CE_CUDA(cudaHostAlloc((void**)&L.h_info, (size_t)cap * cfg->info_mx_width * sizeof(float), cudaHostAllocDefault));
+        CE_CUDA(cudaMalloc((void**)&L.d_gains, (size_t)cap * cw * sizeof(float)));
+        CE_CUDA(cudaMalloc((void**)&L.d_info, (size_t)cap * iw * sizeof(float)));
+        CE_CUDA(cudaHostAlloc((void**)&L.h_gains, (size_t)cap * cw * sizeof(float), cudaHostAllocDefault));
+        CE_CUDA(cudaHostAlloc((void**)&L.h_info, (size_t)cap * iw * sizeof(float), cudaHostAllocDefault));
     }
     s->worker = std::thread(worker_loop, s.get(), device);
     *out = s.release();
@@ -302,7 +318,18 @@ extern "C" {
 CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants,
                                const ce_server_options* opt, ce_server** out) {
     try {
-        create_server(cfg, plant, n_plants, opt, out);
+        create_server(cfg, plant, &n_plants, 1, opt, out);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT int ce_server_create_models(const ce_config* cfgs, const ce_plant* plants, const int32_t* n_plants,
+                                      int32_t n_models, const ce_server_options* opt, ce_server** out) {
+    try {
+        create_server(cfgs, plants, n_plants, n_models, opt, out);
         return 0;
     } catch (const std::exception& e) {
         g_last_error = e.what();
@@ -312,15 +339,17 @@ CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int3
 
 CE_EXPORT void ce_server_destroy(ce_server* s) { destroy_server(s); }
 
-CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, const float* cuda_mx, const float* info_in,
-                               float* info_out, int64_t* request_id) {
+CE_EXPORT int ce_server_submit_model(ce_server* s, int32_t model, int32_t plant_index, int64_t n, const float* cuda_mx,
+                                     const float* info_in, float* info_out, int64_t* request_id) {
     try {
         if (!s || !request_id) fail("ce_server_submit: null argument");
-        if (plant_index < 0 || plant_index >= s->n_plants)
-            fail("plant index {} out of range [0, {})", plant_index, s->n_plants);
+        if (model < 0 || model >= (int)s->cfg.size()) fail("model {} out of range [0, {})", model, s->cfg.size());
+        if (plant_index < 0 || plant_index >= s->n_plants[model])
+            fail("plant index {} out of range [0, {})", plant_index, s->n_plants[model]);
         if (n < 0) fail("candidate count {} is negative", n);
         if (n > 0 && (!cuda_mx || !info_in || !info_out)) fail("ce_server_submit: null buffer");
         auto r = std::make_shared<Request>();
+        r->model = model;
         r->plant = plant_index;
         r->n = n;
         r->gains = cuda_mx;
@@ -346,6 +375,11 @@ CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, con
         g_last_error = e.what();
         return 1;
     }
+}
+
+CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, const float* cuda_mx, const float* info_in,
+                               float* info_out, int64_t* request_id) {
+    return ce_server_submit_model(s, 0, plant_index, n, cuda_mx, info_in, info_out, request_id);
 }
 
 CE_EXPORT int ce_server_wait(ce_server* s, int64_t request_id, int32_t timeout_ms) {

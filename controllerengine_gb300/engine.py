@@ -296,16 +296,25 @@ class Server:
     to `max_batch` candidates, `lanes` batches in flight on the GPU."""
 
     def __init__(self, config: EngineConfig, plant: PlantFiles, n_plants: int = 1, max_batch: int = 0,
-                 lanes: int = 0, hbm_budget_bytes: int = 0, max_wait_us: int = 0):
-        self.config = config
-        self._plant = plant
+                 lanes: int = 0, hbm_budget_bytes: int = 0, max_wait_us: int = 0,
+                 models: list | None = None):
+        """One model (config, plant, n_plants), or with `models` a list of such triples
+        (ce_server_create_models); requests then name their model in `submit`."""
+        models = models or [(config, plant, n_plants)]
+        self.configs = [m[0] for m in models]
+        self.config = self.configs[0]
+        self._plants = [m[1] for m in models]  # keeps the arrays alive for the call
         self._h = C.c_void_p()
         opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us)
-        _check(_lib().ce_server_create(C.byref(config.raw), C.byref(plant.ce_plant()), n_plants, C.byref(opt),
-                                       C.byref(self._h)))
+        k = len(models)
+        cfgs = (_ffi.ce_config * k)(*[m[0].raw for m in models])
+        pls = (_ffi.ce_plant * k)(*[m[1].ce_plant() for m in models])
+        nps = (C.c_int32 * k)(*[m[2] for m in models])
+        _check(_lib().ce_server_create_models(cfgs, pls, nps, k, C.byref(opt), C.byref(self._h)))
 
-    def submit(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, plant_index: int = 0) -> Request:
-        c = self.config
+    def submit(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, plant_index: int = 0,
+               model: int = 0) -> Request:
+        c = self.configs[model]
         g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
         n = g.shape[0]
         if info_in is None:
@@ -313,7 +322,8 @@ class Server:
         i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
         out = np.empty_like(i)
         rid = C.c_int64()
-        _check(_lib().ce_server_submit(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(rid)))
+        _check(_lib().ce_server_submit_model(self._h, model, plant_index, n, _fptr(g), _fptr(i), _fptr(out),
+                                             C.byref(rid)))
         return Request(self, rid.value, g, i, out)
 
     def stats(self) -> dict:

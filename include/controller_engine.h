@@ -304,9 +304,15 @@ typedef struct ce_server_stats {
 
 CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants,
                                const ce_server_options* options, ce_server** out);
+/* Several models (configurations with their plants) in one server: every lane
+ * holds a session per model; a batch holds requests of one model and plant. */
+CE_EXPORT int ce_server_create_models(const ce_config* cfgs, const ce_plant* plants, const int32_t* n_plants,
+                                      int32_t n_models, const ce_server_options* options, ce_server** out);
 CE_EXPORT void ce_server_destroy(ce_server* s); /* serves what is queued, then stops */
 CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, const float* cuda_mx,
                                const float* info_in, float* info_out, int64_t* request_id);
+CE_EXPORT int ce_server_submit_model(ce_server* s, int32_t model, int32_t plant_index, int64_t n,
+                                     const float* cuda_mx, const float* info_in, float* info_out, int64_t* request_id);
 /* 0: done (info_out filled); CE_PENDING: timeout (timeout_ms < 0 waits forever); 1: error. */
 CE_EXPORT int ce_server_wait(ce_server* s, int64_t request_id, int32_t timeout_ms);
 CE_EXPORT int ce_server_get_stats(ce_server* s, ce_server_stats* out);

@@ -119,3 +119,23 @@ def test_timeout_and_empty_request(mass_spring):
         first = r.wait(0)  # usually still running; either way no error
         out = first if first is not None else r.wait()
     assert np.array_equal(_bits(out), _bits(_alone(p)))
+
+
+def test_several_models(mass_spring):
+    """Two configurations in one server (ce_server_create_models): requests of both
+    interleave; each equals its own model's session evaluated alone."""
+    from controllerengine_gb300 import synth
+    a = mass_spring
+    b = synth.random_shape(4, n=600, time=900, freq=60)
+    cfg_a, cfg_b = ce.EngineConfig.parse(a.config_text), ce.EngineConfig.parse(b.config_text)
+    ref_a, ref_b = _alone(a), _alone(b)
+    with ce.Server(None, None, models=[(cfg_a, a.plant, 1), (cfg_b, b.plant, 1)], max_batch=400, lanes=2) as srv:
+        reqs = []
+        for k in range(6):
+            reqs.append((0, k * 256, srv.submit(a.cuda_mx[k * 256:(k + 1) * 256], a.info_mx[k * 256:(k + 1) * 256])))
+            reqs.append((1, k * 100, srv.submit(b.cuda_mx[k * 100:(k + 1) * 100], b.info_mx[k * 100:(k + 1) * 100],
+                                                model=1)))
+        for m, a0, r in reqs:
+            ref = ref_a if m == 0 else ref_b
+            rows = 256 if m == 0 else 100
+            assert np.array_equal(_bits(r.wait()), _bits(ref[a0:a0 + rows]))
