@@ -42,6 +42,28 @@ def workload_args(a):
     return dict(n=a.candidates, time=a.time, freq=a.freq)
 
 
+def precision_report(mixed, fp64, cfg):
+    """Cost rows of the mixed path (the reference's arithmetic) against the plain FP64 form of
+    the same method on the same candidates: agreement of the pass/fail classes and the
+    relative error of each cost term where both paths score the candidate."""
+    s, am, fr = cfg.info_scoring, cfg.info_allmargin, cfg.info_freqresp
+    def classes(x):
+        return np.stack([x[:, s + 1] >= cfg.unstable_err, x[:, s + 2] == np.float32(cfg.unstable_err),
+                         x[:, s + 2] == np.float32(cfg.eig_fail_err), x[:, am + 3] == 1.0], axis=1)
+    cm, cf = classes(mixed), classes(fp64)
+    same = (cm == cf).all(axis=1)
+    scored = same & ~cm[:, 0] & ~cm[:, 1] & ~cm[:, 2]
+    terms = {"total_score": s, "behaviour_err": s + 1, "margin_err": s + 2, "wn": fr, "zeta": fr + 1,
+             "overshoot": fr + 2, "yss": fr + 3, "gm_db": am, "pm_deg": am + 1, "b_pc": am + 4}
+    rel = {}
+    for name, col in terms.items():
+        a_, b_ = mixed[scored, col].astype(np.float64), fp64[scored, col].astype(np.float64)
+        ok = np.isfinite(a_) & np.isfinite(b_) & (np.abs(b_) < 1e30)
+        e = np.abs(a_[ok] - b_[ok]) / np.maximum(np.abs(b_[ok]), 1e-30)
+        rel[name] = {"median": float(np.median(e)) if e.size else None, "p99": float(np.quantile(e, 0.99)) if e.size else None}
+    return {"class_agreement": float(same.mean()), "candidates_compared": int(scored.sum()), "relative_error": rel}
+
+
 def fit_ops(eigen, steps):
     """FP32 operations of the modal fit over one batch: for each stable candidate,
     per window step, the normal-equation FMAs nc(nc+1)/2 + nc and 5 operations per
@@ -409,9 +431,11 @@ def main():
     # ---- FP64 form ----
     fp64 = None
     if a.fp64_steps > 0:
+        mixed_rows = info_out.cpu().numpy()
         sess.set_precision("fp64")
         step()
         torch.cuda.synchronize()
+        fp64_rows = info_out.cpu().numpy()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(a.fp64_steps):
@@ -420,7 +444,8 @@ def main():
         torch.cuda.synchronize()
         f_ms = e0.elapsed_time(e1) / a.fp64_steps
         fp64 = {"value": world * n / (f_ms * 1e-3), "unit": UNIT, "ms_per_step": f_ms,
-                "speedup_of_mixed": (world * n / (ms_per_step * 1e-3)) / (world * n / (f_ms * 1e-3))}
+                "speedup_of_mixed": (world * n / (ms_per_step * 1e-3)) / (world * n / (f_ms * 1e-3)),
+                "mixed_vs_fp64": precision_report(mixed_rows, fp64_rows, cfg)}
         sess.set_precision("mixed")
 
     # ---- roofline of the dominant kernel ----
