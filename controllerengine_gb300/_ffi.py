@@ -28,7 +28,8 @@ EXPORTED_SYMBOLS = (
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
     "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
     "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
-    "ce_server_submit_model", "RunControllerEngine",
+    "ce_server_submit_model", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
+    "RunControllerEngine",
 )
 PENDING = 2
 SIM_TABLE, SIM_SPECIALISED = 0, 1
@@ -84,6 +85,11 @@ class ce_diagnostics(C.Structure):
     _fields_ = [(n, _FP) for n in ("yplant", "lina", "eigen", "ata", "atb")]
 
 
+class ce_tuning(C.Structure):
+    _fields_ = [("eig_lanes", C.c_int32), ("eig_blocks_per_sm", C.c_int32), ("chunks", C.c_int32),
+                ("ms_per_evaluation", C.c_double)]
+
+
 class ce_server_options(C.Structure):
     _fields_ = [("max_batch", C.c_int32), ("lanes", C.c_int32), ("hbm_budget_bytes", C.c_int64),
                 ("max_wait_us", C.c_int32)]
@@ -136,6 +142,10 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
                                             C.POINTER(ce_server_options), C.POINTER(C.c_void_p)]
     lib.ce_server_submit_model.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.POINTER(C.c_int64)]
+    lib.ce_session_set_tuning.argtypes = [C.c_void_p, C.POINTER(ce_tuning)]
+    lib.ce_session_get_tuning.argtypes = [C.c_void_p, C.POINTER(ce_tuning)]
+    lib.ce_session_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(ce_tuning)]
     lib.ce_server_destroy.argtypes = [C.c_void_p]
     lib.ce_server_destroy.restype = None
     lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -98,6 +98,7 @@ struct ce_session {
     // simulation kernel compiled for it, built on first use
     float* d_mc_tab = nullptr;
     const void* sim_kernel_mc = nullptr;
+    ce_tuning tuning{};  // 0 fields: the library defaults
     float* d_fgrid32 = nullptr;   // grid_np x freq x 8
     double* d_fgrid64 = nullptr;  // built on the first FP64 evaluation
     ce::Buffers buf;
@@ -284,13 +285,13 @@ void ensure_plant_table(ce_session* s) {
 // Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
 // CE_CHUNKS (default 2: of 1, 2 and 4 chunks, 2 measured fastest on the
 // eight-state workload of 65,536 candidates).
-int n_chunks(int64_t n) {
-    static const int want = [] {
+int n_chunks(const ce_session* s, int64_t n) {
+    static const int dflt = [] {
         const char* e = std::getenv("CE_CHUNKS");
         const int k = e ? std::atoi(e) : 0;
         return (k >= 1 && k <= MAX_CHUNKS) ? k : 2;
     }();
-    int k = want;
+    int k = (s->tuning.chunks >= 1 && s->tuning.chunks <= MAX_CHUNKS) ? s->tuning.chunks : dflt;
     while (k > 1 && n / k < 16384) --k;
     return k;
 }
@@ -313,6 +314,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
     r.store_traj = traj ? 1 : 0;
+    r.eig_lanes = s->tuning.eig_lanes;
+    r.eig_blocks = s->tuning.eig_blocks_per_sm;
     if (per_candidate) {
         r.mc.tab = s->d_mc_tab;
         r.mc.np = s->n_plants;
@@ -346,7 +349,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // the eigensolves of the next chunks continue.
     const void* sk = per_candidate ? s->sim_kernel_mc : prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
     cudaStream_t fs = s->fast, ss = s->side;
-    const int nch = n_chunks(n);
+    const int nch = n_chunks(s, n);
     const int64_t per = (n + nch - 1) / nch;
     const size_t rsz = prec == CE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
     const int nt = r.nt, cw = r.cuda_w, iw = r.info_w;
@@ -1009,6 +1012,79 @@ CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int6
 }
 
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s) { return s ? s->launches : 0; }
+
+CE_EXPORT int ce_session_set_tuning(ce_session* s, const ce_tuning* t) {
+    return guarded([&] {
+        if (!s || !t) fail("null argument");
+        if (t->eig_lanes != 0 && t->eig_lanes != 1 && t->eig_lanes != 2 && t->eig_lanes != 4)
+            fail("eig_lanes must be 0, 1, 2 or 4, got {}", t->eig_lanes);
+        if (t->eig_blocks_per_sm < 0 || t->eig_blocks_per_sm > 32)
+            fail("eig_blocks_per_sm must be in [0, 32], got {}", t->eig_blocks_per_sm);
+        if (t->chunks < 0 || t->chunks > MAX_CHUNKS) fail("chunks must be in [0, {}], got {}", MAX_CHUNKS, t->chunks);
+        s->tuning = *t;
+    });
+}
+
+CE_EXPORT int ce_session_get_tuning(const ce_session* s, ce_tuning* t) {
+    return guarded([&] {
+        if (!s || !t) fail("null argument");
+        *t = s->tuning;
+    });
+}
+
+// The session autotuner: coordinate descent over the chunk count, the lanes per
+// matrix and the blocks per SM of the FP64 eigensolves, each setting timed with
+// CUDA events on one evaluation of the caller's batch (device buffers, the
+// output rows are overwritten).  None of the settings changes a result.
+CE_EXPORT int ce_session_autotune(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
+                                  const float* d_info_in, float* d_info_out, void* stream, ce_tuning* best) {
+    return guarded([&] {
+        check_eval(s, plant_index, n);
+        if (n == 0) fail("ce_session_autotune: empty batch");
+        cudaStream_t st = (cudaStream_t)stream;
+        cudaEvent_t e0, e1;
+        CE_CUDA(cudaEventCreate(&e0));
+        CE_CUDA(cudaEventCreate(&e1));
+        std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> g0(e0, cudaEventDestroy), g1(e1, cudaEventDestroy);
+        auto time_it = [&](const ce_tuning& t) {
+            s->tuning = t;
+            float best_ms = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {  // first one warms the setting up
+                CE_CUDA(cudaMemcpyAsync(d_info_out, d_info_in, (size_t)n * s->cfg.info_mx_width * sizeof(float),
+                                        cudaMemcpyDeviceToDevice, st));
+                CE_CUDA(cudaEventRecord(e0, st));
+                run_pipeline(s, plant_index, n, d_cuda_mx, d_info_out, st, false);
+                CE_CUDA(cudaEventRecord(e1, st));
+                CE_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                CE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep > 0) best_ms = std::min(best_ms, ms);
+            }
+            return best_ms;
+        };
+        ce_tuning cur{2, 5, 2, 0.0};
+        float cur_ms = time_it(cur);
+        auto try_set = [&](ce_tuning t) {
+            const float ms = time_it(t);
+            if (ms < cur_ms) {
+                cur = t;
+                cur_ms = ms;
+            }
+        };
+        for (int c : {1, 4}) try_set(ce_tuning{cur.eig_lanes, cur.eig_blocks_per_sm, c, 0.0});
+        for (int l : {1, 4}) {
+            const int b = l == 1 ? 3 : 10;  // a full share of shared memory for that width
+            try_set(ce_tuning{l, b, cur.chunks, 0.0});
+        }
+        const int lanes = cur.eig_lanes;
+        const int bmax = lanes == 1 ? 3 : lanes == 2 ? 6 : 12;
+        for (int b = std::max(1, cur.eig_blocks_per_sm - 1); b <= std::min(bmax, cur.eig_blocks_per_sm + 1); ++b)
+            if (b != cur.eig_blocks_per_sm) try_set(ce_tuning{lanes, b, cur.chunks, 0.0});
+        cur.ms_per_evaluation = cur_ms;
+        s->tuning = cur;
+        if (best) *best = cur;
+    });
+}
 
 CE_EXPORT int ce_session_set_sim_kernel(ce_session* s, int32_t kind) {
     return guarded([&] {

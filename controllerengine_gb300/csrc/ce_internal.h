@@ -91,6 +91,8 @@ struct Run {
     double alpha64;  // alpha of the FP64 form
     int store_traj;  // also write the full trajectory (diagnostics)
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
+    int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2 or 4; 0: the default)
+    int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)
 };
 
 // Per-candidate simulation summary (the parts of the trajectory that modalsetup

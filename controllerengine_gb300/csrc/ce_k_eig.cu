@@ -862,13 +862,14 @@ static void set_smem(const void* fn, size_t bytes) {
 // computing the scalar steps redundantly.  Two lanes measured fastest on the
 // eight-state workload (LIN_A eigensolve of 65,536 16x16 matrices: 21.9 ms with
 // one lane, 18.4 ms with two).  CE_EIG_LANES=1|2|4 overrides.
-static int eig_lanes() {
+// A session's tuning (Run::eig_lanes) wins over the default.
+static int eig_lanes(const Run& run) {
     static const int v = [] {
         const char* e = std::getenv("CE_EIG_LANES");
         const int k = e ? std::atoi(e) : 0;
         return (k == 1 || k == 2 || k == 4) ? k : EIG_LANES_DEFAULT;
     }();
-    return v;
+    return (run.eig_lanes == 1 || run.eig_lanes == 2 || run.eig_lanes == 4) ? run.eig_lanes : v;
 }
 
 // Blocks (one warp each) per SM of the persistent FP64 kernels.  Their
@@ -876,12 +877,13 @@ static int eig_lanes() {
 // lanes per matrix); a fixed number per SM keeps the FP64 pipe of every SM
 // fed while leaving the rest of the SM to the FP32 stages that run alongside
 // on the other stream.  CE_EIG_BLOCKS_PER_SM overrides.
-static int eig_grid(int64_t work, int mats) {
-    static const int per_sm = [] {
+static int eig_grid(const Run& run, int64_t work, int mats) {
+    static const int dflt = [] {
         const char* e = std::getenv("CE_EIG_BLOCKS_PER_SM");
         const int k = e ? std::atoi(e) : 0;
         return (k >= 1 && k <= 32) ? k : EIG_BLOCKS_PER_SM_DEFAULT;
     }();
+    const int per_sm = (run.eig_blocks >= 1 && run.eig_blocks <= 32) ? run.eig_blocks : dflt;
     int dev = 0, sms = 0;
     CE_CUDA(cudaGetDevice(&dev));
     CE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -892,7 +894,7 @@ static int eig_grid(int64_t work, int mats) {
 template <int EQ>
 static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                        int* nominal, int* list, int* count, cudaStream_t st) {
-    const int grid = eig_grid(run.n, eig_mats<EQ>());
+    const int grid = eig_grid(run, run.n, eig_mats<EQ>());
     const size_t smem = (size_t)run.nt * run.nt * eig_stride<EQ>() * sizeof(double);
     if (precision == CE_PRECISION_FP64) {
         set_smem((const void*)k_lina_eig64<EQ>, smem);
@@ -906,7 +908,7 @@ static void lina_eig_q(const Run& run, const Plant& P, int precision, const floa
 template <int EQ>
 static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                       const int* list, const int* count, int* nominal, cudaStream_t st) {
-    const int grid = eig_grid(run.n, eig_mats<EQ>());  // the listed count is only known on the device
+    const int grid = eig_grid(run, run.n, eig_mats<EQ>());  // the listed count is only known on the device
     const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
     set_smem((const void*)k_nominal<EQ>, smem);
     k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, precision == CE_PRECISION_FP64,
@@ -916,7 +918,7 @@ static void nominal_q(const Run& run, const Plant& P, int precision, const float
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                      int* nominal, int* list, int* count, cudaStream_t st) {
     CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
-    switch (eig_lanes()) {
+    switch (eig_lanes(run)) {
         case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
         case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
         default: lina_eig_q<4>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
@@ -926,7 +928,7 @@ void launch_lina_eig(const Run& run, const Plant& P, int precision, const float*
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const int* list, const int* count, int* nominal, cudaStream_t st) {
-    switch (eig_lanes()) {
+    switch (eig_lanes(run)) {
         case 1: nominal_q<1>(run, P, precision, gains, lina, list, count, nominal, st); break;
         case 2: nominal_q<2>(run, P, precision, gains, lina, list, count, nominal, st); break;
         default: nominal_q<4>(run, P, precision, gains, lina, list, count, nominal, st); break;

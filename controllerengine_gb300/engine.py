@@ -215,6 +215,24 @@ class Session:
         _check(_lib().ce_sim_specialised_source(self._h, plant, buf, size.value, C.byref(size)))
         return buf.value.decode()
 
+    @property
+    def tuning(self) -> dict:
+        t = _ffi.ce_tuning()
+        _check(_lib().ce_session_get_tuning(self._h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def set_tuning(self, eig_lanes: int = 0, eig_blocks_per_sm: int = 0, chunks: int = 0):
+        t = _ffi.ce_tuning(eig_lanes, eig_blocks_per_sm, chunks, 0.0)
+        _check(_lib().ce_session_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, n: int, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0,
+                 plant_index: int = 0) -> dict:
+        """Time launch settings on this batch (device pointers) and keep the fastest (ce_session_autotune)."""
+        t = _ffi.ce_tuning()
+        _check(_lib().ce_session_autotune(self._h, plant_index, n, C.c_void_p(d_cuda_mx), C.c_void_p(d_info_in),
+                                          C.c_void_p(d_info_out), C.c_void_p(stream), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
     def set_profiling(self, on: bool):
         _check(_lib().ce_session_set_profiling(self._h, 1 if on else 0))
 

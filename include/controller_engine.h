@@ -212,6 +212,24 @@ CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int6
 /* Launches of this library's kernels since the session was created. */
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s);
 
+/* Launch tuning of a session (no counterpart in the reference).  0 fields take
+ * the library defaults (2 lanes per matrix, 5 blocks per SM, 2 chunks for
+ * batches of >= 32,768 candidates).  No setting changes a result.
+ * ce_session_autotune times settings on one batch of the caller's (device
+ * buffers; d_info_out is overwritten) by coordinate descent over the chunk
+ * count, the lanes per matrix and the blocks per SM of the FP64 eigensolves,
+ * keeps the fastest and returns it with its time. */
+typedef struct ce_tuning {
+    int32_t eig_lanes;         /* lanes per matrix of the FP64 eigensolves: 1, 2 or 4 */
+    int32_t eig_blocks_per_sm; /* their persistent one-warp blocks per SM */
+    int32_t chunks;            /* chunks a batch of >= 32,768 candidates is cut into (<= 8) */
+    double ms_per_evaluation;  /* ce_session_autotune: the time of the chosen setting */
+} ce_tuning;
+CE_EXPORT int ce_session_set_tuning(ce_session* s, const ce_tuning* t);
+CE_EXPORT int ce_session_get_tuning(const ce_session* s, ce_tuning* t);
+CE_EXPORT int ce_session_autotune(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
+                                  const float* d_info_in, float* d_info_out, void* stream, ce_tuning* best);
+
 /* Simulation kernel selection (no counterpart in the reference, whose kernel
  * always interprets the decoded instruction tables).
  * CE_SIM_SPECIALISED: the plant's DC/U/NL programs are compiled at session
