@@ -62,7 +62,7 @@ class ce_config(C.Structure):
         ("ts", C.c_float), ("fit_t0", C.c_float), ("fit_t1", C.c_float), ("damping2", C.c_float),
         ("damping4", C.c_float), ("crossover", C.c_float),
         ("fit_start_id", C.c_int32), ("steady_start_id", C.c_int32), ("fit_steps", C.c_int32),
-        ("ref_step_id", C.c_int32),
+        ("ref_step_id", C.c_int32), ("observer", C.c_int32),
     ]
 
 

@@ -25,7 +25,8 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ce_k_sim.cu", "ce_k_eig.cu", "ce_k_modal.cu", "ce_k_sweep.cu", "ce_k_calib.cu", "ce_noalloc.cu", "ce_k_plant.cu"]
+CU_SOURCES = ["ce_k_sim.cu", "ce_k_eig.cu", "ce_k_modal.cu", "ce_k_sweep.cu", "ce_k_calib.cu", "ce_noalloc.cu", "ce_k_plant.cu",
+              "ce_k_kalman.cu"]
 CPP_SOURCES = ["ce_config.cpp", "ce_engine.cpp", "ce_jit.cpp", "ce_server.cpp"]
 # headers the run-time specialiser (ce_jit.cpp) hands to NVRTC, by the name they are #included under
 JIT_HEADERS = [("ce_sim_body.cuh", "ce_sim_body.cuh"), ("ce_device.cuh", "ce_device.cuh"),

@@ -52,7 +52,8 @@ void derive(ce_config& c) {
     c.nl_instructions_total = 0;
     for (int i = 0; i < c.nonlin_dim; i++) c.nl_instructions_total += c.nl_instructions[i];
 
-    c.cuda_mx_width = 2 * c.statespace_dim + 1;
+    // the Kalman row appends R and diag(Q) to the Luenberger row [K, L, N]
+    c.cuda_mx_width = c.observer == CE_OBSERVER_KALMAN ? 3 * c.statespace_dim + 2 : 2 * c.statespace_dim + 1;
     c.info_scoring = c.input_size;
     c.info_freqresp = c.info_scoring + 3;
     c.info_allmargin = c.info_freqresp + 4;
@@ -232,6 +233,14 @@ void parse_config(const std::string& text, const std::string& filename, ce_confi
     if (c.freq_max_key != 0.0f &&
         !(c.freq_max_key > c.freq_min && c.freq_max_key <= PI * (float)c.time / c.duration))
         fail("{}: need freq_min < freq_max <= pi*time/duration (Nyquist)", filename);
+
+    // Additive key: the time-varying Kalman observer (ref: src/discrete_solves.cu:83-185).
+    {
+        const std::string v = take("observer", "luenberger");
+        if (v == "luenberger") c.observer = CE_OBSERVER_LUENBERGER;
+        else if (v == "kalman") c.observer = CE_OBSERVER_KALMAN;
+        else fail("{}: `observer` should be luenberger/kalman, got `{}`", filename, v);
+    }
 
     if (!kv.empty()) fail("{}: unknown key `{}`", filename, kv.begin()->first);
 

@@ -56,18 +56,20 @@ struct Buffers {
     int* sweep_list = nullptr;
     int* sweep_count = nullptr;
     SweepScratch sweep{};
+    KalGroups kal{};  // Kalman observer: candidate grouping by noise weights
     float* traj = nullptr;
     int64_t traj_cap = 0;
     void release() {
         for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
                         (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count,
                         (void*)sweep_list, (void*)sweep_count, sweep.mag, sweep.arg, sweep.bpc, (void*)sweep.fail,
-                        (void*)traj})
+                        (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order})
             if (p) cudaFree(p);
         gains = info = lina = traj = nullptr;
         eig = ywin = summ = ata = atb = nullptr;
         nominal = fit_counts = fit_order = nominal_list = nominal_count = sweep_list = sweep_count = nullptr;
         sweep = SweepScratch{};
+        kal = KalGroups{};
         cap = traj_cap = 0;
     }
 };
@@ -83,7 +85,7 @@ struct ce_session {
     // simulation kernel of each plant in mixed precision: compiled for its
     // instruction program (ce_jit.cpp), or null for the table-driven kernel
     int sim_kind = CE_SIM_SPECIALISED;
-    std::vector<const void*> sim_kernel;
+    std::vector<ce::SimKernels> sim_kernel;
     std::string sim_log;
     // margin plants and their sweep grids: one per plant in serial mode, the
     // observer model shared by all plants in batch mode (ref: src/allmargin.cu:11-15)
@@ -97,7 +99,7 @@ struct ce_session {
     // per-candidate plants: the plant table (MC_FIELDS x n_plants) and the
     // simulation kernel compiled for it, built on first use
     float* d_mc_tab = nullptr;
-    const void* sim_kernel_mc = nullptr;
+    ce::SimKernels sim_kernel_mc;
     ce_tuning tuning{};  // 0 fields: the library defaults
     float* d_fgrid32 = nullptr;   // grid_np x freq x 8
     double* d_fgrid64 = nullptr;  // built on the first FP64 evaluation
@@ -189,6 +191,16 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         CE_CUDA(cudaMalloc(&b.sweep.arg, (size_t)cap * c.freq * rsz + 16));
         CE_CUDA(cudaMalloc(&b.sweep.bpc, (size_t)cap * groups * rsz + 16));
         dev_alloc(b.sweep.fail, (size_t)cap * groups);
+        if (c.observer == CE_OBSERVER_KALMAN) {
+            // one block: cnt | fill | totals (cleared together) | hoff | poff
+            dev_alloc(b.kal.bucket, (size_t)cap);
+            dev_alloc(b.kal.cnt, (size_t)4 * KAL_BUCKETS + 4);
+            b.kal.fill = b.kal.cnt + KAL_BUCKETS;
+            b.kal.totals = b.kal.fill + KAL_BUCKETS;
+            b.kal.hoff = b.kal.totals + 4;
+            b.kal.poff = b.kal.hoff + KAL_BUCKETS;
+            dev_alloc(b.kal.order, (size_t)kal_order_size(cap));
+        }
         b.cap = cap;
         b.nt = nt;
         b.pitch = pitch;
@@ -239,6 +251,7 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
     r.alpha = s->alpha32[s->grid_of(plant)];
     r.alpha64 = s->alpha64.empty() ? 0.0 : s->alpha64[s->grid_of(plant)];
     r.store_traj = 0;
+    r.kalman = c.observer == CE_OBSERVER_KALMAN ? 1 : 0;
     return r;
 }
 
@@ -250,7 +263,8 @@ void ensure_plant_table(ce_session* s) {
     if (!s->sim_kernel_mc) {
         std::string log;
         s->sim_kernel_mc = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
-                                          s->cfg.discrete_dim <= 4 ? 4 : 8, log, true);
+                                          s->cfg.discrete_dim <= 4 ? 4 : 8, log, true,
+                                          s->cfg.observer == CE_OBSERVER_KALMAN);
         if (!s->sim_kernel_mc) fail("per-candidate plants need the specialised simulation kernel: {}", log);
     }
     if (s->d_mc_tab) return;
@@ -347,7 +361,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // rest of each SM and run alongside.  Large batches are cut into chunks so
     // that the fit of a chunk starts as soon as its eigenvalues are known, while
     // the eigensolves of the next chunks continue.
-    const void* sk = per_candidate ? s->sim_kernel_mc : prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : nullptr;
+    const SimKernels sk = per_candidate ? s->sim_kernel_mc : prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : SimKernels{};
     cudaStream_t fs = s->fast, ss = s->side;
     const int nch = n_chunks(s, n);
     const int64_t per = (n + nch - 1) / nch;
@@ -386,8 +400,31 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         CE_CUDA(cudaEventRecord(s->ev_nom[k], ss));
     }
     timed(1, fs, [&] {
-        if (sk) launch_sim_specialised(sk, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, traj ? b.traj : nullptr, fs);
-        else launch_sim(r, P, prec, d_gains, b.ywin, b.summ, traj ? b.traj : nullptr, fs);
+        float* tr = traj ? b.traj : nullptr;
+        if (r.kalman) {
+            // Kalman observer: group the candidates by noise weights, then the
+            // shared-noise form over whole warps of a group and the
+            // per-candidate form over the rest
+            launch_kalman_groups(r, d_gains, b.kal, fs);
+            Run rh = r;
+            rh.kal_order = b.kal.order;
+            rh.kal_totals = b.kal.totals;
+            rh.kal_defer = kal_shared_slots(n) + n;
+            rh.kal_list = 1;
+            Run rp = rh;
+            rp.kal_list = 2;
+            if (sk) {
+                launch_sim_specialised(sk.shared, rh, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+                launch_sim_specialised(sk.main, rp, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+            } else {
+                launch_sim(rh, P, prec, d_gains, b.ywin, b.summ, tr, fs);
+                launch_sim(rp, P, prec, d_gains, b.ywin, b.summ, tr, fs);
+            }
+        } else if (sk) {
+            launch_sim_specialised(sk.main, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+        } else {
+            launch_sim(r, P, prec, d_gains, b.ywin, b.summ, tr, fs);
+        }
     });
     for (int k = 0; k < nch; ++k) {
         Run rc;
@@ -415,7 +452,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     }
     CE_CUDA(cudaEventRecord(s->ev_done, fs));
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_done, 0));
-    s->launches += 1 + 8 * nch;
+    s->launches += 1 + 8 * nch + (r.kalman ? 4 : 0);  // Kalman: three grouping kernels and a second simulation form
 }
 
 std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {
@@ -576,13 +613,14 @@ void build_grids(ce_session* s, int precision) {
 // each distinct instruction program once per process (NVRTC); a failure throws
 // with the compiler's log and leaves the session's kernels unchanged.
 void select_sim_kernel(ce_session* s, int kind) {
-    std::vector<const void*> ks(s->n_plants, nullptr);
+    std::vector<SimKernels> ks(s->n_plants);
     if (kind == CE_SIM_SPECIALISED) {
         // the plants of a session share the DC/U/NL tables, so the programs'
         // structure is the same for all of them: one compiled kernel serves all
         std::string log;
-        const void* k = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
-                                       s->cfg.discrete_dim <= 4 ? 4 : 8, log);
+        const SimKernels k = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                       s->cfg.discrete_dim <= 4 ? 4 : 8, log, false,
+                                       s->cfg.observer == CE_OBSERVER_KALMAN);
         if (!k) fail("specialising the simulation kernel failed: {}", log);
         ks.assign(s->n_plants, k);
     }
@@ -601,6 +639,11 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
         fail("ce_session_create: config dimensions are out of range or not derived");
     if (c.dc_dim != c.discrete_dim || c.u_dim != c.statespace_dim || c.nl_dim != c.discrete_dim + 1)
         fail("ce_session_create: instruction table widths are not derived from the dimensions");
+    if (c.observer != CE_OBSERVER_LUENBERGER && c.observer != CE_OBSERVER_KALMAN)
+        fail("ce_session_create: unknown observer {}", c.observer);
+    if (c.cuda_mx_width != (c.observer == CE_OBSERVER_KALMAN ? 3 : 2) * c.statespace_dim +
+                               (c.observer == CE_OBSERVER_KALMAN ? 2 : 1))
+        fail("ce_session_create: cuda_mx_width is not derived from the dimensions and the observer");
     s->n_plants = n_plants;
     s->plants.resize(n_plants);
     s->plant_err.assign(n_plants, std::string());
@@ -622,7 +665,7 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
     // Default: the specialised kernel.  CE_SIM_KERNEL=table in the environment
     // selects the table-driven one; if compiling fails the session keeps the
     // table-driven kernel and ce_session_sim_kernel reports which one runs.
-    s->sim_kernel.assign(n_plants, nullptr);
+    s->sim_kernel.assign(n_plants, SimKernels{});
     s->sim_kind = CE_SIM_TABLE;
     const char* env = std::getenv("CE_SIM_KERNEL");
     if (!(env && std::string(env) == "table")) {
@@ -959,6 +1002,8 @@ CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {
         if (!s) fail("null session");
         if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64) fail("unknown precision {}", precision);
+        if (precision == CE_PRECISION_FP64 && s->cfg.observer == CE_OBSERVER_KALMAN)
+            fail("the Kalman observer (observer = kalman) runs in mixed precision only");
         s->precision = precision;
     });
 }
@@ -1105,7 +1150,8 @@ CE_EXPORT int ce_sim_specialised_source(const ce_session* s, int32_t plant_index
         if (plant_index < 0 || plant_index >= s->n_plants)
             fail("plant index {} out of range [0, {})", plant_index, s->n_plants);
         const std::string src = specialised_source(s->plants[plant_index], s->cfg.statespace_dim <= 4 ? 4 : 8,
-                                                   s->cfg.discrete_dim <= 4 ? 4 : 8);
+                                                   s->cfg.discrete_dim <= 4 ? 4 : 8,
+                                                   s->cfg.observer == CE_OBSERVER_KALMAN);
         if (size) *size = (int64_t)src.size() + 1;
         if (buf && cap > 0) {
             const size_t k = std::min<size_t>(src.size(), (size_t)cap - 1);

@@ -83,12 +83,44 @@ void launch_sweep(const Run& run, int precision, const float* gains, const float
 
 double measure_fma_rate(bool fp64);
 
-// Simulation kernel specialised to a plant's instruction program (ce_jit.cpp):
-// returns the compiled kernel (cached per program), or nullptr with `log` set.
-const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc = false);
-std::string specialised_source(const Plant& P, int ns, int nd);
+// Simulation kernels specialised to a plant's instruction program
+// (ce_jit.cpp), cached per program: `main` (the Luenberger loop, or the Kalman
+// loop with per-candidate covariance) and, for the Kalman observer, `shared`
+// (the shared-noise form).  main == nullptr: failed, with `log` set.
+struct SimKernels {
+    const void* main = nullptr;
+    const void* shared = nullptr;
+    explicit operator bool() const { return main != nullptr; }
+};
+SimKernels specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc = false, bool kalman = false);
+std::string specialised_source(const Plant& P, int ns, int nd, bool kalman = false);
+// Launches kernel (main or shared) over the candidates `run` selects.
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
                             SimSummary* summ, float* traj, cudaStream_t st);
+
+// Blocks of SIM_BLOCK threads that cover the candidates (or list slots) of `run`.
+int sim_grid(const Run& run);
+
+// Grouping of a Kalman evaluation's candidates by their noise weights (R and
+// the diagonal of Q, bit for bit) for the shared-noise simulation form
+// (ce_k_kalman.cu).  Groups of at least KAL_MIN_GROUP candidates fill whole
+// warps of the shared list (padded with -1); the others form the per-candidate
+// list.
+constexpr int KAL_BUCKETS = 1 << 16;
+constexpr int KAL_MIN_GROUP = 8;
+inline int64_t kal_shared_slots(int64_t n) { return n + 31 * (n / KAL_MIN_GROUP) + 32; }
+inline int64_t kal_order_size(int64_t n) { return kal_shared_slots(n) + 2 * n; }
+struct KalGroups {
+    unsigned* bucket = nullptr;  // n: hash bucket of each candidate
+    int* cnt = nullptr;          // KAL_BUCKETS: candidates per bucket
+    int* fill = nullptr;         // KAL_BUCKETS: scatter counters
+    int* hoff = nullptr;         // KAL_BUCKETS: offset in the shared list
+    int* poff = nullptr;         // KAL_BUCKETS: offset in the per-candidate list
+    int* totals = nullptr;       // 4: shared slots, per-candidate count, deferred count
+    int* order = nullptr;        // kal_order_size(n)
+};
+// Fills g.order / g.totals for the n candidates of `run` (4 launches incl. a memset).
+void launch_kalman_groups(const Run& run, const float* gains, const KalGroups& g, cudaStream_t st);
 
 const Plant* session_plant(const ce_session* s, int plant);
 const ce_config* session_config(const ce_session* s);

@@ -90,6 +90,15 @@ struct Run {
     float bandwidth, damping, overshoot, sse, target_gm, target_pm, target_b, alpha;
     double alpha64;  // alpha of the FP64 form
     int store_traj;  // also write the full trajectory (diagnostics)
+    int kalman;      // 1: time-varying Kalman observer (rows [K, L, N, R, Q]), 0: Luenberger
+    // Kalman candidate lists (kal_list 0: thread i simulates candidate i).  1: the
+    // shared-noise list kal_order[0, kal_totals[0]) in whole warps (-1: padding);
+    // 2: the per-candidate list kal_order[kal_totals[0], + kal_totals[1]), then
+    // the kal_totals[2] candidates deferred by the shared form at kal_order[kal_defer]
+    int kal_list;
+    int* kal_order;
+    int* kal_totals;
+    int64_t kal_defer;
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
     int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2 or 4; 0: the default)
     int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)

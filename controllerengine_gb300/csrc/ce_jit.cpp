@@ -36,7 +36,7 @@ namespace {
 #include "ce_jit_src.inc"
 
 std::mutex g_jit_mu;
-std::map<std::string, const void*> g_jit_cache;  // source -> cudaKernel_t
+std::map<std::string, SimKernels> g_jit_cache;  // source -> compiled kernels
 
 // One chain as straight-line code.  Constant operands come from the launch's
 // Plant, or with `mc` from the candidate's plant-table row (slot numbering of
@@ -77,7 +77,7 @@ std::string fmt_chain(const char* fname, const Instr* ins, int n, bool seed, boo
     return o.str();
 }
 
-std::string jit_source(const Plant& P, int ns, int nd, bool mc) {
+std::string jit_source(const Plant& P, int ns, int nd, bool mc, bool kalman) {
     std::ostringstream o;
     o << "#include \"ce_sim_body.cuh\"\n\nnamespace cejit {\n\n";
     o << fmt_chain("dc", P.dc, P.n_dc, false, false, "dc", 0, mc);
@@ -103,14 +103,24 @@ std::string jit_source(const Plant& P, int ns, int nd, bool mc) {
          "        W[0] = cejit::nl0(P, L, xp, y, 0.0f);\n        W[1] = cejit::nl1(P, L, xp, y, 0.0f);\n"
          "        W[2] = cejit::nl2(P, L, xp, y, 0.0f);\n        W[3] = cejit::nl3(P, L, xp, y, 0.0f);\n    }\n};\n\n"
          "}  // namespace cejit\n\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(ce::SIM_BLOCK) ce_sim_specialised(\n"
-         "    const ce::Run run, const __grid_constant__ ce::Plant P, const float* __restrict__ gains,\n"
-         "    float* __restrict__ ywin, ce::SimSummary* __restrict__ summ, float* __restrict__ traj) {\n"
-      << "    ce::sim_run<" << ns << ", " << nd << ", cejit::Chains>(run, P, gains, ywin, summ, traj);\n}\n";
+    auto kernel = [&](const char* name, int nsc, const char* mode) {
+        o << "extern \"C\" __global__ void __launch_bounds__(ce::SIM_BLOCK) " << name << "(\n"
+             "    const ce::Run run, const __grid_constant__ ce::Plant P, const float* __restrict__ gains,\n"
+             "    float* __restrict__ ywin, ce::SimSummary* __restrict__ summ, float* __restrict__ traj) {\n"
+          << "    ce::sim_run<" << nsc << ", " << nd << ", cejit::Chains, " << mode
+          << ">(run, P, gains, ywin, summ, traj);\n}\n";
+    };
+    // the Kalman loop always runs the full padded observer width
+    if (kalman) {
+        kernel("ce_sim_specialised", MAXS, "ce::SIM_KALMAN_LANE");
+        kernel("ce_sim_kalman_shared", MAXS, "ce::SIM_KALMAN_SHARED");
+    } else {
+        kernel("ce_sim_specialised", ns, "ce::SIM_LUENBERGER");
+    }
     return o.str();
 }
 
-const void* compile(const std::string& src, std::string& log) {
+SimKernels compile(const std::string& src, std::string& log, bool kalman) {
     std::vector<const char*> names, texts;
     for (const auto& h : kJitHeaders) {
         names.push_back(h.name);
@@ -120,7 +130,7 @@ const void* compile(const std::string& src, std::string& log) {
     if (nvrtcCreateProgram(&prog, src.c_str(), "ce_sim_specialised.cu", (int)names.size(), texts.data(),
                            names.data()) != NVRTC_SUCCESS) {
         log = "nvrtcCreateProgram failed";
-        return nullptr;
+        return {};
     }
     const std::string inc = std::string("-I") + CE_CUDA_INCLUDE;
     const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=true", inc.c_str(), "-lineinfo"};
@@ -132,7 +142,7 @@ const void* compile(const std::string& src, std::string& log) {
     if (rc != NVRTC_SUCCESS) {
         log = std::string("NVRTC: ") + nvrtcGetErrorString(rc) + "\n" + plog;
         nvrtcDestroyProgram(&prog);
-        return nullptr;
+        return {};
     }
     size_t csz = 0;
     nvrtcGetCUBINSize(prog, &csz);
@@ -143,40 +153,47 @@ const void* compile(const std::string& src, std::string& log) {
     cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) {
         log = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
-        return nullptr;
+        return {};
     }
-    cudaKernel_t k;
-    e = cudaLibraryGetKernel(&k, lib, "ce_sim_specialised");
-    if (e != cudaSuccess) {
-        log = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
-        return nullptr;
+    SimKernels out;
+    const char* kernel_names[2] = {"ce_sim_specialised", "ce_sim_kalman_shared"};
+    for (int i = 0; i < (kalman ? 2 : 1); ++i) {
+        cudaKernel_t k;
+        e = cudaLibraryGetKernel(&k, lib, kernel_names[i]);
+        if (e != cudaSuccess) {
+            log = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
+            return {};
+        }
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k), cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) {
+            log = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+            return {};
+        }
+        (i == 0 ? out.main : out.shared) = reinterpret_cast<const void*>(k);
     }
-    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k), cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) {
-        log = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-        return nullptr;
-    }
-    return reinterpret_cast<const void*>(k);
+    return out;
 }
 
 }  // namespace
 
-const void* specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc) {
-    const std::string src = jit_source(P, ns, nd, mc);
+SimKernels specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc, bool kalman) {
+    const std::string src = jit_source(P, ns, nd, mc, kalman);
     std::lock_guard<std::mutex> g(g_jit_mu);
     auto it = g_jit_cache.find(src);
     if (it != g_jit_cache.end()) return it->second;
-    const void* k = compile(src, log);
+    const SimKernels k = compile(src, log, kalman);
     if (k) g_jit_cache.emplace(src, k);
     return k;
 }
 
-std::string specialised_source(const Plant& P, int ns, int nd) { return jit_source(P, ns, nd, false); }
+std::string specialised_source(const Plant& P, int ns, int nd, bool kalman) {
+    return jit_source(P, ns, nd, false, kalman);
+}
 
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
                             SimSummary* summ, float* traj, cudaStream_t st) {
-    const int grid = (int)((run.n + SIM_BLOCK - 1) / SIM_BLOCK);
+    const int grid = sim_grid(run);
     void* args[] = {(void*)&run, (void*)&P, (void*)&gains, (void*)&ywin, (void*)&summ, (void*)&traj};
     CE_CUDA(cudaLaunchKernel(kernel, dim3(grid), dim3(SIM_BLOCK), args, 0, st));
 }

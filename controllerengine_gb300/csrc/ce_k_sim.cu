@@ -10,11 +10,11 @@
 
 namespace ce {
 
-template <int NSC, int NDC>
+template <int NSC, int NDC, int KMODE>
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __grid_constant__ Plant P,
                                                          const float* __restrict__ gains, float* __restrict__ ywin,
                                                          SimSummary* __restrict__ summ, float* __restrict__ traj) {
-    sim_run<NSC, NDC, TableChains>(run, P, gains, ywin, summ, traj);
+    sim_run<NSC, NDC, TableChains, KMODE>(run, P, gains, ywin, summ, traj);
 }
 
 // The plain FP64 form of the same recurrence: double state, no hi/lo split.
@@ -93,23 +93,31 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __g
 
 static int dim_class(int d) { return d <= 4 ? 4 : 8; }
 
-template <int NSC, int NDC>
+template <int NSC, int NDC, int KMODE = SIM_LUENBERGER>
 static void sim_launch(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ,
                        float* traj, cudaStream_t st) {
-    const int grid = (int)((run.n + SIM_BLOCK - 1) / SIM_BLOCK);
+    const int grid = sim_grid(run);
     if (precision == CE_PRECISION_FP64) {
+        if (KMODE != SIM_LUENBERGER) throw std::runtime_error("the Kalman observer runs in mixed precision only");
         prefer_shared((const void*)k_sim_fp64<NSC, NDC>);
         k_sim_fp64<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
     } else {
-        prefer_shared((const void*)k_sim_mixed<NSC, NDC>);
-        k_sim_mixed<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
+        prefer_shared((const void*)k_sim_mixed<NSC, NDC, KMODE>);
+        k_sim_mixed<NSC, NDC, KMODE><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
     }
 }
 
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
                 cudaStream_t st) {
     const int cs = dim_class(run.ns), cd = dim_class(run.nd);
-    if (cs == 4 && cd == 4) sim_launch<4, 4>(run, P, precision, gains, ywin, summ, traj, st);
+    if (run.kalman && run.kal_list == 1) {
+        // the shared-noise form; the Kalman loop always runs the full padded observer width
+        if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);
+        else sim_launch<8, 8, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);
+    } else if (run.kalman) {
+        if (cd == 4) sim_launch<8, 4, SIM_KALMAN_LANE>(run, P, precision, gains, ywin, summ, traj, st);
+        else sim_launch<8, 8, SIM_KALMAN_LANE>(run, P, precision, gains, ywin, summ, traj, st);
+    } else if (cs == 4 && cd == 4) sim_launch<4, 4>(run, P, precision, gains, ywin, summ, traj, st);
     else if (cs == 4 && cd == 8) sim_launch<4, 8>(run, P, precision, gains, ywin, summ, traj, st);
     else if (cs == 8 && cd == 4) sim_launch<8, 4>(run, P, precision, gains, ywin, summ, traj, st);
     else sim_launch<8, 8>(run, P, precision, gains, ywin, summ, traj, st);

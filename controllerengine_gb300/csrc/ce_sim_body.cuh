@@ -27,6 +27,16 @@
 // poison flags reproduce when the reference's padded states turn NaN (a zero
 // coefficient times a non-finite operand).
 //
+// Kalman observer (KMODE 1 and 2, ref: src/discrete_solves.cu:83-185): the prediction
+// xh += (A-I)xh + B u, the covariance P = A P A^T + diag(Q), the gain
+// KG = P C^T / (C P C^T + R), the correction xh += KG (y - C xh) in double-float
+// and the Joseph update P = (I - KG C) P (I - KG C)^T + KG R KG^T replace the
+// Luenberger increment, with the reference's fma chains over the full padded
+// width (NSC = 8).  Two of the reference's defects are fixed: its Joseph
+// product writes over its own left factor while reading it (:160), here it
+// has its own storage; its 1/(C P C^T + R) is the approximate __fdividef
+// (:137), here the correctly rounded quotient.  Rows are [K, L, N, R, Q].
+//
 // Chains policy: Chains::kSmem says whether the chains read their sources from
 // the per-thread shared-memory rows srcP (plant states, y in row MAXD) and srcH
 // (observer states); dc / u / nl evaluate the DC, U and NL_k chains;
@@ -73,16 +83,282 @@ struct McLocal {
     __device__ __forceinline__ float c(int k) const { return cst_[k]; }
 };
 
-template <int NSC, int NDC, class Chains>
+// P <- (M P) M^T over the padded 8 x 8 covariance, in place (ABATf, ref:
+// src/main.cu:190-212).  Column j of M P needs only column j of P and row i of
+// (M P) M^T only row i of M P, so eight temporaries suffice.  Every element is
+// the reference's fma chain in k order from 0.
+template <class Mat>
+__device__ __forceinline__ void abat_in_place(float (&Pm)[MAXS * MAXS], const Mat& M) {
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+        float col[MAXS];
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(M(i, k), Pm[k * MAXS + j], a);
+            col[i] = a;
+        }
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) Pm[i * MAXS + j] = col[i];
+    }
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        float r[MAXS];
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(Pm[i * MAXS + k], M(j, k), a);
+            r[j] = a;
+        }
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) Pm[i * MAXS + j] = r[j];
+    }
+}
+
+// Kalman prediction xh += (A-I) xh + B u, then double-float add (ref: src/discrete_solves.cu:118-126).
+__device__ __forceinline__ void kalman_predict(const Plant& P, float (&xh_hi)[MAXS], float (&xh_lo)[MAXS], float u) {
+    float dh[MAXS], dl[MAXS];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        float h = __fmul_rn(P.ss_b[i], u), l = 0.0f;
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) h = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_hi[j], h);
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) l = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_lo[j], l);
+        dh[i] = h;
+        dl[i] = l;
+    }
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) df_add(xh_hi[i], xh_lo[i], dh[i], dl[i]);
+}
+
+// Kalman correction xh += KG (y - C xh): the residual as a (hi, lo) pair and
+// exact products (ref: src/discrete_solves.cu:140-149).
+__device__ __forceinline__ void kalman_correct(const Plant& P, float (&xh_hi)[MAXS], float (&xh_lo)[MAXS], float y,
+                                               const float (&KG)[MAXS]) {
+    float zh = -y, zl = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) zh = __fmaf_rn(P.ss_c[k], xh_hi[k], zh);
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) zl = __fmaf_rn(P.ss_c[k], xh_lo[k], zl);
+    zh = __fmul_rn(-1.0f, zh);
+    zl = __fmul_rn(-1.0f, zl);
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        const float s = __fmul_rn(KG[i], zh);
+        float e = __fmaf_rn(KG[i], zh, -s);
+        e = __fmaf_rn(KG[i], zl, e);
+        df_add(xh_hi[i], xh_lo[i], s, e);
+    }
+}
+
+// -(KG_i C_k - [i == k]): element (i, k) of I - KG C as the reference forms it
+// (matmul, diagonal minus one, negation; ref: src/discrete_solves.cu:152-158).
+__device__ __forceinline__ float ikh(float kg_i, float c_k, bool diag) {
+    float m = __fmaf_rn(kg_i, c_k, 0.0f);
+    if (diag) m = __fsub_rn(m, 1.0f);
+    return -m;
+}
+
+// One candidate's covariance step, all in its own registers (ref:
+// src/discrete_solves.cu:128-163): P = A P A^T + diag(Q); KG = P C^T /
+// (C P C^T + R); P = (I - KG C) P (I - KG C)^T + KG R KG^T.
+__device__ __forceinline__ void kalman_cov_lane(const Plant& P, float (&Pm)[MAXS * MAXS], const float (&Qd)[MAXS],
+                                                float Rn, float (&KG)[MAXS]) {
+    abat_in_place(Pm, [&](int i, int k) { return P.ss_a[i * MAXS + k]; });
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) Pm[i * (MAXS + 1)] = __fadd_rn(Pm[i * (MAXS + 1)], Qd[i]);
+    {
+        float pht[MAXS], cp[MAXS];
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(Pm[i * MAXS + k], P.ss_c[k], a);
+            pht[i] = a;
+        }
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(P.ss_c[k], Pm[k * MAXS + j], a);
+            cp[j] = a;
+        }
+        float hphr = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) hphr = __fmaf_rn(cp[k], P.ss_c[k], hphr);
+        hphr = __fdiv_rn(1.0f, __fadd_rn(hphr, Rn));
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) KG[i] = __fmul_rn(pht[i], hphr);
+    }
+    float M[MAXS * MAXS];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) M[i * MAXS + j] = ikh(KG[i], P.ss_c[j], i == j);
+    abat_in_place(Pm, [&](int i, int k) { return M[i * MAXS + k]; });
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        const float kr = __fmaf_rn(KG[i], Rn, 0.0f);
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) Pm[i * MAXS + j] = __fadd_rn(Pm[i * MAXS + j], __fmaf_rn(kr, KG[j], 0.0f));
+    }
+}
+
+// The covariance recursion depends only on A, C, Q and R, so candidates with
+// the same noise weights share it.  In the shared form a whole warp holds
+// such candidates and computes the recursion once, cooperatively: P lives in
+// shared memory and lane l forms elements l and l + 32 (rows i0 = l/8 and
+// i1 = i0 + 4, column j = l%8) of each product, every element by the same fma
+// chain as in the per-candidate form, so the gains are bit-identical.  Once
+// P_{t+1} equals P_t bit for bit the recursion has reached a fixed point and
+// the gain stays; once P_{t+1} equals P_{t-1} the gains alternate.
+struct KalShared {
+    float a0[MAXS], a1[MAXS], aj[MAXS];  // rows i0, i1 and j of A
+    float q0, q1, r;                     // Q[i0], Q[i1], R
+    float kg[MAXS], kgo[MAXS];           // the gain of this step and of the one before
+    float p0, p1, o0, o1;                // own elements of P at the start of this step and of the one before
+    int mode;                            // 0: recursing; 1: fixed point; 2: period two
+    int t;                               // steps recursed
+};
+
+__device__ __forceinline__ void kalman_cov_shared(const Plant& P, KalShared& S, float* __restrict__ Ps,
+                                                  float* __restrict__ Ts, int lane) {
+    constexpr unsigned FULL = 0xffffffffu;
+    if (S.mode == 1) return;
+    if (S.mode == 2) {
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) {
+            const float k = S.kg[i];
+            S.kg[i] = S.kgo[i];
+            S.kgo[i] = k;
+        }
+        return;
+    }
+    const int j = lane & (MAXS - 1), i0 = lane >> 3, i1 = i0 + 4;
+    // T = A P (column j of P)
+    float pc[MAXS];
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) pc[k] = Ps[k * MAXS + j];
+    float t0 = 0.0f, t1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+        t0 = __fmaf_rn(S.a0[k], pc[k], t0);
+        t1 = __fmaf_rn(S.a1[k], pc[k], t1);
+    }
+    Ts[lane] = t0;
+    Ts[lane + 32] = t1;
+    __syncwarp();
+    // P = T A^T + diag(Q)
+    float u0 = 0.0f, u1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+        u0 = __fmaf_rn(Ts[i0 * MAXS + k], S.aj[k], u0);
+        u1 = __fmaf_rn(Ts[i1 * MAXS + k], S.aj[k], u1);
+    }
+    if (i0 == j) u0 = __fadd_rn(u0, S.q0);
+    if (i1 == j) u1 = __fadd_rn(u1, S.q1);
+    Ps[lane] = u0;
+    Ps[lane + 32] = u1;
+    __syncwarp();
+    // gain: lanes 0-7 form (P C^T)_l, lanes 8-15 (C P)_{l-8}; every lane forms C P C^T + R
+    float v = 0.0f;
+    if (lane < MAXS) {
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(Ps[lane * MAXS + k], P.ss_c[k], v);
+    } else if (lane < 2 * MAXS) {
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(P.ss_c[k], Ps[k * MAXS + lane - MAXS], v);
+    }
+    float h = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) h = __fmaf_rn(__shfl_sync(FULL, v, MAXS + k), P.ss_c[k], h);
+    h = __fdiv_rn(1.0f, __fadd_rn(h, S.r));
+    const float kgl = __fmul_rn(v, h);
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) {
+        S.kgo[i] = S.kg[i];
+        S.kg[i] = __shfl_sync(FULL, kgl, i);
+    }
+    const float kgi0 = __shfl_sync(FULL, kgl, i0), kgi1 = __shfl_sync(FULL, kgl, i1);
+    const float kgj = __shfl_sync(FULL, kgl, j);
+    // T = (I - KG C) P
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) pc[k] = Ps[k * MAXS + j];
+    float w0 = 0.0f, w1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+        w0 = __fmaf_rn(ikh(kgi0, P.ss_c[k], k == i0), pc[k], w0);
+        w1 = __fmaf_rn(ikh(kgi1, P.ss_c[k], k == i1), pc[k], w1);
+    }
+    Ts[lane] = w0;
+    Ts[lane + 32] = w1;
+    __syncwarp();
+    // P = T (I - KG C)^T + KG R KG^T
+    float z0 = 0.0f, z1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+        const float m = ikh(kgj, P.ss_c[k], k == j);
+        z0 = __fmaf_rn(Ts[i0 * MAXS + k], m, z0);
+        z1 = __fmaf_rn(Ts[i1 * MAXS + k], m, z1);
+    }
+    z0 = __fadd_rn(z0, __fmaf_rn(__fmaf_rn(kgi0, S.r, 0.0f), kgj, 0.0f));
+    z1 = __fadd_rn(z1, __fmaf_rn(__fmaf_rn(kgi1, S.r, 0.0f), kgj, 0.0f));
+    const bool same1 = __float_as_uint(z0) == __float_as_uint(S.p0) && __float_as_uint(z1) == __float_as_uint(S.p1);
+    const bool same2 =
+        S.t > 0 && __float_as_uint(z0) == __float_as_uint(S.o0) && __float_as_uint(z1) == __float_as_uint(S.o1);
+    const bool fixed = __all_sync(FULL, same1), period2 = __all_sync(FULL, same2);
+    // every lane read P for the last time before the barrier above
+    Ps[lane] = z0;
+    Ps[lane + 32] = z1;
+    __syncwarp();
+    S.o0 = S.p0;
+    S.o1 = S.p1;
+    S.p0 = z0;
+    S.p1 = z1;
+    ++S.t;
+    S.mode = fixed ? 1 : period2 ? 2 : 0;
+}
+
+// Simulation forms: KMODE 0 the Luenberger observer; 1 the Kalman observer
+// with each candidate's covariance in its own registers; 2 the Kalman observer
+// with the covariance shared by the warp (all 32 lanes hold the same R and Q).
+constexpr int SIM_LUENBERGER = 0, SIM_KALMAN_LANE = 1, SIM_KALMAN_SHARED = 2;
+
+template <int NSC, int NDC, class Chains, int KMODE = SIM_LUENBERGER>
 __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const float* __restrict__ gains,
                                         float* __restrict__ ywin, SimSummary* __restrict__ summ,
                                         float* __restrict__ traj) {
+    constexpr bool KAL = KMODE != SIM_LUENBERGER;
+    constexpr bool SHARED = KMODE == SIM_KALMAN_SHARED;
     __shared__ float stage[8][SIM_BLOCK];
     __shared__ float srcP[Chains::kSmem ? MAXD + 1 : 1][SIM_BLOCK];
     __shared__ float srcH[Chains::kSmem ? MAXS : 1][SIM_BLOCK];
+    __shared__ float kps[SHARED ? SIM_BLOCK / 32 : 1][2][SHARED ? MAXS * MAXS : 1];
     const int tid = threadIdx.x;
-    const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
-    if (c >= run.n) return;  // each thread only touches its own column of the shared rows
+    // each thread only touches its own column of the shared rows
+    const int64_t pos = (int64_t)blockIdx.x * SIM_BLOCK + tid;
+    int64_t c = pos;
+    bool writer = true;
+    if constexpr (SHARED) {
+        // the shared-noise list: whole warps of one group; a padding slot (-1)
+        // shadows the warp's first candidate and writes nothing
+        const int64_t wbase = pos & ~(int64_t)31;
+        if (wbase >= run.kal_totals[0]) return;  // warp-uniform
+        const int own = run.kal_order[pos];
+        writer = own >= 0;
+        c = writer ? own : run.kal_order[wbase];
+    } else if (KAL && run.kal_list == 2) {
+        // the per-candidate list, then the candidates of warps deferred by the shared form
+        const int64_t np = run.kal_totals[1], nd = run.kal_totals[2];
+        if (pos < np) c = run.kal_order[run.kal_totals[0] + pos];
+        else if (pos < np + nd) c = run.kal_order[run.kal_defer + pos - np];
+        else return;
+    } else {
+        if (c >= run.n) return;
+    }
     const typename Chains::template Local<NDC> Lc(run, P, c);
 
     const int ns = run.ns;
@@ -94,6 +370,57 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
         L[i] = i < ns ? row[ns + i] : 0.0f;
     }
     const float N = row[2 * ns];
+    static_assert(!KAL || NSC == MAXS, "the Kalman observer runs the full padded width");
+    // Kalman: noise weights and covariance (ref: src/discrete_solves.cu:88-101,
+    // at the row offsets of [K, L, N, R, Q])
+    float Qd[KMODE == SIM_KALMAN_LANE ? MAXS : 1], Pm[KMODE == SIM_KALMAN_LANE ? MAXS * MAXS : 1];
+    float KG[KAL ? MAXS : 1];
+    float Rn = 0.0f;
+    KalShared S;
+    float *Ps = nullptr, *Ts = nullptr;
+    const int lane = tid & 31;
+    if constexpr (KMODE == SIM_KALMAN_LANE) {
+        Rn = row[2 * ns + 1];
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) Qd[i] = i < ns ? row[2 * ns + 2 + i] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < MAXS * MAXS; ++i) Pm[i] = 0.0f;
+    }
+    if constexpr (SHARED) {
+        // the warp must hold one set of noise weights bit for bit; if not (two
+        // sets in one hash bucket), its candidates go to the per-candidate form
+        unsigned eq = 1u, pred;
+        Rn = row[2 * ns + 1];
+        __match_all_sync(0xffffffffu, __float_as_uint(Rn), (int*)&pred);
+        eq &= pred ? 1u : 0u;
+        for (int i = 0; i < ns; ++i) {
+            __match_all_sync(0xffffffffu, __float_as_uint(row[2 * ns + 2 + i]), (int*)&pred);
+            eq &= pred ? 1u : 0u;
+        }
+        if (!eq) {
+            if (writer) run.kal_order[run.kal_defer + atomicAdd(&run.kal_totals[2], 1)] = (int)c;
+            return;  // warp-uniform
+        }
+        const int j = lane & (MAXS - 1), i0 = lane >> 3, i1 = i0 + 4;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            S.a0[k] = P.ss_a[i0 * MAXS + k];
+            S.a1[k] = P.ss_a[i1 * MAXS + k];
+            S.aj[k] = P.ss_a[j * MAXS + k];
+            S.kg[k] = S.kgo[k] = 0.0f;
+        }
+        S.q0 = i0 < ns ? row[2 * ns + 2 + i0] : 0.0f;
+        S.q1 = i1 < ns ? row[2 * ns + 2 + i1] : 0.0f;
+        S.r = Rn;
+        S.p0 = S.p1 = S.o0 = S.o1 = 0.0f;
+        S.mode = 0;
+        S.t = 0;
+        Ps = kps[tid >> 5][0];
+        Ts = kps[tid >> 5][1];
+        Ps[lane] = 0.0f;
+        Ps[lane + 32] = 0.0f;
+        __syncwarp();
+    }
 
     float xh_hi[NSC], xh_lo[NSC], xp_hi[NDC], xp_lo[NDC];
 #pragma unroll
@@ -131,14 +458,16 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
                     a.x = stage[0][tid]; a.y = stage[1][tid]; a.z = stage[2][tid]; a.w = stage[3][tid];
                     b.x = stage[4][tid]; b.y = stage[5][tid]; b.z = stage[6][tid]; b.w = stage[7][tid];
                     float4* dst = reinterpret_cast<float4*>(wrow + (w & ~7));
-                    dst[0] = a;
-                    dst[1] = b;
+                    if (writer) {
+                        dst[0] = a;
+                        dst[1] = b;
+                    }
                 }
             }
             if (t >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
             ymax = fmaxf(ymax, y);
             ymin = fminf(ymin, y);
-            if (run.store_traj) traj[c * (int64_t)T + t] = y;
+            if (run.store_traj && writer) traj[c * (int64_t)T + t] = y;
         }
 
         // controller output
@@ -153,42 +482,54 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
         const float u_raw = __fmaf_rn(N, ref, -kx);
         const float u = Chains::u(P, Lc, xh_hi, &srcH[0][tid], u_raw);
 
-        // observer output error
-        float yh = 0.0f;
+        if constexpr (KAL) {
+            kalman_predict(P, xh_hi, xh_lo, u);
+            if constexpr (SHARED) {
+                kalman_cov_shared(P, S, Ps, Ts, lane);
 #pragma unroll
-        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_hi[i], yh);
-        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
-#pragma unroll
-        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_lo[i], yh);
-        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
-        yh = __fmaf_rn(P.ss_d, u, yh);
-        const float yerr = __fsub_rn(y, yh);
-
-        // observer increment (A-I)xh + B u + L yerr, then double-float add
-        float dh[NSC], dl[NSC];
-#pragma unroll
-        for (int i = 0; i < NSC; ++i) {
-            float h = __fmaf_rn(L[i], yerr, __fmul_rn(P.ss_b[i], u));
-            float l = 0.0f;
-#pragma unroll
-            for (int j = 0; j < NSC; ++j) h = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_hi[j], h);
-#pragma unroll
-            for (int j = 0; j < NSC; ++j) l = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_lo[j], l);
-            if (NSC < MAXS) {
-                h = __fadd_rn(h, padS);
-                l = __fadd_rn(l, padS);
+                for (int i = 0; i < MAXS; ++i) KG[i] = S.kg[i];
+            } else {
+                kalman_cov_lane(P, Pm, Qd, Rn, KG);
             }
-            dh[i] = h;
-            dl[i] = l;
-        }
-        if (NSC < MAXS) {
-            bool bad = !isfinite(yerr) || !isfinite(u);
+            kalman_correct(P, xh_hi, xh_lo, y, KG);
+        } else {
+            // observer output error
+            float yh = 0.0f;
 #pragma unroll
-            for (int j = 0; j < NSC; ++j) bad = bad || !isfinite(xh_hi[j]) || !isfinite(xh_lo[j]);
-            poisS = poisS || bad;
-        }
+            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_hi[i], yh);
+            if (NSC < MAXS) yh = __fadd_rn(yh, padS);
 #pragma unroll
-        for (int i = 0; i < NSC; ++i) df_add(xh_hi[i], xh_lo[i], dh[i], dl[i]);
+            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_lo[i], yh);
+            if (NSC < MAXS) yh = __fadd_rn(yh, padS);
+            yh = __fmaf_rn(P.ss_d, u, yh);
+            const float yerr = __fsub_rn(y, yh);
+
+            // observer increment (A-I)xh + B u + L yerr, then double-float add
+            float dh[NSC], dl[NSC];
+#pragma unroll
+            for (int i = 0; i < NSC; ++i) {
+                float h = __fmaf_rn(L[i], yerr, __fmul_rn(P.ss_b[i], u));
+                float l = 0.0f;
+#pragma unroll
+                for (int j = 0; j < NSC; ++j) h = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_hi[j], h);
+#pragma unroll
+                for (int j = 0; j < NSC; ++j) l = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_lo[j], l);
+                if (NSC < MAXS) {
+                    h = __fadd_rn(h, padS);
+                    l = __fadd_rn(l, padS);
+                }
+                dh[i] = h;
+                dl[i] = l;
+            }
+            if (NSC < MAXS) {
+                bool bad = !isfinite(yerr) || !isfinite(u);
+#pragma unroll
+                for (int j = 0; j < NSC; ++j) bad = bad || !isfinite(xh_hi[j]) || !isfinite(xh_lo[j]);
+                poisS = poisS || bad;
+            }
+#pragma unroll
+            for (int i = 0; i < NSC; ++i) df_add(xh_hi[i], xh_lo[i], dh[i], dl[i]);
+        }
 
         // nonlinear terms over [xp_hi, y]
         float W[MAXW];
@@ -230,7 +571,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
     sm.ymax = ymax;
     sm.ymin = ymin;
     sm.pad = 0.0f;
-    summ[c] = sm;
+    if (writer) summ[c] = sm;
 }
 
 // The instruction tables of the plant, interpreted (any program, no compile step).

@@ -61,7 +61,7 @@ class Problem:
     name: str
     config_text: str
     plant: PlantFiles
-    cuda_mx: np.ndarray   # n x (2ns+1)
+    cuda_mx: np.ndarray   # n x (2ns+1), or n x (3ns+2) with the Kalman observer
     info_mx: np.ndarray   # n x info_w
     n_plants: int = 1
 
@@ -164,7 +164,10 @@ def output_first_basis(A, B, C):
 
 
 def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 400, pool: int = 64,
-                input_size: int = 17) -> Problem:
+                input_size: int = 17, observer: str = "luenberger") -> Problem:
+    """The eight-state workload.  observer="kalman" runs the time-varying Kalman filter in the
+    simulation: each row becomes [K, L, N, R, Q] with the noise weights (R, diag Q) that L was
+    computed from, and the config says `observer = kalman`."""
     rng = np.random.default_rng(seed)
     ns = nd = 8
     A0 = stable_spectrum_matrix(rng, 8)
@@ -193,7 +196,7 @@ def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 40
         statespace_d=np.zeros(1, F32), discrete_a=Af, discrete_a_i=Af - np.eye(8, dtype=F32), discrete_bu=Bf,
         discrete_bw=Bw.astype(F32), discrete_c=Cz.astype(F32), base_params=bp, dc_info=dc, u_info=u, nl_info=nl)
     # a pool of LQR state-feedback and steady-state Kalman predictor gains from seeded weights
-    Ks, Ls = [], []
+    Ks, Ls, Rs, Qs = [], [], [], []
     for _ in range(pool):
         Qk = np.diag(np.exp(rng.uniform(np.log(1e-2), np.log(1e1), 8)))
         Rk = np.array([[np.exp(rng.uniform(np.log(1e-1), np.log(1e1)))]])
@@ -203,7 +206,9 @@ def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 40
         Ro = np.array([[np.exp(rng.uniform(np.log(1e-2), np.log(1e0)))]])
         S = solve_discrete_are(A.T, Cz.reshape(8, 1), Qo, Ro)
         Ls.append((A @ S @ Cz / (Cz @ S @ Cz + Ro[0, 0])).reshape(8))
-    Ks, Ls = np.array(Ks), np.array(Ls)
+        Rs.append(Ro[0, 0])
+        Qs.append(np.diag(Qo))
+    Ks, Ls, Rs, Qs = np.array(Ks), np.array(Ls), np.array(Rs), np.array(Qs)
     ki = rng.integers(0, pool, n)
     li = rng.integers(0, pool, n)
     scale = np.exp(rng.uniform(np.log(0.3), np.log(4.0), (n, 1)))
@@ -214,6 +219,12 @@ def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 40
     dcg = np.einsum("j,njk,k->n", Cz, np.linalg.inv(np.eye(8)[None] - Acl), B[:, 0])
     N = (1.0 / np.where(np.abs(dcg) > 1e-6, dcg, 1.0)) * rng.uniform(0.8, 1.2, n)
     gains = np.hstack([K, L, N[:, None]]).astype(F32)
+    extra = {}
+    if observer == "kalman":
+        gains = np.hstack([gains, Rs[li][:, None].astype(F32), Qs[li].astype(F32)])
+        extra["observer"] = "kalman"
+    elif observer != "luenberger":
+        raise ValueError(f"observer {observer!r}")
     iw = info_width(ns, nd, input_size)
     info = np.zeros((n, iw), F32)
     info[:, :min(input_size, 17)] = gains[:, :min(input_size, 17)]
@@ -223,8 +234,8 @@ def eight_state(n: int = 65536, seed: int = 2, time: int = 10000, freq: int = 40
         mode="batch", time=time, duration=time * 1e-3, ref_step_time=0.05, ref_amplitude=1.0, fit_start=0.05,
         fit_end=0.75, steady_start=0.75, bandwidth=10.0, damping=0.6, overshoot=0.10, steady_state_error=0.05,
         crossover_coeff=1.0, target_gm=9.0, target_pm=55.0, target_b=0.2, eig_fail_err=1.0e18, unstable_err=1.0e6,
-        freq=freq, freq_min=0.1)
-    return Problem("eight_state", text, plant, gains, info)
+        freq=freq, freq_min=0.1, **extra)
+    return Problem("eight_state" if observer == "luenberger" else "eight_state_kalman", text, plant, gains, info)
 
 
 def stable_matrix(rng, n: int, rmin=0.85, rmax=0.995, thmin=0.01, thmax=0.5) -> np.ndarray:
@@ -350,3 +361,18 @@ def monte_carlo(n_plants: int = 262144, seed: int = 3, time: int = 8000, freq: i
     text = base.config_text.replace("mode = batch", "mode = serial" if serial else "mode = batch")
     text = text.replace("target_gm = 9.0", "target_gm = 6.0").replace("target_pm = 55.0", "target_pm = 45.0")
     return Problem(f"monte_carlo_{n_plants}", text, plant, gains, info, n_plants=n_plants)
+
+
+def with_kalman(p: Problem, seed: int = 7, r_range=(1e-2, 1.0), q_range=(1e-4, 1e-1)) -> Problem:
+    """`p` with the time-varying Kalman observer: every row gets a measurement weight R and
+    the diagonal of Q appended (log-uniform in the given ranges, seeded), and the config says
+    `observer = kalman`.  K, L, N are kept, so LIN_A and the margin sweep see the same loop."""
+    import dataclasses
+    kv = {k.strip(): v.strip() for k, v in (line.split("=", 1) for line in p.config_text.splitlines() if "=" in line)}
+    ns = int(kv["statespace_dim"])
+    rng = np.random.default_rng(seed)
+    n = p.cuda_mx.shape[0]
+    lg = lambda lo, hi, size: np.exp(rng.uniform(np.log(lo), np.log(hi), size))
+    rq = np.hstack([lg(*r_range, (n, 1)), lg(*q_range, (n, ns))]).astype(F32)
+    return dataclasses.replace(p, name=p.name + "_kalman", config_text=p.config_text + "observer = kalman\n",
+                               cuda_mx=np.hstack([p.cuda_mx.astype(F32), rq]))

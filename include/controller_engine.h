@@ -49,6 +49,10 @@ extern "C" {
 #define CE_OPERAND_STATE 1
 #define CE_OPERAND_PREV 2
 
+/* Observer of the simulated loop (ce_config.observer). */
+#define CE_OBSERVER_LUENBERGER 0
+#define CE_OBSERVER_KALMAN 1
+
 /* Arithmetic of a session. */
 #define CE_PRECISION_MIXED 0 /* reference arithmetic: FP32 double-float simulation, FP32 fit and sweep, FP64 eigensolves */
 #define CE_PRECISION_FP64 1  /* the plain FP64 form of the same method: every stage in FP64 */
@@ -89,6 +93,13 @@ typedef struct ce_config {
     int32_t fit_start_id, steady_start_id;
     int32_t fit_steps;   /* number of fit samples: #{t >= 0 : (float)t < (fit_end-fit_start)*time} (ref: src/modalsetup.cu:75-76) */
     int32_t ref_step_id; /* first t with !(t < ref_step_time*time) (ref: src/main.cu:414) */
+    /* extension: observer of the simulated loop (key `observer`, default luenberger).
+       CE_OBSERVER_KALMAN runs the time-varying Kalman filter of discrete_solve<Kalman>
+       (ref: src/discrete_solves.cu:83-185), which the reference never launches; its rows are
+       [K(ns), L(ns), N, R, Q(ns)] (cuda_mx_width = 3ns+2): the simulation uses K, N, R and
+       diag(Q); LIN_A, the eigensolve and the margin sweep use the [K, L, N] prefix as for the
+       Luenberger loop. */
+    int32_t observer;
 } ce_config;
 
 /* A decoded instruction (ref: src/main.cu:75-82). */

@@ -56,6 +56,7 @@ typedef struct oc_cfg {
     float eig_fail_err, unstable_err;
     int32_t freq;
     float freq_min, freq_max_key;
+    int32_t observer; /* 0 Luenberger, 1 time-varying Kalman (key `observer`) */
 } oc_cfg;
 
 /* one round's plant, compact row-major as in the .bin files */
@@ -82,7 +83,7 @@ static void derive(const oc_cfg* c, oc_der* d) {
     d->ts = c->duration / (float)c->time;
     d->freq_max = c->freq_max_key > 0.0f ? c->freq_max_key : PI_F / d->ts;
     d->nt = c->ns + c->nd;
-    d->cuda_w = 2 * c->ns + 1;
+    d->cuda_w = c->observer ? 3 * c->ns + 2 : 2 * c->ns + 1;
     d->info_scoring = c->input_size;
     d->info_freqresp = d->info_scoring + 3;
     d->info_allmargin = d->info_freqresp + 4;
@@ -249,6 +250,143 @@ static void sim_one(const oc_cfg* c, const oc_der* d, const oc_pp* P, const floa
             dl[i] = vdot(&P->ss_ai[i * MS], xh_lo, MS, 0.0f);
         }
         for (int i = 0; i < MS; i++) dfadd(&xh_hi[i], &xh_lo[i], dh[i], dl[i]);
+        float src[MNL];
+        for (int i = 0; i < MD; i++) src[i] = xp_hi[i];
+        src[MD] = y;
+        float W[MW];
+        for (int i = 0; i < MW; i++) W[i] = interp(&P->nl[i * MNLI], MNLI, src, MNL, 0, 0.0f);
+        float ph[MD], pl[MD];
+        for (int i = 0; i < MD; i++) {
+            const float base = vdot(&P->d_bw[i * MW], W, MW, P->d_bu[i] * u);
+            ph[i] = vdot(&P->d_ai[i * MD], xp_hi, MD, base);
+            pl[i] = vdot(&P->d_ai[i * MD], xp_lo, MD, 0.0f);
+        }
+        for (int i = 0; i < MD; i++) dfadd(&xp_hi[i], &xp_lo[i], ph[i], pl[i]);
+    }
+}
+
+/* ---- Kalman observer simulation (ref: src/discrete_solves.cu:83-185) ------
+   The reference's discrete_solve<Kalman>, restated with three changes:
+   - the row is [K(ns), L(ns), N, R, Q(ns)] (3ns+2 floats; the Luenberger row
+     [K, L, N] followed by the noise weights), where the reference reads
+     [K, N, R, Q] (2ns+2 floats) from a row 2ns+1 wide, one float into the
+     next candidate's row (:88-95 against src/config.cu:51);
+   - the Joseph product (I - KG C) P (I - KG C)^T goes to its own buffer; the
+     reference passes IKHP as both the left factor and the output of ABATf
+     (:160), so its rows are overwritten while still being read;
+   - 1/(C P C^T + R) is the correctly rounded quotient; the reference calls
+     the approximate __fdividef (:137), whose last bits are not specified.
+   Everything else -- the 8-wide padded loops, the fma chains in k order from
+   0, the rounded (not fused) products -- is the reference's.  `literal` = 1
+   instead runs the reference's row layout [K, N, R, Q] and its in-place
+   Joseph product in source order (each element written before the next is
+   read), for checking this restatement against the reference's own kernel. */
+/* out = (A B) A^T over the padded 8 x 8 arrays (ref: src/main.cu:190-212, ABATf<8,8>);
+   out may be B.  abat8_inplace_a writes the result over A, each element as
+   soon as it is formed, as the reference's source does for ABATf(IKHP,P,IKHP). */
+static void abat8(const float* A, const float* B, float* out) {
+    float C0[MS * MS];
+    for (int i = 0; i < MS; i++)
+        for (int j = 0; j < MS; j++) {
+            float c = 0.0f;
+            for (int k = 0; k < MS; k++) c = fmaf(A[i * MS + k], B[k * MS + j], c);
+            C0[i * MS + j] = c;
+        }
+    float R[MS * MS];
+    for (int i = 0; i < MS; i++)
+        for (int j = 0; j < MS; j++) {
+            float c = 0.0f;
+            for (int k = 0; k < MS; k++) c = fmaf(C0[i * MS + k], A[j * MS + k], c);
+            R[i * MS + j] = c;
+        }
+    memcpy(out, R, sizeof(R));
+}
+
+static void abat8_inplace_a(float* A, const float* B) {
+    float C0[MS * MS];
+    for (int i = 0; i < MS; i++)
+        for (int j = 0; j < MS; j++) {
+            float c = 0.0f;
+            for (int k = 0; k < MS; k++) c = fmaf(A[i * MS + k], B[k * MS + j], c);
+            C0[i * MS + j] = c;
+        }
+    for (int i = 0; i < MS; i++)
+        for (int j = 0; j < MS; j++) {
+            float c = 0.0f;
+            for (int k = 0; k < MS; k++) c = fmaf(C0[i * MS + k], A[j * MS + k], c);
+            A[i * MS + j] = c;
+        }
+}
+
+static void sim_kalman_one(const oc_cfg* c, const oc_pp* P, const float* row, float* y_out, int literal,
+                           int* steady_step) {
+    const int n = c->ns;
+    float K[MS] = {0}, Q[MS] = {0};
+    const int oN = literal ? n : 2 * n;
+    for (int i = 0; i < MS; i++) {
+        K[i] = i < n ? row[i] : 0.0f;
+        Q[i] = i < n ? row[oN + 2 + i] : 0.0f;
+    }
+    const float N = row[oN], R = row[oN + 1];
+    float xh_hi[MS] = {0}, xh_lo[MS] = {0}, xp_hi[MD] = {0}, xp_lo[MD] = {0};
+    float Pm[MS * MS] = {0}, KG[MS] = {0}, PHT[MS], IKHP[MS * MS], J[MS * MS], C0[MS];
+    if (steady_step) *steady_step = -1;
+    for (int t = 0; t < c->time; t++) {
+        const float y = interp(P->dc, MDC, xp_hi, MD, 0, 0.0f);
+        y_out[t] = y;
+        const float ref = ((double)t < c->ref_step_time * (double)c->time) ? 0.0f : c->ref_amplitude;
+        const float kx = vdot(K, xh_lo, MS, vdot(K, xh_hi, MS, 0.0f));
+        const float u_raw = fmaf(N, ref, -kx);
+        const float u = interp(P->u, MU, xh_hi, MS, 1, u_raw);
+        /* prediction: xh += (A-I) xh + B u */
+        float dh[MS], dl[MS];
+        for (int i = 0; i < MS; i++) {
+            dh[i] = vdot(&P->ss_ai[i * MS], xh_hi, MS, P->ss_b[i] * u);
+            dl[i] = vdot(&P->ss_ai[i * MS], xh_lo, MS, 0.0f);
+        }
+        for (int i = 0; i < MS; i++) dfadd(&xh_hi[i], &xh_lo[i], dh[i], dl[i]);
+        float P0[MS * MS];
+        memcpy(P0, Pm, sizeof(Pm));
+        /* P = A P A^T + diag(Q) */
+        abat8(P->ss_a, Pm, Pm);
+        for (int i = 0; i < MS; i++) Pm[i * MS + i] = Pm[i * MS + i] + Q[i];
+        /* gain: PHT = P C^T, HPHR = 1/(C P C^T + R), KG = PHT HPHR */
+        for (int i = 0; i < MS; i++) PHT[i] = vdot(&Pm[i * MS], P->ss_c, MS, 0.0f);
+        for (int j = 0; j < MS; j++) {
+            float a = 0.0f;
+            for (int k = 0; k < MS; k++) a = fmaf(P->ss_c[k], Pm[k * MS + j], a);
+            C0[j] = a;
+        }
+        const float hphr = 1.0f / (vdot(C0, P->ss_c, MS, 0.0f) + R);
+        for (int i = 0; i < MS; i++) KG[i] = PHT[i] * hphr;
+        /* correction: xh += KG (y - C xh) as double-float products */
+        const float dzh = -1.0f * vdot(P->ss_c, xh_hi, MS, -y);
+        const float dzl = -1.0f * vdot(P->ss_c, xh_lo, MS, 0.0f);
+        for (int i = 0; i < MS; i++) {
+            const float s = KG[i] * dzh;
+            float e = fmaf(KG[i], dzh, -s);
+            e = fmaf(KG[i], dzl, e);
+            dfadd(&xh_hi[i], &xh_lo[i], s, e);
+        }
+        /* P = (I - KG C) P (I - KG C)^T + KG R KG^T, IKHP formed as the reference forms it */
+        for (int i = 0; i < MS; i++)
+            for (int j = 0; j < MS; j++) {
+                float m = fmaf(KG[i], P->ss_c[j], 0.0f);
+                if (i == j) m = m - 1.0f;
+                IKHP[i * MS + j] = -m;
+            }
+        if (literal) {
+            abat8_inplace_a(IKHP, Pm);
+            memcpy(J, IKHP, sizeof(J));
+        } else {
+            abat8(IKHP, Pm, J);
+        }
+        for (int i = 0; i < MS; i++) {
+            const float kr = fmaf(KG[i], R, 0.0f);
+            for (int j = 0; j < MS; j++) Pm[i * MS + j] = J[i * MS + j] + fmaf(kr, KG[j], 0.0f);
+        }
+        if (steady_step && *steady_step < 0 && memcmp(P0, Pm, sizeof(Pm)) == 0) *steady_step = t;
+        /* nonlinear terms and plant, as the Luenberger loop */
         float src[MNL];
         for (int i = 0; i < MD; i++) src[i] = xp_hi[i];
         src[MD] = y;
@@ -1043,7 +1181,25 @@ int oracle_sim(const oc_cfg* c, const oc_plant* p, int64_t n, const float* cuda_
     const int rc = pad_plant(c, p, &P);
     if (rc) return rc;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
-    for (int64_t k = 0; k < n; k++) sim_one(c, &d, &P, cuda_mx + k * d.cuda_w, y + k * (int64_t)c->time);
+    for (int64_t k = 0; k < n; k++) {
+        if (c->observer) sim_kalman_one(c, &P, cuda_mx + k * d.cuda_w, y + k * (int64_t)c->time, 0, NULL);
+        else sim_one(c, &d, &P, cuda_mx + k * d.cuda_w, y + k * (int64_t)c->time);
+    }
+    return 0;
+}
+
+/* The Kalman loop in the reference's literal form (row [K, N, R, Q] of
+   `width` floats, in-place Joseph product), or the engine's form (literal 0,
+   rows of the config's width); steady[k] = first step whose covariance update
+   left P bit for bit unchanged (-1: none). */
+int oracle_sim_kalman(const oc_cfg* c, const oc_plant* p, int64_t n, const float* rows, int width, int literal,
+                      float* y, int32_t* steady, int threads) {
+    oc_pp P;
+    const int rc = pad_plant(c, p, &P);
+    if (rc) return rc;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+    for (int64_t k = 0; k < n; k++)
+        sim_kalman_one(c, &P, rows + k * width, y + k * (int64_t)c->time, literal, steady ? &steady[k] : NULL);
     return 0;
 }
 

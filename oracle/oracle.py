@@ -37,7 +37,8 @@ class oc_cfg(C.Structure):
                 ("bandwidth", C.c_float), ("damping", C.c_float), ("overshoot", C.c_float), ("sse", C.c_float),
                 ("crossover_coeff", C.c_float), ("target_gm", C.c_float), ("target_pm", C.c_float),
                 ("target_b", C.c_float), ("eig_fail_err", C.c_float), ("unstable_err", C.c_float),
-                ("freq", C.c_int32), ("freq_min", C.c_float), ("freq_max_key", C.c_float)]
+                ("freq", C.c_int32), ("freq_min", C.c_float), ("freq_max_key", C.c_float),
+                ("observer", C.c_int32)]
 
 
 _FP = C.POINTER(C.c_float)
@@ -65,6 +66,8 @@ def lib():
         L = C.CDLL(str(LIB))
         i64 = C.c_int64
         L.oracle_sim.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, _FP, C.c_int]
+        L.oracle_sim_kalman.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, C.c_int, C.c_int, _FP,
+                                        _IP, C.c_int]
         L.oracle_lina.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, _FP, C.c_int]
         L.oracle_eigensolve.argtypes = [i64, C.c_int, _FP, _FP, _DP, C.c_int]
         L.oracle_eigensolve.restype = None
@@ -121,6 +124,7 @@ def make_cfg(text: str) -> oc_cfg:
     c.freq = int(float(g("freq")))
     c.freq_min = float(g("freq_min"))
     c.freq_max_key = float(g("freq_max", "0"))
+    c.observer = 1 if g("observer", "luenberger") == "kalman" else 0
     return c
 
 
@@ -157,7 +161,7 @@ class Oracle:
         self.plant = p
         self.nt = c.ns + c.nd
         self.info_w = lib().oracle_info_width(C.byref(c))
-        self.cuda_w = 2 * c.ns + 1
+        self.cuda_w = 3 * c.ns + 2 if c.observer else 2 * c.ns + 1
 
     def _g(self, cuda_mx):
         g = np.ascontiguousarray(cuda_mx, F32).reshape(-1, self.cuda_w)
@@ -170,6 +174,19 @@ class Oracle:
         if rc:
             raise ValueError(f"oracle decode error (digit {rc - 1})")
         return y
+
+    def sim_kalman(self, rows, literal: bool = False):
+        """The Kalman observer loop; `literal`: the reference's own row layout [K, N, R, Q]
+        and in-place Joseph product.  Returns (y, first step at which P stopped changing)."""
+        rows = np.ascontiguousarray(rows, F32)
+        n, w = rows.shape
+        y = np.empty((n, self.cfg.time), F32)
+        steady = np.empty(n, I32)
+        rc = lib().oracle_sim_kalman(C.byref(self.cfg), C.byref(self.plant), n, _f(rows), w, int(literal), _f(y),
+                                     steady.ctypes.data_as(_IP), self.threads)
+        if rc:
+            raise ValueError(f"oracle decode error (digit {rc - 1})")
+        return y, steady
 
     def lina(self, cuda_mx):
         g, n = self._g(cuda_mx)

@@ -50,13 +50,11 @@ def _ops(decoded, count):
     return bytes(buf)
 
 
-def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray):
-    """cfg: an engine EngineConfig (its parser is pinned to the reference's).  Returns
-    (yplant, lina, ata, atb, info) from the reference kernels."""
+def _tables(cfg, plant, n: int, cuda_w: int):
+    """ENGINE bytes, padded constant tables, decoded DC/U/NL records and ref[t]."""
     from oracle import oracle as O
     ns, nd, nw, nt = cfg.statespace_dim, cfg.discrete_dim, cfg.nonlin_dim, cfg.total_dim
-    n = cuda_mx.shape[0]
-    engine = struct.pack("<15i6f", n, cfg.time, ns, nd, nt, cfg.cuda_mx_width, cfg.info_mx_width, cfg.info_scoring,
+    engine = struct.pack("<15i6f", n, cfg.time, ns, nd, nt, cuda_w, cfg.info_mx_width, cfg.info_scoring,
                          cfg.info_freqresp, cfg.eigen_mx_width, cfg.lina_mx_width, cfg.ata_mx_width,
                          cfg.atb_mx_width, cfg.fit_start_id, cfg.steady_start_id, cfg.ts, cfg.fit_start,
                          cfg.fit_end, cfg.fit_t0, cfg.fit_t1, cfg.unstable_err)
@@ -88,8 +86,20 @@ def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray)
     dc = (list(dc) + [skip] * 4)[:4]
     u = (list(u) + [skip] * 4)[:4]
     ref = np.array([0.0 if t < cfg.ref_step_time * cfg.time else cfg.ref_amplitude for t in range(cfg.time)], F32)
+    return engine, tabs, _ops(dc, 4), _ops(u, 4), _ops(nl, 32), ref
+
+
+_fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray):
+    """cfg: an engine EngineConfig (its parser is pinned to the reference's).  Returns
+    (yplant, lina, ata, atb, info) from the reference kernels."""
+    nt = cfg.total_dim
+    n = cuda_mx.shape[0]
+    engine, tabs, dc, u, nl, ref = _tables(cfg, plant, n, cfg.cuda_mx_width)
     L = _runner()
-    tab_ptrs = (C.POINTER(C.c_float) * 11)(*[t.ctypes.data_as(C.POINTER(C.c_float)) for t in tabs])
+    tab_ptrs = (C.POINTER(C.c_float) * 11)(*[_fp(t) for t in tabs])
     g = np.ascontiguousarray(cuda_mx, F32)
     e = np.ascontiguousarray(eigen, F32)
     inf = np.ascontiguousarray(info_in, F32)
@@ -98,10 +108,26 @@ def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray)
     ata = np.empty((n, 4 * nt * nt), F32)
     atb = np.empty((n, 2 * nt), F32)
     out = np.empty_like(inf)
-    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
-    rc = L.ref_run(str(CUBIN).encode(), engine, len(engine), tab_ptrs, _ops(dc, 4), _ops(u, 4), _ops(nl, 32), n,
-                   cfg.time, cfg.cuda_mx_width, nt, cfg.info_mx_width, fp(g), fp(ref), fp(e), fp(inf), fp(y),
-                   fp(lina), fp(ata), fp(atb), fp(out))
+    rc = L.ref_run(str(CUBIN).encode(), engine, len(engine), tab_ptrs, dc, u, nl, n,
+                   cfg.time, cfg.cuda_mx_width, nt, cfg.info_mx_width, _fp(g), _fp(ref), _fp(e), _fp(inf), _fp(y),
+                   _fp(lina), _fp(ata), _fp(atb), _fp(out))
     if rc:
         raise RuntimeError(L.ref_runner_error().decode())
     return y, lina, ata, atb, out
+
+
+def run_kalman(cfg, plant, rows: np.ndarray):
+    """The reference's discrete_solve<Kalman> on rows of its own layout [K(ns), N, R, Q(ns)]
+    (2ns+2 floats, given to the kernel as ENGINE.cuda_mx_width).  Returns yplant."""
+    rows = np.ascontiguousarray(rows, F32)
+    n, w = rows.shape
+    assert w == 2 * cfg.statespace_dim + 2
+    engine, tabs, dc, u, nl, ref = _tables(cfg, plant, n, w)
+    L = _runner()
+    tab_ptrs = (C.POINTER(C.c_float) * 11)(*[_fp(t) for t in tabs])
+    y = np.empty((n, cfg.time), F32)
+    rc = L.ref_run_kalman(str(CUBIN).encode(), engine, len(engine), tab_ptrs, dc, u, nl, n, cfg.time, w, _fp(rows),
+                          _fp(ref), _fp(y))
+    if rc:
+        raise RuntimeError(L.ref_runner_error().decode())
+    return y

@@ -1,5 +1,5 @@
 // ref_kernel_runner.cpp -- runs the REFERENCE's own kernels (discrete_solve<Luenberger>,
-// eigensetup, modalsetup from src/main.cu, compiled into oracle/_ref/ref_kernels.cubin by
+// eigensetup, modalsetup and the unlaunched discrete_solve<Kalman> from src/main.cu, compiled into oracle/_ref/ref_kernels.cubin by
 // oracle/Makefile) through the CUDA driver API, with the reference's launch shape
 // (256 threads per block, one thread per candidate, ref: src/main.cu:408-409) and
 // its __constant__ tables set exactly as init64KB/upload_plant set them.
@@ -31,7 +31,7 @@ std::string g_err;
 
 CUmodule g_mod = nullptr;
 CUcontext g_ctx = nullptr;
-CUfunction g_sim = nullptr, g_setup = nullptr, g_modal = nullptr;
+CUfunction g_sim = nullptr, g_setup = nullptr, g_modal = nullptr, g_kalman = nullptr;
 
 int set_global(const char* name, const void* src, size_t bytes) {
     CUdeviceptr p;
@@ -63,6 +63,8 @@ int load(const char* cubin) {
         CK(cuFuncGetName(&nm, f));
         const std::string s = nm ? nm : "";
         if (s.find("discrete_solve") != std::string::npos && s.find("ControllerType0") != std::string::npos) g_sim = f;
+        else if (s.find("discrete_solve") != std::string::npos && s.find("ControllerType1") != std::string::npos)
+            g_kalman = f;
         else if (s.find("eigensetup") != std::string::npos) g_setup = f;
         else if (s.find("modalsetup") != std::string::npos) g_modal = f;
     }
@@ -139,6 +141,46 @@ int ref_run(const char* cubin, const void* engine, int engine_bytes, const float
     CK(cuMemcpyDtoH(atb, d_b, bsz * 4));
     CK(cuMemcpyDtoH(info_out, d_i, isz * 4));
     for (CUdeviceptr p : {d_g, d_ref, d_y, d_l, d_e, d_a, d_b, d_i}) cuMemFree(p);
+    return 0;
+}
+
+// The reference's discrete_solve<Kalman> (src/discrete_solves.cu:83-185, never
+// launched by the reference itself) on rows of its own layout [K(ns), N, R,
+// Q(ns)]: the caller sets ENGINE.cuda_mx_width = cuda_w = 2ns+2, so every row
+// the kernel reads lies inside `rows`.  Only the trajectory is produced.
+int ref_run_kalman(const char* cubin, const void* engine, int engine_bytes, const float* const* tables,
+                   const void* dc_ops, const void* u_ops, const void* nl_ops, int n, int time, int cuda_w,
+                   const float* rows, const float* ref, float* yplant) {
+    if (load(cubin)) return 1;
+    if (!g_kalman) {
+        g_err = "discrete_solve<Kalman> not found in " + std::string(cubin);
+        return 1;
+    }
+    CK(cuCtxSetCurrent(g_ctx));
+    if (set_global("ENGINE", engine, engine_bytes)) return 1;
+    const char* names[11] = {"STATESPACE_A", "STATESPACE_A_I", "STATESPACE_B", "STATESPACE_C", "STATESPACE_D",
+                             "DISCRETE_A",   "DISCRETE_A_I",   "DISCRETE_BU",  "DISCRETE_BW",  "DISCRETE_C",
+                             "BASE_PARAMS"};
+    const size_t sizes[11] = {64, 64, 8, 8, 1, 64, 64, 8, 32, 8, 34};
+    for (int i = 0; i < 11; ++i)
+        if (set_global(names[i], tables[i], sizes[i] * sizeof(float))) return 1;
+    if (set_global("DC_OPS", dc_ops, 4 * 24) || set_global("U_OPS", u_ops, 4 * 24) ||
+        set_global("NL_OPS", nl_ops, 32 * 24))
+        return 1;
+    const size_t ysz = (size_t)n * time, gsz = (size_t)n * cuda_w;
+    CUdeviceptr d_g, d_ref, d_y;
+    CK(cuMemAlloc(&d_g, gsz * 4));
+    CK(cuMemAlloc(&d_ref, (size_t)time * 4));
+    CK(cuMemAlloc(&d_y, ysz * 4));
+    CK(cuMemcpyHtoD(d_g, rows, gsz * 4));
+    CK(cuMemcpyHtoD(d_ref, ref, (size_t)time * 4));
+    CK(cuMemsetD8(d_y, 0, ysz * 4));
+    const unsigned tpb = 256, blocks = (n + tpb - 1) / tpb;
+    void* args[] = {&d_g, &d_ref, &d_y};
+    CK(cuLaunchKernel(g_kalman, blocks, 1, 1, tpb, 1, 1, 0, nullptr, args, nullptr));
+    CK(cuCtxSynchronize());
+    CK(cuMemcpyDtoH(yplant, d_y, ysz * 4));
+    for (CUdeviceptr p : {d_g, d_ref, d_y}) cuMemFree(p);
     return 0;
 }
 }

@@ -110,6 +110,18 @@ def test_generated_source_names_the_program(mass_spring):
     cfg = EngineConfig.parse(mass_spring.config_text)
     with Session(cfg, mass_spring.plant) as s:
         src = s.specialised_source(0)
-    assert "ce_sim_specialised" in src and "ce::sim_run<4, 4, cejit::Chains>" in src
+    assert "ce_sim_specialised" in src and "ce::sim_run<4, 4, cejit::Chains, ce::SIM_LUENBERGER>" in src
+    assert "ce_sim_kalman_shared" not in src
     # the mass-spring NL chain is k3 * x0^3: three multiplies on x0
     assert src.count("__fmul_rn") >= 4
+
+
+def test_kalman_source_has_both_forms(mass_spring):
+    """A Kalman session's program holds the per-candidate and the shared-noise forms, both
+    over the full padded observer width."""
+    from controllerengine_gb300 import synth
+    p = synth.with_kalman(mass_spring)
+    with Session(EngineConfig.parse(p.config_text), p.plant) as s:
+        src = s.specialised_source(0)
+    assert "ce::sim_run<8, 4, cejit::Chains, ce::SIM_KALMAN_LANE>" in src
+    assert "ce_sim_kalman_shared" in src and "ce::SIM_KALMAN_SHARED" in src

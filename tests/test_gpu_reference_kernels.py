@@ -48,3 +48,32 @@ def test_engine_kernels_equal_reference_kernels(lib, refk, which, request):
     unst = rinfo[:, s0] != p.info_mx[:, s0]  # rows the reference's modalsetup flagged unstable
     assert unst.any()
     assert _eq(info[unst, s0:s0 + 2], rinfo[unst, s0:s0 + 2]), "unstable penalty"
+
+
+def test_oracle_kalman_against_reference_kalman_kernel(refk, oracle_mod):
+    """The reference never launches discrete_solve<Kalman> (src/discrete_solves.cu:83-185);
+    here its compiled kernel runs on rows of its own layout [K, N, R, Q], given to it as the
+    row width so that no read leaves the row, against the oracle's literal form of it (that
+    layout, and the Joseph product written over its own left factor in source order).  The
+    one remaining difference is the reciprocal -- the kernel's approximate __fdividef, the
+    oracle's correctly rounded quotient -- so whole trajectories are compared row by row: at
+    least half must be identical, and the rows that blow up must be the same rows.  The
+    engine's form (own storage for the Joseph product) stays finite where the reference's
+    diverges."""
+    from controllerengine_gb300 import synth
+    for name, p in (("mass", synth.with_kalman(synth.mass_spring(256), seed=5)),
+                    ("eight", synth.eight_state(n=256, time=3000, freq=40, observer="kalman"))):
+        cfg = ce.EngineConfig.parse(p.config_text)
+        ns = cfg.statespace_dim
+        lit = np.ascontiguousarray(np.hstack([p.cuda_mx[:, :ns], p.cuda_mx[:, 2 * ns:]]))
+        y_ref = refk.run_kalman(cfg, p.plant, lit)
+        orc = oracle_mod.Oracle(p.config_text, p.plant)
+        y_lit, _ = orc.sim_kalman(lit, literal=True)
+        same = np.array([_eq(a, b) for a, b in zip(y_ref, y_lit)])
+        assert same.mean() >= 0.5, f"{name}: {same.sum()} of {len(same)} rows identical"
+        assert _eq(y_ref[:, :2], y_lit[:, :2])
+        blown_ref = ~np.isfinite(y_ref).all(axis=1)
+        assert np.array_equal(blown_ref, ~np.isfinite(y_lit).all(axis=1)), name
+        assert np.isfinite(orc.sim(p.cuda_mx)).all(), name
+        if name == "eight":
+            assert blown_ref.mean() > 0.5  # the in-place Joseph product diverges
