@@ -307,6 +307,61 @@ def monte_carlo_bench(n_plants: int, steps: int, warmup: int):
             "session_setup_s": setup, "scored_fraction": float(np.mean(sc < cfg.unstable_err))}
 
 
+def _kalman_time(p, n: int, steps: int, warmup: int):
+    import torch
+    import controllerengine_gb300 as ce
+    cfg = ce.EngineConfig.parse(p.config_text)
+    sess = ce.Session(cfg, p.plant)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = torch.from_numpy(p.cuda_mx).to(dev)
+    info = torch.from_numpy(p.info_mx).to(dev)
+    out = torch.empty_like(info)
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        sess.evaluate_device(n, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+    torch.cuda.synchronize()
+    ms = 0.0
+    sess.set_profiling(True)
+    l0 = sess.kernel_launches
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sess.evaluate_device(n, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    launches = (sess.kernel_launches - l0) // steps
+    stages = {k: v[0] / steps for k, v in sess.stage_times().items() if v[1]}
+    sess.close()
+    keys, counts = np.unique(p.cuda_mx[:, 2 * cfg.statespace_dim + 1:], axis=0, return_counts=True)
+    return {"candidates_per_s": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps,
+            "launches_per_step": launches, "stages_ms_per_step": stages, "noise_weight_sets": len(keys),
+            "shared_noise_fraction": float(counts[counts >= 8].sum() / n)}
+
+
+def kalman_bench(n: int, steps: int, warmup: int, cpu_seconds: float):
+    """The eight-state workload with the time-varying Kalman observer (rows [K, L, N, R, Q]):
+    candidates/s of ce_evaluate_device, inputs resident, CUDA events, L2 flushed between steps,
+    with the simulation stage's share.  Twice: noise weights from the 64-set pool the gains were
+    designed with (candidates share covariance recursions: the shared-noise form), and with R
+    perturbed per candidate by a factor 1 + U[0, 1e-3] (every recursion distinct: the
+    per-candidate form).  The oracle port on the host cores on a bounded sample beside it."""
+    from controllerengine_gb300 import synth
+    p = synth.eight_state(n=n, observer="kalman")
+    res = {"workload": f"eight_state with observer = kalman: {n} candidates, T = 10000, F = 400",
+           "pooled_noise": _kalman_time(p, n, steps, warmup)}
+    q = synth.Problem(p.name, p.config_text, p.plant, p.cuda_mx.copy(), p.info_mx)
+    rng = np.random.default_rng(17)
+    q.cuda_mx[:, 17] *= (1.0 + 1e-3 * rng.random(n)).astype(np.float32)
+    res["distinct_noise"] = _kalman_time(q, n, max(1, steps - 1), 1)
+    res["candidates_per_s"] = res["pooled_noise"]["candidates_per_s"]
+    if cpu_seconds > 0:
+        res["cpu_baseline"] = cpu_baseline(p, cpu_seconds, os.cpu_count() or 1)
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,6 +378,7 @@ def main():
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="Poisson serving run (0: skip)")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
+    ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -507,6 +563,8 @@ def main():
     }
     if rank == 0 and a.mc_plants > 0:
         line["monte_carlo"] = monte_carlo_bench(a.mc_plants, 2, 1)
+    if rank == 0 and a.kalman_candidates > 0:
+        line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
     if rank == 0 and a.serve_seconds > 0:
         line["serving"] = serving_bench(serving_models(), a.serve_seconds)
     if rank == 0 and not a.no_cpu:

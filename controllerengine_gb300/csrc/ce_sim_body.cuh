@@ -212,114 +212,137 @@ __device__ __forceinline__ void kalman_cov_lane(const Plant& P, float (&Pm)[MAXS
 // such candidates and computes the recursion once, cooperatively: P lives in
 // shared memory and lane l forms elements l and l + 32 (rows i0 = l/8 and
 // i1 = i0 + 4, column j = l%8) of each product, every element by the same fma
-// chain as in the per-candidate form, so the gains are bit-identical.  Once
-// P_{t+1} equals P_t bit for bit the recursion has reached a fixed point and
-// the gain stays; once P_{t+1} equals P_{t-1} the gains alternate.
-struct KalShared {
-    float a0[MAXS], a1[MAXS], aj[MAXS];  // rows i0, i1 and j of A
-    float q0, q1, r;                     // Q[i0], Q[i1], R
-    float kg[MAXS], kgo[MAXS];           // the gain of this step and of the one before
-    float p0, p1, o0, o1;                // own elements of P at the start of this step and of the one before
-    int mode;                            // 0: recursing; 1: fixed point; 2: period two
-    int t;                               // steps recursed
+// chain as in the per-candidate form, so the gains are bit-identical.  The
+// gains of the last KAL_PERIOD steps are kept in a ring, and every
+// KAL_PERIOD steps a snapshot of P is taken.  Once P_{t+1} equals the
+// snapshot P_{t0} bit for bit the recursion is periodic with period
+// p = t + 1 - t0 (p = 1: a fixed point), every later gain is the one p steps
+// earlier, and the recursion stops.
+constexpr int KAL_PERIOD = 24;
+
+// Shared memory of one warp in the shared form.
+struct KalWarp {
+    float P[MAXS * MAXS], T[MAXS * MAXS];
+    float A[MAXS * (MAXS + 1)];  // the observer's A, rows padded to 9 (no bank conflicts)
+    float kg[KAL_PERIOD][MAXS];  // KG_s of the last KAL_PERIOD steps s, by slot s % KAL_PERIOD
 };
 
-__device__ __forceinline__ void kalman_cov_shared(const Plant& P, KalShared& S, float* __restrict__ Ps,
-                                                  float* __restrict__ Ts, int lane) {
+struct KalShared {
+    float q0, q1, r;  // Q[i0], Q[i1], R
+    float snap0, snap1;  // own elements of the snapshot of P
+    int t, t_snap;    // steps recursed; step of the snapshot
+    int slot;         // ring slot of the current step
+    int period;       // 0: recursing; p: the gains repeat with period p
+    int rslot;        // periodic: ring slot of the gain p steps back
+};
+
+// The gain KG_s of the current step s into KG; advances the recursion while it runs.
+__device__ __forceinline__ void kalman_gain_shared(const Plant& P, KalShared& S, KalWarp& W, int lane,
+                                                   float (&KG)[MAXS]) {
     constexpr unsigned FULL = 0xffffffffu;
-    if (S.mode == 1) return;
-    if (S.mode == 2) {
+    const int slot = S.slot;
+    S.slot = slot + 1 == KAL_PERIOD ? 0 : slot + 1;
+    if (S.period) {
+        // KG_s = KG_{s-p}; written to this step's slot so the ring stays the last KAL_PERIOD gains
+        const int rs = S.rslot;
+        S.rslot = rs + 1 == KAL_PERIOD ? 0 : rs + 1;
 #pragma unroll
-        for (int i = 0; i < MAXS; ++i) {
-            const float k = S.kg[i];
-            S.kg[i] = S.kgo[i];
-            S.kgo[i] = k;
-        }
+        for (int i = 0; i < MAXS; ++i) KG[i] = W.kg[rs][i];
+        const float mine = W.kg[rs][lane & (MAXS - 1)];
+        __syncwarp();
+        if (lane < MAXS) W.kg[slot][lane] = mine;
+        __syncwarp();
         return;
     }
-    const int j = lane & (MAXS - 1), i0 = lane >> 3, i1 = i0 + 4;
-    // T = A P (column j of P)
-    float pc[MAXS];
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) pc[k] = Ps[k * MAXS + j];
-    float t0 = 0.0f, t1 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) {
-        t0 = __fmaf_rn(S.a0[k], pc[k], t0);
-        t1 = __fmaf_rn(S.a1[k], pc[k], t1);
+    if (S.t - S.t_snap == KAL_PERIOD || S.t == 0) {
+        S.snap0 = W.P[lane];
+        S.snap1 = W.P[lane + 32];
+        S.t_snap = S.t;
     }
-    Ts[lane] = t0;
-    Ts[lane + 32] = t1;
-    __syncwarp();
-    // P = T A^T + diag(Q)
-    float u0 = 0.0f, u1 = 0.0f;
+    {
+        const int j = lane & (MAXS - 1), i0 = lane >> 3, i1 = i0 + 4;
+        constexpr int AS = MAXS + 1;
+        // T = A P (column j of P)
+        float pc[MAXS];
 #pragma unroll
-    for (int k = 0; k < MAXS; ++k) {
-        u0 = __fmaf_rn(Ts[i0 * MAXS + k], S.aj[k], u0);
-        u1 = __fmaf_rn(Ts[i1 * MAXS + k], S.aj[k], u1);
+        for (int k = 0; k < MAXS; ++k) pc[k] = W.P[k * MAXS + j];
+        float t0 = 0.0f, t1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            t0 = __fmaf_rn(W.A[i0 * AS + k], pc[k], t0);
+            t1 = __fmaf_rn(W.A[i1 * AS + k], pc[k], t1);
+        }
+        W.T[lane] = t0;
+        W.T[lane + 32] = t1;
+        __syncwarp();
+        // P = T A^T + diag(Q)
+        float u0 = 0.0f, u1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            const float a = W.A[j * AS + k];
+            u0 = __fmaf_rn(W.T[i0 * MAXS + k], a, u0);
+            u1 = __fmaf_rn(W.T[i1 * MAXS + k], a, u1);
+        }
+        if (i0 == j) u0 = __fadd_rn(u0, S.q0);
+        if (i1 == j) u1 = __fadd_rn(u1, S.q1);
+        W.P[lane] = u0;
+        W.P[lane + 32] = u1;
+        __syncwarp();
+        // gain: lanes 0-7 form (P C^T)_l, lanes 8-15 (C P)_{l-8}; every lane forms C P C^T + R
+        float v = 0.0f;
+        if (lane < MAXS) {
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(W.P[lane * MAXS + k], P.ss_c[k], v);
+        } else if (lane < 2 * MAXS) {
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(P.ss_c[k], W.P[k * MAXS + lane - MAXS], v);
+        }
+        float h = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) h = __fmaf_rn(__shfl_sync(FULL, v, MAXS + k), P.ss_c[k], h);
+        h = __fdiv_rn(1.0f, __fadd_rn(h, S.r));
+        const float kgl = __fmul_rn(v, h);
+        if (lane < MAXS) W.kg[slot][lane] = kgl;
+        const float kgi0 = __shfl_sync(FULL, kgl, i0), kgi1 = __shfl_sync(FULL, kgl, i1);
+        const float kgj = __shfl_sync(FULL, kgl, j);
+        // T = (I - KG C) P
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) pc[k] = W.P[k * MAXS + j];
+        float w0 = 0.0f, w1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            w0 = __fmaf_rn(ikh(kgi0, P.ss_c[k], k == i0), pc[k], w0);
+            w1 = __fmaf_rn(ikh(kgi1, P.ss_c[k], k == i1), pc[k], w1);
+        }
+        W.T[lane] = w0;
+        W.T[lane + 32] = w1;
+        __syncwarp();
+        // P = T (I - KG C)^T + KG R KG^T
+        float z0 = 0.0f, z1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) {
+            const float m = ikh(kgj, P.ss_c[k], k == j);
+            z0 = __fmaf_rn(W.T[i0 * MAXS + k], m, z0);
+            z1 = __fmaf_rn(W.T[i1 * MAXS + k], m, z1);
+        }
+        z0 = __fadd_rn(z0, __fmaf_rn(__fmaf_rn(kgi0, S.r, 0.0f), kgj, 0.0f));
+        z1 = __fadd_rn(z1, __fmaf_rn(__fmaf_rn(kgi1, S.r, 0.0f), kgj, 0.0f));
+        // P_{t+1} against the snapshot (own elements)
+        const bool same = __float_as_uint(z0) == __float_as_uint(S.snap0) &&
+                          __float_as_uint(z1) == __float_as_uint(S.snap1);
+        // every lane read P for the last time before the barrier above
+        W.P[lane] = z0;
+        W.P[lane + 32] = z1;
+        if (__all_sync(FULL, same)) {
+            const int p = S.t + 1 - S.t_snap;  // 1 .. KAL_PERIOD
+            S.period = p;
+            S.rslot = (slot + 1 - p + KAL_PERIOD) % KAL_PERIOD;
+        }
+        ++S.t;
+        __syncwarp();
     }
-    if (i0 == j) u0 = __fadd_rn(u0, S.q0);
-    if (i1 == j) u1 = __fadd_rn(u1, S.q1);
-    Ps[lane] = u0;
-    Ps[lane + 32] = u1;
-    __syncwarp();
-    // gain: lanes 0-7 form (P C^T)_l, lanes 8-15 (C P)_{l-8}; every lane forms C P C^T + R
-    float v = 0.0f;
-    if (lane < MAXS) {
 #pragma unroll
-        for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(Ps[lane * MAXS + k], P.ss_c[k], v);
-    } else if (lane < 2 * MAXS) {
-#pragma unroll
-        for (int k = 0; k < MAXS; ++k) v = __fmaf_rn(P.ss_c[k], Ps[k * MAXS + lane - MAXS], v);
-    }
-    float h = 0.0f;
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) h = __fmaf_rn(__shfl_sync(FULL, v, MAXS + k), P.ss_c[k], h);
-    h = __fdiv_rn(1.0f, __fadd_rn(h, S.r));
-    const float kgl = __fmul_rn(v, h);
-#pragma unroll
-    for (int i = 0; i < MAXS; ++i) {
-        S.kgo[i] = S.kg[i];
-        S.kg[i] = __shfl_sync(FULL, kgl, i);
-    }
-    const float kgi0 = __shfl_sync(FULL, kgl, i0), kgi1 = __shfl_sync(FULL, kgl, i1);
-    const float kgj = __shfl_sync(FULL, kgl, j);
-    // T = (I - KG C) P
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) pc[k] = Ps[k * MAXS + j];
-    float w0 = 0.0f, w1 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) {
-        w0 = __fmaf_rn(ikh(kgi0, P.ss_c[k], k == i0), pc[k], w0);
-        w1 = __fmaf_rn(ikh(kgi1, P.ss_c[k], k == i1), pc[k], w1);
-    }
-    Ts[lane] = w0;
-    Ts[lane + 32] = w1;
-    __syncwarp();
-    // P = T (I - KG C)^T + KG R KG^T
-    float z0 = 0.0f, z1 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < MAXS; ++k) {
-        const float m = ikh(kgj, P.ss_c[k], k == j);
-        z0 = __fmaf_rn(Ts[i0 * MAXS + k], m, z0);
-        z1 = __fmaf_rn(Ts[i1 * MAXS + k], m, z1);
-    }
-    z0 = __fadd_rn(z0, __fmaf_rn(__fmaf_rn(kgi0, S.r, 0.0f), kgj, 0.0f));
-    z1 = __fadd_rn(z1, __fmaf_rn(__fmaf_rn(kgi1, S.r, 0.0f), kgj, 0.0f));
-    const bool same1 = __float_as_uint(z0) == __float_as_uint(S.p0) && __float_as_uint(z1) == __float_as_uint(S.p1);
-    const bool same2 =
-        S.t > 0 && __float_as_uint(z0) == __float_as_uint(S.o0) && __float_as_uint(z1) == __float_as_uint(S.o1);
-    const bool fixed = __all_sync(FULL, same1), period2 = __all_sync(FULL, same2);
-    // every lane read P for the last time before the barrier above
-    Ps[lane] = z0;
-    Ps[lane + 32] = z1;
-    __syncwarp();
-    S.o0 = S.p0;
-    S.o1 = S.p1;
-    S.p0 = z0;
-    S.p1 = z1;
-    ++S.t;
-    S.mode = fixed ? 1 : period2 ? 2 : 0;
+    for (int i = 0; i < MAXS; ++i) KG[i] = W.kg[slot][i];
 }
 
 // Simulation forms: KMODE 0 the Luenberger observer; 1 the Kalman observer
@@ -336,7 +359,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
     __shared__ float stage[8][SIM_BLOCK];
     __shared__ float srcP[Chains::kSmem ? MAXD + 1 : 1][SIM_BLOCK];
     __shared__ float srcH[Chains::kSmem ? MAXS : 1][SIM_BLOCK];
-    __shared__ float kps[SHARED ? SIM_BLOCK / 32 : 1][2][SHARED ? MAXS * MAXS : 1];
+    __shared__ KalWarp kw[SHARED ? SIM_BLOCK / 32 : 1];
     const int tid = threadIdx.x;
     // each thread only touches its own column of the shared rows
     const int64_t pos = (int64_t)blockIdx.x * SIM_BLOCK + tid;
@@ -377,7 +400,6 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
     float KG[KAL ? MAXS : 1];
     float Rn = 0.0f;
     KalShared S;
-    float *Ps = nullptr, *Ts = nullptr;
     const int lane = tid & 31;
     if constexpr (KMODE == SIM_KALMAN_LANE) {
         Rn = row[2 * ns + 1];
@@ -401,24 +423,18 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
             if (writer) run.kal_order[run.kal_defer + atomicAdd(&run.kal_totals[2], 1)] = (int)c;
             return;  // warp-uniform
         }
-        const int j = lane & (MAXS - 1), i0 = lane >> 3, i1 = i0 + 4;
-#pragma unroll
-        for (int k = 0; k < MAXS; ++k) {
-            S.a0[k] = P.ss_a[i0 * MAXS + k];
-            S.a1[k] = P.ss_a[i1 * MAXS + k];
-            S.aj[k] = P.ss_a[j * MAXS + k];
-            S.kg[k] = S.kgo[k] = 0.0f;
-        }
+        const int i0 = lane >> 3, i1 = i0 + 4;
+        KalWarp& W = kw[tid >> 5];
+        for (int e = lane; e < MAXS * MAXS; e += 32) W.A[(e >> 3) * (MAXS + 1) + (e & 7)] = P.ss_a[e];
         S.q0 = i0 < ns ? row[2 * ns + 2 + i0] : 0.0f;
         S.q1 = i1 < ns ? row[2 * ns + 2 + i1] : 0.0f;
         S.r = Rn;
-        S.p0 = S.p1 = S.o0 = S.o1 = 0.0f;
-        S.mode = 0;
-        S.t = 0;
-        Ps = kps[tid >> 5][0];
-        Ts = kps[tid >> 5][1];
-        Ps[lane] = 0.0f;
-        Ps[lane + 32] = 0.0f;
+        S.t = S.t_snap = 0;
+        S.slot = S.rslot = 0;
+        S.period = 0;
+        S.snap0 = S.snap1 = 0.0f;
+        W.P[lane] = 0.0f;
+        W.P[lane + 32] = 0.0f;
         __syncwarp();
     }
 
@@ -485,9 +501,7 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
         if constexpr (KAL) {
             kalman_predict(P, xh_hi, xh_lo, u);
             if constexpr (SHARED) {
-                kalman_cov_shared(P, S, Ps, Ts, lane);
-#pragma unroll
-                for (int i = 0; i < MAXS; ++i) KG[i] = S.kg[i];
+                kalman_gain_shared(P, S, kw[tid >> 5], lane, KG);
             } else {
                 kalman_cov_lane(P, Pm, Qd, Rn, KG);
             }
