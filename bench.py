@@ -12,11 +12,15 @@ margin sweep, producing the INFO cost rows.
 * roofline -- the dominant kernel, timed live with CUDA events on its stream;
 * cpu_baseline -- the CPU oracle (a C port of the reference method, OpenMP) on a
            bounded sample of the same workload on this host's cores;
-* fp64_form -- the same pipeline with every stage in FP64 (the plain FP64 form).
+* fp64_form -- the same pipeline with every stage in FP64 (the plain FP64 form);
+* monte_carlo, kalman, serving -- the per-candidate-plant, Kalman-observer and
+           request-serving workloads.
 
 `--impl reference` times the reference method on the host cores instead: the
 reference's Eigen host path does not build here (Eigen is not vendored), so the
-C port of its method in oracle/ stands in for it.
+C port of its method in oracle/ stands in for it.  Its line also carries
+`reference_gpu_build`: the reference's own kernels (compiled from its sources
+for sm_103a) on the GPU with its Eigen stages restated on the host cores.
 """
 from __future__ import annotations
 
@@ -85,11 +89,12 @@ def modal_stable(eigen):
     return np.hypot(eigen[..., 0].astype(np.float64), eigen[..., 1].astype(np.float64)).max(1) <= 1.0
 
 
-def eig_flops(n):
+def eig_ops(n):
     """Eigenvalues of a real n x n matrix by Householder-Hessenberg reduction and
     Francis double-shift QR: 10 n^3 flops (Golub and Van Loan, Matrix
-    Computations, 4th ed., table 7.5.2)."""
-    return 10 * n ** 3
+    Computations, 4th ed., table 7.5.2), i.e. 5 n^3 fused multiply-adds -- counted
+    here as FP64 pipe operations, the unit of the measured DFMA issue rate."""
+    return 5 * n ** 3
 
 
 def sim_ops_per_step(ns, nd, nw, n_instr):
@@ -160,6 +165,46 @@ def cpu_baseline(problem, seconds: float, threads: int):
             "sample": f"{n_s} of the {n_total} candidates, full horizon, oracle C port with OpenMP ({dt:.1f} s)"}
 
 
+def reference_gpu_build(problem, threads: int, sample: int = 4096):
+    """The reference as it runs, in candidates/s: its own kernels (discrete_solve<Luenberger>,
+    eigensetup, modalsetup from src/main.cu, compiled for sm_103a where the reference lies and
+    launched with its launch shape and constant tables by oracle/ref_kernels.py) on the GPU over
+    the whole batch, and its Eigen host stages (eigensolve, modalsolve, allmargin; Eigen itself
+    is not vendored, so their C restatement in oracle/) on all host cores -- eigensolve and
+    modalsolve over the whole batch, allmargin over `sample` candidates, scaled.  The trajectory
+    stays on the device, as in the reference without dump_diagnostics."""
+    from oracle import oracle as O, ref_kernels as RK
+    if not RK.available():
+        return {"unavailable": "oracle/_ref/ref_kernels.cubin not built (make -C oracle ref needs the reference tree)"}
+    orc = O.Oracle(problem.config_text, problem.plant, threads=threads)
+    cfg = orc.ref_config()
+    g, info = problem.cuda_mx, problem.info_mx
+    n = g.shape[0]
+    zero = np.zeros((n, 2 * cfg.total_dim), np.float32)
+    RK.run(cfg, problem.plant, g[:256], zero[:256], info[:256], want_y=False)  # module load
+    _, lina, _, _, _ = RK.run(cfg, problem.plant, g, zero, info, want_y=False)
+    t0 = time.perf_counter()
+    eig = orc.eigensolve(lina)
+    t_eig = time.perf_counter() - t0
+    tm = {}
+    _, _, ata, atb, info1 = RK.run(cfg, problem.plant, g, eig, info, want_y=False, times=tm)
+    t0 = time.perf_counter()
+    info2 = orc.modalsolve(ata, atb, eig, info1)
+    t_ms = time.perf_counter() - t0
+    m = min(n, sample)
+    t0 = time.perf_counter()
+    orc.allmargin(lina[:m], g[:m], info2[:m])
+    t_am = (time.perf_counter() - t0) * n / m
+    gpu_s = (tm["discrete_solve"] + tm["eigensetup"] + tm["modalsetup"]) * 1e-3
+    copy_s = (tm["h2d"] + tm["d2h"]) * 1e-3
+    total = gpu_s + copy_s + t_eig + t_ms + t_am
+    return {"value": n / total, "unit": UNIT, "candidates": n, "cores": threads,
+            "seconds": {"gpu_kernels": gpu_s, "copies": copy_s, "eigensolve_cpu": t_eig, "modalsolve_cpu": t_ms,
+                        "allmargin_cpu": t_am},
+            "gpu_kernels_ms": {k: tm[k] for k in ("discrete_solve", "eigensetup", "modalsetup")},
+            "sample": f"GPU stages and eigensolve/modalsolve on all {n} candidates, allmargin on {m} (scaled)"}
+
+
 def run_reference(a, rank, world):
     from controllerengine_gb300 import synth
     if rank != 0:
@@ -193,6 +238,8 @@ def run_reference(a, rank, world):
                                        "path is not buildable here (Eigen not vendored), its method is timed "
                                        "through the C port in oracle/"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if a.ref_gpu_build:
+        line["reference_gpu_build"] = reference_gpu_build(problem, threads)
     print(json.dumps(line), flush=True)
 
 
@@ -378,6 +425,8 @@ def main():
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="Poisson serving run (0: skip)")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
+    ap.add_argument("--ref-gpu-build", type=int, default=1,
+                    help="reference arm: also time the reference's own kernels + host stages (0: skip)")
     ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -523,10 +572,11 @@ def main():
                     f"normal-equation FMAs + 5 basis ops per mode-step, {cfg.fit_steps} window steps, "
                     f"summed over the stable candidates ({fit_work / 1e9:.2f} G ops)")}
     nt, n2 = cfg.total_dim, 2 * cfg.statespace_dim
-    work64 = {"lina_eig": ("k_lina_eig<2>", eig_flops(nt) * n,
-                           f"10 n^3 flops of a {nt}x{nt} real eigensolve x {n} candidates"),
-              "nominal": ("k_nominal<2>", eig_flops(n2) * n_listed,
-                          f"10 n^3 flops of a {n2}x{n2} real eigensolve x {n_listed} listed candidates")}
+    work64 = {"lina_eig": ("k_lina_eig<2>", eig_ops(nt) * n,
+                           f"5 n^3 FP64 FMAs (10 n^3 flops) of a {nt}x{nt} real eigensolve x {n} candidates"),
+              "nominal": ("k_nominal<2>", eig_ops(n2) * n_listed,
+                          f"5 n^3 FP64 FMAs (10 n^3 flops) of a {n2}x{n2} real eigensolve x {n_listed} "
+                          "listed candidates")}
     src64 = "measured FP64 DFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"
     rooflines = {}
     for group, bound, pk, sname in ((work, "fp32", peak, src), (work64, "fp64", fp64_rate / 1e12, src64)):

@@ -1167,6 +1167,8 @@ static void allmargin_one(const oc_cfg* c, const oc_der* d, const oc_mp* mp, con
 
 /* ===================== exported stage entry points ======================== */
 
+void oracle_derived(const oc_cfg* c, oc_der* d) { derive(c, d); }
+
 int oracle_info_width(const oc_cfg* c) {
     oc_der d;
     derive(c, &d);

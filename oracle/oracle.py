@@ -41,6 +41,14 @@ class oc_cfg(C.Structure):
                 ("observer", C.c_int32)]
 
 
+class oc_der(C.Structure):
+    _fields_ = [("ts", C.c_float), ("freq_max", C.c_float), ("fit_t0", C.c_float), ("fit_t1", C.c_float),
+                ("crossover", C.c_float), ("nt", C.c_int32), ("cuda_w", C.c_int32), ("info_scoring", C.c_int32),
+                ("info_freqresp", C.c_int32), ("info_allmargin", C.c_int32), ("info_modal", C.c_int32),
+                ("info_w", C.c_int32), ("fit_start_id", C.c_int32), ("steady_start_id", C.c_int32),
+                ("fit_len", C.c_float)]
+
+
 _FP = C.POINTER(C.c_float)
 _IP = C.POINTER(C.c_int32)
 _DP = C.POINTER(C.c_double)
@@ -66,6 +74,8 @@ def lib():
         L = C.CDLL(str(LIB))
         i64 = C.c_int64
         L.oracle_sim.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, _FP, C.c_int]
+        L.oracle_derived.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_der)]
+        L.oracle_derived.restype = None
         L.oracle_sim_kalman.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, C.c_int, C.c_int, _FP,
                                         _IP, C.c_int]
         L.oracle_lina.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, _FP, C.c_int]
@@ -162,6 +172,23 @@ class Oracle:
         self.nt = c.ns + c.nd
         self.info_w = lib().oracle_info_width(C.byref(c))
         self.cuda_w = 3 * c.ns + 2 if c.observer else 2 * c.ns + 1
+
+    def ref_config(self):
+        """The config fields the reference's kernels read (EngineParams and the table sizes), from
+        this oracle's parse and derivation -- for oracle/ref_kernels.py without the engine."""
+        from types import SimpleNamespace
+        c, d = self.cfg, oc_der()
+        lib().oracle_derived(C.byref(c), C.byref(d))
+        nt = d.nt
+        nl = list(c.nl_instr)
+        return SimpleNamespace(
+            statespace_dim=c.ns, discrete_dim=c.nd, nonlin_dim=c.nw, total_dim=nt, time=c.time,
+            cuda_mx_width=d.cuda_w, info_mx_width=d.info_w, info_scoring=d.info_scoring,
+            info_freqresp=d.info_freqresp, eigen_mx_width=2 * nt, lina_mx_width=nt * nt, ata_mx_width=4 * nt * nt,
+            atb_mx_width=2 * nt, fit_start_id=d.fit_start_id, steady_start_id=d.steady_start_id, ts=d.ts,
+            fit_start=c.fit_start, fit_end=c.fit_end, fit_t0=d.fit_t0, fit_t1=d.fit_t1, unstable_err=c.unstable_err,
+            n_params=c.n_params, dc_instructions=c.dc_instr, u_instructions=c.u_instr, nl_instructions=nl,
+            nl_instructions_total=sum(nl), ref_step_time=c.ref_step_time, ref_amplitude=c.ref_amplitude)
 
     def _g(self, cuda_mx):
         g = np.ascontiguousarray(cuda_mx, F32).reshape(-1, self.cuda_w)

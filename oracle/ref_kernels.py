@@ -92,9 +92,11 @@ def _tables(cfg, plant, n: int, cuda_w: int):
 _fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray):
+def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray, want_y: bool = True,
+        times: dict | None = None):
     """cfg: an engine EngineConfig (its parser is pinned to the reference's).  Returns
-    (yplant, lina, ata, atb, info) from the reference kernels."""
+    (yplant, lina, ata, atb, info) from the reference kernels (yplant None unless want_y).
+    `times`, if given, receives the milliseconds of the three kernels and of the copies."""
     nt = cfg.total_dim
     n = cuda_mx.shape[0]
     engine, tabs, dc, u, nl, ref = _tables(cfg, plant, n, cfg.cuda_mx_width)
@@ -103,16 +105,19 @@ def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray)
     g = np.ascontiguousarray(cuda_mx, F32)
     e = np.ascontiguousarray(eigen, F32)
     inf = np.ascontiguousarray(info_in, F32)
-    y = np.empty((n, cfg.time), F32)
+    y = np.empty((n, cfg.time), F32) if want_y else None
     lina = np.empty((n, nt * nt), F32)
     ata = np.empty((n, 4 * nt * nt), F32)
     atb = np.empty((n, 2 * nt), F32)
     out = np.empty_like(inf)
+    tm = np.zeros(5, F32)
     rc = L.ref_run(str(CUBIN).encode(), engine, len(engine), tab_ptrs, dc, u, nl, n,
-                   cfg.time, cfg.cuda_mx_width, nt, cfg.info_mx_width, _fp(g), _fp(ref), _fp(e), _fp(inf), _fp(y),
-                   _fp(lina), _fp(ata), _fp(atb), _fp(out))
+                   cfg.time, cfg.cuda_mx_width, nt, cfg.info_mx_width, _fp(g), _fp(ref), _fp(e), _fp(inf),
+                   _fp(y) if want_y else None, _fp(lina), _fp(ata), _fp(atb), _fp(out), _fp(tm))
     if rc:
         raise RuntimeError(L.ref_runner_error().decode())
+    if times is not None:
+        times.update(zip(("discrete_solve", "eigensetup", "modalsetup", "h2d", "d2h"), map(float, tm)))
     return y, lina, ata, atb, out
 
 

@@ -9,6 +9,7 @@
 //   g++ -O2 -shared -fPIC -I/usr/local/cuda/include ref_kernel_runner.cpp -lcuda
 #include <cuda.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -85,10 +86,13 @@ const char* ref_runner_error() { return g_err.c_str(); }
 // STATESPACE_A, _A_I, _B, _C, _D, DISCRETE_A, _A_I, _BU, _BW, _C, BASE_PARAMS
 // (sizes 64,64,8,8,1,64,64,8,32,8,34 floats); ops: DC_OPS (4), U_OPS (4), NL_OPS (32)
 // Instruction records of 24 bytes.  eigen: the float eigenvalues modalsetup reads.
+// times (optional, 5 floats): milliseconds of discrete_solve, eigensetup and modalsetup (CUDA
+// events), of the input copies and of the output copies (host clock).  yplant may be null (the
+// trajectory stays on the device, as in the reference without dump_diagnostics).
 int ref_run(const char* cubin, const void* engine, int engine_bytes, const float* const* tables, const void* dc_ops,
             const void* u_ops, const void* nl_ops, int n, int time, int cuda_w, int nt, int info_w,
             const float* cuda_mx, const float* ref, const float* eigen, const float* info_in, float* yplant,
-            float* lina, float* ata, float* atb, float* info_out) {
+            float* lina, float* ata, float* atb, float* info_out, float* times) {
     if (load(cubin)) return 1;
     CK(cuCtxSetCurrent(g_ctx));
     if (set_global("ENGINE", engine, engine_bytes)) return 1;
@@ -113,33 +117,51 @@ int ref_run(const char* cubin, const void* engine, int engine_bytes, const float
     CK(cuMemAlloc(&d_a, asz * 4));
     CK(cuMemAlloc(&d_b, bsz * 4));
     CK(cuMemAlloc(&d_i, isz * 4));
-    CK(cuMemcpyHtoD(d_g, cuda_mx, gsz * 4));
-    CK(cuMemcpyHtoD(d_ref, ref, (size_t)time * 4));
-    CK(cuMemcpyHtoD(d_e, eigen, esz * 4));
-    CK(cuMemcpyHtoD(d_i, info_in, isz * 4));
     CK(cuMemsetD8(d_y, 0, ysz * 4));
     CK(cuMemsetD8(d_l, 0, lsz * 4));
     CK(cuMemsetD8(d_a, 0, asz * 4));
     CK(cuMemsetD8(d_b, 0, bsz * 4));
+    CK(cuCtxSynchronize());
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    const auto h0 = now();
+    CK(cuMemcpyHtoD(d_g, cuda_mx, gsz * 4));
+    CK(cuMemcpyHtoD(d_ref, ref, (size_t)time * 4));
+    CK(cuMemcpyHtoD(d_e, eigen, esz * 4));
+    CK(cuMemcpyHtoD(d_i, info_in, isz * 4));
+    const auto h1 = now();
+    CUevent ev[4];
+    for (auto& e : ev) CK(cuEventCreate(&e, CU_EVENT_DEFAULT));
     const unsigned tpb = 256, blocks = (n + tpb - 1) / tpb;
+    CK(cuEventRecord(ev[0], nullptr));
     {
         void* args[] = {&d_g, &d_ref, &d_y};
         CK(cuLaunchKernel(g_sim, blocks, 1, 1, tpb, 1, 1, 0, nullptr, args, nullptr));
     }
+    CK(cuEventRecord(ev[1], nullptr));
     {
         void* args[] = {&d_g, &d_l};
         CK(cuLaunchKernel(g_setup, blocks, 1, 1, tpb, 1, 1, 0, nullptr, args, nullptr));
     }
+    CK(cuEventRecord(ev[2], nullptr));
     {
         void* args[] = {&d_y, &d_e, &d_a, &d_b, &d_i};
         CK(cuLaunchKernel(g_modal, blocks, 1, 1, tpb, 1, 1, 0, nullptr, args, nullptr));
     }
+    CK(cuEventRecord(ev[3], nullptr));
     CK(cuCtxSynchronize());
-    CK(cuMemcpyDtoH(yplant, d_y, ysz * 4));
+    const auto d0 = now();
+    if (yplant) CK(cuMemcpyDtoH(yplant, d_y, ysz * 4));
     CK(cuMemcpyDtoH(lina, d_l, lsz * 4));
     CK(cuMemcpyDtoH(ata, d_a, asz * 4));
     CK(cuMemcpyDtoH(atb, d_b, bsz * 4));
     CK(cuMemcpyDtoH(info_out, d_i, isz * 4));
+    const auto d1 = now();
+    if (times) {
+        for (int k = 0; k < 3; ++k) CK(cuEventElapsedTime(&times[k], ev[k], ev[k + 1]));
+        times[3] = std::chrono::duration<float, std::milli>(h1 - h0).count();
+        times[4] = std::chrono::duration<float, std::milli>(d1 - d0).count();
+    }
+    for (auto& e : ev) cuEventDestroy(e);
     for (CUdeviceptr p : {d_g, d_ref, d_y, d_l, d_e, d_a, d_b, d_i}) cuMemFree(p);
     return 0;
 }

@@ -82,3 +82,16 @@ def test_generator_invariants():
     assert np.all((r > 0.899) & (r < 0.9951))
     np.testing.assert_array_equal(p.plant.discrete_a_i, p.plant.discrete_a - np.eye(8, dtype=np.float32).reshape(-1))
     assert p.cuda_mx.shape == (64, 17) and np.all(np.isfinite(p.cuda_mx))
+
+
+@pytest.mark.parametrize("observer", ["luenberger", "kalman"])
+def test_oracle_ref_config_equals_engine_parse(oracle_mod, observer):
+    """The fields the reference's kernels read, derived by the oracle alone (used to launch
+    them without the engine) equal the engine's parse, for both observers."""
+    import controllerengine_gb300 as ce
+    from controllerengine_gb300 import synth
+    for p in (synth.eight_state(n=8, time=1000, freq=50, observer=observer), synth.random_shape(3, n=8)):
+        rc = oracle_mod.Oracle(p.config_text, p.plant).ref_config()
+        cfg = ce.EngineConfig.parse(p.config_text)
+        for k, v in vars(rc).items():
+            assert getattr(cfg, k) == v, k
