@@ -256,7 +256,7 @@ def serving_models(k: int = 16, seed: int = 5):
     return out
 
 
-def serving_bench(problems, seconds: float, lanes: int = 2, max_batch: int = 16384, seed: int = 7):
+def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7):
     """Request serving (ce_server_*): requests of U[256, 16384] candidates on a model drawn
     uniformly from `problems`.  Saturation: 48 requests submitted at once, candidates/s until
     all are done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of
@@ -423,7 +423,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
-    ap.add_argument("--serve-seconds", type=float, default=6.0, help="Poisson serving run (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="Poisson serving run (0: skip)")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
     ap.add_argument("--ref-gpu-build", type=int, default=1,
                     help="reference arm: also time the reference's own kernels + host stages (0: skip)")

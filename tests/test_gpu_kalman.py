@@ -137,3 +137,56 @@ def test_kalman_hash_collision_is_deferred(oracle_mod):
             _, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("yplant",))
             y_o = oracle_mod.Oracle(p.config_text, p.plant).sim(p.cuda_mx)
             assert _eq(d["yplant"], y_o), f"{kernel}: {_mismatch(d['yplant'], y_o)} mismatches"
+
+
+def test_kalman_file_boundary(tmp_path):
+    """RunControllerEngine() with `observer = kalman` in ControllerEngine.config."""
+    p = synth.eight_state(n=1536, time=1200, freq=60, pool=5, observer="kalman")
+    p.write(tmp_path)
+    assert ce.run_controller_engine(tmp_path) == 0
+    cfg = ce.EngineConfig.parse(p.config_text)
+    out = np.fromfile(tmp_path / "INFO_MX_OUT.bin", np.float32).reshape(-1, cfg.info_mx_width)
+    with ce.Session(cfg, p.plant) as s:
+        ref = s.evaluate(p.cuda_mx, p.info_mx)
+    assert np.array_equal(_bits(out), _bits(ref))
+
+
+def test_kalman_server_and_chunks():
+    """Served requests of assorted sizes, and one chunked batch against its pieces: every row
+    equals the same candidates evaluated alone (the grouping is per evaluation)."""
+    p = synth.eight_state(n=40000, time=800, freq=40, pool=6, observer="kalman")
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        whole = s.evaluate(p.cuda_mx, p.info_mx)
+        parts = np.vstack([s.evaluate(p.cuda_mx[a:a + 10000], p.info_mx[a:a + 10000]) for a in range(0, 40000, 10000)])
+    assert np.array_equal(_bits(whole), _bits(parts))
+    cuts = [0, 37, 3037, 3100, 9000]
+    with ce.Server(cfg, p.plant, max_batch=4096, lanes=2) as srv:
+        reqs = [srv.submit(p.cuda_mx[a:b], p.info_mx[a:b]) for a, b in zip(cuts, cuts[1:])]
+        got = np.vstack([r.wait() for r in reqs])
+    assert np.array_equal(_bits(got), _bits(whole[:9000]))
+
+
+def test_kalman_graph_capture():
+    import torch
+    p = synth.eight_state(n=2048, time=1000, freq=40, pool=4, observer="kalman")
+    cfg = ce.EngineConfig.parse(p.config_text)
+    n = p.cuda_mx.shape[0]
+    with ce.Session(cfg, p.plant) as s:
+        ref = s.evaluate(p.cuda_mx, p.info_mx)
+        dg = torch.from_numpy(p.cuda_mx).cuda()
+        di = torch.from_numpy(p.info_mx).cuda()
+        do = torch.empty_like(di)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            s.evaluate_device(n, dg.data_ptr(), di.data_ptr(), do.data_ptr(), stream=side.cuda_stream)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            s.evaluate_device(n, dg.data_ptr(), di.data_ptr(), do.data_ptr(),
+                              stream=torch.cuda.current_stream().cuda_stream)
+        do.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+    assert np.array_equal(_bits(do.cpu().numpy()), _bits(ref))
