@@ -29,6 +29,7 @@ EXPORTED_SYMBOLS = (
     "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
     "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
     "ce_server_submit_model", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
+    "ce_ragged_create", "ce_ragged_evaluate", "ce_ragged_destroy", "ce_ragged_kernel_launches",
     "RunControllerEngine",
 )
 PENDING = 2
@@ -148,6 +149,12 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
                                         C.c_void_p, C.POINTER(ce_tuning)]
     lib.ce_server_destroy.argtypes = [C.c_void_p]
     lib.ce_server_destroy.restype = None
+    lib.ce_ragged_create.argtypes = [C.c_int32, C.POINTER(ce_config), C.POINTER(ce_plant), C.POINTER(C.c_void_p)]
+    lib.ce_ragged_evaluate.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.ce_ragged_destroy.argtypes = [C.c_void_p]
+    lib.ce_ragged_destroy.restype = None
+    lib.ce_ragged_kernel_launches.argtypes = [C.c_void_p]
+    lib.ce_ragged_kernel_launches.restype = C.c_int64
     lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_int64)]
     lib.ce_server_wait.argtypes = [C.c_void_p, C.c_int64, C.c_int32]

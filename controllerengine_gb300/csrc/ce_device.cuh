@@ -17,6 +17,19 @@
 
 namespace ce {
 
+// The sizes and plant of candidate c: the launch's in a uniform evaluation, its
+// instance's in a ragged one.
+template <bool RG>
+__device__ __forceinline__ const Run& run_of(const Run& run, int64_t c) {
+    if constexpr (RG) return run.rg.runs[run.rg.inst[c]];
+    else return run;
+}
+template <bool RG>
+__device__ __forceinline__ const Plant& plant_of(const Run& run, const Plant& P, int64_t c) {
+    if constexpr (RG) return run.rg.plants[run.rg.inst[c]];
+    else return P;
+}
+
 // ---- scalar ops in a type-generic, contraction-proof form -------------------
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }

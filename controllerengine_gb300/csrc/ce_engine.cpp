@@ -133,6 +133,21 @@ struct ce_session {
     }
 };
 
+// A ragged batch (ce_ragged_*): instances of different configurations and
+// plants evaluated together, one launch per stage over all their candidates.
+struct ce_ragged {
+    std::vector<ce_config> cfg;             // per instance
+    ce_config layout{};                     // the maxima: row widths, dimensions, fit window, sweep size
+    ce_session* s = nullptr;                // streams, scratch and the pipeline, sized by `layout`
+    ce::Plant* d_plants = nullptr;          // per instance
+    ce::Run* d_runs = nullptr;              // per instance, with the strides and slots of `layout`
+    int* d_inst = nullptr;                  // instance of each candidate of the current evaluation
+    int64_t inst_cap = 0;
+    float *h_gains = nullptr, *h_info = nullptr;  // pinned staging rows at the layout widths
+    int64_t host_cap = 0;
+    std::vector<int> h_inst;
+};
+
 namespace ce {
 
 namespace {
@@ -214,8 +229,10 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
     }
 }
 
-Run make_run(const ce_session* s, int plant, int64_t n) {
-    const ce_config& c = s->cfg;
+// The sizes and scalars of configuration c; the row strides and per-candidate
+// slots are those of configuration `layout` (c itself for a uniform
+// evaluation, the maxima of a ragged batch).
+Run run_from_config(const ce_config& c, const ce_config& layout, int64_t n, float alpha, double alpha64) {
     Run r{};
     r.n = n;
     r.ns = c.statespace_dim;
@@ -225,11 +242,11 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
     r.time = c.time;
     r.fit_start_id = c.fit_start_id;
     r.fit_steps = c.fit_steps;
-    r.fit_pitch = fit_pitch(c.fit_steps);
+    r.fit_pitch = fit_pitch(layout.fit_steps);
     r.steady_start_id = c.steady_start_id;
     r.ref_step_id = c.ref_step_id;
-    r.cuda_w = c.cuda_mx_width;
-    r.info_w = c.info_mx_width;
+    r.cuda_w = layout.cuda_mx_width;
+    r.info_w = layout.info_mx_width;
     r.info_scoring = c.info_scoring;
     r.info_freqresp = c.info_freqresp;
     r.info_allmargin = c.info_allmargin;
@@ -248,11 +265,22 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
     r.target_gm = c.target_gm;
     r.target_pm = c.target_pm;
     r.target_b = c.target_b;
-    r.alpha = s->alpha32[s->grid_of(plant)];
-    r.alpha64 = s->alpha64.empty() ? 0.0 : s->alpha64[s->grid_of(plant)];
+    r.alpha = alpha;
+    r.alpha64 = alpha64;
     r.store_traj = 0;
     r.kalman = c.observer == CE_OBSERVER_KALMAN ? 1 : 0;
+    const int lt = layout.total_dim;
+    r.lina_slot = lt * lt;
+    r.eig_slot = 2 * lt;
+    r.ata_slot = 4 * lt * lt;
+    r.atb_slot = 2 * lt;
+    r.grid_off = 0;
     return r;
+}
+
+Run make_run(const ce_session* s, int plant, int64_t n) {
+    return run_from_config(s->cfg, s->cfg, n, s->alpha32[s->grid_of(plant)],
+                           s->alpha64.empty() ? 0.0 : s->alpha64[s->grid_of(plant)]);
 }
 
 void build_grids(ce_session* s, int precision);
@@ -314,7 +342,7 @@ int n_chunks(const ce_session* s, int64_t n) {
 // With per_candidate, candidate c uses plant `plant + c` (its values from the
 // plant table; the instruction structure and the observer model are shared).
 void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
-                  bool traj, bool per_candidate = false) {
+                  bool traj, bool per_candidate = false, const Ragged* ragged = nullptr) {
     const int64_t np_used = per_candidate ? n : 1;
     for (int64_t q = 0; q < np_used; ++q)
         if (!s->plant_err[plant + q].empty()) throw std::runtime_error(s->plant_err[plant + q]);
@@ -327,6 +355,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     ensure_buffers(s, n, traj);
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
+    if (ragged) r.rg = *ragged;
     r.store_traj = traj ? 1 : 0;
     r.eig_lanes = s->tuning.eig_lanes;
     r.eig_blocks = s->tuning.eig_blocks_per_sm;
@@ -372,6 +401,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         rc = r;
         rc.n = std::min<int64_t>(per, n - off);
         rc.mc.first = r.mc.first + off;
+        if (r.rg.inst) rc.rg.inst = r.rg.inst + off;
     };
     auto at = [](const void* p, int64_t off, size_t bytes) {
         return (void*)((const char*)p + (size_t)off * bytes);
@@ -537,29 +567,40 @@ void build_plant(const ce_config& c, const ce_plant& in, int p, Plant& P) {
 // alpha run on the device for all margin plants at once (k_plant_grid).  A
 // margin plant without a finite nonzero gain at the crossover makes its
 // evaluations fail with the reference's message.
+// The z grid of a configuration in float (ref: src/main.cu:424-428, host float
+// libm): per frequency z = (cos, sin) of theta_w = exp(log fmin + w*inc)*ts and
+// arg z; row F is the crossover e^{j w_c ts} (ref: src/allmargin.cu:36-38).
+std::vector<float> zgrid32(const ce_config& c) {
+    const int F = c.freq;
+    std::vector<float> z32((size_t)(F + 1) * 4, 0.0f);
+    const float inc = (logf(c.freq_max) - logf(c.freq_min)) / (float)(F - 1);
+    for (int w = 0; w < F; ++w) {
+        const float th = expf(logf(c.freq_min) + inc * (float)w) * c.ts;
+        z32[4 * w] = cosf(th);
+        z32[4 * w + 1] = sinf(th);
+        z32[4 * w + 2] = std::atan2(z32[4 * w + 1], z32[4 * w]);
+    }
+    const float th = c.crossover * c.ts;
+    z32[4 * F] = 1.0f * cosf(th);
+    z32[4 * F + 1] = 1.0f * sinf(th);
+    return z32;
+}
+
 void build_grids(ce_session* s, int precision) {
     const ce_config& c = s->cfg;
     const int F = c.freq, n = c.serial ? c.discrete_dim : c.statespace_dim, np = s->grid_np;
     const bool f64 = precision == CE_PRECISION_FP64;
     const size_t rsz = f64 ? sizeof(double) : sizeof(float);
     std::vector<double> z64((size_t)(F + 1) * 4, 0.0);
-    std::vector<float> z32((size_t)(F + 1) * 4, 0.0f);
-    const float inc = (logf(c.freq_max) - logf(c.freq_min)) / (float)(F - 1);
+    const std::vector<float> z32 = zgrid32(c);
     const double inc64 = (std::log((double)c.freq_max) - std::log((double)c.freq_min)) / (double)(F - 1);
     for (int w = 0; w < F; ++w) {
-        const float th = expf(logf(c.freq_min) + inc * (float)w) * c.ts;
-        z32[4 * w] = cosf(th);
-        z32[4 * w + 1] = sinf(th);
-        z32[4 * w + 2] = std::atan2(z32[4 * w + 1], z32[4 * w]);
         const double th64 = std::exp(std::log((double)c.freq_min) + inc64 * (double)w) * (double)c.ts;
         z64[4 * w] = std::cos(th64);
         z64[4 * w + 1] = std::sin(th64);
         z64[4 * w + 2] = std::atan2(z64[4 * w + 1], z64[4 * w]);
     }
     {
-        const float th = c.crossover * c.ts;
-        z32[4 * F] = 1.0f * cosf(th);
-        z32[4 * F + 1] = 1.0f * sinf(th);
         const double th64 = (double)c.crossover * (double)c.ts;
         z64[4 * F] = std::cos(th64);
         z64[4 * F + 1] = std::sin(th64);
@@ -628,27 +669,22 @@ void select_sim_kernel(ce_session* s, int kind) {
     s->sim_kind = kind;
 }
 
-void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants, ce_session** out) {
-    if (!cfg_in || !plant || !out) fail("ce_session_create: null argument");
-    if (n_plants < 1) fail("ce_session_create: n_plants must be >= 1, got {}", n_plants);
-    auto s = std::make_unique<ce_session>();
-    s->cfg = *cfg_in;
-    const ce_config& c = s->cfg;
+void check_config(const ce_config& c, const char* who) {
     if (c.statespace_dim < 1 || c.statespace_dim > MAXS || c.discrete_dim < 1 || c.discrete_dim > MAXD ||
         c.nonlin_dim < 0 || c.nonlin_dim > MAXW || c.total_dim != c.statespace_dim + c.discrete_dim)
-        fail("ce_session_create: config dimensions are out of range or not derived");
+        fail("{}: config dimensions are out of range or not derived", who);
     if (c.dc_dim != c.discrete_dim || c.u_dim != c.statespace_dim || c.nl_dim != c.discrete_dim + 1)
-        fail("ce_session_create: instruction table widths are not derived from the dimensions");
+        fail("{}: instruction table widths are not derived from the dimensions", who);
     if (c.observer != CE_OBSERVER_LUENBERGER && c.observer != CE_OBSERVER_KALMAN)
-        fail("ce_session_create: unknown observer {}", c.observer);
+        fail("{}: unknown observer {}", who, c.observer);
     if (c.cuda_mx_width != (c.observer == CE_OBSERVER_KALMAN ? 3 : 2) * c.statespace_dim +
                                (c.observer == CE_OBSERVER_KALMAN ? 2 : 1))
-        fail("ce_session_create: cuda_mx_width is not derived from the dimensions and the observer");
-    s->n_plants = n_plants;
-    s->plants.resize(n_plants);
-    s->plant_err.assign(n_plants, std::string());
-    s->grid_np = c.serial ? n_plants : 1;
-    for (int p = 0; p < n_plants; ++p) build_plant(c, *plant, p, s->plants[p]);
+        fail("{}: cuda_mx_width is not derived from the dimensions and the observer", who);
+}
+
+// The session's streams and events: `stream` for host-buffer evaluations, `fast`
+// (lowest priority) for the FP32 stages, `side` (highest) for the FP64 eigensolves.
+void init_streams(ce_session* s) {
     CE_CUDA(cudaGetDevice(&s->device));
     CE_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     int prio_least = 0, prio_greatest = 0;
@@ -661,6 +697,21 @@ void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig[k], cudaEventDisableTiming));
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_nom[k], cudaEventDisableTiming));
     }
+}
+
+void create_session(const ce_config* cfg_in, const ce_plant* plant, int n_plants, ce_session** out) {
+    if (!cfg_in || !plant || !out) fail("ce_session_create: null argument");
+    if (n_plants < 1) fail("ce_session_create: n_plants must be >= 1, got {}", n_plants);
+    auto s = std::make_unique<ce_session>();
+    s->cfg = *cfg_in;
+    const ce_config& c = s->cfg;
+    check_config(c, "ce_session_create");
+    s->n_plants = n_plants;
+    s->plants.resize(n_plants);
+    s->plant_err.assign(n_plants, std::string());
+    s->grid_np = c.serial ? n_plants : 1;
+    for (int p = 0; p < n_plants; ++p) build_plant(c, *plant, p, s->plants[p]);
+    init_streams(s.get());
     build_grids(s.get(), CE_PRECISION_MIXED);
     // Default: the specialised kernel.  CE_SIM_KERNEL=table in the environment
     // selects the table-driven one; if compiling fails the session keeps the
@@ -954,6 +1005,190 @@ void run_files() {
     }
 }
 
+void destroy_ragged(ce_ragged* r) {
+    if (!r) return;
+    if (r->d_plants) cudaFree(r->d_plants);
+    if (r->d_runs) cudaFree(r->d_runs);
+    if (r->d_inst) cudaFree(r->d_inst);
+    if (r->h_gains) cudaFreeHost(r->h_gains);
+    if (r->h_info) cudaFreeHost(r->h_info);
+    destroy_session(r->s);
+    delete r;
+}
+
+// Instances of any shapes, horizons and sweeps: per-instance plants, margin
+// plants, sweep grids and plant scalings (one grid kernel over all instances),
+// and per-instance Runs whose strides and slots are the batch's maxima.
+void create_ragged(int n_inst, const ce_config* cfgs, const ce_plant* plants, ce_ragged** out) {
+    if (!cfgs || !plants || !out) fail("ce_ragged_create: null argument");
+    if (n_inst < 1) fail("ce_ragged_create: n_inst must be >= 1, got {}", n_inst);
+    std::unique_ptr<ce_ragged, void (*)(ce_ragged*)> r(new ce_ragged, destroy_ragged);
+    r->cfg.assign(cfgs, cfgs + n_inst);
+    ce_config L = cfgs[0];
+    for (int i = 0; i < n_inst; ++i) {
+        const ce_config& c = cfgs[i];
+        const std::string who = std::format("ce_ragged_create: instance {}", i);
+        check_config(c, who.c_str());
+        if (c.observer != CE_OBSERVER_LUENBERGER) fail("{}: a ragged batch runs the Luenberger observer", who);
+        L.statespace_dim = std::max(L.statespace_dim, c.statespace_dim);
+        L.discrete_dim = std::max(L.discrete_dim, c.discrete_dim);
+        L.nonlin_dim = std::max(L.nonlin_dim, c.nonlin_dim);
+        L.total_dim = std::max(L.total_dim, c.total_dim);
+        L.cuda_mx_width = std::max(L.cuda_mx_width, c.cuda_mx_width);
+        L.info_mx_width = std::max(L.info_mx_width, c.info_mx_width);
+        L.fit_steps = std::max(L.fit_steps, c.fit_steps);
+        L.freq = std::max(L.freq, c.freq);
+        L.time = std::max(L.time, c.time);
+    }
+    r->layout = L;
+    std::vector<Plant> P(n_inst);
+    const int ms = margin_plant_stride();
+    std::vector<float> mp((size_t)n_inst * ms, 0.0f), zg;
+    std::vector<int> n_of(n_inst), F_of(n_inst), row_inst, row_w;
+    std::vector<int64_t> zoff(n_inst), goff(n_inst);
+    int64_t gtot = 0;
+    for (int i = 0; i < n_inst; ++i) {
+        const ce_config& c = cfgs[i];
+        build_plant(c, plants[i], 0, P[i]);
+        float* m = mp.data() + (size_t)i * ms;
+        std::memcpy(m, P[i].m_a, sizeof(P[i].m_a));
+        std::memcpy(m + MAXS * MAXS, P[i].m_b, sizeof(P[i].m_b));
+        std::memcpy(m + MAXS * MAXS + MAXS, P[i].m_c, sizeof(P[i].m_c));
+        m[MAXS * MAXS + 2 * MAXS] = P[i].m_d;
+        n_of[i] = c.serial ? c.discrete_dim : c.statespace_dim;
+        F_of[i] = c.freq;
+        zoff[i] = (int64_t)zg.size();
+        const std::vector<float> z = zgrid32(c);
+        zg.insert(zg.end(), z.begin(), z.end());
+        goff[i] = gtot;
+        gtot += (int64_t)c.freq * 8;
+        for (int w = 0; w <= c.freq; ++w) {
+            row_inst.push_back(i);
+            row_w.push_back(w);
+        }
+    }
+    // the pipeline's session: no plant of its own (every candidate's comes from the tables)
+    r->s = new ce_session();
+    ce_session* s = r->s;
+    s->cfg = L;
+    s->n_plants = 1;
+    s->plants.assign(1, Plant{});
+    s->plant_err.assign(1, std::string());
+    s->grid_np = 1;
+    s->alpha32.assign(1, 1.0f);
+    s->sim_kernel.assign(1, SimKernels{});
+    s->sim_kind = CE_SIM_TABLE;
+    init_streams(s);
+    // sweep grids and plant scalings of all instances
+    std::vector<void*> tmp;
+    auto up = [&](const auto& v) {
+        void* d = nullptr;
+        const size_t bytes = v.size() * sizeof(v[0]);
+        CE_CUDA(cudaMalloc(&d, bytes ? bytes : 1));
+        if (bytes) CE_CUDA(cudaMemcpy(d, v.data(), bytes, cudaMemcpyHostToDevice));
+        tmp.push_back(d);
+        return d;
+    };
+    struct Free {
+        std::vector<void*>& t;
+        ~Free() {
+            for (void* p : t) cudaFree(p);
+        }
+    } freer{tmp};
+    float* d_grid = nullptr;
+    CE_CUDA(cudaMalloc((void**)&d_grid, (size_t)gtot * sizeof(float)));
+    s->d_fgrid32 = d_grid;
+    float* d_alpha = (float*)up(std::vector<float>(n_inst, 0.0f));
+    int* d_bad = (int*)up(std::vector<int>(n_inst, 0));
+    launch_plant_grid_rows((int64_t)row_inst.size(), (const int*)up(row_inst), (const int*)up(row_w),
+                           (const int*)up(n_of), (const int*)up(F_of), (const int64_t*)up(zoff),
+                           (const int64_t*)up(goff), (const float*)up(mp), (const float*)up(zg), d_grid, d_alpha,
+                           d_bad, s->stream);
+    std::vector<float> alpha(n_inst);
+    std::vector<int> bad(n_inst);
+    CE_CUDA(cudaMemcpyAsync(alpha.data(), d_alpha, (size_t)n_inst * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CE_CUDA(cudaMemcpyAsync(bad.data(), d_bad, (size_t)n_inst * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CE_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < n_inst; ++i)
+        if (bad[i])
+            fail("ce_ragged_create: instance {}: allmargin: plant has no finite nonzero gain at crossover = {} rad/s",
+                 i, cfgs[i].crossover);
+    std::vector<Run> runs(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+        runs[i] = run_from_config(cfgs[i], L, 0, alpha[i], 0.0);
+        runs[i].grid_off = goff[i];
+    }
+    CE_CUDA(cudaMalloc((void**)&r->d_runs, (size_t)n_inst * sizeof(Run)));
+    CE_CUDA(cudaMemcpy(r->d_runs, runs.data(), (size_t)n_inst * sizeof(Run), cudaMemcpyHostToDevice));
+    CE_CUDA(cudaMalloc((void**)&r->d_plants, (size_t)n_inst * sizeof(Plant)));
+    CE_CUDA(cudaMemcpy(r->d_plants, P.data(), (size_t)n_inst * sizeof(Plant), cudaMemcpyHostToDevice));
+    *out = r.release();
+}
+
+// n_cand[i] candidates of instance i, rows packed instance after instance at
+// each instance's own widths (CUDA_MX and INFO_MX rows as its sessions take them).
+void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, const float* info_in,
+                     float* info_out) {
+    if (!r || !n_cand) fail("ce_ragged_evaluate: null argument");
+    const int I = (int)r->cfg.size();
+    int64_t N = 0;
+    for (int i = 0; i < I; ++i) {
+        if (n_cand[i] < 0) fail("ce_ragged_evaluate: instance {} has a negative candidate count {}", i, n_cand[i]);
+        N += n_cand[i];
+    }
+    if (N == 0) return;
+    if (!cuda_mx || !info_in || !info_out) fail("ce_ragged_evaluate: null buffer");
+    if (N > INT32_MAX) fail("ce_ragged_evaluate: {} candidates exceed the 32-bit candidate index", N);
+    const int64_t LW = r->layout.cuda_mx_width, LI = r->layout.info_mx_width;
+    if (N > r->host_cap) {
+        if (r->h_gains) cudaFreeHost(r->h_gains);
+        if (r->h_info) cudaFreeHost(r->h_info);
+        r->h_gains = r->h_info = nullptr;
+        r->host_cap = 0;
+        CE_CUDA(cudaMallocHost((void**)&r->h_gains, (size_t)N * LW * sizeof(float)));
+        CE_CUDA(cudaMallocHost((void**)&r->h_info, (size_t)N * LI * sizeof(float)));
+        r->host_cap = N;
+    }
+    if (N > r->inst_cap) {
+        if (r->d_inst) cudaFree(r->d_inst);
+        r->d_inst = nullptr;
+        r->inst_cap = 0;
+        CE_CUDA(cudaMalloc((void**)&r->d_inst, (size_t)N * sizeof(int)));
+        r->inst_cap = N;
+    }
+    r->h_inst.resize((size_t)N);
+    {
+        int64_t c = 0;
+        const float *g = cuda_mx, *in = info_in;
+        for (int i = 0; i < I; ++i) {
+            const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
+            for (int64_t k = 0; k < n_cand[i]; ++k, ++c, g += cw, in += iw) {
+                std::memcpy(r->h_gains + c * LW, g, (size_t)cw * sizeof(float));
+                std::memcpy(r->h_info + c * LI, in, (size_t)iw * sizeof(float));
+                r->h_inst[(size_t)c] = i;
+            }
+        }
+    }
+    ce_session* s = r->s;
+    ensure_buffers(s, N, false);
+    Buffers& b = s->buf;
+    CE_CUDA(cudaMemcpyAsync(b.gains, r->h_gains, (size_t)N * LW * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CE_CUDA(cudaMemcpyAsync(b.info, r->h_info, (size_t)N * LI * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CE_CUDA(cudaMemcpyAsync(r->d_inst, r->h_inst.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    const Ragged rg{r->d_runs, r->d_plants, r->d_inst};
+    run_pipeline(s, 0, N, b.gains, b.info, s->stream, false, false, &rg);
+    CE_CUDA(cudaMemcpyAsync(r->h_info, b.info, (size_t)N * LI * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CE_CUDA(cudaStreamSynchronize(s->stream));
+    collect_stage_times(s);
+    int64_t c = 0;
+    float* o = info_out;
+    for (int i = 0; i < I; ++i) {
+        const int iw = r->cfg[i].info_mx_width;
+        for (int64_t k = 0; k < n_cand[i]; ++k, ++c, o += iw)
+            std::memcpy(o, r->h_info + c * LI, (size_t)iw * sizeof(float));
+    }
+}
+
 }  // namespace
 }  // namespace ce
 
@@ -997,6 +1232,19 @@ CE_EXPORT int ce_session_create(const ce_config* cfg, const ce_plant* plant, int
 }
 
 CE_EXPORT void ce_session_destroy(ce_session* s) { destroy_session(s); }
+
+CE_EXPORT int ce_ragged_create(int32_t n_inst, const ce_config* cfgs, const ce_plant* plants, ce_ragged** out) {
+    return guarded([&] { create_ragged(n_inst, cfgs, plants, out); });
+}
+
+CE_EXPORT int ce_ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, const float* info_in,
+                                 float* info_out) {
+    return guarded([&] { ragged_evaluate(r, n_cand, cuda_mx, info_in, info_out); });
+}
+
+CE_EXPORT void ce_ragged_destroy(ce_ragged* r) { destroy_ragged(r); }
+
+CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r) { return r && r->s ? r->s->launches : -1; }
 
 CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {

@@ -49,6 +49,12 @@ void decode_instructions(const int32_t* info, int dim, int count, const float* b
 void launch_plant_grid(int precision, int np, int n, int F, const float* mp, const void* zg, void* grid, void* alpha,
                        int* bad, cudaStream_t st);
 int margin_plant_stride();
+// The same for a ragged batch in mixed precision: grid row t is row row_w[t] of
+// instance row_inst[t] (n_of: its margin-plant dimension, F_of: its frequency
+// count; zoff / goff: element offsets of its z grid and its sweep grid).
+void launch_plant_grid_rows(int64_t rows, const int* row_inst, const int* row_w, const int* n_of, const int* F_of,
+                            const int64_t* zoff, const int64_t* goff, const float* mp, const float* zg, float* grid,
+                            float* alpha, int* bad, cudaStream_t st);
 
 // Kernel launchers (ce_k_*.cu); all enqueue on `st`.
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,

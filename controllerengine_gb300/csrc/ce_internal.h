@@ -78,6 +78,18 @@ struct McPlants {
     int margin;          // 1: the margin plant is the candidate's plant (serial mode), 0: the Plant's
 };
 
+struct Run;
+
+// A ragged batch: instances of different configurations and plants evaluated
+// together.  Candidate c belongs to instance inst[c]; that instance's sizes and
+// scalars are runs[inst[c]] (whose row strides and slot sizes are the batch's
+// common maxima) and its plant plants[inst[c]].
+struct Ragged {
+    const Run* runs;      // null: a uniform evaluation (the launch's Run and Plant for every candidate)
+    const Plant* plants;
+    const int* inst;
+};
+
 // Sizes and scalars of one evaluation (the slice of the config the kernels read,
 // cf. EngineParams, ref: src/config.cu:84-104).
 struct Run {
@@ -102,6 +114,11 @@ struct Run {
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
     int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2 or 4; 0: the default)
     int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)
+    // floats (or reals) per candidate in the LIN_A, eigenvalue, AtA and Atb buffers:
+    // nt^2, 2nt, (2nt)^2, 2nt for a uniform evaluation, the maxima for a ragged one
+    int lina_slot, eig_slot, ata_slot, atb_slot;
+    int64_t grid_off;  // elements from the sweep grid argument to this run's grid
+    Ragged rg;
 };
 
 // Per-candidate simulation summary (the parts of the trajectory that modalsetup

@@ -691,7 +691,7 @@ __device__ __forceinline__ void list_if_stable(bool unstable, int64_t c, int* no
     }
 }
 
-template <int EQ>
+template <int EQ, bool RG = false>
 __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, int* __restrict__ nominal,
@@ -709,8 +709,10 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
         if (base >= run.n) break;
         const int64_t c = base + m;
         if (c < run.n) {
-            const int ns = run.ns, nt = run.nt;
-            const float* row = gains + c * run.cuda_w;
+            const Run& rn = run_of<RG>(run, c);
+            const Plant& PP = plant_of<RG>(run, P, c);
+            const int ns = rn.ns, nt = rn.nt;
+            const float* row = gains + c * rn.cuda_w;
             float K[MAXS], L[MAXS];
 #pragma unroll
             for (int i = 0; i < MAXS; ++i) {
@@ -718,19 +720,19 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
                 L[i] = i < ns ? row[ns + i] : 0.0f;
             }
             SMat T{smem + m, nt, eig_stride<EQ>()};
-            float* lrow = lina + c * (int64_t)(nt * nt);
+            float* lrow = lina + c * (int64_t)rn.lina_slot;
             auto fill = [&](const auto& pv) {
                 for (int e = Q.q; e < nt * nt; e += EQ) {
                     const int i = e / nt, j = e % nt;
-                    const float v = lina_entry(P, pv, K, L, ns, i, j);
+                    const float v = lina_entry(PP, pv, K, L, ns, i, j);
                     lrow[e] = v;
                     T(i, j) = (double)v;
                 }
             };
             if (run.mc.tab) fill(TablePlantValues{run.mc.tab, run.mc.np, run.mc.first + c});
-            else fill(BankPlantValues{P});
+            else fill(BankPlantValues{PP});
             Q.sync();
-            float* out = eig32 + c * (int64_t)(2 * nt);
+            float* out = eig32 + c * (int64_t)rn.eig_slot;
             float mx = 0.0f;
             eig_real(T, Q, nt, [&](int i, double re, double im) {
                 const float fr = (float)re, fi = (float)im;
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
             const int ns = run.ns, nt = run.nt;
             const float* row = gains + c * run.cuda_w;
             SMat T{smem + m, nt, eig_stride<EQ>()};
-            float* lrow = lina + c * (int64_t)(nt * nt);
+            float* lrow = lina + c * (int64_t)run.lina_slot;
             for (int e = Q.q; e < nt * nt; e += EQ) {
                 const int i = e / nt, j = e % nt;
                 double v;
@@ -780,7 +782,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
                 T(i, j) = v;
             }
             Q.sync();
-            double* out = eig64 + c * (int64_t)(2 * nt);
+            double* out = eig64 + c * (int64_t)run.eig_slot;
             double mx = 0.0;
             eig_real(T, Q, nt, [&](int i, double re, double im) {
                 out[2 * i] = re;
@@ -800,7 +802,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
 // unstable, so the only ones the sweep reads) are solved, packed into full
 // warps; the work is independent of the modal stage, so this kernel runs
 // concurrently with it.
-template <int EQ>
+template <int EQ, bool RG = false>
 __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
                                                        const int* __restrict__ list, const int* __restrict__ count,
@@ -815,9 +817,11 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
         const int64_t idx = base + m;
         if (idx < listed) {
             const int64_t c = list[idx];
-            const int ns = run.ns, nt = run.nt, n2 = 2 * ns;
-            const float* row = gains + c * run.cuda_w;
-            const float* la = lina + c * (int64_t)(nt * nt);
+            const Run& rn = run_of<RG>(run, c);
+            const Plant& PP = plant_of<RG>(run, P, c);
+            const int ns = rn.ns, nt = rn.nt, n2 = 2 * ns;
+            const float* row = gains + c * rn.cuda_w;
+            const float* la = lina + c * (int64_t)rn.lina_slot;
             SMat T{smem + m, n2, eig_stride<EQ>()};
             // margin plant: the Plant's (observer model in batch mode, the round's plant in
             // serial mode), or in serial mode with per-candidate plants the candidate's own
@@ -827,8 +831,8 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
                 const int i = e / ns, j = e % ns;
                 const float Li = row[ns + i];
                 const float Kj = row[j];
-                const float md = own ? 0.0f : P.m_d, mcj = own ? tv.c(j) : P.m_c[j], mbi = own ? tv.bu(i) : P.m_b[i];
-                const float maij = own ? tv.a(i, j) : P.m_a[i * MAXS + j];
+                const float md = own ? 0.0f : PP.m_d, mcj = own ? tv.c(j) : PP.m_c[j], mbi = own ? tv.bu(i) : PP.m_b[i];
+                const float maij = own ? tv.a(i, j) : PP.m_a[i * MAXS + j];
                 if (fp64_form) {
                     T(i, j) = (double)la[i * nt + j] - (double)md * (double)Li * (double)Kj;
                     T(i, ns + j) = -((double)Li * (double)mcj);
@@ -899,6 +903,9 @@ static void lina_eig_q(const Run& run, const Plant& P, int precision, const floa
     if (precision == CE_PRECISION_FP64) {
         set_smem((const void*)k_lina_eig64<EQ>, smem);
         k_lina_eig64<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig, nominal, list, count, count + 1);
+    } else if (run.rg.runs) {
+        set_smem((const void*)k_lina_eig<EQ, true>, smem);
+        k_lina_eig<EQ, true><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count, count + 1);
     } else {
         set_smem((const void*)k_lina_eig<EQ>, smem);
         k_lina_eig<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count, count + 1);
@@ -910,9 +917,15 @@ static void nominal_q(const Run& run, const Plant& P, int precision, const float
                       const int* list, const int* count, int* nominal, cudaStream_t st) {
     const int grid = eig_grid(run, run.n, eig_mats<EQ>());  // the listed count is only known on the device
     const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
-    set_smem((const void*)k_nominal<EQ>, smem);
-    k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, precision == CE_PRECISION_FP64,
-                                          const_cast<int*>(count) + 2);
+    if (run.rg.runs) {
+        set_smem((const void*)k_nominal<EQ, true>, smem);
+        k_nominal<EQ, true><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, 0,
+                                                    const_cast<int*>(count) + 2);
+    } else {
+        set_smem((const void*)k_nominal<EQ>, smem);
+        k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal,
+                                              precision == CE_PRECISION_FP64, const_cast<int*>(count) + 2);
+    }
 }
 
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,

@@ -135,16 +135,17 @@ __device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
 // candidates sharing a warp in k_fit run the same loop trip counts.  The slot
 // order inside a class is whatever the atomics give; every candidate's result
 // is computed by one half-warp alone, so it does not depend on that order.
-template <typename R>
-__global__ void __launch_bounds__(128) k_fit_classify(const Run run, const R* __restrict__ eig, int* __restrict__ counts,
-                                                      int* __restrict__ order) {
+template <typename R, bool RG = false>
+__global__ void __launch_bounds__(128) k_fit_classify(const Run run_in, const R* __restrict__ eig,
+                                                      int* __restrict__ counts, int* __restrict__ order) {
     const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
-    if (c >= run.n) return;
+    if (c >= run_in.n) return;
+    const Run& run = run_of<RG>(run_in, c);
     Modes<R> m;
-    load_modes<R>(eig + c * (int64_t)(2 * run.nt), run.nt, R(run.ts), m);
+    load_modes<R>(eig + c * (int64_t)run.eig_slot, run.nt, R(run.ts), m);
     const int cls = m.max_mag > R(1) ? 0 : m.unique;
     const int slot = atomicAdd(&counts[cls], 1);
-    order[(int64_t)cls * run.n + slot] = (int)c;
+    order[(int64_t)cls * run_in.n + slot] = (int)c;
 }
 
 // Candidate of half-warp h: classes in order of decreasing work (MAXT unique
@@ -160,8 +161,8 @@ __device__ __forceinline__ int64_t fit_candidate(const Run& run, const int* coun
     return run.n;
 }
 
-template <typename R, typename Sum>
-__global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __restrict__ eig, const R* __restrict__ ywin,
+template <typename R, typename Sum, bool RG = false>
+__global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __restrict__ eig, const R* __restrict__ ywin,
                                                    const Sum* __restrict__ summ, R* __restrict__ ata,
                                                    R* __restrict__ atb, float* __restrict__ info,
                                                    const int* __restrict__ counts, const int* __restrict__ order) {
@@ -171,18 +172,19 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run, const R* __res
     const int g = threadIdx.x >> 4;
     const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
     const int64_t h = (int64_t)blockIdx.x * FIT_CPB + g;
-    if (h >= run.n) return;  // the whole half-warp leaves together
-    const int64_t c = fit_candidate(run, counts, order, h);
-    if (c >= run.n) return;
+    if (h >= run_in.n) return;  // the whole half-warp leaves together
+    const int64_t c = fit_candidate(run_in, counts, order, h);
+    if (c >= run_in.n) return;
+    const Run& run = run_of<RG>(run_in, c);
     const int nt = run.nt;
     const R ts = R(run.ts);
 
     Modes<R> m;
-    load_modes<R>(eig + c * (int64_t)(2 * nt), nt, ts, m);
+    load_modes<R>(eig + c * (int64_t)run.eig_slot, nt, ts, m);
     float* out = info + c * (int64_t)run.info_w;
     const int n2 = 2 * nt;
-    R* arow = ata + c * (int64_t)(n2 * n2);
-    R* brow = atb + c * (int64_t)n2;
+    R* arow = ata + c * (int64_t)run.ata_slot;
+    R* brow = atb + c * (int64_t)run.atb_slot;
     // AtA is 2nt x 2nt with row stride 2nt; entries outside j <= i < nc stay
     // zero, as after the reference's memset (ref: src/main.cu:520-521)
     for (int e = lane; e < n2 * n2; e += 16) arow[e] = R(0);
@@ -334,8 +336,8 @@ __device__ __forceinline__ float rmin_normal<float>() { return FLT_MIN; }
 template <>
 __device__ __forceinline__ double rmin_normal<double>() { return DBL_MIN; }
 
-template <typename R>
-__global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const R* __restrict__ eig,
+template <typename R, bool RG = false>
+__global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run_in, const R* __restrict__ eig,
                                                             const R* __restrict__ ata, const R* __restrict__ atb,
                                                             float* __restrict__ info) {
     __shared__ R Ms[MODAL_WARPS][MAXNC][MAXNC + 1];
@@ -344,7 +346,8 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const
     __shared__ int trans[MODAL_WARPS][MAXNC];
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int64_t c = (int64_t)blockIdx.x * MODAL_WARPS + wi;
-    if (c >= run.n) return;  // whole warp
+    if (c >= run_in.n) return;  // whole warp
+    const Run& run = run_of<RG>(run_in, c);
     float* out = info + c * (int64_t)run.info_w;
     float* sc = out + run.info_scoring;
     float* fr = out + run.info_freqresp;
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const
     const int nt = run.nt, n = 2 * nt;
     const R ts = R(run.ts);
     Modes<R> m;
-    load_modes<R>(eig + c * (int64_t)(2 * nt), nt, ts, m);
+    load_modes<R>(eig + c * (int64_t)run.eig_slot, nt, ts, m);
     if (m.max_mag > R(1)) {
         if (lane == 0) {
             const float v = (float)radd(R(run.unstable_err), rdiv(rlog(m.max_mag), ts));
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const
         return;
     }
     R (*M)[MAXNC + 1] = Ms[wi];
-    const R* A = ata + c * (int64_t)(n * n);
+    const R* A = ata + c * (int64_t)run.ata_slot;
     // full symmetric copy of the lower triangle, then D^-1 A D^-1 with
     // D = diag(sqrt(a_ii) or 1) (ref: src/modalsolve.cu:154-162)
     if (lane < n)
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run, const
     if (lane < n) {
         const R inv_i = rdiv(R(1), cs[wi][lane]);
         for (int j = 0; j < n; ++j) M[lane][j] = rmul(rmul(inv_i, M[lane][j]), rdiv(R(1), cs[wi][j]));
-        xs[wi][lane] = rdiv(atb[c * (int64_t)n + lane], cs[wi][lane]);
+        xs[wi][lane] = rdiv(atb[c * (int64_t)run.atb_slot + lane], cs[wi][lane]);
     }
     __syncwarp();
 
@@ -552,6 +555,9 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
         if (precision == CE_PRECISION_FP64) {
             prefer_shared((const void*)k_fit_classify<double>);
             k_fit_classify<double><<<cgrid, 128, 0, st>>>(run, (const double*)eig, counts, order);
+        } else if (run.rg.runs) {
+            prefer_shared((const void*)k_fit_classify<float, true>);
+            k_fit_classify<float, true><<<cgrid, 128, 0, st>>>(run, (const float*)eig, counts, order);
         } else {
             prefer_shared((const void*)k_fit_classify<float>);
             k_fit_classify<float><<<cgrid, 128, 0, st>>>(run, (const float*)eig, counts, order);
@@ -559,8 +565,13 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
         CE_CUDA(cudaGetLastError());
     }
     prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_fit<double, double>
+                  : run.rg.runs                  ? (const void*)k_fit<float, SimSummary, true>
                                                  : (const void*)k_fit<float, SimSummary>);
-    if (precision == CE_PRECISION_FP64)
+    if (run.rg.runs && precision != CE_PRECISION_FP64)
+        k_fit<float, SimSummary, true><<<grid, FIT_BLOCK, 0, st>>>(run, (const float*)eig, (const float*)ywin,
+                                                                  (const SimSummary*)summ, (float*)ata, (float*)atb,
+                                                                  info, counts, order);
+    else if (precision == CE_PRECISION_FP64)
         k_fit<double, double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin,
                                                          (const double*)summ, (double*)ata, (double*)atb, info,
                                                          counts, order);
@@ -574,8 +585,13 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st) {
     const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
-    prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_modal<double> : (const void*)k_modal<float>);
-    if (precision == CE_PRECISION_FP64)
+    prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_modal<double>
+                  : run.rg.runs                  ? (const void*)k_modal<float, true>
+                                                 : (const void*)k_modal<float>);
+    if (run.rg.runs && precision != CE_PRECISION_FP64)
+        k_modal<float, true><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const float*)eig, (const float*)ata,
+                                                               (const float*)atb, info);
+    else if (precision == CE_PRECISION_FP64)
         k_modal<double><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
                                                           (const double*)atb, info);
     else

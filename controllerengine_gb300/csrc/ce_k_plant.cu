@@ -87,4 +87,67 @@ void launch_plant_grid(int precision, int np, int n, int F, const float* mp, con
 
 int margin_plant_stride() { return MP_STRIDE; }
 
+// A ragged batch: grid row t belongs to instance row_inst[t] at frequency
+// row_w[t] (row F of an instance: its crossover); every instance in the 8-wide
+// class (the zero padding of the shifted LU is exact).
+__global__ void __launch_bounds__(128) k_plant_grid_rows(int64_t rows, const int* __restrict__ row_inst,
+                                                         const int* __restrict__ row_w, const int* __restrict__ n_of,
+                                                         const int* __restrict__ F_of, const int64_t* __restrict__ zoff,
+                                                         const int64_t* __restrict__ goff, const float* __restrict__ mp,
+                                                         const float* __restrict__ zg, float* __restrict__ grid,
+                                                         float* __restrict__ alpha, int* __restrict__ bad) {
+    constexpr int NS = MAXS;
+    const int64_t t = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (t >= rows) return;
+    const int p = row_inst[t], w = row_w[t], n = n_of[p], F = F_of[p];
+    const float* m = mp + (int64_t)p * MP_STRIDE;
+    const float* zr = zg + zoff[p] + 4 * (int64_t)w;
+    float A[NS * NS], b[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+#pragma unroll
+        for (int j = 0; j < NS; ++j) A[i * NS + j] = (i < n && j < n) ? m[MP_A + i * MAXS + j] : 0.0f;
+        b[i] = i < n ? m[MP_B + i] : 0.0f;
+    }
+    const cplx<float> z{zr[0], zr[1]};
+    cplx<float> x[NS];
+    lu_solve_shifted<float, NS>(z, A, 1, b, x);
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) ok = ok && (i >= n || cfinite(x[i]));
+    cplx<float> P{0.0f, 0.0f};
+    if (ok) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i)
+            if (i < n) {
+                const cplx<float> tt = cmul(cplx<float>{m[MP_C + i], 0.0f}, x[i]);
+                P = cplx<float>{radd(P.re, tt.re), radd(P.im, tt.im)};
+            }
+        P.re = radd(P.re, m[MP_D]);
+    }
+    if (w < F) {
+        float* g = grid + goff[p] + 8 * (int64_t)w;
+        g[0] = z.re;
+        g[1] = z.im;
+        g[2] = zr[2];
+        g[3] = P.re;
+        g[4] = P.im;
+        g[5] = cabs_(P);
+        g[6] = ok ? 1.0f : 0.0f;
+        g[7] = 0.0f;
+    } else {
+        const float pmag = cabs_(P);
+        alpha[p] = rdiv(1.0f, pmag);
+        bad[p] = (!ok || !(pmag > 0.0f) || !isfinite(pmag)) ? 1 : 0;
+    }
+}
+
+void launch_plant_grid_rows(int64_t rows, const int* row_inst, const int* row_w, const int* n_of, const int* F_of,
+                            const int64_t* zoff, const int64_t* goff, const float* mp, const float* zg, float* grid,
+                            float* alpha, int* bad, cudaStream_t st) {
+    k_plant_grid_rows<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(rows, row_inst, row_w, n_of, F_of, zoff, goff,
+                                                                      mp, zg, grid, alpha, bad);
+    CE_CUDA(cudaGetLastError());
+}
+
 }  // namespace ce

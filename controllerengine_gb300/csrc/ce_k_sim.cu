@@ -10,11 +10,11 @@
 
 namespace ce {
 
-template <int NSC, int NDC, int KMODE>
+template <int NSC, int NDC, int KMODE, bool RG = false>
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __grid_constant__ Plant P,
                                                          const float* __restrict__ gains, float* __restrict__ ywin,
                                                          SimSummary* __restrict__ summ, float* __restrict__ traj) {
-    sim_run<NSC, NDC, TableChains, KMODE>(run, P, gains, ywin, summ, traj);
+    sim_run<NSC, NDC, TableChains, KMODE, RG>(run, P, gains, ywin, summ, traj);
 }
 
 // The plain FP64 form of the same recurrence: double state, no hi/lo split.
@@ -110,7 +110,14 @@ static void sim_launch(const Run& run, const Plant& P, int precision, const floa
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
                 cudaStream_t st) {
     const int cs = dim_class(run.ns), cd = dim_class(run.nd);
-    if (run.kalman && run.kal_list == 1) {
+    if (run.rg.runs) {
+        // a ragged batch: every instance at the reference's padded width, its plant from the table
+        if (precision == CE_PRECISION_FP64 || run.kalman)
+            throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
+        prefer_shared((const void*)k_sim_mixed<8, 8, SIM_LUENBERGER, true>);
+        k_sim_mixed<8, 8, SIM_LUENBERGER, true><<<sim_grid(run), SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin,
+                                                                                   (SimSummary*)summ, traj);
+    } else if (run.kalman && run.kal_list == 1) {
         // the shared-noise form; the Kalman loop always runs the full padded observer width
         if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);
         else sim_launch<8, 8, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);

@@ -42,11 +42,13 @@ __device__ __forceinline__ double rsqrtf_(double x) { return sqrt(x); }
 // modal stage (zero margins), or a nominal closed loop that is not stable
 // (the unstable penalty).  The rest are listed for k_sweep, so its warps hold
 // only candidates that run the frequency loop.
-__global__ void __launch_bounds__(128) k_sweep_select(const Run run, const int* __restrict__ nominal,
+template <bool RG = false>
+__global__ void __launch_bounds__(128) k_sweep_select(const Run run_in, const int* __restrict__ nominal,
                                                       float* __restrict__ info, int* __restrict__ list,
                                                       int* __restrict__ count) {
     const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
-    if (c >= run.n) return;
+    if (c >= run_in.n) return;
+    const Run& run = run_of<RG>(run_in, c);
     float* out = info + c * (int64_t)run.info_w;
     float* sc = out + run.info_scoring;
     float* am = out + run.info_allmargin;
@@ -82,8 +84,8 @@ __global__ void __launch_bounds__(128) k_sweep_select(const Run run, const int* 
 // discards.
 
 // fgrid row per frequency: z.re, z.im, arg z, P.re, P.im, |P|, ok, 0
-template <typename R, int NSC>
-__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const float* __restrict__ gains,
+template <typename R, int NSC, bool RG = false>
+__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run_in, const float* __restrict__ gains,
                                                             const float* __restrict__ lina,
                                                             const int* __restrict__ list, const int* __restrict__ count,
                                                             const R* __restrict__ fgrid, R* __restrict__ mag,
@@ -95,11 +97,12 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const
     const int64_t listed = *count;
     if (idx >= listed) return;
     const int g = blockIdx.y;
-    const int w0 = g * SWEEP_FG, w1 = min(run.freq, w0 + SWEEP_FG);
     const int64_t c = list[idx];
+    const Run& run = run_of<RG>(run_in, c);
+    const int w0 = g * SWEEP_FG, w1 = min(run.freq, w0 + SWEEP_FG);
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
-    const float* la = lina + c * (int64_t)(nt * nt);
+    const float* la = lina + c * (int64_t)run.lina_slot;
     R K[NSC], L[NSC];
 #pragma unroll
     for (int i = 0; i < NSC; ++i) {
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const
     const bool own = run.mc.tab && run.mc.grid_stride;
     const R ALPHA = own ? ((const R*)run.mc.alpha)[run.mc.first + c]
                         : (sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64));
-    const R* fgc = fgrid + (own ? c * run.mc.grid_stride : 0);
+    const R* fgc = fgrid + run.grid_off + (own ? c * run.mc.grid_stride : 0);
     R bmin = R(1);
     int first_bad = INT_MAX;
     for (int w = w0; w < w1; ++w) {
@@ -151,8 +154,8 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run, const
     fail[(int64_t)g * listed + idx] = first_bad;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(128) k_sweep_scan(const Run run, const int* __restrict__ list,
+template <typename R, bool RG = false>
+__global__ void __launch_bounds__(128) k_sweep_scan(const Run run_in, const int* __restrict__ list,
                                                     const int* __restrict__ count, const R* __restrict__ fgrid,
                                                     const R* __restrict__ mag, const R* __restrict__ arg,
                                                     const R* __restrict__ bpc, const int* __restrict__ fail,
@@ -161,11 +164,13 @@ __global__ void __launch_bounds__(128) k_sweep_scan(const Run run, const int* __
     const int64_t listed = *count;
     if (idx >= listed) return;
     const int64_t c = list[idx];
+    const Run& run = run_of<RG>(run_in, c);
     float* out = info + c * (int64_t)run.info_w;
     float* sc = out + run.info_scoring;
     float* am = out + run.info_allmargin;
     const float sc0 = sc[0];
     const float EIGF = run.eig_fail_err;
+    const R* fgc = fgrid + run.grid_off;
     const int groups = (run.freq + SWEEP_FG - 1) / SWEEP_FG;
     int first_bad = INT_MAX;
     R BPC = R(1);
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(128) k_sweep_scan(const Run run, const int* __
     for (int w = 0; w < run.freq; ++w) {
         const R m = mag[(int64_t)w * listed + idx];
         const R raw = arg[(int64_t)w * listed + idx];
-        const R theta = fgrid[8 * (int64_t)w + 2];
+        const R theta = fgc[8 * (int64_t)w + 2];
         if (w > 0) {
             R delta = rsub(raw, prevRaw);
             if (delta > PI) delta = rsub(delta, TWO_PI);
@@ -250,6 +255,18 @@ static void sweep_dispatch(const Run& run, const float* gains, const float* lina
     R* mag = (R*)sw.mag;
     R* arg = (R*)sw.arg;
     R* bpc = (R*)sw.bpc;
+    if constexpr (sizeof(R) == 4) {
+        if (run.rg.runs) {
+            // a ragged batch: every instance in the 8-wide class (the padding is exact)
+            prefer_shared((const void*)k_sweep_resp<R, 8, true>);
+            k_sweep_resp<R, 8, true><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, list, count, fgrid, mag, arg, bpc,
+                                                                   sw.fail);
+            prefer_shared((const void*)k_sweep_scan<R, true>);
+            k_sweep_scan<R, true><<<(unsigned)((run.n + 127) / 128), 128, 0, st>>>(run, list, count, fgrid, mag, arg,
+                                                                                  bpc, sw.fail, info);
+            return;
+        }
+    }
     if (run.ns <= 2) {
         prefer_shared((const void*)k_sweep_resp<R, 2>);
         k_sweep_resp<R, 2><<<grid, SWEEP_BLOCK, 0, st>>>(run, gains, lina, list, count, fgrid, mag, arg, bpc, sw.fail);
@@ -268,8 +285,13 @@ static void sweep_dispatch(const Run& run, const float* gains, const float* lina
 void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
                   const void* fgrid, float* info, int* list, int* count, const SweepScratch& sw, cudaStream_t st) {
     CE_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
-    prefer_shared((const void*)k_sweep_select);
-    k_sweep_select<<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, nominal, info, list, count);
+    if (run.rg.runs) {
+        prefer_shared((const void*)k_sweep_select<true>);
+        k_sweep_select<true><<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, nominal, info, list, count);
+    } else {
+        prefer_shared((const void*)k_sweep_select<false>);
+        k_sweep_select<false><<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, nominal, info, list, count);
+    }
     if (precision == CE_PRECISION_FP64)
         sweep_dispatch<double>(run, gains, lina, list, count, (const double*)fgrid, info, sw, st);
     else

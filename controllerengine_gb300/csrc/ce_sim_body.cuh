@@ -350,10 +350,19 @@ __device__ __forceinline__ void kalman_gain_shared(const Plant& P, KalShared& S,
 // with the covariance shared by the warp (all 32 lanes hold the same R and Q).
 constexpr int SIM_LUENBERGER = 0, SIM_KALMAN_LANE = 1, SIM_KALMAN_SHARED = 2;
 
-template <int NSC, int NDC, class Chains, int KMODE = SIM_LUENBERGER>
-__device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const float* __restrict__ gains,
+template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
+__device__ __forceinline__ void sim_candidate(const Run& run, const Plant& P, int64_t c, bool writer,
+                                              const float* __restrict__ gains, float* __restrict__ ywin,
+                                              SimSummary* __restrict__ summ, float* __restrict__ traj, Stage& stage,
+                                              SrcP& srcP, SrcH& srcH, KW& kw);
+
+// Maps the thread to its candidate (its own index, or an entry of a Kalman
+// candidate list) and runs that candidate with its sizes and plant.
+template <int NSC, int NDC, class Chains, int KMODE = SIM_LUENBERGER, bool RG = false>
+__device__ __forceinline__ void sim_run(const Run& run_in, const Plant& P_in, const float* __restrict__ gains,
                                         float* __restrict__ ywin, SimSummary* __restrict__ summ,
                                         float* __restrict__ traj) {
+    const Run& run = run_in;
     constexpr bool KAL = KMODE != SIM_LUENBERGER;
     constexpr bool SHARED = KMODE == SIM_KALMAN_SHARED;
     __shared__ float stage[8][SIM_BLOCK];
@@ -382,6 +391,18 @@ __device__ __forceinline__ void sim_run(const Run& run, const Plant& P, const fl
     } else {
         if (c >= run.n) return;
     }
+    return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_of<RG>(run_in, c), plant_of<RG>(run_in, P_in, c), c,
+                                                       writer, gains, ywin, summ, traj, stage, srcP, srcH, kw);
+}
+
+template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
+__device__ __forceinline__ void sim_candidate(const Run& run, const Plant& P, int64_t c, bool writer,
+                                              const float* __restrict__ gains, float* __restrict__ ywin,
+                                              SimSummary* __restrict__ summ, float* __restrict__ traj, Stage& stage,
+                                              SrcP& srcP, SrcH& srcH, KW& kw) {
+    constexpr bool KAL = KMODE != SIM_LUENBERGER;
+    constexpr bool SHARED = KMODE == SIM_KALMAN_SHARED;
+    const int tid = threadIdx.x;
     const typename Chains::template Local<NDC> Lc(run, P, c);
 
     const int ns = run.ns;

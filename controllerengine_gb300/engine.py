@@ -157,6 +157,68 @@ class PlantFiles:
         return p
 
 
+class Ragged:
+    """Instances of different configurations and plants evaluated together
+    (ce_ragged_create): one launch per stage over the candidates of all instances.
+    `instances` is a list of (EngineConfig, PlantFiles); `evaluate` takes one
+    (cuda_mx, info_mx) pair per instance (any row counts, zero included) and returns
+    the INFO rows per instance, each bit-identical to its own session's."""
+
+    def __init__(self, instances: list):
+        self.configs = [c for c, _ in instances]
+        self._plants = [p for _, p in instances]  # keeps the arrays alive for the call
+        k = len(instances)
+        cfgs = (_ffi.ce_config * k)(*[c.raw for c in self.configs])
+        pls = (_ffi.ce_plant * k)(*[p.ce_plant() for p in self._plants])
+        self._h = C.c_void_p()
+        _check(_lib().ce_ragged_create(k, cfgs, pls, C.byref(self._h)))
+
+    def evaluate(self, rows: list) -> list:
+        if len(rows) != len(self.configs):
+            raise ValueError(f"{len(rows)} row sets for {len(self.configs)} instances")
+        gs, infos, counts = [], [], []
+        for c, (g, i) in zip(self.configs, rows):
+            g = np.ascontiguousarray(g, dtype=F32).reshape(-1, c.cuda_mx_width)
+            n = g.shape[0]
+            i = np.zeros((n, c.info_mx_width), F32) if i is None else i
+            gs.append(g.reshape(-1))
+            infos.append(np.ascontiguousarray(i, dtype=F32).reshape(n, c.info_mx_width).reshape(-1))
+            counts.append(n)
+        g_all = np.concatenate(gs) if gs else np.zeros(0, F32)
+        i_all = np.concatenate(infos) if infos else np.zeros(0, F32)
+        out = np.empty_like(i_all)
+        nc = (C.c_int64 * len(counts))(*counts)
+        _check(_lib().ce_ragged_evaluate(self._h, nc, _fptr(g_all) if g_all.size else None,
+                                         _fptr(i_all) if i_all.size else None, _fptr(out) if out.size else None))
+        res, off = [], 0
+        for c, n in zip(self.configs, counts):
+            w = c.info_mx_width
+            res.append(out[off:off + n * w].reshape(n, w))
+            off += n * w
+        return res
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(_lib().ce_ragged_kernel_launches(self._h))
+
+    def close(self):
+        if self._h:
+            _lib().ce_ragged_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Session:
     """Plant + config resident on the current CUDA device (ce_session_create)."""
 

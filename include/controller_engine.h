@@ -223,6 +223,25 @@ CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int6
 /* Launches of this library's kernels since the session was created. */
 CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s);
 
+/*
+ * Ragged batches (no counterpart in the reference, which runs one configuration
+ * per call): n_inst instances, each with its own configuration (dimensions,
+ * nonlinear terms, instruction programs, horizon, sweep) and plant, evaluated
+ * together -- one launch per stage over the candidates of all instances, each
+ * candidate with its instance's sizes and plant.  Every instance's rows equal,
+ * bit for bit, what a session of its own configuration and plant returns.
+ * Mixed precision and the Luenberger observer; plants[i] holds one plant.
+ * ce_ragged_evaluate takes n_cand[i] candidates of instance i, the CUDA_MX and
+ * INFO_MX rows packed instance after instance at each instance's own widths,
+ * and writes the INFO rows the same way (host buffers, synchronous).
+ */
+typedef struct ce_ragged ce_ragged;
+CE_EXPORT int ce_ragged_create(int32_t n_inst, const ce_config* cfgs, const ce_plant* plants, ce_ragged** out);
+CE_EXPORT int ce_ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, const float* info_in,
+                                 float* info_out);
+CE_EXPORT void ce_ragged_destroy(ce_ragged* r);
+CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r);
+
 /* Launch tuning of a session (no counterpart in the reference).  0 fields take
  * the library defaults (2 lanes per matrix, 5 blocks per SM, 2 chunks for
  * batches of >= 32,768 candidates).  No setting changes a result.

@@ -40,3 +40,16 @@ def test_version_and_error_channel(lib):
     import pytest
     with pytest.raises(ce.ControllerEngineError, match="missing `statespace_dim`"):
         ce.EngineConfig.parse("time = 5\n")
+
+
+def test_ragged_rejects_before_any_device_work(lib):
+    """Configuration checks of ce_ragged_create run before it touches the device."""
+    import pytest
+    from controllerengine_gb300 import synth
+    p = synth.mass_spring(4)
+    k = synth.with_kalman(p)
+    cfgs = [ce.EngineConfig.parse(p.config_text), ce.EngineConfig.parse(k.config_text)]
+    with pytest.raises(ce.ControllerEngineError, match="instance 1: a ragged batch runs the Luenberger observer"):
+        ce.Ragged([(cfgs[0], p.plant), (cfgs[1], k.plant)])
+    with pytest.raises(ce.ControllerEngineError, match="n_inst must be >= 1"):
+        ce.Ragged([])

@@ -1,0 +1,75 @@
+"""Ragged batches (ce_ragged_*): instances of different shapes -- dimensions 2..8, 0..4
+nonlinear terms with their own instruction programs, horizons, sweep sizes, batch and serial
+margin plants -- evaluated together with one launch per stage must give every instance's rows
+bit for bit as a session of its own configuration and plant does."""
+import numpy as np
+import pytest
+
+import controllerengine_gb300 as ce
+from controllerengine_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def _instances():
+    rng = np.random.default_rng(21)
+    probs = []
+    for k in range(10):
+        probs.append(synth.random_shape(300 + k, n=int(rng.integers(1, 60)), time=int(rng.integers(400, 2500)),
+                                        freq=int(rng.integers(30, 160))))
+    probs.append(synth.mass_spring(40))
+    mc = synth.monte_carlo(n_plants=1, time=900, freq=50, serial=True)
+    probs.append(synth.Problem(mc.name, mc.config_text, mc.plant, np.repeat(mc.cuda_mx, 7, 0),
+                               np.repeat(mc.info_mx, 7, 0)))
+    return probs
+
+
+def test_ragged_equals_own_sessions():
+    probs = _instances()
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    assert len({(c.statespace_dim, c.discrete_dim, c.nonlin_dim) for c in cfgs}) >= 6
+    assert any(c.serial for c in cfgs)
+    with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+        l0 = rb.kernel_launches
+        outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+        assert rb.kernel_launches - l0 == 9  # one launch per stage for all instances together
+        again = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+    for c, p, o, o2 in zip(cfgs, probs, outs, again):
+        with ce.Session(c, p.plant) as s:
+            ref = s.evaluate(p.cuda_mx, p.info_mx)
+        assert np.array_equal(_bits(o), _bits(ref)), p.name
+        assert np.array_equal(_bits(o2), _bits(ref)), p.name
+    sc = np.concatenate([o[:, c.info_scoring] for c, o in zip(cfgs, outs)])
+    assert (sc < 1e6).sum() > 20 and (sc >= 1e6).sum() > 0  # scored and unstable loops both present
+
+
+def test_ragged_many_single_candidate_instances():
+    """One candidate per instance, as in the uneven-size configuration; a sample of the
+    instances against their own sessions."""
+    probs = [synth.random_shape(2000 + k, n=1, time=int(400 + 37 * k % 1500), freq=int(30 + 7 * k % 120))
+             for k in range(400)]
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+        outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+    for k in range(0, 400, 23):
+        with ce.Session(cfgs[k], probs[k].plant) as s:
+            ref = s.evaluate(probs[k].cuda_mx, probs[k].info_mx)
+        assert np.array_equal(_bits(outs[k]), _bits(ref)), k
+
+
+def test_ragged_empty_and_uneven_counts():
+    probs = _instances()[:4]
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+        outs = rb.evaluate([(p.cuda_mx[:0], p.info_mx[:0]) if k % 2 else (p.cuda_mx, p.info_mx)
+                            for k, p in enumerate(probs)])
+        none = rb.evaluate([(p.cuda_mx[:0], p.info_mx[:0]) for p in probs])
+    assert all(o.shape[0] == 0 for k, o in enumerate(outs) if k % 2)
+    assert all(o.shape[0] == 0 for o in none)
+    for k in (0, 2):
+        with ce.Session(cfgs[k], probs[k].plant) as s:
+            assert np.array_equal(_bits(outs[k]), _bits(s.evaluate(probs[k].cuda_mx, probs[k].info_mx)))
