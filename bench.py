@@ -354,6 +354,82 @@ def monte_carlo_bench(n_plants: int, steps: int, warmup: int):
             "session_setup_s": setup, "scored_fraction": float(np.mean(sc < cfg.unstable_err))}
 
 
+def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
+    """The uneven-size workload (synth.uneven: n_inst instances of one candidate each, dimensions
+    2..8, 0-4 nonlinear terms with their own instruction programs, horizons 1e3..2e4 steps,
+    50..400 sweep points): instances/s of one ragged batch (ce_ragged_evaluate, host buffers, every
+    stage one launch over all instances), beside (a) the same instances evaluated one session each
+    (a sample of them, sessions created beforehand), and (b) the padded-to-max form: n_inst
+    candidates of the 8-state plant at the largest horizon and sweep (20,000 steps, 400 points)
+    in one session."""
+    import controllerengine_gb300 as ce
+    from controllerengine_gb300 import synth
+    t0 = time.perf_counter()
+    probs = synth.uneven(n_inst)
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    rb = ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)])
+    setup = time.perf_counter() - t0
+    # the C ABI's packed rows (instance after instance at each instance's widths)
+    counts = [p.cuda_mx.shape[0] for p in probs]
+    g_all = np.concatenate([p.cuda_mx.reshape(-1) for p in probs])
+    i_all = np.concatenate([p.info_mx.reshape(-1) for p in probs])
+    for _ in range(warmup):
+        rb.evaluate_packed(counts, g_all, i_all)
+    l0 = rb.kernel_launches
+    rb.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = rb.evaluate_packed(counts, g_all, i_all)
+    wall = (time.perf_counter() - t0) / steps
+    stages = {k: v[0] / steps for k, v in rb.stage_times().items() if v[1]}
+    launches = (rb.kernel_launches - l0) // steps
+    rb.close()
+    offs = np.cumsum([0] + [c.info_mx_width for c in cfgs])
+    scored = float(np.mean([out[offs[k] + c.info_scoring] < c.unstable_err for k, c in enumerate(cfgs)]))
+    # (a) one session per instance, on a sample (table-driven simulation: no compile per instance)
+    rng = np.random.default_rng(3)
+    pick = rng.choice(n_inst, size=min(sample, n_inst), replace=False)
+    prev = os.environ.get("CE_SIM_KERNEL")
+    os.environ["CE_SIM_KERNEL"] = "table"
+    try:
+        sess = [ce.Session(cfgs[k], probs[k].plant) for k in pick]
+    finally:
+        if prev is None:
+            os.environ.pop("CE_SIM_KERNEL")
+        else:
+            os.environ["CE_SIM_KERNEL"] = prev
+    for s_, k in zip(sess, pick):
+        s_.evaluate(probs[k].cuda_mx, probs[k].info_mx)
+    t0 = time.perf_counter()
+    for s_, k in zip(sess, pick):
+        s_.evaluate(probs[k].cuda_mx, probs[k].info_mx)
+    per_inst = (time.perf_counter() - t0) / len(pick)
+    for s_ in sess:
+        s_.close()
+    # (b) padded to the largest shape, horizon and sweep
+    pm = synth.eight_state(n=n_inst, time=20000, freq=400)
+    pc = ce.EngineConfig.parse(pm.config_text)
+    with ce.Session(pc, pm.plant) as s_:
+        for _ in range(warmup):
+            s_.evaluate(pm.cuda_mx, pm.info_mx)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            s_.evaluate(pm.cuda_mx, pm.info_mx)
+        padded = (time.perf_counter() - t0) / steps
+    shapes = {(c.statespace_dim, c.discrete_dim, c.nonlin_dim) for c in cfgs}
+    return {"workload": f"{n_inst} instances x 1 candidate: dims 2..8 ({len(shapes)} distinct (ns, nd, nw)), "
+                        "0-4 NL terms, horizons 1e3..2e4, 50..400 sweep points",
+            "instances_per_s": n_inst / wall, "ms_per_step": 1e3 * wall, "steps": steps,
+            "launches_per_step": launches, "stages_ms_per_step": stages, "setup_s": setup,
+            "scored_fraction": scored,
+            "one_session_per_instance": {"instances_per_s": 1.0 / per_inst, "ms_per_instance": 1e3 * per_inst,
+                                         "sample": len(pick)},
+            "padded_to_max": {"instances_per_s": n_inst / padded, "ms_per_step": 1e3 * padded,
+                              "shape": "8-state, 4 NL terms, 20000 steps, 400 points"},
+            "timing": "wall clock around the synchronous host-buffer call ce_ragged_evaluate (packing to the "
+                      "device layout, copies and kernels)"}
+
+
 def _kalman_time(p, n: int, steps: int, warmup: int):
     import torch
     import controllerengine_gb300 as ce
@@ -428,6 +504,7 @@ def main():
     ap.add_argument("--ref-gpu-build", type=int, default=1,
                     help="reference arm: also time the reference's own kernels + host stages (0: skip)")
     ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
+    ap.add_argument("--uneven-instances", type=int, default=16384, help="uneven-size ragged batch (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -613,6 +690,8 @@ def main():
     }
     if rank == 0 and a.mc_plants > 0:
         line["monte_carlo"] = monte_carlo_bench(a.mc_plants, 2, 1)
+    if rank == 0 and a.uneven_instances > 0:
+        line["uneven"] = uneven_bench(a.uneven_instances, 3, 2)
     if rank == 0 and a.kalman_candidates > 0:
         line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
     if rank == 0 and a.serve_seconds > 0:

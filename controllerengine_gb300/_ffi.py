@@ -30,6 +30,7 @@ EXPORTED_SYMBOLS = (
     "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
     "ce_server_submit_model", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
     "ce_ragged_create", "ce_ragged_evaluate", "ce_ragged_destroy", "ce_ragged_kernel_launches",
+    "ce_ragged_set_profiling", "ce_ragged_stage_times",
     "RunControllerEngine",
 )
 PENDING = 2
@@ -155,6 +156,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_ragged_destroy.restype = None
     lib.ce_ragged_kernel_launches.argtypes = [C.c_void_p]
     lib.ce_ragged_kernel_launches.restype = C.c_int64
+    lib.ce_ragged_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    lib.ce_ragged_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_int64)]
     lib.ce_server_wait.argtypes = [C.c_void_p, C.c_int64, C.c_int32]

@@ -142,6 +142,7 @@ struct ce_ragged {
     ce::Plant* d_plants = nullptr;          // per instance
     ce::Run* d_runs = nullptr;              // per instance, with the strides and slots of `layout`
     int* d_inst = nullptr;                  // instance of each candidate of the current evaluation
+    float* d_tab = nullptr;                 // their simulation table (RT_FIELDS x inst_cap)
     int64_t inst_cap = 0;
     float *h_gains = nullptr, *h_info = nullptr;  // pinned staging rows at the layout widths
     int64_t host_cap = 0;
@@ -1010,6 +1011,7 @@ void destroy_ragged(ce_ragged* r) {
     if (r->d_plants) cudaFree(r->d_plants);
     if (r->d_runs) cudaFree(r->d_runs);
     if (r->d_inst) cudaFree(r->d_inst);
+    if (r->d_tab) cudaFree(r->d_tab);
     if (r->h_gains) cudaFreeHost(r->h_gains);
     if (r->h_info) cudaFreeHost(r->h_info);
     destroy_session(r->s);
@@ -1151,17 +1153,34 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
     }
     if (N > r->inst_cap) {
         if (r->d_inst) cudaFree(r->d_inst);
+        if (r->d_tab) cudaFree(r->d_tab);
         r->d_inst = nullptr;
+        r->d_tab = nullptr;
         r->inst_cap = 0;
         CE_CUDA(cudaMalloc((void**)&r->d_inst, (size_t)N * sizeof(int)));
+        CE_CUDA(cudaMalloc((void**)&r->d_tab, (size_t)RT_FIELDS * N * sizeof(float)));
         r->inst_cap = N;
     }
     r->h_inst.resize((size_t)N);
+    // the caller's row offsets of each instance, then the device order: instances by
+    // decreasing horizon, so a warp's candidates run similar step counts
+    std::vector<int64_t> goff(I), ioff(I);
+    int64_t gi = 0, ii = 0;
+    for (int i = 0; i < I; ++i) {
+        goff[i] = gi;
+        ioff[i] = ii;
+        gi += n_cand[i] * r->cfg[i].cuda_mx_width;
+        ii += n_cand[i] * r->cfg[i].info_mx_width;
+    }
+    std::vector<int> order(I);
+    for (int i = 0; i < I; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
     {
         int64_t c = 0;
-        const float *g = cuda_mx, *in = info_in;
-        for (int i = 0; i < I; ++i) {
+        for (int i : order) {
             const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
+            const float* g = cuda_mx + goff[i];
+            const float* in = info_in + ioff[i];
             for (int64_t k = 0; k < n_cand[i]; ++k, ++c, g += cw, in += iw) {
                 std::memcpy(r->h_gains + c * LW, g, (size_t)cw * sizeof(float));
                 std::memcpy(r->h_info + c * LI, in, (size_t)iw * sizeof(float));
@@ -1175,15 +1194,17 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
     CE_CUDA(cudaMemcpyAsync(b.gains, r->h_gains, (size_t)N * LW * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CE_CUDA(cudaMemcpyAsync(b.info, r->h_info, (size_t)N * LI * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CE_CUDA(cudaMemcpyAsync(r->d_inst, r->h_inst.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-    const Ragged rg{r->d_runs, r->d_plants, r->d_inst};
+    launch_ragged_table(N, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, s->stream);
+    s->launches += 1;
+    const Ragged rg{r->d_runs, r->d_plants, r->d_inst, r->d_tab, r->inst_cap};
     run_pipeline(s, 0, N, b.gains, b.info, s->stream, false, false, &rg);
     CE_CUDA(cudaMemcpyAsync(r->h_info, b.info, (size_t)N * LI * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     CE_CUDA(cudaStreamSynchronize(s->stream));
     collect_stage_times(s);
     int64_t c = 0;
-    float* o = info_out;
-    for (int i = 0; i < I; ++i) {
+    for (int i : order) {
         const int iw = r->cfg[i].info_mx_width;
+        float* o = info_out + ioff[i];
         for (int64_t k = 0; k < n_cand[i]; ++k, ++c, o += iw)
             std::memcpy(o, r->h_info + c * LI, (size_t)iw * sizeof(float));
     }
@@ -1245,6 +1266,20 @@ CE_EXPORT int ce_ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const floa
 CE_EXPORT void ce_ragged_destroy(ce_ragged* r) { destroy_ragged(r); }
 
 CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r) { return r && r->s ? r->s->launches : -1; }
+
+CE_EXPORT int ce_ragged_set_profiling(ce_ragged* r, int32_t on) {
+    return guarded([&] {
+        if (!r) fail("null ragged batch");
+        if (ce_session_set_profiling(r->s, on)) fail("{}", g_last_error);
+    });
+}
+
+CE_EXPORT int ce_ragged_stage_times(ce_ragged* r, double* ms, int64_t* launches) {
+    return guarded([&] {
+        if (!r) fail("null ragged batch");
+        if (ce_session_stage_times(r->s, ms, launches)) fail("{}", g_last_error);
+    });
+}
 
 CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {

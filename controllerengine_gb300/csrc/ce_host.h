@@ -106,6 +106,9 @@ void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, 
 
 // Blocks of SIM_BLOCK threads that cover the candidates (or list slots) of `run`.
 int sim_grid(const Run& run);
+// The per-candidate table of a ragged batch (RT_FIELDS x stride floats) for n candidates.
+void launch_ragged_table(int64_t n, const Plant* plants, const int* inst, float* tab, int64_t stride,
+                         cudaStream_t st);
 
 // Grouping of a Kalman evaluation's candidates by their noise weights (R and
 // the diagonal of Q, bit for bit) for the shared-noise simulation form

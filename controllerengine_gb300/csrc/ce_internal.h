@@ -88,7 +88,25 @@ struct Ragged {
     const Run* runs;      // null: a uniform evaluation (the launch's Run and Plant for every candidate)
     const Plant* plants;
     const int* inst;
+    // the simulation's plant values per candidate, field-major: field f of
+    // candidate c at tab[f * tab_stride + c] (consecutive candidates read
+    // consecutive words whatever their instances)
+    const float* tab;
+    int64_t tab_stride;
 };
+
+// Fields of that table: observer model, plant, instruction counts and slots.
+constexpr int RT_SAI = 0;                       // ss_a - I, row stride MAXS
+constexpr int RT_SB = RT_SAI + MAXS * MAXS;     // ss_b
+constexpr int RT_SC = RT_SB + MAXS;             // ss_c
+constexpr int RT_SD = RT_SC + MAXS;             // ss_d
+constexpr int RT_DAI = RT_SD + 1;               // d_a - I, row stride MAXD
+constexpr int RT_DBU = RT_DAI + MAXD * MAXD;    // d_bu
+constexpr int RT_DBW = RT_DBU + MAXD;           // d_bw, row stride MAXW
+constexpr int RT_CNT = RT_DBW + MAXD * MAXW;    // counts: n_dc | n_u << 8 | n_nl[0] << 16 | n_nl[1] << 24, then n_nl[2] | n_nl[3] << 8
+constexpr int RT_INS = RT_CNT + 2;              // per slot: code (op | col << 8 | akind << 16 | bkind << 24), aval, bval
+constexpr int RT_SLOTS = MAX_DC + MAX_U + MAXW * MAX_NL;  // DC k: k; U k: MAX_DC + k; NL w, k: MAX_DC + MAX_U + w MAX_NL + k
+constexpr int RT_FIELDS = RT_INS + 3 * RT_SLOTS;
 
 // Sizes and scalars of one evaluation (the slice of the config the kernels read,
 // cf. EngineParams, ref: src/config.cu:84-104).

@@ -17,6 +17,54 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_mixed(const Run run, const __
     sim_run<NSC, NDC, TableChains, KMODE, RG>(run, P, gains, ywin, summ, traj);
 }
 
+// A ragged batch: every candidate with its instance's sizes, its plant and
+// instruction program from the per-candidate table, at the reference's padded width.
+__global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const __grid_constant__ Plant P,
+                                                          const float* __restrict__ gains, float* __restrict__ ywin,
+                                                          SimSummary* __restrict__ summ, float* __restrict__ traj) {
+    sim_run<MAXS, MAXD, RagChains, SIM_LUENBERGER, true>(run, P, gains, ywin, summ, traj);
+}
+
+// The per-candidate table of a ragged batch (the RT_* fields) from the
+// instances' plants: one thread per candidate, each field a coalesced store.
+__global__ void __launch_bounds__(128) k_ragged_table(int64_t n, const Plant* __restrict__ plants,
+                                                      const int* __restrict__ inst, float* __restrict__ tab,
+                                                      int64_t stride) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (c >= n) return;
+    const Plant& P = plants[inst[c]];
+    auto put = [&](int f, float v) { tab[(int64_t)f * stride + c] = v; };
+    auto put_u = [&](int f, unsigned v) { put(f, __uint_as_float(v)); };
+    for (int e = 0; e < MAXS * MAXS; ++e) put(RT_SAI + e, P.ss_ai[e]);
+    for (int i = 0; i < MAXS; ++i) {
+        put(RT_SB + i, P.ss_b[i]);
+        put(RT_SC + i, P.ss_c[i]);
+    }
+    put(RT_SD, P.ss_d);
+    for (int e = 0; e < MAXD * MAXD; ++e) put(RT_DAI + e, P.d_ai[e]);
+    for (int i = 0; i < MAXD; ++i) put(RT_DBU + i, P.d_bu[i]);
+    for (int e = 0; e < MAXD * MAXW; ++e) put(RT_DBW + e, P.d_bw[e]);
+    put_u(RT_CNT, (unsigned)P.n_dc | (unsigned)P.n_u << 8 | (unsigned)P.n_nl[0] << 16 | (unsigned)P.n_nl[1] << 24);
+    put_u(RT_CNT + 1, (unsigned)P.n_nl[2] | (unsigned)P.n_nl[3] << 8);
+    auto slot = [&](int sl, const Instr& I) {
+        // an op outside 1..6 leaves the result unchanged whatever its value
+        const unsigned op = (I.op >= 1 && I.op <= 6) ? (unsigned)I.op : 7u;
+        put_u(RT_INS + 3 * sl, op | (unsigned)I.col << 8 | (unsigned)I.akind << 16 | (unsigned)I.bkind << 24);
+        put(RT_INS + 3 * sl + 1, I.aval);
+        put(RT_INS + 3 * sl + 2, I.bval);
+    };
+    for (int k = 0; k < P.n_dc; ++k) slot(k, P.dc[k]);
+    for (int k = 0; k < P.n_u; ++k) slot(MAX_DC + k, P.u[k]);
+    for (int w = 0; w < MAXW; ++w)
+        for (int k = 0; k < P.n_nl[w]; ++k) slot(MAX_DC + MAX_U + w * MAX_NL + k, P.nl[w][k]);
+}
+
+void launch_ragged_table(int64_t n, const Plant* plants, const int* inst, float* tab, int64_t stride,
+                         cudaStream_t st) {
+    k_ragged_table<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, plants, inst, tab, stride);
+    CE_CUDA(cudaGetLastError());
+}
+
 // The plain FP64 form of the same recurrence: double state, no hi/lo split.
 template <int NSC, int NDC>
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __grid_constant__ Plant P,
@@ -114,9 +162,11 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
         // a ragged batch: every instance at the reference's padded width, its plant from the table
         if (precision == CE_PRECISION_FP64 || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
-        prefer_shared((const void*)k_sim_mixed<8, 8, SIM_LUENBERGER, true>);
-        k_sim_mixed<8, 8, SIM_LUENBERGER, true><<<sim_grid(run), SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin,
-                                                                                   (SimSummary*)summ, traj);
+        const size_t cols = (size_t)RT_FIELDS * SIM_BLOCK * sizeof(float);  // the candidates' table columns
+        CE_CUDA(cudaFuncSetAttribute((const void*)k_sim_ragged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cols));
+        prefer_shared((const void*)k_sim_ragged);
+        k_sim_ragged<<<sim_grid(run), SIM_BLOCK, cols, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
     } else if (run.kalman && run.kal_list == 1) {
         // the shared-noise form; the Kalman loop always runs the full padded observer width
         if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);

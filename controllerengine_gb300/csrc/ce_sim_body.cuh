@@ -55,6 +55,37 @@ struct BankLocal {
     __device__ __forceinline__ float ai(int i, int j) const { return P.d_ai[i * MAXD + j]; }
     __device__ __forceinline__ float bu(int i) const { return P.d_bu[i]; }
     __device__ __forceinline__ float bw(int i, int k) const { return P.d_bw[i * MAXW + k]; }
+    // the observer model
+    __device__ __forceinline__ float sai(int i, int j) const { return P.ss_ai[i * MAXS + j]; }
+    __device__ __forceinline__ float sb(int i) const { return P.ss_b[i]; }
+    __device__ __forceinline__ float sc(int i) const { return P.ss_c[i]; }
+    __device__ __forceinline__ float sd() const { return P.ss_d; }
+};
+
+// ...or, in a ragged batch, the candidate's column of the per-candidate table
+// (observer model, plant and instruction program alike), copied once into this
+// thread's column of the block's dynamic shared memory (RT_FIELDS x SIM_BLOCK
+// words), where every step reads it.
+template <int NDC>
+struct RagLocal {
+    const float* t;
+    int s;
+    __device__ __forceinline__ RagLocal(const Run& run, const Plant&, int64_t c) : s(SIM_BLOCK) {
+        extern __shared__ float rag_cols[];
+        const float* __restrict__ g = run.rg.tab + c;
+        const int64_t gs = run.rg.tab_stride;
+        float* col = rag_cols + threadIdx.x;
+        for (int f = 0; f < RT_FIELDS; ++f) col[f * SIM_BLOCK] = g[(int64_t)f * gs];
+        t = col;
+    }
+    __device__ __forceinline__ float f(int field) const { return t[field * s]; }
+    __device__ __forceinline__ float ai(int i, int j) const { return f(RT_DAI + i * MAXD + j); }
+    __device__ __forceinline__ float bu(int i) const { return f(RT_DBU + i); }
+    __device__ __forceinline__ float bw(int i, int k) const { return f(RT_DBW + i * MAXW + k); }
+    __device__ __forceinline__ float sai(int i, int j) const { return f(RT_SAI + i * MAXS + j); }
+    __device__ __forceinline__ float sb(int i) const { return f(RT_SB + i); }
+    __device__ __forceinline__ float sc(int i) const { return f(RT_SC + i); }
+    __device__ __forceinline__ float sd() const { return f(RT_SD); }
 };
 
 // ...or the candidate's own plant from the per-candidate plant table, loaded
@@ -63,7 +94,7 @@ struct BankLocal {
 template <int NDC>
 struct McLocal {
     float ai_[NDC * NDC], bu_[NDC], bw_[NDC * MAXW], cst_[2 * MC_SLOTS];
-    __device__ __forceinline__ McLocal(const Run& run, const Plant&, int64_t c) {
+    __device__ __forceinline__ McLocal(const Run& run, const Plant& plant, int64_t c) : P(plant) {
         const float* __restrict__ t = run.mc.tab;
         const int64_t np = run.mc.np, p = run.mc.first + c;
 #pragma unroll
@@ -81,6 +112,12 @@ struct McLocal {
     __device__ __forceinline__ float bu(int i) const { return bu_[i]; }
     __device__ __forceinline__ float bw(int i, int k) const { return bw_[i * MAXW + k]; }
     __device__ __forceinline__ float c(int k) const { return cst_[k]; }
+    // the observer model is the launch's, shared by all plants
+    const Plant& P;
+    __device__ __forceinline__ float sai(int i, int j) const { return P.ss_ai[i * MAXS + j]; }
+    __device__ __forceinline__ float sb(int i) const { return P.ss_b[i]; }
+    __device__ __forceinline__ float sc(int i) const { return P.ss_c[i]; }
+    __device__ __forceinline__ float sd() const { return P.ss_d; }
 };
 
 // P <- (M P) M^T over the padded 8 x 8 covariance, in place (ABATf, ref:
@@ -351,8 +388,8 @@ __device__ __forceinline__ void kalman_gain_shared(const Plant& P, KalShared& S,
 constexpr int SIM_LUENBERGER = 0, SIM_KALMAN_LANE = 1, SIM_KALMAN_SHARED = 2;
 
 template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
-__device__ __forceinline__ void sim_candidate(const Run& run, const Plant& P, int64_t c, bool writer,
-                                              const float* __restrict__ gains, float* __restrict__ ywin,
+__device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run, const Plant& P, int64_t c,
+                                              bool writer, const float* __restrict__ gains, float* __restrict__ ywin,
                                               SimSummary* __restrict__ summ, float* __restrict__ traj, Stage& stage,
                                               SrcP& srcP, SrcH& srcH, KW& kw);
 
@@ -391,19 +428,19 @@ __device__ __forceinline__ void sim_run(const Run& run_in, const Plant& P_in, co
     } else {
         if (c >= run.n) return;
     }
-    return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_of<RG>(run_in, c), plant_of<RG>(run_in, P_in, c), c,
-                                                       writer, gains, ywin, summ, traj, stage, srcP, srcH, kw);
+    return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_in, run_of<RG>(run_in, c), plant_of<RG>(run_in, P_in, c),
+                                                       c, writer, gains, ywin, summ, traj, stage, srcP, srcH, kw);
 }
 
 template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
-__device__ __forceinline__ void sim_candidate(const Run& run, const Plant& P, int64_t c, bool writer,
-                                              const float* __restrict__ gains, float* __restrict__ ywin,
+__device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run, const Plant& P, int64_t c,
+                                              bool writer, const float* __restrict__ gains, float* __restrict__ ywin,
                                               SimSummary* __restrict__ summ, float* __restrict__ traj, Stage& stage,
                                               SrcP& srcP, SrcH& srcH, KW& kw) {
     constexpr bool KAL = KMODE != SIM_LUENBERGER;
     constexpr bool SHARED = KMODE == SIM_KALMAN_SHARED;
     const int tid = threadIdx.x;
-    const typename Chains::template Local<NDC> Lc(run, P, c);
+    const typename Chains::template Local<NDC> Lc(launch, P, c);
 
     const int ns = run.ns;
     const float* row = gains + c * run.cuda_w;
@@ -531,24 +568,24 @@ __device__ __forceinline__ void sim_candidate(const Run& run, const Plant& P, in
             // observer output error
             float yh = 0.0f;
 #pragma unroll
-            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_hi[i], yh);
+            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(Lc.sc(i), xh_hi[i], yh);
             if (NSC < MAXS) yh = __fadd_rn(yh, padS);
 #pragma unroll
-            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(P.ss_c[i], xh_lo[i], yh);
+            for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(Lc.sc(i), xh_lo[i], yh);
             if (NSC < MAXS) yh = __fadd_rn(yh, padS);
-            yh = __fmaf_rn(P.ss_d, u, yh);
+            yh = __fmaf_rn(Lc.sd(), u, yh);
             const float yerr = __fsub_rn(y, yh);
 
             // observer increment (A-I)xh + B u + L yerr, then double-float add
             float dh[NSC], dl[NSC];
 #pragma unroll
             for (int i = 0; i < NSC; ++i) {
-                float h = __fmaf_rn(L[i], yerr, __fmul_rn(P.ss_b[i], u));
+                float h = __fmaf_rn(L[i], yerr, __fmul_rn(Lc.sb(i), u));
                 float l = 0.0f;
 #pragma unroll
-                for (int j = 0; j < NSC; ++j) h = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_hi[j], h);
+                for (int j = 0; j < NSC; ++j) h = __fmaf_rn(Lc.sai(i, j), xh_hi[j], h);
 #pragma unroll
-                for (int j = 0; j < NSC; ++j) l = __fmaf_rn(P.ss_ai[i * MAXS + j], xh_lo[j], l);
+                for (int j = 0; j < NSC; ++j) l = __fmaf_rn(Lc.sai(i, j), xh_lo[j], l);
                 if (NSC < MAXS) {
                     h = __fadd_rn(h, padS);
                     l = __fadd_rn(l, padS);
@@ -628,6 +665,66 @@ struct TableChains {
                                               float (&W)[MAXW]) {
 #pragma unroll
         for (int k = 0; k < MAXW; ++k) W[k] = run_chain_sm<float, MAX_NL, false>(P.nl[k], P.n_nl[k], sp, SIM_BLOCK, 0.0f);
+    }
+};
+
+// A ragged batch: each candidate's own instruction program, read from its
+// column of the per-candidate table (the interpreter of run_chain_sm, with the
+// instruction fields unpacked from the table words).
+template <bool HAS_SEED, int MAXC>
+__device__ __forceinline__ float run_chain_tab(const float* t, int s, int slot0, int n, const float* src,
+                                               float seed) {
+    float result = 0.0f;
+#pragma unroll
+    for (int r = 0; r < MAXC; ++r) {
+        if (r >= n) break;
+        const int f = RT_INS + 3 * (slot0 + r);
+        const unsigned code = __float_as_uint(t[f * s]);
+        const int op = (int)(code & 0xFFu), col = (int)((code >> 8) & 0xFFu);
+        const int ak = (int)((code >> 16) & 0xFFu), bk = (int)(code >> 24);
+        const float pos = src[col * SIM_BLOCK];
+        float prev;
+        if (r == 0) prev = (HAS_SEED && !isnan(seed)) ? seed : pos;
+        else prev = result;
+        const float a = ak == CE_OPERAND_CONST ? t[(f + 1) * s] : (ak == CE_OPERAND_STATE ? pos : prev);
+        const float b = bk == CE_OPERAND_CONST ? t[(f + 2) * s] : (bk == CE_OPERAND_STATE ? pos : prev);
+        switch (op) {
+            case 1: result = radd(a, b); break;
+            case 2: result = rsub(a, b); break;
+            case 3: result = rmul(a, b); break;
+            case 4: result = rdiv(a, b); break;
+            case 5: result = fmin(fmax(prev, a), b); break;
+            case 6: result = (float)((0.0f < a) - (a < 0.0f)); break;
+            default: break;
+        }
+    }
+    return result;
+}
+
+struct RagChains {
+    static constexpr bool kSmem = true;
+    template <int NDC>
+    using Local = RagLocal<NDC>;
+    template <int NDC>
+    __device__ static __forceinline__ float dc(const Plant&, const RagLocal<NDC>& L, const float (&)[NDC],
+                                               const float* sp) {
+        const unsigned cnt = __float_as_uint(L.f(RT_CNT));
+        return run_chain_tab<false, MAX_DC>(L.t, L.s, 0, (int)(cnt & 0xFFu), sp, 0.0f);
+    }
+    template <int NSC, int NDC>
+    __device__ static __forceinline__ float u(const Plant&, const RagLocal<NDC>& L, const float (&)[NSC],
+                                              const float* sh, float seed) {
+        const unsigned cnt = __float_as_uint(L.f(RT_CNT));
+        return run_chain_tab<true, MAX_U>(L.t, L.s, MAX_DC, (int)((cnt >> 8) & 0xFFu), sh, seed);
+    }
+    template <int NDC>
+    __device__ static __forceinline__ void nl(const Plant&, const RagLocal<NDC>& L, const float (&)[NDC], float,
+                                              const float* sp, float (&W)[MAXW]) {
+        const unsigned c0 = __float_as_uint(L.f(RT_CNT)), c1 = __float_as_uint(L.f(RT_CNT + 1));
+        const int n[MAXW] = {(int)((c0 >> 16) & 0xFFu), (int)(c0 >> 24), (int)(c1 & 0xFFu), (int)((c1 >> 8) & 0xFFu)};
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k)
+            W[k] = run_chain_tab<false, MAX_NL>(L.t, L.s, MAX_DC + MAX_U + k * MAX_NL, n[k], sp, 0.0f);
     }
 };
 

@@ -197,9 +197,35 @@ class Ragged:
             off += n * w
         return res
 
+    def evaluate_packed(self, n_cand, cuda_mx: np.ndarray, info_in: np.ndarray) -> np.ndarray:
+        """The C ABI's form: n_cand[i] candidates of instance i, the rows packed instance
+        after instance at each instance's widths (flat float32 arrays); returns the INFO rows
+        packed the same way."""
+        counts = [int(k) for k in n_cand]
+        g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1)
+        i = np.ascontiguousarray(info_in, dtype=F32).reshape(-1)
+        if g.size != sum(k * c.cuda_mx_width for k, c in zip(counts, self.configs)) or \
+                i.size != sum(k * c.info_mx_width for k, c in zip(counts, self.configs)):
+            raise ValueError("packed rows do not match the candidate counts")
+        out = np.empty_like(i)
+        nc = (C.c_int64 * len(counts))(*counts)
+        _check(_lib().ce_ragged_evaluate(self._h, nc, _fptr(g) if g.size else None, _fptr(i) if i.size else None,
+                                         _fptr(out) if out.size else None))
+        return out
+
     @property
     def kernel_launches(self) -> int:
         return int(_lib().ce_ragged_kernel_launches(self._h))
+
+    def set_profiling(self, on: bool):
+        _check(_lib().ce_ragged_set_profiling(self._h, 1 if on else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (milliseconds summed, launches)} since profiling was switched on."""
+        ms = (C.c_double * _ffi.NUM_STAGES)()
+        n = (C.c_int64 * _ffi.NUM_STAGES)()
+        _check(_lib().ce_ragged_stage_times(self._h, ms, n))
+        return {name: (ms[i], n[i]) for i, name in enumerate(_ffi.STAGE_NAMES)}
 
     def close(self):
         if self._h:

@@ -376,3 +376,39 @@ def with_kalman(p: Problem, seed: int = 7, r_range=(1e-2, 1.0), q_range=(1e-4, 1
     rq = np.hstack([lg(*r_range, (n, 1)), lg(*q_range, (n, ns))]).astype(F32)
     return dataclasses.replace(p, name=p.name + "_kalman", config_text=p.config_text + "observer = kalman\n",
                                cuda_mx=np.hstack([p.cuda_mx.astype(F32), rq]))
+
+
+def _with_keys(text: str, **kv) -> str:
+    """`text` with the given config keys set (replaced where present, appended otherwise)."""
+    lines, seen = [], set()
+    for line in text.splitlines():
+        key = line.split("=", 1)[0].strip() if "=" in line else None
+        if key in kv:
+            lines.append(f"{key} = {kv[key]}")
+            seen.add(key)
+        else:
+            lines.append(line)
+    lines += [f"{k} = {v}" for k, v in kv.items() if k not in seen]
+    return "\n".join(lines) + "\n"
+
+
+def uneven(n_inst: int = 16384, seed: int = 9, bases: int = 512) -> list:
+    """The uneven-size workload: n_inst instances of one candidate each.  `bases` plants and
+    candidate pools are drawn as in random_shape (dimensions U{2..8}, 0-4 nonlinear terms with
+    1-8 instructions, observer model, plant, LQR and Kalman-predictor gains); each instance takes
+    one of them with its own horizon (log-uniform in [1e3, 2e4] steps), sweep size (U{50..400})
+    and one of the base's candidate gain sets."""
+    rng = np.random.default_rng(seed)
+    per = -(-n_inst // bases)
+    out = []
+    for b in range(bases):
+        base = random_shape(seed * 100003 + b, n=per)
+        for k in range(per):
+            if len(out) == n_inst:
+                break
+            T = int(np.exp(rng.uniform(np.log(1e3), np.log(2e4))))
+            F = int(rng.integers(50, 401))
+            text = _with_keys(base.config_text, time=T, duration=T * 1e-3, freq=F, n_cores=128)
+            out.append(Problem(f"uneven_{len(out)}", text, base.plant, base.cuda_mx[k:k + 1].copy(),
+                               base.info_mx[k:k + 1].copy()))
+    return out

@@ -241,6 +241,9 @@ CE_EXPORT int ce_ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const floa
                                  float* info_out);
 CE_EXPORT void ce_ragged_destroy(ce_ragged* r);
 CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r);
+/* Stage timing of a ragged batch, as ce_session_set_profiling / ce_session_stage_times. */
+CE_EXPORT int ce_ragged_set_profiling(ce_ragged* r, int32_t on);
+CE_EXPORT int ce_ragged_stage_times(ce_ragged* r, double* ms, int64_t* launches);
 
 /* Launch tuning of a session (no counterpart in the reference).  0 fields take
  * the library defaults (2 lanes per matrix, 5 blocks per SM, 2 chunks for

@@ -36,7 +36,7 @@ def test_ragged_equals_own_sessions():
     with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
         l0 = rb.kernel_launches
         outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
-        assert rb.kernel_launches - l0 == 9  # one launch per stage for all instances together
+        assert rb.kernel_launches - l0 == 10  # the candidate table, then one launch per stage for all instances
         again = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
     for c, p, o, o2 in zip(cfgs, probs, outs, again):
         with ce.Session(c, p.plant) as s:
