@@ -499,6 +499,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch settings")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="Poisson serving run (0: skip)")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
     ap.add_argument("--ref-gpu-build", type=int, default=1,
@@ -543,7 +544,10 @@ def main():
         sess.evaluate_device(n, g.data_ptr(), info_in.data_ptr(), info_out.data_ptr(), stream=stream.cuda_stream)
 
     # the session autotuner picks the launch settings on this batch (untimed; results do not depend on them)
-    tuning = sess.autotune(n, g.data_ptr(), info_in.data_ptr(), info_out.data_ptr(), stream=stream.cuda_stream)
+    if a.no_autotune:
+        tuning = sess.tuning
+    else:
+        tuning = sess.autotune(n, g.data_ptr(), info_in.data_ptr(), info_out.data_ptr(), stream=stream.cuda_stream)
     # eigenvalues of every candidate (untimed): the fit's work depends on the mode count
     _, diag = sess.evaluate_diagnostics(problem.cuda_mx, problem.info_mx, want=("eigen",))
     eig_all = diag["eigen"].reshape(n, cfg.total_dim, 2)
