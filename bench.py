@@ -256,7 +256,8 @@ def serving_models(k: int = 16, seed: int = 5):
     return out
 
 
-def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7):
+def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7,
+                  precision: str = "mixed"):
     """Request serving (ce_server_*): requests of U[256, 16384] candidates on a model drawn
     uniformly from `problems`.  Saturation: 48 requests submitted at once, candidates/s until
     all are done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of
@@ -273,7 +274,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
         return k, p.cuda_mx[a:a + m], p.info_mx[a:a + m]
 
     models = [(c, p.plant, 1) for c, p in zip(cfgs, problems)]
-    with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes) as srv:
+    with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes, precision=precision) as srv:
         # warm-up: every lane sizes its scratch for a full batch of every model
         for _ in range(lanes):
             for r in [srv.submit(p.cuda_mx[:max_batch], p.info_mx[:max_batch], model=k)
@@ -307,6 +308,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
     shapes = sorted({(c.statespace_dim, c.discrete_dim, c.time, c.freq) for c in cfgs})
     return {"request_mix": f"U[256, 16384] candidates on one of {len(problems)} plants of the uneven-shape "
                            "workload (dims 2..8, horizons 1e3..1e4, 50..400 sweep points)",
+            "precision": precision,
             "models": [list(x) for x in shapes],
             "lanes": lanes, "max_batch": st["capacity"], "saturation_candidates_per_s": sat,
             "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
@@ -430,6 +432,41 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
                       "device layout, copies and kernels)"}
 
 
+def small_bench(steps: int, warmup: int, cpu: bool):
+    """The small mass-spring case (1,024 candidates, 3-state observer, 2,000 steps, 200 sweep
+    points: the reference's CPU-runnable configuration): candidates/s of the mixed and the FP64
+    form (ce_evaluate_device, inputs resident, CUDA events) and of the oracle port on all host
+    cores (bounded sample)."""
+    import torch
+    import controllerengine_gb300 as ce
+    from controllerengine_gb300 import synth
+    p = synth.mass_spring(1024)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = torch.from_numpy(p.cuda_mx).to(dev)
+    info = torch.from_numpy(p.info_mx).to(dev)
+    out = torch.empty_like(info)
+    st = torch.cuda.current_stream(dev)
+    res = {"workload": "mass_spring: 1024 candidates, 2-state plant + cubic spring, 3-state observer, "
+                       "T = 2000, F = 200"}
+    for prec in ("mixed", "fp64"):
+        with ce.Session(cfg, p.plant, precision=prec) as s_:
+            for _ in range(warmup):
+                s_.evaluate_device(1024, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            for _ in range(steps):
+                s_.evaluate_device(1024, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+        res[prec] = {"candidates_per_s": 1024 / (ms * 1e-3), "ms_per_step": ms}
+    if cpu:
+        res["cpu_baseline"] = cpu_baseline(p, 5.0, os.cpu_count() or 1)
+    return res
+
+
 def _kalman_time(p, n: int, steps: int, warmup: int):
     import torch
     import controllerengine_gb300 as ce
@@ -506,6 +543,7 @@ def main():
                     help="reference arm: also time the reference's own kernels + host stages (0: skip)")
     ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
     ap.add_argument("--uneven-instances", type=int, default=16384, help="uneven-size ragged batch (0: skip)")
+    ap.add_argument("--small-steps", type=int, default=10, help="the small mass-spring case (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -698,12 +736,21 @@ def main():
     }
     if rank == 0 and a.mc_plants > 0:
         line["monte_carlo"] = monte_carlo_bench(a.mc_plants, 2, 1)
+    if rank == 0 and a.small_steps > 0:
+        line["small"] = small_bench(a.small_steps, 3, not a.no_cpu)
     if rank == 0 and a.uneven_instances > 0:
         line["uneven"] = uneven_bench(a.uneven_instances, 3, 2)
     if rank == 0 and a.kalman_candidates > 0:
         line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
     if rank == 0 and a.serve_seconds > 0:
-        line["serving"] = serving_bench(serving_models(), a.serve_seconds)
+        models = serving_models()
+        line["serving"] = serving_bench(models, a.serve_seconds)
+        # the same request stream served by the plain FP64 form (at its own 70% load)
+        line["serving"]["fp64_form"] = {k: v for k, v in serving_bench(models, a.serve_seconds / 2,
+                                                                       precision="fp64").items()
+                                        if k in ("saturation_candidates_per_s", "offered_requests_per_s",
+                                                 "achieved_candidates_per_s", "latency_p50_ms", "latency_p99_ms",
+                                                 "latency_max_ms", "requests")}
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

@@ -94,7 +94,7 @@ class ce_tuning(C.Structure):
 
 class ce_server_options(C.Structure):
     _fields_ = [("max_batch", C.c_int32), ("lanes", C.c_int32), ("hbm_budget_bytes", C.c_int64),
-                ("max_wait_us", C.c_int32)]
+                ("max_wait_us", C.c_int32), ("precision", C.c_int32)]
 
 
 class ce_server_stats(C.Structure):

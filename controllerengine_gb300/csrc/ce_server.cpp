@@ -96,16 +96,17 @@ namespace {
 
 // Device bytes one evaluation needs per candidate (session scratch + the
 // lane's batch buffers), from the sizes the session allocates.
-int64_t bytes_per_candidate(const ce_config& c) {
+int64_t bytes_per_candidate(const ce_config& c, int precision) {
     const int64_t nt = c.total_dim, pitch = ((c.fit_steps + 7) / 8) * 8;
     const int64_t groups = (c.freq + SWEEP_FG - 1) / SWEEP_FG;
+    const int64_t real = precision == CE_PRECISION_FP64 ? 2 : 1;  // 4-byte words per real of the session
     int64_t f = 0;
     f += 2 * (int64_t)c.cuda_mx_width + 2 * (int64_t)c.info_mx_width;  // gains + INFO, session and lane
     f += nt * nt;                                                      // LIN_A
-    f += 2 * nt + pitch + 4;                                           // eigenvalues, fit window, summary
-    f += 4 * nt * nt + 2 * nt;                                         // AtA, Atb
+    f += real * (2 * nt + pitch + 4);                                  // eigenvalues, fit window, summary
+    f += real * (4 * nt * nt + 2 * nt);                                // AtA, Atb
     f += 1 + (MAXT + 1) + 1 + 1;                                       // nominal, fit order, lists
-    f += 2 * (int64_t)c.freq + 2 * groups;                             // sweep scratch
+    f += real * (2 * (int64_t)c.freq + groups) + groups;               // sweep scratch
     return 4 * f;
 }
 
@@ -269,11 +270,13 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     if (opt) o = *opt;
     const int lanes = o.lanes > 0 ? o.lanes : 2;
     if (lanes > 8) fail("ce_server_create: at most 8 lanes, got {}", lanes);
+    if (o.precision != CE_PRECISION_MIXED && o.precision != CE_PRECISION_FP64)
+        fail("ce_server_create: unknown precision {}", o.precision);
     int64_t cap = o.max_batch > 0 ? o.max_batch : 65536;
     // every lane may hold a full batch's scratch for every model
     int64_t per = 0, cw = 0, iw = 0;
     for (int m = 0; m < n_models; ++m) {
-        per += bytes_per_candidate(cfg[m]);
+        per += bytes_per_candidate(cfg[m], o.precision);
         cw = std::max<int64_t>(cw, cfg[m].cuda_mx_width);
         iw = std::max<int64_t>(iw, cfg[m].info_mx_width);
     }
@@ -295,7 +298,8 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     for (Lane& L : s->lanes) {
         L.sess.assign(n_models, nullptr);
         for (int m = 0; m < n_models; ++m)
-            if (ce_session_create(&cfg[m], &plant[m], n_plants[m], &L.sess[m]) != 0)
+            if (ce_session_create(&cfg[m], &plant[m], n_plants[m], &L.sess[m]) != 0 ||
+                ce_session_set_precision(L.sess[m], o.precision) != 0)
                 throw std::runtime_error(ce_last_error());
         CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
         CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));

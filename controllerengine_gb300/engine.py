@@ -403,7 +403,7 @@ class Server:
 
     def __init__(self, config: EngineConfig, plant: PlantFiles, n_plants: int = 1, max_batch: int = 0,
                  lanes: int = 0, hbm_budget_bytes: int = 0, max_wait_us: int = 0,
-                 models: list | None = None):
+                 models: list | None = None, precision: str = "mixed"):
         """One model (config, plant, n_plants), or with `models` a list of such triples
         (ce_server_create_models); requests then name their model in `submit`."""
         models = models or [(config, plant, n_plants)]
@@ -411,7 +411,8 @@ class Server:
         self.config = self.configs[0]
         self._plants = [m[1] for m in models]  # keeps the arrays alive for the call
         self._h = C.c_void_p()
-        opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us)
+        prec = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64}[precision]
+        opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us, prec)
         k = len(models)
         cfgs = (_ffi.ce_config * k)(*[m[0].raw for m in models])
         pls = (_ffi.ce_plant * k)(*[m[1].ce_plant() for m in models])

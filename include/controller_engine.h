@@ -339,6 +339,7 @@ typedef struct ce_server_options {
     int32_t lanes;            /* concurrent batches (0: 2, at most 8) */
     int64_t hbm_budget_bytes; /* device memory for all lanes (0: no limit); capacity shrinks to fit */
     int32_t max_wait_us;      /* a partial batch waits up to this long for more requests (0: none) */
+    int32_t precision;        /* CE_PRECISION_MIXED (0, the default) or CE_PRECISION_FP64 for every lane */
 } ce_server_options;
 
 typedef struct ce_server_stats {

@@ -139,3 +139,16 @@ def test_several_models(mass_spring):
             ref = ref_a if m == 0 else ref_b
             rows = 256 if m == 0 else 100
             assert np.array_equal(_bits(r.wait()), _bits(ref[a0:a0 + rows]))
+
+
+def test_fp64_server_equals_fp64_session(mass_spring):
+    """Every lane of a server created with the FP64 form runs it; rows equal an FP64 session's."""
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, precision="fp64") as s:
+        ref = s.evaluate(p.cuda_mx, p.info_mx)
+    mixed = _alone(p)
+    with ce.Server(cfg, p.plant, max_batch=700, lanes=2, precision="fp64") as srv:
+        got = np.vstack([srv.submit(p.cuda_mx[a:a + 512], p.info_mx[a:a + 512]).wait() for a in range(0, 1536, 512)])
+    assert np.array_equal(_bits(got), _bits(ref))
+    assert not np.array_equal(_bits(got), _bits(mixed))

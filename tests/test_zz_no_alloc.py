@@ -27,9 +27,12 @@ def _noalloc(lib, sess, n, g, eig, ata, atb, info, stream):
     assert rc == 0, _ffi.last_error(lib)
 
 
-def test_noalloc_matches_session_pipeline_twice(lib):
+@pytest.mark.parametrize("observer", ["luenberger", "kalman"])
+def test_noalloc_matches_session_pipeline_twice(lib, observer):
     import torch
     p = synth.mass_spring(1536)
+    if observer == "kalman":
+        p = synth.with_kalman(p, seed=5)
     cfg = ce.EngineConfig.parse(p.config_text)
     nt = cfg.total_dim
     fr, s0 = cfg.info_freqresp, cfg.info_scoring
