@@ -19,6 +19,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 CUBIN = HERE / "_ref" / "ref_kernels.cubin"
+# the same build with the approximate __fdividef read as the correctly rounded quotient (oracle/Makefile)
+CUBIN_RN = HERE / "_ref" / "ref_kernels_rn.cubin"
 RUNNER = HERE / "_build" / "libref_runner.so"
 F32, I32 = np.float32, np.int32
 
@@ -121,9 +123,10 @@ def run(cfg, plant, cuda_mx: np.ndarray, eigen: np.ndarray, info_in: np.ndarray,
     return y, lina, ata, atb, out
 
 
-def run_kalman(cfg, plant, rows: np.ndarray):
+def run_kalman(cfg, plant, rows: np.ndarray, rounded_reciprocal: bool = False):
     """The reference's discrete_solve<Kalman> on rows of its own layout [K(ns), N, R, Q(ns)]
-    (2ns+2 floats, given to the kernel as ENGINE.cuda_mx_width).  Returns yplant."""
+    (2ns+2 floats, given to the kernel as ENGINE.cuda_mx_width).  Returns yplant.  With
+    rounded_reciprocal, from the build whose __fdividef is the correctly rounded quotient."""
     rows = np.ascontiguousarray(rows, F32)
     n, w = rows.shape
     assert w == 2 * cfg.statespace_dim + 2
@@ -131,7 +134,8 @@ def run_kalman(cfg, plant, rows: np.ndarray):
     L = _runner()
     tab_ptrs = (C.POINTER(C.c_float) * 11)(*[_fp(t) for t in tabs])
     y = np.empty((n, cfg.time), F32)
-    rc = L.ref_run_kalman(str(CUBIN).encode(), engine, len(engine), tab_ptrs, dc, u, nl, n, cfg.time, w, _fp(rows),
+    cubin = CUBIN_RN if rounded_reciprocal else CUBIN
+    rc = L.ref_run_kalman(str(cubin).encode(), engine, len(engine), tab_ptrs, dc, u, nl, n, cfg.time, w, _fp(rows),
                           _fp(ref), _fp(y))
     if rc:
         raise RuntimeError(L.ref_runner_error().decode())

@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -30,8 +31,14 @@ std::string g_err;
         }                                                                       \
     } while (0)
 
-CUmodule g_mod = nullptr;
+// one loaded module per cubin path (the plain build and the one with the correctly rounded reciprocal)
+struct Module {
+    CUmodule mod = nullptr;
+    CUfunction sim = nullptr, setup = nullptr, modal = nullptr, kalman = nullptr;
+};
+std::map<std::string, Module> g_mods;
 CUcontext g_ctx = nullptr;
+CUmodule g_mod = nullptr;
 CUfunction g_sim = nullptr, g_setup = nullptr, g_modal = nullptr, g_kalman = nullptr;
 
 int set_global(const char* name, const void* src, size_t bytes) {
@@ -48,11 +55,22 @@ int set_global(const char* name, const void* src, size_t bytes) {
 }
 
 int load(const char* cubin) {
-    if (g_mod) return 0;
-    CK(cuInit(0));
-    CUdevice dev;
-    CK(cuDeviceGet(&dev, 0));
-    CK(cuDevicePrimaryCtxRetain(&g_ctx, dev));
+    auto it = g_mods.find(cubin);
+    if (it != g_mods.end()) {
+        g_mod = it->second.mod;
+        g_sim = it->second.sim;
+        g_setup = it->second.setup;
+        g_modal = it->second.modal;
+        g_kalman = it->second.kalman;
+        return 0;
+    }
+    g_sim = g_setup = g_modal = g_kalman = nullptr;
+    if (!g_ctx) {
+        CK(cuInit(0));
+        CUdevice dev;
+        CK(cuDeviceGet(&dev, 0));
+        CK(cuDevicePrimaryCtxRetain(&g_ctx, dev));
+    }
     CK(cuCtxSetCurrent(g_ctx));
     CK(cuModuleLoad(&g_mod, cubin));
     unsigned int count = 0;
@@ -73,6 +91,7 @@ int load(const char* cubin) {
         g_err = "kernels not found in " + std::string(cubin);
         return 1;
     }
+    g_mods[cubin] = Module{g_mod, g_sim, g_setup, g_modal, g_kalman};
     return 0;
 }
 

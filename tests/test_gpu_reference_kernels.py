@@ -57,8 +57,9 @@ def test_oracle_kalman_against_reference_kalman_kernel(refk, oracle_mod):
     layout, and the Joseph product written over its own left factor in source order).  The
     one remaining difference is the reciprocal -- the kernel's approximate __fdividef, the
     oracle's correctly rounded quotient -- so whole trajectories are compared row by row: at
-    least half must be identical, and the rows that blow up must be the same rows.  The
-    engine's form (own storage for the Joseph product) stays finite where the reference's
+    least half must be identical, and the rows that blow up must be the same rows; the same
+    kernel built with __fdividef read as the correctly rounded quotient must match every row.
+    The engine's form (own storage for the Joseph product) stays finite where the reference's
     diverges."""
     from controllerengine_gb300 import synth
     for name, p in (("mass", synth.with_kalman(synth.mass_spring(256), seed=5)),
@@ -77,3 +78,9 @@ def test_oracle_kalman_against_reference_kalman_kernel(refk, oracle_mod):
         assert np.isfinite(orc.sim(p.cuda_mx)).all(), name
         if name == "eight":
             assert blown_ref.mean() > 0.5  # the in-place Joseph product diverges
+        # the reference's kernel with its reciprocal correctly rounded (built beside the plain
+        # one by `make -C oracle ref`): every row identical
+        assert refk.CUBIN_RN.exists()
+        y_rn = refk.run_kalman(cfg, p.plant, lit, rounded_reciprocal=True)
+        assert _eq(y_rn, y_lit), f"{name}: {_bad(y_rn, y_lit)} values differ"
+
