@@ -35,7 +35,7 @@
 // width (NSC = 8).  Two of the reference's defects are fixed: its Joseph
 // product writes over its own left factor while reading it (:160), here it
 // has its own storage; its 1/(C P C^T + R) is the approximate __fdividef
-// (:137), here the correctly rounded quotient.  Rows are [K, L, N, R, Q].
+// (:136), here the correctly rounded quotient.  Rows are [K, L, N, R, Q].
 //
 // Chains policy: Chains::kSmem says whether the chains read their sources from
 // the per-thread shared-memory rows srcP (plant states, y in row MAXD) and srcH

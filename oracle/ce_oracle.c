@@ -275,7 +275,7 @@ static void sim_one(const oc_cfg* c, const oc_der* d, const oc_pp* P, const floa
      reference passes IKHP as both the left factor and the output of ABATf
      (:160), so its rows are overwritten while still being read;
    - 1/(C P C^T + R) is the correctly rounded quotient; the reference calls
-     the approximate __fdividef (:137), whose last bits are not specified.
+     the approximate __fdividef (:136), whose last bits are not specified.
    Everything else -- the 8-wide padded loops, the fma chains in k order from
    0, the rounded (not fused) products -- is the reference's.  `literal` = 1
    instead runs the reference's row layout [K, N, R, Q] and its in-place
