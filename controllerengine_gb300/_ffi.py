@@ -28,7 +28,7 @@ EXPORTED_SYMBOLS = (
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
     "ce_server_create", "ce_server_destroy", "ce_server_submit", "ce_server_wait", "ce_server_get_stats",
     "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
-    "ce_server_submit_model", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
+    "ce_server_submit_model", "ce_server_submit_plants", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
     "ce_ragged_create", "ce_ragged_evaluate", "ce_ragged_destroy", "ce_ragged_kernel_launches",
     "ce_ragged_set_profiling", "ce_ragged_stage_times",
     "RunControllerEngine",
@@ -144,6 +144,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
                                             C.POINTER(ce_server_options), C.POINTER(C.c_void_p)]
     lib.ce_server_submit_model.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.POINTER(C.c_int64)]
+    lib.ce_server_submit_plants.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.POINTER(C.c_int64)]
     lib.ce_session_set_tuning.argtypes = [C.c_void_p, C.POINTER(ce_tuning)]
     lib.ce_session_get_tuning.argtypes = [C.c_void_p, C.POINTER(ce_tuning)]
     lib.ce_session_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -30,6 +30,11 @@ __device__ __forceinline__ const Plant& plant_of(const Run& run, const Plant& P,
     else return P;
 }
 
+// The plant of candidate c in a per-candidate-plant evaluation.
+__device__ __forceinline__ int64_t mc_plant(const McPlants& m, int64_t c) {
+    return m.idx ? (int64_t)m.idx[c] : m.first + c;
+}
+
 // ---- scalar ops in a type-generic, contraction-proof form -------------------
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }

@@ -55,6 +55,7 @@ struct Buffers {
     int* nominal_count = nullptr;
     int* sweep_list = nullptr;
     int* sweep_count = nullptr;
+    int* plant_idx = nullptr;  // per candidate: its plant (indexed per-candidate-plant evaluations)
     SweepScratch sweep{};
     KalGroups kal{};  // Kalman observer: candidate grouping by noise weights
     float* traj = nullptr;
@@ -63,11 +64,12 @@ struct Buffers {
         for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
                         (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count,
                         (void*)sweep_list, (void*)sweep_count, sweep.mag, sweep.arg, sweep.bpc, (void*)sweep.fail,
-                        (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order})
+                        (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order, (void*)plant_idx})
             if (p) cudaFree(p);
         gains = info = lina = traj = nullptr;
         eig = ywin = summ = ata = atb = nullptr;
         nominal = fit_counts = fit_order = nominal_list = nominal_count = sweep_list = sweep_count = nullptr;
+        plant_idx = nullptr;
         sweep = SweepScratch{};
         kal = KalGroups{};
         cap = traj_cap = 0;
@@ -201,6 +203,7 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         dev_alloc(b.nominal_count, (size_t)3 * MAX_CHUNKS);
         dev_alloc(b.sweep_list, (size_t)cap);
         dev_alloc(b.sweep_count, (size_t)MAX_CHUNKS);
+        dev_alloc(b.plant_idx, (size_t)cap);
         // shared by the chunks, which the sweep processes one after the other
         const size_t groups = (size_t)(c.freq + SWEEP_FG - 1) / SWEEP_FG;
         CE_CUDA(cudaMalloc(&b.sweep.mag, (size_t)cap * c.freq * rsz + 16));
@@ -342,9 +345,12 @@ int n_chunks(const ce_session* s, int64_t n) {
 // One evaluation: gains and info rows already on the device in d_gains / d_info.
 // With per_candidate, candidate c uses plant `plant + c` (its values from the
 // plant table; the instruction structure and the observer model are shared).
+// With plant_idx (device, per_candidate only), candidate c uses plant plant_idx[c]
+// instead of plant + c; the caller has checked those plants.
 void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, float* d_info, cudaStream_t st,
-                  bool traj, bool per_candidate = false, const Ragged* ragged = nullptr) {
-    const int64_t np_used = per_candidate ? n : 1;
+                  bool traj, bool per_candidate = false, const Ragged* ragged = nullptr,
+                  const int* plant_idx = nullptr) {
+    const int64_t np_used = plant_idx ? 0 : per_candidate ? n : 1;
     for (int64_t q = 0; q < np_used; ++q)
         if (!s->plant_err[plant + q].empty()) throw std::runtime_error(s->plant_err[plant + q]);
     const int prec = s->precision;
@@ -367,6 +373,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         r.mc.grid_stride = s->cfg.serial ? (int64_t)s->cfg.freq * 8 : 0;
         r.mc.alpha = s->d_alpha32;
         r.mc.margin = s->cfg.serial ? 1 : 0;
+        r.mc.idx = plant_idx;
     }
     const Plant& P = s->plants[plant];
     const size_t goff = (size_t)s->grid_of(plant) * s->cfg.freq * 8;
@@ -401,7 +408,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         off = k * per;
         rc = r;
         rc.n = std::min<int64_t>(per, n - off);
-        rc.mc.first = r.mc.first + off;
+        if (r.mc.idx) rc.mc.idx = r.mc.idx + off;
+        else rc.mc.first = r.mc.first + off;
         if (r.rg.inst) rc.rg.inst = r.rg.inst + off;
     };
     auto at = [](const void* p, int64_t off, size_t bytes) {
@@ -1214,6 +1222,27 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
 }  // namespace ce
 
 namespace ce {
+// One plant per candidate, candidate c on plant h_idx[c] (host array, pinned
+// for an asynchronous copy): the serving front end's batches of Monte Carlo
+// requests.  Device rows, the caller's stream.
+void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n, const float* d_cuda_mx,
+                                     const float* d_info_in, float* d_info_out, cudaStream_t st) {
+    check_eval(s, 0, n);
+    if (s->precision != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
+    for (int64_t c = 0; c < n; ++c) {
+        const int p = h_idx[c];
+        if (p < 0 || p >= s->n_plants) fail("plant index {} out of range [0, {})", p, s->n_plants);
+        if (!s->plant_err[p].empty()) throw std::runtime_error(s->plant_err[p]);
+    }
+    if (n == 0) return;
+    ensure_buffers(s, n, false);
+    CE_CUDA(cudaMemcpyAsync(s->buf.plant_idx, h_idx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (d_info_out != d_info_in)
+        CE_CUDA(cudaMemcpyAsync(d_info_out, d_info_in, (size_t)n * s->cfg.info_mx_width * sizeof(float),
+                                cudaMemcpyDeviceToDevice, st));
+    run_pipeline(s, 0, n, d_cuda_mx, d_info_out, st, false, true, nullptr, s->buf.plant_idx);
+}
+
 // Read-only views of a session for other translation units of the library.
 const Plant* session_plant(const ce_session* s, int plant) { return &s->plants[plant]; }
 const ce_config* session_config(const ce_session* s) { return &s->cfg; }

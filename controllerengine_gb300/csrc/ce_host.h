@@ -136,5 +136,7 @@ const ce_config* session_config(const ce_session* s);
 int session_plants(const ce_session* s);
 Run session_run(const ce_session* s, int plant, int64_t n);
 void session_count_launches(ce_session* s, int k);
+void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n, const float* d_cuda_mx,
+                                     const float* d_info_in, float* d_info_out, cudaStream_t st);
 
 }  // namespace ce

@@ -76,6 +76,7 @@ struct McPlants {
     int64_t grid_stride; // elements between consecutive plants' sweep grids (0: one grid for all)
     const void* alpha;   // per sweep grid: the plant scaling (float or double as the precision)
     int margin;          // 1: the margin plant is the candidate's plant (serial mode), 0: the Plant's
+    const int* idx;      // non-null: candidate c uses plant idx[c] (first is then 0)
 };
 
 struct Run;

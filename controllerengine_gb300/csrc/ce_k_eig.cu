@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
                     T(i, j) = (double)v;
                 }
             };
-            if (run.mc.tab) fill(TablePlantValues{run.mc.tab, run.mc.np, run.mc.first + c});
+            if (run.mc.tab) fill(TablePlantValues{run.mc.tab, run.mc.np, mc_plant(run.mc, c)});
             else fill(BankPlantValues{PP});
             Q.sync();
             float* out = eig32 + c * (int64_t)rn.eig_slot;
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
             SMat T{smem + m, n2, eig_stride<EQ>()};
             // margin plant: the Plant's (observer model in batch mode, the round's plant in
             // serial mode), or in serial mode with per-candidate plants the candidate's own
-            const TablePlantValues tv{run.mc.tab, run.mc.np, run.mc.first + c};
+            const TablePlantValues tv{run.mc.tab, run.mc.np, run.mc.tab ? mc_plant(run.mc, c) : 0};
             const bool own = run.mc.tab && run.mc.margin;
             for (int e = Q.q; e < ns * ns; e += EQ) {
                 const int i = e / ns, j = e % ns;

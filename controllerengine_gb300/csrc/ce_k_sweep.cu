@@ -113,9 +113,10 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run_in, co
     }
     // per-candidate plants in serial mode: the candidate's own grid and scaling
     const bool own = run.mc.tab && run.mc.grid_stride;
-    const R ALPHA = own ? ((const R*)run.mc.alpha)[run.mc.first + c]
-                        : (sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64));
-    const R* fgc = fgrid + run.grid_off + (own ? c * run.mc.grid_stride : 0);
+    const int64_t pc = own ? mc_plant(run.mc, c) : 0;  // the candidate's plant
+    const R ALPHA = own ? ((const R*)run.mc.alpha)[pc] : (sizeof(R) == 4 ? R(run.alpha) : R(run.alpha64));
+    // the grid argument is the grid of plant mc.first
+    const R* fgc = fgrid + run.grid_off + (own ? (pc - run.mc.first) * run.mc.grid_stride : 0);
     R bmin = R(1);
     int first_bad = INT_MAX;
     for (int w = w0; w < w1; ++w) {

@@ -41,7 +41,8 @@ using Clock = std::chrono::steady_clock;
 struct Request {
     int64_t id = 0;
     int model = 0;
-    int plant = 0;
+    int plant = 0;        // the plant of every row, or with `plants` the plant of row 0
+    bool plants = false;  // one plant per row: row k on plant `plant + k` (a Monte Carlo request)
     int64_t n = 0;
     const float* gains = nullptr;
     const float* info_in = nullptr;
@@ -66,6 +67,7 @@ struct Lane {
     float* d_info = nullptr;
     float* h_gains = nullptr;  // pinned
     float* h_info = nullptr;   // pinned
+    int* h_idx = nullptr;      // pinned: the plant of each row of a Monte Carlo batch
     bool busy = false;
     std::vector<Piece> pieces;
 };
@@ -77,6 +79,7 @@ struct ce_server {
     std::vector<int> n_plants;   // per model
     int64_t capacity = 0;        // candidates per batch (per lane)
     int max_wait_us = 0;
+    int precision = CE_PRECISION_MIXED;
     std::vector<Lane> lanes;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -146,16 +149,18 @@ void fail_pieces(ce_server* s, Lane& L, const std::string& msg) {
 
 // Take rows for one batch from the queue (caller holds the lock): the oldest
 // request's model and plant, then the queued requests of the same model and
-// plant in arrival order.
+// plant in arrival order.  Monte Carlo requests (a plant per row) batch with
+// the other Monte Carlo requests of their model, whatever their plants
+// (plant = -1 for such a batch).
 std::vector<Piece> form_batch(ce_server* s, int& model, int& plant) {
     std::vector<Piece> out;
     if (s->queue.empty()) return out;
     model = s->queue.front()->model;
-    plant = s->queue.front()->plant;
+    plant = s->queue.front()->plants ? -1 : s->queue.front()->plant;
     int64_t room = s->capacity, off = 0;
     for (auto it = s->queue.begin(); it != s->queue.end() && room > 0;) {
         Request& r = **it;
-        if (r.model != model || r.plant != plant) {
+        if (r.model != model || (r.plants ? -1 : r.plant) != plant) {
             ++it;
             continue;
         }
@@ -180,8 +185,13 @@ void dispatch(ce_server* s, Lane& L, int model, int plant) {
     }
     CE_CUDA(cudaMemcpyAsync(L.d_gains, L.h_gains, (size_t)n * cw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
     CE_CUDA(cudaMemcpyAsync(L.d_info, L.h_info, (size_t)n * iw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
-    if (ce_evaluate_device(L.sess[model], plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0)
+    if (plant < 0) {
+        for (const Piece& p : L.pieces)
+            for (int64_t k = 0; k < p.rows; ++k) L.h_idx[p.off + k] = p.req->plant + (int)(p.row0 + k);
+        session_evaluate_plants_indexed(L.sess[model], L.h_idx, n, L.d_gains, L.d_info, L.d_info, L.stream);
+    } else if (ce_evaluate_device(L.sess[model], plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0) {
         throw std::runtime_error(ce_last_error());
+    }
     CE_CUDA(cudaMemcpyAsync(L.h_info, L.d_info, (size_t)n * iw * sizeof(float), cudaMemcpyDeviceToHost, L.stream));
     CE_CUDA(cudaEventRecord(L.done, L.stream));
     std::lock_guard<std::mutex> g(s->mu);
@@ -258,6 +268,7 @@ void destroy_server(ce_server* s) {
         if (L.d_info) cudaFree(L.d_info);
         if (L.h_gains) cudaFreeHost(L.h_gains);
         if (L.h_info) cudaFreeHost(L.h_info);
+        if (L.h_idx) cudaFreeHost(L.h_idx);
     }
     delete s;
 }
@@ -292,6 +303,7 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     s->n_plants.assign(n_plants, n_plants + n_models);
     s->capacity = cap;
     s->max_wait_us = std::max(0, o.max_wait_us);
+    s->precision = o.precision;
     s->lanes.resize(lanes);
     int device = 0;
     CE_CUDA(cudaGetDevice(&device));
@@ -307,6 +319,7 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
         CE_CUDA(cudaMalloc((void**)&L.d_info, (size_t)cap * iw * sizeof(float)));
         CE_CUDA(cudaHostAlloc((void**)&L.h_gains, (size_t)cap * cw * sizeof(float), cudaHostAllocDefault));
         CE_CUDA(cudaHostAlloc((void**)&L.h_info, (size_t)cap * iw * sizeof(float), cudaHostAllocDefault));
+        CE_CUDA(cudaHostAlloc((void**)&L.h_idx, (size_t)cap * sizeof(int), cudaHostAllocDefault));
     }
     s->worker = std::thread(worker_loop, s.get(), device);
     *out = s.release();
@@ -343,37 +356,67 @@ CE_EXPORT int ce_server_create_models(const ce_config* cfgs, const ce_plant* pla
 
 CE_EXPORT void ce_server_destroy(ce_server* s) { destroy_server(s); }
 
+}  // extern "C"
+
+namespace {
+
+void submit(ce_server* s, int32_t model, int32_t plant_index, bool plants, int64_t n, const float* cuda_mx,
+            const float* info_in, float* info_out, int64_t* request_id) {
+    if (!s || !request_id) fail("ce_server_submit: null argument");
+    if (model < 0 || model >= (int)s->cfg.size()) fail("model {} out of range [0, {})", model, s->cfg.size());
+    if (plant_index < 0 || plant_index >= s->n_plants[model])
+        fail("plant index {} out of range [0, {})", plant_index, s->n_plants[model]);
+    if (n < 0) fail("candidate count {} is negative", n);
+    if (plants && plant_index + n > s->n_plants[model])
+        fail("plants [{}, {}) exceed the model's {} plants (one plant per candidate)", plant_index, plant_index + n,
+             s->n_plants[model]);
+    if (plants && s->precision != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
+    if (n > 0 && (!cuda_mx || !info_in || !info_out)) fail("ce_server_submit: null buffer");
+    auto r = std::make_shared<Request>();
+    r->model = model;
+    r->plant = plant_index;
+    r->plants = plants;
+    r->n = n;
+    r->gains = cuda_mx;
+    r->info_in = info_in;
+    r->info_out = info_out;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (s->stop) fail("ce_server_submit: server is shutting down");
+        r->id = s->next_id++;
+        s->live.emplace(r->id, r);
+        if (n == 0) {
+            r->done = true;
+            r->t_done = r->t_submit;
+        } else {
+            s->queue.push_back(r);
+        }
+        *request_id = r->id;
+    }
+    s->cv_work.notify_one();
+}
+
+}  // namespace
+
+extern "C" {
+
 CE_EXPORT int ce_server_submit_model(ce_server* s, int32_t model, int32_t plant_index, int64_t n, const float* cuda_mx,
                                      const float* info_in, float* info_out, int64_t* request_id) {
     try {
-        if (!s || !request_id) fail("ce_server_submit: null argument");
-        if (model < 0 || model >= (int)s->cfg.size()) fail("model {} out of range [0, {})", model, s->cfg.size());
-        if (plant_index < 0 || plant_index >= s->n_plants[model])
-            fail("plant index {} out of range [0, {})", plant_index, s->n_plants[model]);
-        if (n < 0) fail("candidate count {} is negative", n);
-        if (n > 0 && (!cuda_mx || !info_in || !info_out)) fail("ce_server_submit: null buffer");
-        auto r = std::make_shared<Request>();
-        r->model = model;
-        r->plant = plant_index;
-        r->n = n;
-        r->gains = cuda_mx;
-        r->info_in = info_in;
-        r->info_out = info_out;
-        r->t_submit = Clock::now();
-        {
-            std::lock_guard<std::mutex> g(s->mu);
-            if (s->stop) fail("ce_server_submit: server is shutting down");
-            r->id = s->next_id++;
-            s->live.emplace(r->id, r);
-            if (n == 0) {
-                r->done = true;
-                r->t_done = r->t_submit;
-            } else {
-                s->queue.push_back(r);
-            }
-            *request_id = r->id;
-        }
-        s->cv_work.notify_one();
+        submit(s, model, plant_index, false, n, cuda_mx, info_in, info_out, request_id);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+CE_EXPORT int ce_server_submit_plants(ce_server* s, int32_t model, int32_t first_plant, int64_t n,
+                                      const float* cuda_mx, const float* info_in, float* info_out,
+                                      int64_t* request_id) {
+    try {
+        submit(s, model, first_plant, true, n, cuda_mx, info_in, info_out, request_id);
         return 0;
     } catch (const std::exception& e) {
         g_last_error = e.what();

@@ -96,7 +96,7 @@ struct McLocal {
     float ai_[NDC * NDC], bu_[NDC], bw_[NDC * MAXW], cst_[2 * MC_SLOTS];
     __device__ __forceinline__ McLocal(const Run& run, const Plant& plant, int64_t c) : P(plant) {
         const float* __restrict__ t = run.mc.tab;
-        const int64_t np = run.mc.np, p = run.mc.first + c;
+        const int64_t np = run.mc.np, p = mc_plant(run.mc, c);
 #pragma unroll
         for (int i = 0; i < NDC; ++i) {
 #pragma unroll

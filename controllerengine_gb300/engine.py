@@ -433,6 +433,21 @@ class Server:
                                              C.byref(rid)))
         return Request(self, rid.value, g, i, out)
 
+    def submit_plants(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, first_plant: int = 0,
+                      model: int = 0) -> Request:
+        """A Monte Carlo request: row k on plant first_plant + k (ce_server_submit_plants)."""
+        c = self.configs[model]
+        g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
+        n = g.shape[0]
+        if info_in is None:
+            info_in = np.zeros((n, c.info_mx_width), F32)
+        i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
+        out = np.empty_like(i)
+        rid = C.c_int64()
+        _check(_lib().ce_server_submit_plants(self._h, model, first_plant, n, _fptr(g), _fptr(i), _fptr(out),
+                                              C.byref(rid)))
+        return Request(self, rid.value, g, i, out)
+
     def stats(self) -> dict:
         st = _ffi.ce_server_stats()
         _check(_lib().ce_server_get_stats(self._h, C.byref(st)))

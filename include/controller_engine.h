@@ -365,6 +365,12 @@ CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, con
                                const float* info_in, float* info_out, int64_t* request_id);
 CE_EXPORT int ce_server_submit_model(ce_server* s, int32_t model, int32_t plant_index, int64_t n,
                                      const float* cuda_mx, const float* info_in, float* info_out, int64_t* request_id);
+/* A Monte Carlo request: row k is evaluated on plant first_plant + k of the model (as
+ * ce_evaluate_plants; mixed precision).  Such requests batch with the model's other Monte
+ * Carlo requests whatever their plants. */
+CE_EXPORT int ce_server_submit_plants(ce_server* s, int32_t model, int32_t first_plant, int64_t n,
+                                      const float* cuda_mx, const float* info_in, float* info_out,
+                                      int64_t* request_id);
 /* 0: done (info_out filled); CE_PENDING: timeout (timeout_ms < 0 waits forever); 1: error. */
 CE_EXPORT int ce_server_wait(ce_server* s, int64_t request_id, int32_t timeout_ms);
 CE_EXPORT int ce_server_get_stats(ce_server* s, ce_server_stats* out);

@@ -152,3 +152,31 @@ def test_fp64_server_equals_fp64_session(mass_spring):
         got = np.vstack([srv.submit(p.cuda_mx[a:a + 512], p.info_mx[a:a + 512]).wait() for a in range(0, 1536, 512)])
     assert np.array_equal(_bits(got), _bits(ref))
     assert not np.array_equal(_bits(got), _bits(mixed))
+
+
+def test_monte_carlo_requests_batch_with_each_other():
+    """Monte Carlo requests (row k on plant first + k) of assorted plant ranges are packed into
+    the same batches, between ordinary requests on one plant; every row equals ce_evaluate_plants
+    (or ce_evaluate for the ordinary ones)."""
+    from controllerengine_gb300 import synth
+    p = synth.monte_carlo(n_plants=600, time=900, freq=50, serial=True)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, n_plants=600) as s:
+        ref_mc = s.evaluate_plants(p.cuda_mx, p.info_mx)
+        ref_one = s.evaluate(p.cuda_mx[:90], p.info_mx[:90], plant_index=7)
+    ranges = [(0, 120), (300, 450), (120, 125), (500, 600), (125, 300)]
+    with ce.Server(cfg, p.plant, n_plants=600, max_batch=256, lanes=2) as srv:
+        reqs = []
+        for k, (a, b) in enumerate(ranges):
+            reqs.append(("mc", a, b, srv.submit_plants(p.cuda_mx[a:b], p.info_mx[a:b], first_plant=a)))
+            if k % 2 == 0:
+                reqs.append(("one", 0, 90, srv.submit(p.cuda_mx[:90], p.info_mx[:90], plant_index=7)))
+        for kind, a, b, r in reqs:
+            out = r.wait()
+            ref = ref_mc[a:b] if kind == "mc" else ref_one
+            assert np.array_equal(_bits(out), _bits(ref)), (kind, a, b)
+        st = srv.stats()
+    assert st["batches"] < len(reqs)  # Monte Carlo requests of different plant ranges shared batches
+    with ce.Server(cfg, p.plant, n_plants=600, max_batch=256, lanes=1) as srv:
+        with pytest.raises(ce.ControllerEngineError, match="exceed the model"):
+            srv.submit_plants(p.cuda_mx[:10], p.info_mx[:10], first_plant=595)
