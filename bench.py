@@ -257,62 +257,108 @@ def serving_models(k: int = 16, seed: int = 5):
 
 
 def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7,
-                  precision: str = "mixed"):
-    """Request serving (ce_server_*): requests of U[256, 16384] candidates on a model drawn
-    uniformly from `problems`.  Saturation: 48 requests submitted at once, candidates/s until
-    all are done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of
-    submit -> results in the caller's buffer (measured by the server)."""
+                  precision: str = "mixed", n_plants: int = 16384, mc_fraction: float = 0.25):
+    """Request serving (ce_server_*): every model of `problems` holds n_plants perturbed copies
+    of its plant (synth.perturbed_plants); a request carries U[256, 16384] candidates on a model
+    drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
+    many consecutive plants, ce_server_submit_plants), else a tuning request (distinct gain
+    sets on one plant).  Saturation: 48 requests submitted at once, candidates/s until all are
+    done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of submit ->
+    results in the caller's buffer (measured by the server)."""
     import controllerengine_gb300 as ce
+    from controllerengine_gb300 import synth
     rng = np.random.default_rng(seed)
     cfgs = [ce.EngineConfig.parse(p.config_text) for p in problems]
+    plant_sets = [synth.perturbed_plants(p.plant, n_plants, 200 + k) for k, p in enumerate(problems)]
+    mc_rows = [(np.repeat(p.cuda_mx[:1], 16384, axis=0), np.repeat(p.info_mx[:1], 16384, axis=0)) for p in problems]
 
     def draw():
         k = int(rng.integers(0, len(problems)))
         p = problems[k]
         m = int(rng.integers(256, 16385))
+        if rng.random() < mc_fraction:
+            first = int(rng.integers(0, n_plants - m + 1))
+            return k, True, first, mc_rows[k][0][:m], mc_rows[k][1][:m]
         a = int(rng.integers(0, p.cuda_mx.shape[0] - m + 1))
-        return k, p.cuda_mx[a:a + m], p.info_mx[a:a + m]
+        return k, False, int(rng.integers(0, n_plants)), p.cuda_mx[a:a + m], p.info_mx[a:a + m]
 
-    models = [(c, p.plant, 1) for c, p in zip(cfgs, problems)]
+    def submit(srv, req):
+        k, mc, plant, g, i = req
+        if mc:
+            return srv.submit_plants(g, i, first_plant=plant, model=k)
+        return srv.submit(g, i, plant_index=plant, model=k)
+
+    def draw_submit(srv):
+        # a request naming a plant whose sweep grid failed is refused at submit: draw again
+        for _ in range(100):
+            req = draw()
+            try:
+                return req, submit(srv, req)
+            except ce.ControllerEngineError:
+                refused[0] += 1
+        raise RuntimeError("no servable request in 100 draws")
+
+    refused = [0]
+    models = [(c, ps, n_plants) for c, ps in zip(cfgs, plant_sets)]
     with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes, precision=precision) as srv:
-        # warm-up: every lane sizes its scratch for a full batch of every model
+        # warm-up: every lane sizes its scratch for a full batch of every model, and compiles
+        # the per-candidate-plant kernels of every model
         for _ in range(lanes):
-            for r in [srv.submit(p.cuda_mx[:max_batch], p.info_mx[:max_batch], model=k)
-                      for k, p in enumerate(problems)]:
-                r.wait()
+            hs = []
+            for k, p in enumerate(problems):
+                hs.append(srv.submit(p.cuda_mx[:max_batch], p.info_mx[:max_batch], model=k))
+                for first in (0, n_plants // 2):
+                    try:
+                        hs.append(srv.submit_plants(mc_rows[k][0][:4096], mc_rows[k][1][:4096], first_plant=first,
+                                                    model=k))
+                    except ce.ControllerEngineError:
+                        pass
+            for h in hs:
+                h.wait()
+        refused[0] = 0
         reqs = [draw() for _ in range(48)]
-        total = sum(g.shape[0] for _, g, _ in reqs)
+        total = sum(r[3].shape[0] for r in reqs)
         t0 = time.perf_counter()
-        hs = [srv.submit(g, i, model=k) for k, g, i in reqs]
+        hs = []
+        for r in reqs:
+            try:
+                hs.append(submit(srv, r))
+            except ce.ControllerEngineError:
+                total -= r[3].shape[0]
+                refused[0] += 1
         for h in hs:
             h.wait()
         sat = total / (time.perf_counter() - t0)
         mean_size = (256 + 16384) / 2
         rate = 0.7 * sat / mean_size  # requests/s
         srv.reset_stats()
-        hs, offered = [], 0
+        hs, offered, n_mc = [], 0, 0
         t0 = time.perf_counter()
         t_next = t0
         while t_next - t0 < seconds:
             now = time.perf_counter()
             if now < t_next:
                 time.sleep(t_next - now)
-            k, g, i = draw()
-            offered += g.shape[0]
-            hs.append(srv.submit(g, i, model=k))
+            req, h = draw_submit(srv)
+            offered += req[3].shape[0]
+            n_mc += req[1]
+            hs.append(h)
             t_next += rng.exponential(1.0 / rate)
         for h in hs:
             h.wait()
         wall = time.perf_counter() - t0
         st = srv.stats()
     shapes = sorted({(c.statespace_dim, c.discrete_dim, c.time, c.freq) for c in cfgs})
-    return {"request_mix": f"U[256, 16384] candidates on one of {len(problems)} plants of the uneven-shape "
-                           "workload (dims 2..8, horizons 1e3..1e4, 50..400 sweep points)",
+    return {"request_mix": f"U[256, 16384] candidates on one of {len(problems)} models of the uneven-shape "
+                           f"workload (dims 2..8, horizons 1e3..1e4, 50..400 sweep points), each with {n_plants} "
+                           f"perturbed plants; {mc_fraction:.0%} Monte Carlo requests (one gain set on as many "
+                           "consecutive plants), the rest tuning requests (distinct gain sets on one plant)",
             "precision": precision,
             "models": [list(x) for x in shapes],
             "lanes": lanes, "max_batch": st["capacity"], "saturation_candidates_per_s": sat,
             "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
-            "requests": st["completed"], "achieved_candidates_per_s": offered / wall,
+            "requests": st["completed"], "monte_carlo_requests": n_mc, "refused_requests": refused[0],
+            "achieved_candidates_per_s": offered / wall,
             "batches": st["batches"], "mean_batch": st["batched_candidates"] / max(1, st["batches"]),
             "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
             "latency_max_ms": st["latency_max_ms"]}
@@ -750,7 +796,7 @@ def main():
                                                                        precision="fp64").items()
                                         if k in ("saturation_candidates_per_s", "offered_requests_per_s",
                                                  "achieved_candidates_per_s", "latency_p50_ms", "latency_p99_ms",
-                                                 "latency_max_ms", "requests")}
+                                                 "latency_max_ms", "requests", "monte_carlo_requests")}
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

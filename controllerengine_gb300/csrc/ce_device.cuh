@@ -72,9 +72,12 @@ __device__ __forceinline__ void df_add(float& HI, float& LO, float hi, float lo)
 // source values addressed by the instruction column; column `ycol` (if >= 0)
 // addresses `yval` instead (the NL chains' plant-output slot).  The first
 // instruction's running value is the seed when HAS_SEED and the seed is not NaN,
-// else the state under its column; later ones use the running result.
-template <typename R, int NSRC, int MAXC, bool HAS_SEED>
-__device__ __forceinline__ R run_chain(const Instr* __restrict__ ins, int n, const R* src, int ycol, R yval, R seed) {
+// else the state under its column; later ones use the running result.  With
+// TAB the constant operands come from a per-candidate table instead of the
+// instructions: instruction r's (a, b) at cst[2 r * cs] and cst[(2 r + 1) * cs].
+template <typename R, int NSRC, int MAXC, bool HAS_SEED, bool TAB = false>
+__device__ __forceinline__ R run_chain(const Instr* __restrict__ ins, int n, const R* src, int ycol, R yval, R seed,
+                                       const float* __restrict__ cst = nullptr, int64_t cs = 0) {
     R result = R(0);
 #pragma unroll
     for (int r = 0; r < MAXC; ++r) {
@@ -88,8 +91,10 @@ __device__ __forceinline__ R run_chain(const Instr* __restrict__ ins, int n, con
         R prev;
         if (r == 0) prev = (HAS_SEED && !isnan(seed)) ? seed : pos;
         else prev = result;
-        const R a = ak == CE_OPERAND_CONST ? R(ins[r].aval) : (ak == CE_OPERAND_STATE ? pos : prev);
-        const R b = bk == CE_OPERAND_CONST ? R(ins[r].bval) : (bk == CE_OPERAND_STATE ? pos : prev);
+        const float av = !TAB ? ins[r].aval : ak == CE_OPERAND_CONST ? cst[2 * r * cs] : 0.0f;
+        const float bv = !TAB ? ins[r].bval : bk == CE_OPERAND_CONST ? cst[(2 * r + 1) * cs] : 0.0f;
+        const R a = ak == CE_OPERAND_CONST ? R(av) : (ak == CE_OPERAND_STATE ? pos : prev);
+        const R b = bk == CE_OPERAND_CONST ? R(bv) : (bk == CE_OPERAND_STATE ? pos : prev);
         switch (op) {
             case 1: result = radd(a, b); break;
             case 2: result = rsub(a, b); break;

@@ -289,10 +289,11 @@ Run make_run(const ce_session* s, int plant, int64_t n) {
 
 void build_grids(ce_session* s, int precision);
 
-// The per-candidate plant table (MC_FIELDS x n_plants, field-major) and the
-// simulation kernel compiled for it, built on first use.
-void ensure_plant_table(ce_session* s) {
-    if (!s->sim_kernel_mc) {
+// The per-candidate plant table (MC_FIELDS x n_plants, field-major) and, for
+// the mixed-precision form, the simulation kernel compiled for it, built on
+// first use.
+void ensure_plant_table(ce_session* s, int precision) {
+    if (precision == CE_PRECISION_MIXED && !s->sim_kernel_mc) {
         std::string log;
         s->sim_kernel_mc = specialise_sim(s->plants[0], s->cfg.statespace_dim <= 4 ? 4 : 8,
                                           s->cfg.discrete_dim <= 4 ? 4 : 8, log, true,
@@ -355,10 +356,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         if (!s->plant_err[plant + q].empty()) throw std::runtime_error(s->plant_err[plant + q]);
     const int prec = s->precision;
     if (prec == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
-    if (per_candidate) {
-        if (prec != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
-        ensure_plant_table(s);
-    }
+    if (per_candidate) ensure_plant_table(s, prec);
     ensure_buffers(s, n, traj);
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
@@ -371,14 +369,16 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         r.mc.np = s->n_plants;
         r.mc.first = plant;
         r.mc.grid_stride = s->cfg.serial ? (int64_t)s->cfg.freq * 8 : 0;
-        r.mc.alpha = s->d_alpha32;
+        r.mc.alpha = prec == CE_PRECISION_FP64 ? (const void*)s->d_alpha64 : (const void*)s->d_alpha32;
         r.mc.margin = s->cfg.serial ? 1 : 0;
         r.mc.idx = plant_idx;
     }
     const Plant& P = s->plants[plant];
     const size_t goff = (size_t)s->grid_of(plant) * s->cfg.freq * 8;
     const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + goff) : (const void*)(s->d_fgrid32 + goff);
-    const size_t gstep = (size_t)(per_candidate ? r.mc.grid_stride : 0) * (prec == CE_PRECISION_FP64 ? 8 : 4);
+    // a chunk's grid argument is the grid of its first plant (mc.first); with
+    // plant indices every chunk keeps plant 0's
+    const size_t gstep = (size_t)(per_candidate && !plant_idx ? r.mc.grid_stride : 0) * (prec == CE_PRECISION_FP64 ? 8 : 4);
     // each launch optionally bracketed by events on the stream it runs on
     auto timed = [&](int stage, cudaStream_t on, auto&& launch) {
         if (!s->profiling) {
@@ -398,7 +398,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // rest of each SM and run alongside.  Large batches are cut into chunks so
     // that the fit of a chunk starts as soon as its eigenvalues are known, while
     // the eigensolves of the next chunks continue.
-    const SimKernels sk = per_candidate ? s->sim_kernel_mc : prec == CE_PRECISION_MIXED ? s->sim_kernel[plant] : SimKernels{};
+    const SimKernels sk = prec != CE_PRECISION_MIXED ? SimKernels{} : per_candidate ? s->sim_kernel_mc : s->sim_kernel[plant];
     cudaStream_t fs = s->fast, ss = s->side;
     const int nch = n_chunks(s, n);
     const int64_t per = (n + nch - 1) / nch;
@@ -1228,7 +1228,6 @@ namespace ce {
 void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n, const float* d_cuda_mx,
                                      const float* d_info_in, float* d_info_out, cudaStream_t st) {
     check_eval(s, 0, n);
-    if (s->precision != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
     for (int64_t c = 0; c < n; ++c) {
         const int p = h_idx[c];
         if (p < 0 || p >= s->n_plants) fail("plant index {} out of range [0, {})", p, s->n_plants);
@@ -1247,6 +1246,19 @@ void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n,
 const Plant* session_plant(const ce_session* s, int plant) { return &s->plants[plant]; }
 const ce_config* session_config(const ce_session* s) { return &s->cfg; }
 int session_plants(const ce_session* s) { return s->n_plants; }
+const std::string& session_plant_error(const ce_session* s, int plant) { return s->plant_err[plant]; }
+
+// Everything an evaluation of up to n candidates would otherwise allocate or
+// build on first use: the scratch buffers, the FP64 sweep grids of an FP64
+// session and, with `plants`, the per-candidate plant table (and its
+// simulation kernel).  A server prepares its sessions at creation so that no
+// batch waits on an allocation.
+void session_prepare(ce_session* s, int64_t n, bool plants) {
+    ensure_buffers(s, std::max<int64_t>(n, 1), false);
+    if (s->precision == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
+    if (plants) ensure_plant_table(s, s->precision);
+    CE_CUDA(cudaDeviceSynchronize());
+}
 Run session_run(const ce_session* s, int plant, int64_t n) { return make_run(s, plant, n); }
 void session_count_launches(ce_session* s, int k) { s->launches += k; }
 }  // namespace ce

@@ -134,6 +134,11 @@ void launch_kalman_groups(const Run& run, const float* gains, const KalGroups& g
 const Plant* session_plant(const ce_session* s, int plant);
 const ce_config* session_config(const ce_session* s);
 int session_plants(const ce_session* s);
+// Empty, or why plant `plant` cannot be evaluated (its sweep grid failed at creation).
+const std::string& session_plant_error(const ce_session* s, int plant);
+// Allocate and build, now, what an evaluation of up to n candidates (with `plants`: on
+// per-candidate plants) would otherwise set up on first use.
+void session_prepare(ce_session* s, int64_t n, bool plants);
 Run session_run(const ce_session* s, int plant, int64_t n);
 void session_count_launches(ce_session* s, int k);
 void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n, const float* d_cuda_mx,

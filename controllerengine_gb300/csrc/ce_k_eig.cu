@@ -765,22 +765,27 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
             const float* row = gains + c * run.cuda_w;
             SMat T{smem + m, nt, eig_stride<EQ>()};
             float* lrow = lina + c * (int64_t)run.lina_slot;
-            for (int e = Q.q; e < nt * nt; e += EQ) {
-                const int i = e / nt, j = e % nt;
-                double v;
-                if (i < ns && j < ns) {
-                    const double Kj = row[j], Li = row[ns + i];
-                    v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj - Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
-                } else if (i < ns) {
-                    v = (double)row[ns + i] * (double)P.d_c[j - ns];
-                } else if (j < ns) {
-                    v = -(double)P.d_bu[i - ns] * (double)row[j];
-                } else {
-                    v = P.d_a[(i - ns) * MAXD + (j - ns)];
+            auto fill = [&](const auto& pv) {
+                for (int e = Q.q; e < nt * nt; e += EQ) {
+                    const int i = e / nt, j = e % nt;
+                    double v;
+                    if (i < ns && j < ns) {
+                        const double Kj = row[j], Li = row[ns + i];
+                        v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj -
+                            Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
+                    } else if (i < ns) {
+                        v = (double)row[ns + i] * (double)pv.c(j - ns);
+                    } else if (j < ns) {
+                        v = -(double)pv.bu(i - ns) * (double)row[j];
+                    } else {
+                        v = pv.a(i - ns, j - ns);
+                    }
+                    lrow[e] = (float)v;
+                    T(i, j) = v;
                 }
-                lrow[e] = (float)v;
-                T(i, j) = v;
-            }
+            };
+            if (run.mc.tab) fill(TablePlantValues{run.mc.tab, run.mc.np, mc_plant(run.mc, c)});
+            else fill(BankPlantValues{P});
             Q.sync();
             double* out = eig64 + c * (int64_t)run.eig_slot;
             double mx = 0.0;

@@ -65,14 +65,58 @@ void launch_ragged_table(int64_t n, const Plant* plants, const int* inst, float*
     CE_CUDA(cudaGetLastError());
 }
 
+// The discrete-plant values and instruction constants the FP64 step reads: the
+// launch's Plant, or with per-candidate plants (MC) the candidate's row of the
+// plant table -- matrices staged once into this thread's column of dynamic
+// shared memory (FIELDS x SIM_BLOCK words), constants read from the table
+// where an instruction uses one.
+template <int NDC, bool MC>
+struct F64Plant {
+    static constexpr int F_BU = NDC * NDC, F_BW = F_BU + NDC, FIELDS = F_BW + NDC * MAXW;
+    const Plant& P;
+    const float* col = nullptr;
+    const float* cst = nullptr;
+    int64_t cs = 0;
+    __device__ __forceinline__ F64Plant(const Run& run, const Plant& plant, int64_t c) : P(plant) {
+        if constexpr (MC) {
+            extern __shared__ float f64_cols[];
+            const float* __restrict__ t = run.mc.tab;
+            const int64_t np = run.mc.np, pc = mc_plant(run.mc, c);
+            float* w = f64_cols + threadIdx.x;
+#pragma unroll
+            for (int i = 0; i < NDC; ++i) {
+#pragma unroll
+                for (int j = 0; j < NDC; ++j) w[(i * NDC + j) * SIM_BLOCK] = t[(int64_t)(MC_AI + i * MAXD + j) * np + pc];
+                w[(F_BU + i) * SIM_BLOCK] = t[(int64_t)(MC_BU + i) * np + pc];
+#pragma unroll
+                for (int k = 0; k < MAXW; ++k)
+                    w[(F_BW + i * MAXW + k) * SIM_BLOCK] = t[(int64_t)(MC_BW + i * MAXW + k) * np + pc];
+            }
+            col = w;
+            cst = t + (int64_t)MC_CST * np + pc;
+            cs = np;
+        }
+    }
+    __device__ __forceinline__ double ai(int i, int j) const {
+        return MC ? (double)col[(i * NDC + j) * SIM_BLOCK] : (double)P.d_ai[i * MAXD + j];
+    }
+    __device__ __forceinline__ double bu(int i) const { return MC ? (double)col[(F_BU + i) * SIM_BLOCK] : (double)P.d_bu[i]; }
+    __device__ __forceinline__ double bw(int i, int k) const {
+        return MC ? (double)col[(F_BW + i * MAXW + k) * SIM_BLOCK] : (double)P.d_bw[i * MAXW + k];
+    }
+    // the constants of the chain whose first instruction is constant slot slot0
+    __device__ __forceinline__ const float* k(int slot0) const { return MC ? cst + (int64_t)2 * slot0 * cs : nullptr; }
+};
+
 // The plain FP64 form of the same recurrence: double state, no hi/lo split.
-template <int NSC, int NDC>
+template <int NSC, int NDC, bool MC = false>
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, double* __restrict__ ywin,
                                                         double* __restrict__ summ) {
     const int tid = threadIdx.x;
     const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
     if (c >= run.n) return;
+    const F64Plant<NDC, MC> pv(run, P, c);
     const int ns = run.ns;
     const float* row = gains + c * run.cuda_w;
     double K[NSC], L[NSC];
@@ -91,7 +135,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __g
     double* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int T = run.time;
     for (int t = 0; t < T; ++t) {
-        const double y = run_chain<double, NDC, MAX_DC, false>(P.dc, P.n_dc, xp, -1, 0.0, 0.0);
+        const double y = run_chain<double, NDC, MAX_DC, false, MC>(P.dc, P.n_dc, xp, -1, 0.0, 0.0, pv.k(0), pv.cs);
         const int w = t - run.fit_start_id;
         if (w >= 0 && w < run.fit_steps) wrow[w] = y;
         if (t >= run.steady_start_id) ysum = __dadd_rn(ysum, y);
@@ -101,7 +145,8 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __g
 #pragma unroll
         for (int i = 0; i < NSC; ++i) kx = __fma_rn(K[i], xh[i], kx);
         const double ref = t < run.ref_step_id ? 0.0 : (double)run.ref_amp;
-        const double u = run_chain<double, NSC, MAX_U, true>(P.u, P.n_u, xh, -1, 0.0, __fma_rn(N, ref, -kx));
+        const double u = run_chain<double, NSC, MAX_U, true, MC>(P.u, P.n_u, xh, -1, 0.0, __fma_rn(N, ref, -kx),
+                                                                  pv.k(MAX_DC), pv.cs);
         double yh = 0.0;
 #pragma unroll
         for (int i = 0; i < NSC; ++i) yh = __fma_rn((double)P.ss_c[i], xh[i], yh);
@@ -119,15 +164,17 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __g
         for (int i = 0; i < NSC; ++i) xh[i] = __dadd_rn(xh[i], dh[i]);
         double W[MAXW];
 #pragma unroll
-        for (int k = 0; k < MAXW; ++k) W[k] = run_chain<double, NDC, MAX_NL, false>(P.nl[k], P.n_nl[k], xp, MAXD, y, 0.0);
+        for (int k = 0; k < MAXW; ++k)
+            W[k] = run_chain<double, NDC, MAX_NL, false, MC>(P.nl[k], P.n_nl[k], xp, MAXD, y, 0.0,
+                                                             pv.k(MAX_DC + MAX_U + k * MAX_NL), pv.cs);
         double ph[NDC];
 #pragma unroll
         for (int i = 0; i < NDC; ++i) {
-            double h = __dmul_rn((double)P.d_bu[i], u);
+            double h = __dmul_rn(pv.bu(i), u);
 #pragma unroll
-            for (int k = 0; k < MAXW; ++k) h = __fma_rn((double)P.d_bw[i * MAXW + k], W[k], h);
+            for (int k = 0; k < MAXW; ++k) h = __fma_rn(pv.bw(i, k), W[k], h);
 #pragma unroll
-            for (int j = 0; j < NDC; ++j) h = __fma_rn((double)P.d_ai[i * MAXD + j], xp[j], h);
+            for (int j = 0; j < NDC; ++j) h = __fma_rn(pv.ai(i, j), xp[j], h);
             ph[i] = h;
         }
 #pragma unroll
@@ -147,6 +194,13 @@ static void sim_launch(const Run& run, const Plant& P, int precision, const floa
     const int grid = sim_grid(run);
     if (precision == CE_PRECISION_FP64) {
         if (KMODE != SIM_LUENBERGER) throw std::runtime_error("the Kalman observer runs in mixed precision only");
+        if (run.mc.tab) {
+            // per-candidate plants: each thread's plant matrices in its shared-memory column
+            const size_t cols = (size_t)F64Plant<NDC, true>::FIELDS * SIM_BLOCK * sizeof(float);
+            prefer_shared((const void*)k_sim_fp64<NSC, NDC, true>);
+            k_sim_fp64<NSC, NDC, true><<<grid, SIM_BLOCK, cols, st>>>(run, P, gains, (double*)ywin, (double*)summ);
+            return;
+        }
         prefer_shared((const void*)k_sim_fp64<NSC, NDC>);
         k_sim_fp64<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
     } else {

@@ -6,8 +6,9 @@
 // (ref: src/main.cu:467-582, 592-602).  A server here keeps `lanes` sessions of
 // the same configuration (each with its own device scratch and streams) and a
 // scheduler thread.  Requests (gains and INFO rows in host memory) queue in
-// arrival order; when a lane is free the scheduler packs the oldest request's
-// plant with the requests behind it that use the same plant, up to the lane's
+// arrival order; when a lane is free the scheduler packs the oldest request
+// with the requests behind it of the same model, whatever their plants (a
+// batch on several plants carries a plant index per row), up to the lane's
 // capacity (a request larger than that is served in pieces), copies their
 // rows into the lane's pinned staging buffers, and enqueues H2D, the
 // evaluation and D2H on the lane's stream.  While one lane's batch is on the
@@ -148,10 +149,11 @@ void fail_pieces(ce_server* s, Lane& L, const std::string& msg) {
 }
 
 // Take rows for one batch from the queue (caller holds the lock): the oldest
-// request's model and plant, then the queued requests of the same model and
-// plant in arrival order.  Monte Carlo requests (a plant per row) batch with
-// the other Monte Carlo requests of their model, whatever their plants
-// (plant = -1 for such a batch).
+// request's model, then the queued requests of the same model in arrival
+// order, whatever their plants.  A batch whose rows all use one plant (tuning
+// requests on that plant) runs as an evaluation of that plant; any other batch
+// -- tuning requests on several plants, Monte Carlo requests (a plant per row)
+// -- runs with a plant index per row (plant = -1).
 std::vector<Piece> form_batch(ce_server* s, int& model, int& plant) {
     std::vector<Piece> out;
     if (s->queue.empty()) return out;
@@ -160,10 +162,11 @@ std::vector<Piece> form_batch(ce_server* s, int& model, int& plant) {
     int64_t room = s->capacity, off = 0;
     for (auto it = s->queue.begin(); it != s->queue.end() && room > 0;) {
         Request& r = **it;
-        if (r.model != model || (r.plants ? -1 : r.plant) != plant) {
+        if (r.model != model) {
             ++it;
             continue;
         }
+        if (r.plants || r.plant != plant) plant = -1;
         const int64_t take = std::min(room, r.n - r.next);
         out.push_back(Piece{*it, r.next, take, off});
         r.next += take;
@@ -187,7 +190,8 @@ void dispatch(ce_server* s, Lane& L, int model, int plant) {
     CE_CUDA(cudaMemcpyAsync(L.d_info, L.h_info, (size_t)n * iw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
     if (plant < 0) {
         for (const Piece& p : L.pieces)
-            for (int64_t k = 0; k < p.rows; ++k) L.h_idx[p.off + k] = p.req->plant + (int)(p.row0 + k);
+            for (int64_t k = 0; k < p.rows; ++k)
+                L.h_idx[p.off + k] = p.req->plants ? p.req->plant + (int)(p.row0 + k) : p.req->plant;
         session_evaluate_plants_indexed(L.sess[model], L.h_idx, n, L.d_gains, L.d_info, L.d_info, L.stream);
     } else if (ce_evaluate_device(L.sess[model], plant, n, L.d_gains, L.d_info, L.d_info, L.stream) != 0) {
         throw std::runtime_error(ce_last_error());
@@ -309,10 +313,14 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     CE_CUDA(cudaGetDevice(&device));
     for (Lane& L : s->lanes) {
         L.sess.assign(n_models, nullptr);
-        for (int m = 0; m < n_models; ++m)
+        for (int m = 0; m < n_models; ++m) {
             if (ce_session_create(&cfg[m], &plant[m], n_plants[m], &L.sess[m]) != 0 ||
                 ce_session_set_precision(L.sess[m], o.precision) != 0)
                 throw std::runtime_error(ce_last_error());
+            // a full batch's scratch and, with several plants, the plant table that
+            // batches on several plants read
+            session_prepare(L.sess[m], cap, n_plants[m] > 1);
+        }
         CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
         CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
         CE_CUDA(cudaMalloc((void**)&L.d_gains, (size_t)cap * cw * sizeof(float)));
@@ -370,8 +378,12 @@ void submit(ce_server* s, int32_t model, int32_t plant_index, bool plants, int64
     if (plants && plant_index + n > s->n_plants[model])
         fail("plants [{}, {}) exceed the model's {} plants (one plant per candidate)", plant_index, plant_index + n,
              s->n_plants[model]);
-    if (plants && s->precision != CE_PRECISION_MIXED) fail("per-candidate plants run in mixed precision");
     if (n > 0 && (!cuda_mx || !info_in || !info_out)) fail("ce_server_submit: null buffer");
+    // a plant that cannot be evaluated fails its request here, before the
+    // request can share a batch with others
+    const ce_session* s0 = s->lanes[0].sess[model];
+    for (int64_t p = plant_index, last = plants ? plant_index + n : plant_index + 1; p < last; ++p)
+        if (const std::string& e = session_plant_error(s0, (int)p); !e.empty()) fail("plant {}: {}", p, e);
     auto r = std::make_shared<Request>();
     r->model = model;
     r->plant = plant_index;

@@ -331,6 +331,27 @@ def random_shape(seed: int, n: int = 256, time: int | None = None, freq: int | N
     return Problem(f"random_shape_{seed}", text, plant, gains, info)
 
 
+def perturbed_plants(pl: PlantFiles, n_plants: int, seed: int) -> PlantFiles:
+    """n_plants copies of plant `pl` stacked as the plant files of a multi-plant session: A and
+    B_u scaled elementwise by (1 + 0.1 N(0,1)) and BASE_PARAMS by U[0.8, 1.2] per plant (A_I
+    recomputed), B_w and C kept; the observer model and the instruction tables are shared."""
+    rng = np.random.default_rng(seed)
+    nd = int(np.sqrt(pl.discrete_a.size))
+    A0 = pl.discrete_a.reshape(nd, nd).astype(np.float64)
+    Bu0 = pl.discrete_bu.astype(np.float64)
+    A = A0[None] * (1.0 + 0.1 * rng.standard_normal((n_plants, nd, nd)))
+    Bu = Bu0[None] * (1.0 + 0.1 * rng.standard_normal((n_plants, nd)))
+    bp = pl.base_params.astype(np.float64)[None] * rng.uniform(0.8, 1.2, (n_plants, pl.base_params.size))
+    Af = A.astype(F32)
+    return PlantFiles(
+        statespace_a=pl.statespace_a, statespace_a_i=pl.statespace_a_i, statespace_b=pl.statespace_b,
+        statespace_c=pl.statespace_c, statespace_d=pl.statespace_d,
+        discrete_a=Af.ravel(), discrete_a_i=(Af - np.eye(nd, dtype=F32)[None]).ravel(),
+        discrete_bu=Bu.astype(F32).ravel(), discrete_bw=np.tile(pl.discrete_bw, n_plants),
+        discrete_c=np.tile(pl.discrete_c, n_plants), base_params=bp.astype(F32).ravel(),
+        dc_info=pl.dc_info, u_info=pl.u_info, nl_info=pl.nl_info)
+
+
 def monte_carlo(n_plants: int = 262144, seed: int = 3, time: int = 8000, freq: int = 400, serial: bool = True,
                 base_seed: int = 2) -> Problem:
     """Monte Carlo over plants: the eight-state plant with A and B_u scaled elementwise by
@@ -340,22 +361,7 @@ def monte_carlo(n_plants: int = 262144, seed: int = 3, time: int = 8000, freq: i
     each plant itself.  Returns a Problem whose plant files hold n_plants stacked plants and
     whose CUDA_MX / INFO_MX hold one row per plant."""
     base = eight_state(n=1, seed=base_seed, time=time, freq=freq)
-    rng = np.random.default_rng(seed)
-    pl = base.plant
-    nd = int(np.sqrt(pl.discrete_a.size))
-    A0 = pl.discrete_a.reshape(nd, nd).astype(np.float64)
-    Bu0 = pl.discrete_bu.astype(np.float64)
-    A = A0[None] * (1.0 + 0.1 * rng.standard_normal((n_plants, nd, nd)))
-    Bu = Bu0[None] * (1.0 + 0.1 * rng.standard_normal((n_plants, nd)))
-    bp = pl.base_params.astype(np.float64)[None] * rng.uniform(0.8, 1.2, (n_plants, pl.base_params.size))
-    Af = A.astype(F32)
-    plant = PlantFiles(
-        statespace_a=pl.statespace_a, statespace_a_i=pl.statespace_a_i, statespace_b=pl.statespace_b,
-        statespace_c=pl.statespace_c, statespace_d=pl.statespace_d,
-        discrete_a=Af.ravel(), discrete_a_i=(Af - np.eye(nd, dtype=F32)[None]).ravel(),
-        discrete_bu=Bu.astype(F32).ravel(), discrete_bw=np.tile(pl.discrete_bw, n_plants),
-        discrete_c=np.tile(pl.discrete_c, n_plants), base_params=bp.astype(F32).ravel(),
-        dc_info=pl.dc_info, u_info=pl.u_info, nl_info=pl.nl_info)
+    plant = perturbed_plants(base.plant, n_plants, seed)
     gains = np.repeat(base.cuda_mx[:1], n_plants, axis=0)
     info = np.repeat(base.info_mx[:1], n_plants, axis=0)
     text = base.config_text.replace("mode = batch", "mode = serial" if serial else "mode = batch")

@@ -212,9 +212,9 @@ CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n,
  * and the observer model; their discrete matrices and BASE_PARAMS differ.  In
  * mode = serial the margin check and the sweep use each candidate's own plant,
  * as a serial round would.  Rows are bit-identical to evaluating each
- * candidate with ce_evaluate(s, first_plant + c, 1, ...).  Mixed precision and
- * the specialised simulation kernel (compiled for the plant table on first
- * use) only. */
+ * candidate with ce_evaluate(s, first_plant + c, 1, ...), in either precision
+ * (mixed: the specialised simulation kernel, compiled for the plant table on
+ * first use; FP64: the plain form reading the table). */
 CE_EXPORT int ce_evaluate_plants(ce_session* s, int32_t first_plant, int64_t n, const float* cuda_mx,
                                  const float* info_in, float* info_out);
 CE_EXPORT int ce_evaluate_plants_device(ce_session* s, int32_t first_plant, int64_t n, const float* d_cuda_mx,
@@ -357,7 +357,8 @@ typedef struct ce_server_stats {
 CE_EXPORT int ce_server_create(const ce_config* cfg, const ce_plant* plant, int32_t n_plants,
                                const ce_server_options* options, ce_server** out);
 /* Several models (configurations with their plants) in one server: every lane
- * holds a session per model; a batch holds requests of one model and plant. */
+ * holds a session per model; a batch holds requests of one model (on any of
+ * its plants: a batch on several plants evaluates each row on its own plant). */
 CE_EXPORT int ce_server_create_models(const ce_config* cfgs, const ce_plant* plants, const int32_t* n_plants,
                                       int32_t n_models, const ce_server_options* options, ce_server** out);
 CE_EXPORT void ce_server_destroy(ce_server* s); /* serves what is queued, then stops */
@@ -366,8 +367,8 @@ CE_EXPORT int ce_server_submit(ce_server* s, int32_t plant_index, int64_t n, con
 CE_EXPORT int ce_server_submit_model(ce_server* s, int32_t model, int32_t plant_index, int64_t n,
                                      const float* cuda_mx, const float* info_in, float* info_out, int64_t* request_id);
 /* A Monte Carlo request: row k is evaluated on plant first_plant + k of the model (as
- * ce_evaluate_plants; mixed precision).  Such requests batch with the model's other Monte
- * Carlo requests whatever their plants. */
+ * ce_evaluate_plants, in the server's precision).  Such requests batch with the model's
+ * other Monte Carlo requests whatever their plants. */
 CE_EXPORT int ce_server_submit_plants(ce_server* s, int32_t model, int32_t first_plant, int64_t n,
                                       const float* cuda_mx, const float* info_in, float* info_out,
                                       int64_t* request_id);

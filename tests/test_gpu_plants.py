@@ -47,9 +47,28 @@ def test_per_candidate_plants_errors():
     with ce.Session(cfg, p.plant, n_plants=8) as s:
         with pytest.raises(ce.ControllerEngineError, match="exceed the session"):
             s.evaluate_plants(p.cuda_mx, p.info_mx, first_plant=1)
+
+
+@pytest.mark.parametrize("serial", [True, False])
+def test_per_candidate_plants_fp64_form(serial):
+    """The plain FP64 form with one plant per candidate: rows equal the FP64 form of each
+    candidate alone with its plant, and differ from the mixed form's."""
+    p = synth.monte_carlo(n_plants=64, time=1200, freq=60, serial=serial)
+    rng = np.random.default_rng(12)
+    p.cuda_mx[:, :8] *= rng.uniform(0.5, 3.0, (64, 1)).astype(np.float32)
+    p.info_mx[:, :8] = p.cuda_mx[:, :8]
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, n_plants=64) as s:
+        mixed = s.evaluate_plants(p.cuda_mx, p.info_mx)
         s.set_precision("fp64")
-        with pytest.raises(ce.ControllerEngineError, match="mixed precision"):
-            s.evaluate_plants(p.cuda_mx, p.info_mx)
+        f64 = s.evaluate_plants(p.cuda_mx, p.info_mx)
+        part = s.evaluate_plants(p.cuda_mx[10:30], p.info_mx[10:30], first_plant=10)
+        ref = _alone(s, p, 0, 64)
+    assert np.array_equal(_bits(f64), _bits(ref))
+    assert np.array_equal(_bits(part), _bits(ref[10:30]))
+    assert not np.array_equal(_bits(f64), _bits(mixed))
+    sc = f64[:, cfg.info_scoring:cfg.info_scoring + 3]
+    assert len(np.unique(sc[:, 0])) > 32 and (sc[:, 1] < cfg.unstable_err).sum() > 5
 
 
 def test_per_candidate_device_api():

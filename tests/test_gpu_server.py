@@ -1,5 +1,6 @@
 """The serving front end (ce_server_*): requests of assorted sizes are packed into
-batches per plant, split when larger than a batch, and run on concurrent lanes;
+batches per model (on any of its plants), split when larger than a batch, and run on
+concurrent lanes;
 every request's rows must equal the rows of the same candidates evaluated alone,
 bit for bit.  Also: several plants in one server, submissions from several
 threads, HBM-budget admission and the latency statistics."""
@@ -73,6 +74,13 @@ def test_two_plants_in_one_server(mass_spring):
                 for a in range(0, 1536, 192) for k in range(2)]
         for k, a, r in reqs:
             assert np.array_equal(_bits(r.wait()), _bits(refs[k][a:a + 192]))
+    # one lane that waits for full batches: requests on both plants share every batch
+    with ce.Server(cfg, pl2, n_plants=2, max_batch=512, lanes=1, max_wait_us=200000) as srv:
+        reqs = [(k, a, srv.submit(p.cuda_mx[a:a + 192], p.info_mx[a:a + 192], plant_index=k))
+                for a in range(0, 1536, 192) for k in range(2)]
+        for k, a, r in reqs:
+            assert np.array_equal(_bits(r.wait()), _bits(refs[k][a:a + 192]))
+        assert srv.stats()["batches"] == 6  # 16 x 192 rows in batches of 512
 
 
 def test_concurrent_submitters(eight_state_small):
@@ -180,3 +188,54 @@ def test_monte_carlo_requests_batch_with_each_other():
     with ce.Server(cfg, p.plant, n_plants=600, max_batch=256, lanes=1) as srv:
         with pytest.raises(ce.ControllerEngineError, match="exceed the model"):
             srv.submit_plants(p.cuda_mx[:10], p.info_mx[:10], first_plant=595)
+
+
+def test_monte_carlo_batch_in_two_chunks():
+    """A Monte Carlo batch of 40,000 rows runs as two chunks; in serial mode every row's sweep
+    reads its own plant's grid, in the second chunk as in the first."""
+    from controllerengine_gb300 import synth
+    p = synth.monte_carlo(n_plants=40000, time=300, freq=40, serial=True)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, n_plants=40000) as s:
+        ref = s.evaluate_plants(p.cuda_mx, p.info_mx)
+    with ce.Server(cfg, p.plant, n_plants=40000, max_batch=40000, lanes=1) as srv:
+        got = srv.submit_plants(p.cuda_mx, p.info_mx, first_plant=0).wait()
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
+def test_monte_carlo_requests_fp64_server():
+    """Monte Carlo requests on a server of the FP64 form equal the FP64 form of
+    ce_evaluate_plants, beside ordinary requests."""
+    from controllerengine_gb300 import synth
+    p = synth.monte_carlo(n_plants=300, time=900, freq=50, serial=True)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, n_plants=300, precision="fp64") as s:
+        ref_mc = s.evaluate_plants(p.cuda_mx, p.info_mx)
+        ref_one = s.evaluate(p.cuda_mx[:50], p.info_mx[:50], plant_index=3)
+    with ce.Server(cfg, p.plant, n_plants=300, max_batch=128, lanes=2, precision="fp64") as srv:
+        a = srv.submit_plants(p.cuda_mx[:200], p.info_mx[:200], first_plant=0)
+        b = srv.submit(p.cuda_mx[:50], p.info_mx[:50], plant_index=3)
+        c = srv.submit_plants(p.cuda_mx[250:300], p.info_mx[250:300], first_plant=250)
+        assert np.array_equal(_bits(a.wait()), _bits(ref_mc[:200]))
+        assert np.array_equal(_bits(b.wait()), _bits(ref_one))
+        assert np.array_equal(_bits(c.wait()), _bits(ref_mc[250:300]))
+
+
+def test_request_on_unusable_plant_fails_alone():
+    """A plant whose sweep grid failed (here: C = 0, no gain at the crossover) fails the requests
+    that name it when they are submitted; requests on the other plants are served."""
+    from controllerengine_gb300 import synth
+    p = synth.monte_carlo(n_plants=64, time=600, freq=40, serial=True)
+    p.plant.discrete_c[5 * 8:6 * 8] = 0.0
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, n_plants=64) as s:
+        ref = s.evaluate_plants(p.cuda_mx[10:], p.info_mx[10:], first_plant=10)
+        with pytest.raises(ce.ControllerEngineError, match="crossover"):
+            s.evaluate_plants(p.cuda_mx[:10], p.info_mx[:10])
+    with ce.Server(cfg, p.plant, n_plants=64, max_batch=256, lanes=1) as srv:
+        with pytest.raises(ce.ControllerEngineError, match="plant 5"):
+            srv.submit_plants(p.cuda_mx[:10], p.info_mx[:10], first_plant=0)
+        with pytest.raises(ce.ControllerEngineError, match="plant 5"):
+            srv.submit(p.cuda_mx[:3], p.info_mx[:3], plant_index=5)
+        got = srv.submit_plants(p.cuda_mx[10:], p.info_mx[10:], first_plant=10).wait()
+    assert np.array_equal(_bits(got), _bits(ref))
