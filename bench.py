@@ -743,13 +743,21 @@ def main():
                           f"5 n^3 FP64 FMAs (10 n^3 flops) of a {n2}x{n2} real eigensolve x {n_listed} "
                           "listed candidates")}
     src64 = "measured FP64 DFMA issue rate (ce_measure_fma_rate), not in MEASURED_PEAKS"
+    # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each stage's launch over one
+    # 16,384-candidate chunk of this workload, from ncu captures (summaries in the profiles
+    # directory); scaled to this step's candidates in proportion.  Writes still resident in L2
+    # when a kernel ends are not counted (the fit window: 459 MB written per chunk, 404 MB seen).
+    dram_mb_16k = {"sim": 2.33 + 403.96, "fit": 358.21 + 84.60, "lina_eig": 1.29 + 0.03, "nominal": 7.62,
+                   "sweep": 7.57 + 0.66}
     rooflines = {}
     for group, bound, pk, sname in ((work, "fp32", peak, src), (work64, "fp64", fp64_rate / 1e12, src64)):
         for st, (kname, ops, desc) in group.items():
             ach = ops / (per_step[st] * 1e-3) / 1e12 if per_step.get(st) else None
             rooflines[st] = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "Tops/s",
-                             "frac": ach / pk if ach else None, "traffic": None, "work_per_launch": desc,
-                             "peak_source": sname}
+                             "frac": ach / pk if ach else None,
+                             "traffic": dram_mb_16k[st] * 1e6 * n / 16384 if st in dram_mb_16k else None,
+                             "traffic_unit": "bytes per step (ncu capture of a 16,384-candidate launch, scaled)",
+                             "work_per_launch": desc, "peak_source": sname}
             if bound == "fp64" and ach:
                 # the reference's Eigen stages run unfused (separate multiply and add), so a
                 # bit-exact restatement issues two FP64 instructions per multiply-add
