@@ -148,7 +148,8 @@ struct ce_ragged {
     int64_t inst_cap = 0;
     float *h_gains = nullptr, *h_info = nullptr;  // pinned staging rows at the layout widths
     int64_t host_cap = 0;
-    std::vector<int> h_inst;
+    std::vector<int> h_inst;        // device position -> instance
+    std::vector<int64_t> dev_k;     // device position -> candidate within its instance
 };
 
 namespace ce {
@@ -1170,8 +1171,7 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
         r->inst_cap = N;
     }
     r->h_inst.resize((size_t)N);
-    // the caller's row offsets of each instance, then the device order: instances by
-    // decreasing horizon, so a warp's candidates run similar step counts
+    // the caller's row offsets of each instance
     std::vector<int64_t> goff(I), ioff(I);
     int64_t gi = 0, ii = 0;
     for (int i = 0; i < I; ++i) {
@@ -1180,21 +1180,46 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
         gi += n_cand[i] * r->cfg[i].cuda_mx_width;
         ii += n_cand[i] * r->cfg[i].info_mx_width;
     }
-    std::vector<int> order(I);
-    for (int i = 0; i < I; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
+    // The device order.  Candidates sorted by decreasing horizon are dealt to the
+    // W = ceil(N / 32) warps in turn: warp w holds sorted candidates w, W + w,
+    // 2W + w, ..., one from each horizon tier.  A warp's lanes interpret
+    // different instruction programs, so a step costs about as many passes as
+    // its active lanes hold distinct operations; with the horizons spread, the
+    // short lanes leave early and the long ones finish with few lanes active,
+    // instead of the longest instances sharing warps for their whole horizon.
+    std::vector<int> sorted_inst;
+    std::vector<int64_t> sorted_k;
+    sorted_inst.reserve((size_t)N);
+    sorted_k.reserve((size_t)N);
     {
-        int64_t c = 0;
-        for (int i : order) {
-            const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
-            const float* g = cuda_mx + goff[i];
-            const float* in = info_in + ioff[i];
-            for (int64_t k = 0; k < n_cand[i]; ++k, ++c, g += cw, in += iw) {
-                std::memcpy(r->h_gains + c * LW, g, (size_t)cw * sizeof(float));
-                std::memcpy(r->h_info + c * LI, in, (size_t)iw * sizeof(float));
-                r->h_inst[(size_t)c] = i;
+        std::vector<int> order(I);
+        for (int i = 0; i < I; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
+        for (int i : order)
+            for (int64_t k = 0; k < n_cand[i]; ++k) {
+                sorted_inst.push_back(i);
+                sorted_k.push_back(k);
             }
-        }
+    }
+    const int64_t W = (N + 31) / 32;
+    r->dev_k.resize((size_t)N);
+    {
+        int64_t p = 0;
+        for (int64_t w = 0; w < W; ++w)
+            for (int64_t l = 0; l < 32; ++l) {
+                const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, 32 W)
+                if (q >= N) continue;
+                r->h_inst[(size_t)p] = sorted_inst[(size_t)q];
+                r->dev_k[(size_t)p] = sorted_k[(size_t)q];
+                ++p;
+            }
+    }
+    for (int64_t c = 0; c < N; ++c) {
+        const int i = r->h_inst[(size_t)c];
+        const int64_t k = r->dev_k[(size_t)c];
+        const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
+        std::memcpy(r->h_gains + c * LW, cuda_mx + goff[i] + k * cw, (size_t)cw * sizeof(float));
+        std::memcpy(r->h_info + c * LI, info_in + ioff[i] + k * iw, (size_t)iw * sizeof(float));
     }
     ce_session* s = r->s;
     ensure_buffers(s, N, false);
@@ -1209,12 +1234,10 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
     CE_CUDA(cudaMemcpyAsync(r->h_info, b.info, (size_t)N * LI * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     CE_CUDA(cudaStreamSynchronize(s->stream));
     collect_stage_times(s);
-    int64_t c = 0;
-    for (int i : order) {
+    for (int64_t c = 0; c < N; ++c) {
+        const int i = r->h_inst[(size_t)c];
         const int iw = r->cfg[i].info_mx_width;
-        float* o = info_out + ioff[i];
-        for (int64_t k = 0; k < n_cand[i]; ++k, ++c, o += iw)
-            std::memcpy(o, r->h_info + c * LI, (size_t)iw * sizeof(float));
+        std::memcpy(info_out + ioff[i] + r->dev_k[(size_t)c] * iw, r->h_info + c * LI, (size_t)iw * sizeof(float));
     }
 }
 
