@@ -331,6 +331,33 @@ def random_shape(seed: int, n: int = 256, time: int | None = None, freq: int | N
     return Problem(f"random_shape_{seed}", text, plant, gains, info)
 
 
+def first_order_loop(freq: int = 2000, a: float = 0.99, b: float = 0.01, gains=((5.0, 0.05),)) -> Problem:
+    """A loop whose margins have a closed form: a first-order observer model P(z) = c b / (z - a)
+    (c = 1, d = 0; batch mode, so the margin check uses this model) and per row gains (k, l, N = 1),
+    whose compensator is G(z) = k l / (z - a_cl) with a_cl = a - b k - l c, the observer block of
+    LIN_A.  The loop P G = c b k l / ((z - a)(z - a_cl)) has one gain crossover and one phase
+    crossover in (0, pi).  The simulated plant is a first-order lag; no nonlinear terms."""
+    bp = np.array([1.0, -1e6, 1e6], F32)
+    dc = instr_rows([(MUL, 0, STATE, 1)], 1)                                   # y = x0 * 1
+    u = instr_rows([(SAT, 0, 2, 3)], 1)                                        # clamp(u_raw, -1e6, 1e6)
+    plant = PlantFiles(
+        statespace_a=np.array([a], F32), statespace_a_i=np.array([a], F32) - F32(1),
+        statespace_b=np.array([b], F32), statespace_c=np.array([1.0], F32), statespace_d=np.zeros(1, F32),
+        discrete_a=np.array([0.95], F32), discrete_a_i=np.array([0.95], F32) - F32(1),
+        discrete_bu=np.array([0.05], F32), discrete_bw=np.zeros(0, F32), discrete_c=np.array([1.0], F32),
+        base_params=bp, dc_info=dc, u_info=u, nl_info=np.zeros((0, 2), np.int32))
+    g = np.array([[k, l, 1.0] for k, l in gains], F32)
+    info = np.zeros((g.shape[0], info_width(1, 1, 3)), F32)
+    info[:, :3] = g
+    text = _config_text(
+        statespace_dim=1, discrete_dim=1, nonlin_dim=0, n_params=3, input_size=3, dc_instructions=1,
+        u_instructions=1, nl_instructions="", n_cores=128, n_rounds=1, mode="batch", time=2000, duration=2.0,
+        ref_step_time=0.05, ref_amplitude=1.0, fit_start=0.05, fit_end=0.75, steady_start=0.75, bandwidth=2.0,
+        damping=0.6, overshoot=0.1, steady_state_error=0.05, crossover_coeff=1.0, target_gm=6.0, target_pm=45.0,
+        target_b=0.2, eig_fail_err=1.0e18, unstable_err=1.0e6, freq=freq, freq_min=0.01)
+    return Problem(f"first_order_loop_{freq}", text, plant, g, info)
+
+
 def perturbed_plants(pl: PlantFiles, n_plants: int, seed: int) -> PlantFiles:
     """n_plants copies of plant `pl` stacked as the plant files of a multi-plant session: A and
     B_u scaled elementwise by (1 + 0.1 N(0,1)) and BASE_PARAMS by U[0.8, 1.2] per plant (A_I

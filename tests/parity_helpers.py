@@ -84,3 +84,35 @@ def _stagewise(problem, oracle_mod, score_atol=1e-6):
     # the user columns pass through untouched
     assert _eq(info[:, :cfg.input_size], problem.info_mx[:, :cfg.input_size])
     return cfg, info
+
+
+def closed_form_margins(problem, oa, crossover, row=0):
+    """Margins of synth.first_order_loop's loop L(z) = c b k l / ((z - a)(z - a_cl)) in float64 from
+    its float32 coefficients (a_cl = oa, the observer block of LIN_A as computed): the gain
+    crossover |L| = 1 and the phase crossover arg L = -pi solved by bracketing on (0, pi); GM (dB),
+    PM (deg), DM (ms) there.  b_PC is the minimum over the sweep's own grid (theta_w in float32 as
+    the sweep forms it) of |1 + L| / (sqrt(1 + |alpha P|^2) sqrt(1 + |G / alpha|^2)), alpha =
+    1 / |P| at the crossover frequency."""
+    from scipy.optimize import brentq
+    cfg = ce.EngineConfig.parse(problem.config_text)
+    pl = problem.plant
+    a, b, c = (np.float64(x[0]) for x in (pl.statespace_a, pl.statespace_b, pl.statespace_c))
+    k, l = (np.float64(x) for x in problem.cuda_mx[row, :2])
+    oa = np.float64(oa)
+    P = lambda th: c * b / (np.exp(1j * th) - a)
+    G = lambda th: k * l / (np.exp(1j * th) - oa)
+    phase = lambda th: -(np.angle(np.exp(1j * th) - a) + np.angle(np.exp(1j * th) - oa))
+    ts = np.float64(np.float32(cfg.ts))
+    th_g = brentq(lambda t: abs(P(t) * G(t)) - 1.0, 1e-9, np.pi - 1e-9, xtol=1e-15)
+    th_p = brentq(lambda t: phase(t) + np.pi, 1e-9, np.pi - 1e-9, xtol=1e-15)
+    pm = 180.0 + np.degrees(phase(th_g))
+    gm = -20.0 * np.log10(abs(P(th_p) * G(th_p)))
+    dm = np.radians(pm) / th_g * ts * 1000.0
+    F = cfg.freq
+    f32 = np.float32
+    inc = (np.log(f32(cfg.freq_max)) - np.log(f32(cfg.freq_min))) / f32(F - 1)
+    th = np.exp(np.log(f32(cfg.freq_min)) + inc * np.arange(F, dtype=f32)).astype(f32) * f32(ts)
+    th = th.astype(np.float64)
+    alpha = 1.0 / abs(P(np.float64(crossover) * ts))
+    bw = abs(1.0 + P(th) * G(th)) / (np.sqrt(1.0 + (alpha * abs(P(th))) ** 2) * np.sqrt(1.0 + (abs(G(th)) / alpha) ** 2))
+    return dict(gm=gm, pm=pm, dm=dm, bpc=min(1.0, bw.min()))

@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import controllerengine_gb300 as ce
+from controllerengine_gb300 import synth
 from parity_helpers import _classes, _close, _cols, _eq, _stagewise
 
 pytestmark = pytest.mark.gpu
@@ -126,3 +127,23 @@ def test_fp64_form_runs_and_agrees_on_classification(lib, eight_state_small):
     c = _cols(cfg)
     ok = ~(ca != cb).any(axis=1) & (mix[:, c["am"]][:, 3] == 1)
     np.testing.assert_allclose(mix[ok][:, c["am"]][:, 4], f64[ok][:, c["am"]][:, 4], rtol=1e-3)
+
+
+def test_margins_closed_form(lib, oracle_mod):
+    """The margin sweep on a loop with a closed form (synth.first_order_loop, 2,000 points): GM, PM
+    and DM within 1e-3 dB / deg / ms of the exact margins, b_PC within 1e-5 of the minimum over
+    the grid, and LIN_A bit-identical to the oracle's."""
+    from parity_helpers import closed_form_margins
+    p = synth.first_order_loop(freq=2000, gains=((5.0, 0.05), (20.0, 0.2)))
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        out, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("lina",))
+    lina_o = oracle_mod.Oracle(p.config_text, p.plant).lina(p.cuda_mx)
+    assert _eq(d["lina"].reshape(lina_o.shape), lina_o)
+    for r in range(2):
+        am = out[r, cfg.info_allmargin:cfg.info_allmargin + 5]
+        want = closed_form_margins(p, lina_o[r, 0], cfg.crossover, row=r)
+        assert am[3] == 1.0
+        err = np.abs(am[[0, 1, 2]] - [want["gm"], want["pm"], want["dm"]])
+        assert (err < 1e-3).all(), (am, want)
+        assert abs(am[4] - want["bpc"]) <= 1e-5 * want["bpc"], (am[4], want["bpc"])

@@ -1,9 +1,13 @@
 """Pins of the CPU oracle itself: the FP64 eigensolver against LAPACK and closed
-forms, the simulation against an independent float64 recurrence, and the
-workload generator's invariants.  CPU only."""
+forms, the simulation against an independent float64 recurrence, the margins
+against a loop with a closed form, and the workload generator's invariants.
+CPU only."""
 import numpy as np
 import pytest
 from scipy.linalg import expm
+
+import controllerengine_gb300 as ce
+from controllerengine_gb300 import synth
 
 
 def test_eig_matches_lapack(oracle_mod):
@@ -95,3 +99,30 @@ def test_oracle_ref_config_equals_engine_parse(oracle_mod, observer):
         cfg = ce.EngineConfig.parse(p.config_text)
         for k, v in vars(rc).items():
             assert getattr(cfg, k) == v, k
+
+
+def test_margins_closed_form(oracle_mod):
+    """The margin restatement (ref: src/allmargin.cu:1-182) against a loop with a closed form,
+    synth.first_order_loop: GM, PM and DM from the sweep's interpolated crossovers converge to the
+    exact margins at second order in the grid spacing (linear interpolation between grid points),
+    and lie within 1e-3 dB / deg / ms of them at 2,000 points; b_PC equals the minimum over the
+    same grid."""
+    from parity_helpers import closed_form_margins
+    errs = {}
+    for F in (200, 400, 2000):
+        p = synth.first_order_loop(freq=F, gains=((5.0, 0.05), (20.0, 0.2)))
+        cfg = ce.EngineConfig.parse(p.config_text)
+        orc = oracle_mod.Oracle(p.config_text, p.plant)
+        lina = orc.lina(p.cuda_mx)
+        out = orc.allmargin(lina, p.cuda_mx, p.info_mx)
+        for r in range(2):
+            am = out[r, cfg.info_allmargin:cfg.info_allmargin + 5]
+            want = closed_form_margins(p, lina[r, 0], cfg.crossover, row=r)
+            assert am[3] == 1.0  # nominal loop stable
+            errs[F, r] = np.abs(am[[0, 1, 2]] - [want["gm"], want["pm"], want["dm"]])
+            assert abs(am[4] - want["bpc"]) <= 1e-5 * want["bpc"], (am[4], want["bpc"])
+    for r in range(2):
+        assert (errs[2000, r] < 1e-3).all(), errs[2000, r]
+        # second order while the interpolation error dominates (at 2,000 points float32
+        # rounding is of the same size): twice the points, ~4x smaller error (at least 3x)
+        assert (errs[200, r] > 3 * errs[400, r]).all(), (errs[200, r], errs[400, r])
