@@ -14,6 +14,7 @@
 // in two chunks so the fit of the first starts while the second's eigensolve
 // runs.  Only gains in and cost rows out cross the host boundary.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -150,6 +151,8 @@ struct ce_ragged {
     int64_t host_cap = 0;
     std::vector<int> h_inst;        // device position -> instance
     std::vector<int64_t> dev_k;     // device position -> candidate within its instance
+    // per instance: the operation of every interpreted slot (NL chains, then DC and U; 0 = empty)
+    std::vector<std::array<uint8_t, ce::MAXW * ce::MAX_NL + ce::MAX_DC + ce::MAX_U>> sig;
 };
 
 namespace ce {
@@ -1058,9 +1061,15 @@ void create_ragged(int n_inst, const ce_config* cfgs, const ce_plant* plants, ce
     std::vector<int> n_of(n_inst), F_of(n_inst), row_inst, row_w;
     std::vector<int64_t> zoff(n_inst), goff(n_inst);
     int64_t gtot = 0;
+    r->sig.assign(n_inst, {});
     for (int i = 0; i < n_inst; ++i) {
         const ce_config& c = cfgs[i];
         build_plant(c, plants[i], 0, P[i]);
+        auto& g = r->sig[i];
+        for (int w = 0; w < MAXW; ++w)
+            for (int k = 0; k < P[i].n_nl[w] && k < MAX_NL; ++k) g[w * MAX_NL + k] = (uint8_t)P[i].nl[w][k].op;
+        for (int k = 0; k < P[i].n_dc && k < MAX_DC; ++k) g[MAXW * MAX_NL + k] = (uint8_t)P[i].dc[k].op;
+        for (int k = 0; k < P[i].n_u && k < MAX_U; ++k) g[MAXW * MAX_NL + MAX_DC + k] = (uint8_t)P[i].u[k].op;
         float* m = mp.data() + (size_t)i * ms;
         std::memcpy(m, P[i].m_a, sizeof(P[i].m_a));
         std::memcpy(m + MAXS * MAXS, P[i].m_b, sizeof(P[i].m_b));
@@ -1202,6 +1211,28 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
             }
     }
     const int64_t W = (N + 31) / 32;
+    // Within each tier of W consecutive candidates, order by the programs'
+    // operation sequences, so that the candidates dealt to one warp (the same
+    // rank in every tier) tend to interpret the same operations in the same
+    // slots and the warp executes fewer distinct paths per slot.
+    {
+        std::vector<int64_t> idx((size_t)N);
+        for (int64_t q = 0; q < N; ++q) idx[(size_t)q] = q;
+        for (int64_t t0 = 0; t0 < N; t0 += W) {
+            const int64_t t1 = std::min(N, t0 + W);
+            std::stable_sort(idx.begin() + t0, idx.begin() + t1, [&](int64_t a, int64_t b) {
+                return r->sig[sorted_inst[(size_t)a]] < r->sig[sorted_inst[(size_t)b]];
+            });
+        }
+        std::vector<int> si((size_t)N);
+        std::vector<int64_t> sk((size_t)N);
+        for (int64_t q = 0; q < N; ++q) {
+            si[(size_t)q] = sorted_inst[(size_t)idx[(size_t)q]];
+            sk[(size_t)q] = sorted_k[(size_t)idx[(size_t)q]];
+        }
+        sorted_inst.swap(si);
+        sorted_k.swap(sk);
+    }
     r->dev_k.resize((size_t)N);
     {
         int64_t p = 0;
