@@ -1190,8 +1190,9 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
         ii += n_cand[i] * r->cfg[i].info_mx_width;
     }
     // The device order.  Candidates sorted by decreasing horizon are dealt to the
-    // W = ceil(N / 32) warps in turn: warp w holds sorted candidates w, W + w,
-    // 2W + w, ..., one from each horizon tier.  A warp's lanes interpret
+    // W warps of the simulation (32 / ragged_lanes_per_candidate() candidates
+    // each) in turn: warp w holds sorted candidates w, W + w, 2W + w, ..., one
+    // from each horizon tier.  A warp's lanes interpret
     // different instruction programs, so a step costs about as many passes as
     // its active lanes hold distinct operations; with the horizons spread, the
     // short lanes leave early and the long ones finish with few lanes active,
@@ -1210,7 +1211,8 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
                 sorted_k.push_back(k);
             }
     }
-    const int64_t W = (N + 31) / 32;
+    const int64_t per_warp = 32 / ragged_lanes_per_candidate();
+    const int64_t W = (N + per_warp - 1) / per_warp;
     // Within each tier of W consecutive candidates, order by the programs'
     // operation sequences, so that the candidates dealt to one warp (the same
     // rank in every tier) tend to interpret the same operations in the same
@@ -1237,8 +1239,8 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
     {
         int64_t p = 0;
         for (int64_t w = 0; w < W; ++w)
-            for (int64_t l = 0; l < 32; ++l) {
-                const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, 32 W)
+            for (int64_t l = 0; l < per_warp; ++l) {
+                const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, per_warp W)
                 if (q >= N) continue;
                 r->h_inst[(size_t)p] = sorted_inst[(size_t)q];
                 r->dev_k[(size_t)p] = sorted_k[(size_t)q];

@@ -139,6 +139,8 @@ const std::string& session_plant_error(const ce_session* s, int plant);
 // Allocate and build, now, what an evaluation of up to n candidates (with `plants`: on
 // per-candidate plants) would otherwise set up on first use.
 void session_prepare(ce_session* s, int64_t n, bool plants);
+// Lanes per candidate of a ragged batch's simulation (4: the wide form; 1: one thread each).
+int ragged_lanes_per_candidate();
 Run session_run(const ce_session* s, int plant, int64_t n);
 void session_count_launches(ce_session* s, int k);
 void session_evaluate_plants_indexed(ce_session* s, const int* h_idx, int64_t n, const float* d_cuda_mx,

@@ -5,6 +5,8 @@
 // session whose plant program has been compiled into straight-line code
 // (ce_jit.cpp) launches that kernel instead.  k_sim_fp64 is the plain FP64
 // form of the recurrence.
+#include <cstdlib>
+
 #include "ce_sim_body.cuh"
 #include "ce_host.h"
 
@@ -23,6 +25,200 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const _
                                                           const float* __restrict__ gains, float* __restrict__ ywin,
                                                           SimSummary* __restrict__ summ, float* __restrict__ traj) {
     sim_run<MAXS, MAXD, RagChains, SIM_LUENBERGER, true>(run, P, gains, ywin, summ, traj);
+}
+
+// The wide form of a ragged batch.  One thread per candidate runs the whole
+// horizon as one chain of dependent steps, reloading the plant from shared
+// memory every step; at the sizes of an uneven batch too few warps are resident
+// to hide that latency, and the longest horizons set the launch's length.
+// Here four lanes (a quad) share a candidate, eight candidates per warp.
+// Lane q owns rows 2q and 2q+1 of the observer and plant updates, with their
+// matrix rows in registers, and NL chain q.  Every lane of the quad forms the
+// step's scalars itself -- y (the DC chain), K.xh, u (the U chain), C.xh --
+// from the same state and in the same order.  Each value is therefore formed by
+// one lane with the operations and order of the one-thread form, so the
+// results are bit-identical to it.  The quad exchanges y, W and its new state
+// rows through the candidate's slot in shared memory: three quad barriers per
+// step.
+constexpr int WIDE_LANES = 4, WIDE_CPB = SIM_BLOCK / WIDE_LANES;  // candidates per block
+// slot layout: the NL chains read [xp_hi, y] as columns 0..MAXD; rows are
+// 16-byte aligned, and a stride of 52 words puts the 16-byte loads of a warp's
+// eight candidates on disjoint banks
+constexpr int WS_XH_HI = 0, WS_XH_LO = 8, WS_XP_HI = 16, WS_Y = WS_XP_HI + MAXD, WS_XP_LO = 28, WS_W = 36,
+              WS_STRIDE = 52;
+static_assert(MAXS == 8 && MAXD == 8 && MAXW == WIDE_LANES, "the quad splits 8 rows and 4 NL chains");
+
+__global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch, const float* __restrict__ gains,
+                                                               float* __restrict__ ywin,
+                                                               SimSummary* __restrict__ summ) {
+    __shared__ float tab[RT_FIELDS * WIDE_CPB];
+    __shared__ __align__(16) float slots[WIDE_CPB * WS_STRIDE];
+    __shared__ float stage[8][WIDE_CPB];
+    const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
+    const unsigned qm = 0xFu << (threadIdx.x & 28);
+    const int64_t c = (int64_t)blockIdx.x * WIDE_CPB + cl;
+    if (c >= launch.n) return;  // the whole quad leaves together
+    const Run& run = run_of<true>(launch, c);
+    {
+        // the candidate's table column, copied once by its quad
+        const float* __restrict__ g = launch.rg.tab + c;
+        const int64_t gs = launch.rg.tab_stride;
+        for (int f = q; f < RT_FIELDS; f += WIDE_LANES) tab[f * WIDE_CPB + cl] = g[(int64_t)f * gs];
+    }
+    float* st = slots + cl * WS_STRIDE;
+    const int r0 = 2 * q;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+        st[WS_XH_HI + r0 + rr] = 0.0f;
+        st[WS_XH_LO + r0 + rr] = 0.0f;
+        st[WS_XP_HI + r0 + rr] = 0.0f;
+        st[WS_XP_LO + r0 + rr] = 0.0f;
+    }
+    __syncwarp(qm);
+    const float* t = tab + cl;  // field f at t[f * WIDE_CPB]
+    float sai[2][MAXS], dai[2][MAXD], dbw[2][MAXW], sb[2], dbu[2], sc[MAXS];
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) sai[rr][j] = t[(RT_SAI + (r0 + rr) * MAXS + j) * WIDE_CPB];
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) dai[rr][j] = t[(RT_DAI + (r0 + rr) * MAXD + j) * WIDE_CPB];
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k) dbw[rr][k] = t[(RT_DBW + (r0 + rr) * MAXW + k) * WIDE_CPB];
+        sb[rr] = t[(RT_SB + r0 + rr) * WIDE_CPB];
+        dbu[rr] = t[(RT_DBU + r0 + rr) * WIDE_CPB];
+    }
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_CPB];
+    const float sd = t[RT_SD * WIDE_CPB];
+    const unsigned cnt0 = __float_as_uint(t[RT_CNT * WIDE_CPB]), cnt1 = __float_as_uint(t[(RT_CNT + 1) * WIDE_CPB]);
+    const int n_dc = (int)(cnt0 & 0xFFu), n_u = (int)((cnt0 >> 8) & 0xFFu);
+    const int n_nl = q == 0 ? (int)((cnt0 >> 16) & 0xFFu) : q == 1 ? (int)(cnt0 >> 24)
+                   : q == 2 ? (int)(cnt1 & 0xFFu) : (int)((cnt1 >> 8) & 0xFFu);
+    const int ns = run.ns;
+    const float* row = gains + c * run.cuda_w;
+    float K[MAXS], Lr[2];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) K[i] = i < ns ? row[i] : 0.0f;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) Lr[rr] = r0 + rr < ns ? row[ns + r0 + rr] : 0.0f;
+    const float N = row[2 * ns];
+
+    float xh_hi[MAXS], xh_lo[MAXS], xp_hi[MAXD], xp_lo[MAXD];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) xh_hi[i] = xh_lo[i] = xp_hi[i] = xp_lo[i] = 0.0f;
+    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float* wrow = ywin + c * (int64_t)run.fit_pitch;
+    const int T = run.time;
+    for (int tt = 0; tt < T; ++tt) {
+        // plant output
+        const float y = run_chain_tab<false, MAX_DC, 1>(t, WIDE_CPB, 0, n_dc, st + WS_XP_HI, 0.0f);
+        if (q == 0) {
+            st[WS_Y] = y;
+            // fit window, steady-state sum, extremes
+            const int w = tt - run.fit_start_id;
+            if (w >= 0 && w < run.fit_steps) {
+                stage[w & 7][cl] = y;
+                if ((w & 7) == 7 || w == run.fit_steps - 1 || tt == T - 1) {
+                    float4 a, b;
+                    a.x = stage[0][cl]; a.y = stage[1][cl]; a.z = stage[2][cl]; a.w = stage[3][cl];
+                    b.x = stage[4][cl]; b.y = stage[5][cl]; b.z = stage[6][cl]; b.w = stage[7][cl];
+                    float4* dst = reinterpret_cast<float4*>(wrow + (w & ~7));
+                    dst[0] = a;
+                    dst[1] = b;
+                }
+            }
+            if (tt >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            ymax = fmaxf(ymax, y);
+            ymin = fminf(ymin, y);
+        }
+        // controller output
+        float kx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) kx = __fmaf_rn(K[i], xh_hi[i], kx);
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) kx = __fmaf_rn(K[i], xh_lo[i], kx);
+        const float ref = tt < run.ref_step_id ? 0.0f : run.ref_amp;
+        const float u_raw = __fmaf_rn(N, ref, -kx);
+        const float u = run_chain_tab<true, MAX_U, 1>(t, WIDE_CPB, MAX_DC, n_u, st + WS_XH_HI, u_raw);
+        // observer output error
+        float yh = 0.0f;
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) yh = __fmaf_rn(sc[i], xh_hi[i], yh);
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) yh = __fmaf_rn(sc[i], xh_lo[i], yh);
+        yh = __fmaf_rn(sd, u, yh);
+        const float yerr = __fsub_rn(y, yh);
+        // this lane's observer rows: increment, then double-float add
+        float nh[2], nlo[2];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            float h = __fmaf_rn(Lr[rr], yerr, __fmul_rn(sb[rr], u));
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < MAXS; ++j) h = __fmaf_rn(sai[rr][j], xh_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < MAXS; ++j) l = __fmaf_rn(sai[rr][j], xh_lo[j], l);
+            // the row's old value from the slot (an index by lane would put the
+            // state arrays in local memory); nothing writes the slot before the
+            // second barrier of the step
+            nh[rr] = st[WS_XH_HI + r0 + rr];
+            nlo[rr] = st[WS_XH_LO + r0 + rr];
+            df_add(nh[rr], nlo[rr], h, l);
+        }
+        __syncwarp(qm);  // y is in the slot
+        // this lane's nonlinear term over [xp_hi, y]
+        st[WS_W + q] = run_chain_tab<false, MAX_NL, 1>(t, WIDE_CPB, MAX_DC + MAX_U + q * MAX_NL, n_nl,
+                                                        st + WS_XP_HI, 0.0f);
+        __syncwarp(qm);  // every W is in the slot; every read of this step's state is done
+        float W[MAXW];
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k) W[k] = st[WS_W + k];
+        // this lane's plant rows
+        float ph[2], plo[2];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            float h = __fmul_rn(dbu[rr], u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(dbw[rr][k], W[k], h);
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < MAXD; ++j) h = __fmaf_rn(dai[rr][j], xp_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < MAXD; ++j) l = __fmaf_rn(dai[rr][j], xp_lo[j], l);
+            ph[rr] = st[WS_XP_HI + r0 + rr];
+            plo[rr] = st[WS_XP_LO + r0 + rr];
+            df_add(ph[rr], plo[rr], h, l);
+        }
+        // publish this lane's rows, then read the whole new state
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            st[WS_XH_HI + r0 + rr] = nh[rr];
+            st[WS_XH_LO + r0 + rr] = nlo[rr];
+            st[WS_XP_HI + r0 + rr] = ph[rr];
+            st[WS_XP_LO + r0 + rr] = plo[rr];
+        }
+        __syncwarp(qm);
+#pragma unroll
+        for (int i = 0; i < MAXS; i += 4) {
+            const float4 a = *reinterpret_cast<const float4*>(st + WS_XH_HI + i);
+            const float4 b = *reinterpret_cast<const float4*>(st + WS_XH_LO + i);
+            const float4 e = *reinterpret_cast<const float4*>(st + WS_XP_HI + i);
+            const float4 f = *reinterpret_cast<const float4*>(st + WS_XP_LO + i);
+            xh_hi[i] = a.x; xh_hi[i + 1] = a.y; xh_hi[i + 2] = a.z; xh_hi[i + 3] = a.w;
+            xh_lo[i] = b.x; xh_lo[i + 1] = b.y; xh_lo[i + 2] = b.z; xh_lo[i + 3] = b.w;
+            xp_hi[i] = e.x; xp_hi[i + 1] = e.y; xp_hi[i + 2] = e.z; xp_hi[i + 3] = e.w;
+            xp_lo[i] = f.x; xp_lo[i + 1] = f.y; xp_lo[i + 2] = f.z; xp_lo[i + 3] = f.w;
+        }
+    }
+    if (q == 0) {
+        SimSummary sm;
+        sm.ysum = ysum;
+        sm.ymax = ymax;
+        sm.ymin = ymin;
+        sm.pad = 0.0f;
+        summ[c] = sm;
+    }
 }
 
 // The per-candidate table of a ragged batch (the RT_* fields) from the
@@ -188,6 +384,17 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __g
 
 static int dim_class(int d) { return d <= 4 ? 4 : 8; }
 
+// Lanes per candidate of a ragged batch's simulation: 4 (the wide form,
+// default) or 1 (CE_RAGGED_WIDE=0).  The host deals a batch's candidates to
+// warps of 32 / lanes.
+int ragged_lanes_per_candidate() {
+    static const int v = [] {
+        const char* e = std::getenv("CE_RAGGED_WIDE");
+        return (e && e[0] == '0') ? 1 : WIDE_LANES;
+    }();
+    return v;
+}
+
 template <int NSC, int NDC, int KMODE = SIM_LUENBERGER>
 static void sim_launch(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ,
                        float* traj, cudaStream_t st) {
@@ -216,11 +423,18 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
         // a ragged batch: every instance at the reference's padded width, its plant from the table
         if (precision == CE_PRECISION_FP64 || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
-        const size_t cols = (size_t)RT_FIELDS * SIM_BLOCK * sizeof(float);  // the candidates' table columns
-        CE_CUDA(cudaFuncSetAttribute((const void*)k_sim_ragged, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cols));
-        prefer_shared((const void*)k_sim_ragged);
-        k_sim_ragged<<<sim_grid(run), SIM_BLOCK, cols, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
+        if (ragged_lanes_per_candidate() == WIDE_LANES && !traj) {
+            prefer_shared((const void*)k_sim_ragged_wide);
+            k_sim_ragged_wide<<<(unsigned)((run.n + WIDE_CPB - 1) / WIDE_CPB), SIM_BLOCK, 0, st>>>(
+                run, gains, (float*)ywin, (SimSummary*)summ);
+        } else {
+            const size_t cols = (size_t)RT_FIELDS * SIM_BLOCK * sizeof(float);  // the candidates' table columns
+            CE_CUDA(cudaFuncSetAttribute((const void*)k_sim_ragged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cols));
+            prefer_shared((const void*)k_sim_ragged);
+            k_sim_ragged<<<sim_grid(run), SIM_BLOCK, cols, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ,
+                                                                 traj);
+        }
     } else if (run.kalman && run.kal_list == 1) {
         // the shared-noise form; the Kalman loop always runs the full padded observer width
         if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);

@@ -670,8 +670,9 @@ struct TableChains {
 
 // A ragged batch: each candidate's own instruction program, read from its
 // column of the per-candidate table (the interpreter of run_chain_sm, with the
-// instruction fields unpacked from the table words).
-template <bool HAS_SEED, int MAXC>
+// instruction fields unpacked from the table words).  Source column k is
+// src[k * SS].
+template <bool HAS_SEED, int MAXC, int SS = SIM_BLOCK>
 __device__ __forceinline__ float run_chain_tab(const float* t, int s, int slot0, int n, const float* src,
                                                float seed) {
     float result = 0.0f;
@@ -682,7 +683,7 @@ __device__ __forceinline__ float run_chain_tab(const float* t, int s, int slot0,
         const unsigned code = __float_as_uint(t[f * s]);
         const int op = (int)(code & 0xFFu), col = (int)((code >> 8) & 0xFFu);
         const int ak = (int)((code >> 16) & 0xFFu), bk = (int)(code >> 24);
-        const float pos = src[col * SIM_BLOCK];
+        const float pos = src[col * SS];
         float prev;
         if (r == 0) prev = (HAS_SEED && !isnan(seed)) ? seed : pos;
         else prev = result;
