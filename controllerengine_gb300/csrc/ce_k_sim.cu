@@ -41,6 +41,10 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const _
 // rows through the candidate's slot in shared memory: three quad barriers per
 // step.
 constexpr int WIDE_LANES = 4, WIDE_CPB = SIM_BLOCK / WIDE_LANES;  // candidates per block
+// words between consecutive fields of the block's table columns: with 17 the
+// four lanes of a quad, reading fields of their NL chains 24 fields apart, and
+// the warp's eight candidates, reading one field, fall on 32 different banks
+constexpr int WIDE_TS = WIDE_CPB + 1;
 // slot layout: the NL chains read [xp_hi, y] as columns 0..MAXD; rows are
 // 16-byte aligned, and a stride of 52 words puts the 16-byte loads of a warp's
 // eight candidates on disjoint banks
@@ -51,7 +55,7 @@ static_assert(MAXS == 8 && MAXD == 8 && MAXW == WIDE_LANES, "the quad splits 8 r
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch, const float* __restrict__ gains,
                                                                float* __restrict__ ywin,
                                                                SimSummary* __restrict__ summ) {
-    __shared__ float tab[RT_FIELDS * WIDE_CPB];
+    __shared__ float tab[RT_FIELDS * WIDE_TS];
     __shared__ __align__(16) float slots[WIDE_CPB * WS_STRIDE];
     __shared__ float stage[8][WIDE_CPB];
     const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
@@ -63,7 +67,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         // the candidate's table column, copied once by its quad
         const float* __restrict__ g = launch.rg.tab + c;
         const int64_t gs = launch.rg.tab_stride;
-        for (int f = q; f < RT_FIELDS; f += WIDE_LANES) tab[f * WIDE_CPB + cl] = g[(int64_t)f * gs];
+        for (int f = q; f < RT_FIELDS; f += WIDE_LANES) tab[f * WIDE_TS + cl] = g[(int64_t)f * gs];
     }
     float* st = slots + cl * WS_STRIDE;
     const int r0 = 2 * q;
@@ -75,23 +79,23 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         st[WS_XP_LO + r0 + rr] = 0.0f;
     }
     __syncwarp(qm);
-    const float* t = tab + cl;  // field f at t[f * WIDE_CPB]
+    const float* t = tab + cl;  // field f at t[f * WIDE_TS]
     float sai[2][MAXS], dai[2][MAXD], dbw[2][MAXW], sb[2], dbu[2], sc[MAXS];
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
 #pragma unroll
-        for (int j = 0; j < MAXS; ++j) sai[rr][j] = t[(RT_SAI + (r0 + rr) * MAXS + j) * WIDE_CPB];
+        for (int j = 0; j < MAXS; ++j) sai[rr][j] = t[(RT_SAI + (r0 + rr) * MAXS + j) * WIDE_TS];
 #pragma unroll
-        for (int j = 0; j < MAXD; ++j) dai[rr][j] = t[(RT_DAI + (r0 + rr) * MAXD + j) * WIDE_CPB];
+        for (int j = 0; j < MAXD; ++j) dai[rr][j] = t[(RT_DAI + (r0 + rr) * MAXD + j) * WIDE_TS];
 #pragma unroll
-        for (int k = 0; k < MAXW; ++k) dbw[rr][k] = t[(RT_DBW + (r0 + rr) * MAXW + k) * WIDE_CPB];
-        sb[rr] = t[(RT_SB + r0 + rr) * WIDE_CPB];
-        dbu[rr] = t[(RT_DBU + r0 + rr) * WIDE_CPB];
+        for (int k = 0; k < MAXW; ++k) dbw[rr][k] = t[(RT_DBW + (r0 + rr) * MAXW + k) * WIDE_TS];
+        sb[rr] = t[(RT_SB + r0 + rr) * WIDE_TS];
+        dbu[rr] = t[(RT_DBU + r0 + rr) * WIDE_TS];
     }
 #pragma unroll
-    for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_CPB];
-    const float sd = t[RT_SD * WIDE_CPB];
-    const unsigned cnt0 = __float_as_uint(t[RT_CNT * WIDE_CPB]), cnt1 = __float_as_uint(t[(RT_CNT + 1) * WIDE_CPB]);
+    for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_TS];
+    const float sd = t[RT_SD * WIDE_TS];
+    const unsigned cnt0 = __float_as_uint(t[RT_CNT * WIDE_TS]), cnt1 = __float_as_uint(t[(RT_CNT + 1) * WIDE_TS]);
     const int n_dc = (int)(cnt0 & 0xFFu), n_u = (int)((cnt0 >> 8) & 0xFFu);
     const int n_nl = q == 0 ? (int)((cnt0 >> 16) & 0xFFu) : q == 1 ? (int)(cnt0 >> 24)
                    : q == 2 ? (int)(cnt1 & 0xFFu) : (int)((cnt1 >> 8) & 0xFFu);
@@ -112,7 +116,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
     const int T = run.time;
     for (int tt = 0; tt < T; ++tt) {
         // plant output
-        const float y = run_chain_tab<false, MAX_DC, 1>(t, WIDE_CPB, 0, n_dc, st + WS_XP_HI, 0.0f);
+        const float y = run_chain_tab<false, MAX_DC, 1>(t, WIDE_TS, 0, n_dc, st + WS_XP_HI, 0.0f);
         if (q == 0) {
             st[WS_Y] = y;
             // fit window, steady-state sum, extremes
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         for (int i = 0; i < MAXS; ++i) kx = __fmaf_rn(K[i], xh_lo[i], kx);
         const float ref = tt < run.ref_step_id ? 0.0f : run.ref_amp;
         const float u_raw = __fmaf_rn(N, ref, -kx);
-        const float u = run_chain_tab<true, MAX_U, 1>(t, WIDE_CPB, MAX_DC, n_u, st + WS_XH_HI, u_raw);
+        const float u = run_chain_tab<true, MAX_U, 1>(t, WIDE_TS, MAX_DC, n_u, st + WS_XH_HI, u_raw);
         // observer output error
         float yh = 0.0f;
 #pragma unroll
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         }
         __syncwarp(qm);  // y is in the slot
         // this lane's nonlinear term over [xp_hi, y]
-        st[WS_W + q] = run_chain_tab<false, MAX_NL, 1>(t, WIDE_CPB, MAX_DC + MAX_U + q * MAX_NL, n_nl,
+        st[WS_W + q] = run_chain_tab<false, MAX_NL, 1>(t, WIDE_TS, MAX_DC + MAX_U + q * MAX_NL, n_nl,
                                                         st + WS_XP_HI, 0.0f);
         __syncwarp(qm);  // every W is in the slot; every read of this step's state is done
         float W[MAXW];
@@ -249,6 +253,12 @@ __global__ void __launch_bounds__(128) k_ragged_table(int64_t n, const Plant* __
         put(RT_INS + 3 * sl + 1, I.aval);
         put(RT_INS + 3 * sl + 2, I.bval);
     };
+    // every slot defined: unused ones are empty instructions (code 0, column 0)
+    for (int sl = 0; sl < RT_SLOTS; ++sl) {
+        put_u(RT_INS + 3 * sl, 0u);
+        put(RT_INS + 3 * sl + 1, 0.0f);
+        put(RT_INS + 3 * sl + 2, 0.0f);
+    }
     for (int k = 0; k < P.n_dc; ++k) slot(k, P.dc[k]);
     for (int k = 0; k < P.n_u; ++k) slot(MAX_DC + k, P.u[k]);
     for (int w = 0; w < MAXW; ++w)
