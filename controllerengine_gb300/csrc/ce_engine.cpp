@@ -151,6 +151,7 @@ struct ce_ragged {
     int64_t host_cap = 0;
     std::vector<int> h_inst;        // device position -> instance
     std::vector<int64_t> dev_k;     // device position -> candidate within its instance
+    std::vector<int64_t> order_counts;  // the candidate counts the device order was built for
     // per instance: the operation of every interpreted slot (NL chains, then DC and U; 0 = empty)
     std::vector<std::array<uint8_t, ce::MAXW * ce::MAX_NL + ce::MAX_DC + ce::MAX_U>> sig;
 };
@@ -1189,63 +1190,69 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
         gi += n_cand[i] * r->cfg[i].cuda_mx_width;
         ii += n_cand[i] * r->cfg[i].info_mx_width;
     }
-    // The device order.  Candidates sorted by decreasing horizon are dealt to the
-    // W warps of the simulation (32 / ragged_lanes_per_candidate() candidates
-    // each) in turn: warp w holds sorted candidates w, W + w, 2W + w, ..., one
-    // from each horizon tier.  A warp's lanes interpret
-    // different instruction programs, so a step costs about as many passes as
-    // its active lanes hold distinct operations; with the horizons spread, the
-    // short lanes leave early and the long ones finish with few lanes active,
-    // instead of the longest instances sharing warps for their whole horizon.
-    std::vector<int> sorted_inst;
-    std::vector<int64_t> sorted_k;
-    sorted_inst.reserve((size_t)N);
-    sorted_k.reserve((size_t)N);
-    {
-        std::vector<int> order(I);
-        for (int i = 0; i < I; ++i) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
-        for (int i : order)
-            for (int64_t k = 0; k < n_cand[i]; ++k) {
-                sorted_inst.push_back(i);
-                sorted_k.push_back(k);
-            }
-    }
-    const int64_t per_warp = 32 / ragged_lanes_per_candidate();
-    const int64_t W = (N + per_warp - 1) / per_warp;
-    // Within each tier of W consecutive candidates, order by the programs'
-    // operation sequences, so that the candidates dealt to one warp (the same
-    // rank in every tier) tend to interpret the same operations in the same
-    // slots and the warp executes fewer distinct paths per slot.
-    {
-        std::vector<int64_t> idx((size_t)N);
-        for (int64_t q = 0; q < N; ++q) idx[(size_t)q] = q;
-        for (int64_t t0 = 0; t0 < N; t0 += W) {
-            const int64_t t1 = std::min(N, t0 + W);
-            std::stable_sort(idx.begin() + t0, idx.begin() + t1, [&](int64_t a, int64_t b) {
-                return r->sig[sorted_inst[(size_t)a]] < r->sig[sorted_inst[(size_t)b]];
-            });
+    // The device order depends only on the instances and their candidate
+    // counts: it is kept from the previous call when the counts repeat.
+    const std::vector<int64_t> counts(n_cand, n_cand + I);
+    if (counts != r->order_counts || r->dev_k.size() != (size_t)N) {
+        // The device order.  Candidates sorted by decreasing horizon are dealt to the
+        // W warps of the simulation (32 / ragged_lanes_per_candidate() candidates
+        // each) in turn: warp w holds sorted candidates w, W + w, 2W + w, ..., one
+        // from each horizon tier.  A warp's lanes interpret
+        // different instruction programs, so a step costs about as many passes as
+        // its active lanes hold distinct operations; with the horizons spread, the
+        // short lanes leave early and the long ones finish with few lanes active,
+        // instead of the longest instances sharing warps for their whole horizon.
+        std::vector<int> sorted_inst;
+        std::vector<int64_t> sorted_k;
+        sorted_inst.reserve((size_t)N);
+        sorted_k.reserve((size_t)N);
+        {
+            std::vector<int> order(I);
+            for (int i = 0; i < I; ++i) order[i] = i;
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
+            for (int i : order)
+                for (int64_t k = 0; k < n_cand[i]; ++k) {
+                    sorted_inst.push_back(i);
+                    sorted_k.push_back(k);
+                }
         }
-        std::vector<int> si((size_t)N);
-        std::vector<int64_t> sk((size_t)N);
-        for (int64_t q = 0; q < N; ++q) {
-            si[(size_t)q] = sorted_inst[(size_t)idx[(size_t)q]];
-            sk[(size_t)q] = sorted_k[(size_t)idx[(size_t)q]];
-        }
-        sorted_inst.swap(si);
-        sorted_k.swap(sk);
-    }
-    r->dev_k.resize((size_t)N);
-    {
-        int64_t p = 0;
-        for (int64_t w = 0; w < W; ++w)
-            for (int64_t l = 0; l < per_warp; ++l) {
-                const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, per_warp W)
-                if (q >= N) continue;
-                r->h_inst[(size_t)p] = sorted_inst[(size_t)q];
-                r->dev_k[(size_t)p] = sorted_k[(size_t)q];
-                ++p;
+        const int64_t per_warp = 32 / ragged_lanes_per_candidate();
+        const int64_t W = (N + per_warp - 1) / per_warp;
+        // Within each tier of W consecutive candidates, order by the programs'
+        // operation sequences, so that the candidates dealt to one warp (the same
+        // rank in every tier) tend to interpret the same operations in the same
+        // slots and the warp executes fewer distinct paths per slot.
+        {
+            std::vector<int64_t> idx((size_t)N);
+            for (int64_t q = 0; q < N; ++q) idx[(size_t)q] = q;
+            for (int64_t t0 = 0; t0 < N; t0 += W) {
+                const int64_t t1 = std::min(N, t0 + W);
+                std::stable_sort(idx.begin() + t0, idx.begin() + t1, [&](int64_t a, int64_t b) {
+                    return r->sig[sorted_inst[(size_t)a]] < r->sig[sorted_inst[(size_t)b]];
+                });
             }
+            std::vector<int> si((size_t)N);
+            std::vector<int64_t> sk((size_t)N);
+            for (int64_t q = 0; q < N; ++q) {
+                si[(size_t)q] = sorted_inst[(size_t)idx[(size_t)q]];
+                sk[(size_t)q] = sorted_k[(size_t)idx[(size_t)q]];
+            }
+            sorted_inst.swap(si);
+            sorted_k.swap(sk);
+        }
+        r->dev_k.resize((size_t)N);
+        {
+            int64_t p = 0;
+            for (int64_t w = 0; w < W; ++w)
+                for (int64_t l = 0; l < per_warp; ++l) {
+                    const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, per_warp W)
+                    if (q >= N) continue;
+                    r->h_inst[(size_t)p] = sorted_inst[(size_t)q];
+                    r->dev_k[(size_t)p] = sorted_k[(size_t)q];
+                    ++p;
+                }
+        }
+        r->order_counts = counts;
     }
     for (int64_t c = 0; c < N; ++c) {
         const int i = r->h_inst[(size_t)c];

@@ -73,3 +73,33 @@ def test_ragged_empty_and_uneven_counts():
     for k in (0, 2):
         with ce.Session(cfgs[k], probs[k].plant) as s:
             assert np.array_equal(_bits(outs[k]), _bits(s.evaluate(probs[k].cuda_mx, probs[k].info_mx)))
+
+
+def test_ragged_order_reused_across_calls():
+    """The device order is kept while the candidate counts repeat: one ragged batch evaluated
+    with counts A, then B, then A again on other gains, every time equal to the sessions."""
+    probs = _instances()
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    rng = np.random.default_rng(5)
+
+    def rows(sub, scale):
+        # K and L scaled (N kept); the INFO rows' user columns pass through unchanged
+        out = []
+        for p, m in zip(probs, sub):
+            g = p.cuda_mx[:m].copy()
+            g[:, :-1] *= np.float32(scale)
+            out.append((g, p.info_mx[:m].copy()))
+        return out
+
+    full = [p.cuda_mx.shape[0] for p in probs]
+    part = [max(0, m - int(rng.integers(0, 3))) for m in full]
+    with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+        for sub, scale in ((full, 1.0), (part, 1.0), (full, 0.9)):
+            batch = rows(sub, scale)
+            outs = rb.evaluate(batch)
+            for c, p, (g, i), o in zip(cfgs, probs, batch, outs):
+                if g.shape[0] == 0:
+                    continue
+                with ce.Session(c, p.plant) as s:
+                    ref = s.evaluate(g, i)
+                assert np.array_equal(_bits(o), _bits(ref)), (p.name, scale, g.shape[0])
