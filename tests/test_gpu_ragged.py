@@ -103,3 +103,34 @@ def test_ragged_order_reused_across_calls():
                 with ce.Session(c, p.plant) as s:
                     ref = s.evaluate(g, i)
                 assert np.array_equal(_bits(o), _bits(ref)), (p.name, scale, g.shape[0])
+
+
+_ONE_THREAD_SCRIPT = r"""
+import sys, numpy as np
+import controllerengine_gb300 as ce
+from controllerengine_gb300 import synth
+probs = [synth.random_shape(2000 + k, n=3, time=int(400 + 37 * k % 1500), freq=int(30 + 7 * k % 120))
+         for k in range(120)]
+cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+    outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+np.save(sys.argv[1], np.concatenate([o.ravel() for o in outs]))
+"""
+
+
+def test_ragged_one_thread_form_equals_wide_form(tmp_path):
+    """The one-thread simulation form (CE_RAGGED_WIDE=0, read once per process) and the default
+    wide form give the same rows bit for bit."""
+    import os
+    import subprocess
+    import sys
+    script = tmp_path / "ragged_form.py"
+    script.write_text(_ONE_THREAD_SCRIPT)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for form, env in (("wide", {}), ("one", {"CE_RAGGED_WIDE": "0"})):
+        out = tmp_path / f"{form}.npy"
+        subprocess.run([sys.executable, str(script), str(out)], check=True, cwd=root,
+                       env={**os.environ, **env, "PYTHONPATH": root})
+        res[form] = np.load(out)
+    assert np.array_equal(_bits(res["wide"]), _bits(res["one"]))
