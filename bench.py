@@ -407,9 +407,9 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
     2..8, 0-4 nonlinear terms with their own instruction programs, horizons 1e3..2e4 steps,
     50..400 sweep points): instances/s of one ragged batch (ce_ragged_evaluate, host buffers, every
     stage one launch over all instances), beside (a) the same instances evaluated one session each
-    (a sample of them, sessions created beforehand), and (b) the padded-to-max form: n_inst
-    candidates of the 8-state plant at the largest horizon and sweep (20,000 steps, 400 points)
-    in one session."""
+    (a sample of them, sessions created beforehand), (b) padded to max: the same instances with
+    every horizon and sweep raised to the largest (20,000 steps, 400 points), and (c) n_inst
+    candidates of one 8-state plant at that size in one session."""
     import controllerengine_gb300 as ce
     from controllerengine_gb300 import synth
     t0 = time.perf_counter()
@@ -454,7 +454,27 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
     per_inst = (time.perf_counter() - t0) / len(pick)
     for s_ in sess:
         s_.close()
-    # (b) padded to the largest shape, horizon and sweep
+    # (b) padded to max: the same instances (their own plants and programs, the simulation already
+    # at the padded 8/8 width) with every horizon raised to the largest, 20,000 steps at the
+    # instance's own step size, and every sweep to 400 points, through the same ragged path
+    import re
+
+    def pad(p, c):
+        t = re.sub(r"(?m)^time = .*$", "time = 20000", p.config_text)
+        t = re.sub(r"(?m)^duration = .*$", f"duration = {20000 * float(c.ts)!r}", t)
+        return re.sub(r"(?m)^freq = .*$", "freq = 400", t)
+
+    pcfgs = [ce.EngineConfig.parse(pad(p, c)) for p, c in zip(probs, cfgs)]
+    assert all(c.time == 20000 and c.freq == 400 for c in pcfgs)
+    with ce.Ragged([(c, p.plant) for c, p in zip(pcfgs, probs)]) as rp:
+        for _ in range(warmup):
+            rp.evaluate_packed(counts, g_all, i_all)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            rp.evaluate_packed(counts, g_all, i_all)
+        padded = (time.perf_counter() - t0) / steps
+    # (c) one uniform plant at the largest shape (8-state, 4 NL terms, 20,000 steps, 400 points):
+    # another problem, run by one compiled program with no interpretation
     pm = synth.eight_state(n=n_inst, time=20000, freq=400)
     pc = ce.EngineConfig.parse(pm.config_text)
     with ce.Session(pc, pm.plant) as s_:
@@ -463,7 +483,7 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
         t0 = time.perf_counter()
         for _ in range(steps):
             s_.evaluate(pm.cuda_mx, pm.info_mx)
-        padded = (time.perf_counter() - t0) / steps
+        uniform = (time.perf_counter() - t0) / steps
     shapes = {(c.statespace_dim, c.discrete_dim, c.nonlin_dim) for c in cfgs}
     return {"workload": f"{n_inst} instances x 1 candidate: dims 2..8 ({len(shapes)} distinct (ns, nd, nw)), "
                         "0-4 NL terms, horizons 1e3..2e4, 50..400 sweep points",
@@ -473,7 +493,11 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
             "one_session_per_instance": {"instances_per_s": 1.0 / per_inst, "ms_per_instance": 1e3 * per_inst,
                                          "sample": len(pick)},
             "padded_to_max": {"instances_per_s": n_inst / padded, "ms_per_step": 1e3 * padded,
-                              "shape": "8-state, 4 NL terms, 20000 steps, 400 points"},
+                              "padding": "the same instances, every horizon 20000 steps and every sweep 400 "
+                                         "points (the simulation always runs at the padded 8/8 width)"},
+            "uniform_max_plant": {"instances_per_s": n_inst / uniform, "ms_per_step": 1e3 * uniform,
+                                  "shape": "one 8-state, 4 NL-term plant and program for every candidate, "
+                                           "20000 steps, 400 points (a different problem)"},
             "timing": "wall clock around the synchronous host-buffer call ce_ragged_evaluate (packing to the "
                       "device layout, copies and kernels)"}
 
