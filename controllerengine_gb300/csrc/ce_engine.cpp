@@ -1448,8 +1448,9 @@ CE_EXPORT int64_t ce_session_kernel_launches(const ce_session* s) { return s ? s
 CE_EXPORT int ce_session_set_tuning(ce_session* s, const ce_tuning* t) {
     return guarded([&] {
         if (!s || !t) fail("null argument");
-        if (t->eig_lanes != 0 && t->eig_lanes != 1 && t->eig_lanes != 2 && t->eig_lanes != 4)
-            fail("eig_lanes must be 0, 1, 2 or 4, got {}", t->eig_lanes);
+        if (t->eig_lanes != 0 && t->eig_lanes != 1 && t->eig_lanes != 2 && t->eig_lanes != 4 && t->eig_lanes != 8 &&
+            t->eig_lanes != 16)
+            fail("eig_lanes must be 0, 1, 2, 4, 8 or 16, got {}", t->eig_lanes);
         if (t->eig_blocks_per_sm < 0 || t->eig_blocks_per_sm > 32)
             fail("eig_blocks_per_sm must be in [0, 32], got {}", t->eig_blocks_per_sm);
         if (t->chunks < 0 || t->chunks > MAX_CHUNKS) fail("chunks must be in [0, {}], got {}", MAX_CHUNKS, t->chunks);

@@ -131,7 +131,7 @@ struct Run {
     int* kal_totals;
     int64_t kal_defer;
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
-    int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2 or 4; 0: the default)
+    int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2, 4, 8 or 16; 0: by batch size)
     int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)
     // floats (or reals) per candidate in the LIN_A, eigenvalue, AtA and Atb buffers:
     // nt^2, 2nt, (2nt)^2, 2nt for a uniform evaluation, the maxima for a ragged one

@@ -865,39 +865,57 @@ static void set_smem(const void* fn, size_t bytes) {
     prefer_shared(fn);
 }
 
-// Lanes per matrix of the FP64 eigensolves.  One lane per matrix issues the
-// fewest FP64 instructions; more lanes per matrix put more warps on each SM
-// (the matrices of a warp share its shared-memory footprint), at the price of
-// computing the scalar steps redundantly.  Two lanes measured fastest on the
-// eight-state workload (LIN_A eigensolve of 65,536 16x16 matrices: 21.9 ms with
-// one lane, 18.4 ms with two).  CE_EIG_LANES=1|2|4 overrides.
-// A session's tuning (Run::eig_lanes) wins over the default.
-static int eig_lanes(const Run& run) {
-    static const int v = [] {
-        const char* e = std::getenv("CE_EIG_LANES");
-        const int k = e ? std::atoi(e) : 0;
-        return (k == 1 || k == 2 || k == 4) ? k : EIG_LANES_DEFAULT;
-    }();
-    return (run.eig_lanes == 1 || run.eig_lanes == 2 || run.eig_lanes == 4) ? run.eig_lanes : v;
-}
-
 // Blocks (one warp each) per SM of the persistent FP64 kernels.  Their
 // footprint is mostly shared memory (16 matrices x 2 KB per warp with two
 // lanes per matrix); a fixed number per SM keeps the FP64 pipe of every SM
 // fed while leaving the rest of the SM to the FP32 stages that run alongside
 // on the other stream.  CE_EIG_BLOCKS_PER_SM overrides.
-static int eig_grid(const Run& run, int64_t work, int mats) {
+static int eig_blocks_per_sm(const Run& run) {
     static const int dflt = [] {
         const char* e = std::getenv("CE_EIG_BLOCKS_PER_SM");
         const int k = e ? std::atoi(e) : 0;
         return (k >= 1 && k <= 32) ? k : EIG_BLOCKS_PER_SM_DEFAULT;
     }();
-    const int per_sm = (run.eig_blocks >= 1 && run.eig_blocks <= 32) ? run.eig_blocks : dflt;
+    return (run.eig_blocks >= 1 && run.eig_blocks <= 32) ? run.eig_blocks : dflt;
+}
+
+static int sm_count() {
     int dev = 0, sms = 0;
     CE_CUDA(cudaGetDevice(&dev));
     CE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+}
+
+static int eig_grid(const Run& run, int64_t work, int mats) {
     const int64_t need = (work + mats - 1) / mats;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)per_sm * sms));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)eig_blocks_per_sm(run) * sm_count()));
+}
+
+static bool valid_lanes(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16; }
+
+// Lanes per matrix of the FP64 eigensolves of n matrices.  An FP64 warp
+// instruction occupies the pipe for its full time whatever its active lanes,
+// so the lanes of a matrix cost nothing extra while they are spare: they split
+// the row and column loops (every element is still updated by exactly one
+// lane in the same order, so results do not depend on the split) and compute
+// the scalar steps redundantly.  A large batch fills the persistent grid with
+// two lanes per matrix (LIN_A eigensolve of 65,536 16x16 matrices: 21.9 ms
+// with one lane, 18.4 ms with two); a batch too small to fill it gets more
+// lanes per matrix, up to 16 -- the most that still hold every matrix in one
+// resident pass -- which shortens each matrix's chain of instructions.  A
+// session's tuning (Run::eig_lanes) or CE_EIG_LANES=1|2|4|8|16 overrides.
+static int eig_lanes(const Run& run, int64_t n) {
+    static const int env = [] {
+        const char* e = std::getenv("CE_EIG_LANES");
+        const int k = e ? std::atoi(e) : 0;
+        return valid_lanes(k) ? k : 0;
+    }();
+    if (valid_lanes(run.eig_lanes)) return run.eig_lanes;
+    if (env) return env;
+    const int64_t warps = (int64_t)eig_blocks_per_sm(run) * sm_count();
+    int eq = EIG_LANES_DEFAULT;
+    while (eq < 16 && (n * (2 * eq) + 31) / 32 <= warps) eq *= 2;
+    return eq;
 }
 
 template <int EQ>
@@ -936,20 +954,25 @@ static void nominal_q(const Run& run, const Plant& P, int precision, const float
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
                      int* nominal, int* list, int* count, cudaStream_t st) {
     CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
-    switch (eig_lanes(run)) {
+    switch (eig_lanes(run, run.n)) {
         case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
         case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
-        default: lina_eig_q<4>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
+        case 4: lina_eig_q<4>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
+        case 8: lina_eig_q<8>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
+        default: lina_eig_q<16>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
     }
     CE_CUDA(cudaGetLastError());
 }
 
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const int* list, const int* count, int* nominal, cudaStream_t st) {
-    switch (eig_lanes(run)) {
+    // the listed count is only known on the device: lanes as for all n candidates
+    switch (eig_lanes(run, run.n)) {
         case 1: nominal_q<1>(run, P, precision, gains, lina, list, count, nominal, st); break;
         case 2: nominal_q<2>(run, P, precision, gains, lina, list, count, nominal, st); break;
-        default: nominal_q<4>(run, P, precision, gains, lina, list, count, nominal, st); break;
+        case 4: nominal_q<4>(run, P, precision, gains, lina, list, count, nominal, st); break;
+        case 8: nominal_q<8>(run, P, precision, gains, lina, list, count, nominal, st); break;
+        default: nominal_q<16>(run, P, precision, gains, lina, list, count, nominal, st); break;
     }
     CE_CUDA(cudaGetLastError());
 }

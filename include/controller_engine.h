@@ -253,7 +253,7 @@ CE_EXPORT int ce_ragged_stage_times(ce_ragged* r, double* ms, int64_t* launches)
  * count, the lanes per matrix and the blocks per SM of the FP64 eigensolves,
  * keeps the fastest and returns it with its time. */
 typedef struct ce_tuning {
-    int32_t eig_lanes;         /* lanes per matrix of the FP64 eigensolves: 1, 2 or 4 */
+    int32_t eig_lanes;         /* lanes per matrix of the FP64 eigensolves: 1, 2, 4, 8 or 16 (0: by batch size) */
     int32_t eig_blocks_per_sm; /* their persistent one-warp blocks per SM */
     int32_t chunks;            /* chunks a batch of >= 32,768 candidates is cut into (<= 8) */
     double ms_per_evaluation;  /* ce_session_autotune: the time of the chosen setting */

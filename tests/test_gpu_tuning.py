@@ -16,7 +16,7 @@ def test_tuning_does_not_change_results():
     cfg = ce.EngineConfig.parse(p.config_text)
     with ce.Session(cfg, p.plant) as s:
         ref = s.evaluate(p.cuda_mx, p.info_mx)
-        for lanes, blocks, chunks in [(1, 3, 1), (4, 10, 2), (2, 6, 2), (2, 4, 1)]:
+        for lanes, blocks, chunks in [(1, 3, 1), (4, 10, 2), (2, 6, 2), (2, 4, 1), (8, 5, 2), (16, 5, 1)]:
             s.set_tuning(lanes, blocks, chunks)
             out = s.evaluate(p.cuda_mx, p.info_mx)
             assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), (lanes, blocks, chunks)
@@ -31,3 +31,16 @@ def test_tuning_does_not_change_results():
         assert s.tuning["eig_lanes"] == best["eig_lanes"]
         after = s.evaluate(p.cuda_mx, p.info_mx)
     assert np.array_equal(after.view(np.uint32), ref.view(np.uint32))
+
+
+def test_small_batch_lanes_do_not_change_results():
+    """A batch too small to fill the persistent eigensolve grid gets more lanes per matrix by
+    default (up to 16); its rows equal those of every explicit setting."""
+    p = synth.eight_state(n=700, time=1500, freq=80)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        auto = s.evaluate(p.cuda_mx, p.info_mx)
+        for lanes in (1, 2, 4, 8, 16):
+            s.set_tuning(lanes, 0, 0)
+            out = s.evaluate(p.cuda_mx, p.info_mx)
+            assert np.array_equal(out.view(np.uint32), auto.view(np.uint32)), lanes
