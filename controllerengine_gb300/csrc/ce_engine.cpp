@@ -1312,12 +1312,12 @@ int session_plants(const ce_session* s) { return s->n_plants; }
 const std::string& session_plant_error(const ce_session* s, int plant) { return s->plant_err[plant]; }
 
 // Everything an evaluation of up to n candidates would otherwise allocate or
-// build on first use: the scratch buffers, the FP64 sweep grids of an FP64
-// session and, with `plants`, the per-candidate plant table (and its
-// simulation kernel).  A server prepares its sessions at creation so that no
+// build on first use: the scratch buffers (none for n = 0), the FP64 sweep
+// grids of an FP64 session and, with `plants`, the per-candidate plant table
+// (and its simulation kernel).  A server prepares its sessions at creation so that no
 // batch waits on an allocation.
 void session_prepare(ce_session* s, int64_t n, bool plants) {
-    ensure_buffers(s, std::max<int64_t>(n, 1), false);
+    if (n > 0) ensure_buffers(s, n, false);
     if (s->precision == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
     if (plants) ensure_plant_table(s, s->precision);
     CE_CUDA(cudaDeviceSynchronize());

@@ -136,8 +136,8 @@ const ce_config* session_config(const ce_session* s);
 int session_plants(const ce_session* s);
 // Empty, or why plant `plant` cannot be evaluated (its sweep grid failed at creation).
 const std::string& session_plant_error(const ce_session* s, int plant);
-// Allocate and build, now, what an evaluation of up to n candidates (with `plants`: on
-// per-candidate plants) would otherwise set up on first use.
+// Allocate and build, now, what an evaluation of up to n candidates (n = 0: no scratch; with
+// `plants`: on per-candidate plants) would otherwise set up on first use.
 void session_prepare(ce_session* s, int64_t n, bool plants);
 // Lanes per candidate of a ragged batch's simulation (4: the wide form; 1: one thread each).
 int ragged_lanes_per_candidate();

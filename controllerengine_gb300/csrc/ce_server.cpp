@@ -311,6 +311,11 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     s->lanes.resize(lanes);
     int device = 0;
     CE_CUDA(cudaGetDevice(&device));
+    // every lane's full-batch scratch is allocated now when it fits in 80% of the
+    // free device memory (otherwise it grows with the batches, as in a session)
+    size_t free_b = 0, total_b = 0;
+    CE_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const bool eager = (double)lanes * (double)per * (double)cap <= 0.8 * (double)free_b;
     for (Lane& L : s->lanes) {
         L.sess.assign(n_models, nullptr);
         for (int m = 0; m < n_models; ++m) {
@@ -319,7 +324,7 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
                 throw std::runtime_error(ce_last_error());
             // a full batch's scratch and, with several plants, the plant table that
             // batches on several plants read
-            session_prepare(L.sess[m], cap, n_plants[m] > 1);
+            session_prepare(L.sess[m], eager ? cap : 0, n_plants[m] > 1);
         }
         CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
         CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
