@@ -465,7 +465,11 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
                 launch_sim(rp, P, prec, d_gains, b.ywin, b.summ, tr, fs);
             }
         } else if (sk) {
-            launch_sim_specialised(sk.main, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+            // a batch too small to fill the GPU runs four lanes per candidate
+            const bool wide = sk.wide && use_wide_sim(n, s->cfg.statespace_dim <= 4 ? 4 : 8,
+                                                      s->cfg.discrete_dim <= 4 ? 4 : 8);
+            launch_sim_specialised(wide ? sk.wide : sk.main, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr,
+                                   fs, wide);
         } else {
             launch_sim(r, P, prec, d_gains, b.ywin, b.summ, tr, fs);
         }

@@ -96,13 +96,18 @@ double measure_fma_rate(bool fp64);
 struct SimKernels {
     const void* main = nullptr;
     const void* shared = nullptr;
+    const void* wide = nullptr;  // four lanes per candidate (Luenberger, one plant)
     explicit operator bool() const { return main != nullptr; }
 };
 SimKernels specialise_sim(const Plant& P, int ns, int nd, std::string& log, bool mc = false, bool kalman = false);
 std::string specialised_source(const Plant& P, int ns, int nd, bool kalman = false);
-// Launches kernel (main or shared) over the candidates `run` selects.
+// Launches kernel (main or shared; with `wide`, the wide form) over the candidates `run` selects.
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
-                            SimSummary* summ, float* traj, cudaStream_t st);
+                            SimSummary* summ, float* traj, cudaStream_t st, bool wide = false);
+// Whether an evaluation of n candidates of dimension classes (nsc, ndc) runs the
+// wide simulation form: not for the 4/4 class, and only when the one-thread grid
+// would occupy fewer than half the SMs (CE_SIM_WIDE=0 never, =1 always).
+bool use_wide_sim(int64_t n, int nsc, int ndc);
 
 // Blocks of SIM_BLOCK threads that cover the candidates (or list slots) of `run`.
 int sim_grid(const Run& run);

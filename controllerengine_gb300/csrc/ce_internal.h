@@ -20,6 +20,8 @@ typedef long long int64_t;
 namespace ce {
 
 constexpr int SIM_BLOCK = 64;   // threads per simulation block (one candidate per thread)
+// the wide simulation forms: lanes per candidate and candidates per block
+constexpr int SW_LANES = 4, SW_CPB = SIM_BLOCK / SW_LANES;
 constexpr int MAX_CHUNKS = 8;  // largest number of chunks one evaluation is cut into
 constexpr int SWEEP_FG = 16;   // frequencies per thread in the LU pass of the margin sweep
 

@@ -15,6 +15,7 @@
 // (ref: src/main.cu:260-291) with the same roundings, so results are
 // bit-identical to the table-driven kernel's.  Compiled kernels are cached per
 // process by their source text.
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -116,6 +117,13 @@ std::string jit_source(const Plant& P, int ns, int nd, bool mc, bool kalman) {
         kernel("ce_sim_kalman_shared", MAXS, "ce::SIM_KALMAN_SHARED");
     } else {
         kernel("ce_sim_specialised", ns, "ce::SIM_LUENBERGER");
+        if (!mc) {
+            // the wide form (four lanes per candidate) for batches too small to fill the GPU
+            o << "extern \"C\" __global__ void __launch_bounds__(ce::SIM_BLOCK) ce_sim_wide(\n"
+                 "    const ce::Run run, const __grid_constant__ ce::Plant P, const float* __restrict__ gains,\n"
+                 "    float* __restrict__ ywin, ce::SimSummary* __restrict__ summ, float* __restrict__ traj) {\n"
+              << "    ce::sim_wide<" << ns << ", " << nd << ", cejit::Chains>(run, P, gains, ywin, summ, traj);\n}\n";
+        }
     }
     return o.str();
 }
@@ -156,10 +164,12 @@ SimKernels compile(const std::string& src, std::string& log, bool kalman) {
         return {};
     }
     SimKernels out;
-    const char* kernel_names[2] = {"ce_sim_specialised", "ce_sim_kalman_shared"};
-    for (int i = 0; i < (kalman ? 2 : 1); ++i) {
+    std::vector<std::pair<const char*, const void**>> wanted{{"ce_sim_specialised", &out.main}};
+    if (kalman) wanted.push_back({"ce_sim_kalman_shared", &out.shared});
+    if (src.find("ce_sim_wide(") != std::string::npos) wanted.push_back({"ce_sim_wide", &out.wide});
+    for (const auto& [name, slot] : wanted) {
         cudaKernel_t k;
-        e = cudaLibraryGetKernel(&k, lib, kernel_names[i]);
+        e = cudaLibraryGetKernel(&k, lib, name);
         if (e != cudaSuccess) {
             log = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
             return {};
@@ -170,7 +180,7 @@ SimKernels compile(const std::string& src, std::string& log, bool kalman) {
             log = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
             return {};
         }
-        (i == 0 ? out.main : out.shared) = reinterpret_cast<const void*>(k);
+        *slot = reinterpret_cast<const void*>(k);
     }
     return out;
 }
@@ -191,9 +201,28 @@ std::string specialised_source(const Plant& P, int ns, int nd, bool kalman) {
     return jit_source(P, ns, nd, false, kalman);
 }
 
+bool use_wide_sim(int64_t n, int nsc, int ndc) {
+    static const int mode = [] {
+        const char* e = std::getenv("CE_SIM_WIDE");
+        return e ? (e[0] == '0' ? 0 : 1) : -1;
+    }();
+    if (mode >= 0) return mode == 1;
+    static const int sms = [] {
+        int dev = 0, k = 0;
+        CE_CUDA(cudaGetDevice(&dev));
+        CE_CUDA(cudaDeviceGetAttribute(&k, cudaDevAttrMultiProcessorCount, dev));
+        return k;
+    }();
+    // measured: faster up to ~4,096 candidates with an 8-class observer or plant
+    // (one 8-state candidate: 4.0 -> 2.8 ms for 10,000 steps), slower at 16,384,
+    // and slower for the 4/4 class at any size (one row per lane is too little
+    // work to pay for the exchange)
+    return !(nsc == 4 && ndc == 4) && 2 * ((n + SIM_BLOCK - 1) / SIM_BLOCK) < (int64_t)sms;
+}
+
 void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, const float* gains, float* ywin,
-                            SimSummary* summ, float* traj, cudaStream_t st) {
-    const int grid = sim_grid(run);
+                            SimSummary* summ, float* traj, cudaStream_t st, bool wide) {
+    const int grid = wide ? (int)((run.n + SW_CPB - 1) / SW_CPB) : sim_grid(run);
     void* args[] = {(void*)&run, (void*)&P, (void*)&gains, (void*)&ywin, (void*)&summ, (void*)&traj};
     CE_CUDA(cudaLaunchKernel(kernel, dim3(grid), dim3(SIM_BLOCK), args, 0, st));
 }

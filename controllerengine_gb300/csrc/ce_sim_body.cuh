@@ -646,6 +646,222 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
     if (writer) summ[c] = sm;
 }
 
+// ---- the wide form of a session's simulation --------------------------------
+// One thread per candidate runs its horizon as one chain of dependent steps;
+// a batch too small to fill the GPU (a served request, a small tuning batch)
+// leaves that latency exposed.  Here four lanes (a quad) share a candidate,
+// sixteen candidates per block.  Lane q holds rows q*RS.. of the observer
+// update and q*RD.. of the plant update, with their matrix rows in registers;
+// every lane forms the step's scalars itself -- y and u (the compiled DC and U
+// programs), K.xh, C.xh, the NL terms -- from the same state in the same
+// order, so every value is formed by one lane with the operations and order of
+// sim_candidate and the rows are bit-identical to it.  The quad exchanges its
+// new state rows through a double-buffered slot in shared memory, one quad
+// barrier per step.  Luenberger observer, compiled programs, one plant for
+// all candidates.
+// slot: xh_hi, xh_lo (MAXS each), xp_hi, xp_lo (MAXD each); a stride of 36 words
+// keeps rows 16-byte aligned and the 16-byte loads of a warp's eight candidates
+// on disjoint banks
+constexpr int SW_XH_HI = 0, SW_XH_LO = MAXS, SW_XP_HI = 2 * MAXS, SW_XP_LO = 2 * MAXS + MAXD, SW_STRIDE = 36;
+
+template <int NSC, int NDC, class Chains>
+__device__ __forceinline__ void sim_wide(const Run& run, const Plant& P, const float* __restrict__ gains,
+                                         float* __restrict__ ywin, SimSummary* __restrict__ summ,
+                                         float* __restrict__ traj) {
+    static_assert(!Chains::kSmem, "the wide form runs compiled programs");
+    static_assert(NSC % SW_LANES == 0 && NDC % SW_LANES == 0, "the rows split evenly over the quad");
+    constexpr int RS = NSC / SW_LANES, RD = NDC / SW_LANES;
+    __shared__ __align__(16) float slots[2][SW_CPB * SW_STRIDE];
+    __shared__ float stage[8][SW_CPB];
+    const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
+    const unsigned qm = 0xFu << (threadIdx.x & 28);
+    const int64_t c = (int64_t)blockIdx.x * SW_CPB + cl;
+    if (c >= run.n) return;  // the whole quad leaves together
+    const typename Chains::template Local<NDC> Lc(run, P, c);
+    const int ns = run.ns;
+    const float* row = gains + c * run.cuda_w;
+    float K[NSC], sc[NSC], Lr[RS], sb[RS], sai[RS][NSC], dbu[RD], dai[RD][NDC], dbw[RD][MAXW];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) {
+        K[i] = i < ns ? row[i] : 0.0f;
+        sc[i] = Lc.sc(i);
+    }
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+        const int i = q * RS + rr;
+        Lr[rr] = i < ns ? row[ns + i] : 0.0f;
+        sb[rr] = Lc.sb(i);
+#pragma unroll
+        for (int j = 0; j < NSC; ++j) sai[rr][j] = Lc.sai(i, j);
+    }
+#pragma unroll
+    for (int rr = 0; rr < RD; ++rr) {
+        const int i = q * RD + rr;
+        dbu[rr] = Lc.bu(i);
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k) dbw[rr][k] = Lc.bw(i, k);
+#pragma unroll
+        for (int j = 0; j < NDC; ++j) dai[rr][j] = Lc.ai(i, j);
+    }
+    const float N = row[2 * ns], sd = Lc.sd();
+    {
+        float* s0 = slots[0] + cl * SW_STRIDE;
+#pragma unroll
+        for (int rr = 0; rr < RS; ++rr) s0[SW_XH_HI + q * RS + rr] = s0[SW_XH_LO + q * RS + rr] = 0.0f;
+#pragma unroll
+        for (int rr = 0; rr < RD; ++rr) s0[SW_XP_HI + q * RD + rr] = s0[SW_XP_LO + q * RD + rr] = 0.0f;
+    }
+    __syncwarp(qm);
+    float xh_hi[NSC], xh_lo[NSC], xp_hi[NDC], xp_lo[NDC];
+#pragma unroll
+    for (int i = 0; i < NSC; ++i) xh_hi[i] = xh_lo[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NDC; ++i) xp_hi[i] = xp_lo[i] = 0.0f;
+    bool poisS = false, poisD = false;
+    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float* wrow = ywin + c * (int64_t)run.fit_pitch;
+    const int T = run.time;
+    for (int t = 0; t < T; ++t) {
+        const float* cur = slots[t & 1] + cl * SW_STRIDE;
+        float* nxt = slots[(t + 1) & 1] + cl * SW_STRIDE;
+        const float padS = poisS ? CUDART_NAN_F : 0.0f;
+        const float padD = poisD ? CUDART_NAN_F : 0.0f;
+        // plant output
+        const float y = Chains::dc(P, Lc, xp_hi, nullptr);
+        if (q == 0) {
+            // fit window, steady-state sum, extremes, optional full trajectory
+            const int w = t - run.fit_start_id;
+            if (w >= 0 && w < run.fit_steps) {
+                stage[w & 7][cl] = y;
+                if ((w & 7) == 7 || w == run.fit_steps - 1 || t == T - 1) {
+                    float4 a, b;
+                    a.x = stage[0][cl]; a.y = stage[1][cl]; a.z = stage[2][cl]; a.w = stage[3][cl];
+                    b.x = stage[4][cl]; b.y = stage[5][cl]; b.z = stage[6][cl]; b.w = stage[7][cl];
+                    float4* dst = reinterpret_cast<float4*>(wrow + (w & ~7));
+                    dst[0] = a;
+                    dst[1] = b;
+                }
+            }
+            if (t >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            ymax = fmaxf(ymax, y);
+            ymin = fminf(ymin, y);
+            if (run.store_traj) traj[c * (int64_t)T + t] = y;
+        }
+        // controller output
+        float kx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) kx = __fmaf_rn(K[i], xh_hi[i], kx);
+        if (NSC < MAXS) kx = __fadd_rn(kx, padS);
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) kx = __fmaf_rn(K[i], xh_lo[i], kx);
+        if (NSC < MAXS) kx = __fadd_rn(kx, padS);
+        const float ref = t < run.ref_step_id ? 0.0f : run.ref_amp;
+        const float u_raw = __fmaf_rn(N, ref, -kx);
+        const float u = Chains::u(P, Lc, xh_hi, nullptr, u_raw);
+        // observer output error
+        float yh = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(sc[i], xh_hi[i], yh);
+        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
+#pragma unroll
+        for (int i = 0; i < NSC; ++i) yh = __fmaf_rn(sc[i], xh_lo[i], yh);
+        if (NSC < MAXS) yh = __fadd_rn(yh, padS);
+        yh = __fmaf_rn(sd, u, yh);
+        const float yerr = __fsub_rn(y, yh);
+        // this lane's observer rows: increment, then double-float add on the
+        // row's old value (read from the slot: an index by lane would put the
+        // state arrays in local memory)
+        float nh[RS], nlo[RS];
+#pragma unroll
+        for (int rr = 0; rr < RS; ++rr) {
+            float h = __fmaf_rn(Lr[rr], yerr, __fmul_rn(sb[rr], u));
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) h = __fmaf_rn(sai[rr][j], xh_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) l = __fmaf_rn(sai[rr][j], xh_lo[j], l);
+            if (NSC < MAXS) {
+                h = __fadd_rn(h, padS);
+                l = __fadd_rn(l, padS);
+            }
+            nh[rr] = cur[SW_XH_HI + q * RS + rr];
+            nlo[rr] = cur[SW_XH_LO + q * RS + rr];
+            df_add(nh[rr], nlo[rr], h, l);
+        }
+        if (NSC < MAXS) {
+            bool bad = !isfinite(yerr) || !isfinite(u);
+#pragma unroll
+            for (int j = 0; j < NSC; ++j) bad = bad || !isfinite(xh_hi[j]) || !isfinite(xh_lo[j]);
+            poisS = poisS || bad;
+        }
+        // nonlinear terms over [xp_hi, y]
+        float W[MAXW];
+        Chains::nl(P, Lc, xp_hi, y, nullptr, W);
+        // this lane's plant rows
+        float ph[RD], plo[RD];
+#pragma unroll
+        for (int rr = 0; rr < RD; ++rr) {
+            float h = __fmul_rn(dbu[rr], u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(dbw[rr][k], W[k], h);
+            float l = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) h = __fmaf_rn(dai[rr][j], xp_hi[j], h);
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) l = __fmaf_rn(dai[rr][j], xp_lo[j], l);
+            if (NDC < MAXD) {
+                h = __fadd_rn(h, padD);
+                l = __fadd_rn(l, padD);
+            }
+            ph[rr] = cur[SW_XP_HI + q * RD + rr];
+            plo[rr] = cur[SW_XP_LO + q * RD + rr];
+            df_add(ph[rr], plo[rr], h, l);
+        }
+        if (NDC < MAXD) {
+            bool bad = !isfinite(u);
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) bad = bad || !isfinite(W[k]);
+#pragma unroll
+            for (int j = 0; j < NDC; ++j) bad = bad || !isfinite(xp_hi[j]) || !isfinite(xp_lo[j]);
+            poisD = poisD || bad;
+        }
+        // publish this lane's rows into the other buffer, then read the new state
+#pragma unroll
+        for (int rr = 0; rr < RS; ++rr) {
+            nxt[SW_XH_HI + q * RS + rr] = nh[rr];
+            nxt[SW_XH_LO + q * RS + rr] = nlo[rr];
+        }
+#pragma unroll
+        for (int rr = 0; rr < RD; ++rr) {
+            nxt[SW_XP_HI + q * RD + rr] = ph[rr];
+            nxt[SW_XP_LO + q * RD + rr] = plo[rr];
+        }
+        __syncwarp(qm);
+#pragma unroll
+        for (int i = 0; i < NSC; i += 4) {
+            const float4 a = *reinterpret_cast<const float4*>(nxt + SW_XH_HI + i);
+            const float4 b = *reinterpret_cast<const float4*>(nxt + SW_XH_LO + i);
+            xh_hi[i] = a.x; xh_hi[i + 1] = a.y; xh_hi[i + 2] = a.z; xh_hi[i + 3] = a.w;
+            xh_lo[i] = b.x; xh_lo[i + 1] = b.y; xh_lo[i + 2] = b.z; xh_lo[i + 3] = b.w;
+        }
+#pragma unroll
+        for (int i = 0; i < NDC; i += 4) {
+            const float4 a = *reinterpret_cast<const float4*>(nxt + SW_XP_HI + i);
+            const float4 b = *reinterpret_cast<const float4*>(nxt + SW_XP_LO + i);
+            xp_hi[i] = a.x; xp_hi[i + 1] = a.y; xp_hi[i + 2] = a.z; xp_hi[i + 3] = a.w;
+            xp_lo[i] = b.x; xp_lo[i + 1] = b.y; xp_lo[i + 2] = b.z; xp_lo[i + 3] = b.w;
+        }
+    }
+    if (q == 0) {
+        SimSummary sm;
+        sm.ysum = ysum;
+        sm.ymax = ymax;
+        sm.ymin = ymin;
+        sm.pad = 0.0f;
+        summ[c] = sm;
+    }
+}
+
 // The instruction tables of the plant, interpreted (any program, no compile step).
 struct TableChains {
     static constexpr bool kSmem = true;

@@ -125,3 +125,39 @@ def test_kalman_source_has_both_forms(mass_spring):
         src = s.specialised_source(0)
     assert "ce::sim_run<8, 4, cejit::Chains, ce::SIM_KALMAN_LANE>" in src
     assert "ce_sim_kalman_shared" in src and "ce::SIM_KALMAN_SHARED" in src
+
+
+_WIDE_SCRIPT = r"""
+import sys, numpy as np
+import controllerengine_gb300 as ce
+from controllerengine_gb300 import synth
+probs = [synth.mass_spring(300), synth.eight_state(n=200, time=1500, freq=60)]
+probs += [synth.random_shape(700 + k, n=150, time=900, freq=50) for k in range(6)]
+outs = []
+for p in probs:
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        _, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("yplant",))
+        outs.append(d["yplant"].ravel())
+        outs.append(s.evaluate(p.cuda_mx, p.info_mx).ravel())
+np.save(sys.argv[1], np.concatenate(outs))
+"""
+
+
+def test_wide_simulation_form_equals_one_thread_form(tmp_path):
+    """The wide simulation form (four lanes per candidate; CE_SIM_WIDE=1 forces it, =0 forbids it,
+    read once per process) gives the one-thread form's trajectories and rows bit for bit, for
+    every dimension class including the padded 4/4 class."""
+    import os
+    import subprocess
+    import sys
+    script = tmp_path / "wide_form.py"
+    script.write_text(_WIDE_SCRIPT)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("1", "0"):
+        out = tmp_path / f"wide{mode}.npy"
+        subprocess.run([sys.executable, str(script), str(out)], check=True, cwd=root,
+                       env={**os.environ, "CE_SIM_WIDE": mode, "PYTHONPATH": root})
+        res[mode] = np.load(out)
+    assert np.array_equal(res["1"].view(np.uint32), res["0"].view(np.uint32))
