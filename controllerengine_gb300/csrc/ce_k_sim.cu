@@ -40,34 +40,33 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const _
 // results are bit-identical to it.  The quad exchanges y, W and its new state
 // rows through the candidate's slot in shared memory: three quad barriers per
 // step.
-constexpr int WIDE_LANES = 4, WIDE_CPB = SIM_BLOCK / WIDE_LANES;  // candidates per block
 // words between consecutive fields of the block's table columns: with 17 the
 // four lanes of a quad, reading fields of their NL chains 24 fields apart, and
 // the warp's eight candidates, reading one field, fall on 32 different banks
-constexpr int WIDE_TS = WIDE_CPB + 1;
+constexpr int WIDE_TS = SW_CPB + 1;  // SW_LANES lanes per candidate, SW_CPB candidates per block
 // slot layout: the NL chains read [xp_hi, y] as columns 0..MAXD; rows are
 // 16-byte aligned, and a stride of 52 words puts the 16-byte loads of a warp's
 // eight candidates on disjoint banks
 constexpr int WS_XH_HI = 0, WS_XH_LO = 8, WS_XP_HI = 16, WS_Y = WS_XP_HI + MAXD, WS_XP_LO = 28, WS_W = 36,
               WS_STRIDE = 52;
-static_assert(MAXS == 8 && MAXD == 8 && MAXW == WIDE_LANES, "the quad splits 8 rows and 4 NL chains");
+static_assert(MAXS == 8 && MAXD == 8 && MAXW == SW_LANES, "the quad splits 8 rows and 4 NL chains");
 
 __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch, const float* __restrict__ gains,
                                                                float* __restrict__ ywin,
                                                                SimSummary* __restrict__ summ) {
     __shared__ float tab[RT_FIELDS * WIDE_TS];
-    __shared__ __align__(16) float slots[WIDE_CPB * WS_STRIDE];
-    __shared__ float stage[8][WIDE_CPB];
+    __shared__ __align__(16) float slots[SW_CPB * WS_STRIDE];
+    __shared__ float stage[8][SW_CPB];
     const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
     const unsigned qm = 0xFu << (threadIdx.x & 28);
-    const int64_t c = (int64_t)blockIdx.x * WIDE_CPB + cl;
+    const int64_t c = (int64_t)blockIdx.x * SW_CPB + cl;
     if (c >= launch.n) return;  // the whole quad leaves together
     const Run& run = run_of<true>(launch, c);
     {
         // the candidate's table column, copied once by its quad
         const float* __restrict__ g = launch.rg.tab + c;
         const int64_t gs = launch.rg.tab_stride;
-        for (int f = q; f < RT_FIELDS; f += WIDE_LANES) tab[f * WIDE_TS + cl] = g[(int64_t)f * gs];
+        for (int f = q; f < RT_FIELDS; f += SW_LANES) tab[f * WIDE_TS + cl] = g[(int64_t)f * gs];
     }
     float* st = slots + cl * WS_STRIDE;
     const int r0 = 2 * q;
@@ -400,7 +399,7 @@ static int dim_class(int d) { return d <= 4 ? 4 : 8; }
 int ragged_lanes_per_candidate() {
     static const int v = [] {
         const char* e = std::getenv("CE_RAGGED_WIDE");
-        return (e && e[0] == '0') ? 1 : WIDE_LANES;
+        return (e && e[0] == '0') ? 1 : SW_LANES;
     }();
     return v;
 }
@@ -433,9 +432,9 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
         // a ragged batch: every instance at the reference's padded width, its plant from the table
         if (precision == CE_PRECISION_FP64 || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
-        if (ragged_lanes_per_candidate() == WIDE_LANES && !traj) {
+        if (ragged_lanes_per_candidate() == SW_LANES && !traj) {
             prefer_shared((const void*)k_sim_ragged_wide);
-            k_sim_ragged_wide<<<(unsigned)((run.n + WIDE_CPB - 1) / WIDE_CPB), SIM_BLOCK, 0, st>>>(
+            k_sim_ragged_wide<<<(unsigned)((run.n + SW_CPB - 1) / SW_CPB), SIM_BLOCK, 0, st>>>(
                 run, gains, (float*)ywin, (SimSummary*)summ);
         } else {
             const size_t cols = (size_t)RT_FIELDS * SIM_BLOCK * sizeof(float);  // the candidates' table columns
