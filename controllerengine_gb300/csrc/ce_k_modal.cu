@@ -161,12 +161,18 @@ __device__ __forceinline__ int64_t fit_candidate(const Run& run, const int* coun
     return run.n;
 }
 
-template <typename R, typename Sum, bool RG = false>
+// CH window steps per chunk: each chunk spreads the basis of its steps over the
+// lanes, then accumulates them step by step, so every entry still takes one
+// fused multiply-add per step in the order of t whatever CH is.  Large batches
+// use 8 (small shared-memory footprint beside the FP64 eigensolves); a batch
+// too small to fill the GPU uses 32, which pays the chunk's basis latency and
+// barriers once per 32 steps of its latency-bound loop.
+template <typename R, typename Sum, bool RG = false, int CH = FIT_CHUNK>
 __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __restrict__ eig, const R* __restrict__ ywin,
                                                    const Sum* __restrict__ summ, R* __restrict__ ata,
                                                    R* __restrict__ atb, float* __restrict__ info,
                                                    const int* __restrict__ counts, const int* __restrict__ order) {
-    __shared__ __align__(16) R cb[FIT_CPB][FIT_CHUNK][FIT_PITCH];
+    __shared__ __align__(16) R cb[FIT_CPB][CH][FIT_PITCH];
     __shared__ __align__(16) R mp[FIT_CPB][MAXT][4];
     const int lane = threadIdx.x & 15;
     const int g = threadIdx.x >> 4;
@@ -228,13 +234,13 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __
     // Atb (row nc) are the lower triangle of one rank-1 accumulation of size
     // N = nc + 1, tiled into 4x4 blocks spread over the 16 lanes.  Each entry
     // is still one fused multiply-add per step in the order of t.
-    for (int e = lane; e < FIT_CHUNK * FIT_PITCH; e += 16) (&cb[g][0][0])[e] = R(0);
+    for (int e = lane; e < CH * FIT_PITCH; e += 16) (&cb[g][0][0])[e] = R(0);
     const int N = nc + 1, NB = (N + 3) >> 2, nblk = NB * (NB + 1) / 2;
     // basis work item k = (step k / unique, mode k % unique) of a chunk; lane l
-    // takes k = l, l + 16, ... < FIT_CHUNK * unique
+    // takes k = l, l + 16, ... < CH * unique
     const int s0 = lane / unique, m0 = lane - s0 * unique;
     const int ds = 16 / unique, dm = 16 - ds * unique;
-    const int items = FIT_CHUNK * unique;
+    const int items = CH * unique;
     const R* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
     const int steps = run.fit_steps;
@@ -257,11 +263,11 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __
         for (int r = 0; r < FIT_ROUNDS; ++r)
 #pragma unroll
             for (int k = 0; k < 16; ++k) acc[r][k] = R(0);
-        for (int w0 = 0; w0 < steps; w0 += FIT_CHUNK) {
-            if (lane < FIT_CHUNK) {
-                const int idx = w0 + lane;
+        for (int w0 = 0; w0 < steps; w0 += CH) {
+            for (int k = lane; k < CH; k += 16) {
+                const int idx = w0 + k;
                 const R yw = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
-                cb[g][lane][nc] = rsub(yw, yss);
+                cb[g][k][nc] = rsub(yw, yss);
             }
             int s = s0, md = m0;
             for (int k = lane; k < items; k += 16) {
@@ -283,7 +289,7 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __
                 }
             }
             __syncwarp(hmask);
-            const int cnt = min(FIT_CHUNK, steps - w0);
+            const int cnt = min(CH, steps - w0);
             for (int st = 0; st < cnt; ++st) {
                 const R* row = &cb[g][st][0];
                 if (act0) {
@@ -546,6 +552,18 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run_in, co
     }
 }
 
+// A batch whose fit grid holds at most two blocks per SM (n <= ~2,400
+// candidates at 8 per block) is latency-bound and runs 32-step chunks.
+static bool fit_long_chunks(int64_t n) {
+    static const int sms = [] {
+        int dev = 0, k = 0;
+        CE_CUDA(cudaGetDevice(&dev));
+        CE_CUDA(cudaDeviceGetAttribute(&k, cudaDevAttrMultiProcessorCount, dev));
+        return k;
+    }();
+    return (n + FIT_CPB - 1) / FIT_CPB <= 2 * (int64_t)sms;
+}
+
 void launch_fit(const Run& run, int precision, const void* eig, const void* ywin, const void* summ, void* ata,
                 void* atb, float* info, int* counts, int* order, cudaStream_t st) {
     const int grid = (int)((run.n + FIT_CPB - 1) / FIT_CPB);
@@ -575,7 +593,12 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
         k_fit<double, double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin,
                                                          (const double*)summ, (double*)ata, (double*)atb, info,
                                                          counts, order);
-    else
+    else if (fit_long_chunks(run.n)) {
+        prefer_shared((const void*)k_fit<float, SimSummary, false, 32>);
+        k_fit<float, SimSummary, false, 32><<<grid, FIT_BLOCK, 0, st>>>(
+            run, (const float*)eig, (const float*)ywin, (const SimSummary*)summ, (float*)ata, (float*)atb, info, counts,
+            order);
+    } else
         k_fit<float, SimSummary><<<grid, FIT_BLOCK, 0, st>>>(run, (const float*)eig, (const float*)ywin,
                                                             (const SimSummary*)summ, (float*)ata, (float*)atb, info,
                                                             counts, order);
