@@ -110,6 +110,7 @@ struct ce_session {
     // stream: host-buffer evaluations; fast: the FP32 stages (lowest
     // priority); side: the FP64 eigensolves (highest priority)
     cudaStream_t stream = nullptr, fast = nullptr, side = nullptr;
+    cudaStream_t side2 = nullptr;  // the nominal eigensolve of a small batch, beside LIN_A's
     cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
     cudaEvent_t ev_eig[ce::MAX_CHUNKS] = {}, ev_nom[ce::MAX_CHUNKS] = {};
     int64_t launches = 0;
@@ -337,6 +338,16 @@ void ensure_plant_table(ce_session* s, int precision) {
 // Chunks of one evaluation: 1 below 16,384 candidates per chunk, else
 // CE_CHUNKS (default 2: of 1, 2 and 4 chunks, 2 measured fastest on the
 // eight-state workload of 65,536 candidates).
+// Whether a single-chunk evaluation of n candidates runs the nominal eigensolve
+// over all candidates beside LIN_A's (n <= 4,096; CE_NOMINAL_ALL=0 never).
+bool concurrent_nominal(int64_t n) {
+    static const bool off = [] {
+        const char* e = std::getenv("CE_NOMINAL_ALL");
+        return e && e[0] == '0';
+    }();
+    return !off && n <= 4096;
+}
+
 int n_chunks(const ce_session* s, int64_t n) {
     static const int dflt = [] {
         const char* e = std::getenv("CE_CHUNKS");
@@ -420,16 +431,26 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     auto at = [](const void* p, int64_t off, size_t bytes) {
         return (void*)((const char*)p + (size_t)off * bytes);
     };
+    // A small single-chunk batch in mixed precision runs the nominal eigensolve
+    // over all its candidates on a third stream, concurrently with LIN_A's,
+    // instead of over LIN_A's list after it: the two are independent, and a
+    // batch that small leaves the GPU room for both.  Their work counters are
+    // cleared here, before either stream starts.
+    const bool nom_all = nch == 1 && prec == CE_PRECISION_MIXED && !ragged && concurrent_nominal(n);
+    cudaStream_t ns2 = s->side2;
+    if (nom_all) CE_CUDA(cudaMemsetAsync(b.nominal_count, 0, 3 * sizeof(int), st));
     CE_CUDA(cudaEventRecord(s->ev_fork, st));
     CE_CUDA(cudaStreamWaitEvent(fs, s->ev_fork, 0));
     CE_CUDA(cudaStreamWaitEvent(ss, s->ev_fork, 0));
+    if (nom_all) CE_CUDA(cudaStreamWaitEvent(ns2, s->ev_fork, 0));
     for (int k = 0; k < nch; ++k) {
         Run rc;
         int64_t off;
         chunk(k, rc, off);
         timed(0, ss, [&] {
             launch_lina_eig(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt, at(b.eig, off, 2 * nt * rsz),
-                            b.nominal + off, b.nominal_list + off, b.nominal_count + 3 * k, ss);
+                            b.nominal + off, nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, ss,
+                            !nom_all);
         });
         CE_CUDA(cudaEventRecord(s->ev_eig[k], ss));
     }
@@ -437,11 +458,12 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         Run rc;
         int64_t off;
         chunk(k, rc, off);
-        timed(4, ss, [&] {
-            launch_nominal(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal_list + off,
-                           b.nominal_count + 3 * k, b.nominal + off, ss);
+        cudaStream_t on = nom_all ? ns2 : ss;
+        timed(4, on, [&] {
+            launch_nominal(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt,
+                           nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, b.nominal + off, on);
         });
-        CE_CUDA(cudaEventRecord(s->ev_nom[k], ss));
+        CE_CUDA(cudaEventRecord(s->ev_nom[k], on));
     }
     timed(1, fs, [&] {
         float* tr = traj ? b.traj : nullptr;
@@ -709,6 +731,7 @@ void init_streams(ce_session* s) {
     CE_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
     CE_CUDA(cudaStreamCreateWithPriority(&s->fast, cudaStreamNonBlocking, prio_least));
     CE_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_greatest));
+    CE_CUDA(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, prio_greatest));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     for (int k = 0; k < MAX_CHUNKS; ++k) {
@@ -781,6 +804,7 @@ void destroy_session(ce_session* s) {
     }
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->side) cudaStreamDestroy(s->side);
+    if (s->side2) cudaStreamDestroy(s->side2);
     if (s->fast) cudaStreamDestroy(s->fast);
     if (s->ev_done) cudaEventDestroy(s->ev_done);
     delete s;

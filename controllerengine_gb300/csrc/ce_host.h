@@ -62,8 +62,10 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
 // LIN_A and its FP64 eigenvalues; candidates that pass the modal stability
 // test are appended to list, the others get nominal = -1.  count holds three
 // ints (reset here): the listed count and the work counters of both kernels.
+// list null: no list of stable candidates (the nominal eigensolve then runs on all);
+// clear: zero the work counters first (else the caller has).
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                     int* nominal, int* list, int* count, cudaStream_t st);
+                     int* nominal, int* list, int* count, cudaStream_t st, bool clear = true);
 // Nominal closed-loop stability (nominal = 1 / 0) of the listed candidates.
 void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                     const int* list, const int* count, int* nominal, cudaStream_t st);
@@ -108,6 +110,9 @@ void launch_sim_specialised(const void* kernel, const Run& run, const Plant& P, 
 // wide simulation form: not for the 4/4 class, and only when the one-thread grid
 // would occupy fewer than half the SMs (CE_SIM_WIDE=0 never, =1 always).
 bool use_wide_sim(int64_t n, int nsc, int ndc);
+// Whether a single-chunk evaluation of n candidates runs the nominal eigensolve on all
+// candidates beside LIN_A's (small batches; CE_NOMINAL_ALL=0 never).
+bool concurrent_nominal(int64_t n);
 
 // Blocks of SIM_BLOCK threads that cover the candidates (or list slots) of `run`.
 int sim_grid(const Run& run);

@@ -740,7 +740,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
                 out[2 * i + 1] = fi;
                 mx = fmaxf(mx, hypotf(fr, fi));
             });
-            if (Q.lead()) list_if_stable(mx > 1.0f, c, nominal, list, count);
+            if (Q.lead() && list) list_if_stable(mx > 1.0f, c, nominal, list, count);  // no list: nominal runs on all
         }
         __syncwarp();  // the slots are rewritten for the next matrices
     }
@@ -806,7 +806,10 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
 // Only the candidates k_lina_eig listed (those the modal stage does not flag
 // unstable, so the only ones the sweep reads) are solved, packed into full
 // warps; the work is independent of the modal stage, so this kernel runs
-// concurrently with it.
+// concurrently with it.  With no list (a small batch) every candidate is
+// solved, OPEN_A is formed here with LIN_A's own float operations, and the
+// kernel runs concurrently with k_lina_eig (which then lists nothing): the
+// flags of the candidates the modal stage flags are computed but never read.
 template <int EQ, bool RG = false>
 __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
@@ -815,13 +818,13 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
     extern __shared__ double smem[];
     const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
-    const int64_t listed = *count;
+    const int64_t listed = list ? (int64_t)*count : run.n;
     for (;;) {
         const int64_t base = take_work<EQ>(next);
         if (base >= listed) break;
         const int64_t idx = base + m;
         if (idx < listed) {
-            const int64_t c = list[idx];
+            const int64_t c = list ? (int64_t)list[idx] : idx;
             const Run& rn = run_of<RG>(run, c);
             const Plant& PP = plant_of<RG>(run, P, c);
             const int ns = rn.ns, nt = rn.nt, n2 = 2 * ns;
@@ -838,12 +841,15 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
                 const float Kj = row[j];
                 const float md = own ? 0.0f : PP.m_d, mcj = own ? tv.c(j) : PP.m_c[j], mbi = own ? tv.bu(i) : PP.m_b[i];
                 const float maij = own ? tv.a(i, j) : PP.m_a[i * MAXS + j];
+                // OPEN_A: LIN_A's entry as k_lina_eig stored it, or formed here by the same
+                // function when the two kernels run concurrently (mixed precision only)
+                const float oa = list ? la[i * nt + j] : lina_entry(PP, BankPlantValues{PP}, row, row + ns, ns, i, j);
                 if (fp64_form) {
-                    T(i, j) = (double)la[i * nt + j] - (double)md * (double)Li * (double)Kj;
+                    T(i, j) = (double)oa - (double)md * (double)Li * (double)Kj;
                     T(i, ns + j) = -((double)Li * (double)mcj);
                     T(ns + i, j) = (double)mbi * (double)Kj;
                 } else {
-                    T(i, j) = (double)__fsub_rn(la[i * nt + j], __fmul_rn(__fmul_rn(md, Li), Kj));
+                    T(i, j) = (double)__fsub_rn(oa, __fmul_rn(__fmul_rn(md, Li), Kj));
                     T(i, ns + j) = (double)(-__fmul_rn(Li, mcj));
                     T(ns + i, j) = (double)__fmul_rn(mbi, Kj);
                 }
@@ -952,8 +958,8 @@ static void nominal_q(const Run& run, const Plant& P, int precision, const float
 }
 
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                     int* nominal, int* list, int* count, cudaStream_t st) {
-    CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
+                     int* nominal, int* list, int* count, cudaStream_t st, bool clear) {
+    if (clear) CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
     switch (eig_lanes(run, run.n)) {
         case 1: lina_eig_q<1>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
         case 2: lina_eig_q<2>(run, P, precision, gains, lina, eig, nominal, list, count, st); break;
