@@ -263,7 +263,8 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
     drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
     many consecutive plants, ce_server_submit_plants), else a tuning request (distinct gain
     sets on one plant).  Saturation: 48 requests submitted at once, candidates/s until all are
-    done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, p50/p99 of submit ->
+    done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, then at 50 requests/s
+    (light load, when below that) for half as long; p50/p99 of submit ->
     results in the caller's buffer (measured by the server)."""
     import controllerengine_gb300 as ce
     from controllerengine_gb300 import synth
@@ -348,6 +349,27 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
             h.wait()
         wall = time.perf_counter() - t0
         st = srv.stats()
+        # light load: 50 requests/s, the low end of the serving configuration's arrival rates
+        # (when that is below 70% of saturation), where a request is mostly served alone
+        light = None
+        if 50.0 < rate:
+            srv.reset_stats()
+            hs = []
+            t0 = time.perf_counter()
+            t_next = t0
+            while t_next - t0 < max(3.0, seconds / 2):
+                now = time.perf_counter()
+                if now < t_next:
+                    time.sleep(t_next - now)
+                hs.append(draw_submit(srv)[1])
+                t_next += rng.exponential(1.0 / 50.0)
+            for h in hs:
+                h.wait()
+            sl = srv.stats()
+            light = {"offered_requests_per_s": 50.0, "requests": sl["completed"],
+                     "mean_batch": sl["batched_candidates"] / max(1, sl["batches"]),
+                     "latency_p50_ms": sl["latency_p50_ms"], "latency_p99_ms": sl["latency_p99_ms"],
+                     "latency_max_ms": sl["latency_max_ms"]}
     shapes = sorted({(c.statespace_dim, c.discrete_dim, c.time, c.freq) for c in cfgs})
     return {"request_mix": f"U[256, 16384] candidates on one of {len(problems)} models of the uneven-shape "
                            f"workload (dims 2..8, horizons 1e3..1e4, 50..400 sweep points), each with {n_plants} "
@@ -361,7 +383,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
             "achieved_candidates_per_s": offered / wall,
             "batches": st["batches"], "mean_batch": st["batched_candidates"] / max(1, st["batches"]),
             "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
-            "latency_max_ms": st["latency_max_ms"]}
+            "latency_max_ms": st["latency_max_ms"], "light_load": light}
 
 
 def monte_carlo_bench(n_plants: int, steps: int, warmup: int):
