@@ -111,6 +111,9 @@ struct ce_session {
     // priority); side: the FP64 eigensolves (highest priority)
     cudaStream_t stream = nullptr, fast = nullptr, side = nullptr;
     cudaStream_t side2 = nullptr;  // the nominal eigensolve of a small batch, beside LIN_A's
+    // the latency forms of a small batch (wide simulation, more lanes per matrix in the FP64
+    // eigensolves, the nominal eigensolve beside LIN_A's); a server's sessions run without them
+    bool small_forms = true;
     cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
     cudaEvent_t ev_eig[ce::MAX_CHUNKS] = {}, ev_nom[ce::MAX_CHUNKS] = {};
     int64_t launches = 0;
@@ -378,7 +381,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     Run r = make_run(s, plant, n);
     if (ragged) r.rg = *ragged;
     r.store_traj = traj ? 1 : 0;
-    r.eig_lanes = s->tuning.eig_lanes;
+    // without the small-batch forms the eigensolves keep two lanes per matrix
+    r.eig_lanes = s->tuning.eig_lanes != 0 || s->small_forms ? s->tuning.eig_lanes : 2;
     r.eig_blocks = s->tuning.eig_blocks_per_sm;
     if (per_candidate) {
         r.mc.tab = s->d_mc_tab;
@@ -436,7 +440,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // instead of over LIN_A's list after it: the two are independent, and a
     // batch that small leaves the GPU room for both.  Their work counters are
     // cleared here, before either stream starts.
-    const bool nom_all = nch == 1 && prec == CE_PRECISION_MIXED && !ragged && concurrent_nominal(n);
+    const bool nom_all = s->small_forms && nch == 1 && prec == CE_PRECISION_MIXED && !ragged && concurrent_nominal(n);
     cudaStream_t ns2 = s->side2;
     if (nom_all) CE_CUDA(cudaMemsetAsync(b.nominal_count, 0, 3 * sizeof(int), st));
     CE_CUDA(cudaEventRecord(s->ev_fork, st));
@@ -488,8 +492,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
             }
         } else if (sk) {
             // a batch too small to fill the GPU runs four lanes per candidate
-            const bool wide = sk.wide && use_wide_sim(n, s->cfg.statespace_dim <= 4 ? 4 : 8,
-                                                      s->cfg.discrete_dim <= 4 ? 4 : 8);
+            const bool wide = s->small_forms && sk.wide &&
+                              use_wide_sim(n, s->cfg.statespace_dim <= 4 ? 4 : 8, s->cfg.discrete_dim <= 4 ? 4 : 8);
             launch_sim_specialised(wide ? sk.wide : sk.main, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr,
                                    fs, wide);
         } else {
@@ -1338,6 +1342,7 @@ const Plant* session_plant(const ce_session* s, int plant) { return &s->plants[p
 const ce_config* session_config(const ce_session* s) { return &s->cfg; }
 int session_plants(const ce_session* s) { return s->n_plants; }
 const std::string& session_plant_error(const ce_session* s, int plant) { return s->plant_err[plant]; }
+void session_set_small_batch_forms(ce_session* s, bool on) { s->small_forms = on; }
 
 // Everything an evaluation of up to n candidates would otherwise allocate or
 // build on first use: the scratch buffers (none for n = 0), the FP64 sweep

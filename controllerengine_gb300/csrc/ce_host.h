@@ -149,6 +149,10 @@ const std::string& session_plant_error(const ce_session* s, int plant);
 // Allocate and build, now, what an evaluation of up to n candidates (n = 0: no scratch; with
 // `plants`: on per-candidate plants) would otherwise set up on first use.
 void session_prepare(ce_session* s, int64_t n, bool plants);
+// The latency forms of small batches (on by default): the wide simulation, more lanes per
+// matrix in the FP64 eigensolves, the nominal eigensolve beside LIN_A's.  They shorten an
+// evaluation on an idle GPU and cost throughput when batches share it, so a server turns them off.
+void session_set_small_batch_forms(ce_session* s, bool on);
 // Lanes per candidate of a ragged batch's simulation (4: the wide form; 1: one thread each).
 int ragged_lanes_per_candidate();
 Run session_run(const ce_session* s, int plant, int64_t n);
