@@ -262,7 +262,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
     of its plant (synth.perturbed_plants); a request carries U[256, 16384] candidates on a model
     drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
     many consecutive plants, ce_server_submit_plants), else a tuning request (distinct gain
-    sets on one plant).  Saturation: 48 requests submitted at once, candidates/s until all are
+    sets on one plant).  Saturation: 96 requests submitted at once, candidates/s until all are
     done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, then at 50 requests/s
     (light load, when below that) for half as long; p50/p99 of submit ->
     results in the caller's buffer (measured by the server)."""
@@ -317,7 +317,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
             for h in hs:
                 h.wait()
         refused[0] = 0
-        reqs = [draw() for _ in range(48)]
+        reqs = [draw() for _ in range(96)]
         total = sum(r[3].shape[0] for r in reqs)
         t0 = time.perf_counter()
         hs = []
