@@ -257,7 +257,8 @@ def serving_models(k: int = 16, seed: int = 5):
 
 
 def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7,
-                  precision: str = "mixed", n_plants: int = 16384, mc_fraction: float = 0.25):
+                  precision: str = "mixed", n_plants: int = 16384, mc_fraction: float = 0.25,
+                  max_wait_us: int = 0):
     """Request serving (ce_server_*): every model of `problems` holds n_plants perturbed copies
     of its plant (synth.perturbed_plants); a request carries U[256, 16384] candidates on a model
     drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
@@ -301,7 +302,8 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
 
     refused = [0]
     models = [(c, ps, n_plants) for c, ps in zip(cfgs, plant_sets)]
-    with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes, precision=precision) as srv:
+    with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes, precision=precision,
+                   max_wait_us=max_wait_us) as srv:
         # warm-up: every lane sizes its scratch for a full batch of every model, and compiles
         # the per-candidate-plant kernels of every model
         for _ in range(lanes):
@@ -377,7 +379,8 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
                            "consecutive plants), the rest tuning requests (distinct gain sets on one plant)",
             "precision": precision,
             "models": [list(x) for x in shapes],
-            "lanes": lanes, "max_batch": st["capacity"], "saturation_candidates_per_s": sat,
+            "lanes": lanes, "max_batch": st["capacity"], "max_wait_us": max_wait_us,
+            "saturation_candidates_per_s": sat,
             "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
             "requests": st["completed"], "monte_carlo_requests": n_mc, "refused_requests": refused[0],
             "achieved_candidates_per_s": offered / wall,
@@ -630,6 +633,8 @@ def main():
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch settings")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="Poisson serving run (0: skip)")
+    ap.add_argument("--serve-max-wait-us", type=int, default=0,
+                    help="serving: how long a partial batch may wait for more requests")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
     ap.add_argument("--ref-gpu-build", type=int, default=1,
                     help="reference arm: also time the reference's own kernels + host stages (0: skip)")
@@ -844,7 +849,7 @@ def main():
         line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
     if rank == 0 and a.serve_seconds > 0:
         models = serving_models()
-        line["serving"] = serving_bench(models, a.serve_seconds)
+        line["serving"] = serving_bench(models, a.serve_seconds, max_wait_us=a.serve_max_wait_us)
         # the same request stream served by the plain FP64 form (at its own 70% load)
         line["serving"]["fp64_form"] = {k: v for k, v in serving_bench(models, a.serve_seconds / 2,
                                                                        precision="fp64").items()
