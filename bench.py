@@ -159,10 +159,40 @@ def cpu_baseline(problem, seconds: float, threads: int):
     rate = probe / max(time.perf_counter() - t0, 1e-6)
     n_s = int(min(n_total, max(probe, rate * seconds)))
     t0 = time.perf_counter()
-    orc.evaluate(problem.cuda_mx[:n_s], problem.info_mx[:n_s])
+    rows = orc.evaluate(problem.cuda_mx[:n_s], problem.info_mx[:n_s])
     dt = time.perf_counter() - t0
     return {"value": n_s / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n_s} of the {n_total} candidates, full horizon, oracle C port with OpenMP ({dt:.1f} s)"}
+            "sample": f"{n_s} of the {n_total} candidates, full horizon, oracle C port with OpenMP ({dt:.1f} s)"}, rows
+
+
+def parity_report(gpu, ref, cfg):
+    """The engine's rows against the oracle's (the reference method restated on the CPU, its own
+    trajectories, eigenvalues and libm) on the same candidates: identity of the pass/fail classes
+    (modal-unstable, nominal-unstable, eig-fail, margin status), the gain / phase margins in dB /
+    deg, and the per-term difference of the scored candidates.  Fit-derived terms (wn, zeta,
+    behaviour error) carry the FP32 normal equations' sensitivity to last-ulp libm differences."""
+    s, am, fr = cfg.info_scoring, cfg.info_allmargin, cfg.info_freqresp
+    def classes(x):
+        return np.stack([x[:, s + 1] >= cfg.unstable_err, x[:, s + 2] == np.float32(cfg.unstable_err),
+                         x[:, s + 2] == np.float32(cfg.eig_fail_err), x[:, am + 3] == 1.0], axis=1)
+    cg, co = classes(gpu), classes(ref)
+    same = (cg == co).all(axis=1)
+    scored = same & (gpu[:, am + 3] == 1.0) & ~cg[:, 0]
+    def stats(e):
+        e = e[np.isfinite(e)]
+        return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)), "max": float(e.max())} if e.size \
+            else None
+    g64, r64 = gpu.astype(np.float64), ref.astype(np.float64)
+    absd = {"gm_db": stats(np.abs(g64[scored, am] - r64[scored, am])),
+            "pm_deg": stats(np.abs(g64[scored, am + 1] - r64[scored, am + 1]))}
+    terms = {"total_score": s, "behaviour_err": s + 1, "margin_err": s + 2, "wn": fr, "zeta": fr + 1,
+             "overshoot": fr + 2, "yss": fr + 3, "gm_db": am, "pm_deg": am + 1, "dm_ms": am + 2, "b_pc": am + 4}
+    rel = {k: stats(np.abs(g64[scored, c] - r64[scored, c]) / np.maximum(np.abs(r64[scored, c]), 1e-6))
+           for k, c in terms.items()}
+    return {"candidates": int(len(gpu)), "class_identity": float(same.mean()),
+            "class_mismatches": int((~same).sum()), "scored_compared": int(scored.sum()),
+            "margin_abs_diff": absd, "relative_diff": rel,
+            "margins_within_1e-3": bool(all(v is None or v["max"] <= 1e-3 for v in absd.values()))}
 
 
 def reference_gpu_build(problem, threads: int, sample: int = 4096):
@@ -558,7 +588,7 @@ def small_bench(steps: int, warmup: int, cpu: bool):
             ms = e0.elapsed_time(e1) / steps
         res[prec] = {"candidates_per_s": 1024 / (ms * 1e-3), "ms_per_step": ms}
     if cpu:
-        res["cpu_baseline"] = cpu_baseline(p, 5.0, os.cpu_count() or 1)
+        res["cpu_baseline"] = cpu_baseline(p, 5.0, os.cpu_count() or 1)[0]
     return res
 
 
@@ -613,7 +643,7 @@ def kalman_bench(n: int, steps: int, warmup: int, cpu_seconds: float):
     res["distinct_noise"] = _kalman_time(q, n, max(1, steps - 1), 1)
     res["candidates_per_s"] = res["pooled_noise"]["candidates_per_s"]
     if cpu_seconds > 0:
-        res["cpu_baseline"] = cpu_baseline(p, cpu_seconds, os.cpu_count() or 1)
+        res["cpu_baseline"] = cpu_baseline(p, cpu_seconds, os.cpu_count() or 1)[0]
     return res
 
 
@@ -641,6 +671,8 @@ def main():
     ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
     ap.add_argument("--uneven-instances", type=int, default=16384, help="uneven-size ragged batch (0: skip)")
     ap.add_argument("--small-steps", type=int, default=10, help="the small mass-spring case (0: skip)")
+    ap.add_argument("--eig-compare", type=int, default=1,
+                    help="also run the other eigensolve arithmetic on the batch and compare rows (0: skip)")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -725,6 +757,7 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / a.steps
     value = world * n * a.steps / (ms * 1e-3)
+    value_rows = info_out.cpu().numpy()  # the rows of the timed steps (identical in every step)
 
     # ---- e2e through the C ABI with pinned host buffers ----
     pin_g = torch.from_numpy(problem.cuda_mx).pin_memory().numpy()
@@ -735,7 +768,7 @@ def main():
     from controllerengine_gb300 import _ffi
     fp = lambda arr: arr.ctypes.data_as(_ffi._FP)
     lib.ce_evaluate(sess._h, 0, n, fp(pin_g), fp(pin_i), fp(pin_o))  # warm
-    e2e_steps = max(2, min(a.steps, 3))
+    e2e_steps = a.steps  # the same step count as the device-resident value
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
@@ -770,6 +803,33 @@ def main():
                 "speedup_of_mixed": (world * n / (ms_per_step * 1e-3)) / (world * n / (f_ms * 1e-3)),
                 "mixed_vs_fp64": precision_report(mixed_rows, fp64_rows, cfg)}
         sess.set_precision("mixed")
+
+    # ---- eigensolve arithmetic: the separate (reference) form on the same batch ----
+    eig_cmp = None
+    if a.eig_compare:
+        arith0 = sess.eig_arith
+        other = "separate" if arith0 == "fused" else "fused"
+        sess.set_eig_arith(other)
+        for _ in range(2):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        o_rows = info_out.cpu().numpy()
+        sess.set_profiling(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        o_stages = {k: v[0] / 2 for k, v in sess.stage_times().items()}
+        sess.set_profiling(False)
+        sess.set_eig_arith(arith0)
+        rep = parity_report(value_rows, o_rows, cfg)
+        eig_cmp = {"default": arith0, "other": other, "other_ms_per_step": e0.elapsed_time(e1) / 2,
+                   "other_stages_ms_per_step": o_stages,
+                   "rows_bit_identical": float((value_rows.view(np.uint32) == o_rows.view(np.uint32)).all(axis=1).mean()),
+                   "class_identity": rep["class_identity"], "margin_abs_diff": rep["margin_abs_diff"]}
 
     # ---- roofline of the dominant kernel ----
     per_launch = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
@@ -836,6 +896,7 @@ def main():
                            "peak_gbs": hbm_peak},
         "peaks_measured": {"fp32_tops": fp32_rate / 1e12, "fp64_tops": fp64_rate / 1e12},
         "fp64_form": fp64,
+        "eig_arith": eig_cmp,
         "clocks": clk,
         "wall_s_timed": wall,
     }
@@ -857,7 +918,12 @@ def main():
                                                  "achieved_candidates_per_s", "latency_p50_ms", "latency_p99_ms",
                                                  "latency_max_ms", "requests", "monte_carlo_requests")}
     if rank == 0 and not a.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"], orc_rows = cpu_baseline(problem, a.cpu_seconds, os.cpu_count() or 1)
+        # the rows the oracle computed for the baseline, against the engine's rows of the timed steps
+        line["parity"] = parity_report(value_rows[:len(orc_rows)], orc_rows, cfg)
+        line["parity"]["what"] = ("engine rows of the timed headline batch (default eigensolve arithmetic: "
+                                  f"{sess.eig_arith}) vs the oracle's rows (the reference's separate arithmetic) "
+                                  "on the cpu_baseline sample")
     if rank == 0:
         print(json.dumps(line), flush=True)
     sess.close()

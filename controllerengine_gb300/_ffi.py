@@ -19,10 +19,13 @@ MAX_NONLIN_DIM = 4
 MAX_TOTAL_DIM = 16
 PRECISION_MIXED = 0
 PRECISION_FP64 = 1
+EIG_ARITH_SEPARATE = 0
+EIG_ARITH_FUSED = 1
 
 EXPORTED_SYMBOLS = (
     "ce_last_error", "ce_version", "ce_parse_config", "ce_decode_instructions",
     "ce_session_create", "ce_session_destroy", "ce_session_set_precision", "ce_session_get_config",
+    "ce_session_set_eig_arith", "ce_session_get_eig_arith",
     "ce_evaluate", "ce_evaluate_diagnostics", "ce_evaluate_device", "ce_session_kernel_launches",
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
@@ -124,6 +127,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_session_destroy.argtypes = [C.c_void_p]
     lib.ce_session_destroy.restype = None
     lib.ce_session_set_precision.argtypes = [C.c_void_p, C.c_int32]
+    lib.ce_session_set_eig_arith.argtypes = [C.c_void_p, C.c_int32]
+    lib.ce_session_get_eig_arith.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     lib.ce_session_get_config.argtypes = [C.c_void_p, C.POINTER(ce_config)]
     lib.ce_evaluate.argtypes = [C.c_void_p, C.c_int32, C.c_int64, _FP, _FP, _FP]
     lib.ce_evaluate_diagnostics.argtypes = [C.c_void_p, C.c_int32, C.c_int64, _FP, _FP, _FP,

@@ -114,6 +114,7 @@ struct ce_session {
     // the latency forms of a small batch (wide simulation, more lanes per matrix in the FP64
     // eigensolves, the nominal eigensolve beside LIN_A's); a server's sessions run without them
     bool small_forms = true;
+    int eig_arith = CE_EIG_ARITH_FUSED;  // arithmetic of the FP64 eigensolves
     cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
     cudaEvent_t ev_eig[ce::MAX_CHUNKS] = {}, ev_nom[ce::MAX_CHUNKS] = {};
     int64_t launches = 0;
@@ -384,6 +385,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // without the small-batch forms the eigensolves keep two lanes per matrix
     r.eig_lanes = s->tuning.eig_lanes != 0 || s->small_forms ? s->tuning.eig_lanes : 2;
     r.eig_blocks = s->tuning.eig_blocks_per_sm;
+    r.eig_fused = s->eig_arith == CE_EIG_ARITH_FUSED ? 1 : 0;
     if (per_candidate) {
         r.mc.tab = s->d_mc_tab;
         r.mc.np = s->n_plants;
@@ -1415,6 +1417,21 @@ CE_EXPORT int ce_ragged_stage_times(ce_ragged* r, double* ms, int64_t* launches)
     return guarded([&] {
         if (!r) fail("null ragged batch");
         if (ce_session_stage_times(r->s, ms, launches)) fail("{}", g_last_error);
+    });
+}
+
+CE_EXPORT int ce_session_set_eig_arith(ce_session* s, int32_t arith) {
+    return guarded([&] {
+        if (!s) fail("null session");
+        if (arith != CE_EIG_ARITH_SEPARATE && arith != CE_EIG_ARITH_FUSED) fail("unknown eigensolve arithmetic {}", arith);
+        s->eig_arith = arith;
+    });
+}
+
+CE_EXPORT int ce_session_get_eig_arith(const ce_session* s, int32_t* arith) {
+    return guarded([&] {
+        if (!s || !arith) fail("null argument");
+        *arith = s->eig_arith;
     });
 }
 

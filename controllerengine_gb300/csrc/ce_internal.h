@@ -135,6 +135,7 @@ struct Run {
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
     int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2, 4, 8 or 16; 0: by batch size)
     int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)
+    int eig_fused;   // FP64 eigensolves: 1 fuses each multiply-add into one DFMA, 0 rounds both
     // floats (or reals) per candidate in the LIN_A, eigenvalue, AtA and Atb buffers:
     // nt^2, 2nt, (2nt)^2, 2nt for a uniform evaluation, the maxima for a ragged one
     int lina_slot, eig_slot, ata_slot, atb_slot;

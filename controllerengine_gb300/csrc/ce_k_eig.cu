@@ -80,20 +80,37 @@ struct Quad {
     __device__ __forceinline__ bool lead() const { return q == 0; }
 };
 
+// The eigensolver's arithmetic: F = false rounds every product and every sum
+// separately (the reference's Eigen stages compiled without contraction, a
+// multiply and an add per multiply-add); F = true fuses each x + a b and
+// x - a b into one DFMA, which halves the FP64 instructions of the reflector
+// updates.  The operation sequence is otherwise the same in both forms.
+template <bool F>
+__device__ __forceinline__ double mac(double x, double a, double b) {
+    if constexpr (F) return __fma_rn(a, b, x);
+    else return __dadd_rn(x, __dmul_rn(a, b));
+}
+template <bool F>
+__device__ __forceinline__ double nmac(double x, double a, double b) {
+    if constexpr (F) return __fma_rn(-a, b, x);
+    else return __dsub_rn(x, __dmul_rn(a, b));
+}
+
 // Householder of the column segment T(r0 .. r0+m-1, col): returns tau and beta
 // (read phase only; the caller writes the essential part).
+template <bool F>
 __device__ __forceinline__ void house_coeffs(const SMat& T, int r0, int m, int col, double& tau, double& beta,
                                              double& d) {
     const double c0 = T(r0, col);
     double tail = 0.0;
-    for (int k = r0 + 1; k < r0 + m; ++k) tail = __dadd_rn(tail, __dmul_rn(T(k, col), T(k, col)));
+    for (int k = r0 + 1; k < r0 + m; ++k) tail = mac<F>(tail, T(k, col), T(k, col));
     if (m == 1) tail = 0.0;
     if (tail <= DMIN_) {
         tau = 0.0;
         beta = c0;
         d = 0.0;
     } else {
-        beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+        beta = sqrt(mac<F>(tail, c0, c0));
         if (c0 >= 0.0) beta = -beta;
         d = __dsub_rn(c0, beta);
         tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
@@ -101,17 +118,18 @@ __device__ __forceinline__ void house_coeffs(const SMat& T, int r0, int m, int c
 }
 
 // Householder of a short register vector v[0..m-1] (m = 2 or 3).
+template <bool F>
 __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, double& tau, double& beta) {
     const double c0 = v[0];
     double tail = __dmul_rn(v[1], v[1]);
-    if (m == 3) tail = __dadd_rn(tail, __dmul_rn(v[2], v[2]));
+    if (m == 3) tail = mac<F>(tail, v[2], v[2]);
     if (tail <= DMIN_) {
         tau = 0.0;
         beta = c0;
         ess[0] = 0.0;
         ess[1] = 0.0;
     } else {
-        beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+        beta = sqrt(mac<F>(tail, c0, c0));
         if (c0 >= 0.0) beta = -beta;
         const double d = __dsub_rn(c0, beta);
         ess[0] = __ddiv_rn(v[1], d);
@@ -125,7 +143,7 @@ __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, d
 // T(r0), T(r0) -= tau tmp, T(r0+k+1) -= tmp (tau ess_k).  Four columns are
 // processed per iteration so that their independent chains overlap; each
 // column's operations and their order are unchanged.
-template <class Qd, typename E>
+template <bool F, class Qd, typename E>
 __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, int m, int c0, int c1, E ess_at,
                                            double tau) {
     constexpr int S = Qd::N;
@@ -144,18 +162,18 @@ __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, i
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(ek, T(r0 + 1 + k, j + u * S)));
+            for (int u = 0; u < 4; ++u) t[u] = mac<F>(t[u], ek, T(r0 + 1 + k, j + u * S));
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             t[u] = __dadd_rn(t[u], T(r0, j + u * S));
-            T(r0, j + u * S) = __dsub_rn(T(r0, j + u * S), __dmul_rn(tau, t[u]));
+            T(r0, j + u * S) = nmac<F>(T(r0, j + u * S), tau, t[u]);
         }
         for (int k = 0; k < m - 1; ++k) {
             const double te = __dmul_rn(tau, ess_at(k));
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                T(r0 + 1 + k, j + u * S) = __dsub_rn(T(r0 + 1 + k, j + u * S), __dmul_rn(t[u], te));
+                T(r0 + 1 + k, j + u * S) = nmac<F>(T(r0 + 1 + k, j + u * S), t[u], te);
         }
     }
     if (j + S < c1) {
@@ -166,34 +184,34 @@ __device__ __forceinline__ void house_left(const SMat& T, const Qd& Q, int r0, i
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
-            for (int u = 0; u < 2; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(ek, T(r0 + 1 + k, j + u * S)));
+            for (int u = 0; u < 2; ++u) t[u] = mac<F>(t[u], ek, T(r0 + 1 + k, j + u * S));
         }
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             t[u] = __dadd_rn(t[u], T(r0, j + u * S));
-            T(r0, j + u * S) = __dsub_rn(T(r0, j + u * S), __dmul_rn(tau, t[u]));
+            T(r0, j + u * S) = nmac<F>(T(r0, j + u * S), tau, t[u]);
         }
         for (int k = 0; k < m - 1; ++k) {
             const double te = __dmul_rn(tau, ess_at(k));
 #pragma unroll
             for (int u = 0; u < 2; ++u)
-                T(r0 + 1 + k, j + u * S) = __dsub_rn(T(r0 + 1 + k, j + u * S), __dmul_rn(t[u], te));
+                T(r0 + 1 + k, j + u * S) = nmac<F>(T(r0 + 1 + k, j + u * S), t[u], te);
         }
         j += 2 * S;
     }
     for (; j < c1; j += S) {
         double tmp = __dmul_rn(ess_at(0), T(r0 + 1, j));
-        for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(ess_at(k), T(r0 + 1 + k, j)));
+        for (int k = 1; k < m - 1; ++k) tmp = mac<F>(tmp, ess_at(k), T(r0 + 1 + k, j));
         tmp = __dadd_rn(tmp, T(r0, j));
-        T(r0, j) = __dsub_rn(T(r0, j), __dmul_rn(tau, tmp));
-        for (int k = 0; k < m - 1; ++k) T(r0 + 1 + k, j) = __dsub_rn(T(r0 + 1 + k, j), __dmul_rn(tmp, __dmul_rn(tau, ess_at(k))));
+        T(r0, j) = nmac<F>(T(r0, j), tau, tmp);
+        for (int k = 0; k < m - 1; ++k) T(r0 + 1 + k, j) = nmac<F>(T(r0 + 1 + k, j), tmp, __dmul_rn(tau, ess_at(k)));
     }
 }
 
 // H from the right on rows r0..r1-1 (split over the group), columns
 // c0..c0+m-1.  Per row: tmp = T(i,c0+1..).ess + T(i,c0), T(i,c0) -= tau tmp,
 // T(i,c0+k+1) -= ess_k (tau tmp).  Four rows per iteration.
-template <class Qd, typename E>
+template <bool F, class Qd, typename E>
 __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, int r1, int c0, int m, E ess_at,
                                             double tau) {
     constexpr int S = Qd::N;
@@ -212,20 +230,20 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(T(i + u * S, c0 + 1 + k), ek));
+            for (int u = 0; u < 4; ++u) t[u] = mac<F>(t[u], T(i + u * S, c0 + 1 + k), ek);
         }
         double tt[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             t[u] = __dadd_rn(t[u], T(i + u * S, c0));
-            T(i + u * S, c0) = __dsub_rn(T(i + u * S, c0), __dmul_rn(tau, t[u]));
+            T(i + u * S, c0) = nmac<F>(T(i + u * S, c0), tau, t[u]);
             tt[u] = __dmul_rn(tau, t[u]);
         }
         for (int k = 0; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                T(i + u * S, c0 + 1 + k) = __dsub_rn(T(i + u * S, c0 + 1 + k), __dmul_rn(ek, tt[u]));
+                T(i + u * S, c0 + 1 + k) = nmac<F>(T(i + u * S, c0 + 1 + k), ek, tt[u]);
         }
     }
     if (i + S < r1) {
@@ -236,30 +254,30 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
         for (int k = 1; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
-            for (int u = 0; u < 2; ++u) t[u] = __dadd_rn(t[u], __dmul_rn(T(i + u * S, c0 + 1 + k), ek));
+            for (int u = 0; u < 2; ++u) t[u] = mac<F>(t[u], T(i + u * S, c0 + 1 + k), ek);
         }
         double tt[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             t[u] = __dadd_rn(t[u], T(i + u * S, c0));
-            T(i + u * S, c0) = __dsub_rn(T(i + u * S, c0), __dmul_rn(tau, t[u]));
+            T(i + u * S, c0) = nmac<F>(T(i + u * S, c0), tau, t[u]);
             tt[u] = __dmul_rn(tau, t[u]);
         }
         for (int k = 0; k < m - 1; ++k) {
             const double ek = ess_at(k);
 #pragma unroll
             for (int u = 0; u < 2; ++u)
-                T(i + u * S, c0 + 1 + k) = __dsub_rn(T(i + u * S, c0 + 1 + k), __dmul_rn(ek, tt[u]));
+                T(i + u * S, c0 + 1 + k) = nmac<F>(T(i + u * S, c0 + 1 + k), ek, tt[u]);
         }
         i += 2 * S;
     }
     for (; i < r1; i += S) {
         double tmp = __dmul_rn(T(i, c0 + 1), ess_at(0));
-        for (int k = 1; k < m - 1; ++k) tmp = __dadd_rn(tmp, __dmul_rn(T(i, c0 + 1 + k), ess_at(k)));
+        for (int k = 1; k < m - 1; ++k) tmp = mac<F>(tmp, T(i, c0 + 1 + k), ess_at(k));
         tmp = __dadd_rn(tmp, T(i, c0));
-        T(i, c0) = __dsub_rn(T(i, c0), __dmul_rn(tau, tmp));
+        T(i, c0) = nmac<F>(T(i, c0), tau, tmp);
         const double tt = __dmul_rn(tau, tmp);
-        for (int k = 0; k < m - 1; ++k) T(i, c0 + 1 + k) = __dsub_rn(T(i, c0 + 1 + k), __dmul_rn(ess_at(k), tt));
+        for (int k = 0; k < m - 1; ++k) T(i, c0 + 1 + k) = nmac<F>(T(i, c0 + 1 + k), ess_at(k), tt);
     }
 }
 
@@ -268,30 +286,30 @@ __device__ __forceinline__ void house_right(const SMat& T, const Qd& Q, int r0, 
 // Several columns (rows) per step: the work per element is a short chain of
 // dependent FP64 operations, and independent chains per lane hide most of
 // their latency.
-template <int M>
+template <bool F, int M>
 __device__ __forceinline__ void left_col(double& a0, double& a1, double& a2, double e0, double e1, double tau,
                                          double te0, double te1) {
     double t = __dmul_rn(e0, a1);
-    if (M == 3) t = __dadd_rn(t, __dmul_rn(e1, a2));
+    if (M == 3) t = mac<F>(t, e1, a2);
     t = __dadd_rn(t, a0);
-    a0 = __dsub_rn(a0, __dmul_rn(tau, t));
-    a1 = __dsub_rn(a1, __dmul_rn(t, te0));
-    if (M == 3) a2 = __dsub_rn(a2, __dmul_rn(t, te1));
+    a0 = nmac<F>(a0, tau, t);
+    a1 = nmac<F>(a1, t, te0);
+    if (M == 3) a2 = nmac<F>(a2, t, te1);
 }
 
-template <int M>
+template <bool F, int M>
 __device__ __forceinline__ void right_row(double& a0, double& a1, double& a2, double e0, double e1, double tau) {
     double t = __dmul_rn(a1, e0);
-    if (M == 3) t = __dadd_rn(t, __dmul_rn(a2, e1));
+    if (M == 3) t = mac<F>(t, a2, e1);
     t = __dadd_rn(t, a0);
-    a0 = __dsub_rn(a0, __dmul_rn(tau, t));
+    a0 = nmac<F>(a0, tau, t);
     const double tt = __dmul_rn(tau, t);
-    a1 = __dsub_rn(a1, __dmul_rn(e0, tt));
-    if (M == 3) a2 = __dsub_rn(a2, __dmul_rn(e1, tt));
+    a1 = nmac<F>(a1, e0, tt);
+    if (M == 3) a2 = nmac<F>(a2, e1, tt);
 }
 
 // U columns j, j+S, .., j+(U-1)S of the left reflector.
-template <int M, int U, int S>
+template <bool F, int M, int U, int S>
 __device__ __forceinline__ void left_cols(const SMat& T, int r0, int j, double e0, double e1, double tau, double te0,
                                           double te1) {
     double a[U][3];
@@ -302,7 +320,7 @@ __device__ __forceinline__ void left_cols(const SMat& T, int r0, int j, double e
         a[u][2] = M == 3 ? T(r0 + 2, j + u * S) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) left_col<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau, te0, te1);
+    for (int u = 0; u < U; ++u) left_col<F, M>(a[u][0], a[u][1], a[u][2], e0, e1, tau, te0, te1);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         T(r0, j + u * S) = a[u][0];
@@ -312,7 +330,7 @@ __device__ __forceinline__ void left_cols(const SMat& T, int r0, int j, double e
 }
 
 // U rows i, i+S, .., i+(U-1)S of the right reflector.
-template <int M, int U, int S>
+template <bool F, int M, int U, int S>
 __device__ __forceinline__ void right_rows(const SMat& T, int i, int c0, double e0, double e1, double tau) {
     double a[U][3];
 #pragma unroll
@@ -322,7 +340,7 @@ __device__ __forceinline__ void right_rows(const SMat& T, int i, int c0, double 
         a[u][2] = M == 3 ? T(i + u * S, c0 + 2) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) right_row<M>(a[u][0], a[u][1], a[u][2], e0, e1, tau);
+    for (int u = 0; u < U; ++u) right_row<F, M>(a[u][0], a[u][1], a[u][2], e0, e1, tau);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         T(i + u * S, c0) = a[u][0];
@@ -332,36 +350,37 @@ __device__ __forceinline__ void right_rows(const SMat& T, int i, int c0, double 
 }
 
 // Columns (rows) go four at a time, then a pair, then one.
-template <class Qd, int M>
+template <bool F, class Qd, int M>
 __device__ __forceinline__ void house_left_small(const SMat& T, const Qd& Q, int r0, int c0, int c1, double e0,
                                                  double e1, double tau) {
     if (tau == 0.0) return;
     const double te0 = __dmul_rn(tau, e0), te1 = __dmul_rn(tau, e1);
     constexpr int S = Qd::N;
     int j = c0 + Q.q;
-    for (; j + 3 * S < c1; j += 4 * S) left_cols<M, 4, S>(T, r0, j, e0, e1, tau, te0, te1);
+    for (; j + 3 * S < c1; j += 4 * S) left_cols<F, M, 4, S>(T, r0, j, e0, e1, tau, te0, te1);
     if (j + S < c1) {
-        left_cols<M, 2, S>(T, r0, j, e0, e1, tau, te0, te1);
+        left_cols<F, M, 2, S>(T, r0, j, e0, e1, tau, te0, te1);
         j += 2 * S;
     }
-    if (j < c1) left_cols<M, 1, S>(T, r0, j, e0, e1, tau, te0, te1);
+    if (j < c1) left_cols<F, M, 1, S>(T, r0, j, e0, e1, tau, te0, te1);
 }
 
-template <class Qd, int M>
+template <bool F, class Qd, int M>
 __device__ __forceinline__ void house_right_small(const SMat& T, const Qd& Q, int r0, int r1, int c0, double e0,
                                                   double e1, double tau) {
     if (tau == 0.0) return;
     constexpr int S = Qd::N;
     int i = r0 + Q.q;
-    for (; i + 3 * S < r1; i += 4 * S) right_rows<M, 4, S>(T, i, c0, e0, e1, tau);
+    for (; i + 3 * S < r1; i += 4 * S) right_rows<F, M, 4, S>(T, i, c0, e0, e1, tau);
     if (i + S < r1) {
-        right_rows<M, 2, S>(T, i, c0, e0, e1, tau);
+        right_rows<F, M, 2, S>(T, i, c0, e0, e1, tau);
         i += 2 * S;
     }
-    if (i < r1) right_rows<M, 1, S>(T, i, c0, e0, e1, tau);
+    if (i < r1) right_rows<F, M, 1, S>(T, i, c0, e0, e1, tau);
 }
 
 // Givens rotation (c, s) with [c -s; s c] [p; q] = [r; 0].
+template <bool F>
 __device__ __forceinline__ void make_givens(double p, double q, double& c, double& s) {
     if (q == 0.0) {
         c = p < 0.0 ? -1.0 : 1.0;
@@ -371,13 +390,13 @@ __device__ __forceinline__ void make_givens(double p, double q, double& c, doubl
         s = q < 0.0 ? 1.0 : -1.0;
     } else if (fabs(p) > fabs(q)) {
         const double t = __ddiv_rn(q, p);
-        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+        double u = sqrt(mac<F>(1.0, t, t));
         if (p < 0.0) u = -u;
         c = __ddiv_rn(1.0, u);
         s = __dmul_rn(-t, c);
     } else {
         const double t = __ddiv_rn(p, q);
-        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+        double u = sqrt(mac<F>(1.0, t, t));
         if (q < 0.0) u = -u;
         s = __ddiv_rn(-1.0, u);
         c = __dmul_rn(-t, s);
@@ -385,16 +404,17 @@ __device__ __forceinline__ void make_givens(double p, double q, double& c, doubl
 }
 
 // x' = c x - s y, y' = s x + c y (the rotation's adjoint applied to the pair).
+template <bool F>
 __device__ __forceinline__ void rot_pair(double& x, double& y, double c, double s) {
     const double xi = x, yi = y;
-    x = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
-    y = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+    x = mac<F>(__dmul_rn(c, xi), -s, yi);
+    y = mac<F>(__dmul_rn(s, xi), c, yi);
 }
 
 // Eigenvalues of the n x n matrix in T (overwritten), computed by a quad.
 // emit(i, re, im) is called by the quad's lane 0 for i = 0..n-1 in Schur
 // order; returns true on success (the same value in every lane).
-template <class Qd, typename Emit>
+template <bool F, class Qd, typename Emit>
 __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
     const int nn = n * n;
     double scale = 0.0;
@@ -411,15 +431,15 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
         for (int i = 0; i < n - 1; ++i) {
             const int rs = n - i - 1;
             double tau, beta, d;
-            house_coeffs(T, i + 1, rs, i, tau, beta, d);
+            house_coeffs<F>(T, i + 1, rs, i, tau, beta, d);
             Q.sync();
             for (int k = i + 2 + Q.q; k < n; k += Qd::N) T(k, i) = d == 0.0 ? 0.0 : __ddiv_rn(T(k, i), d);
             if (Q.lead()) T(i + 1, i) = beta;
             Q.sync();
             auto ess = [&](int k) { return T(i + 2 + k, i); };
-            house_left(T, Q, i + 1, rs, i + 1, n, ess, tau);
+            house_left<F>(T, Q, i + 1, rs, i + 1, n, ess, tau);
             Q.sync();
-            house_right(T, Q, 0, n, i + 1, rs, ess, tau);
+            house_right<F>(T, Q, 0, n, i + 1, rs, ess, tau);
             Q.sync();
         }
         for (int e = Q.q; e < nn; e += Qd::N)
@@ -455,7 +475,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                     iter = 0;
                 } else if (il == iu - 1) {
                     const double p = __dmul_rn(0.5, __dsub_rn(T(iu - 1, iu - 1), T(iu, iu)));
-                    const double q = __dadd_rn(__dmul_rn(p, p), __dmul_rn(T(iu, iu - 1), T(iu - 1, iu)));
+                    const double q = mac<F>(__dmul_rn(p, p), T(iu, iu - 1), T(iu - 1, iu));
                     const double sub = T(iu, iu - 1);
                     Q.sync();
                     if (Q.lead()) {
@@ -466,18 +486,18 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                     if (q >= 0.0) {
                         const double z = sqrt(fabs(q));
                         double c, s;
-                        make_givens(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), sub, c, s);
+                        make_givens<F>(p >= 0.0 ? __dadd_rn(p, z) : __dsub_rn(p, z), sub, c, s);
                         if (!(c == 1.0 && s == 0.0)) {
                             for (int j = iu - 1 + Q.q; j <= iu; j += Qd::N) {
                                 double x = T(iu - 1, j), y = T(iu, j);
-                                rot_pair(x, y, c, s);
+                                rot_pair<F>(x, y, c, s);
                                 T(iu - 1, j) = x;
                                 T(iu, j) = y;
                             }
                             Q.sync();
                             for (int i = iu - 1 + Q.q; i <= iu; i += Qd::N) {
                                 double x = T(i, iu - 1), y = T(i, iu);
-                                rot_pair(x, y, c, s);
+                                rot_pair<F>(x, y, c, s);
                                 T(i, iu - 1) = x;
                                 T(i, iu) = y;
                             }
@@ -503,7 +523,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                     }
                     if (iter == 30) {
                         double s = __ddiv_rn(__dsub_rn(sh1, sh0), 2.0);
-                        s = __dadd_rn(__dmul_rn(s, s), sh2);
+                        s = mac<F>(sh2, s, s);
                         if (s > 0.0) {
                             s = sqrt(s);
                             if (sh1 < sh0) s = -s;
@@ -544,29 +564,29 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                             w[0] = T(k, k - 1); w[1] = T(k + 1, k - 1); w[2] = T(k + 2, k - 1);
                         }
                         double ess[2], tau, beta;
-                        house_vec(w, 3, ess, tau, beta);
+                        house_vec<F>(w, 3, ess, tau, beta);
                         Q.sync();
                         if (beta != 0.0) {
                             if (Q.lead()) {
                                 if (first && k > il) T(k, k - 1) = -T(k, k - 1);
                                 else if (!first) T(k, k - 1) = beta;
                             }
-                            house_left_small<Qd, 3>(T, Q, k, k, iu + 1, ess[0], ess[1], tau);
+                            house_left_small<F, Qd, 3>(T, Q, k, k, iu + 1, ess[0], ess[1], tau);
                             Q.sync();
-                            house_right_small<Qd, 3>(T, Q, il, min(iu, k + 3) + 1, k, ess[0], ess[1], tau);
+                            house_right_small<F, Qd, 3>(T, Q, il, min(iu, k + 3) + 1, k, ess[0], ess[1], tau);
                             Q.sync();
                         }
                     }
                     {
                         double w[2] = {T(iu - 1, iu - 2), T(iu, iu - 2)};
                         double ess[2], tau, beta;
-                        house_vec(w, 2, ess, tau, beta);
+                        house_vec<F>(w, 2, ess, tau, beta);
                         Q.sync();
                         if (beta != 0.0) {
                             if (Q.lead()) T(iu - 1, iu - 2) = beta;
-                            house_left_small<Qd, 2>(T, Q, iu - 1, iu - 1, iu + 1, ess[0], 0.0, tau);
+                            house_left_small<F, Qd, 2>(T, Q, iu - 1, iu - 1, iu + 1, ess[0], 0.0, tau);
                             Q.sync();
-                            house_right_small<Qd, 2>(T, Q, il, iu + 1, iu - 1, ess[0], 0.0, tau);
+                            house_right_small<F, Qd, 2>(T, Q, il, iu + 1, iu - 1, ess[0], 0.0, tau);
                             Q.sync();
                         }
                     }
@@ -614,7 +634,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
             t0 = __ddiv_rn(t0, maxval);
             t1 = __ddiv_rn(t1, maxval);
             const double p0 = __ddiv_rn(p, maxval);
-            const double z = __dmul_rn(maxval, sqrt(fabs(__dadd_rn(__dmul_rn(p0, p0), __dmul_rn(t0, t1)))));
+            const double z = __dmul_rn(maxval, sqrt(fabs(mac<F>(__dmul_rn(p0, p0), t0, t1))));
             const double re = __dadd_rn(T(i + 1, i + 1), p);
             if (!(isfinite(re) && isfinite(z))) {
                 if (Q.lead())
@@ -691,7 +711,7 @@ __device__ __forceinline__ void list_if_stable(bool unstable, int64_t c, int* no
     }
 }
 
-template <int EQ, bool RG = false>
+template <int EQ, bool RG = false, bool F = false>
 __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, int* __restrict__ nominal,
@@ -734,7 +754,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
             Q.sync();
             float* out = eig32 + c * (int64_t)rn.eig_slot;
             float mx = 0.0f;
-            eig_real(T, Q, nt, [&](int i, double re, double im) {
+            eig_real<F>(T, Q, nt, [&](int i, double re, double im) {
                 const float fr = (float)re, fi = (float)im;
                 out[2 * i] = fr;
                 out[2 * i + 1] = fi;
@@ -747,7 +767,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
 }
 
 // FP64-form LIN_A: the same blocks formed in double from the float inputs.
-template <int EQ>
+template <int EQ, bool F = false>
 __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
                                                           const float* __restrict__ gains, float* __restrict__ lina,
                                                           double* __restrict__ eig64, int* __restrict__ nominal,
@@ -789,7 +809,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
             Q.sync();
             double* out = eig64 + c * (int64_t)run.eig_slot;
             double mx = 0.0;
-            eig_real(T, Q, nt, [&](int i, double re, double im) {
+            eig_real<F>(T, Q, nt, [&](int i, double re, double im) {
                 out[2 * i] = re;
                 out[2 * i + 1] = im;
                 mx = fmax(mx, hypot(re, im));
@@ -810,7 +830,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
 // solved, OPEN_A is formed here with LIN_A's own float operations, and the
 // kernel runs concurrently with k_lina_eig (which then lists nothing): the
 // flags of the candidates the modal stage flags are computed but never read.
-template <int EQ, bool RG = false>
+template <int EQ, bool RG = false, bool F = false>
 __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const float* __restrict__ lina,
                                                        const int* __restrict__ list, const int* __restrict__ count,
@@ -857,7 +877,7 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
             }
             Q.sync();
             bool stable = true;
-            const bool ok = eig_real(T, Q, n2, [&](int, double re, double im) {
+            const bool ok = eig_real<F>(T, Q, n2, [&](int, double re, double im) {
                 if (hypot(re, im) >= 1.0) stable = false;
             });
             if (Q.lead()) nominal[c] = (ok && stable) ? 1 : 0;
@@ -924,37 +944,53 @@ static int eig_lanes(const Run& run, int64_t n) {
     return eq;
 }
 
-template <int EQ>
-static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
-                       int* nominal, int* list, int* count, cudaStream_t st) {
+template <int EQ, bool F>
+static void lina_eig_qf(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+                        int* nominal, int* list, int* count, cudaStream_t st) {
     const int grid = eig_grid(run, run.n, eig_mats<EQ>());
     const size_t smem = (size_t)run.nt * run.nt * eig_stride<EQ>() * sizeof(double);
     if (precision == CE_PRECISION_FP64) {
-        set_smem((const void*)k_lina_eig64<EQ>, smem);
-        k_lina_eig64<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig, nominal, list, count, count + 1);
+        set_smem((const void*)k_lina_eig64<EQ, F>, smem);
+        k_lina_eig64<EQ, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig, nominal, list, count, count + 1);
     } else if (run.rg.runs) {
-        set_smem((const void*)k_lina_eig<EQ, true>, smem);
-        k_lina_eig<EQ, true><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count, count + 1);
+        set_smem((const void*)k_lina_eig<EQ, true, F>, smem);
+        k_lina_eig<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count,
+                                                         count + 1);
     } else {
-        set_smem((const void*)k_lina_eig<EQ>, smem);
-        k_lina_eig<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count, count + 1);
+        set_smem((const void*)k_lina_eig<EQ, false, F>, smem);
+        k_lina_eig<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count,
+                                                          count + 1);
+    }
+}
+
+template <int EQ>
+static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+                       int* nominal, int* list, int* count, cudaStream_t st) {
+    if (run.eig_fused) lina_eig_qf<EQ, true>(run, P, precision, gains, lina, eig, nominal, list, count, st);
+    else lina_eig_qf<EQ, false>(run, P, precision, gains, lina, eig, nominal, list, count, st);
+}
+
+template <int EQ, bool F>
+static void nominal_qf(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+                       const int* list, const int* count, int* nominal, cudaStream_t st) {
+    const int grid = eig_grid(run, run.n, eig_mats<EQ>());  // the listed count is only known on the device
+    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
+    if (run.rg.runs) {
+        set_smem((const void*)k_nominal<EQ, true, F>, smem);
+        k_nominal<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, 0,
+                                                       const_cast<int*>(count) + 2);
+    } else {
+        set_smem((const void*)k_nominal<EQ, false, F>, smem);
+        k_nominal<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal,
+                                                        precision == CE_PRECISION_FP64, const_cast<int*>(count) + 2);
     }
 }
 
 template <int EQ>
 static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
                       const int* list, const int* count, int* nominal, cudaStream_t st) {
-    const int grid = eig_grid(run, run.n, eig_mats<EQ>());  // the listed count is only known on the device
-    const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
-    if (run.rg.runs) {
-        set_smem((const void*)k_nominal<EQ, true>, smem);
-        k_nominal<EQ, true><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, 0,
-                                                    const_cast<int*>(count) + 2);
-    } else {
-        set_smem((const void*)k_nominal<EQ>, smem);
-        k_nominal<EQ><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal,
-                                              precision == CE_PRECISION_FP64, const_cast<int*>(count) + 2);
-    }
+    if (run.eig_fused) nominal_qf<EQ, true>(run, P, precision, gains, lina, list, count, nominal, st);
+    else nominal_qf<EQ, false>(run, P, precision, gains, lina, list, count, nominal, st);
 }
 
 void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,

@@ -2,11 +2,11 @@
 //
 // Who needs this: callers that must not allocate device memory at the time
 // they evaluate -- a real-time tuning loop that cannot take the latency and
-// jitter of cudaMalloc, code that issues its work inside a stream capture
-// (where a blocking cudaMalloc is not allowed), or a host application whose
-// device memory is owned entirely by its own allocator.  The session API
-// (ce_evaluate_device) grows its scratch with cudaMalloc when a batch is
-// larger than any before it; this entry point never does.
+// jitter of cudaMalloc (it may synchronise the device), or a host application
+// whose device memory is owned entirely by its own allocator or budgeted up
+// front.  The session API (ce_evaluate_device) grows its scratch with
+// cudaMalloc when a batch is larger than any before it; this entry point never
+// allocates: no cudaMalloc, no cudaFree, no allocating library routine.
 //
 // What it computes: the simulation and the modal setup of the fit window for
 // n candidates (k_sim + k_fit, the same kernels the session pipeline runs):
@@ -26,9 +26,16 @@
 //    same call.  Two calls whose work overlaps on the GPU (different streams,
 //    or different host threads) race on the array and produce garbage: the
 //    caller serialises them (one stream, or events).
-//  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress, with that device current, and keeps it; make that
-//    first call before any stream capture that the later calls run inside.
+//  * The first call on a device (whichever host thread makes it) looks up the
+//    array's device address with cudaGetSymbolAddress, with that device
+//    current, once, and keeps it; make that first call before any stream
+//    capture.  In host code the array's name is only a host-side stand-in,
+//    never a device address, so the kernels get the looked-up address.
+//  * The session's plant must be usable: a plant whose sweep grid failed at
+//    session creation is refused with its message, as ce_evaluate_device
+//    refuses it.
+#include <mutex>
+
 #include "ce_device.cuh"
 #include "ce_host.h"
 
@@ -39,19 +46,25 @@ static __device__ __align__(256) float g_fit_scratch[CE_NOALLOC_SCRATCH_FLOATS];
 namespace {
 
 constexpr int MAX_DEVICES = 64;
+// Per device: the array's device address, looked up once.  Concurrent first
+// calls from several host threads run the lookup once (std::call_once) and all
+// read the published address.
+std::once_flag g_scratch_once[MAX_DEVICES];
 float* g_scratch_ptr[MAX_DEVICES] = {};
+cudaError_t g_scratch_rc[MAX_DEVICES] = {};
 
 float* scratch_address() {
     int dev = 0;
     CE_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= MAX_DEVICES) fail("ce_modal_fit_noalloc: device {} out of range", dev);
-    if (!g_scratch_ptr[dev]) {
+    std::call_once(g_scratch_once[dev], [dev] {
         void* p = nullptr;
-        const cudaError_t rc = cudaGetSymbolAddress(&p, g_fit_scratch);
-        if (rc != cudaSuccess)
-            fail("ce_modal_fit_noalloc: cudaGetSymbolAddress of the static scratch failed: {}", cudaGetErrorString(rc));
+        g_scratch_rc[dev] = cudaGetSymbolAddress(&p, g_fit_scratch);
         g_scratch_ptr[dev] = static_cast<float*>(p);
-    }
+    });
+    if (g_scratch_rc[dev] != cudaSuccess || !g_scratch_ptr[dev])
+        fail("ce_modal_fit_noalloc: cudaGetSymbolAddress of the static scratch failed: {}",
+             cudaGetErrorString(g_scratch_rc[dev]));
     return g_scratch_ptr[dev];
 }
 
@@ -68,13 +81,17 @@ extern "C" CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index
             fail("ce_modal_fit_noalloc: plant index {} out of range [0, {})", plant_index, session_plants(s));
         if (n < 0) fail("ce_modal_fit_noalloc: candidate count {} is negative", n);
         if (n == 0) return 0;
+        if (const std::string& e = session_plant_error(s, plant_index); !e.empty())
+            fail("ce_modal_fit_noalloc: plant {}: {}", plant_index, e);
         Run r = session_run(s, plant_index, n);
-        const int64_t win = (int64_t)n * r.fit_pitch;
-        const int64_t need = win + 4 * (int64_t)n;
-        if (need > (int64_t)CE_NOALLOC_SCRATCH_FLOATS)
-            fail("ce_modal_fit_noalloc: {} candidates need {} scratch floats (fit window {} + 4 per candidate); "
-                 "the static scratch holds {} floats",
-                 n, need, r.fit_pitch, (int64_t)CE_NOALLOC_SCRATCH_FLOATS);
+        // the limit is checked by division first, so that no product can overflow
+        const int64_t per = (int64_t)r.fit_pitch + 4;
+        const int64_t cap = (int64_t)CE_NOALLOC_SCRATCH_FLOATS / per;
+        if (n > cap)
+            fail("ce_modal_fit_noalloc: {} candidates need {} scratch floats each (fit window {} + 4), more than "
+                 "the {} that fit; the static scratch holds {} floats",
+                 n, per, r.fit_pitch, cap, (int64_t)CE_NOALLOC_SCRATCH_FLOATS);
+        const int64_t win = n * (int64_t)r.fit_pitch;
         float* base = scratch_address();
         float* ywin = base;
         SimSummary* summ = reinterpret_cast<SimSummary*>(base + win);  // win is a multiple of 8 floats: 32-byte aligned

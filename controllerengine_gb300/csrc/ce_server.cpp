@@ -50,6 +50,7 @@ struct Request {
     float* info_out = nullptr;
     int64_t next = 0;      // first row not yet dispatched
     int64_t finished = 0;  // rows completed
+    int64_t failed = 0;    // rows that failed, or were dropped from the queue after a failure
     bool done = false;
     std::string error;
     Clock::time_point t_submit, t_done;
@@ -114,8 +115,23 @@ int64_t bytes_per_candidate(const ce_config& c, int precision) {
     return 4 * f;
 }
 
+// A request is done once every row is accounted for: dispatched and retired,
+// successfully or not.  Until then a piece of it may still be on the GPU or in
+// a lane's staging buffer, and the caller's buffers must stay untouched by the
+// caller, so ce_server_wait keeps waiting.  Caller holds the lock.
+void settle(ce_server* s, Request& r, Clock::time_point now) {
+    if (r.done || r.next != r.n || r.finished + r.failed != r.n) return;
+    r.done = true;
+    r.t_done = now;
+    if (r.error.empty()) {
+        s->completed++;
+        s->latency_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_submit).count());
+    }
+}
+
 void complete_lane(ce_server* s, Lane& L) {
-    // each piece's rows go to a disjoint slice of its request's output
+    // each piece's rows go to a disjoint slice of its request's output; the
+    // request is not done before this piece retires, so the buffer is still valid
     for (const Piece& p : L.pieces) {
         const int64_t iw = s->cfg[p.req->model].info_mx_width;
         std::memcpy(p.req->info_out + p.row0 * iw, L.h_info + p.off * iw, (size_t)p.rows * iw * sizeof(float));
@@ -124,24 +140,34 @@ void complete_lane(ce_server* s, Lane& L) {
     std::lock_guard<std::mutex> g(s->mu);
     for (const Piece& p : L.pieces) {
         p.req->finished += p.rows;
-        if (p.req->finished == p.req->n && !p.req->done) {
-            p.req->done = true;
-            p.req->t_done = now;
-            s->completed++;
-            s->latency_ms.push_back(std::chrono::duration<double, std::milli>(now - p.req->t_submit).count());
-        }
+        settle(s, *p.req, now);
     }
     L.pieces.clear();
     L.busy = false;
     s->cv_done.notify_all();
 }
 
+// The batch on lane L failed (nothing of it is in flight any more).  Each of
+// its requests records the first error, its rows still queued are withdrawn
+// (they would read the caller's buffers after ce_server_wait returned), and it
+// is done once its pieces on other lanes have retired as well.
 void fail_pieces(ce_server* s, Lane& L, const std::string& msg) {
+    const auto now = Clock::now();
     std::lock_guard<std::mutex> g(s->mu);
     for (const Piece& p : L.pieces) {
-        p.req->error = msg;
-        p.req->done = true;
-        p.req->t_done = Clock::now();
+        Request& r = *p.req;
+        if (r.error.empty()) r.error = msg;
+        r.failed += p.rows;
+        if (r.next < r.n) {
+            r.failed += r.n - r.next;
+            r.next = r.n;
+            for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+                if (it->get() == &r) {
+                    s->queue.erase(it);
+                    break;
+                }
+        }
+        settle(s, r, now);
     }
     L.pieces.clear();
     L.busy = false;

@@ -261,6 +261,18 @@ class Session:
         _check(_lib().ce_session_set_precision(self._h, code))
         self.precision = precision
 
+    @property
+    def eig_arith(self) -> str:
+        """Arithmetic of the FP64 eigensolves: "fused" (one DFMA per multiply-add, the default) or
+        "separate" (every product and sum rounded, the reference's host arithmetic)."""
+        v = C.c_int32()
+        _check(_lib().ce_session_get_eig_arith(self._h, C.byref(v)))
+        return {_ffi.EIG_ARITH_SEPARATE: "separate", _ffi.EIG_ARITH_FUSED: "fused"}[v.value]
+
+    def set_eig_arith(self, arith: str):
+        code = {"separate": _ffi.EIG_ARITH_SEPARATE, "fused": _ffi.EIG_ARITH_FUSED}[arith]
+        _check(_lib().ce_session_set_eig_arith(self._h, code))
+
     def close(self):
         if self._h:
             _lib().ce_session_destroy(self._h)

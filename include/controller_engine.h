@@ -260,6 +260,20 @@ typedef struct ce_tuning {
 } ce_tuning;
 CE_EXPORT int ce_session_set_tuning(ce_session* s, const ce_tuning* t);
 CE_EXPORT int ce_session_get_tuning(const ce_session* s, ce_tuning* t);
+
+/* Arithmetic of the FP64 eigensolves, LIN_A's and the nominal closed loop's
+ * (no counterpart in the reference, whose Eigen stage on the host rounds every
+ * product and every sum, ref: src/eigensolve.cu:6-16, src/allmargin.cu:66-79).
+ * CE_EIG_ARITH_FUSED (the default): each multiply-add of the Householder and
+ * Givens updates is one DFMA, half the FP64 instructions of the separate form;
+ * CE_EIG_ARITH_SEPARATE: every product and sum rounded on its own, as the
+ * reference's host code computes them.  The two forms run the same algorithm
+ * in the same order and differ by rounding alone (eigenvalues within ~1e-14
+ * relative of each other on the eight-state workload). */
+#define CE_EIG_ARITH_SEPARATE 0
+#define CE_EIG_ARITH_FUSED 1
+CE_EXPORT int ce_session_set_eig_arith(ce_session* s, int32_t arith);
+CE_EXPORT int ce_session_get_eig_arith(const ce_session* s, int32_t* arith);
 CE_EXPORT int ce_session_autotune(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
                                   const float* d_info_in, float* d_info_out, void* stream, ce_tuning* best);
 
@@ -301,9 +315,9 @@ CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second);
 
 /* Allocation-free variant of the modal-fit path.  No counterpart in the
  * reference.  For callers that must not allocate device memory when they
- * evaluate: a real-time tuning loop that cannot afford cudaMalloc's latency,
- * work issued inside a stream capture, or a host application whose device
- * memory belongs to its own allocator.  It runs the simulation and the modal
+ * evaluate: a real-time tuning loop that cannot afford cudaMalloc's latency
+ * (it may synchronise the device), or a host application whose device memory
+ * belongs to its own allocator or is budgeted up front.  It runs the simulation and the modal
  * setup (the same kernels as the session pipeline) for n candidates of plant
  * `plant_index`: d_cuda_mx (n x cuda_mx_width gains) and d_eigen (n x 2nt float
  * eigenvalues, e.g. from a previous evaluation) in; d_ata (n x (2nt)^2), d_atb
@@ -315,9 +329,12 @@ CE_EXPORT int ce_measure_fma_rate(int32_t fp64, double* ops_per_second);
  * device that loads the library until exit); a call needs
  * n * (round_up(fit_steps, 8) + 4) floats and is rejected with an error if that
  * is more.  It calls no cudaMalloc/cudaFree.  The first call on a device looks
- * up the array's address (cudaGetSymbolAddress, with that device current):
- * make it before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU race; serialise them. */
+ * up the array's address once (cudaGetSymbolAddress, with that device
+ * current; safe from several host threads): make it before any stream capture.
+ * All calls share the array, which keeps the last call's contents (nothing in
+ * it must start at zero: the simulation writes every element the fit reads):
+ * calls whose work overlaps on the GPU race; serialise them.  A plant whose
+ * sweep grid failed at session creation is refused, as in ce_evaluate_device. */
 #define CE_NOALLOC_SCRATCH_FLOATS (8 * 1024 * 1024)
 CE_EXPORT int ce_modal_fit_noalloc(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,
                                    const float* d_eigen, float* d_ata, float* d_atb, float* d_info, void* stream);

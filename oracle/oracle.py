@@ -22,8 +22,8 @@ F32, I32 = np.float32, np.int32
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "ce_oracle.c"
-    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    newest = max((HERE / f).stat().st_mtime for f in ("ce_oracle.c", "ce_oracle_eig.h"))
+    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "all"], check=True)
     return LIB
 
@@ -82,6 +82,8 @@ def lib():
         L.oracle_eigensolve.argtypes = [i64, C.c_int, _FP, _FP, _DP, C.c_int]
         L.oracle_eigensolve.restype = None
         L.oracle_eig_matrix.argtypes = [_DP, C.c_int, _DP, _DP]
+        L.oracle_set_eig_fused.argtypes = [C.c_int]
+        L.oracle_set_eig_fused.restype = None
         L.oracle_modalsetup.argtypes = [C.POINTER(oc_cfg), i64, _FP, _FP, _FP, _FP, _FP, C.c_int]
         L.oracle_modalsetup.restype = None
         L.oracle_modalsolve.argtypes = [C.POINTER(oc_cfg), i64, _FP, _FP, _FP, _FP, C.c_int]
@@ -145,7 +147,12 @@ def _f(a):
 class Oracle:
     """One round of the reference method on the CPU for a (config text, plant) pair."""
 
-    def __init__(self, config_text: str, plant, round_index: int = 0, threads: int | None = None):
+    def __init__(self, config_text: str, plant, round_index: int = 0, threads: int | None = None,
+                 eig_fused: bool = False):
+        """eig_fused: the eigensolves (LIN_A and the nominal closed loop) fuse each multiply-add into
+        one fma, as the engine's fused eigensolve arithmetic does; False: every product and sum is
+        rounded, the reference's arithmetic."""
+        self.eig_fused = bool(eig_fused)
         self.cfg = make_cfg(config_text)
         self.threads = threads or default_threads()
         c = self.cfg
@@ -228,6 +235,7 @@ class Oracle:
         n = lina.shape[0]
         e = np.empty((n, 2 * self.nt), F32)
         e64 = np.empty((n, 2 * self.nt), np.float64)
+        lib().oracle_set_eig_fused(int(self.eig_fused))
         lib().oracle_eigensolve(n, self.nt, _f(lina), _f(e), e64.ctypes.data_as(_DP), self.threads)
         return e64 if fp64 else e
 
@@ -252,6 +260,7 @@ class Oracle:
     def allmargin(self, lina, cuda_mx, info):
         g, n = self._g(cuda_mx)
         info = np.array(info, F32, copy=True, order="C")
+        lib().oracle_set_eig_fused(int(self.eig_fused))
         rc = lib().oracle_allmargin(C.byref(self.cfg), C.byref(self.plant), n, _f(np.ascontiguousarray(lina, F32)),
                                     _f(g), _f(info), self.threads)
         if rc:
@@ -268,6 +277,7 @@ class Oracle:
                      eigen=np.empty((n, 2 * nt), F32), ata=np.empty((n, 4 * nt * nt), F32),
                      atb=np.empty((n, 2 * nt), F32))
         dd = d or {}
+        lib().oracle_set_eig_fused(int(self.eig_fused))
         rc = lib().oracle_evaluate(C.byref(self.cfg), C.byref(self.plant), n, _f(g), _f(info),
                                    _f(dd.get("yplant")), _f(dd.get("lina")), _f(dd.get("eigen")), _f(dd.get("ata")),
                                    _f(dd.get("atb")), self.threads)
@@ -278,11 +288,12 @@ class Oracle:
         return (info, d) if diagnostics else info
 
 
-def eig_matrix(A: np.ndarray):
+def eig_matrix(A: np.ndarray, fused: bool = False):
     A = np.ascontiguousarray(A, np.float64)
     n = A.shape[0]
     wr = np.empty(n)
     wi = np.empty(n)
+    lib().oracle_set_eig_fused(int(fused))
     ok = lib().oracle_eig_matrix(A.ctypes.data_as(_DP), n, wr.ctypes.data_as(_DP), wi.ctypes.data_as(_DP))
     return bool(ok), wr + 1j * wi
 

@@ -35,15 +35,20 @@ def _close(a, b, rtol, atol=0.0):
     return ok
 
 
-def _stagewise(problem, oracle_mod, score_atol=1e-6):
+def _stagewise(problem, oracle_mod, score_atol=1e-6, eig_arith=None):
+    """eig_arith: the session's eigensolve arithmetic ("fused" / "separate"; None: the library
+    default); the oracle's eigensolves use the same one, so eigenvalues compare bit for bit."""
     cfg = ce.EngineConfig.parse(problem.config_text)
     with ce.Session(cfg, problem.plant) as s:
+        if eig_arith:
+            s.set_eig_arith(eig_arith)
+        arith = s.eig_arith
         info, d = s.evaluate_diagnostics(problem.cuda_mx, problem.info_mx)
         launches = s.kernel_launches
     # lina+eig, sim, fit classes, fit, modal, nominal, sweep selection, LU pass, scan; the
     # Kalman observer adds three grouping kernels and its second simulation form
     assert launches == (13 if cfg.observer else 9)
-    orc = oracle_mod.Oracle(problem.config_text, problem.plant)
+    orc = oracle_mod.Oracle(problem.config_text, problem.plant, eig_fused=arith == "fused")
     g = problem.cuda_mx
 
     y_o = orc.sim(g)

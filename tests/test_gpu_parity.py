@@ -35,8 +35,9 @@ def test_stagewise_mass_spring(lib, oracle_mod, mass_spring):
         assert info[3, s + 1] == np.float32(5.0)
 
 
-def test_stagewise_eight_state(lib, oracle_mod, eight_state_small):
-    _stagewise(eight_state_small, oracle_mod)
+@pytest.mark.parametrize("eig_arith", ["fused", "separate"])
+def test_stagewise_eight_state(lib, oracle_mod, eight_state_small, eig_arith):
+    _stagewise(eight_state_small, oracle_mod, eig_arith=eig_arith)
 
 
 def _fit_condition(info, ata, cfg):
@@ -68,7 +69,8 @@ def test_end_to_end_against_independent_oracle(lib, oracle_mod, mass_spring, eig
         cfg = ce.EngineConfig.parse(p.config_text)
         with ce.Session(cfg, p.plant) as s:
             info, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("ata",))
-        ref = oracle_mod.Oracle(p.config_text, p.plant).evaluate(p.cuda_mx, p.info_mx)
+            fused = s.eig_arith == "fused"
+        ref = oracle_mod.Oracle(p.config_text, p.plant, eig_fused=fused).evaluate(p.cuda_mx, p.info_mx)
         cls_a, cls_b = _classes(info, cfg), _classes(ref, cfg)
         assert _eq(cls_a, cls_b), f"classification mismatches: {int((cls_a != cls_b).any(axis=1).sum())}"
         c = _cols(cfg)

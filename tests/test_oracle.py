@@ -126,3 +126,50 @@ def test_margins_closed_form(oracle_mod):
         # second order while the interpolation error dominates (at 2,000 points float32
         # rounding is of the same size): twice the points, ~4x smaller error (at least 3x)
         assert (errs[200, r] > 3 * errs[400, r]).all(), (errs[200, r], errs[400, r])
+
+
+def test_fused_eigensolve_lapack(oracle_mod):
+    """The fused eigensolve arithmetic (one fma per multiply-add) against LAPACK, as the separate
+    form is above."""
+    rng = np.random.default_rng(4)
+    for n in list(range(1, 17)) * 2:
+        A = rng.standard_normal((n, n))
+        ok, ev = oracle_mod.eig_matrix(A, fused=True)
+        assert ok
+        ref = np.linalg.eigvals(A)
+        key = lambda z: (round(z.real, 6), round(abs(z.imag), 6), np.sign(z.imag))
+        np.testing.assert_allclose(sorted(ev, key=key), sorted(ref, key=key), rtol=1e-9,
+                                   atol=1e-9 * max(1.0, np.abs(ref).max()))
+
+
+def test_fused_eigensolve_agrees_with_separate_on_the_eight_state_workload(oracle_mod):
+    """The engine's default eigensolve arithmetic against the reference's, both restated in the
+    oracle, on every candidate of the 65,536-candidate eight-state workload (T = 10,000, F = 400):
+    LIN_A's FP64 eigenvalues within 1e-9 of each other relative to the matrix's largest |lambda|
+    (they are ~1e-14 apart), the same modal-stability class for every candidate, and the same
+    nominal closed-loop verdict and margins (the margin stage on every candidate, none pre-flagged).
+    For a few matrices (82 of 65,536) the QR iteration deflates two eigenvalues in the other order,
+    so they are compared as matched sets and the reordered ones are bounded."""
+    p = synth.eight_state()
+    sep = oracle_mod.Oracle(p.config_text, p.plant, eig_fused=False)
+    fus = oracle_mod.Oracle(p.config_text, p.plant, eig_fused=True)
+    lina = sep.lina(p.cuda_mx)
+    a = sep.eigensolve(lina, fp64=True).reshape(len(lina), -1, 2)
+    b = fus.eigensolve(lina, fp64=True).reshape(len(lina), -1, 2)
+    za, zb = a[..., 0] + 1j * a[..., 1], b[..., 0] + 1j * b[..., 1]
+    assert np.isfinite(za).all() and np.isfinite(zb).all()
+    scale = np.abs(za).max(axis=1)
+    rel = np.abs(za - zb).max(axis=1) / scale
+    reordered = np.where(rel > 1e-9)[0]
+    assert len(reordered) <= 0.005 * len(za), len(reordered)
+    for k in reordered:  # the same eigenvalues in another Schur order
+        d = np.abs(za[k][:, None] - zb[k][None, :])
+        assert d.min(axis=1).max() <= 1e-9 * scale[k] and d.min(axis=0).max() <= 1e-9 * scale[k], k
+    # modal stability as the modal stage tests it, on the float eigenvalues
+    fa = np.hypot(a[..., 0].astype(np.float32), a[..., 1].astype(np.float32)).max(axis=1) > 1
+    fb = np.hypot(b[..., 0].astype(np.float32), b[..., 1].astype(np.float32)).max(axis=1) > 1
+    assert np.array_equal(fa, fb)
+    # the nominal closed loop's verdict (and with it the margins) on every candidate
+    ra = sep.allmargin(lina, p.cuda_mx, p.info_mx)
+    rb = fus.allmargin(lina, p.cuda_mx, p.info_mx)
+    assert np.array_equal(ra, rb, equal_nan=True)
