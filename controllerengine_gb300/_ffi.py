@@ -25,7 +25,7 @@ EIG_ARITH_FUSED = 1
 EXPORTED_SYMBOLS = (
     "ce_last_error", "ce_version", "ce_parse_config", "ce_decode_instructions",
     "ce_session_create", "ce_session_destroy", "ce_session_set_precision", "ce_session_get_config",
-    "ce_session_set_eig_arith", "ce_session_get_eig_arith",
+    "ce_session_set_eig_arith", "ce_session_get_eig_arith", "ce_evaluate_diagnostics64",
     "ce_evaluate", "ce_evaluate_diagnostics", "ce_evaluate_device", "ce_session_kernel_launches",
     "ce_session_set_profiling", "ce_session_stage_times", "ce_measure_fma_rate", "ce_modal_fit_noalloc",
     "ce_session_set_sim_kernel", "ce_session_sim_kernel", "ce_session_sim_log", "ce_sim_specialised_source",
@@ -90,6 +90,13 @@ class ce_diagnostics(C.Structure):
     _fields_ = [(n, _FP) for n in ("yplant", "lina", "eigen", "ata", "atb")]
 
 
+_DP = C.POINTER(C.c_double)
+
+
+class ce_diagnostics64(C.Structure):
+    _fields_ = [(n, _DP) for n in ("ywin", "summ", "lina", "eigen", "ata", "atb")]
+
+
 class ce_tuning(C.Structure):
     _fields_ = [("eig_lanes", C.c_int32), ("eig_blocks_per_sm", C.c_int32), ("chunks", C.c_int32),
                 ("ms_per_evaluation", C.c_double)]
@@ -133,6 +140,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_evaluate.argtypes = [C.c_void_p, C.c_int32, C.c_int64, _FP, _FP, _FP]
     lib.ce_evaluate_diagnostics.argtypes = [C.c_void_p, C.c_int32, C.c_int64, _FP, _FP, _FP,
                                             C.POINTER(ce_diagnostics)]
+    lib.ce_evaluate_diagnostics64.argtypes = [C.c_void_p, C.c_int32, C.c_int64, _FP, _FP, _FP,
+                                              C.POINTER(ce_diagnostics64)]
     lib.ce_evaluate_device.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]
     lib.ce_session_kernel_launches.argtypes = [C.c_void_p]

@@ -43,7 +43,7 @@ struct Buffers {
     int nt = 0, time = 0, pitch = 0, precision = -1;
     float* gains = nullptr;
     float* info = nullptr;
-    float* lina = nullptr;
+    void* lina = nullptr;  // float, or double in the FP64 form
     void* eig = nullptr;
     void* ywin = nullptr;
     void* summ = nullptr;
@@ -67,8 +67,8 @@ struct Buffers {
                         (void*)sweep_list, (void*)sweep_count, sweep.mag, sweep.arg, sweep.bpc, (void*)sweep.fail,
                         (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order, (void*)plant_idx})
             if (p) cudaFree(p);
-        gains = info = lina = traj = nullptr;
-        eig = ywin = summ = ata = atb = nullptr;
+        gains = info = traj = nullptr;
+        lina = eig = ywin = summ = ata = atb = nullptr;
         nominal = fit_counts = fit_order = nominal_list = nominal_count = sweep_list = sweep_count = nullptr;
         plant_idx = nullptr;
         sweep = SweepScratch{};
@@ -199,7 +199,7 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         const int64_t cap = n;
         dev_alloc(b.gains, (size_t)cap * c.cuda_mx_width);
         dev_alloc(b.info, (size_t)cap * c.info_mx_width);
-        dev_alloc(b.lina, (size_t)cap * nt * nt);
+        CE_CUDA(cudaMalloc(&b.lina, (size_t)cap * nt * nt * rsz + 16));
         CE_CUDA(cudaMalloc(&b.eig, (size_t)cap * 2 * nt * rsz + 16));
         CE_CUDA(cudaMalloc(&b.ywin, (size_t)cap * pitch * rsz + 64));
         CE_CUDA(cudaMalloc(&b.summ, (size_t)cap * 4 * rsz + 64));
@@ -454,7 +454,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         int64_t off;
         chunk(k, rc, off);
         timed(0, ss, [&] {
-            launch_lina_eig(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt, at(b.eig, off, 2 * nt * rsz),
+            launch_lina_eig(rc, P, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz), at(b.eig, off, 2 * nt * rsz),
                             b.nominal + off, nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, ss,
                             !nom_all);
         });
@@ -466,7 +466,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         cudaStream_t on = nom_all ? ns2 : ss;
         timed(4, on, [&] {
-            launch_nominal(rc, P, prec, d_gains + off * cw, b.lina + off * nt * nt,
+            launch_nominal(rc, P, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz),
                            nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, b.nominal + off, on);
         });
         CE_CUDA(cudaEventRecord(s->ev_nom[k], on));
@@ -522,7 +522,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         CE_CUDA(cudaStreamWaitEvent(fs, s->ev_nom[k], 0));
         timed(5, fs, [&] {
-            launch_sweep(rc, prec, d_gains + off * cw, b.lina + off * nt * nt, b.nominal + off, at(fgrid, off, gstep),
+            launch_sweep(rc, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz), b.nominal + off, at(fgrid, off, gstep),
                          d_info + off * iw, b.sweep_list + off, b.sweep_count + k, b.sweep, fs);
         });
     }
@@ -848,8 +848,6 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
     if (diag) {
         if (diag->yplant)
             CE_CUDA(cudaMemcpyAsync(diag->yplant, b.traj, (size_t)n * c.time * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (diag->lina)
-            CE_CUDA(cudaMemcpyAsync(diag->lina, b.lina, (size_t)n * nt * nt * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
     CE_CUDA(cudaStreamSynchronize(st));
     if (diag) {
@@ -863,10 +861,49 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
                 for (size_t i = 0; i < count; ++i) dst[i] = (float)tmp[i];
             }
         };
+        pull(diag->lina, b.lina, (size_t)n * nt * nt);
         pull(diag->eigen, b.eig, (size_t)n * 2 * nt);
         pull(diag->ata, b.ata, (size_t)n * 4 * nt * nt);
         pull(diag->atb, b.atb, (size_t)n * 2 * nt);
     }
+}
+
+// Element size in bytes of each per-candidate buffer of the session's precision.
+struct BufElems {
+    size_t ywin, summ, lina, eig, ata;
+};
+BufElems buf_elems(int precision) {
+    if (precision == CE_PRECISION_FP64) return {8, 8, 8, 8, 8};
+    return {4, 4, 4, 4, 4};
+}
+
+// Device buffer of n records of `count` elements (`stride` elements apart,
+// `bytes` each: 4 = float, 8 = double) into n x count doubles.
+void pull64(double* dst, const void* src, int64_t n, int64_t count, int64_t stride, size_t bytes) {
+    if (!dst) return;
+    std::vector<char> h((size_t)n * stride * bytes);
+    CE_CUDA(cudaMemcpy(h.data(), src, h.size(), cudaMemcpyDeviceToHost));
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t k = 0; k < count; ++k) {
+            const char* e = h.data() + ((size_t)c * stride + k) * bytes;
+            dst[c * count + k] = bytes == 8 ? *(const double*)e : (double)*(const float*)e;
+        }
+}
+
+void evaluate_host64(ce_session* s, int plant, int64_t n, const float* cuda_mx, const float* info_in,
+                     float* info_out, const ce_diagnostics64* diag) {
+    evaluate_host(s, plant, n, cuda_mx, info_in, info_out, nullptr);
+    if (!diag || n == 0) return;
+    const ce_config& c = s->cfg;
+    const Buffers& b = s->buf;
+    const int64_t nt = c.total_dim;
+    const BufElems e = buf_elems(s->precision);
+    pull64(diag->ywin, b.ywin, n, c.fit_steps, fit_pitch(c.fit_steps), e.ywin);
+    pull64(diag->summ, b.summ, n, 3, 4, e.summ);
+    pull64(diag->lina, b.lina, n, nt * nt, nt * nt, e.lina);
+    pull64(diag->eigen, b.eig, n, 2 * nt, 2 * nt, e.eig);
+    pull64(diag->ata, b.ata, n, 4 * nt * nt, 4 * nt * nt, e.ata);
+    pull64(diag->atb, b.atb, n, 2 * nt, 2 * nt, e.ata);
 }
 
 // ---- file boundary ----------------------------------------------------------
@@ -1460,6 +1497,11 @@ CE_EXPORT int ce_evaluate(ce_session* s, int32_t plant_index, int64_t n, const f
 CE_EXPORT int ce_evaluate_diagnostics(ce_session* s, int32_t plant_index, int64_t n, const float* cuda_mx,
                                       const float* info_in, float* info_out, const ce_diagnostics* diag) {
     return guarded([&] { evaluate_host(s, plant_index, n, cuda_mx, info_in, info_out, diag); });
+}
+
+CE_EXPORT int ce_evaluate_diagnostics64(ce_session* s, int32_t plant_index, int64_t n, const float* cuda_mx,
+                                        const float* info_in, float* info_out, const ce_diagnostics64* diag) {
+    return guarded([&] { evaluate_host64(s, plant_index, n, cuda_mx, info_in, info_out, diag); });
 }
 
 CE_EXPORT int ce_evaluate_device(ce_session* s, int32_t plant_index, int64_t n, const float* d_cuda_mx,

@@ -59,15 +59,15 @@ void launch_plant_grid_rows(int64_t rows, const int* row_inst, const int* row_w,
 // Kernel launchers (ce_k_*.cu); all enqueue on `st`.
 void launch_sim(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ, float* traj,
                 cudaStream_t st);
-// LIN_A and its FP64 eigenvalues; candidates that pass the modal stability
+// LIN_A (float; double in the FP64 form) and its FP64 eigenvalues; candidates that pass the modal stability
 // test are appended to list, the others get nominal = -1.  count holds three
 // ints (reset here): the listed count and the work counters of both kernels.
 // list null: no list of stable candidates (the nominal eigensolve then runs on all);
 // clear: zero the work counters first (else the caller has).
-void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, void* lina, void* eig,
                      int* nominal, int* list, int* count, cudaStream_t st, bool clear = true);
 // Nominal closed-loop stability (nominal = 1 / 0) of the listed candidates.
-void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const void* lina,
                     const int* list, const int* count, int* nominal, cudaStream_t st);
 // counts (MAXT + 1 ints) and order ((MAXT + 1) * n ints) bucket the candidates
 // by fit class before the fit; both null: candidates in index order.
@@ -86,7 +86,7 @@ struct SweepScratch {
 };
 // The margin sweep; list (n ints) and count (1 int) are scratch for the
 // candidates that run the frequency loop.
-void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
+void launch_sweep(const Run& run, int precision, const float* gains, const void* lina, const int* nominal,
                   const void* fgrid, float* info, int* list, int* count, const SweepScratch& sw, cudaStream_t st);
 
 double measure_fma_rate(bool fp64);

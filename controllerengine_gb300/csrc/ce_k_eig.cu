@@ -766,10 +766,18 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
     }
 }
 
-// FP64-form LIN_A: the same blocks formed in double from the float inputs.
+// FP64-form LIN_A: the same blocks formed in double from the float inputs,
+// every product and difference rounded on its own, and kept in double.
+__device__ __forceinline__ double lina_entry64(const Plant& P, double Kj, double Li, int i, int j) {
+    const double pbk = __dmul_rn((double)P.ss_b[i], Kj);
+    const double pdk = __dmul_rn((double)P.ss_d, Kj);
+    const double lpc = __dmul_rn(Li, __dsub_rn((double)P.ss_c[j], pdk));
+    return __dsub_rn(__dsub_rn((double)P.ss_a[i * MAXS + j], pbk), lpc);
+}
+
 template <int EQ, bool F = false>
 __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
-                                                          const float* __restrict__ gains, float* __restrict__ lina,
+                                                          const float* __restrict__ gains, double* __restrict__ lina,
                                                           double* __restrict__ eig64, int* __restrict__ nominal,
                                                           int* __restrict__ list, int* __restrict__ count,
                                                           int* __restrict__ next) {
@@ -784,23 +792,21 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
             const int ns = run.ns, nt = run.nt;
             const float* row = gains + c * run.cuda_w;
             SMat T{smem + m, nt, eig_stride<EQ>()};
-            float* lrow = lina + c * (int64_t)run.lina_slot;
+            double* lrow = lina + c * (int64_t)run.lina_slot;
             auto fill = [&](const auto& pv) {
                 for (int e = Q.q; e < nt * nt; e += EQ) {
                     const int i = e / nt, j = e % nt;
                     double v;
                     if (i < ns && j < ns) {
-                        const double Kj = row[j], Li = row[ns + i];
-                        v = (double)P.ss_a[i * MAXS + j] - (double)P.ss_b[i] * Kj -
-                            Li * ((double)P.ss_c[j] - (double)P.ss_d * Kj);
+                        v = lina_entry64(P, (double)row[j], (double)row[ns + i], i, j);
                     } else if (i < ns) {
-                        v = (double)row[ns + i] * (double)pv.c(j - ns);
+                        v = __dmul_rn((double)row[ns + i], (double)pv.c(j - ns));
                     } else if (j < ns) {
-                        v = -(double)pv.bu(i - ns) * (double)row[j];
+                        v = -__dmul_rn((double)pv.bu(i - ns), (double)row[j]);
                     } else {
                         v = pv.a(i - ns, j - ns);
                     }
-                    lrow[e] = (float)v;
+                    lrow[e] = v;
                     T(i, j) = v;
                 }
             };
@@ -832,7 +838,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
 // flags of the candidates the modal stage flags are computed but never read.
 template <int EQ, bool RG = false, bool F = false>
 __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
-                                                       const float* __restrict__ gains, const float* __restrict__ lina,
+                                                       const float* __restrict__ gains, const void* __restrict__ lina,
                                                        const int* __restrict__ list, const int* __restrict__ count,
                                                        int* __restrict__ nominal, int fp64_form, int* __restrict__ next) {
     extern __shared__ double smem[];
@@ -849,7 +855,8 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
             const Plant& PP = plant_of<RG>(run, P, c);
             const int ns = rn.ns, nt = rn.nt, n2 = 2 * ns;
             const float* row = gains + c * rn.cuda_w;
-            const float* la = lina + c * (int64_t)rn.lina_slot;
+            const float* la = (const float*)lina + c * (int64_t)rn.lina_slot;
+            const double* la64 = (const double*)lina + c * (int64_t)rn.lina_slot;  // the FP64 form's LIN_A
             SMat T{smem + m, n2, eig_stride<EQ>()};
             // margin plant: the Plant's (observer model in batch mode, the round's plant in
             // serial mode), or in serial mode with per-candidate plants the candidate's own
@@ -861,14 +868,16 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
                 const float Kj = row[j];
                 const float md = own ? 0.0f : PP.m_d, mcj = own ? tv.c(j) : PP.m_c[j], mbi = own ? tv.bu(i) : PP.m_b[i];
                 const float maij = own ? tv.a(i, j) : PP.m_a[i * MAXS + j];
-                // OPEN_A: LIN_A's entry as k_lina_eig stored it, or formed here by the same
-                // function when the two kernels run concurrently (mixed precision only)
-                const float oa = list ? la[i * nt + j] : lina_entry(PP, BankPlantValues{PP}, row, row + ns, ns, i, j);
                 if (fp64_form) {
-                    T(i, j) = (double)oa - (double)md * (double)Li * (double)Kj;
-                    T(i, ns + j) = -((double)Li * (double)mcj);
-                    T(ns + i, j) = (double)mbi * (double)Kj;
+                    // OPEN_A from the FP64 form's double LIN_A
+                    const double oa = la64[i * nt + j];
+                    T(i, j) = __dsub_rn(oa, __dmul_rn(__dmul_rn((double)md, (double)Li), (double)Kj));
+                    T(i, ns + j) = -__dmul_rn((double)Li, (double)mcj);
+                    T(ns + i, j) = __dmul_rn((double)mbi, (double)Kj);
                 } else {
+                    // OPEN_A: LIN_A's entry as k_lina_eig stored it, or formed here by the same
+                    // function when the two kernels run concurrently (mixed precision only)
+                    const float oa = list ? la[i * nt + j] : lina_entry(PP, BankPlantValues{PP}, row, row + ns, ns, i, j);
                     T(i, j) = (double)__fsub_rn(oa, __fmul_rn(__fmul_rn(md, Li), Kj));
                     T(i, ns + j) = (double)(-__fmul_rn(Li, mcj));
                     T(ns + i, j) = (double)__fmul_rn(mbi, Kj);
@@ -945,33 +954,34 @@ static int eig_lanes(const Run& run, int64_t n) {
 }
 
 template <int EQ, bool F>
-static void lina_eig_qf(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+static void lina_eig_qf(const Run& run, const Plant& P, int precision, const float* gains, void* lina, void* eig,
                         int* nominal, int* list, int* count, cudaStream_t st) {
     const int grid = eig_grid(run, run.n, eig_mats<EQ>());
     const size_t smem = (size_t)run.nt * run.nt * eig_stride<EQ>() * sizeof(double);
     if (precision == CE_PRECISION_FP64) {
         set_smem((const void*)k_lina_eig64<EQ, F>, smem);
-        k_lina_eig64<EQ, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (double*)eig, nominal, list, count, count + 1);
+        k_lina_eig64<EQ, F><<<grid, 32, smem, st>>>(run, P, gains, (double*)lina, (double*)eig, nominal, list, count,
+                                                     count + 1);
     } else if (run.rg.runs) {
         set_smem((const void*)k_lina_eig<EQ, true, F>, smem);
-        k_lina_eig<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count,
-                                                         count + 1);
+        k_lina_eig<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, (float*)lina, (float*)eig, nominal, list,
+                                                         count, count + 1);
     } else {
         set_smem((const void*)k_lina_eig<EQ, false, F>, smem);
-        k_lina_eig<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, lina, (float*)eig, nominal, list, count,
-                                                          count + 1);
+        k_lina_eig<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, (float*)lina, (float*)eig, nominal, list,
+                                                          count, count + 1);
     }
 }
 
 template <int EQ>
-static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+static void lina_eig_q(const Run& run, const Plant& P, int precision, const float* gains, void* lina, void* eig,
                        int* nominal, int* list, int* count, cudaStream_t st) {
     if (run.eig_fused) lina_eig_qf<EQ, true>(run, P, precision, gains, lina, eig, nominal, list, count, st);
     else lina_eig_qf<EQ, false>(run, P, precision, gains, lina, eig, nominal, list, count, st);
 }
 
 template <int EQ, bool F>
-static void nominal_qf(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+static void nominal_qf(const Run& run, const Plant& P, int precision, const float* gains, const void* lina,
                        const int* list, const int* count, int* nominal, cudaStream_t st) {
     const int grid = eig_grid(run, run.n, eig_mats<EQ>());  // the listed count is only known on the device
     const size_t smem = (size_t)(2 * run.ns) * (2 * run.ns) * eig_stride<EQ>() * sizeof(double);
@@ -987,13 +997,13 @@ static void nominal_qf(const Run& run, const Plant& P, int precision, const floa
 }
 
 template <int EQ>
-static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+static void nominal_q(const Run& run, const Plant& P, int precision, const float* gains, const void* lina,
                       const int* list, const int* count, int* nominal, cudaStream_t st) {
     if (run.eig_fused) nominal_qf<EQ, true>(run, P, precision, gains, lina, list, count, nominal, st);
     else nominal_qf<EQ, false>(run, P, precision, gains, lina, list, count, nominal, st);
 }
 
-void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, float* lina, void* eig,
+void launch_lina_eig(const Run& run, const Plant& P, int precision, const float* gains, void* lina, void* eig,
                      int* nominal, int* list, int* count, cudaStream_t st, bool clear) {
     if (clear) CE_CUDA(cudaMemsetAsync(count, 0, 3 * sizeof(int), st));  // listed, lina work, nominal work
     switch (eig_lanes(run, run.n)) {
@@ -1006,7 +1016,7 @@ void launch_lina_eig(const Run& run, const Plant& P, int precision, const float*
     CE_CUDA(cudaGetLastError());
 }
 
-void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const float* lina,
+void launch_nominal(const Run& run, const Plant& P, int precision, const float* gains, const void* lina,
                     const int* list, const int* count, int* nominal, cudaStream_t st) {
     // the listed count is only known on the device: lanes as for all n candidates
     switch (eig_lanes(run, run.n)) {

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(128) k_sweep_select(const Run run_in, const in
 // fgrid row per frequency: z.re, z.im, arg z, P.re, P.im, |P|, ok, 0
 template <typename R, int NSC, bool RG = false>
 __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run_in, const float* __restrict__ gains,
-                                                            const float* __restrict__ lina,
+                                                            const R* __restrict__ lina,
                                                             const int* __restrict__ list, const int* __restrict__ count,
                                                             const R* __restrict__ fgrid, R* __restrict__ mag,
                                                             R* __restrict__ arg, R* __restrict__ bpc,
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_resp(const Run run_in, co
     const int w0 = g * SWEEP_FG, w1 = min(run.freq, w0 + SWEEP_FG);
     const int ns = run.ns, nt = run.nt;
     const float* row = gains + c * run.cuda_w;
-    const float* la = lina + c * (int64_t)run.lina_slot;
+    const R* la = lina + c * (int64_t)run.lina_slot;  // OPEN_A = LIN_A[:ns, :ns]
     R K[NSC], L[NSC];
 #pragma unroll
     for (int i = 0; i < NSC; ++i) {
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128) k_sweep_scan(const Run run_in, const int*
 }
 
 template <typename R>
-static void sweep_dispatch(const Run& run, const float* gains, const float* lina, const int* list, const int* count,
+static void sweep_dispatch(const Run& run, const float* gains, const R* lina, const int* list, const int* count,
                            const R* fgrid, float* info, const SweepScratch& sw, cudaStream_t st) {
     // the listed count is only known on the device: grids cover all n
     const dim3 grid((unsigned)((run.n + SWEEP_BLOCK - 1) / SWEEP_BLOCK), (unsigned)((run.freq + SWEEP_FG - 1) / SWEEP_FG));
@@ -283,7 +283,7 @@ static void sweep_dispatch(const Run& run, const float* gains, const float* lina
                                                                      info);
 }
 
-void launch_sweep(const Run& run, int precision, const float* gains, const float* lina, const int* nominal,
+void launch_sweep(const Run& run, int precision, const float* gains, const void* lina, const int* nominal,
                   const void* fgrid, float* info, int* list, int* count, const SweepScratch& sw, cudaStream_t st) {
     CE_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
     if (run.rg.runs) {
@@ -294,9 +294,9 @@ void launch_sweep(const Run& run, int precision, const float* gains, const float
         k_sweep_select<false><<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, nominal, info, list, count);
     }
     if (precision == CE_PRECISION_FP64)
-        sweep_dispatch<double>(run, gains, lina, list, count, (const double*)fgrid, info, sw, st);
+        sweep_dispatch<double>(run, gains, (const double*)lina, list, count, (const double*)fgrid, info, sw, st);
     else
-        sweep_dispatch<float>(run, gains, lina, list, count, (const float*)fgrid, info, sw, st);
+        sweep_dispatch<float>(run, gains, (const float*)lina, list, count, (const float*)fgrid, info, sw, st);
     CE_CUDA(cudaGetLastError());
 }
 

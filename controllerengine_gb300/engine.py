@@ -372,6 +372,21 @@ class Session:
         _check(_lib().ce_evaluate_diagnostics(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(d)))
         return out, arrs
 
+    def evaluate_diagnostics64(self, cuda_mx, info_in=None, plant_index: int = 0,
+                               want=("ywin", "summ", "lina", "eigen", "ata", "atb")):
+        """Intermediates in double as the session's precision computed them (ce_evaluate_diagnostics64)."""
+        g, i, n = self._rows(cuda_mx, info_in)
+        c = self.config
+        nt = c.total_dim
+        shapes = {"ywin": (n, c.fit_steps), "summ": (n, 3), "lina": (n, nt * nt), "eigen": (n, 2 * nt),
+                  "ata": (n, 4 * nt * nt), "atb": (n, 2 * nt)}
+        arrs = {k: np.empty(shapes[k], np.float64) for k in want}
+        dp = lambda a: None if a is None else a.ctypes.data_as(_ffi._DP)
+        d = _ffi.ce_diagnostics64(*[dp(arrs.get(k)) for k in ("ywin", "summ", "lina", "eigen", "ata", "atb")])
+        out = np.empty_like(i)
+        _check(_lib().ce_evaluate_diagnostics64(self._h, plant_index, n, _fptr(g), _fptr(i), _fptr(out), C.byref(d)))
+        return out, arrs
+
     def evaluate_plants(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, first_plant: int = 0) -> np.ndarray:
         """One plant per candidate: row c uses plant first_plant + c (ce_evaluate_plants)."""
         g, i, n = self._rows(cuda_mx, info_in)

@@ -146,6 +146,19 @@ typedef struct ce_diagnostics {
     float* atb;    /* n * 2nt           modal right-hand side       (ATB_MX_OUT.bin)   */
 } ce_diagnostics;
 
+/* The same intermediates in double, as the session's precision computed them
+ * (no counterpart in the reference): the FP64 form's values unrounded, the
+ * mixed form's floats widened.  For pinning the FP64 form against an FP64
+ * restatement of the method.  Any pointer may be NULL. */
+typedef struct ce_diagnostics64 {
+    double* ywin;  /* n * fit_steps     the trajectory's fit window, y(fit_start_id + w) */
+    double* summ;  /* n * 3             sum of y over [steady_start_id, time), max y, min y */
+    double* lina;  /* n * nt*nt         linearised closed loop */
+    double* eigen; /* n * 2nt           eigenvalues (re, im) */
+    double* ata;   /* n * (2nt)^2       modal normal matrix */
+    double* atb;   /* n * 2nt           modal right-hand side */
+} ce_diagnostics64;
+
 typedef struct ce_session ce_session;
 
 /* The functions are host API; device code compiled at run time (NVRTC) sees
@@ -196,6 +209,12 @@ CE_EXPORT int ce_evaluate(ce_session* s, int32_t plant_index, int64_t n,
 CE_EXPORT int ce_evaluate_diagnostics(ce_session* s, int32_t plant_index, int64_t n,
                                       const float* cuda_mx, const float* info_in, float* info_out,
                                       const ce_diagnostics* diag);
+
+/* As ce_evaluate, and also returns the intermediates requested in `diag` in
+ * double (no counterpart in the reference). */
+CE_EXPORT int ce_evaluate_diagnostics64(ce_session* s, int32_t plant_index, int64_t n,
+                                        const float* cuda_mx, const float* info_in, float* info_out,
+                                        const ce_diagnostics64* diag);
 
 /* Device-memory variant: pointers are device pointers, work is enqueued on
  * `stream` (a cudaStream_t; NULL = legacy default stream) and the call returns

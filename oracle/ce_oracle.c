@@ -1114,3 +1114,6 @@ int oracle_evaluate(const oc_cfg* c, const oc_plant* p, int64_t n, const float* 
     if (!atb_out) free(atb);
     return rc;
 }
+
+/* the plain FP64 form of the method (the engine's CE_PRECISION_FP64) */
+#include "ce_oracle64.h"

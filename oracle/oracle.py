@@ -22,7 +22,7 @@ F32, I32 = np.float32, np.int32
 
 
 def build(force: bool = False) -> Path:
-    newest = max((HERE / f).stat().st_mtime for f in ("ce_oracle.c", "ce_oracle_eig.h"))
+    newest = max((HERE / f).stat().st_mtime for f in ("ce_oracle.c", "ce_oracle_eig.h", "ce_oracle64.h"))
     if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "all"], check=True)
     return LIB
@@ -82,6 +82,8 @@ def lib():
         L.oracle_eigensolve.argtypes = [i64, C.c_int, _FP, _FP, _DP, C.c_int]
         L.oracle_eigensolve.restype = None
         L.oracle_eig_matrix.argtypes = [_DP, C.c_int, _DP, _DP]
+        L.oracle64_evaluate.argtypes = [C.POINTER(oc_cfg), C.POINTER(oc_plant), i64, _FP, _FP, _DP, _DP, _DP, _DP,
+                                        _DP, _DP, C.c_int]
         L.oracle_set_eig_fused.argtypes = [C.c_int]
         L.oracle_set_eig_fused.restype = None
         L.oracle_modalsetup.argtypes = [C.POINTER(oc_cfg), i64, _FP, _FP, _FP, _FP, _FP, C.c_int]
@@ -286,6 +288,30 @@ class Oracle:
         if rc < 0:
             raise ValueError("allmargin: plant has no finite nonzero gain at crossover")
         return (info, d) if diagnostics else info
+
+
+    def evaluate64(self, cuda_mx, info_in):
+        """One round in the plain FP64 form of the method (the engine's fp64 precision): the INFO
+        rows and the double intermediates ywin (n x fit_steps), summ (n x 3: sum of y over the
+        steady window, max, min), lina, eigen, ata, atb."""
+        g, n = self._g(cuda_mx)
+        info = np.array(info_in, F32, copy=True, order="C").reshape(n, self.info_w)
+        nt = self.nt
+        d = oc_der()
+        lib().oracle_derived(C.byref(self.cfg), C.byref(d))
+        fit_steps = int(np.ceil(np.float32(d.fit_len))) if d.fit_len > 0 else 0
+        out = dict(ywin=np.empty((n, fit_steps)), summ=np.empty((n, 3)), lina=np.empty((n, nt * nt)),
+                   eigen=np.empty((n, 2 * nt)), ata=np.empty((n, 4 * nt * nt)), atb=np.empty((n, 2 * nt)))
+        dp = lambda a: a.ctypes.data_as(_DP)
+        lib().oracle_set_eig_fused(int(self.eig_fused))
+        rc = lib().oracle64_evaluate(C.byref(self.cfg), C.byref(self.plant), n, _f(g), _f(info), dp(out["ywin"]),
+                                     dp(out["summ"]), dp(out["lina"]), dp(out["eigen"]), dp(out["ata"]),
+                                     dp(out["atb"]), self.threads)
+        if rc > 0:
+            raise ValueError(f"oracle decode error (digit {rc - 1})")
+        if rc < 0:
+            raise ValueError("allmargin: plant has no finite nonzero gain at crossover")
+        return info, out
 
 
 def eig_matrix(A: np.ndarray, fused: bool = False):

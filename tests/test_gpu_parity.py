@@ -117,20 +117,6 @@ def test_batch_size_independence(lib, eight_state_small):
     assert _eq(full, part) and _eq(full[100:101], one)
 
 
-def test_fp64_form_runs_and_agrees_on_classification(lib, eight_state_small):
-    p = eight_state_small
-    cfg = ce.EngineConfig.parse(p.config_text)
-    with ce.Session(cfg, p.plant, precision="fp64") as s:
-        f64 = s.evaluate(p.cuda_mx, p.info_mx)
-    with ce.Session(cfg, p.plant) as s:
-        mix = s.evaluate(p.cuda_mx, p.info_mx)
-    ca, cb = _classes(mix, cfg), _classes(f64, cfg)
-    assert (ca != cb).any(axis=1).mean() < 0.01
-    c = _cols(cfg)
-    ok = ~(ca != cb).any(axis=1) & (mix[:, c["am"]][:, 3] == 1)
-    np.testing.assert_allclose(mix[ok][:, c["am"]][:, 4], f64[ok][:, c["am"]][:, 4], rtol=1e-3)
-
-
 def test_margins_closed_form(lib, oracle_mod):
     """The margin sweep on a loop with a closed form (synth.first_order_loop, 2,000 points): GM, PM
     and DM within 1e-3 dB / deg / ms of the exact margins, b_PC within 1e-5 of the minimum over

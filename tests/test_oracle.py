@@ -173,3 +173,51 @@ def test_fused_eigensolve_agrees_with_separate_on_the_eight_state_workload(oracl
     ra = sep.allmargin(lina, p.cuda_mx, p.info_mx)
     rb = fus.allmargin(lina, p.cuda_mx, p.info_mx)
     assert np.array_equal(ra, rb, equal_nan=True)
+
+
+def test_fp64_sim_linear_matches_float64_recurrence(oracle_mod):
+    """The oracle's FP64 form of the simulation, with no nonlinearity and K = L = 0, is the plant's
+    step response to u = N r computed in float64 (the same recurrence, fused as the engine fuses
+    it): 1e-12 relative, against 1e-5 for the float form above."""
+    p = synth.mass_spring(1536)
+    p.plant.nl_info[:] = 0
+    g = np.zeros((1, 7), np.float32)
+    g[0, 6] = 2.0
+    cfg = ce.EngineConfig.parse(p.config_text)
+    _, d = oracle_mod.Oracle(p.config_text, p.plant).evaluate64(g, p.info_mx[:1])
+    A = p.plant.discrete_a.reshape(2, 2).astype(np.float64)
+    B = p.plant.discrete_bu.astype(np.float64)
+    x = np.zeros(2)
+    ref = np.empty(cfg.time)
+    for t in range(cfg.time):
+        ref[t] = x[0]
+        u = 0.0 if t < cfg.ref_step_id else 2.0
+        x = A @ x + B * u
+    w = ref[cfg.fit_start_id:cfg.fit_start_id + cfg.fit_steps]
+    np.testing.assert_allclose(d["ywin"][0], w, rtol=1e-12, atol=1e-15 * np.abs(w).max())
+    np.testing.assert_allclose(d["summ"][0, 0], ref[cfg.steady_start_id:].sum(), rtol=1e-12)
+
+
+def test_fp64_margins_closed_form(oracle_mod):
+    """The oracle's FP64 margins on the loop with a closed form converge to the exact margins at
+    second order in the grid spacing, like the float restatement, and sit within 1e-3 of them at
+    2,000 points; the remaining error is the linear interpolation between grid points."""
+    from parity_helpers import closed_form_margins
+    errs = {}
+    for F in (200, 400, 2000):
+        p = synth.first_order_loop(freq=F, gains=((5.0, 0.05), (20.0, 0.2)))
+        cfg = ce.EngineConfig.parse(p.config_text)
+        orc = oracle_mod.Oracle(p.config_text, p.plant)
+        out, d = orc.evaluate64(p.cuda_mx, p.info_mx)
+        for r in range(2):
+            am = out[r, cfg.info_allmargin:cfg.info_allmargin + 5]
+            want = closed_form_margins(p, d["lina"][r, 0], cfg.crossover, row=r)
+            if am[3] != 1.0:
+                continue
+            errs[F, r] = np.abs(am[[0, 1]] - [want["gm"], want["pm"]])
+    assert errs, "no candidate reached the margin sweep"
+    for (F, r), e in errs.items():
+        if F == 2000:
+            assert (e < 1e-3).all(), e
+        if F == 200 and (400, r) in errs:
+            assert (e > 3 * errs[400, r]).all(), (e, errs[400, r])
