@@ -46,26 +46,84 @@ def workload_args(a):
     return dict(n=a.candidates, time=a.time, freq=a.freq)
 
 
-def precision_report(mixed, fp64, cfg):
-    """Cost rows of the mixed path (the reference's arithmetic) against the plain FP64 form of
-    the same method on the same candidates: agreement of the pass/fail classes and the
-    relative error of each cost term where both paths score the candidate."""
+def precision_report(rows, fp64, cfg):
+    """Cost rows of one form (the mixed form: the reference's arithmetic; or the compensated
+    form) against the plain FP64 form of the same method on the same candidates: agreement of
+    the pass/fail classes, and per cost term, over the candidates both forms score, the
+    relative error (median, p99, max, and the fraction within 1e-6).  The overshoot is a
+    fraction that is often ~0, so its error is absolute."""
     s, am, fr = cfg.info_scoring, cfg.info_allmargin, cfg.info_freqresp
     def classes(x):
         return np.stack([x[:, s + 1] >= cfg.unstable_err, x[:, s + 2] == np.float32(cfg.unstable_err),
                          x[:, s + 2] == np.float32(cfg.eig_fail_err), x[:, am + 3] == 1.0], axis=1)
-    cm, cf = classes(mixed), classes(fp64)
+    cm, cf = classes(rows), classes(fp64)
     same = (cm == cf).all(axis=1)
     scored = same & ~cm[:, 0] & ~cm[:, 1] & ~cm[:, 2]
     terms = {"total_score": s, "behaviour_err": s + 1, "margin_err": s + 2, "wn": fr, "zeta": fr + 1,
-             "overshoot": fr + 2, "yss": fr + 3, "gm_db": am, "pm_deg": am + 1, "b_pc": am + 4}
+             "overshoot_abs": fr + 2, "yss": fr + 3, "gm_db": am, "pm_deg": am + 1, "dm_ms": am + 2,
+             "b_pc": am + 4}
     rel = {}
     for name, col in terms.items():
-        a_, b_ = mixed[scored, col].astype(np.float64), fp64[scored, col].astype(np.float64)
+        a_, b_ = rows[scored, col].astype(np.float64), fp64[scored, col].astype(np.float64)
         ok = np.isfinite(a_) & np.isfinite(b_) & (np.abs(b_) < 1e30)
-        e = np.abs(a_[ok] - b_[ok]) / np.maximum(np.abs(b_[ok]), 1e-30)
-        rel[name] = {"median": float(np.median(e)) if e.size else None, "p99": float(np.quantile(e, 0.99)) if e.size else None}
+        den = 1.0 if name.endswith("_abs") else np.maximum(np.abs(b_[ok]), 1e-30)
+        e = np.abs(a_[ok] - b_[ok]) / den
+        rel[name] = ({"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)), "max": float(e.max()),
+                      "within_1e-6": float((e <= 1e-6).mean())} if e.size else None)
     return {"class_agreement": float(same.mean()), "candidates_compared": int(scored.sum()), "relative_error": rel}
+
+
+def precision_floor(sess, problem, cfg, sample: int = 4096):
+    """Where the compensated form's fit-derived terms miss 1e-6 of the FP64 form: on a sample of
+    the batch, per candidate, the FP32 trajectory's difference from the FP64 one (max over the
+    fit window, relative to the window's largest |y|) and the condition number of the scaled
+    normal matrix (the system the modal solve factors, from the FP64 form); then, binned by that
+    condition number, the median relative error of wn, zeta and the behaviour error for the
+    compensated and the mixed forms.  Error ~ condition x trajectory difference marks the FP32
+    trajectory as the floor."""
+    g, info = problem.cuda_mx[:sample], problem.info_mx[:sample]
+    nt = cfg.total_dim
+    out = {}
+    prev = sess.precision
+    for form in ("fp64", "compensated", "mixed"):
+        sess.set_precision(form)
+        out[form] = sess.evaluate_diagnostics64(g, info, want=("ywin", "ata"))
+    sess.set_precision(prev)
+    (f64, d64), (cmp_, dc), (mix, _) = out["fp64"], out["compensated"], out["mixed"]
+    s, fr, md = cfg.info_scoring, cfg.info_freqresp, cfg.info_modal
+    yscale = np.maximum(np.abs(d64["ywin"]).max(axis=1), 1e-30)
+    traj = np.abs(dc["ywin"] - d64["ywin"]).max(axis=1) / yscale
+    uniq = f64[:, md + 3 * nt].astype(int)
+    cond = np.full(len(g), np.inf)
+    ata = d64["ata"].reshape(-1, 2 * nt, 2 * nt)
+    for u in np.unique(uniq):
+        if u <= 0:
+            continue
+        idx = np.where(uniq == u)[0]
+        A = ata[idx, :2 * u, :2 * u]
+        A = np.tril(A) + np.transpose(np.tril(A, -1), (0, 2, 1))
+        dg = np.sqrt(np.abs(np.einsum("kii->ki", A)))
+        dg[dg <= 1e-6] = 1.0
+        with np.errstate(all="ignore"):
+            cond[idx] = np.linalg.cond(A / dg[:, :, None] / dg[:, None, :])
+    scored = (f64[:, s + 1] < cfg.unstable_err) & (cmp_[:, s + 1] < cfg.unstable_err) & np.isfinite(cond)
+    def rel(x, col):
+        a_, b_ = x[:, col].astype(np.float64), f64[:, col].astype(np.float64)
+        return np.abs(a_ - b_) / np.maximum(np.abs(b_), 1e-30)
+    bins = []
+    for lo in range(0, 12, 2):
+        sel = scored & (cond >= 10.0 ** lo) & (cond < 10.0 ** (lo + 2))
+        if sel.sum() < 4:
+            continue
+        row = {"cond": f"1e{lo}..1e{lo + 2}", "candidates": int(sel.sum()),
+               "trajectory_rel_diff_median": float(np.median(traj[sel]))}
+        for name, col in (("wn", fr), ("zeta", fr + 1), ("behaviour_err", s + 1)):
+            row[f"{name}_compensated"] = float(np.median(rel(cmp_, col)[sel]))
+            row[f"{name}_mixed"] = float(np.median(rel(mix, col)[sel]))
+        bins.append(row)
+    return {"sample": int(len(g)), "trajectory_rel_diff": {"median": float(np.median(traj)),
+                                                            "p99": float(np.quantile(traj, 0.99))},
+            "by_condition": bins}
 
 
 def fit_ops(eigen, steps):
@@ -671,6 +729,8 @@ def main():
     ap.add_argument("--kalman-candidates", type=int, default=65536, help="Kalman-observer workload (0: skip)")
     ap.add_argument("--uneven-instances", type=int, default=16384, help="uneven-size ragged batch (0: skip)")
     ap.add_argument("--small-steps", type=int, default=10, help="the small mass-spring case (0: skip)")
+    ap.add_argument("--floor-sample", type=int, default=4096,
+                    help="candidates of the precision-floor analysis (trajectory difference, conditioning; 0: skip)")
     ap.add_argument("--eig-compare", type=int, default=1,
                     help="also run the other eigensolve arithmetic on the batch and compare rows (0: skip)")
     a = ap.parse_args()
@@ -802,7 +862,27 @@ def main():
         fp64 = {"value": world * n / (f_ms * 1e-3), "unit": UNIT, "ms_per_step": f_ms,
                 "speedup_of_mixed": (world * n / (ms_per_step * 1e-3)) / (world * n / (f_ms * 1e-3)),
                 "mixed_vs_fp64": precision_report(mixed_rows, fp64_rows, cfg)}
+        # the compensated form on the same batch, against the same FP64 rows
+        sess.set_precision("compensated")
+        step()
+        torch.cuda.synchronize()
+        comp_rows = info_out.cpu().numpy()
+        sess.set_profiling(True)
+        e0.record(stream)
+        for _ in range(a.fp64_steps + 1):
+            flush.zero_()
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        c_stages = {k: v[0] / (a.fp64_steps + 1) for k, v in sess.stage_times().items()}
+        sess.set_profiling(False)
+        c_ms = e0.elapsed_time(e1) / (a.fp64_steps + 1)
+        fp64["compensated"] = {"value": world * n / (c_ms * 1e-3), "unit": UNIT, "ms_per_step": c_ms,
+                               "speedup_of_fp64_form": f_ms / c_ms, "stages_ms_per_step": c_stages,
+                               "compensated_vs_fp64": precision_report(comp_rows, fp64_rows, cfg)}
         sess.set_precision("mixed")
+        if a.floor_sample > 0:
+            fp64["precision_floor"] = precision_floor(sess, problem, cfg, a.floor_sample)
 
     # ---- eigensolve arithmetic: the separate (reference) form on the same batch ----
     eig_cmp = None

@@ -19,6 +19,7 @@ MAX_NONLIN_DIM = 4
 MAX_TOTAL_DIM = 16
 PRECISION_MIXED = 0
 PRECISION_FP64 = 1
+PRECISION_COMPENSATED = 2
 EIG_ARITH_SEPARATE = 0
 EIG_ARITH_FUSED = 1
 

@@ -67,6 +67,19 @@ __device__ __forceinline__ void df_add(float& HI, float& LO, float hi, float lo)
     LO = __fsub_rn(v, __fsub_rn(HI, sh));
 }
 
+// Steady-state sum of the trajectory.  s is the plain float sum in t order
+// (the reference's, ref: src/modalsetup.cu:54-56), unchanged; comp collects
+// the exact rounding error of each addition (TwoSum), so s + comp is the
+// compensated sum (the Kahan-Babuska / Neumaier form) that the compensated
+// precision reads.
+__device__ __forceinline__ void ysum_add(float& s, float& comp, float y) {
+    const float t = __fadd_rn(s, y);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(y, bp));
+    comp = __fadd_rn(comp, err);
+    s = t;
+}
+
 // ---- the instruction interpreter (ref: src/main.cu:260-291) ------------------
 // Evaluates one SKIP-free chain of `n` instructions.  `src` holds the NSRC
 // source values addressed by the instruction column; column `ycol` (if >= 0)

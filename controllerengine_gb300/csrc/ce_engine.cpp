@@ -189,22 +189,40 @@ void dev_alloc(T*& p, size_t count) {
     CE_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
 }
 
+// Element size in bytes of each per-candidate buffer of a precision: the fit
+// window and the trajectory summaries (FP32 simulation: float), LIN_A and the
+// eigenvalues, AtA / Atb, and the sweep scratch.
+struct BufElems {
+    size_t ywin, summ, lina, eig, ata, sweep;
+};
+BufElems buf_elems(int precision) {
+    if (precision == CE_PRECISION_FP64) return {8, 8, 8, 8, 8, 8};
+    if (precision == CE_PRECISION_COMPENSATED) return {4, 4, 8, 8, 8, 8};
+    return {4, 4, 4, 4, 4, 4};
+}
+// The arithmetic each stage runs in under a session precision: the compensated
+// form simulates in FP32 (the mixed kernels) and runs LIN_A, the eigensolves and
+// the sweep in FP64 (the FP64 form's kernels).
+int sim_precision(int prec) { return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_MIXED : prec; }
+int eig_precision(int prec) { return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_FP64 : prec; }
+bool grids64(int prec) { return prec != CE_PRECISION_MIXED; }
+
 void ensure_buffers(ce_session* s, int64_t n, bool traj) {
     Buffers& b = s->buf;
     const ce_config& c = s->cfg;
     const int nt = c.total_dim, pitch = fit_pitch(c.fit_steps);
-    const size_t rsz = s->precision == CE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    const BufElems e = buf_elems(s->precision);
     if (n > b.cap || b.precision != s->precision || b.nt != nt || b.pitch != pitch) {
         b.release();
         const int64_t cap = n;
         dev_alloc(b.gains, (size_t)cap * c.cuda_mx_width);
         dev_alloc(b.info, (size_t)cap * c.info_mx_width);
-        CE_CUDA(cudaMalloc(&b.lina, (size_t)cap * nt * nt * rsz + 16));
-        CE_CUDA(cudaMalloc(&b.eig, (size_t)cap * 2 * nt * rsz + 16));
-        CE_CUDA(cudaMalloc(&b.ywin, (size_t)cap * pitch * rsz + 64));
-        CE_CUDA(cudaMalloc(&b.summ, (size_t)cap * 4 * rsz + 64));
-        CE_CUDA(cudaMalloc(&b.ata, (size_t)cap * 4 * nt * nt * rsz + 16));
-        CE_CUDA(cudaMalloc(&b.atb, (size_t)cap * 2 * nt * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.lina, (size_t)cap * nt * nt * e.lina + 16));
+        CE_CUDA(cudaMalloc(&b.eig, (size_t)cap * 2 * nt * e.eig + 16));
+        CE_CUDA(cudaMalloc(&b.ywin, (size_t)cap * pitch * e.ywin + 64));
+        CE_CUDA(cudaMalloc(&b.summ, (size_t)cap * 4 * e.summ + 64));
+        CE_CUDA(cudaMalloc(&b.ata, (size_t)cap * 4 * nt * nt * e.ata + 16));
+        CE_CUDA(cudaMalloc(&b.atb, (size_t)cap * 2 * nt * e.ata + 16));
         dev_alloc(b.nominal, (size_t)cap);
         dev_alloc(b.fit_counts, (size_t)(MAXT + 1) * MAX_CHUNKS);
         dev_alloc(b.fit_order, (size_t)(MAXT + 1) * cap);
@@ -216,9 +234,9 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         dev_alloc(b.plant_idx, (size_t)cap);
         // shared by the chunks, which the sweep processes one after the other
         const size_t groups = (size_t)(c.freq + SWEEP_FG - 1) / SWEEP_FG;
-        CE_CUDA(cudaMalloc(&b.sweep.mag, (size_t)cap * c.freq * rsz + 16));
-        CE_CUDA(cudaMalloc(&b.sweep.arg, (size_t)cap * c.freq * rsz + 16));
-        CE_CUDA(cudaMalloc(&b.sweep.bpc, (size_t)cap * groups * rsz + 16));
+        CE_CUDA(cudaMalloc(&b.sweep.mag, (size_t)cap * c.freq * e.sweep + 16));
+        CE_CUDA(cudaMalloc(&b.sweep.arg, (size_t)cap * c.freq * e.sweep + 16));
+        CE_CUDA(cudaMalloc(&b.sweep.bpc, (size_t)cap * groups * e.sweep + 16));
         dev_alloc(b.sweep.fail, (size_t)cap * groups);
         if (c.observer == CE_OBSERVER_KALMAN) {
             // one block: cnt | fill | totals (cleared together) | hoff | poff
@@ -375,8 +393,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     for (int64_t q = 0; q < np_used; ++q)
         if (!s->plant_err[plant + q].empty()) throw std::runtime_error(s->plant_err[plant + q]);
     const int prec = s->precision;
-    if (prec == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
-    if (per_candidate) ensure_plant_table(s, prec);
+    if (grids64(prec) && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
+    if (per_candidate) ensure_plant_table(s, sim_precision(prec));
     ensure_buffers(s, n, traj);
     Buffers& b = s->buf;
     Run r = make_run(s, plant, n);
@@ -391,16 +409,16 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         r.mc.np = s->n_plants;
         r.mc.first = plant;
         r.mc.grid_stride = s->cfg.serial ? (int64_t)s->cfg.freq * 8 : 0;
-        r.mc.alpha = prec == CE_PRECISION_FP64 ? (const void*)s->d_alpha64 : (const void*)s->d_alpha32;
+        r.mc.alpha = grids64(prec) ? (const void*)s->d_alpha64 : (const void*)s->d_alpha32;
         r.mc.margin = s->cfg.serial ? 1 : 0;
         r.mc.idx = plant_idx;
     }
     const Plant& P = s->plants[plant];
     const size_t goff = (size_t)s->grid_of(plant) * s->cfg.freq * 8;
-    const void* fgrid = prec == CE_PRECISION_FP64 ? (const void*)(s->d_fgrid64 + goff) : (const void*)(s->d_fgrid32 + goff);
+    const void* fgrid = grids64(prec) ? (const void*)(s->d_fgrid64 + goff) : (const void*)(s->d_fgrid32 + goff);
     // a chunk's grid argument is the grid of its first plant (mc.first); with
     // plant indices every chunk keeps plant 0's
-    const size_t gstep = (size_t)(per_candidate && !plant_idx ? r.mc.grid_stride : 0) * (prec == CE_PRECISION_FP64 ? 8 : 4);
+    const size_t gstep = (size_t)(per_candidate && !plant_idx ? r.mc.grid_stride : 0) * (grids64(prec) ? 8 : 4);
     // each launch optionally bracketed by events on the stream it runs on
     auto timed = [&](int stage, cudaStream_t on, auto&& launch) {
         if (!s->profiling) {
@@ -420,11 +438,12 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     // rest of each SM and run alongside.  Large batches are cut into chunks so
     // that the fit of a chunk starts as soon as its eigenvalues are known, while
     // the eigensolves of the next chunks continue.
-    const SimKernels sk = prec != CE_PRECISION_MIXED ? SimKernels{} : per_candidate ? s->sim_kernel_mc : s->sim_kernel[plant];
+    const int sprec = sim_precision(prec), eprec = eig_precision(prec);
+    const SimKernels sk = sprec != CE_PRECISION_MIXED ? SimKernels{} : per_candidate ? s->sim_kernel_mc : s->sim_kernel[plant];
     cudaStream_t fs = s->fast, ss = s->side;
     const int nch = n_chunks(s, n);
     const int64_t per = (n + nch - 1) / nch;
-    const size_t rsz = prec == CE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    const BufElems be = buf_elems(prec);
     const int nt = r.nt, cw = r.cuda_w, iw = r.info_w;
     auto chunk = [&](int k, Run& rc, int64_t& off) {
         off = k * per;
@@ -454,7 +473,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         int64_t off;
         chunk(k, rc, off);
         timed(0, ss, [&] {
-            launch_lina_eig(rc, P, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz), at(b.eig, off, 2 * nt * rsz),
+            launch_lina_eig(rc, P, eprec, d_gains + off * cw, at(b.lina, off, nt * nt * be.lina), at(b.eig, off, 2 * nt * be.eig),
                             b.nominal + off, nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, ss,
                             !nom_all);
         });
@@ -466,7 +485,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         cudaStream_t on = nom_all ? ns2 : ss;
         timed(4, on, [&] {
-            launch_nominal(rc, P, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz),
+            launch_nominal(rc, P, eprec, d_gains + off * cw, at(b.lina, off, nt * nt * be.lina),
                            nom_all ? nullptr : b.nominal_list + off, b.nominal_count + 3 * k, b.nominal + off, on);
         });
         CE_CUDA(cudaEventRecord(s->ev_nom[k], on));
@@ -489,8 +508,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
                 launch_sim_specialised(sk.shared, rh, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
                 launch_sim_specialised(sk.main, rp, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
             } else {
-                launch_sim(rh, P, prec, d_gains, b.ywin, b.summ, tr, fs);
-                launch_sim(rp, P, prec, d_gains, b.ywin, b.summ, tr, fs);
+                launch_sim(rh, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
+                launch_sim(rp, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
             }
         } else if (sk) {
             // a batch too small to fill the GPU runs four lanes per candidate
@@ -499,7 +518,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
             launch_sim_specialised(wide ? sk.wide : sk.main, r, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr,
                                    fs, wide);
         } else {
-            launch_sim(r, P, prec, d_gains, b.ywin, b.summ, tr, fs);
+            launch_sim(r, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
         }
     });
     for (int k = 0; k < nch; ++k) {
@@ -507,12 +526,18 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         int64_t off;
         chunk(k, rc, off);
         CE_CUDA(cudaStreamWaitEvent(fs, s->ev_eig[k], 0));
-        const void* eig = at(b.eig, off, 2 * nt * rsz);
-        void* ata = at(b.ata, off, 4 * nt * nt * rsz);
-        void* atb = at(b.atb, off, 2 * nt * rsz);
+        const void* eig = at(b.eig, off, 2 * nt * be.eig);
+        void* ata = at(b.ata, off, 4 * nt * nt * be.ata);
+        void* atb = at(b.atb, off, 2 * nt * be.ata);
+        const void* ywin = at(b.ywin, off, (size_t)r.fit_pitch * be.ywin);
+        const void* summ = at(b.summ, off, 4 * be.summ);
         timed(2, fs, [&] {
-            launch_fit(rc, prec, eig, at(b.ywin, off, (size_t)r.fit_pitch * rsz), at(b.summ, off, 4 * rsz), ata, atb,
-                       d_info + off * iw, b.fit_counts + (MAXT + 1) * k, b.fit_order + (MAXT + 1) * off, fs);
+            if (prec == CE_PRECISION_COMPENSATED)
+                launch_fit_comp(rc, eig, ywin, summ, ata, atb, d_info + off * iw, b.fit_counts + (MAXT + 1) * k,
+                                b.fit_order + (MAXT + 1) * off, fs);
+            else
+                launch_fit(rc, prec, eig, ywin, summ, ata, atb, d_info + off * iw, b.fit_counts + (MAXT + 1) * k,
+                           b.fit_order + (MAXT + 1) * off, fs);
         });
         timed(3, fs, [&] { launch_modal(rc, prec, eig, ata, atb, d_info + off * iw, fs); });
     }
@@ -522,7 +547,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         chunk(k, rc, off);
         CE_CUDA(cudaStreamWaitEvent(fs, s->ev_nom[k], 0));
         timed(5, fs, [&] {
-            launch_sweep(rc, prec, d_gains + off * cw, at(b.lina, off, nt * nt * rsz), b.nominal + off, at(fgrid, off, gstep),
+            launch_sweep(rc, eprec, d_gains + off * cw, at(b.lina, off, nt * nt * be.lina), b.nominal + off, at(fgrid, off, gstep),
                          d_info + off * iw, b.sweep_list + off, b.sweep_count + k, b.sweep, fs);
         });
     }
@@ -843,7 +868,7 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
     run_pipeline(s, plant, n, b.gains, b.info, st, traj, per_candidate);
     CE_CUDA(cudaMemcpyAsync(info_out, b.info, (size_t)n * c.info_mx_width * sizeof(float), cudaMemcpyDeviceToHost, st));
     const int nt = c.total_dim;
-    const bool f64 = s->precision == CE_PRECISION_FP64;
+    const BufElems be = buf_elems(s->precision);
     std::vector<double> tmp;
     if (diag) {
         if (diag->yplant)
@@ -851,9 +876,9 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
     }
     CE_CUDA(cudaStreamSynchronize(st));
     if (diag) {
-        auto pull = [&](float* dst, const void* src, size_t count) {
+        auto pull = [&](float* dst, const void* src, size_t count, size_t bytes) {
             if (!dst) return;
-            if (!f64) {
+            if (bytes == sizeof(float)) {
                 CE_CUDA(cudaMemcpy(dst, src, count * sizeof(float), cudaMemcpyDeviceToHost));
             } else {
                 tmp.resize(count);
@@ -861,20 +886,11 @@ void evaluate_host(ce_session* s, int plant, int64_t n, const float* cuda_mx, co
                 for (size_t i = 0; i < count; ++i) dst[i] = (float)tmp[i];
             }
         };
-        pull(diag->lina, b.lina, (size_t)n * nt * nt);
-        pull(diag->eigen, b.eig, (size_t)n * 2 * nt);
-        pull(diag->ata, b.ata, (size_t)n * 4 * nt * nt);
-        pull(diag->atb, b.atb, (size_t)n * 2 * nt);
+        pull(diag->lina, b.lina, (size_t)n * nt * nt, be.lina);
+        pull(diag->eigen, b.eig, (size_t)n * 2 * nt, be.eig);
+        pull(diag->ata, b.ata, (size_t)n * 4 * nt * nt, be.ata);
+        pull(diag->atb, b.atb, (size_t)n * 2 * nt, be.ata);
     }
-}
-
-// Element size in bytes of each per-candidate buffer of the session's precision.
-struct BufElems {
-    size_t ywin, summ, lina, eig, ata;
-};
-BufElems buf_elems(int precision) {
-    if (precision == CE_PRECISION_FP64) return {8, 8, 8, 8, 8};
-    return {4, 4, 4, 4, 4};
 }
 
 // Device buffer of n records of `count` elements (`stride` elements apart,
@@ -899,7 +915,7 @@ void evaluate_host64(ce_session* s, int plant, int64_t n, const float* cuda_mx, 
     const int64_t nt = c.total_dim;
     const BufElems e = buf_elems(s->precision);
     pull64(diag->ywin, b.ywin, n, c.fit_steps, fit_pitch(c.fit_steps), e.ywin);
-    pull64(diag->summ, b.summ, n, 3, 4, e.summ);
+    pull64(diag->summ, b.summ, n, 4, 4, e.summ);
     pull64(diag->lina, b.lina, n, nt * nt, nt * nt, e.lina);
     pull64(diag->eigen, b.eig, n, 2 * nt, 2 * nt, e.eig);
     pull64(diag->ata, b.ata, n, 4 * nt * nt, 4 * nt * nt, e.ata);
@@ -1390,8 +1406,8 @@ void session_set_small_batch_forms(ce_session* s, bool on) { s->small_forms = on
 // batch waits on an allocation.
 void session_prepare(ce_session* s, int64_t n, bool plants) {
     if (n > 0) ensure_buffers(s, n, false);
-    if (s->precision == CE_PRECISION_FP64 && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
-    if (plants) ensure_plant_table(s, s->precision);
+    if (grids64(s->precision) && !s->d_fgrid64) build_grids(s, CE_PRECISION_FP64);
+    if (plants) ensure_plant_table(s, sim_precision(s->precision));
     CE_CUDA(cudaDeviceSynchronize());
 }
 Run session_run(const ce_session* s, int plant, int64_t n) { return make_run(s, plant, n); }
@@ -1475,7 +1491,8 @@ CE_EXPORT int ce_session_get_eig_arith(const ce_session* s, int32_t* arith) {
 CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {
         if (!s) fail("null session");
-        if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64) fail("unknown precision {}", precision);
+        if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64 && precision != CE_PRECISION_COMPENSATED)
+            fail("unknown precision {}", precision);
         if (precision == CE_PRECISION_FP64 && s->cfg.observer == CE_OBSERVER_KALMAN)
             fail("the Kalman observer (observer = kalman) runs in mixed precision only");
         s->precision = precision;

@@ -146,10 +146,10 @@ struct Run {
 // Per-candidate simulation summary (the parts of the trajectory that modalsetup
 // reads besides the fit window).
 struct SimSummary {
-    float ysum;  // plain float sum of y over [steady_start_id, time), in t order
-    float ymax;  // NaN-ignoring max of y over [0, time)
-    float ymin;  // NaN-ignoring min of y over [0, time)
-    float pad;
+    float ysum;   // plain float sum of y over [steady_start_id, time), in t order
+    float ymax;   // NaN-ignoring max of y over [0, time)
+    float ymin;   // NaN-ignoring min of y over [0, time)
+    float ycomp;  // the rounding errors of that sum (TwoSum): ysum + ycomp is the compensated sum
 };
 
 }  // namespace ce

@@ -333,6 +333,254 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __
 }
 
 // ---------------------------------------------------------------------------
+// The modal setup of the compensated precision (CE_PRECISION_COMPENSATED).
+//
+// Same quantities as k_fit -- yss, overshoot, AtA and Atb of the fit of
+// y - yss to e^{sigma t - shift} (cos, sin)(omega t) over the window -- from
+// the FP32 trajectory, with the modes from the FP64 eigenvalues (never cast
+// to float), and with no unstructured rounding in the normal equations:
+//  * yss from the compensated steady-state sum (ysum + ycomp) in double;
+//  * AtA in closed form.  Every entry is a sum over the window of a product
+//    of two basis functions, i.e. of e^{(s_m + s_k) t} or e^{(conj(s_m) + s_k) t}
+//    (s = sigma + i omega), and such a sum is geometric:
+//      sum_{w<n} e^{s (t0 + w ts)} = e^{s t0} expm1(n s ts) / expm1(s ts),
+//    evaluated in FP64 with complex expm1 so that ratios near 1 lose nothing;
+//  * Atb = sum_w b(t_w) (y_w - yss) = sum_w b(t_w) y_w - yss sum_w b(t_w): the
+//    second sum geometric as above, the first a projection of the trajectory
+//    onto e^{s t}, accumulated by a complex recurrence z <- z e^{s ts} in
+//    double-float arithmetic on the FP32 pipe (two floats per real; products
+//    exact by FMA, sums by TwoSum), the accumulator as a TwoSum high part with
+//    a float low part collecting every error term; z is re-anchored from an
+//    FP64 exp / sincos every FC_ANCHOR steps, so its drift stays below
+//    FC_ANCHOR x 2^-47 relative.
+// AtA and the projection agree with the exact values of the same basis to
+// ~1e-14 relative, so the solve sees no rounding of the normal equations that
+// its conditioning could amplify; what remains is the FP32 trajectory itself.
+//
+// Layout: 16 lanes per candidate (the k_fit layout and its class order).  A
+// mode's projection is split into 16 / unique contiguous window segments, one
+// lane each, combined in segment order; the Gram pairs are spread over the
+// lanes.
+
+// double-float number h + l on the FP32 pipe
+struct dff {
+    float h, l;
+};
+__device__ __forceinline__ dff dff_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(__dsub_rn(x, (double)h))};
+}
+__device__ __forceinline__ dff dff_norm(float a, float b) {  // TwoSum renormalisation of a + b
+    float s, e;
+    df_two_sum(a, b, s, e);
+    return {s, e};
+}
+__device__ __forceinline__ dff dff_mul(dff a, dff b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return dff_norm(p, e);
+}
+__device__ __forceinline__ dff dff_add(dff a, dff b) {
+    float s, e;
+    df_two_sum(a.h, b.h, s, e);
+    return dff_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dff dff_neg(dff a) { return {-a.h, -a.l}; }
+struct cdff {
+    dff re, im;
+};
+__device__ __forceinline__ cdff cdff_mul(cdff a, cdff b) {
+    return {dff_add(dff_mul(a.re, b.re), dff_neg(dff_mul(a.im, b.im))),
+            dff_add(dff_mul(a.re, b.im), dff_mul(a.im, b.re))};
+}
+// sum of y * z (y a float, z double-float): TwoSum high part, every error
+// term into the float low part
+struct acc2 {
+    float h, l;
+};
+__device__ __forceinline__ void acc2_add(acc2& s, float y, dff z) {
+    const float p = __fmul_rn(y, z.h);
+    float e = __fmaf_rn(y, z.h, -p);
+    e = __fmaf_rn(y, z.l, e);
+    float t, err;
+    df_two_sum(s.h, p, t, err);
+    s.h = t;
+    s.l = __fadd_rn(s.l, __fadd_rn(err, e));
+}
+
+// complex e^z - 1, accurate near 0: (expm1(x) cos y - 2 sin^2(y/2), e^x sin y)
+__device__ __forceinline__ cplx<double> cexpm1_(double x, double y) {
+    double sy, cy, sh, ch;
+    sincos(y, &sy, &cy);
+    sincos(0.5 * y, &sh, &ch);
+    const double em = expm1(x);
+    return {__dsub_rn(__dmul_rn(em, cy), __dmul_rn(2.0, __dmul_rn(sh, sh))), __dmul_rn(exp(x), sy)};
+}
+
+// sum_{w<n} e^{(x + i y) (t0 + w ts) - sh}
+__device__ __forceinline__ cplx<double> geo_sum(double x, double y, double t0, double ts, int n, double sh) {
+    double sy, cy;
+    sincos(__dmul_rn(y, t0), &sy, &cy);
+    const double a = exp(__fma_rn(x, t0, -sh));
+    const cplx<double> first{__dmul_rn(a, cy), __dmul_rn(a, sy)};
+    if (x == 0.0 && y == 0.0) return {__dmul_rn(first.re, (double)n), __dmul_rn(first.im, (double)n)};
+    const cplx<double> num = cexpm1_(__dmul_rn((double)n, __dmul_rn(x, ts)), __dmul_rn((double)n, __dmul_rn(y, ts)));
+    const cplx<double> den = cexpm1_(__dmul_rn(x, ts), __dmul_rn(y, ts));
+    return cmul(first, cdiv(num, den));
+}
+
+constexpr int FC_ANCHOR = 256;  // window steps between FP64 re-anchorings of the projection recurrence
+
+__global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const double* __restrict__ eig,
+                                                       const float* __restrict__ ywin,
+                                                       const SimSummary* __restrict__ summ,
+                                                       double* __restrict__ ata, double* __restrict__ atb,
+                                                       float* __restrict__ info, const int* __restrict__ counts,
+                                                       const int* __restrict__ order) {
+    __shared__ float part[FIT_CPB][16][4];
+    __shared__ double ms[FIT_CPB][MAXT][3];  // per unique mode: sigma, |omega|, shift
+    const int lane = threadIdx.x & 15;
+    const int g = threadIdx.x >> 4;
+    const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
+    const int64_t h = (int64_t)blockIdx.x * FIT_CPB + g;
+    if (h >= run.n) return;
+    const int64_t c = fit_candidate(run, counts, order, h);
+    if (c >= run.n) return;
+    const int nt = run.nt, n2 = 2 * nt;
+    const double ts = (double)run.ts;
+    Modes<double> m;
+    load_modes<double>(eig + c * (int64_t)run.eig_slot, nt, ts, m);
+    float* out = info + c * (int64_t)run.info_w;
+    double* arow = ata + c * (int64_t)run.ata_slot;
+    double* brow = atb + c * (int64_t)run.atb_slot;
+    for (int e = lane; e < n2 * n2; e += 16) arow[e] = 0.0;
+    for (int e = lane; e < n2; e += 16) brow[e] = 0.0;
+    if (m.max_mag > 1.0) {
+        if (lane == 0) {
+            const float v = (float)__dadd_rn((double)run.unstable_err, __ddiv_rn(log(m.max_mag), ts));
+            out[run.info_scoring] = v;
+            out[run.info_scoring + 1] = v;
+        }
+        return;
+    }
+    const int unique = m.unique, nc = 2 * unique;
+    {
+        double sig, om;
+        mode_of<double>(m, nt, lane, sig, om);
+        ms[g][lane][0] = sig;
+        ms[g][lane][1] = om;
+        ms[g][lane][2] = fmax(__dmul_rn(sig, (double)run.fit_t0), __dmul_rn(sig, (double)run.fit_t1));
+    }
+    // steady state from the compensated sum (the plain sum alone where the
+    // compensation is not finite, i.e. the trajectory overflowed)
+    const SimSummary sm = summ[c];
+    const double ysum = isfinite(sm.ycomp) ? __dadd_rn((double)sm.ysum, (double)sm.ycomp) : (double)sm.ysum;
+    const double yss = __ddiv_rn(ysum, (double)(run.time - run.steady_start_id));
+    if (lane == 0) {
+        const double pk = fmax(0.0, yss >= 0.0 ? __dmul_rn((double)sm.ymax, yss) : __dmul_rn((double)sm.ymin, yss));
+        out[run.info_freqresp + 2] = (float)__dsub_rn(__ddiv_rn(pk, fmax(__dmul_rn(yss, yss), (double)TINY_E6)), 1.0);
+        out[run.info_freqresp + 3] = (float)yss;
+    }
+    __syncwarp(hmask);
+    const int steps = run.fit_steps;
+    const double t0 = __dmul_rn((double)run.fit_start_id, ts);
+
+    // projection of the trajectory: mode md, window segment sg of nseg
+    const int nseg = unique > 0 ? 16 / unique : 1;
+    const int md = lane / nseg, sg = lane - md * nseg;
+    acc2 gre{0.0f, 0.0f}, gim{0.0f, 0.0f};
+    if (md < unique) {
+        const double sig = ms[g][md][0], om = ms[g][md][1], sh = ms[g][md][2];
+        double rs, rc;
+        sincos(__dmul_rn(om, ts), &rs, &rc);
+        const double ra = exp(__dmul_rn(sig, ts));
+        const cdff rho{dff_of(__dmul_rn(ra, rc)), dff_of(__dmul_rn(ra, rs))};
+        const int seg = (((steps + nseg - 1) / nseg) + 7) & ~7;
+        const int wb = sg * seg, we = min(steps, wb + seg);
+        const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
+        const float* wrow = ywin + c * (int64_t)run.fit_pitch;
+        for (int w0 = wb; w0 < we; w0 += FC_ANCHOR) {
+            const double tw = __dmul_rn((double)(run.fit_start_id + w0), ts);
+            double zs, zc;
+            sincos(__dmul_rn(om, tw), &zs, &zc);
+            const double za = exp(__fma_rn(sig, tw, -sh));
+            cdff z{dff_of(__dmul_rn(za, zc)), dff_of(__dmul_rn(za, zs))};
+            const int w1 = min(we, w0 + FC_ANCHOR);
+            for (int w = w0; w < w1; w += 4) {
+                const float4 y4 = *reinterpret_cast<const float4*>(wrow + w);  // w is a multiple of 4
+                const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (w + k < w1) {
+                        const float y = (w + k < wlimit) ? yv[k] : 0.0f;
+                        acc2_add(gre, y, z.re);
+                        acc2_add(gim, y, z.im);
+                        z = cdff_mul(z, rho);
+                    }
+                }
+            }
+        }
+    }
+    part[g][lane][0] = gre.h;
+    part[g][lane][1] = gre.l;
+    part[g][lane][2] = gim.h;
+    part[g][lane][3] = gim.l;
+    __syncwarp(hmask);
+    if (lane < unique) {
+        double pre = 0.0, pim = 0.0;
+        for (int k = 0; k < nseg; ++k) {
+            const float* q = part[g][lane * nseg + k];
+            pre = __dadd_rn(pre, __dadd_rn((double)q[0], (double)q[1]));
+            pim = __dadd_rn(pim, __dadd_rn((double)q[2], (double)q[3]));
+        }
+        const double sig = ms[g][lane][0], om = ms[g][lane][1], sh = ms[g][lane][2];
+        const cplx<double> bs = geo_sum(sig, om, t0, ts, steps, sh);  // sum of the basis over the window
+        brow[2 * lane] = __dsub_rn(pre, __dmul_rn(yss, bs.re));
+        brow[2 * lane + 1] = __dsub_rn(pim, __dmul_rn(yss, bs.im));
+    }
+    // the Gram matrix: pair (a, b), a >= b, of unique modes
+    const int npairs = unique * (unique + 1) / 2;
+    for (int pidx = lane; pidx < npairs; pidx += 16) {
+        int a = 0;
+        while ((a + 1) * (a + 2) / 2 <= pidx) ++a;
+        const int b = pidx - a * (a + 1) / 2;
+        const double sa = ms[g][a][0], oa = ms[g][a][1], sha = ms[g][a][2];
+        const double sb = ms[g][b][0], ob = ms[g][b][1], shb = ms[g][b][2];
+        const double x = __dadd_rn(sa, sb), sh = __dadd_rn(sha, shb);
+        // A = sum e^{(s_a + s_b) t}, B = sum e^{(conj(s_a) + s_b) t}
+        const cplx<double> A = geo_sum(x, __dadd_rn(oa, ob), t0, ts, steps, sh);
+        const cplx<double> B = geo_sum(x, __dsub_rn(ob, oa), t0, ts, steps, sh);
+        // Re a Re b, Im a Im b, Re a Im b, Im a Re b (a, b the two modes' e^{s t})
+        const double cc = __dmul_rn(0.5, __dadd_rn(A.re, B.re));
+        const double ss = __dmul_rn(0.5, __dsub_rn(B.re, A.re));
+        const double cs = __dmul_rn(0.5, __dadd_rn(A.im, B.im));
+        const double sc = __dmul_rn(0.5, __dsub_rn(A.im, B.im));
+        arow[(2 * a) * n2 + 2 * b] = cc;
+        arow[(2 * a + 1) * n2 + 2 * b] = sc;
+        arow[(2 * a + 1) * n2 + 2 * b + 1] = ss;
+        if (a != b) arow[(2 * a) * n2 + 2 * b + 1] = cs;
+    }
+    (void)nc;
+}
+
+void launch_fit_comp(const Run& run, const void* eig, const void* ywin, const void* summ, void* ata, void* atb,
+                     float* info, int* counts, int* order, cudaStream_t st) {
+    const int grid = (int)((run.n + FIT_CPB - 1) / FIT_CPB);
+    if (counts) {
+        CE_CUDA(cudaMemsetAsync(counts, 0, FIT_CLASSES * sizeof(int), st));
+        prefer_shared((const void*)k_fit_classify<double>);
+        k_fit_classify<double><<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, (const double*)eig, counts, order);
+        CE_CUDA(cudaGetLastError());
+    }
+    prefer_shared((const void*)k_fit_comp);
+    k_fit_comp<<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const float*)ywin, (const SimSummary*)summ,
+                                           (double*)ata, (double*)atb, info, counts, order);
+    CE_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
 constexpr int MODAL_WARPS = 4;
 
 template <typename R>
@@ -342,12 +590,16 @@ __device__ __forceinline__ float rmin_normal<float>() { return FLT_MIN; }
 template <>
 __device__ __forceinline__ double rmin_normal<double>() { return DBL_MIN; }
 
-template <typename R, bool RG = false>
+// REFINE (the compensated precision): after the solve, one step of iterative
+// refinement in FP64 -- the residual of the scaled system from the unfactored
+// normal equations, solved with the same factors and added to the solution.
+template <typename R, bool RG = false, bool REFINE = false>
 __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run_in, const R* __restrict__ eig,
                                                             const R* __restrict__ ata, const R* __restrict__ atb,
                                                             float* __restrict__ info) {
     __shared__ R Ms[MODAL_WARPS][MAXNC][MAXNC + 1];
     __shared__ R xs[MODAL_WARPS][MAXNC];
+    __shared__ R rs[MODAL_WARPS][REFINE ? MAXNC : 1];
     __shared__ R cs[MODAL_WARPS][MAXNC];
     __shared__ int trans[MODAL_WARPS][MAXNC];
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
@@ -466,38 +718,57 @@ __global__ void __launch_bounds__(32 * MODAL_WARPS) k_modal(const Run run_in, co
         __syncwarp();
     }
 
-    // solve: P, L, D^+, L^T, P^T
-    if (lane == 0)
-        for (int k = 0; k < n; ++k) {
-            const int p = trans[wi][k];
-            const R t = xs[wi][k];
-            xs[wi][k] = xs[wi][p];
-            xs[wi][p] = t;
+    // solve: P, L, D^+, L^T, P^T, in place on v
+    auto solve = [&](R* v) {
+        if (lane == 0)
+            for (int k = 0; k < n; ++k) {
+                const int p = trans[wi][k];
+                const R t = v[k];
+                v[k] = v[p];
+                v[p] = t;
+            }
+        __syncwarp();
+        for (int i = 0; i < n; ++i) {
+            const R xi = v[i];
+            if (lane > i && lane < n) v[lane] = rsub(v[lane], rmul(xi, M[lane][i]));
+            __syncwarp();
         }
-    __syncwarp();
-    for (int i = 0; i < n; ++i) {
-        const R xi = xs[wi][i];
-        if (lane > i && lane < n) xs[wi][lane] = rsub(xs[wi][lane], rmul(xi, M[lane][i]));
+        if (lane < n) {
+            const R d = M[lane][lane];
+            v[lane] = fabs(d) > rmin_normal<R>() ? rdiv(v[lane], d) : R(0);
+        }
+        __syncwarp();
+        for (int i = n - 1; i >= 0; --i) {
+            const R xi = v[i];
+            if (lane < i) v[lane] = rsub(v[lane], rmul(M[i][lane], xi));
+            __syncwarp();
+        }
+        if (lane == 0)
+            for (int k = n - 1; k >= 0; --k) {
+                const int p = trans[wi][k];
+                const R t = v[k];
+                v[k] = v[p];
+                v[p] = t;
+            }
+        __syncwarp();
+    };
+    solve(xs[wi]);
+    if constexpr (REFINE) {
+        // r = D^-1 Atb - (D^-1 AtA D^-1) x, the scaled entries formed as above
+        if (lane < n) {
+            const R inv_i = rdiv(R(1), cs[wi][lane]);
+            R r = rdiv(atb[c * (int64_t)run.atb_slot + lane], cs[wi][lane]);
+            for (int j = 0; j < n; ++j) {
+                const R a = j <= lane ? A[lane * n + j] : A[j * n + lane];
+                r = rsub(r, rmul(rmul(rmul(inv_i, a), rdiv(R(1), cs[wi][j])), xs[wi][j]));
+            }
+            rs[wi][lane] = r;
+        }
+        __syncwarp();
+        solve(rs[wi]);
+        if (lane < n) xs[wi][lane] = radd(xs[wi][lane], rs[wi][lane]);
         __syncwarp();
     }
-    if (lane < n) {
-        const R d = M[lane][lane];
-        xs[wi][lane] = fabs(d) > rmin_normal<R>() ? rdiv(xs[wi][lane], d) : R(0);
-    }
-    __syncwarp();
-    for (int i = n - 1; i >= 0; --i) {
-        const R xi = xs[wi][i];
-        if (lane < i) xs[wi][lane] = rsub(xs[wi][lane], rmul(M[i][lane], xi));
-        __syncwarp();
-    }
-    if (lane == 0)
-        for (int k = n - 1; k >= 0; --k) {
-            const int p = trans[wi][k];
-            const R t = xs[wi][k];
-            xs[wi][k] = xs[wi][p];
-            xs[wi][p] = t;
-        }
-    __syncwarp();
     if (lane < n) xs[wi][lane] = rdiv(xs[wi][lane], cs[wi][lane]);
     __syncwarp();
 
@@ -608,6 +879,13 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st) {
     const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
+    if (precision == CE_PRECISION_COMPENSATED) {
+        prefer_shared((const void*)k_modal<double, false, true>);
+        k_modal<double, false, true><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
+                                                                       (const double*)atb, info);
+        CE_CUDA(cudaGetLastError());
+        return;
+    }
     prefer_shared(precision == CE_PRECISION_FP64 ? (const void*)k_modal<double>
                   : run.rg.runs                  ? (const void*)k_modal<float, true>
                                                  : (const void*)k_modal<float>);

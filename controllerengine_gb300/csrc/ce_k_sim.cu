@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
     float xh_hi[MAXS], xh_lo[MAXS], xp_hi[MAXD], xp_lo[MAXD];
 #pragma unroll
     for (int i = 0; i < MAXS; ++i) xh_hi[i] = xh_lo[i] = xp_hi[i] = xp_lo[i] = 0.0f;
-    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float ysum = 0.0f, ycomp = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
     float* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int T = run.time;
     for (int tt = 0; tt < T; ++tt) {
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
                     dst[1] = b;
                 }
             }
-            if (tt >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            if (tt >= run.steady_start_id) ysum_add(ysum, ycomp, y);
             ymax = fmaxf(ymax, y);
             ymin = fminf(ymin, y);
         }
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         sm.ysum = ysum;
         sm.ymax = ymax;
         sm.ymin = ymin;
-        sm.pad = 0.0f;
+        sm.ycomp = ycomp;
         summ[c] = sm;
     }
 }

@@ -104,11 +104,14 @@ namespace {
 int64_t bytes_per_candidate(const ce_config& c, int precision) {
     const int64_t nt = c.total_dim, pitch = ((c.fit_steps + 7) / 8) * 8;
     const int64_t groups = (c.freq + SWEEP_FG - 1) / SWEEP_FG;
-    const int64_t real = precision == CE_PRECISION_FP64 ? 2 : 1;  // 4-byte words per real of the session
+    // 4-byte words per real of each buffer: the simulation's (fit window, summary)
+    // and the rest's (LIN_A, eigenvalues, normal equations, sweep scratch)
+    const int64_t sim = precision == CE_PRECISION_FP64 ? 2 : 1;
+    const int64_t real = precision == CE_PRECISION_MIXED ? 1 : 2;
     int64_t f = 0;
     f += 2 * (int64_t)c.cuda_mx_width + 2 * (int64_t)c.info_mx_width;  // gains + INFO, session and lane
-    f += nt * nt;                                                      // LIN_A
-    f += real * (2 * nt + pitch + 4);                                  // eigenvalues, fit window, summary
+    f += real * (nt * nt + 2 * nt);                                    // LIN_A, eigenvalues
+    f += sim * (pitch + 4);                                            // fit window, summary
     f += real * (4 * nt * nt + 2 * nt);                                // AtA, Atb
     f += 1 + (MAXT + 1) + 1 + 1;                                       // nominal, fit order, lists
     f += real * (2 * (int64_t)c.freq + groups) + groups;               // sweep scratch
@@ -311,7 +314,7 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     if (opt) o = *opt;
     const int lanes = o.lanes > 0 ? o.lanes : 2;
     if (lanes > 8) fail("ce_server_create: at most 8 lanes, got {}", lanes);
-    if (o.precision != CE_PRECISION_MIXED && o.precision != CE_PRECISION_FP64)
+    if (o.precision != CE_PRECISION_MIXED && o.precision != CE_PRECISION_FP64 && o.precision != CE_PRECISION_COMPENSATED)
         fail("ce_server_create: unknown precision {}", o.precision);
     int64_t cap = o.max_batch > 0 ? o.max_batch : 65536;
     // every lane may hold a full batch's scratch for every model

@@ -503,7 +503,7 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
     for (int i = 0; i < NDC; ++i) xp_hi[i] = xp_lo[i] = 0.0f;
     bool poisS = false, poisD = false;
 
-    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float ysum = 0.0f, ycomp = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
     float* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int T = run.time;
 
@@ -538,7 +538,7 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
                     }
                 }
             }
-            if (t >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            if (t >= run.steady_start_id) ysum_add(ysum, ycomp, y);
             ymax = fmaxf(ymax, y);
             ymin = fminf(ymin, y);
             if (run.store_traj && writer) traj[c * (int64_t)T + t] = y;
@@ -642,7 +642,7 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
     sm.ysum = ysum;
     sm.ymax = ymax;
     sm.ymin = ymin;
-    sm.pad = 0.0f;
+    sm.ycomp = ycomp;
     if (writer) summ[c] = sm;
 }
 
@@ -718,7 +718,7 @@ __device__ __forceinline__ void sim_wide(const Run& run, const Plant& P, const f
 #pragma unroll
     for (int i = 0; i < NDC; ++i) xp_hi[i] = xp_lo[i] = 0.0f;
     bool poisS = false, poisD = false;
-    float ysum = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
+    float ysum = 0.0f, ycomp = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
     float* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int T = run.time;
     for (int t = 0; t < T; ++t) {
@@ -742,7 +742,7 @@ __device__ __forceinline__ void sim_wide(const Run& run, const Plant& P, const f
                     dst[1] = b;
                 }
             }
-            if (t >= run.steady_start_id) ysum = __fadd_rn(ysum, y);
+            if (t >= run.steady_start_id) ysum_add(ysum, ycomp, y);
             ymax = fmaxf(ymax, y);
             ymin = fminf(ymin, y);
             if (run.store_traj) traj[c * (int64_t)T + t] = y;
@@ -857,7 +857,7 @@ __device__ __forceinline__ void sim_wide(const Run& run, const Plant& P, const f
         sm.ysum = ysum;
         sm.ymax = ymax;
         sm.ymin = ymin;
-        sm.pad = 0.0f;
+        sm.ycomp = ycomp;
         summ[c] = sm;
     }
 }

@@ -257,7 +257,8 @@ class Session:
         self.set_precision(precision)
 
     def set_precision(self, precision: str):
-        code = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64}[precision]
+        code = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
+                "compensated": _ffi.PRECISION_COMPENSATED}[precision]
         _check(_lib().ce_session_set_precision(self._h, code))
         self.precision = precision
 
@@ -378,7 +379,7 @@ class Session:
         g, i, n = self._rows(cuda_mx, info_in)
         c = self.config
         nt = c.total_dim
-        shapes = {"ywin": (n, c.fit_steps), "summ": (n, 3), "lina": (n, nt * nt), "eigen": (n, 2 * nt),
+        shapes = {"ywin": (n, c.fit_steps), "summ": (n, 4), "lina": (n, nt * nt), "eigen": (n, 2 * nt),
                   "ata": (n, 4 * nt * nt), "atb": (n, 2 * nt)}
         arrs = {k: np.empty(shapes[k], np.float64) for k in want}
         dp = lambda a: None if a is None else a.ctypes.data_as(_ffi._DP)
@@ -438,7 +439,8 @@ class Server:
         self.config = self.configs[0]
         self._plants = [m[1] for m in models]  # keeps the arrays alive for the call
         self._h = C.c_void_p()
-        prec = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64}[precision]
+        prec = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
+                "compensated": _ffi.PRECISION_COMPENSATED}[precision]
         opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us, prec)
         k = len(models)
         cfgs = (_ffi.ce_config * k)(*[m[0].raw for m in models])

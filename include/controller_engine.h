@@ -56,6 +56,10 @@ extern "C" {
 /* Arithmetic of a session. */
 #define CE_PRECISION_MIXED 0 /* reference arithmetic: FP32 double-float simulation, FP32 fit and sweep, FP64 eigensolves */
 #define CE_PRECISION_FP64 1  /* the plain FP64 form of the same method: every stage in FP64 */
+/* FP32 simulation with a compensated steady-state sum; FP64 LIN_A, eigenvalues, nominal check and
+ * sweep; the fit's normal matrix in closed form (FP64) and its right-hand side by a double-float
+ * projection of the FP32 trajectory; FP64 LDLT solve with one step of iterative refinement */
+#define CE_PRECISION_COMPENSATED 2
 
 /*
  * Parsed ControllerEngine.config plus the sizes derived from it.
@@ -152,7 +156,8 @@ typedef struct ce_diagnostics {
  * restatement of the method.  Any pointer may be NULL. */
 typedef struct ce_diagnostics64 {
     double* ywin;  /* n * fit_steps     the trajectory's fit window, y(fit_start_id + w) */
-    double* summ;  /* n * 3             sum of y over [steady_start_id, time), max y, min y */
+    double* summ;  /* n * 4             sum of y over [steady_start_id, time), max y, min y, and the
+                                        sum's rounding-error compensation (FP32 simulation; 0 in FP64) */
     double* lina;  /* n * nt*nt         linearised closed loop */
     double* eigen; /* n * 2nt           eigenvalues (re, im) */
     double* ata;   /* n * (2nt)^2       modal normal matrix */
@@ -375,7 +380,7 @@ typedef struct ce_server_options {
     int32_t lanes;            /* concurrent batches (0: 2, at most 8) */
     int64_t hbm_budget_bytes; /* device memory for all lanes (0: no limit); capacity shrinks to fit */
     int32_t max_wait_us;      /* a partial batch waits up to this long for more requests (0: none) */
-    int32_t precision;        /* CE_PRECISION_MIXED (0, the default) or CE_PRECISION_FP64 for every lane */
+    int32_t precision;        /* CE_PRECISION_MIXED (0, the default), _FP64 or _COMPENSATED for every lane */
 } ce_server_options;
 
 typedef struct ce_server_stats {
