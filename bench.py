@@ -121,9 +121,21 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
             row[f"{name}_compensated"] = float(np.median(rel(cmp_, col)[sel]))
             row[f"{name}_mixed"] = float(np.median(rel(mix, col)[sel]))
         bins.append(row)
+    # the same errors binned by the trajectory's own difference from the FP64 one
+    tbins = []
+    for lo in range(-9, 1):
+        sel = scored & (traj >= 10.0 ** lo) & (traj < 10.0 ** (lo + 1))
+        if sel.sum() < 4:
+            continue
+        row = {"trajectory_rel_diff": f"1e{lo}..1e{lo + 1}", "candidates": int(sel.sum())}
+        for name, col in (("wn", fr), ("zeta", fr + 1), ("behaviour_err", s + 1)):
+            e = rel(cmp_, col)[sel]
+            row[f"{name}_compensated_median"] = float(np.median(e))
+            row[f"{name}_compensated_within_1e-6"] = float((e <= 1e-6).mean())
+        tbins.append(row)
     return {"sample": int(len(g)), "trajectory_rel_diff": {"median": float(np.median(traj)),
                                                             "p99": float(np.quantile(traj, 0.99))},
-            "by_condition": bins}
+            "by_condition": bins, "by_trajectory_difference": tbins}
 
 
 def fit_ops(eigen, steps):

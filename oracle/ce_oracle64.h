@@ -676,11 +676,9 @@ int oracle64_evaluate(const oc_cfg* c, const oc_plant* p, int64_t n, const float
             eig[2 * i] = wr[i];
             eig[2 * i + 1] = wi[i];
         }
-        if (out[d.info_scoring] == 0.0f) modalsetup64_one(c, &d, fit_steps, ywin, summ, eig, ata, atb, out);
-        else {
-            for (int e = 0; e < 4 * nt * nt; e++) ata[e] = 0.0;
-            for (int e = 0; e < 2 * nt; e++) atb[e] = 0.0;
-        }
+        /* the modal setup runs for every candidate (a pre-flagged one included:
+           ref: src/modalsetup.cu:18-26); the modal solve skips the flagged ones */
+        modalsetup64_one(c, &d, fit_steps, ywin, summ, eig, ata, atb, out);
         modalsolve64_one(c, &d, ata, atb, eig, out);
         if (rc == 0) allmargin64_one(c, &d, &mp, &g, lina, row, out);
         if (ywin_out)

@@ -7,9 +7,11 @@ hypot, log10: CUDA's on the GPU, glibc's here, each within an ulp or two), so:
   and are compared to 1e-12 relative (they come out bit-identical);
 * AtA / Atb (the basis calls exp, sin and cos) within 1e-12 of each row's scale;
 * every pass/fail class (modal-unstable, nominal-unstable, eig-fail, margin status) identical;
-* the INFO row's cost terms, the double results rounded to float, within 1e-6 relative, and
-  all but a few per mille of them identical (a double difference of ~1e-14, amplified by the
-  fit's normal-equation conditioning, crosses a float rounding boundary now and then).
+* the INFO row's cost terms, the double results rounded to float: at least 99% of them
+  identical, and all within 1e-6 relative, except the fit-derived terms (wn, zeta, the
+  behaviour error and the total score, the modal columns) of candidates whose scaled normal
+  matrix has a condition number above 1e9, where the libm's last-ulp differences in the basis
+  (1e-16) are amplified beyond 1e-7 -- two correct FP64 evaluations disagree there.
 The same form against the mixed form: identical classes on these workloads."""
 import numpy as np
 import pytest
@@ -28,6 +30,24 @@ def _rel(a, b):
     d = np.abs(a - b) / scale
     d[np.isnan(a) & np.isnan(b)] = 0.0
     return float(np.nanmax(d)) if d.size else 0.0
+
+
+def _fit_condition(info, ata, cfg):
+    """Condition number of each candidate's diagonally scaled normal matrix (the system the modal
+    solve factors); 0 for a candidate the fit does not model."""
+    nt = cfg.total_dim
+    uniq = info[:, cfg.info_modal + 3 * nt].astype(int)
+    out = np.zeros(info.shape[0])
+    for k in range(info.shape[0]):
+        nc = 2 * uniq[k]
+        if nc == 0 or info[k, cfg.info_scoring + 1] >= cfg.unstable_err:
+            continue
+        A = ata[k].reshape(2 * nt, 2 * nt)[:nc, :nc]
+        A = np.tril(A) + np.tril(A, -1).T
+        dg = np.sqrt(np.abs(np.diag(A)))
+        dg[dg <= 1e-6] = 1.0
+        out[k] = np.linalg.cond(A / dg[:, None] / dg[None, :])
+    return out
 
 
 def _problems():
@@ -52,11 +72,14 @@ def test_fp64_form_against_fp64_oracle(lib, oracle_mod, name):
     c = _cols(cfg)
     cols = np.r_[c["sc"], c["fr"], c["am"], c["md"]]
     a, b = info[:, cols].astype(np.float64), ref[:, cols].astype(np.float64)
-    both = np.isfinite(a) & np.isfinite(b)
     assert np.array_equal(np.isfinite(a), np.isfinite(b))
-    rel = np.abs(a - b)[both] / np.maximum(np.abs(b)[both], 1e-30)
-    assert rel.max() <= 1e-6, rel.max()
+    with np.errstate(invalid="ignore"):
+        rel = np.where(np.isfinite(a) & np.isfinite(b), np.abs(a - b) / np.maximum(np.abs(b), 1e-30), 0.0)
     assert (rel == 0).mean() >= 0.99, (rel == 0).mean()
+    cond = _fit_condition(info, d["ata"], cfg)
+    fit_cols = np.isin(cols, np.r_[c["sc"], c["fr"][:2], c["md"]])
+    ill = (cond > 1e9)[:, None] & fit_cols[None, :]
+    assert rel[~ill].max() <= 1e-6, (rel[~ill].max(), np.unravel_index(np.argmax(np.where(ill, 0, rel)), rel.shape))
 
 
 def test_fp64_form_classes_equal_mixed(lib, eight_state_small):
