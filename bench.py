@@ -556,6 +556,35 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
     wall = (time.perf_counter() - t0) / steps
     stages = {k: v[0] / steps for k, v in rb.stage_times().items() if v[1]}
     launches = (rb.kernel_launches - l0) // steps
+    rb.set_profiling(False)
+    # the device path: rows resident, the autotuner's setting, one evaluation captured into a CUDA
+    # graph and replayed (CUDA events on the replay stream)
+    import torch
+    dg = torch.from_numpy(g_all).cuda()
+    di = torch.from_numpy(i_all).cuda()
+    do = torch.empty_like(di)
+    rb.prepare(counts)
+    tuned = rb.autotune(dg.data_ptr(), di.data_ptr(), do.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        rb.evaluate_device(dg.data_ptr(), di.data_ptr(), do.data_ptr(), stream=side.cuda_stream)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rb.evaluate_device(dg.data_ptr(), di.data_ptr(), do.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    graph_ms = e0.elapsed_time(e1) / steps
+    same = bool(np.array_equal(do.cpu().numpy().view(np.uint32), out.view(np.uint32)))
+    del graph
     rb.close()
     offs = np.cumsum([0] + [c.info_mx_width for c in cfgs])
     scored = float(np.mean([out[offs[k] + c.info_scoring] < c.unstable_err for k, c in enumerate(cfgs)]))
@@ -615,6 +644,10 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
             "instances_per_s": n_inst / wall, "ms_per_step": 1e3 * wall, "steps": steps,
             "launches_per_step": launches, "stages_ms_per_step": stages, "setup_s": setup,
             "scored_fraction": scored,
+            "graph": {"instances_per_s": n_inst / (graph_ms * 1e-3), "ms_per_step": graph_ms, "tuning": tuned,
+                      "rows_equal_host_path": same,
+                      "what": "ce_ragged_evaluate_device captured in one CUDA graph (gather, one launch per "
+                              "stage, scatter), device-resident rows, the ragged autotuner's setting"},
             "one_session_per_instance": {"instances_per_s": 1.0 / per_inst, "ms_per_instance": 1e3 * per_inst,
                                          "sample": len(pick)},
             "padded_to_max": {"instances_per_s": n_inst / padded, "ms_per_step": 1e3 * padded,

@@ -34,7 +34,8 @@ EXPORTED_SYMBOLS = (
     "ce_server_reset_stats", "ce_evaluate_plants", "ce_evaluate_plants_device", "ce_server_create_models",
     "ce_server_submit_model", "ce_server_submit_plants", "ce_session_set_tuning", "ce_session_get_tuning", "ce_session_autotune",
     "ce_ragged_create", "ce_ragged_evaluate", "ce_ragged_destroy", "ce_ragged_kernel_launches",
-    "ce_ragged_set_profiling", "ce_ragged_stage_times",
+    "ce_ragged_set_profiling", "ce_ragged_stage_times", "ce_ragged_prepare", "ce_ragged_evaluate_device",
+    "ce_ragged_set_tuning", "ce_ragged_get_tuning", "ce_ragged_autotune",
     "RunControllerEngine",
 )
 PENDING = 2
@@ -96,6 +97,11 @@ _DP = C.POINTER(C.c_double)
 
 class ce_diagnostics64(C.Structure):
     _fields_ = [(n, _DP) for n in ("ywin", "summ", "lina", "eigen", "ata", "atb")]
+
+
+class ce_ragged_tuning(C.Structure):
+    _fields_ = [("sim_lanes", C.c_int32), ("instance_order", C.c_int32), ("eig_blocks_per_sm", C.c_int32),
+                ("ms_per_evaluation", C.c_double)]
 
 
 class ce_tuning(C.Structure):
@@ -175,6 +181,12 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ce_ragged_kernel_launches.restype = C.c_int64
     lib.ce_ragged_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     lib.ce_ragged_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.ce_ragged_prepare.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    lib.ce_ragged_evaluate_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.ce_ragged_set_tuning.argtypes = [C.c_void_p, C.POINTER(ce_ragged_tuning)]
+    lib.ce_ragged_get_tuning.argtypes = [C.c_void_p, C.POINTER(ce_ragged_tuning)]
+    lib.ce_ragged_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(ce_ragged_tuning)]
     lib.ce_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_int64)]
     lib.ce_server_wait.argtypes = [C.c_void_p, C.c_int64, C.c_int32]

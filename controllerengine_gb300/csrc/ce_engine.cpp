@@ -152,11 +152,24 @@ struct ce_ragged {
     int* d_inst = nullptr;                  // instance of each candidate of the current evaluation
     float* d_tab = nullptr;                 // their simulation table (RT_FIELDS x inst_cap)
     int64_t inst_cap = 0;
-    float *h_gains = nullptr, *h_info = nullptr;  // pinned staging rows at the layout widths
-    int64_t host_cap = 0;
+    // the host path's staging of the caller's packed rows: pinned, and on the device
+    float *h_gains = nullptr, *h_info = nullptr;
+    int64_t host_g_cap = 0, host_i_cap = 0;
+    float *d_g_in = nullptr, *d_i_in = nullptr, *d_i_out = nullptr;
+    int64_t dev_g_cap = 0, dev_i_cap = 0;
     std::vector<int> h_inst;        // device position -> instance
     std::vector<int64_t> dev_k;     // device position -> candidate within its instance
-    std::vector<int64_t> order_counts;  // the candidate counts the device order was built for
+    // the prepared evaluation (ce_ragged_prepare): its candidate counts, the device
+    // order's settings, and per device position the caller's row offsets and widths
+    std::vector<int64_t> prep_counts;
+    int prep_lanes = 0, prep_inst_order = -1;
+    bool prepared = false;
+    int64_t prep_n = 0, g_total = 0, i_total = 0;
+    int64_t* d_goff = nullptr;
+    int64_t* d_ioff = nullptr;
+    int2* d_wid = nullptr;
+    int64_t map_cap = 0;
+    ce_ragged_tuning tuning{};
     // per instance: the operation of every interpreted slot (NL chains, then DC and U; 0 = empty)
     std::vector<std::array<uint8_t, ce::MAXW * ce::MAX_NL + ce::MAX_DC + ce::MAX_U>> sig;
 };
@@ -1114,6 +1127,9 @@ void destroy_ragged(ce_ragged* r) {
     if (r->d_tab) cudaFree(r->d_tab);
     if (r->h_gains) cudaFreeHost(r->h_gains);
     if (r->h_info) cudaFreeHost(r->h_info);
+    for (void* p : {(void*)r->d_g_in, (void*)r->d_i_in, (void*)r->d_i_out, (void*)r->d_goff, (void*)r->d_ioff,
+                    (void*)r->d_wid})
+        if (p) cudaFree(p);
     destroy_session(r->s);
     delete r;
 }
@@ -1235,27 +1251,106 @@ void create_ragged(int n_inst, const ce_config* cfgs, const ce_plant* plants, ce
 
 // n_cand[i] candidates of instance i, rows packed instance after instance at
 // each instance's own widths (CUDA_MX and INFO_MX rows as its sessions take them).
-void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, const float* info_in,
-                     float* info_out) {
-    if (!r || !n_cand) fail("ce_ragged_evaluate: null argument");
+// Lanes per candidate of a ragged batch's simulation under its tuning.
+int ragged_lanes(const ce_ragged* r) {
+    return r->tuning.sim_lanes == 1 || r->tuning.sim_lanes == SW_LANES ? r->tuning.sim_lanes
+                                                                      : ragged_lanes_per_candidate();
+}
+
+// Everything an evaluation of n_cand[i] candidates per instance needs before
+// it runs: the device order of the candidates, their simulation table, the
+// caller-row maps and the session scratch.  Synchronous; the order is rebuilt
+// only when the counts or the order's settings change.
+void ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
+    if (!r || !n_cand) fail("ce_ragged_prepare: null argument");
     const int I = (int)r->cfg.size();
     int64_t N = 0;
     for (int i = 0; i < I; ++i) {
         if (n_cand[i] < 0) fail("ce_ragged_evaluate: instance {} has a negative candidate count {}", i, n_cand[i]);
         N += n_cand[i];
     }
-    if (N == 0) return;
-    if (!cuda_mx || !info_in || !info_out) fail("ce_ragged_evaluate: null buffer");
     if (N > INT32_MAX) fail("ce_ragged_evaluate: {} candidates exceed the 32-bit candidate index", N);
-    const int64_t LW = r->layout.cuda_mx_width, LI = r->layout.info_mx_width;
-    if (N > r->host_cap) {
-        if (r->h_gains) cudaFreeHost(r->h_gains);
-        if (r->h_info) cudaFreeHost(r->h_info);
-        r->h_gains = r->h_info = nullptr;
-        r->host_cap = 0;
-        CE_CUDA(cudaMallocHost((void**)&r->h_gains, (size_t)N * LW * sizeof(float)));
-        CE_CUDA(cudaMallocHost((void**)&r->h_info, (size_t)N * LI * sizeof(float)));
-        r->host_cap = N;
+    const std::vector<int64_t> counts(n_cand, n_cand + I);
+    const int lanes = ragged_lanes(r), inst_order = r->tuning.instance_order ? 1 : 0;
+    if (r->prepared && counts == r->prep_counts && lanes == r->prep_lanes && inst_order == r->prep_inst_order)
+        return;
+    r->prepared = false;
+    ce_session* s = r->s;
+    if (r->tuning.eig_blocks_per_sm >= 0) s->tuning.eig_blocks_per_sm = r->tuning.eig_blocks_per_sm;
+    // the caller's row offsets of each instance
+    std::vector<int64_t> goff(I), ioff(I);
+    int64_t gi = 0, ii = 0;
+    for (int i = 0; i < I; ++i) {
+        goff[i] = gi;
+        ioff[i] = ii;
+        gi += n_cand[i] * r->cfg[i].cuda_mx_width;
+        ii += n_cand[i] * r->cfg[i].info_mx_width;
+    }
+    r->h_inst.resize((size_t)N);
+    r->dev_k.resize((size_t)N);
+    // The device order.  Candidates sorted by decreasing horizon are dealt to the
+    // W warps of the simulation (32 / lanes candidates each) in turn: warp w
+    // holds sorted candidates w, W + w, 2W + w, ..., one from each horizon tier.
+    // A warp's lanes interpret different instruction programs, so a step costs
+    // about as many passes as its active lanes hold distinct operations; with the
+    // horizons spread, the short lanes leave early and the long ones finish with
+    // few lanes active, instead of the longest instances sharing warps for their
+    // whole horizon.  (instance_order: the candidates in the caller's order.)
+    std::vector<int> sorted_inst;
+    std::vector<int64_t> sorted_k;
+    sorted_inst.reserve((size_t)N);
+    sorted_k.reserve((size_t)N);
+    {
+        std::vector<int> order(I);
+        for (int i = 0; i < I; ++i) order[i] = i;
+        if (!inst_order)
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
+        for (int i : order)
+            for (int64_t k = 0; k < n_cand[i]; ++k) {
+                sorted_inst.push_back(i);
+                sorted_k.push_back(k);
+            }
+    }
+    if (inst_order) {
+        for (int64_t q = 0; q < N; ++q) {
+            r->h_inst[(size_t)q] = sorted_inst[(size_t)q];
+            r->dev_k[(size_t)q] = sorted_k[(size_t)q];
+        }
+    } else {
+        const int64_t per_warp = 32 / lanes;
+        const int64_t W = std::max<int64_t>(1, (N + per_warp - 1) / per_warp);
+        // Within each tier of W consecutive candidates, order by the programs'
+        // operation sequences, so that the candidates dealt to one warp (the same
+        // rank in every tier) tend to interpret the same operations in the same
+        // slots and the warp executes fewer distinct paths per slot.
+        std::vector<int64_t> idx((size_t)N);
+        for (int64_t q = 0; q < N; ++q) idx[(size_t)q] = q;
+        for (int64_t t0 = 0; t0 < N; t0 += W) {
+            const int64_t t1 = std::min(N, t0 + W);
+            std::stable_sort(idx.begin() + t0, idx.begin() + t1, [&](int64_t a, int64_t b) {
+                return r->sig[sorted_inst[(size_t)a]] < r->sig[sorted_inst[(size_t)b]];
+            });
+        }
+        int64_t p = 0;
+        for (int64_t w = 0; w < W; ++w)
+            for (int64_t l = 0; l < per_warp; ++l) {
+                const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, per_warp W)
+                if (q >= N) continue;
+                r->h_inst[(size_t)p] = sorted_inst[(size_t)idx[(size_t)q]];
+                r->dev_k[(size_t)p] = sorted_k[(size_t)idx[(size_t)q]];
+                ++p;
+            }
+    }
+    // per device position: the caller's row offsets and the instance's widths
+    std::vector<int64_t> hg((size_t)N), hi((size_t)N);
+    std::vector<int2> hw((size_t)N);
+    for (int64_t c = 0; c < N; ++c) {
+        const int i = r->h_inst[(size_t)c];
+        const int64_t k = r->dev_k[(size_t)c];
+        const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
+        hg[(size_t)c] = goff[i] + k * cw;
+        hi[(size_t)c] = ioff[i] + k * iw;
+        hw[(size_t)c] = int2{cw, iw};
     }
     if (N > r->inst_cap) {
         if (r->d_inst) cudaFree(r->d_inst);
@@ -1267,105 +1362,164 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
         CE_CUDA(cudaMalloc((void**)&r->d_tab, (size_t)RT_FIELDS * N * sizeof(float)));
         r->inst_cap = N;
     }
-    r->h_inst.resize((size_t)N);
-    // the caller's row offsets of each instance
-    std::vector<int64_t> goff(I), ioff(I);
-    int64_t gi = 0, ii = 0;
-    for (int i = 0; i < I; ++i) {
-        goff[i] = gi;
-        ioff[i] = ii;
-        gi += n_cand[i] * r->cfg[i].cuda_mx_width;
-        ii += n_cand[i] * r->cfg[i].info_mx_width;
+    if (N > r->map_cap) {
+        for (void* p : {(void*)r->d_goff, (void*)r->d_ioff, (void*)r->d_wid})
+            if (p) cudaFree(p);
+        r->d_goff = r->d_ioff = nullptr;
+        r->d_wid = nullptr;
+        r->map_cap = 0;
+        CE_CUDA(cudaMalloc((void**)&r->d_goff, (size_t)N * sizeof(int64_t)));
+        CE_CUDA(cudaMalloc((void**)&r->d_ioff, (size_t)N * sizeof(int64_t)));
+        CE_CUDA(cudaMalloc((void**)&r->d_wid, (size_t)N * sizeof(int2)));
+        r->map_cap = N;
     }
-    // The device order depends only on the instances and their candidate
-    // counts: it is kept from the previous call when the counts repeat.
-    const std::vector<int64_t> counts(n_cand, n_cand + I);
-    if (counts != r->order_counts || r->dev_k.size() != (size_t)N) {
-        // The device order.  Candidates sorted by decreasing horizon are dealt to the
-        // W warps of the simulation (32 / ragged_lanes_per_candidate() candidates
-        // each) in turn: warp w holds sorted candidates w, W + w, 2W + w, ..., one
-        // from each horizon tier.  A warp's lanes interpret
-        // different instruction programs, so a step costs about as many passes as
-        // its active lanes hold distinct operations; with the horizons spread, the
-        // short lanes leave early and the long ones finish with few lanes active,
-        // instead of the longest instances sharing warps for their whole horizon.
-        std::vector<int> sorted_inst;
-        std::vector<int64_t> sorted_k;
-        sorted_inst.reserve((size_t)N);
-        sorted_k.reserve((size_t)N);
-        {
-            std::vector<int> order(I);
-            for (int i = 0; i < I; ++i) order[i] = i;
-            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
-            for (int i : order)
-                for (int64_t k = 0; k < n_cand[i]; ++k) {
-                    sorted_inst.push_back(i);
-                    sorted_k.push_back(k);
-                }
-        }
-        const int64_t per_warp = 32 / ragged_lanes_per_candidate();
-        const int64_t W = (N + per_warp - 1) / per_warp;
-        // Within each tier of W consecutive candidates, order by the programs'
-        // operation sequences, so that the candidates dealt to one warp (the same
-        // rank in every tier) tend to interpret the same operations in the same
-        // slots and the warp executes fewer distinct paths per slot.
-        {
-            std::vector<int64_t> idx((size_t)N);
-            for (int64_t q = 0; q < N; ++q) idx[(size_t)q] = q;
-            for (int64_t t0 = 0; t0 < N; t0 += W) {
-                const int64_t t1 = std::min(N, t0 + W);
-                std::stable_sort(idx.begin() + t0, idx.begin() + t1, [&](int64_t a, int64_t b) {
-                    return r->sig[sorted_inst[(size_t)a]] < r->sig[sorted_inst[(size_t)b]];
-                });
-            }
-            std::vector<int> si((size_t)N);
-            std::vector<int64_t> sk((size_t)N);
-            for (int64_t q = 0; q < N; ++q) {
-                si[(size_t)q] = sorted_inst[(size_t)idx[(size_t)q]];
-                sk[(size_t)q] = sorted_k[(size_t)idx[(size_t)q]];
-            }
-            sorted_inst.swap(si);
-            sorted_k.swap(sk);
-        }
-        r->dev_k.resize((size_t)N);
-        {
-            int64_t p = 0;
-            for (int64_t w = 0; w < W; ++w)
-                for (int64_t l = 0; l < per_warp; ++l) {
-                    const int64_t q = l * W + w;  // (l, w) <-> q is a bijection onto [0, per_warp W)
-                    if (q >= N) continue;
-                    r->h_inst[(size_t)p] = sorted_inst[(size_t)q];
-                    r->dev_k[(size_t)p] = sorted_k[(size_t)q];
-                    ++p;
-                }
-        }
-        r->order_counts = counts;
+    if (N > 0) {
+        CE_CUDA(cudaMemcpyAsync(r->d_inst, r->h_inst.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CE_CUDA(cudaMemcpyAsync(r->d_goff, hg.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
+        CE_CUDA(cudaMemcpyAsync(r->d_ioff, hi.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
+        CE_CUDA(cudaMemcpyAsync(r->d_wid, hw.data(), (size_t)N * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
+        launch_ragged_table(N, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, s->stream);
+        s->launches += 1;
+        ensure_buffers(s, N, false);
     }
-    for (int64_t c = 0; c < N; ++c) {
-        const int i = r->h_inst[(size_t)c];
-        const int64_t k = r->dev_k[(size_t)c];
-        const int cw = r->cfg[i].cuda_mx_width, iw = r->cfg[i].info_mx_width;
-        std::memcpy(r->h_gains + c * LW, cuda_mx + goff[i] + k * cw, (size_t)cw * sizeof(float));
-        std::memcpy(r->h_info + c * LI, info_in + ioff[i] + k * iw, (size_t)iw * sizeof(float));
+    CE_CUDA(cudaStreamSynchronize(s->stream));
+    r->prep_counts = counts;
+    r->prep_lanes = lanes;
+    r->prep_inst_order = inst_order;
+    r->prep_n = N;
+    r->g_total = gi;
+    r->i_total = ii;
+    r->prepared = true;
+}
+
+// One prepared evaluation on device rows packed as the host API packs them:
+// gather into the device order, one launch per stage, scatter the INFO rows
+// back.  Enqueued on st; no allocation, no synchronisation.
+void ragged_enqueue(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
+                    cudaStream_t st) {
+    const int64_t N = r->prep_n;
+    if (N == 0) return;
+    ce_session* s = r->s;
+    Buffers& b = s->buf;
+    const int LW = r->layout.cuda_mx_width, LI = r->layout.info_mx_width;
+    launch_ragged_gather(N, r->d_goff, r->d_ioff, r->d_wid, LW, LI, d_cuda_mx, d_info_in, b.gains, b.info, st);
+    const Ragged rg{r->d_runs, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, r->prep_lanes};
+    run_pipeline(s, 0, N, b.gains, b.info, st, false, false, &rg);
+    launch_ragged_scatter(N, r->d_ioff, r->d_wid, LI, b.info, d_info_out, st);
+    s->launches += 2;
+}
+
+void ragged_evaluate_device(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
+                            void* stream) {
+    if (!r) fail("ce_ragged_evaluate_device: null ragged batch");
+    if (!r->prepared) fail("ce_ragged_evaluate_device: no prepared candidate counts (call ce_ragged_prepare first)");
+    if (r->prep_n > 0 && (!d_cuda_mx || !d_info_in || !d_info_out)) fail("ce_ragged_evaluate_device: null buffer");
+    ragged_enqueue(r, d_cuda_mx, d_info_in, d_info_out, (cudaStream_t)stream);
+}
+
+void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, const float* info_in,
+                     float* info_out) {
+    if (!r || !n_cand) fail("ce_ragged_evaluate: null argument");
+    ragged_prepare(r, n_cand);
+    if (r->prep_n == 0) return;
+    if (!cuda_mx || !info_in || !info_out) fail("ce_ragged_evaluate: null buffer");
+    const int64_t G = r->g_total, Iw = r->i_total;
+    if (G > r->host_g_cap) {
+        if (r->h_gains) cudaFreeHost(r->h_gains);
+        r->h_gains = nullptr;
+        r->host_g_cap = 0;
+        CE_CUDA(cudaMallocHost((void**)&r->h_gains, (size_t)G * sizeof(float)));
+        r->host_g_cap = G;
+    }
+    if (Iw > r->host_i_cap) {
+        if (r->h_info) cudaFreeHost(r->h_info);
+        r->h_info = nullptr;
+        r->host_i_cap = 0;
+        CE_CUDA(cudaMallocHost((void**)&r->h_info, (size_t)Iw * sizeof(float)));
+        r->host_i_cap = Iw;
+    }
+    if (G > r->dev_g_cap) {
+        if (r->d_g_in) cudaFree(r->d_g_in);
+        r->d_g_in = nullptr;
+        r->dev_g_cap = 0;
+        CE_CUDA(cudaMalloc((void**)&r->d_g_in, (size_t)G * sizeof(float)));
+        r->dev_g_cap = G;
+    }
+    if (Iw > r->dev_i_cap) {
+        for (float* p : {r->d_i_in, r->d_i_out})
+            if (p) cudaFree(p);
+        r->d_i_in = r->d_i_out = nullptr;
+        r->dev_i_cap = 0;
+        CE_CUDA(cudaMalloc((void**)&r->d_i_in, (size_t)Iw * sizeof(float)));
+        CE_CUDA(cudaMalloc((void**)&r->d_i_out, (size_t)Iw * sizeof(float)));
+        r->dev_i_cap = Iw;
     }
     ce_session* s = r->s;
-    ensure_buffers(s, N, false);
-    Buffers& b = s->buf;
-    CE_CUDA(cudaMemcpyAsync(b.gains, r->h_gains, (size_t)N * LW * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CE_CUDA(cudaMemcpyAsync(b.info, r->h_info, (size_t)N * LI * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CE_CUDA(cudaMemcpyAsync(r->d_inst, r->h_inst.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-    launch_ragged_table(N, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, s->stream);
-    s->launches += 1;
-    const Ragged rg{r->d_runs, r->d_plants, r->d_inst, r->d_tab, r->inst_cap};
-    run_pipeline(s, 0, N, b.gains, b.info, s->stream, false, false, &rg);
-    CE_CUDA(cudaMemcpyAsync(r->h_info, b.info, (size_t)N * LI * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    std::memcpy(r->h_gains, cuda_mx, (size_t)G * sizeof(float));
+    std::memcpy(r->h_info, info_in, (size_t)Iw * sizeof(float));
+    CE_CUDA(cudaMemcpyAsync(r->d_g_in, r->h_gains, (size_t)G * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CE_CUDA(cudaMemcpyAsync(r->d_i_in, r->h_info, (size_t)Iw * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    ragged_enqueue(r, r->d_g_in, r->d_i_in, r->d_i_out, s->stream);
+    CE_CUDA(cudaMemcpyAsync(r->h_info, r->d_i_out, (size_t)Iw * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     CE_CUDA(cudaStreamSynchronize(s->stream));
     collect_stage_times(s);
-    for (int64_t c = 0; c < N; ++c) {
-        const int i = r->h_inst[(size_t)c];
-        const int iw = r->cfg[i].info_mx_width;
-        std::memcpy(info_out + ioff[i] + r->dev_k[(size_t)c] * iw, r->h_info + c * LI, (size_t)iw * sizeof(float));
+    std::memcpy(info_out, r->h_info, (size_t)Iw * sizeof(float));
+}
+
+// The ragged autotuner: coordinate descent over the simulation form (the wide
+// four-lane form or one thread per candidate), the device order (dealt by
+// horizon or the caller's order) and the FP64 eigensolves' blocks per SM, each
+// setting timed over three evaluations of the prepared batch on the caller's
+// rows; the fastest is kept.  Results do not depend on the setting.
+void ragged_autotune(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out, void* stream,
+                     ce_ragged_tuning* best) {
+    if (!r) fail("ce_ragged_autotune: null ragged batch");
+    if (!r->prepared) fail("ce_ragged_autotune: no prepared candidate counts (call ce_ragged_prepare first)");
+    cudaStream_t st = (cudaStream_t)stream;
+    const std::vector<int64_t> counts = r->prep_counts;
+    cudaEvent_t e0, e1;
+    CE_CUDA(cudaEventCreate(&e0));
+    CE_CUDA(cudaEventCreate(&e1));
+    std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> g0(e0, cudaEventDestroy), g1(e1, cudaEventDestroy);
+    auto time_of = [&](const ce_ragged_tuning& t) {
+        r->tuning = t;
+        ragged_prepare(r, counts.data());
+        ragged_enqueue(r, d_cuda_mx, d_info_in, d_info_out, st);  // warm
+        CE_CUDA(cudaEventRecord(e0, st));
+        for (int k = 0; k < 3; ++k) ragged_enqueue(r, d_cuda_mx, d_info_in, d_info_out, st);
+        CE_CUDA(cudaEventRecord(e1, st));
+        CE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        CE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        return (double)ms / 3.0;
+    };
+    ce_ragged_tuning cur = r->tuning;
+    if (cur.sim_lanes != 1 && cur.sim_lanes != SW_LANES) cur.sim_lanes = ragged_lanes_per_candidate();
+    if (cur.eig_blocks_per_sm <= 0) cur.eig_blocks_per_sm = 5;
+    cur.ms_per_evaluation = time_of(cur);
+    auto try_set = [&](ce_ragged_tuning t) {
+        t.ms_per_evaluation = time_of(t);
+        if (t.ms_per_evaluation < cur.ms_per_evaluation) cur = t;
+    };
+    {
+        ce_ragged_tuning t = cur;
+        t.sim_lanes = cur.sim_lanes == 1 ? SW_LANES : 1;
+        try_set(t);
     }
+    {
+        ce_ragged_tuning t = cur;
+        t.instance_order = cur.instance_order ? 0 : 1;
+        try_set(t);
+    }
+    for (int b : {cur.eig_blocks_per_sm - 1, cur.eig_blocks_per_sm + 1})
+        if (b >= 1 && b <= 8) {
+            ce_ragged_tuning t = cur;
+            t.eig_blocks_per_sm = b;
+            try_set(t);
+        }
+    r->tuning = cur;
+    ragged_prepare(r, counts.data());
+    if (best) *best = cur;
 }
 
 }  // namespace
@@ -1456,6 +1610,42 @@ CE_EXPORT int ce_ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const floa
 }
 
 CE_EXPORT void ce_ragged_destroy(ce_ragged* r) { destroy_ragged(r); }
+
+CE_EXPORT int ce_ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
+    return guarded([&] { ragged_prepare(r, n_cand); });
+}
+
+CE_EXPORT int ce_ragged_evaluate_device(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in,
+                                        float* d_info_out, void* stream) {
+    return guarded([&] { ragged_evaluate_device(r, d_cuda_mx, d_info_in, d_info_out, stream); });
+}
+
+CE_EXPORT int ce_ragged_set_tuning(ce_ragged* r, const ce_ragged_tuning* t) {
+    return guarded([&] {
+        if (!r || !t) fail("null argument");
+        if (t->sim_lanes != 0 && t->sim_lanes != 1 && t->sim_lanes != SW_LANES)
+            fail("sim_lanes must be 0, 1 or {}, got {}", SW_LANES, t->sim_lanes);
+        if (t->instance_order != 0 && t->instance_order != 1)
+            fail("instance_order must be 0 or 1, got {}", t->instance_order);
+        if (t->eig_blocks_per_sm < 0 || t->eig_blocks_per_sm > 32)
+            fail("eig_blocks_per_sm must be in [0, 32], got {}", t->eig_blocks_per_sm);
+        r->tuning = *t;
+        r->tuning.ms_per_evaluation = 0.0;
+        r->prepared = false;  // the next evaluation rebuilds the device order
+    });
+}
+
+CE_EXPORT int ce_ragged_get_tuning(const ce_ragged* r, ce_ragged_tuning* t) {
+    return guarded([&] {
+        if (!r || !t) fail("null argument");
+        *t = r->tuning;
+    });
+}
+
+CE_EXPORT int ce_ragged_autotune(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
+                                 void* stream, ce_ragged_tuning* best) {
+    return guarded([&] { ragged_autotune(r, d_cuda_mx, d_info_in, d_info_out, stream, best); });
+}
 
 CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r) { return r && r->s ? r->s->launches : -1; }
 

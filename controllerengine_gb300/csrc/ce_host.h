@@ -119,6 +119,11 @@ bool concurrent_nominal(int64_t n);
 
 // Blocks of SIM_BLOCK threads that cover the candidates (or list slots) of `run`.
 int sim_grid(const Run& run);
+// A ragged batch's rows between the caller's packing and the device order (see ce_k_sim.cu).
+void launch_ragged_gather(int64_t n, const int64_t* goff, const int64_t* ioff, const int2* wid, int LW, int LI,
+                          const float* g_in, const float* i_in, float* g_dev, float* i_dev, cudaStream_t st);
+void launch_ragged_scatter(int64_t n, const int64_t* ioff, const int2* wid, int LI, const float* i_dev, float* i_out,
+                           cudaStream_t st);
 // The per-candidate table of a ragged batch (RT_FIELDS x stride floats) for n candidates.
 void launch_ragged_table(int64_t n, const Plant* plants, const int* inst, float* tab, int64_t stride,
                          cudaStream_t st);

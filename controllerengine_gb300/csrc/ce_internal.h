@@ -96,6 +96,7 @@ struct Ragged {
     // consecutive words whatever their instances)
     const float* tab;
     int64_t tab_stride;
+    int lanes;  // lanes per candidate of the simulation: SW_LANES (the wide form) or 1
 };
 
 // Fields of that table: observer model, plant, instruction counts and slots.

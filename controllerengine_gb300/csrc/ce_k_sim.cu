@@ -264,6 +264,51 @@ __global__ void __launch_bounds__(128) k_ragged_table(int64_t n, const Plant* __
         for (int k = 0; k < P.n_nl[w]; ++k) slot(MAX_DC + MAX_U + w * MAX_NL + k, P.nl[w][k]);
 }
 
+// Rows of a ragged batch between the caller's packing (instance after
+// instance, each row at its instance's widths) and the device order at the
+// batch's widths LW / LI (padding written as 0).  Device position c holds the
+// caller's gains row at goff[c] and INFO row at ioff[c], wid[c] = (cuda_w, info_w).
+// One thread per element of the device rows: the stores are coalesced.
+__global__ void __launch_bounds__(256) k_ragged_gather(int64_t n, const int64_t* __restrict__ goff,
+                                                       const int64_t* __restrict__ ioff, const int2* __restrict__ wid,
+                                                       int LW, int LI, const float* __restrict__ g_in,
+                                                       const float* __restrict__ i_in, float* __restrict__ g_dev,
+                                                       float* __restrict__ i_dev) {
+    const int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t per = LW + LI;
+    if (t >= n * per) return;
+    const int64_t c = t / per;
+    const int e = (int)(t - c * per);
+    const int2 w = wid[c];
+    if (e < LW) g_dev[c * LW + e] = e < w.x ? g_in[goff[c] + e] : 0.0f;
+    else i_dev[c * LI + (e - LW)] = e - LW < w.y ? i_in[ioff[c] + (e - LW)] : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_ragged_scatter(int64_t n, const int64_t* __restrict__ ioff,
+                                                        const int2* __restrict__ wid, int LI,
+                                                        const float* __restrict__ i_dev, float* __restrict__ i_out) {
+    const int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (t >= n * LI) return;
+    const int64_t c = t / LI;
+    const int e = (int)(t - c * LI);
+    if (e < wid[c].y) i_out[ioff[c] + e] = i_dev[c * LI + e];
+}
+
+void launch_ragged_gather(int64_t n, const int64_t* goff, const int64_t* ioff, const int2* wid, int LW, int LI,
+                          const float* g_in, const float* i_in, float* g_dev, float* i_dev, cudaStream_t st) {
+    const int64_t total = n * (LW + LI);
+    k_ragged_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, goff, ioff, wid, LW, LI, g_in, i_in, g_dev,
+                                                                      i_dev);
+    CE_CUDA(cudaGetLastError());
+}
+
+void launch_ragged_scatter(int64_t n, const int64_t* ioff, const int2* wid, int LI, const float* i_dev, float* i_out,
+                           cudaStream_t st) {
+    const int64_t total = n * LI;
+    k_ragged_scatter<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, ioff, wid, LI, i_dev, i_out);
+    CE_CUDA(cudaGetLastError());
+}
+
 void launch_ragged_table(int64_t n, const Plant* plants, const int* inst, float* tab, int64_t stride,
                          cudaStream_t st) {
     k_ragged_table<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, plants, inst, tab, stride);
@@ -432,7 +477,7 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
         // a ragged batch: every instance at the reference's padded width, its plant from the table
         if (precision == CE_PRECISION_FP64 || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
-        if (ragged_lanes_per_candidate() == SW_LANES && !traj) {
+        if (run.rg.lanes == SW_LANES && !traj) {
             prefer_shared((const void*)k_sim_ragged_wide);
             k_sim_ragged_wide<<<(unsigned)((run.n + SW_CPB - 1) / SW_CPB), SIM_BLOCK, 0, st>>>(
                 run, gains, (float*)ywin, (SimSummary*)summ);

@@ -197,6 +197,33 @@ class Ragged:
             off += n * w
         return res
 
+    def prepare(self, n_cand):
+        """Fix the candidate counts per instance for evaluate_device (ce_ragged_prepare)."""
+        nc = (C.c_int64 * len(n_cand))(*[int(k) for k in n_cand])
+        _check(_lib().ce_ragged_prepare(self._h, nc))
+
+    def evaluate_device(self, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0):
+        """Enqueue one evaluation of the prepared counts on device rows packed instance after
+        instance (ce_ragged_evaluate_device); no synchronisation, no allocation."""
+        _check(_lib().ce_ragged_evaluate_device(self._h, C.c_void_p(d_cuda_mx), C.c_void_p(d_info_in),
+                                                C.c_void_p(d_info_out), C.c_void_p(stream)))
+
+    @property
+    def tuning(self) -> dict:
+        t = _ffi.ce_ragged_tuning()
+        _check(_lib().ce_ragged_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_tuning(self, sim_lanes: int = 0, instance_order: int = 0, eig_blocks_per_sm: int = 0):
+        t = _ffi.ce_ragged_tuning(sim_lanes, instance_order, eig_blocks_per_sm, 0.0)
+        _check(_lib().ce_ragged_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0) -> dict:
+        t = _ffi.ce_ragged_tuning()
+        _check(_lib().ce_ragged_autotune(self._h, C.c_void_p(d_cuda_mx), C.c_void_p(d_info_in),
+                                         C.c_void_p(d_info_out), C.c_void_p(stream), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
     def evaluate_packed(self, n_cand, cuda_mx: np.ndarray, info_in: np.ndarray) -> np.ndarray:
         """The C ABI's form: n_cand[i] candidates of instance i, the rows packed instance
         after instance at each instance's widths (flat float32 arrays); returns the INFO rows

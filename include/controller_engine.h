@@ -269,6 +269,38 @@ CE_EXPORT int64_t ce_ragged_kernel_launches(const ce_ragged* r);
 CE_EXPORT int ce_ragged_set_profiling(ce_ragged* r, int32_t on);
 CE_EXPORT int ce_ragged_stage_times(ce_ragged* r, double* ms, int64_t* launches);
 
+/* Device-buffer form of a ragged evaluation (no counterpart in the reference).
+ * ce_ragged_prepare fixes the candidate counts n_cand[i] and sets up, once and
+ * synchronously, everything an evaluation of those counts needs: the device
+ * order of the candidates, their simulation table, the maps of the caller's
+ * rows and the scratch.  ce_ragged_evaluate_device then takes device rows packed
+ * as ce_ragged_evaluate's host rows (instance after instance, each at its own
+ * widths; d_info_out may alias d_info_in), enqueues on `stream` a gather into
+ * the device order, one launch per pipeline stage and a scatter of the INFO rows,
+ * and returns without synchronising.  It allocates nothing, so a call can be
+ * captured into a CUDA graph (stream capture) and replayed; calls on one
+ * ragged batch must not overlap.  ce_ragged_evaluate prepares its counts the
+ * same way (keeping the preparation while the counts repeat). */
+CE_EXPORT int ce_ragged_prepare(ce_ragged* r, const int64_t* n_cand);
+CE_EXPORT int ce_ragged_evaluate_device(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in,
+                                        float* d_info_out, void* stream);
+
+/* Launch settings of a ragged batch and its autotuner (no counterpart in the
+ * reference).  None of them changes a result.  ce_ragged_autotune times, on the
+ * prepared counts and the caller's device rows, by coordinate descent: the
+ * simulation form, the device order and the FP64 eigensolves' blocks per SM;
+ * it keeps the fastest and returns it (with its time per evaluation). */
+typedef struct ce_ragged_tuning {
+    int32_t sim_lanes;         /* lanes per candidate of the simulation: 4 (the wide form), 1, or 0: the default */
+    int32_t instance_order;    /* 0: candidates dealt to warps by decreasing horizon (default); 1: the caller's order */
+    int32_t eig_blocks_per_sm; /* FP64 eigensolves: one-warp blocks per SM (0: the library default) */
+    double ms_per_evaluation;  /* ce_ragged_autotune: the chosen setting's time */
+} ce_ragged_tuning;
+CE_EXPORT int ce_ragged_set_tuning(ce_ragged* r, const ce_ragged_tuning* t);
+CE_EXPORT int ce_ragged_get_tuning(const ce_ragged* r, ce_ragged_tuning* t);
+CE_EXPORT int ce_ragged_autotune(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out,
+                                 void* stream, ce_ragged_tuning* best);
+
 /* Launch tuning of a session (no counterpart in the reference).  0 fields take
  * the library defaults (2 lanes per matrix, 5 blocks per SM, 2 chunks for
  * batches of >= 32,768 candidates).  No setting changes a result.

@@ -36,8 +36,12 @@ def test_ragged_equals_own_sessions():
     with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
         l0 = rb.kernel_launches
         outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
-        assert rb.kernel_launches - l0 == 10  # the candidate table, then one launch per stage for all instances
+        # the candidate table (once per candidate counts), the gather into the device order, one
+        # launch per stage for all instances, the scatter of the INFO rows
+        assert rb.kernel_launches - l0 == 12
+        l1 = rb.kernel_launches
         again = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+        assert rb.kernel_launches - l1 == 11
     for c, p, o, o2 in zip(cfgs, probs, outs, again):
         with ce.Session(c, p.plant) as s:
             ref = s.evaluate(p.cuda_mx, p.info_mx)
