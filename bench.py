@@ -85,11 +85,14 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
     nt = cfg.total_dim
     out = {}
     prev = sess.precision
-    for form in ("fp64", "compensated", "mixed"):
+    for form in ("fp64", "compensated", "mixed", "compensated_traj64"):
         sess.set_precision(form)
         out[form] = sess.evaluate_diagnostics64(g, info, want=("ywin", "ata"))
     sess.set_precision(prev)
     (f64, d64), (cmp_, dc), (mix, _) = out["fp64"], out["compensated"], out["mixed"]
+    # the compensated form's arithmetic on the FP64 trajectory: what remains against the FP64 form
+    # once the FP32 trajectory is taken out
+    t64 = precision_report(out["compensated_traj64"][0], f64, cfg)
     s, fr, md = cfg.info_scoring, cfg.info_freqresp, cfg.info_modal
     yscale = np.maximum(np.abs(d64["ywin"]).max(axis=1), 1e-30)
     traj = np.abs(dc["ywin"] - d64["ywin"]).max(axis=1) / yscale
@@ -135,7 +138,8 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
         tbins.append(row)
     return {"sample": int(len(g)), "trajectory_rel_diff": {"median": float(np.median(traj)),
                                                             "p99": float(np.quantile(traj, 0.99))},
-            "by_condition": bins, "by_trajectory_difference": tbins}
+            "by_condition": bins, "by_trajectory_difference": tbins,
+            "compensated_on_fp64_trajectory_vs_fp64": t64}
 
 
 def fit_ops(eigen, steps):
@@ -358,7 +362,7 @@ def serving_models(k: int = 16, seed: int = 5):
 
 def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 16384, seed: int = 7,
                   precision: str = "mixed", n_plants: int = 16384, mc_fraction: float = 0.25,
-                  max_wait_us: int = 0):
+                  max_wait_us: int = 0, max_batch_work: int = 0, runs: int = 1):
     """Request serving (ce_server_*): every model of `problems` holds n_plants perturbed copies
     of its plant (synth.perturbed_plants); a request carries U[256, 16384] candidates on a model
     drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
@@ -403,7 +407,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
     refused = [0]
     models = [(c, ps, n_plants) for c, ps in zip(cfgs, plant_sets)]
     with ce.Server(None, None, models=models, max_batch=max_batch, lanes=lanes, precision=precision,
-                   max_wait_us=max_wait_us) as srv:
+                   max_wait_us=max_wait_us, max_batch_work=max_batch_work) as srv:
         # warm-up: every lane sizes its scratch for a full batch of every model, and compiles
         # the per-candidate-plant kernels of every model
         for _ in range(lanes):
@@ -434,23 +438,31 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
         sat = total / (time.perf_counter() - t0)
         mean_size = (256 + 16384) / 2
         rate = 0.7 * sat / mean_size  # requests/s
-        srv.reset_stats()
-        hs, offered, n_mc = [], 0, 0
-        t0 = time.perf_counter()
-        t_next = t0
-        while t_next - t0 < seconds:
-            now = time.perf_counter()
-            if now < t_next:
-                time.sleep(t_next - now)
-            req, h = draw_submit(srv)
-            offered += req[3].shape[0]
-            n_mc += req[1]
-            hs.append(h)
-            t_next += rng.exponential(1.0 / rate)
-        for h in hs:
-            h.wait()
-        wall = time.perf_counter() - t0
-        st = srv.stats()
+        # consecutive loaded runs; the line's main figures are the last run's, every run's are listed
+        per_run = []
+        for _ in range(max(1, runs)):
+            srv.reset_stats()
+            hs, offered, n_mc = [], 0, 0
+            t0 = time.perf_counter()
+            t_next = t0
+            while t_next - t0 < seconds:
+                now = time.perf_counter()
+                if now < t_next:
+                    time.sleep(t_next - now)
+                req, h = draw_submit(srv)
+                offered += req[3].shape[0]
+                n_mc += req[1]
+                hs.append(h)
+                t_next += rng.exponential(1.0 / rate)
+            for h in hs:
+                h.wait()
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            per_run.append({"requests": st["completed"], "latency_p50_ms": st["latency_p50_ms"],
+                            "latency_p99_ms": st["latency_p99_ms"], "latency_max_ms": st["latency_max_ms"],
+                            "queue_p99_ms": st["queue_p99_ms"], "service_p99_ms": st["service_p99_ms"],
+                            "batch_p99_ms": st["batch_p99_ms"], "tail_queue_ms": st["tail_queue_ms"],
+                            "tail_service_ms": st["tail_service_ms"], "tail_busy_lanes": st["tail_busy_lanes"]})
         # light load: 50 requests/s, the low end of the serving configuration's arrival rates
         # (when that is below 70% of saturation), where a request is mostly served alone
         light = None
@@ -480,13 +492,19 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
             "precision": precision,
             "models": [list(x) for x in shapes],
             "lanes": lanes, "max_batch": st["capacity"], "max_wait_us": max_wait_us,
+            "max_batch_work": max_batch_work, "loaded_runs": per_run,
+            "p99_all_runs_ms": max(r["latency_p99_ms"] for r in per_run),
             "saturation_candidates_per_s": sat,
             "offered_requests_per_s": rate, "offered_load": "70% of saturation, Poisson arrivals",
             "requests": st["completed"], "monte_carlo_requests": n_mc, "refused_requests": refused[0],
             "achieved_candidates_per_s": offered / wall,
             "batches": st["batches"], "mean_batch": st["batched_candidates"] / max(1, st["batches"]),
             "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
-            "latency_max_ms": st["latency_max_ms"], "light_load": light}
+            "latency_max_ms": st["latency_max_ms"],
+            "breakdown": {k: st[k] for k in ("queue_p50_ms", "queue_p99_ms", "service_p50_ms", "service_p99_ms",
+                                             "batch_p50_ms", "batch_p99_ms", "batch_max_ms", "tail_requests",
+                                             "tail_queue_ms", "tail_service_ms", "tail_busy_lanes")},
+            "light_load": light}
 
 
 def monte_carlo_bench(n_plants: int, steps: int, warmup: int):
@@ -766,6 +784,10 @@ def main():
     ap.add_argument("--sim-kernel", default="specialised", choices=["specialised", "table"])
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch settings")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="Poisson serving run (0: skip)")
+    ap.add_argument("--serve-runs", type=int, default=5, help="consecutive loaded serving runs")
+    ap.add_argument("--serve-lanes", type=int, default=3)
+    ap.add_argument("--serve-max-work", type=int, default=0,
+                    help="serving: candidate-steps per batch (0: no cap)")
     ap.add_argument("--serve-max-wait-us", type=int, default=0,
                     help="serving: how long a partial batch may wait for more requests")
     ap.add_argument("--mc-plants", type=int, default=262144, help="Monte Carlo plants, one per candidate (0: skip)")
@@ -1035,7 +1057,8 @@ def main():
         line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
     if rank == 0 and a.serve_seconds > 0:
         models = serving_models()
-        line["serving"] = serving_bench(models, a.serve_seconds, max_wait_us=a.serve_max_wait_us)
+        line["serving"] = serving_bench(models, a.serve_seconds, lanes=a.serve_lanes, max_wait_us=a.serve_max_wait_us,
+                                        max_batch_work=a.serve_max_work, runs=a.serve_runs)
         # the same request stream served by the plain FP64 form (at its own 70% load)
         line["serving"]["fp64_form"] = {k: v for k, v in serving_bench(models, a.serve_seconds / 2,
                                                                        precision="fp64").items()

@@ -20,6 +20,7 @@ MAX_TOTAL_DIM = 16
 PRECISION_MIXED = 0
 PRECISION_FP64 = 1
 PRECISION_COMPENSATED = 2
+PRECISION_COMPENSATED_TRAJ64 = 3
 EIG_ARITH_SEPARATE = 0
 EIG_ARITH_FUSED = 1
 
@@ -111,13 +112,17 @@ class ce_tuning(C.Structure):
 
 class ce_server_options(C.Structure):
     _fields_ = [("max_batch", C.c_int32), ("lanes", C.c_int32), ("hbm_budget_bytes", C.c_int64),
-                ("max_wait_us", C.c_int32), ("precision", C.c_int32)]
+                ("max_wait_us", C.c_int32), ("precision", C.c_int32), ("max_batch_work", C.c_int64)]
 
 
 class ce_server_stats(C.Structure):
     _fields_ = [("capacity", C.c_int64), ("lanes", C.c_int32), ("completed", C.c_int64), ("batches", C.c_int64),
                 ("batched_candidates", C.c_int64), ("queued", C.c_int64), ("latency_p50_ms", C.c_double),
-                ("latency_p99_ms", C.c_double), ("latency_max_ms", C.c_double)]
+                ("latency_p99_ms", C.c_double), ("latency_max_ms", C.c_double), ("queue_p50_ms", C.c_double),
+                ("queue_p99_ms", C.c_double), ("service_p50_ms", C.c_double), ("service_p99_ms", C.c_double),
+                ("batch_p50_ms", C.c_double), ("batch_p99_ms", C.c_double), ("batch_max_ms", C.c_double),
+                ("tail_requests", C.c_int64), ("tail_queue_ms", C.c_double), ("tail_service_ms", C.c_double),
+                ("tail_busy_lanes", C.c_double)]
 
 
 _lib = None

@@ -211,13 +211,18 @@ struct BufElems {
 BufElems buf_elems(int precision) {
     if (precision == CE_PRECISION_FP64) return {8, 8, 8, 8, 8, 8};
     if (precision == CE_PRECISION_COMPENSATED) return {4, 4, 8, 8, 8, 8};
+    if (precision == CE_PRECISION_COMPENSATED_TRAJ64) return {8, 8, 8, 8, 8, 8};
     return {4, 4, 4, 4, 4, 4};
 }
 // The arithmetic each stage runs in under a session precision: the compensated
 // form simulates in FP32 (the mixed kernels) and runs LIN_A, the eigensolves and
 // the sweep in FP64 (the FP64 form's kernels).
-int sim_precision(int prec) { return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_MIXED : prec; }
-int eig_precision(int prec) { return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_FP64 : prec; }
+bool compensated(int prec) { return prec == CE_PRECISION_COMPENSATED || prec == CE_PRECISION_COMPENSATED_TRAJ64; }
+int sim_precision(int prec) {
+    return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_MIXED
+           : prec == CE_PRECISION_COMPENSATED_TRAJ64 ? CE_PRECISION_FP64 : prec;
+}
+int eig_precision(int prec) { return compensated(prec) ? CE_PRECISION_FP64 : prec; }
 bool grids64(int prec) { return prec != CE_PRECISION_MIXED; }
 
 void ensure_buffers(ce_session* s, int64_t n, bool traj) {
@@ -545,9 +550,10 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         const void* ywin = at(b.ywin, off, (size_t)r.fit_pitch * be.ywin);
         const void* summ = at(b.summ, off, 4 * be.summ);
         timed(2, fs, [&] {
-            if (prec == CE_PRECISION_COMPENSATED)
-                launch_fit_comp(rc, eig, ywin, summ, ata, atb, d_info + off * iw, b.fit_counts + (MAXT + 1) * k,
-                                b.fit_order + (MAXT + 1) * off, fs);
+            if (compensated(prec))
+                launch_fit_comp(rc, prec == CE_PRECISION_COMPENSATED_TRAJ64, eig, ywin, summ, ata, atb,
+                                d_info + off * iw, b.fit_counts + (MAXT + 1) * k, b.fit_order + (MAXT + 1) * off,
+                                fs);
             else
                 launch_fit(rc, prec, eig, ywin, summ, ata, atb, d_info + off * iw, b.fit_counts + (MAXT + 1) * k,
                            b.fit_order + (MAXT + 1) * off, fs);
@@ -1681,10 +1687,11 @@ CE_EXPORT int ce_session_get_eig_arith(const ce_session* s, int32_t* arith) {
 CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {
         if (!s) fail("null session");
-        if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64 && precision != CE_PRECISION_COMPENSATED)
+        if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64 && precision != CE_PRECISION_COMPENSATED &&
+            precision != CE_PRECISION_COMPENSATED_TRAJ64)
             fail("unknown precision {}", precision);
-        if (precision == CE_PRECISION_FP64 && s->cfg.observer == CE_OBSERVER_KALMAN)
-            fail("the Kalman observer (observer = kalman) runs in mixed precision only");
+        if (sim_precision(precision) == CE_PRECISION_FP64 && s->cfg.observer == CE_OBSERVER_KALMAN)
+            fail("the Kalman observer (observer = kalman) simulates in FP32 only (mixed or compensated precision)");
         s->precision = precision;
     });
 }

@@ -75,9 +75,10 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
                 void* atb, float* info, int* counts, int* order, cudaStream_t st);
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st);
-// The modal setup of the compensated precision: eig, ata, atb double; ywin float; summ SimSummary.
-void launch_fit_comp(const Run& run, const void* eig, const void* ywin, const void* summ, void* ata, void* atb,
-                     float* info, int* counts, int* order, cudaStream_t st);
+// The modal setup of the compensated precision: eig, ata, atb double; ywin float and summ SimSummary
+// (traj64: ywin double and summ 4 doubles per candidate, the FP64 simulation's).
+void launch_fit_comp(const Run& run, bool traj64, const void* eig, const void* ywin, const void* summ, void* ata,
+                     void* atb, float* info, int* counts, int* order, cudaStream_t st);
 // Scratch of the margin sweep for up to `cap` listed candidates: |PG| and
 // arg(PG) per frequency (freq x cap values each, float or double as the
 // precision), and per frequency group the b(w) minimum and the first failure.

@@ -433,9 +433,12 @@ __device__ __forceinline__ cplx<double> geo_sum(double x, double y, double t0, d
 
 constexpr int FC_ANCHOR = 256;  // window steps between FP64 re-anchorings of the projection recurrence
 
+// YT: the trajectory's type -- float (the FP32 simulation), or double (the
+// FP64 simulation, CE_PRECISION_COMPENSATED_TRAJ64: each sample split into
+// two floats, hi + lo, both projected).
+template <typename YT>
 __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const double* __restrict__ eig,
-                                                       const float* __restrict__ ywin,
-                                                       const SimSummary* __restrict__ summ,
+                                                       const YT* __restrict__ ywin, const void* __restrict__ summ,
                                                        double* __restrict__ ata, double* __restrict__ atb,
                                                        float* __restrict__ info, const int* __restrict__ counts,
                                                        const int* __restrict__ order) {
@@ -474,12 +477,23 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const dou
         ms[g][lane][2] = fmax(__dmul_rn(sig, (double)run.fit_t0), __dmul_rn(sig, (double)run.fit_t1));
     }
     // steady state from the compensated sum (the plain sum alone where the
-    // compensation is not finite, i.e. the trajectory overflowed)
-    const SimSummary sm = summ[c];
-    const double ysum = isfinite(sm.ycomp) ? __dadd_rn((double)sm.ysum, (double)sm.ycomp) : (double)sm.ysum;
+    // compensation is not finite, i.e. the trajectory overflowed); the FP64
+    // simulation's summary is (sum, max, min, 0) in double
+    double ysum, ymax, ymin;
+    if constexpr (sizeof(YT) == 4) {
+        const SimSummary sm = static_cast<const SimSummary*>(summ)[c];
+        ysum = isfinite(sm.ycomp) ? __dadd_rn((double)sm.ysum, (double)sm.ycomp) : (double)sm.ysum;
+        ymax = sm.ymax;
+        ymin = sm.ymin;
+    } else {
+        const double* sd = static_cast<const double*>(summ) + 4 * c;
+        ysum = sd[0];
+        ymax = sd[1];
+        ymin = sd[2];
+    }
     const double yss = __ddiv_rn(ysum, (double)(run.time - run.steady_start_id));
     if (lane == 0) {
-        const double pk = fmax(0.0, yss >= 0.0 ? __dmul_rn((double)sm.ymax, yss) : __dmul_rn((double)sm.ymin, yss));
+        const double pk = fmax(0.0, yss >= 0.0 ? __dmul_rn(ymax, yss) : __dmul_rn(ymin, yss));
         out[run.info_freqresp + 2] = (float)__dsub_rn(__ddiv_rn(pk, fmax(__dmul_rn(yss, yss), (double)TINY_E6)), 1.0);
         out[run.info_freqresp + 3] = (float)yss;
     }
@@ -500,7 +514,7 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const dou
         const int seg = (((steps + nseg - 1) / nseg) + 7) & ~7;
         const int wb = sg * seg, we = min(steps, wb + seg);
         const int wlimit = run.time - run.fit_start_id;  // window samples past the horizon read as 0
-        const float* wrow = ywin + c * (int64_t)run.fit_pitch;
+        const YT* wrow = ywin + c * (int64_t)run.fit_pitch;
         for (int w0 = wb; w0 < we; w0 += FC_ANCHOR) {
             const double tw = __dmul_rn((double)(run.fit_start_id + w0), ts);
             double zs, zc;
@@ -509,14 +523,29 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const dou
             cdff z{dff_of(__dmul_rn(za, zc)), dff_of(__dmul_rn(za, zs))};
             const int w1 = min(we, w0 + FC_ANCHOR);
             for (int w = w0; w < w1; w += 4) {
-                const float4 y4 = *reinterpret_cast<const float4*>(wrow + w);  // w is a multiple of 4
-                const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
+                YT yv[4];
+                if constexpr (sizeof(YT) == 4) {
+                    const float4 y4 = *reinterpret_cast<const float4*>(wrow + w);  // w is a multiple of 4
+                    yv[0] = y4.x; yv[1] = y4.y; yv[2] = y4.z; yv[3] = y4.w;
+                } else {
+                    const double2 a = reinterpret_cast<const double2*>(wrow + w)[0];
+                    const double2 b = reinterpret_cast<const double2*>(wrow + w)[1];
+                    yv[0] = a.x; yv[1] = a.y; yv[2] = b.x; yv[3] = b.y;
+                }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     if (w + k < w1) {
-                        const float y = (w + k < wlimit) ? yv[k] : 0.0f;
-                        acc2_add(gre, y, z.re);
-                        acc2_add(gim, y, z.im);
+                        const YT y = (w + k < wlimit) ? yv[k] : YT(0);
+                        if constexpr (sizeof(YT) == 4) {
+                            acc2_add(gre, y, z.re);
+                            acc2_add(gim, y, z.im);
+                        } else {
+                            const dff ys = dff_of(y);
+                            acc2_add(gre, ys.h, z.re);
+                            acc2_add(gim, ys.h, z.im);
+                            acc2_add(gre, ys.l, z.re);
+                            acc2_add(gim, ys.l, z.im);
+                        }
                         z = cdff_mul(z, rho);
                     }
                 }
@@ -565,8 +594,8 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const dou
     (void)nc;
 }
 
-void launch_fit_comp(const Run& run, const void* eig, const void* ywin, const void* summ, void* ata, void* atb,
-                     float* info, int* counts, int* order, cudaStream_t st) {
+void launch_fit_comp(const Run& run, bool traj64, const void* eig, const void* ywin, const void* summ, void* ata,
+                     void* atb, float* info, int* counts, int* order, cudaStream_t st) {
     const int grid = (int)((run.n + FIT_CPB - 1) / FIT_CPB);
     if (counts) {
         CE_CUDA(cudaMemsetAsync(counts, 0, FIT_CLASSES * sizeof(int), st));
@@ -574,9 +603,15 @@ void launch_fit_comp(const Run& run, const void* eig, const void* ywin, const vo
         k_fit_classify<double><<<(int)((run.n + 127) / 128), 128, 0, st>>>(run, (const double*)eig, counts, order);
         CE_CUDA(cudaGetLastError());
     }
-    prefer_shared((const void*)k_fit_comp);
-    k_fit_comp<<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const float*)ywin, (const SimSummary*)summ,
-                                           (double*)ata, (double*)atb, info, counts, order);
+    if (traj64) {
+        prefer_shared((const void*)k_fit_comp<double>);
+        k_fit_comp<double><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const double*)ywin, summ,
+                                                       (double*)ata, (double*)atb, info, counts, order);
+    } else {
+        prefer_shared((const void*)k_fit_comp<float>);
+        k_fit_comp<float><<<grid, FIT_BLOCK, 0, st>>>(run, (const double*)eig, (const float*)ywin, summ,
+                                                      (double*)ata, (double*)atb, info, counts, order);
+    }
     CE_CUDA(cudaGetLastError());
 }
 
@@ -879,7 +914,7 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st) {
     const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
-    if (precision == CE_PRECISION_COMPENSATED) {
+    if (precision == CE_PRECISION_COMPENSATED || precision == CE_PRECISION_COMPENSATED_TRAJ64) {
         prefer_shared((const void*)k_modal<double, false, true>);
         k_modal<double, false, true><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
                                                                        (const double*)atb, info);

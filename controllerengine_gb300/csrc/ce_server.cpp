@@ -54,6 +54,9 @@ struct Request {
     bool done = false;
     std::string error;
     Clock::time_point t_submit, t_done;
+    Clock::time_point t_dispatch;  // its first piece handed to a lane
+    bool dispatched = false;
+    int busy_at_dispatch = 0;      // lanes busy then (this one included)
 };
 
 struct Piece {
@@ -64,6 +67,7 @@ struct Piece {
 struct Lane {
     std::vector<ce_session*> sess;  // one per model
     cudaStream_t stream = nullptr;
+    cudaEvent_t start = nullptr;  // the batch's first stream work (timing)
     cudaEvent_t done = nullptr;
     float* d_gains = nullptr;
     float* d_info = nullptr;
@@ -80,6 +84,7 @@ struct ce_server {
     std::vector<ce_config> cfg;  // per model
     std::vector<int> n_plants;   // per model
     int64_t capacity = 0;        // candidates per batch (per lane)
+    int64_t max_work = 0;        // candidate-steps per batch (0: no cap)
     int max_wait_us = 0;
     int precision = CE_PRECISION_MIXED;
     std::vector<Lane> lanes;
@@ -92,7 +97,9 @@ struct ce_server {
     std::thread worker;
     // statistics
     int64_t batches = 0, batched_rows = 0, completed = 0;
-    std::vector<double> latency_ms;  // completed requests, in completion order
+    // completed requests, in completion order: latency, queue and service time, busy lanes
+    std::vector<double> latency_ms, queue_ms, service_ms, busy_lanes;
+    std::vector<double> batch_ms;  // per retired batch: its stream work
 };
 
 namespace ce {
@@ -127,8 +134,12 @@ void settle(ce_server* s, Request& r, Clock::time_point now) {
     r.done = true;
     r.t_done = now;
     if (r.error.empty()) {
+        using ms = std::chrono::duration<double, std::milli>;
         s->completed++;
-        s->latency_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_submit).count());
+        s->latency_ms.push_back(ms(now - r.t_submit).count());
+        s->queue_ms.push_back(ms(r.t_dispatch - r.t_submit).count());
+        s->service_ms.push_back(ms(now - r.t_dispatch).count());
+        s->busy_lanes.push_back((double)r.busy_at_dispatch);
     }
 }
 
@@ -140,7 +151,10 @@ void complete_lane(ce_server* s, Lane& L) {
         std::memcpy(p.req->info_out + p.row0 * iw, L.h_info + p.off * iw, (size_t)p.rows * iw * sizeof(float));
     }
     const auto now = Clock::now();
+    float gpu_ms = 0.0f;
+    const bool timed = cudaEventElapsedTime(&gpu_ms, L.start, L.done) == cudaSuccess;
     std::lock_guard<std::mutex> g(s->mu);
+    if (timed) s->batch_ms.push_back((double)gpu_ms);
     for (const Piece& p : L.pieces) {
         p.req->finished += p.rows;
         settle(s, *p.req, now);
@@ -189,6 +203,8 @@ std::vector<Piece> form_batch(ce_server* s, int& model, int& plant) {
     model = s->queue.front()->model;
     plant = s->queue.front()->plants ? -1 : s->queue.front()->plant;
     int64_t room = s->capacity, off = 0;
+    if (s->max_work > 0)  // every row of the batch runs the model's horizon
+        room = std::min(room, std::max<int64_t>(1, s->max_work / std::max(1, s->cfg[model].time)));
     for (auto it = s->queue.begin(); it != s->queue.end() && room > 0;) {
         Request& r = **it;
         if (r.model != model) {
@@ -215,6 +231,7 @@ void dispatch(ce_server* s, Lane& L, int model, int plant) {
         std::memcpy(L.h_info + p.off * iw, p.req->info_in + p.row0 * iw, (size_t)p.rows * iw * sizeof(float));
         n = std::max(n, p.off + p.rows);
     }
+    CE_CUDA(cudaEventRecord(L.start, L.stream));
     CE_CUDA(cudaMemcpyAsync(L.d_gains, L.h_gains, (size_t)n * cw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
     CE_CUDA(cudaMemcpyAsync(L.d_info, L.h_info, (size_t)n * iw * sizeof(float), cudaMemcpyHostToDevice, L.stream));
     if (plant < 0) {
@@ -271,6 +288,17 @@ void worker_loop(ce_server* s, int device) {
             }
             freeL->pieces = form_batch(s, model, plant);
             freeL->busy = !freeL->pieces.empty();
+            if (freeL->busy) {
+                int busy = 0;
+                for (Lane& L : s->lanes) busy += L.busy ? 1 : 0;
+                const auto now = Clock::now();
+                for (const Piece& p : freeL->pieces)
+                    if (!p.req->dispatched) {
+                        p.req->dispatched = true;
+                        p.req->t_dispatch = now;
+                        p.req->busy_at_dispatch = busy;
+                    }
+            }
         }
         if (freeL->busy) {
             try {
@@ -296,6 +324,7 @@ void destroy_server(ce_server* s) {
         for (ce_session* x : L.sess)
             if (x) ce_session_destroy(x);
         if (L.done) cudaEventDestroy(L.done);
+        if (L.start) cudaEventDestroy(L.start);
         if (L.stream) cudaStreamDestroy(L.stream);
         if (L.d_gains) cudaFree(L.d_gains);
         if (L.d_info) cudaFree(L.d_info);
@@ -336,6 +365,7 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     s->n_plants.assign(n_plants, n_plants + n_models);
     s->capacity = cap;
     s->max_wait_us = std::max(0, o.max_wait_us);
+    s->max_work = std::max<int64_t>(0, o.max_batch_work);
     s->precision = o.precision;
     s->lanes.resize(lanes);
     int device = 0;
@@ -359,7 +389,8 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
             session_set_small_batch_forms(L.sess[m], false);
         }
         CE_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
-        CE_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+        CE_CUDA(cudaEventCreate(&L.start));
+        CE_CUDA(cudaEventCreate(&L.done));
         CE_CUDA(cudaMalloc((void**)&L.d_gains, (size_t)cap * cw * sizeof(float)));
         CE_CUDA(cudaMalloc((void**)&L.d_info, (size_t)cap * iw * sizeof(float)));
         CE_CUDA(cudaHostAlloc((void**)&L.h_gains, (size_t)cap * cw * sizeof(float), cudaHostAllocDefault));
@@ -508,16 +539,41 @@ CE_EXPORT int ce_server_get_stats(ce_server* s, ce_server_stats* out) {
         st.batches = s->batches;
         st.batched_candidates = s->batched_rows;
         st.queued = (int64_t)s->queue.size();
-        std::vector<double> v = s->latency_ms;
-        if (!v.empty()) {
+        auto pct = [](std::vector<double> v, double p) {
+            if (v.empty()) return 0.0;
             std::sort(v.begin(), v.end());
-            auto pct = [&](double p) {
-                const size_t k = std::min(v.size() - 1, (size_t)std::ceil(p * (double)v.size()) - 1);
-                return v[k];
-            };
-            st.latency_p50_ms = pct(0.50);
-            st.latency_p99_ms = pct(0.99);
-            st.latency_max_ms = v.back();
+            const size_t k = std::min(v.size() - 1, (size_t)std::ceil(p * (double)v.size()) - 1);
+            return v[k];
+        };
+        const std::vector<double>& lat = s->latency_ms;
+        if (!lat.empty()) {
+            st.latency_p50_ms = pct(lat, 0.50);
+            st.latency_p99_ms = pct(lat, 0.99);
+            st.latency_max_ms = *std::max_element(lat.begin(), lat.end());
+            st.queue_p50_ms = pct(s->queue_ms, 0.50);
+            st.queue_p99_ms = pct(s->queue_ms, 0.99);
+            st.service_p50_ms = pct(s->service_ms, 0.50);
+            st.service_p99_ms = pct(s->service_ms, 0.99);
+            double q = 0.0, sv = 0.0, b = 0.0;
+            int64_t k = 0;
+            for (size_t i = 0; i < lat.size(); ++i)
+                if (lat[i] >= st.latency_p99_ms) {
+                    q += s->queue_ms[i];
+                    sv += s->service_ms[i];
+                    b += s->busy_lanes[i];
+                    ++k;
+                }
+            st.tail_requests = k;
+            if (k) {
+                st.tail_queue_ms = q / (double)k;
+                st.tail_service_ms = sv / (double)k;
+                st.tail_busy_lanes = b / (double)k;
+            }
+        }
+        if (!s->batch_ms.empty()) {
+            st.batch_p50_ms = pct(s->batch_ms, 0.50);
+            st.batch_p99_ms = pct(s->batch_ms, 0.99);
+            st.batch_max_ms = *std::max_element(s->batch_ms.begin(), s->batch_ms.end());
         }
         *out = st;
         return 0;
@@ -531,6 +587,10 @@ CE_EXPORT int ce_server_reset_stats(ce_server* s) {
     if (!s) return 1;
     std::lock_guard<std::mutex> g(s->mu);
     s->latency_ms.clear();
+    s->queue_ms.clear();
+    s->service_ms.clear();
+    s->busy_lanes.clear();
+    s->batch_ms.clear();
     s->completed = s->batches = s->batched_rows = 0;
     return 0;
 }

@@ -285,7 +285,8 @@ class Session:
 
     def set_precision(self, precision: str):
         code = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
-                "compensated": _ffi.PRECISION_COMPENSATED}[precision]
+                "compensated": _ffi.PRECISION_COMPENSATED,
+                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64}[precision]
         _check(_lib().ce_session_set_precision(self._h, code))
         self.precision = precision
 
@@ -458,7 +459,7 @@ class Server:
 
     def __init__(self, config: EngineConfig, plant: PlantFiles, n_plants: int = 1, max_batch: int = 0,
                  lanes: int = 0, hbm_budget_bytes: int = 0, max_wait_us: int = 0,
-                 models: list | None = None, precision: str = "mixed"):
+                 models: list | None = None, precision: str = "mixed", max_batch_work: int = 0):
         """One model (config, plant, n_plants), or with `models` a list of such triples
         (ce_server_create_models); requests then name their model in `submit`."""
         models = models or [(config, plant, n_plants)]
@@ -467,8 +468,9 @@ class Server:
         self._plants = [m[1] for m in models]  # keeps the arrays alive for the call
         self._h = C.c_void_p()
         prec = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
-                "compensated": _ffi.PRECISION_COMPENSATED}[precision]
-        opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us, prec)
+                "compensated": _ffi.PRECISION_COMPENSATED,
+                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64}[precision]
+        opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us, prec, max_batch_work)
         k = len(models)
         cfgs = (_ffi.ce_config * k)(*[m[0].raw for m in models])
         pls = (_ffi.ce_plant * k)(*[m[1].ce_plant() for m in models])

@@ -60,6 +60,10 @@ extern "C" {
  * sweep; the fit's normal matrix in closed form (FP64) and its right-hand side by a double-float
  * projection of the FP32 trajectory; FP64 LDLT solve with one step of iterative refinement */
 #define CE_PRECISION_COMPENSATED 2
+/* A diagnostic form: the compensated form's fit, solve, eigensolves and sweep on the FP64 form's
+ * trajectory.  Against the FP64 form it isolates how much of the compensated form's difference
+ * is the FP32 trajectory's own. */
+#define CE_PRECISION_COMPENSATED_TRAJ64 3
 
 /*
  * Parsed ControllerEngine.config plus the sizes derived from it.
@@ -413,6 +417,8 @@ typedef struct ce_server_options {
     int64_t hbm_budget_bytes; /* device memory for all lanes (0: no limit); capacity shrinks to fit */
     int32_t max_wait_us;      /* a partial batch waits up to this long for more requests (0: none) */
     int32_t precision;        /* CE_PRECISION_MIXED (0, the default), _FP64 or _COMPENSATED for every lane */
+    int64_t max_batch_work;   /* candidate-steps (candidates x horizon) per batch (0: no cap); a request
+                                 above it is served in pieces on several lanes at once */
 } ce_server_options;
 
 typedef struct ce_server_stats {
@@ -423,6 +429,15 @@ typedef struct ce_server_stats {
     int64_t batched_candidates; /* candidates in those batches */
     int64_t queued;             /* requests waiting for dispatch */
     double latency_p50_ms, latency_p99_ms, latency_max_ms; /* submit -> results in the caller's buffer */
+    /* where a request's latency goes: queue = submit -> its first piece dispatched to a lane;
+     * service = that dispatch -> done (staging, copies, the evaluation and the GPU it shares) */
+    double queue_p50_ms, queue_p99_ms, service_p50_ms, service_p99_ms;
+    /* per batch: its work on the lane's stream, H2D start to D2H end (CUDA events) */
+    double batch_p50_ms, batch_p99_ms, batch_max_ms;
+    /* the requests at or above the p99 latency: their count, mean queue and service time, and the
+     * mean number of lanes busy when their first piece was dispatched */
+    int64_t tail_requests;
+    double tail_queue_ms, tail_service_ms, tail_busy_lanes;
 } ce_server_stats;
 
 #define CE_PENDING 2 /* ce_server_wait: the timeout passed first */

@@ -7,11 +7,12 @@ hypot, log10: CUDA's on the GPU, glibc's here, each within an ulp or two), so:
   and are compared to 1e-12 relative (they come out bit-identical);
 * AtA / Atb (the basis calls exp, sin and cos) within 1e-12 of each row's scale;
 * every pass/fail class (modal-unstable, nominal-unstable, eig-fail, margin status) identical;
-* the INFO row's cost terms, the double results rounded to float: at least 99% of them
-  identical, and all within 1e-6 relative, except the fit-derived terms (wn, zeta, the
-  behaviour error and the total score, the modal columns) of candidates whose scaled normal
-  matrix has a condition number above 1e9, where the libm's last-ulp differences in the basis
-  (1e-16) are amplified beyond 1e-7 -- two correct FP64 evaluations disagree there.
+* the INFO row's cost terms, the double results rounded to float: the terms no fit enters
+  (yss, overshoot, the margins) identical for at least 99% of the values, and every term within
+  1e-6 relative, except the fit-derived terms (wn, zeta, the behaviour error and the total score,
+  the modal columns) of candidates whose scaled normal matrix has a condition number above 1e9,
+  where the libm's last-ulp differences in the basis (1e-16) are amplified beyond 1e-7 -- two
+  correct FP64 evaluations disagree there.
 The same form against the mixed form: identical classes on these workloads."""
 import numpy as np
 import pytest
@@ -75,9 +76,11 @@ def test_fp64_form_against_fp64_oracle(lib, oracle_mod, name):
     assert np.array_equal(np.isfinite(a), np.isfinite(b))
     with np.errstate(invalid="ignore"):
         rel = np.where(np.isfinite(a) & np.isfinite(b), np.abs(a - b) / np.maximum(np.abs(b), 1e-30), 0.0)
-    assert (rel == 0).mean() >= 0.99, (rel == 0).mean()
+    fr = c["fr"].start
+    fit_cols = np.isin(cols, np.r_[c["sc"], fr, fr + 1, c["md"]])
+    # the terms no fit enters (yss, overshoot, the margins): the same floats, all but a few
+    assert (rel[:, ~fit_cols] == 0).mean() >= 0.99, (rel[:, ~fit_cols] == 0).mean()
     cond = _fit_condition(info, d["ata"], cfg)
-    fit_cols = np.isin(cols, np.r_[c["sc"], c["fr"][:2], c["md"]])
     ill = (cond > 1e9)[:, None] & fit_cols[None, :]
     assert rel[~ill].max() <= 1e-6, (rel[~ill].max(), np.unravel_index(np.argmax(np.where(ill, 0, rel)), rel.shape))
 
