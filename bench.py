@@ -123,6 +123,9 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
         for name, col in (("wn", fr), ("zeta", fr + 1), ("behaviour_err", s + 1)):
             row[f"{name}_compensated"] = float(np.median(rel(cmp_, col)[sel]))
             row[f"{name}_mixed"] = float(np.median(rel(mix, col)[sel]))
+            e = rel(out["compensated_traj64"][0], col)[sel]
+            row[f"{name}_compensated_on_fp64_trajectory"] = float(np.median(e))
+            row[f"{name}_compensated_on_fp64_trajectory_within_1e-6"] = float((e <= 1e-6).mean())
         bins.append(row)
     # the same errors binned by the trajectory's own difference from the FP64 one
     tbins = []
@@ -367,10 +370,12 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
     of its plant (synth.perturbed_plants); a request carries U[256, 16384] candidates on a model
     drawn uniformly -- with probability mc_fraction a Monte Carlo request (one gain set on as
     many consecutive plants, ce_server_submit_plants), else a tuning request (distinct gain
-    sets on one plant).  Saturation: 96 requests submitted at once, candidates/s until all are
+    sets on one plant).  Saturation: 256 requests submitted at once, candidates/s until all are
     done.  Latency: Poisson arrivals at 70% of that rate for `seconds`, then at 50 requests/s
     (light load, when below that) for half as long; p50/p99 of submit ->
-    results in the caller's buffer (measured by the server)."""
+    results in the caller's buffer (measured by the server).  The loaded runs draw their requests
+    and arrival times beforehand and keep Python's garbage collector off, so the generator itself
+    adds no bursts."""
     import controllerengine_gb300 as ce
     from controllerengine_gb300 import synth
     rng = np.random.default_rng(seed)
@@ -423,7 +428,7 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
             for h in hs:
                 h.wait()
         refused[0] = 0
-        reqs = [draw() for _ in range(96)]
+        reqs = [draw() for _ in range(256)]
         total = sum(r[3].shape[0] for r in reqs)
         t0 = time.perf_counter()
         hs = []
@@ -440,23 +445,33 @@ def serving_bench(problems, seconds: float, lanes: int = 3, max_batch: int = 163
         rate = 0.7 * sat / mean_size  # requests/s
         # consecutive loaded runs; the line's main figures are the last run's, every run's are listed
         per_run = []
+        import gc
         for _ in range(max(1, runs)):
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 16))
+            arrivals = arrivals[arrivals < seconds]
+            plan = [draw() for _ in range(len(arrivals))]
             srv.reset_stats()
             hs, offered, n_mc = [], 0, 0
-            t0 = time.perf_counter()
-            t_next = t0
-            while t_next - t0 < seconds:
-                now = time.perf_counter()
-                if now < t_next:
-                    time.sleep(t_next - now)
-                req, h = draw_submit(srv)
-                offered += req[3].shape[0]
-                n_mc += req[1]
-                hs.append(h)
-                t_next += rng.exponential(1.0 / rate)
-            for h in hs:
-                h.wait()
-            wall = time.perf_counter() - t0
+            gc.disable()
+            try:
+                t0 = time.perf_counter()
+                for t_at, req in zip(arrivals, plan):
+                    now = time.perf_counter() - t0
+                    if now < t_at:
+                        time.sleep(t_at - now)
+                    try:
+                        h = submit(srv, req)
+                    except ce.ControllerEngineError:
+                        refused[0] += 1  # a plant whose sweep grid failed: refused at submit
+                        continue
+                    offered += req[3].shape[0]
+                    n_mc += req[1]
+                    hs.append(h)
+                for h in hs:
+                    h.wait()
+                wall = time.perf_counter() - t0
+            finally:
+                gc.enable()
             st = srv.stats()
             per_run.append({"requests": st["completed"], "latency_p50_ms": st["latency_p50_ms"],
                             "latency_p99_ms": st["latency_p99_ms"], "latency_max_ms": st["latency_max_ms"],

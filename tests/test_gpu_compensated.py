@@ -137,3 +137,48 @@ def test_compensated_rows_do_not_depend_on_the_batch(lib):
         full = s.evaluate(p.cuda_mx, p.info_mx)
         part = np.vstack([s.evaluate(p.cuda_mx[a:a + 97], p.info_mx[a:a + 97]) for a in range(0, 512, 97)])
     assert np.array_equal(full, part, equal_nan=True)
+
+
+def _fit_condition(info, ata, cfg):
+    nt = cfg.total_dim
+    uniq = info[:, cfg.info_modal + 3 * nt].astype(int)
+    out = np.zeros(info.shape[0])
+    for k in range(info.shape[0]):
+        nc = 2 * uniq[k]
+        if nc == 0 or info[k, cfg.info_scoring + 1] >= cfg.unstable_err:
+            continue
+        A = ata[k].reshape(2 * nt, 2 * nt)[:nc, :nc]
+        A = np.tril(A) + np.tril(A, -1).T
+        dg = np.sqrt(np.abs(np.diag(A)))
+        dg[dg <= 1e-6] = 1.0
+        out[k] = np.linalg.cond(A / dg[:, None] / dg[None, :])
+    return out
+
+
+@pytest.mark.parametrize("name", ["mass_spring", "eight_state"])
+def test_compensated_arithmetic_on_the_fp64_trajectory(lib, name):
+    """The diagnostic precision "compensated_traj64": the compensated form's fit, solve,
+    eigensolves and sweep fed with the FP64 form's trajectory.  Against the FP64 form, everything
+    that does not pass through the fit is identical (classes, yss, overshoot, margins), and the fit
+    terms agree within 1e-6 wherever the scaled normal matrix is conditioned below 1e8 -- so the
+    compensated form's larger differences on those candidates are its FP32 trajectory's."""
+    p = _problems()[name]
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, precision="fp64") as s:
+        f64, d64 = s.evaluate_diagnostics64(p.cuda_mx, p.info_mx, want=("ata",))
+    with ce.Session(cfg, p.plant, precision="compensated_traj64") as s:
+        t64 = s.evaluate(p.cuda_mx, p.info_mx)
+    assert np.array_equal(_classes(t64, cfg), _classes(f64, cfg))
+    c = _cols(cfg)
+    fr = c["fr"].start
+    for col in (fr + 2, fr + 3):
+        assert np.array_equal(t64[:, col], f64[:, col], equal_nan=True)
+    assert np.array_equal(t64[:, c["am"]], f64[:, c["am"]], equal_nan=True)
+    cond = _fit_condition(f64, d64["ata"], cfg)
+    good = (cond > 0) & (cond < 1e8) & (f64[:, cfg.info_scoring + 1] < cfg.unstable_err)
+    if good.sum() == 0:
+        pytest.skip("no well-conditioned fit in this workload")
+    for col in (fr, fr + 1, cfg.info_scoring + 1):
+        a, b = t64[good, col].astype(np.float64), f64[good, col].astype(np.float64)
+        rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+        assert rel.max() <= 1e-6, (col, rel.max(), int(good.sum()))

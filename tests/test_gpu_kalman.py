@@ -75,8 +75,9 @@ def test_kalman_per_candidate_plants():
 def test_kalman_fp64_form_refused(mass_kalman):
     cfg = ce.EngineConfig.parse(mass_kalman.config_text)
     with ce.Session(cfg, mass_kalman.plant) as s:
-        with pytest.raises(ce.ControllerEngineError, match="mixed precision"):
+        with pytest.raises(ce.ControllerEngineError, match="simulates in FP32 only"):
             s.set_precision("fp64")
+        s.set_precision("compensated")  # the compensated form simulates in FP32: accepted
 
 
 def _bucket(r, q):
