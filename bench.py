@@ -267,6 +267,7 @@ def parity_report(gpu, ref, cfg):
     rel = {k: stats(np.abs(g64[scored, c] - r64[scored, c]) / np.maximum(np.abs(r64[scored, c]), 1e-6))
            for k, c in terms.items()}
     return {"candidates": int(len(gpu)), "class_identity": float(same.mean()),
+            "rows_bit_identical": float((gpu.view(np.uint32) == ref.view(np.uint32)).all(axis=1).mean()),
             "class_mismatches": int((~same).sum()), "scored_compared": int(scored.sum()),
             "margin_abs_diff": absd, "relative_diff": rel,
             "margins_within_1e-3": bool(all(v is None or v["max"] <= 1e-3 for v in absd.values()))}
@@ -641,9 +642,9 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
     per_inst = (time.perf_counter() - t0) / len(pick)
     for s_ in sess:
         s_.close()
-    # (b) padded to max: the same instances (their own plants and programs, the simulation already
-    # at the padded 8/8 width) with every horizon raised to the largest, 20,000 steps at the
-    # instance's own step size, and every sweep to 400 points, through the same ragged path
+    # (b) padded to max: the same instances (their own plants and programs) with the simulation at
+    # the padded 8/8 width, every horizon raised to the largest, 20,000 steps at the instance's own
+    # step size, and every sweep to 400 points, through the same ragged path
     import re
 
     def pad(p, c):
@@ -654,6 +655,7 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
     pcfgs = [ce.EngineConfig.parse(pad(p, c)) for p, c in zip(probs, cfgs)]
     assert all(c.time == 20000 and c.freq == 400 for c in pcfgs)
     with ce.Ragged([(c, p.plant) for c, p in zip(pcfgs, probs)]) as rp:
+        rp.set_tuning(sim_width=8)  # every candidate at the padded 8/8 width, as the reference pads
         for _ in range(warmup):
             rp.evaluate_packed(counts, g_all, i_all)
         t0 = time.perf_counter()
@@ -685,7 +687,7 @@ def uneven_bench(n_inst: int, steps: int, warmup: int, sample: int = 24):
                                          "sample": len(pick)},
             "padded_to_max": {"instances_per_s": n_inst / padded, "ms_per_step": 1e3 * padded,
                               "padding": "the same instances, every horizon 20000 steps and every sweep 400 "
-                                         "points (the simulation always runs at the padded 8/8 width)"},
+                                         "points, the simulation at the padded 8/8 width (ce_ragged_tuning.sim_width = 8)"},
             "uniform_max_plant": {"instances_per_s": n_inst / uniform, "ms_per_step": 1e3 * uniform,
                                   "shape": "one 8-state, 4 NL-term plant and program for every candidate, "
                                            "20000 steps, 400 points (a different problem)"},
@@ -988,6 +990,7 @@ def main():
         sess.set_profiling(False)
         sess.set_eig_arith(arith0)
         rep = parity_report(value_rows, o_rows, cfg)
+        other_rows = o_rows
         eig_cmp = {"default": arith0, "other": other, "other_ms_per_step": e0.elapsed_time(e1) / 2,
                    "other_stages_ms_per_step": o_stages,
                    "rows_bit_identical": float((value_rows.view(np.uint32) == o_rows.view(np.uint32)).all(axis=1).mean()),
@@ -1087,6 +1090,12 @@ def main():
         line["parity"]["what"] = ("engine rows of the timed headline batch (default eigensolve arithmetic: "
                                   f"{sess.eig_arith}) vs the oracle's rows (the reference's separate arithmetic) "
                                   "on the cpu_baseline sample")
+        if eig_cmp is not None and eig_cmp["other"] == "separate":
+            # the same sample evaluated with the reference's own (separate) eigensolve arithmetic
+            sep = parity_report(other_rows[:len(orc_rows)], orc_rows, cfg)
+            sep["what"] = ("engine rows of the same headline batch with the separate eigensolve arithmetic "
+                           "(the oracle's) vs the oracle's rows on the cpu_baseline sample")
+            line["parity"]["separate_arithmetic"] = sep
     if rank == 0:
         print(json.dumps(line), flush=True)
     sess.close()

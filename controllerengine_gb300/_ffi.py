@@ -102,7 +102,7 @@ class ce_diagnostics64(C.Structure):
 
 class ce_ragged_tuning(C.Structure):
     _fields_ = [("sim_lanes", C.c_int32), ("instance_order", C.c_int32), ("eig_blocks_per_sm", C.c_int32),
-                ("ms_per_evaluation", C.c_double)]
+                ("sim_width", C.c_int32), ("ms_per_evaluation", C.c_double)]
 
 
 class ce_tuning(C.Structure):

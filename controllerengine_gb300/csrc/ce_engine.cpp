@@ -1277,7 +1277,7 @@ void ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
     }
     if (N > INT32_MAX) fail("ce_ragged_evaluate: {} candidates exceed the 32-bit candidate index", N);
     const std::vector<int64_t> counts(n_cand, n_cand + I);
-    const int lanes = ragged_lanes(r), inst_order = r->tuning.instance_order ? 1 : 0;
+    const int lanes = ragged_lanes(r), inst_order = r->tuning.instance_order;
     if (r->prepared && counts == r->prep_counts && lanes == r->prep_lanes && inst_order == r->prep_inst_order)
         return;
     r->prepared = false;
@@ -1294,14 +1294,22 @@ void ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
     }
     r->h_inst.resize((size_t)N);
     r->dev_k.resize((size_t)N);
-    // The device order.  Candidates sorted by decreasing horizon are dealt to the
-    // W warps of the simulation (32 / lanes candidates each) in turn: warp w
-    // holds sorted candidates w, W + w, 2W + w, ..., one from each horizon tier.
-    // A warp's lanes interpret different instruction programs, so a step costs
-    // about as many passes as its active lanes hold distinct operations; with the
-    // horizons spread, the short lanes leave early and the long ones finish with
-    // few lanes active, instead of the longest instances sharing warps for their
-    // whole horizon.  (instance_order: the candidates in the caller's order.)
+    // The device order (instance_order):
+    // 0 (default): grouped by program.  Instances are sorted by the dimension
+    //   class of their simulation (4 or 8 observer / plant rows), then by the
+    //   operation sequence of their programs, then by decreasing horizon, and
+    //   each instance's candidates stay together.  A warp's lanes then interpret
+    //   the same operations in the same slots (one path per slot instead of one
+    //   per program), run the dimension class of their own plants, and have
+    //   similar horizons, so few lanes idle after their horizon ends.
+    // 1: the caller's order.
+    // 2: dealt by horizon.  Candidates sorted by decreasing horizon are dealt to
+    //   the W warps of the simulation (32 / lanes candidates each) in turn: warp w
+    //   holds sorted candidates w, W + w, 2W + w, ..., one from each horizon tier,
+    //   each tier ordered by program.
+    auto sim_class = [&](int i) {
+        return (r->cfg[i].statespace_dim > 4 ? 2 : 0) + (r->cfg[i].discrete_dim > 4 ? 1 : 0);
+    };
     std::vector<int> sorted_inst;
     std::vector<int64_t> sorted_k;
     sorted_inst.reserve((size_t)N);
@@ -1309,7 +1317,14 @@ void ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
     {
         std::vector<int> order(I);
         for (int i = 0; i < I; ++i) order[i] = i;
-        if (!inst_order)
+        if (inst_order == 0)
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                const int ca = sim_class(a), cb = sim_class(b);
+                if (ca != cb) return ca < cb;
+                if (r->sig[a] != r->sig[b]) return r->sig[a] < r->sig[b];
+                return r->cfg[a].time > r->cfg[b].time;
+            });
+        else if (inst_order == 2)
             std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r->cfg[a].time > r->cfg[b].time; });
         for (int i : order)
             for (int64_t k = 0; k < n_cand[i]; ++k) {
@@ -1317,7 +1332,7 @@ void ragged_prepare(ce_ragged* r, const int64_t* n_cand) {
                 sorted_k.push_back(k);
             }
     }
-    if (inst_order) {
+    if (inst_order != 2) {
         for (int64_t q = 0; q < N; ++q) {
             r->h_inst[(size_t)q] = sorted_inst[(size_t)q];
             r->dev_k[(size_t)q] = sorted_k[(size_t)q];
@@ -1409,7 +1424,8 @@ void ragged_enqueue(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in
     Buffers& b = s->buf;
     const int LW = r->layout.cuda_mx_width, LI = r->layout.info_mx_width;
     launch_ragged_gather(N, r->d_goff, r->d_ioff, r->d_wid, LW, LI, d_cuda_mx, d_info_in, b.gains, b.info, st);
-    const Ragged rg{r->d_runs, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, r->prep_lanes};
+    const Ragged rg{r->d_runs, r->d_plants, r->d_inst, r->d_tab, r->inst_cap, r->prep_lanes,
+                    r->tuning.sim_width == 8 ? 1 : 0};
     run_pipeline(s, 0, N, b.gains, b.info, st, false, false, &rg);
     launch_ragged_scatter(N, r->d_ioff, r->d_wid, LI, b.info, d_info_out, st);
     s->launches += 2;
@@ -1473,8 +1489,9 @@ void ragged_evaluate(ce_ragged* r, const int64_t* n_cand, const float* cuda_mx, 
 }
 
 // The ragged autotuner: coordinate descent over the simulation form (the wide
-// four-lane form or one thread per candidate), the device order (dealt by
-// horizon or the caller's order) and the FP64 eigensolves' blocks per SM, each
+// four-lane form or one thread per candidate), the device order (grouped by
+// program, the caller's order, or dealt by horizon) and the FP64 eigensolves'
+// blocks per SM, each
 // setting timed over three evaluations of the prepared batch on the caller's
 // rows; the fastest is kept.  Results do not depend on the setting.
 void ragged_autotune(ce_ragged* r, const float* d_cuda_mx, const float* d_info_in, float* d_info_out, void* stream,
@@ -1512,9 +1529,9 @@ void ragged_autotune(ce_ragged* r, const float* d_cuda_mx, const float* d_info_i
         t.sim_lanes = cur.sim_lanes == 1 ? SW_LANES : 1;
         try_set(t);
     }
-    {
+    for (int o = 1; o <= 2; ++o) {
         ce_ragged_tuning t = cur;
-        t.instance_order = cur.instance_order ? 0 : 1;
+        t.instance_order = (cur.instance_order + o) % 3;
         try_set(t);
     }
     for (int b : {cur.eig_blocks_per_sm - 1, cur.eig_blocks_per_sm + 1})
@@ -1631,10 +1648,11 @@ CE_EXPORT int ce_ragged_set_tuning(ce_ragged* r, const ce_ragged_tuning* t) {
         if (!r || !t) fail("null argument");
         if (t->sim_lanes != 0 && t->sim_lanes != 1 && t->sim_lanes != SW_LANES)
             fail("sim_lanes must be 0, 1 or {}, got {}", SW_LANES, t->sim_lanes);
-        if (t->instance_order != 0 && t->instance_order != 1)
-            fail("instance_order must be 0 or 1, got {}", t->instance_order);
+        if (t->instance_order < 0 || t->instance_order > 2)
+            fail("instance_order must be 0, 1 or 2, got {}", t->instance_order);
         if (t->eig_blocks_per_sm < 0 || t->eig_blocks_per_sm > 32)
             fail("eig_blocks_per_sm must be in [0, 32], got {}", t->eig_blocks_per_sm);
+        if (t->sim_width != 0 && t->sim_width != 8) fail("sim_width must be 0 or 8, got {}", t->sim_width);
         r->tuning = *t;
         r->tuning.ms_per_evaluation = 0.0;
         r->prepared = false;  // the next evaluation rebuilds the device order

@@ -97,6 +97,7 @@ struct Ragged {
     const float* tab;
     int64_t tab_stride;
     int lanes;  // lanes per candidate of the simulation: SW_LANES (the wide form) or 1
+    int full_width;  // 1: the wide form runs every warp at the padded 8/8 width
 };
 
 // Fields of that table: observer model, plant, instruction counts and slots.

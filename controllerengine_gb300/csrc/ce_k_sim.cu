@@ -39,7 +39,8 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const _
 // one lane with the operations and order of the one-thread form, so the
 // results are bit-identical to it.  The quad exchanges y, W and its new state
 // rows through the candidate's slot in shared memory: three quad barriers per
-// step.
+// step.  A warp whose candidates all have ns <= 4 (nd <= 4) runs the 4-row
+// observer (plant) step, one row per lane, with the padding beyond 4 virtual.
 // words between consecutive fields of the block's table columns: with 17 the
 // four lanes of a quad, reading fields of their NL chains 24 fields apart, and
 // the warp's eight candidates, reading one field, fall on 32 different banks
@@ -51,78 +52,130 @@ constexpr int WS_XH_HI = 0, WS_XH_LO = 8, WS_XP_HI = 16, WS_Y = WS_XP_HI + MAXD,
               WS_STRIDE = 52;
 static_assert(MAXS == 8 && MAXD == 8 && MAXW == SW_LANES, "the quad splits 8 rows and 4 NL chains");
 
-__global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch, const float* __restrict__ gains,
-                                                               float* __restrict__ ywin,
-                                                               SimSummary* __restrict__ summ) {
-    __shared__ float tab[RT_FIELDS * WIDE_TS];
-    __shared__ __align__(16) float slots[SW_CPB * WS_STRIDE];
-    __shared__ float stage[8][SW_CPB];
-    const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
-    const unsigned qm = 0xFu << (threadIdx.x & 28);
-    const int64_t c = (int64_t)blockIdx.x * SW_CPB + cl;
-    if (c >= launch.n) return;  // the whole quad leaves together
-    const Run& run = run_of<true>(launch, c);
-    {
-        // the candidate's table column, copied once by its quad
-        const float* __restrict__ g = launch.rg.tab + c;
-        const int64_t gs = launch.rg.tab_stride;
-        for (int f = q; f < RT_FIELDS; f += SW_LANES) tab[f * WIDE_TS + cl] = g[(int64_t)f * gs];
+// The quad's row arithmetic at dimension class NC (4 or 8 rows): lane q owns
+// NC / 4 rows.  Loops run to the class, with the padding beyond it virtual as
+// in sim_run: `pad` stands for the reference's zero-coefficient terms over the
+// padded states (+0, or NaN once a padded state has turned NaN), so every
+// class gives the padded 8/8 result bit for bit.
+// K.x over the double-float state (hi terms, then lo terms)
+template <int NC>
+__device__ __forceinline__ float rw_dot(const float* k, const float* hi, const float* lo, float pad) {
+    float a = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) a = __fmaf_rn(k[i], hi[i], a);
+    if (NC < MAXS) a = __fadd_rn(a, pad);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) a = __fmaf_rn(k[i], lo[i], a);
+    if (NC < MAXS) a = __fadd_rn(a, pad);
+    return a;
+}
+// this lane's observer rows: the increment (A-I)xh + B u + L yerr, then the
+// double-float add onto the row's old value (old_hi / old_lo in, new out)
+template <int NC>
+__device__ __forceinline__ void rw_obs(const float (*sai)[MAXS], const float* sb, const float* Lr, float u, float yerr,
+                                       const float* xh_hi, const float* xh_lo, float pad, float* nh, float* nlo) {
+#pragma unroll
+    for (int rr = 0; rr < NC / SW_LANES; ++rr) {
+        float h = __fmaf_rn(Lr[rr], yerr, __fmul_rn(sb[rr], u));
+        float l = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NC; ++j) h = __fmaf_rn(sai[rr][j], xh_hi[j], h);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) l = __fmaf_rn(sai[rr][j], xh_lo[j], l);
+        if (NC < MAXS) {
+            h = __fadd_rn(h, pad);
+            l = __fadd_rn(l, pad);
+        }
+        df_add(nh[rr], nlo[rr], h, l);
     }
-    float* st = slots + cl * WS_STRIDE;
-    const int r0 = 2 * q;
+}
+// this lane's plant rows: (Ad-I)xp + Bu u + Bw W, then the double-float add
+template <int NC>
+__device__ __forceinline__ void rw_plant(const float (*dai)[MAXD], const float (*dbw)[MAXW], const float* dbu,
+                                         float u, const float* W, const float* xp_hi, const float* xp_lo, float pad,
+                                         float* ph, float* plo) {
+#pragma unroll
+    for (int rr = 0; rr < NC / SW_LANES; ++rr) {
+        float h = __fmul_rn(dbu[rr], u);
+#pragma unroll
+        for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(dbw[rr][k], W[k], h);
+        float l = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NC; ++j) h = __fmaf_rn(dai[rr][j], xp_hi[j], h);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) l = __fmaf_rn(dai[rr][j], xp_lo[j], l);
+        if (NC < MAXD) {
+            h = __fadd_rn(h, pad);
+            l = __fadd_rn(l, pad);
+        }
+        df_add(ph[rr], plo[rr], h, l);
+    }
+}
+// a padded state turns NaN once a zero coefficient meets a non-finite operand
+template <int NC>
+__device__ __forceinline__ bool rw_bad(const float* hi, const float* lo) {
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) bad = bad || !isfinite(hi[j]) || !isfinite(lo[j]);
+    return bad;
+}
+
+// The quad's steps.  s8 / d8: the warp's observer / plant class is 8 rows
+// (two per lane) rather than 4 (one per lane); both are warp-uniform, so the
+// class only selects the row arithmetic and the chain interpreters, the bulk
+// of the code, exist once.
+__device__ __forceinline__ void ragged_wide_steps(const Run& run, const float* t, float* st, float (*stage)[SW_CPB],
+                                                  const int cl, const int q, const unsigned qm, const bool s8,
+                                                  const bool d8, const float* __restrict__ row,
+                                                  float* __restrict__ wrow, SimSummary* __restrict__ out) {
+    const int rs = s8 ? 2 : 1, rd = d8 ? 2 : 1;  // rows per lane
+    const int rs0 = q * rs, rd0 = q * rd;
+    const int ns = run.ns;
+    float sai[2][MAXS], dai[2][MAXD], sb[2], dbu[2], Lr[2], K[MAXS];
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
-        st[WS_XH_HI + r0 + rr] = 0.0f;
-        st[WS_XH_LO + r0 + rr] = 0.0f;
-        st[WS_XP_HI + r0 + rr] = 0.0f;
-        st[WS_XP_LO + r0 + rr] = 0.0f;
-    }
-    __syncwarp(qm);
-    const float* t = tab + cl;  // field f at t[f * WIDE_TS]
-    float sai[2][MAXS], dai[2][MAXD], dbw[2][MAXW], sb[2], dbu[2], sc[MAXS];
+        const int i = rs0 + (rr < rs ? rr : 0);  // a second row only in class 8
 #pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
+        for (int j = 0; j < MAXS; ++j) sai[rr][j] = t[(RT_SAI + i * MAXS + j) * WIDE_TS];
+        sb[rr] = t[(RT_SB + i) * WIDE_TS];
+        Lr[rr] = i < ns ? row[ns + i] : 0.0f;
+        const int d = rd0 + (rr < rd ? rr : 0);
 #pragma unroll
-        for (int j = 0; j < MAXS; ++j) sai[rr][j] = t[(RT_SAI + (r0 + rr) * MAXS + j) * WIDE_TS];
-#pragma unroll
-        for (int j = 0; j < MAXD; ++j) dai[rr][j] = t[(RT_DAI + (r0 + rr) * MAXD + j) * WIDE_TS];
-#pragma unroll
-        for (int k = 0; k < MAXW; ++k) dbw[rr][k] = t[(RT_DBW + (r0 + rr) * MAXW + k) * WIDE_TS];
-        sb[rr] = t[(RT_SB + r0 + rr) * WIDE_TS];
-        dbu[rr] = t[(RT_DBU + r0 + rr) * WIDE_TS];
+        for (int j = 0; j < MAXD; ++j) dai[rr][j] = t[(RT_DAI + d * MAXD + j) * WIDE_TS];
+        dbu[rr] = t[(RT_DBU + d) * WIDE_TS];
     }
 #pragma unroll
-    for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_TS];
+    for (int j = 0; j < MAXS; ++j) K[j] = j < ns ? row[j] : 0.0f;
     const float sd = t[RT_SD * WIDE_TS];
     const unsigned cnt0 = __float_as_uint(t[RT_CNT * WIDE_TS]), cnt1 = __float_as_uint(t[(RT_CNT + 1) * WIDE_TS]);
     const int n_dc = (int)(cnt0 & 0xFFu), n_u = (int)((cnt0 >> 8) & 0xFFu);
     const int n_nl = q == 0 ? (int)((cnt0 >> 16) & 0xFFu) : q == 1 ? (int)(cnt0 >> 24)
                    : q == 2 ? (int)(cnt1 & 0xFFu) : (int)((cnt1 >> 8) & 0xFFu);
-    const int ns = run.ns;
-    const float* row = gains + c * run.cuda_w;
-    float K[MAXS], Lr[2];
-#pragma unroll
-    for (int i = 0; i < MAXS; ++i) K[i] = i < ns ? row[i] : 0.0f;
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr) Lr[rr] = r0 + rr < ns ? row[ns + r0 + rr] : 0.0f;
     const float N = row[2 * ns];
 
     float xh_hi[MAXS], xh_lo[MAXS], xp_hi[MAXD], xp_lo[MAXD];
 #pragma unroll
     for (int i = 0; i < MAXS; ++i) xh_hi[i] = xh_lo[i] = xp_hi[i] = xp_lo[i] = 0.0f;
+    bool poisS = false, poisD = false;
     float ysum = 0.0f, ycomp = 0.0f, ymax = -CUDART_INF_F, ymin = CUDART_INF_F;
-    float* wrow = ywin + c * (int64_t)run.fit_pitch;
-    const int T = run.time;
+    // the instance's scalars in registers: its Run lives in global memory, and
+    // the fit-window stores could alias it, so reads inside the loop would be
+    // reloaded every step
+    const int T = run.time, fit0 = run.fit_start_id, fitn = run.fit_steps, ss0 = run.steady_start_id,
+              rstep = run.ref_step_id;
+    const float ramp = run.ref_amp;
     for (int tt = 0; tt < T; ++tt) {
+        const float padS = poisS ? CUDART_NAN_F : 0.0f;
+        const float padD = poisD ? CUDART_NAN_F : 0.0f;
         // plant output
         const float y = run_chain_tab<false, MAX_DC, 1>(t, WIDE_TS, 0, n_dc, st + WS_XP_HI, 0.0f);
         if (q == 0) {
             st[WS_Y] = y;
             // fit window, steady-state sum, extremes
-            const int w = tt - run.fit_start_id;
-            if (w >= 0 && w < run.fit_steps) {
+            const int w = tt - fit0;
+            if (w >= 0 && w < fitn) {
                 stage[w & 7][cl] = y;
-                if ((w & 7) == 7 || w == run.fit_steps - 1 || tt == T - 1) {
+                if ((w & 7) == 7 || w == fitn - 1 || tt == T - 1) {
                     float4 a, b;
                     a.x = stage[0][cl]; a.y = stage[1][cl]; a.z = stage[2][cl]; a.w = stage[3][cl];
                     b.x = stage[4][cl]; b.y = stage[5][cl]; b.z = stage[6][cl]; b.w = stage[7][cl];
@@ -131,77 +184,78 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
                     dst[1] = b;
                 }
             }
-            if (tt >= run.steady_start_id) ysum_add(ysum, ycomp, y);
+            if (tt >= ss0) ysum_add(ysum, ycomp, y);
             ymax = fmaxf(ymax, y);
             ymin = fminf(ymin, y);
         }
         // controller output
-        float kx = 0.0f;
-#pragma unroll
-        for (int i = 0; i < MAXS; ++i) kx = __fmaf_rn(K[i], xh_hi[i], kx);
-#pragma unroll
-        for (int i = 0; i < MAXS; ++i) kx = __fmaf_rn(K[i], xh_lo[i], kx);
-        const float ref = tt < run.ref_step_id ? 0.0f : run.ref_amp;
+        const float kx = s8 ? rw_dot<8>(K, xh_hi, xh_lo, padS) : rw_dot<4>(K, xh_hi, xh_lo, padS);
+        const float ref = tt < rstep ? 0.0f : ramp;
         const float u_raw = __fmaf_rn(N, ref, -kx);
         const float u = run_chain_tab<true, MAX_U, 1>(t, WIDE_TS, MAX_DC, n_u, st + WS_XH_HI, u_raw);
         // observer output error
-        float yh = 0.0f;
+        float sc[MAXS];  // C of the observer model, from the table (registers are short here)
 #pragma unroll
-        for (int i = 0; i < MAXS; ++i) yh = __fmaf_rn(sc[i], xh_hi[i], yh);
-#pragma unroll
-        for (int i = 0; i < MAXS; ++i) yh = __fmaf_rn(sc[i], xh_lo[i], yh);
+        for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_TS];
+        float yh = s8 ? rw_dot<8>(sc, xh_hi, xh_lo, padS) : rw_dot<4>(sc, xh_hi, xh_lo, padS);
         yh = __fmaf_rn(sd, u, yh);
         const float yerr = __fsub_rn(y, yh);
-        // this lane's observer rows: increment, then double-float add
+        // this lane's observer rows; the rows' old values from the slot (an index
+        // by lane would put the state arrays in local memory); nothing writes the
+        // slot before the second barrier of the step
         float nh[2], nlo[2];
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-            float h = __fmaf_rn(Lr[rr], yerr, __fmul_rn(sb[rr], u));
-            float l = 0.0f;
-#pragma unroll
-            for (int j = 0; j < MAXS; ++j) h = __fmaf_rn(sai[rr][j], xh_hi[j], h);
-#pragma unroll
-            for (int j = 0; j < MAXS; ++j) l = __fmaf_rn(sai[rr][j], xh_lo[j], l);
-            // the row's old value from the slot (an index by lane would put the
-            // state arrays in local memory); nothing writes the slot before the
-            // second barrier of the step
-            nh[rr] = st[WS_XH_HI + r0 + rr];
-            nlo[rr] = st[WS_XH_LO + r0 + rr];
-            df_add(nh[rr], nlo[rr], h, l);
+        nh[0] = st[WS_XH_HI + rs0];
+        nlo[0] = st[WS_XH_LO + rs0];
+        if (s8) {
+            nh[1] = st[WS_XH_HI + rs0 + 1];
+            nlo[1] = st[WS_XH_LO + rs0 + 1];
+            rw_obs<8>(sai, sb, Lr, u, yerr, xh_hi, xh_lo, padS, nh, nlo);
+        } else {
+            rw_obs<4>(sai, sb, Lr, u, yerr, xh_hi, xh_lo, padS, nh, nlo);
+            poisS = poisS || !isfinite(yerr) || !isfinite(u) || rw_bad<4>(xh_hi, xh_lo);
         }
         __syncwarp(qm);  // y is in the slot
         // this lane's nonlinear term over [xp_hi, y]
         st[WS_W + q] = run_chain_tab<false, MAX_NL, 1>(t, WIDE_TS, MAX_DC + MAX_U + q * MAX_NL, n_nl,
                                                         st + WS_XP_HI, 0.0f);
         __syncwarp(qm);  // every W is in the slot; every read of this step's state is done
-        float W[MAXW];
+        float W[MAXW], dbw[2][MAXW];  // Bw rows from the table (registers are short here)
 #pragma unroll
         for (int k = 0; k < MAXW; ++k) W[k] = st[WS_W + k];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) dbw[rr][k] = t[(RT_DBW + (rd0 + (rr < rd ? rr : 0)) * MAXW + k) * WIDE_TS];
         // this lane's plant rows
         float ph[2], plo[2];
+        ph[0] = st[WS_XP_HI + rd0];
+        plo[0] = st[WS_XP_LO + rd0];
+        if (d8) {
+            ph[1] = st[WS_XP_HI + rd0 + 1];
+            plo[1] = st[WS_XP_LO + rd0 + 1];
+            rw_plant<8>(dai, dbw, dbu, u, W, xp_hi, xp_lo, padD, ph, plo);
+        } else {
+            rw_plant<4>(dai, dbw, dbu, u, W, xp_hi, xp_lo, padD, ph, plo);
+            bool bad = !isfinite(u);
 #pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-            float h = __fmul_rn(dbu[rr], u);
-#pragma unroll
-            for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(dbw[rr][k], W[k], h);
-            float l = 0.0f;
-#pragma unroll
-            for (int j = 0; j < MAXD; ++j) h = __fmaf_rn(dai[rr][j], xp_hi[j], h);
-#pragma unroll
-            for (int j = 0; j < MAXD; ++j) l = __fmaf_rn(dai[rr][j], xp_lo[j], l);
-            ph[rr] = st[WS_XP_HI + r0 + rr];
-            plo[rr] = st[WS_XP_LO + r0 + rr];
-            df_add(ph[rr], plo[rr], h, l);
+            for (int k = 0; k < MAXW; ++k) bad = bad || !isfinite(W[k]);
+            poisD = poisD || bad || rw_bad<4>(xp_hi, xp_lo);
         }
         // publish this lane's rows, then read the whole new state
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-            st[WS_XH_HI + r0 + rr] = nh[rr];
-            st[WS_XH_LO + r0 + rr] = nlo[rr];
-            st[WS_XP_HI + r0 + rr] = ph[rr];
-            st[WS_XP_LO + r0 + rr] = plo[rr];
+        st[WS_XH_HI + rs0] = nh[0];
+        st[WS_XH_LO + rs0] = nlo[0];
+        if (s8) {
+            st[WS_XH_HI + rs0 + 1] = nh[1];
+            st[WS_XH_LO + rs0 + 1] = nlo[1];
+        }
+        st[WS_XP_HI + rd0] = ph[0];
+        st[WS_XP_LO + rd0] = plo[0];
+        if (d8) {
+            st[WS_XP_HI + rd0 + 1] = ph[1];
+            st[WS_XP_LO + rd0 + 1] = plo[1];
         }
         __syncwarp(qm);
+        // rows 4..7 stay zero in class 4 (no lane owns them)
 #pragma unroll
         for (int i = 0; i < MAXS; i += 4) {
             const float4 a = *reinterpret_cast<const float4*>(st + WS_XH_HI + i);
@@ -220,8 +274,43 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged_wide(const Run launch,
         sm.ymax = ymax;
         sm.ymin = ymin;
         sm.ycomp = ycomp;
-        summ[c] = sm;
+        *out = sm;
     }
+}
+
+__global__ void __launch_bounds__(SIM_BLOCK, 8) k_sim_ragged_wide(const Run launch, const float* __restrict__ gains,
+                                                               float* __restrict__ ywin,
+                                                               SimSummary* __restrict__ summ) {
+    __shared__ float tab[RT_FIELDS * WIDE_TS];
+    __shared__ __align__(16) float slots[SW_CPB * WS_STRIDE];
+    __shared__ float stage[8][SW_CPB];
+    const int q = threadIdx.x & 3, cl = threadIdx.x >> 2;
+    const unsigned qm = 0xFu << (threadIdx.x & 28);
+    const int64_t c = (int64_t)blockIdx.x * SW_CPB + cl;
+    if (c >= launch.n) return;  // the whole quad leaves together
+    const Run& run = run_of<true>(launch, c);
+    {
+        // the candidate's table column, copied once by its quad
+        const float* __restrict__ g = launch.rg.tab + c;
+        const int64_t gs = launch.rg.tab_stride;
+        for (int f = q; f < RT_FIELDS; f += SW_LANES) tab[f * WIDE_TS + cl] = g[(int64_t)f * gs];
+    }
+    float* st = slots + cl * WS_STRIDE;
+    // the state slot starts at zero, padded rows included (they stay zero for a
+    // class below 8: no lane owns them, and no program reads them)
+    for (int k = q; k < WS_STRIDE; k += SW_LANES) st[k] = 0.0f;
+    // The warp runs the largest dimension class among its candidates (any
+    // class at least the candidate's own gives its result), so its quads do
+    // not diverge; a device order grouped by class keeps most warps at their
+    // candidates' own class.  The lanes still here are whole quads.
+    const unsigned live = __activemask();
+    const bool s8 = launch.rg.full_width || __any_sync(live, run.ns > 4);
+    const bool d8 = launch.rg.full_width || __any_sync(live, run.nd > 4);
+    __syncwarp(qm);
+    const float* t = tab + cl;  // field f at t[f * WIDE_TS]
+    const float* row = gains + c * run.cuda_w;
+    float* wrow = ywin + c * (int64_t)run.fit_pitch;
+    ragged_wide_steps(run, t, st, stage, cl, q, qm, s8, d8, row, wrow, summ + c);
 }
 
 // The per-candidate table of a ragged batch (the RT_* fields) from the
@@ -474,7 +563,8 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
                 cudaStream_t st) {
     const int cs = dim_class(run.ns), cd = dim_class(run.nd);
     if (run.rg.runs) {
-        // a ragged batch: every instance at the reference's padded width, its plant from the table
+        // a ragged batch: every instance's plant and program from the table; the
+        // wide form runs each warp at the dimension class of its candidates
         if (precision == CE_PRECISION_FP64 || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
         if (run.rg.lanes == SW_LANES && !traj) {

@@ -214,8 +214,13 @@ class Ragged:
         _check(_lib().ce_ragged_get_tuning(self._h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
 
-    def set_tuning(self, sim_lanes: int = 0, instance_order: int = 0, eig_blocks_per_sm: int = 0):
-        t = _ffi.ce_ragged_tuning(sim_lanes, instance_order, eig_blocks_per_sm, 0.0)
+    def set_tuning(self, sim_lanes: int = 0, instance_order: int = 0, eig_blocks_per_sm: int = 0,
+                   sim_width: int = 0):
+        """Launch settings (none changes a result): sim_lanes 4 (the wide form) or 1; instance_order
+        0 (grouped by dimension class, program and horizon), 1 (the caller's order) or 2 (dealt by
+        horizon); eig_blocks_per_sm; sim_width 0 (each warp at its candidates' dimension class) or 8
+        (every candidate at the padded 8/8 width).  0 takes the default."""
+        t = _ffi.ce_ragged_tuning(sim_lanes, instance_order, eig_blocks_per_sm, sim_width, 0.0)
         _check(_lib().ce_ragged_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, d_cuda_mx: int, d_info_in: int, d_info_out: int, stream: int = 0) -> dict:

@@ -296,8 +296,11 @@ CE_EXPORT int ce_ragged_evaluate_device(ce_ragged* r, const float* d_cuda_mx, co
  * it keeps the fastest and returns it (with its time per evaluation). */
 typedef struct ce_ragged_tuning {
     int32_t sim_lanes;         /* lanes per candidate of the simulation: 4 (the wide form), 1, or 0: the default */
-    int32_t instance_order;    /* 0: candidates dealt to warps by decreasing horizon (default); 1: the caller's order */
+    int32_t instance_order;    /* device order of the candidates: 0 (default) grouped by dimension class, program
+                                  and decreasing horizon; 1: the caller's order; 2: dealt to warps by horizon tier */
     int32_t eig_blocks_per_sm; /* FP64 eigensolves: one-warp blocks per SM (0: the library default) */
+    int32_t sim_width;         /* the wide simulation's row count: 0 (default) each warp at the dimension class (4 or
+                                  8) of its candidates; 8: every candidate at the padded 8/8 width */
     double ms_per_evaluation;  /* ce_ragged_autotune: the chosen setting's time */
 } ce_ragged_tuning;
 CE_EXPORT int ce_ragged_set_tuning(ce_ragged* r, const ce_ragged_tuning* t);

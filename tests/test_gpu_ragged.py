@@ -138,3 +138,40 @@ def test_ragged_one_thread_form_equals_wide_form(tmp_path):
                        env={**os.environ, **env, "PYTHONPATH": root})
         res[form] = np.load(out)
     assert np.array_equal(_bits(res["wide"]), _bits(res["one"]))
+
+
+def _dims_of(seed):
+    rng = np.random.default_rng(seed)
+    return int(rng.integers(2, 9)), int(rng.integers(2, 9))
+
+
+def test_ragged_dimension_classes_with_diverging_loops():
+    """Warps of small plants run the 4-row steps with the padding beyond 4 virtual: rows equal the
+    instances' own sessions bit for bit, also for loops whose gains are scaled until the trajectory
+    overflows (the padded states of the reference then turn NaN and poison every row)."""
+    want = {(4, 4): 3, (4, 8): 1, (8, 4): 1, (8, 8): 1}
+    seeds = []
+    for seed in range(5000, 5400):
+        ns, nd = _dims_of(seed)
+        cls = (4 if ns <= 4 else 8, 4 if nd <= 4 else 8)
+        if want.get(cls, 0) > 0:
+            want[cls] -= 1
+            seeds.append(seed)
+    assert not any(want.values())
+    probs = []
+    for seed in seeds:
+        p = synth.random_shape(seed, n=48, time=1500, freq=60)
+        g = p.cuda_mx.copy()
+        ns = _dims_of(seed)[0]
+        g[::2, :2 * ns] *= np.float32(30.0)  # K and L of every other candidate
+        probs.append(synth.Problem(p.name, p.config_text, p.plant, g, p.info_mx))
+    cfgs = [ce.EngineConfig.parse(p.config_text) for p in probs]
+    with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
+        outs = rb.evaluate([(p.cuda_mx, p.info_mx) for p in probs])
+    unstable = 0
+    for c, p, o in zip(cfgs, probs, outs):
+        with ce.Session(c, p.plant) as s:
+            ref = s.evaluate(p.cuda_mx, p.info_mx)
+        assert np.array_equal(_bits(o), _bits(ref)), p.name
+        unstable += int((o[:, c.info_scoring + 1] >= c.unstable_err).sum())
+    assert unstable > 20, unstable

@@ -73,8 +73,9 @@ def test_ragged_tunings_and_autotune_keep_results():
     g, i = _packed(probs)
     with ce.Ragged([(c, p.plant) for c, p in zip(cfgs, probs)]) as rb:
         ref = rb.evaluate_packed(counts, g, i)
-        for t in ({"sim_lanes": 1}, {"instance_order": 1}, {"sim_lanes": 1, "instance_order": 1},
-                  {"eig_blocks_per_sm": 3}):
+        for t in ({"sim_lanes": 1}, {"instance_order": 1}, {"instance_order": 2}, {"sim_lanes": 1, "instance_order": 1},
+                  {"sim_lanes": 1, "instance_order": 2}, {"eig_blocks_per_sm": 3},
+                  {"sim_width": 8}, {"sim_width": 8, "instance_order": 2}):
             rb.set_tuning(**t)
             assert np.array_equal(_bits(rb.evaluate_packed(counts, g, i)), _bits(ref)), t
         rb.set_tuning()
@@ -84,7 +85,7 @@ def test_ragged_tunings_and_autotune_keep_results():
         rb.prepare(counts)
         best = rb.autotune(dg.data_ptr(), di.data_ptr(), do.data_ptr(),
                            stream=torch.cuda.current_stream().cuda_stream)
-        assert best["sim_lanes"] in (1, 4) and best["instance_order"] in (0, 1) and best["ms_per_evaluation"] > 0
+        assert best["sim_lanes"] in (1, 4) and best["instance_order"] in (0, 1, 2) and best["ms_per_evaluation"] > 0
         assert rb.tuning["sim_lanes"] == best["sim_lanes"]
         torch.cuda.synchronize()
         assert np.array_equal(_bits(do.cpu().numpy()), _bits(ref))
