@@ -69,46 +69,73 @@ __device__ __forceinline__ float rw_dot(const float* k, const float* hi, const f
     if (NC < MAXS) a = __fadd_rn(a, pad);
     return a;
 }
+// K.x and C.x together: two independent chains, each in its own order
+template <int NC>
+__device__ __forceinline__ void rw_dot2(const float* k, const float* c, const float* hi, const float* lo, float pad,
+                                        float& kx, float& cx) {
+    float a = 0.0f, b = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        a = __fmaf_rn(k[i], hi[i], a);
+        b = __fmaf_rn(c[i], hi[i], b);
+    }
+    if (NC < MAXS) {
+        a = __fadd_rn(a, pad);
+        b = __fadd_rn(b, pad);
+    }
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        a = __fmaf_rn(k[i], lo[i], a);
+        b = __fmaf_rn(c[i], lo[i], b);
+    }
+    if (NC < MAXS) {
+        a = __fadd_rn(a, pad);
+        b = __fadd_rn(b, pad);
+    }
+    kx = a;
+    cx = b;
+}
+// the lo-part sums of this lane's rows (sum_j M(i,j) x_lo[j], then the
+// padding term): independent of this step's inputs, formed ahead of them
+template <int NC, int MC>
+__device__ __forceinline__ void rw_lo(const float (*m)[MC], const float* lo, float pad, float* out) {
+#pragma unroll
+    for (int rr = 0; rr < NC / SW_LANES; ++rr) {
+        float l = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NC; ++j) l = __fmaf_rn(m[rr][j], lo[j], l);
+        if (NC < MC) l = __fadd_rn(l, pad);
+        out[rr] = l;
+    }
+}
 // this lane's observer rows: the increment (A-I)xh + B u + L yerr, then the
 // double-float add onto the row's old value (old_hi / old_lo in, new out)
 template <int NC>
 __device__ __forceinline__ void rw_obs(const float (*sai)[MAXS], const float* sb, const float* Lr, float u, float yerr,
-                                       const float* xh_hi, const float* xh_lo, float pad, float* nh, float* nlo) {
+                                       const float* xh_hi, const float* lsum, float pad, float* nh, float* nlo) {
 #pragma unroll
     for (int rr = 0; rr < NC / SW_LANES; ++rr) {
         float h = __fmaf_rn(Lr[rr], yerr, __fmul_rn(sb[rr], u));
-        float l = 0.0f;
 #pragma unroll
         for (int j = 0; j < NC; ++j) h = __fmaf_rn(sai[rr][j], xh_hi[j], h);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) l = __fmaf_rn(sai[rr][j], xh_lo[j], l);
-        if (NC < MAXS) {
-            h = __fadd_rn(h, pad);
-            l = __fadd_rn(l, pad);
-        }
-        df_add(nh[rr], nlo[rr], h, l);
+        if (NC < MAXS) h = __fadd_rn(h, pad);
+        df_add(nh[rr], nlo[rr], h, lsum[rr]);
     }
 }
 // this lane's plant rows: (Ad-I)xp + Bu u + Bw W, then the double-float add
 template <int NC>
 __device__ __forceinline__ void rw_plant(const float (*dai)[MAXD], const float (*dbw)[MAXW], const float* dbu,
-                                         float u, const float* W, const float* xp_hi, const float* xp_lo, float pad,
+                                         float u, const float* W, const float* xp_hi, const float* lsum, float pad,
                                          float* ph, float* plo) {
 #pragma unroll
     for (int rr = 0; rr < NC / SW_LANES; ++rr) {
         float h = __fmul_rn(dbu[rr], u);
 #pragma unroll
         for (int k = 0; k < MAXW; ++k) h = __fmaf_rn(dbw[rr][k], W[k], h);
-        float l = 0.0f;
 #pragma unroll
         for (int j = 0; j < NC; ++j) h = __fmaf_rn(dai[rr][j], xp_hi[j], h);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) l = __fmaf_rn(dai[rr][j], xp_lo[j], l);
-        if (NC < MAXD) {
-            h = __fadd_rn(h, pad);
-            l = __fadd_rn(l, pad);
-        }
-        df_add(ph[rr], plo[rr], h, l);
+        if (NC < MAXD) h = __fadd_rn(h, pad);
+        df_add(ph[rr], plo[rr], h, lsum[rr]);
     }
 }
 // a padded state turns NaN once a zero coefficient meets a non-finite operand
@@ -118,6 +145,41 @@ __device__ __forceinline__ bool rw_bad(const float* hi, const float* lo) {
 #pragma unroll
     for (int j = 0; j < NC; ++j) bad = bad || !isfinite(hi[j]) || !isfinite(lo[j]);
     return bad;
+}
+
+// The chain interpreter of the wide form.  Each slot forms add, subtract and
+// multiply as one fused multiply-add (a + b = fma(b, 1, a), a - b = fma(b, -1, a),
+// a b = fma(a, b, -0): each rounds once, exactly as the separate operation, -0
+// included), the saturation and the sign without branches, and the quotient
+// only in lanes whose slot divides.  Lanes interpreting different operations
+// (a quad's four NL chains) then execute one path instead of one per
+// operation.  Source column MAXD of the plant-side chains is the plant output
+// y, taken from a register (yv).
+template <bool HAS_SEED, int MAXC, bool YCOL>
+__device__ __forceinline__ float chain_sel(const float* __restrict__ t, int slot0, int n, const float* src, float yv,
+                                           float seed) {
+    float result = 0.0f;
+#pragma unroll
+    for (int r = 0; r < MAXC; ++r) {
+        if (r >= n) break;
+        const int f = RT_INS + 3 * (slot0 + r);
+        const unsigned code = __float_as_uint(t[f * WIDE_TS]);
+        const int op = (int)(code & 0xFFu), col = (int)((code >> 8) & 0xFFu);
+        const int ak = (int)((code >> 16) & 0xFFu), bk = (int)(code >> 24);
+        float pos = src[col];
+        if (YCOL && col == MAXD) pos = yv;
+        const float prev = r == 0 ? ((HAS_SEED && !isnan(seed)) ? seed : pos) : result;
+        const float a = ak == CE_OPERAND_CONST ? t[(f + 1) * WIDE_TS] : (ak == CE_OPERAND_STATE ? pos : prev);
+        const float b = bk == CE_OPERAND_CONST ? t[(f + 2) * WIDE_TS] : (bk == CE_OPERAND_STATE ? pos : prev);
+        const bool m = op == 3;
+        const float f3 = __fmaf_rn(m ? a : b, m ? b : (op == 1 ? 1.0f : -1.0f), m ? -0.0f : a);
+        const float sat = fmin(fmax(prev, a), b);
+        const float sg = (float)((0.0f < a) - (a < 0.0f));
+        float v = (op >= 1 && op <= 3) ? f3 : op == 5 ? sat : op == 6 ? sg : result;
+        if (op == 4) v = rdiv(a, b);
+        result = v;
+    }
+    return result;
 }
 
 // The quad's steps.  s8 / d8: the warp's observer / plant class is 8 rows
@@ -164,16 +226,32 @@ __device__ __forceinline__ void ragged_wide_steps(const Run& run, const float* t
     const int T = run.time, fit0 = run.fit_start_id, fitn = run.fit_steps, ss0 = run.steady_start_id,
               rstep = run.ref_step_id;
     const float ramp = run.ref_amp;
+    float y = 0.0f;  // the plant output of the previous step (a DC source column MAXD reads it)
     for (int tt = 0; tt < T; ++tt) {
         const float padS = poisS ? CUDART_NAN_F : 0.0f;
         const float padD = poisD ? CUDART_NAN_F : 0.0f;
+        // the sums that do not depend on this step's y, u or W first (independent
+        // chains the warp can overlap with the interpreted ones)
+        float sc[MAXS];  // C of the observer model, from the table (registers are short here)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_TS];
+        float kx, cx, lo_s[2], lo_d[2];
+        if (s8) {
+            rw_dot2<8>(K, sc, xh_hi, xh_lo, padS, kx, cx);
+            rw_lo<8, MAXS>(sai, xh_lo, padS, lo_s);
+        } else {
+            rw_dot2<4>(K, sc, xh_hi, xh_lo, padS, kx, cx);
+            rw_lo<4, MAXS>(sai, xh_lo, padS, lo_s);
+        }
+        if (d8) rw_lo<8, MAXD>(dai, xp_lo, padD, lo_d);
+        else rw_lo<4, MAXD>(dai, xp_lo, padD, lo_d);
         // plant output
-        const float y = run_chain_tab<false, MAX_DC, 1>(t, WIDE_TS, 0, n_dc, st + WS_XP_HI, 0.0f);
-        if (q == 0) {
-            st[WS_Y] = y;
-            // fit window, steady-state sum, extremes
+        y = chain_sel<false, MAX_DC, true>(t, 0, n_dc, st + WS_XP_HI, y, 0.0f);
+        // fit window (lane 0), steady-state sum and extremes (every lane keeps
+        // them, lane 0 stores them)
+        {
             const int w = tt - fit0;
-            if (w >= 0 && w < fitn) {
+            if (q == 0 && w >= 0 && w < fitn) {
                 stage[w & 7][cl] = y;
                 if ((w & 7) == 7 || w == fitn - 1 || tt == T - 1) {
                     float4 a, b;
@@ -189,35 +267,28 @@ __device__ __forceinline__ void ragged_wide_steps(const Run& run, const float* t
             ymin = fminf(ymin, y);
         }
         // controller output
-        const float kx = s8 ? rw_dot<8>(K, xh_hi, xh_lo, padS) : rw_dot<4>(K, xh_hi, xh_lo, padS);
         const float ref = tt < rstep ? 0.0f : ramp;
         const float u_raw = __fmaf_rn(N, ref, -kx);
-        const float u = run_chain_tab<true, MAX_U, 1>(t, WIDE_TS, MAX_DC, n_u, st + WS_XH_HI, u_raw);
+        const float u = chain_sel<true, MAX_U, false>(t, MAX_DC, n_u, st + WS_XH_HI, 0.0f, u_raw);
         // observer output error
-        float sc[MAXS];  // C of the observer model, from the table (registers are short here)
-#pragma unroll
-        for (int j = 0; j < MAXS; ++j) sc[j] = t[(RT_SC + j) * WIDE_TS];
-        float yh = s8 ? rw_dot<8>(sc, xh_hi, xh_lo, padS) : rw_dot<4>(sc, xh_hi, xh_lo, padS);
-        yh = __fmaf_rn(sd, u, yh);
+        const float yh = __fmaf_rn(sd, u, cx);
         const float yerr = __fsub_rn(y, yh);
+        // this lane's nonlinear term over [xp_hi, y]
+        st[WS_W + q] = chain_sel<false, MAX_NL, true>(t, MAX_DC + MAX_U + q * MAX_NL, n_nl, st + WS_XP_HI, y, 0.0f);
         // this lane's observer rows; the rows' old values from the slot (an index
         // by lane would put the state arrays in local memory); nothing writes the
-        // slot before the second barrier of the step
+        // slot's state before the barrier below
         float nh[2], nlo[2];
         nh[0] = st[WS_XH_HI + rs0];
         nlo[0] = st[WS_XH_LO + rs0];
         if (s8) {
             nh[1] = st[WS_XH_HI + rs0 + 1];
             nlo[1] = st[WS_XH_LO + rs0 + 1];
-            rw_obs<8>(sai, sb, Lr, u, yerr, xh_hi, xh_lo, padS, nh, nlo);
+            rw_obs<8>(sai, sb, Lr, u, yerr, xh_hi, lo_s, padS, nh, nlo);
         } else {
-            rw_obs<4>(sai, sb, Lr, u, yerr, xh_hi, xh_lo, padS, nh, nlo);
+            rw_obs<4>(sai, sb, Lr, u, yerr, xh_hi, lo_s, padS, nh, nlo);
             poisS = poisS || !isfinite(yerr) || !isfinite(u) || rw_bad<4>(xh_hi, xh_lo);
         }
-        __syncwarp(qm);  // y is in the slot
-        // this lane's nonlinear term over [xp_hi, y]
-        st[WS_W + q] = run_chain_tab<false, MAX_NL, 1>(t, WIDE_TS, MAX_DC + MAX_U + q * MAX_NL, n_nl,
-                                                        st + WS_XP_HI, 0.0f);
         __syncwarp(qm);  // every W is in the slot; every read of this step's state is done
         float W[MAXW], dbw[2][MAXW];  // Bw rows from the table (registers are short here)
 #pragma unroll
@@ -233,9 +304,9 @@ __device__ __forceinline__ void ragged_wide_steps(const Run& run, const float* t
         if (d8) {
             ph[1] = st[WS_XP_HI + rd0 + 1];
             plo[1] = st[WS_XP_LO + rd0 + 1];
-            rw_plant<8>(dai, dbw, dbu, u, W, xp_hi, xp_lo, padD, ph, plo);
+            rw_plant<8>(dai, dbw, dbu, u, W, xp_hi, lo_d, padD, ph, plo);
         } else {
-            rw_plant<4>(dai, dbw, dbu, u, W, xp_hi, xp_lo, padD, ph, plo);
+            rw_plant<4>(dai, dbw, dbu, u, W, xp_hi, lo_d, padD, ph, plo);
             bool bad = !isfinite(u);
 #pragma unroll
             for (int k = 0; k < MAXW; ++k) bad = bad || !isfinite(W[k]);
