@@ -45,11 +45,11 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ragged(const Run run, const _
 // four lanes of a quad, reading fields of their NL chains 24 fields apart, and
 // the warp's eight candidates, reading one field, fall on 32 different banks
 constexpr int WIDE_TS = SW_CPB + 1;  // SW_LANES lanes per candidate, SW_CPB candidates per block
-// slot layout: the NL chains read [xp_hi, y] as columns 0..MAXD; rows are
-// 16-byte aligned, and a stride of 52 words puts the 16-byte loads of a warp's
-// eight candidates on disjoint banks
-constexpr int WS_XH_HI = 0, WS_XH_LO = 8, WS_XP_HI = 16, WS_Y = WS_XP_HI + MAXD, WS_XP_LO = 28, WS_W = 36,
-              WS_STRIDE = 52;
+// slot layout: the plant-side chains read xp_hi as columns 0..MAXD-1 (their
+// column MAXD, y, comes from a register; word WS_XP_HI + MAXD is a zero pad);
+// rows are 16-byte aligned, and a stride of 52 words puts the 16-byte loads of
+// a warp's eight candidates on disjoint banks
+constexpr int WS_XH_HI = 0, WS_XH_LO = 8, WS_XP_HI = 16, WS_XP_LO = 28, WS_W = 36, WS_STRIDE = 52;
 static_assert(MAXS == 8 && MAXD == 8 && MAXW == SW_LANES, "the quad splits 8 rows and 4 NL chains");
 
 // The quad's row arithmetic at dimension class NC (4 or 8 rows): lane q owns
