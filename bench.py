@@ -80,12 +80,13 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
     normal matrix (the system the modal solve factors, from the FP64 form); then, binned by that
     condition number, the median relative error of wn, zeta and the behaviour error for the
     compensated and the mixed forms.  Error ~ condition x trajectory difference marks the FP32
-    trajectory as the floor."""
+    trajectory as the floor; beside them the compensated arithmetic on the FP64 trajectory and the
+    compensated_df form (the same arithmetic on a double-float trajectory)."""
     g, info = problem.cuda_mx[:sample], problem.info_mx[:sample]
     nt = cfg.total_dim
     out = {}
     prev = sess.precision
-    for form in ("fp64", "compensated", "mixed", "compensated_traj64"):
+    for form in ("fp64", "compensated", "mixed", "compensated_traj64", "compensated_df"):
         sess.set_precision(form)
         out[form] = sess.evaluate_diagnostics64(g, info, want=("ywin", "ata"))
     sess.set_precision(prev)
@@ -93,9 +94,11 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
     # the compensated form's arithmetic on the FP64 trajectory: what remains against the FP64 form
     # once the FP32 trajectory is taken out
     t64 = precision_report(out["compensated_traj64"][0], f64, cfg)
+    dfr, ddf_ = out["compensated_df"]
     s, fr, md = cfg.info_scoring, cfg.info_freqresp, cfg.info_modal
     yscale = np.maximum(np.abs(d64["ywin"]).max(axis=1), 1e-30)
     traj = np.abs(dc["ywin"] - d64["ywin"]).max(axis=1) / yscale
+    traj_df = np.abs(ddf_["ywin"] - d64["ywin"]).max(axis=1) / yscale
     uniq = f64[:, md + 3 * nt].astype(int)
     cond = np.full(len(g), np.inf)
     ata = d64["ata"].reshape(-1, 2 * nt, 2 * nt)
@@ -126,6 +129,9 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
             e = rel(out["compensated_traj64"][0], col)[sel]
             row[f"{name}_compensated_on_fp64_trajectory"] = float(np.median(e))
             row[f"{name}_compensated_on_fp64_trajectory_within_1e-6"] = float((e <= 1e-6).mean())
+            e = rel(dfr, col)[sel]
+            row[f"{name}_compensated_df"] = float(np.median(e))
+            row[f"{name}_compensated_df_within_1e-6"] = float((e <= 1e-6).mean())
         bins.append(row)
     # the same errors binned by the trajectory's own difference from the FP64 one
     tbins = []
@@ -141,6 +147,9 @@ def precision_floor(sess, problem, cfg, sample: int = 4096):
         tbins.append(row)
     return {"sample": int(len(g)), "trajectory_rel_diff": {"median": float(np.median(traj)),
                                                             "p99": float(np.quantile(traj, 0.99))},
+            "df_trajectory_rel_diff": {"median": float(np.median(traj_df)),
+                                       "p99": float(np.quantile(traj_df, 0.99))},
+            "compensated_df_vs_fp64": precision_report(dfr, f64, cfg),
             "by_condition": bins, "by_trajectory_difference": tbins,
             "compensated_on_fp64_trajectory_vs_fp64": t64}
 
@@ -964,6 +973,26 @@ def main():
         fp64["compensated"] = {"value": world * n / (c_ms * 1e-3), "unit": UNIT, "ms_per_step": c_ms,
                                "speedup_of_fp64_form": f_ms / c_ms, "stages_ms_per_step": c_stages,
                                "compensated_vs_fp64": precision_report(comp_rows, fp64_rows, cfg)}
+        # the compensated form with the double-float simulation, on the same batch
+        sess.set_precision("compensated_df")
+        step()
+        torch.cuda.synchronize()
+        df_rows = info_out.cpu().numpy()
+        sess.set_profiling(True)
+        e0.record(stream)
+        for _ in range(a.fp64_steps + 1):
+            flush.zero_()
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        d_stages = {k: v[0] / (a.fp64_steps + 1) for k, v in sess.stage_times().items()}
+        sess.set_profiling(False)
+        d_ms = e0.elapsed_time(e1) / (a.fp64_steps + 1)
+        fp64["compensated_df"] = {"value": world * n / (d_ms * 1e-3), "unit": UNIT, "ms_per_step": d_ms,
+                                  "speedup_of_fp64_form": f_ms / d_ms, "stages_ms_per_step": d_stages,
+                                  "compensated_df_vs_fp64": precision_report(df_rows, fp64_rows, cfg),
+                                  "what": "the compensated form with the simulation in double-float arithmetic "
+                                          "(pairs of FP32 values) instead of FP32"}
         sess.set_precision("mixed")
         if a.floor_sample > 0:
             fp64["precision_floor"] = precision_floor(sess, problem, cfg, a.floor_sample)

@@ -21,6 +21,7 @@ PRECISION_MIXED = 0
 PRECISION_FP64 = 1
 PRECISION_COMPENSATED = 2
 PRECISION_COMPENSATED_TRAJ64 = 3
+PRECISION_COMPENSATED_DF = 4
 EIG_ARITH_SEPARATE = 0
 EIG_ARITH_FUSED = 1
 

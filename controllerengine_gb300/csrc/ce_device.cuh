@@ -47,9 +47,91 @@ __device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 
+// ---- double-float numbers: an unevaluated sum hi + lo of two floats ---------
+// (|lo| <= half an ulp of hi), about 48 significant bits on the FP32 pipe.
+// The operations are the classical error-free transformations (Knuth's
+// TwoSum, Dekker's Fast2Sum, the fused-multiply-add TwoProduct) composed into
+// the usual double-double add, multiply and divide; each result is within a
+// few units of 2^-48 relative.  Used by the simulation of the compensated_df
+// precision, where FP32 products would bound the trajectory at ~1e-7.
+// The type and its operations live in namespace dd and are found by
+// argument-dependent lookup, so they never hide the float and double
+// overloads (fmax, radd, ...) that code in this namespace calls.
+namespace dd {
+struct ddf {
+    float hi, lo;
+    ddf() = default;
+    __device__ __forceinline__ constexpr ddf(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ constexpr ddf(float h) : hi(h), lo(0.0f) {}
+    __device__ __forceinline__ constexpr ddf(int h) : hi((float)h), lo(0.0f) {}
+    __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ ddf dd_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return ddf(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ ddf dd_fast_sum(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return ddf(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+// A sum or product that overflows (or meets an infinity or NaN) is returned as
+// (hi, 0) with hi the plain float result, as a double would be inf or NaN.
+__device__ __forceinline__ ddf radd(ddf x, ddf y) {
+    const ddf s = dd_two_sum(x.hi, y.hi), t = dd_two_sum(x.lo, y.lo);
+    if (!isfinite(s.hi)) return ddf(s.hi, 0.0f);
+    ddf r = dd_fast_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    r = dd_fast_sum(r.hi, __fadd_rn(r.lo, t.lo));
+    return isfinite(r.hi) ? r : ddf(r.hi, 0.0f);
+}
+__device__ __forceinline__ ddf rneg(ddf x) { return ddf(-x.hi, -x.lo); }
+__device__ __forceinline__ ddf rsub(ddf x, ddf y) { return radd(x, rneg(y)); }
+__device__ __forceinline__ ddf rmul(ddf x, ddf y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    if (!isfinite(p)) return ddf(p, 0.0f);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return dd_fast_sum(p, e);
+}
+// a float coefficient times a double-float: the exact product of a and hi plus a lo
+__device__ __forceinline__ ddf rmul(float a, ddf y) {
+    const float p = __fmul_rn(a, y.hi);
+    if (!isfinite(p)) return ddf(p, 0.0f);
+    return dd_fast_sum(p, __fmaf_rn(a, y.lo, __fmaf_rn(a, y.hi, -p)));
+}
+__device__ __forceinline__ ddf rdiv(ddf x, ddf y) {
+    // long division: three float quotient digits, each remainder formed in double-float
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    if (!isfinite(q1) || q1 == 0.0f) return ddf(q1, 0.0f);
+    ddf r = rsub(x, rmul(q1, y));
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    r = rsub(r, rmul(q2, y));
+    const float q3 = __fdiv_rn(r.hi, y.hi);
+    const ddf q = dd_fast_sum(q1, q2);
+    return radd(q, ddf(q3));
+}
+__device__ __forceinline__ ddf rfma(ddf a, ddf b, ddf c) { return radd(rmul(a, b), c); }
+__device__ __forceinline__ ddf rfma(float a, ddf b, ddf c) { return radd(rmul(a, b), c); }
+__device__ __forceinline__ bool operator<(ddf a, ddf b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(ddf a, ddf b) { return b < a; }
+// (a self-comparison: inside this namespace the name isnan would find this
+// overload again, not the float one)
+__device__ __forceinline__ bool isnan(ddf a) { return a.hi != a.hi || a.lo != a.lo; }
+__device__ __forceinline__ ddf fmax(ddf a, ddf b) { return isnan(a) ? b : isnan(b) ? a : a < b ? b : a; }
+__device__ __forceinline__ ddf fmin(ddf a, ddf b) { return isnan(a) ? b : isnan(b) ? a : b < a ? b : a; }
+}  // namespace dd
+using dd::ddf;
+__device__ __forceinline__ double rfma(float a, double b, double c) { return __fma_rn((double)a, b, c); }
+__device__ __forceinline__ double rmul(float a, double b) { return __dmul_rn((double)a, b); }
+__device__ __forceinline__ double rneg(double x) { return -x; }
+
 template <typename R> __device__ __forceinline__ R rnan();
 template <> __device__ __forceinline__ float rnan<float>() { return CUDART_NAN_F; }
 template <> __device__ __forceinline__ double rnan<double>() { return CUDART_NAN; }
+template <> __device__ __forceinline__ ddf rnan<ddf>() { return ddf(CUDART_NAN_F, CUDART_NAN_F); }
+template <typename R> __device__ __forceinline__ R rinf();
+template <> __device__ __forceinline__ double rinf<double>() { return CUDART_INF; }
+template <> __device__ __forceinline__ ddf rinf<ddf>() { return ddf(CUDART_INF_F, 0.0f); }
 
 // ---- double-float accumulation (ref: src/main.cu:129-155) --------------------
 // TwoSum of a and b.

@@ -211,17 +211,24 @@ struct BufElems {
 BufElems buf_elems(int precision) {
     if (precision == CE_PRECISION_FP64) return {8, 8, 8, 8, 8, 8};
     if (precision == CE_PRECISION_COMPENSATED) return {4, 4, 8, 8, 8, 8};
-    if (precision == CE_PRECISION_COMPENSATED_TRAJ64) return {8, 8, 8, 8, 8, 8};
+    if (precision == CE_PRECISION_COMPENSATED_TRAJ64 || precision == CE_PRECISION_COMPENSATED_DF)
+        return {8, 8, 8, 8, 8, 8};
     return {4, 4, 4, 4, 4, 4};
 }
 // The arithmetic each stage runs in under a session precision: the compensated
-// form simulates in FP32 (the mixed kernels) and runs LIN_A, the eigensolves and
-// the sweep in FP64 (the FP64 form's kernels).
-bool compensated(int prec) { return prec == CE_PRECISION_COMPENSATED || prec == CE_PRECISION_COMPENSATED_TRAJ64; }
+// form simulates in FP32 (the mixed kernels), compensated_df in double-float,
+// and both run LIN_A, the eigensolves and the sweep in FP64 (the FP64 form's
+// kernels).
+bool compensated(int prec) {
+    return prec == CE_PRECISION_COMPENSATED || prec == CE_PRECISION_COMPENSATED_TRAJ64 ||
+           prec == CE_PRECISION_COMPENSATED_DF;
+}
 int sim_precision(int prec) {
     return prec == CE_PRECISION_COMPENSATED ? CE_PRECISION_MIXED
            : prec == CE_PRECISION_COMPENSATED_TRAJ64 ? CE_PRECISION_FP64 : prec;
 }
+// the simulation writes a double trajectory (the FP64 and double-float recurrences)
+bool sim_double(int prec) { return sim_precision(prec) != CE_PRECISION_MIXED; }
 int eig_precision(int prec) { return compensated(prec) ? CE_PRECISION_FP64 : prec; }
 bool grids64(int prec) { return prec != CE_PRECISION_MIXED; }
 
@@ -551,7 +558,7 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
         const void* summ = at(b.summ, off, 4 * be.summ);
         timed(2, fs, [&] {
             if (compensated(prec))
-                launch_fit_comp(rc, prec == CE_PRECISION_COMPENSATED_TRAJ64, eig, ywin, summ, ata, atb,
+                launch_fit_comp(rc, sim_double(prec), eig, ywin, summ, ata, atb,
                                 d_info + off * iw, b.fit_counts + (MAXT + 1) * k, b.fit_order + (MAXT + 1) * off,
                                 fs);
             else
@@ -1706,9 +1713,9 @@ CE_EXPORT int ce_session_set_precision(ce_session* s, int32_t precision) {
     return guarded([&] {
         if (!s) fail("null session");
         if (precision != CE_PRECISION_MIXED && precision != CE_PRECISION_FP64 && precision != CE_PRECISION_COMPENSATED &&
-            precision != CE_PRECISION_COMPENSATED_TRAJ64)
+            precision != CE_PRECISION_COMPENSATED_TRAJ64 && precision != CE_PRECISION_COMPENSATED_DF)
             fail("unknown precision {}", precision);
-        if (sim_precision(precision) == CE_PRECISION_FP64 && s->cfg.observer == CE_OBSERVER_KALMAN)
+        if (sim_precision(precision) != CE_PRECISION_MIXED && s->cfg.observer == CE_OBSERVER_KALMAN)
             fail("the Kalman observer (observer = kalman) simulates in FP32 only (mixed or compensated precision)");
         s->precision = precision;
     });

@@ -434,8 +434,9 @@ __device__ __forceinline__ cplx<double> geo_sum(double x, double y, double t0, d
 constexpr int FC_ANCHOR = 256;  // window steps between FP64 re-anchorings of the projection recurrence
 
 // YT: the trajectory's type -- float (the FP32 simulation), or double (the
-// FP64 simulation, CE_PRECISION_COMPENSATED_TRAJ64: each sample split into
-// two floats, hi + lo, both projected).
+// FP64 simulation of CE_PRECISION_COMPENSATED_TRAJ64 or the double-float one of
+// CE_PRECISION_COMPENSATED_DF: each sample split into two floats, hi + lo,
+// both projected).
 template <typename YT>
 __global__ void __launch_bounds__(FIT_BLOCK) k_fit_comp(const Run run, const double* __restrict__ eig,
                                                        const YT* __restrict__ ywin, const void* __restrict__ summ,
@@ -914,7 +915,8 @@ void launch_fit(const Run& run, int precision, const void* eig, const void* ywin
 void launch_modal(const Run& run, int precision, const void* eig, const void* ata, const void* atb, float* info,
                   cudaStream_t st) {
     const int grid = (int)((run.n + MODAL_WARPS - 1) / MODAL_WARPS);
-    if (precision == CE_PRECISION_COMPENSATED || precision == CE_PRECISION_COMPENSATED_TRAJ64) {
+    if (precision == CE_PRECISION_COMPENSATED || precision == CE_PRECISION_COMPENSATED_TRAJ64 ||
+        precision == CE_PRECISION_COMPENSATED_DF) {
         prefer_shared((const void*)k_modal<double, false, true>);
         k_modal<double, false, true><<<grid, 32 * MODAL_WARPS, 0, st>>>(run, (const double*)eig, (const double*)ata,
                                                                        (const double*)atb, info);

@@ -3,8 +3,9 @@
 // k_sim_mixed: the step loop of ce_sim_body.cuh with the instruction tables
 // interpreted (TableChains); it runs any program with no compile step.  A
 // session whose plant program has been compiled into straight-line code
-// (ce_jit.cpp) launches that kernel instead.  k_sim_fp64 is the plain FP64
-// form of the recurrence.
+// (ce_jit.cpp) launches that kernel instead.  k_sim_ext is the recurrence in
+// FP64 (the plain FP64 form) or in double-float arithmetic (the compensated_df
+// form).
 #include <cstdlib>
 
 #include "ce_sim_body.cuh"
@@ -507,92 +508,133 @@ struct F64Plant {
             cs = np;
         }
     }
-    __device__ __forceinline__ double ai(int i, int j) const {
-        return MC ? (double)col[(i * NDC + j) * SIM_BLOCK] : (double)P.d_ai[i * MAXD + j];
+    // the plant values, floats as stored
+    __device__ __forceinline__ float ai(int i, int j) const {
+        return MC ? col[(i * NDC + j) * SIM_BLOCK] : P.d_ai[i * MAXD + j];
     }
-    __device__ __forceinline__ double bu(int i) const { return MC ? (double)col[(F_BU + i) * SIM_BLOCK] : (double)P.d_bu[i]; }
-    __device__ __forceinline__ double bw(int i, int k) const {
-        return MC ? (double)col[(F_BW + i * MAXW + k) * SIM_BLOCK] : (double)P.d_bw[i * MAXW + k];
+    __device__ __forceinline__ float bu(int i) const { return MC ? col[(F_BU + i) * SIM_BLOCK] : P.d_bu[i]; }
+    __device__ __forceinline__ float bw(int i, int k) const {
+        return MC ? col[(F_BW + i * MAXW + k) * SIM_BLOCK] : P.d_bw[i * MAXW + k];
     }
     // the constants of the chain whose first instruction is constant slot slot0
     __device__ __forceinline__ const float* k(int slot0) const { return MC ? cst + (int64_t)2 * slot0 * cs : nullptr; }
 };
 
-// The plain FP64 form of the same recurrence: double state, no hi/lo split.
-template <int NSC, int NDC, bool MC = false>
-__global__ void __launch_bounds__(SIM_BLOCK) k_sim_fp64(const Run run, const __grid_constant__ Plant P,
-                                                        const float* __restrict__ gains, double* __restrict__ ywin,
-                                                        double* __restrict__ summ) {
+// The extended-precision forms of the same recurrence, one value per state (no
+// hi/lo split of the mixed form): R = double is the plain FP64 form; R = ddf
+// (double-float) the simulation of the compensated_df precision, the same
+// operations in double-float arithmetic on the FP32 pipe.  The float
+// coefficients enter exactly in both; the trajectory and the summaries are
+// written as doubles.
+template <typename R>
+__device__ __forceinline__ double as_double(R v) { return (double)v; }
+
+// The running sums of the recurrence (x + sum_k a_k v_k with float
+// coefficients a_k): for double one fused multiply-add per term, in order; for
+// double-float a compensated dot product (Ogita, Rump and Oishi's Dot2): the
+// float running sum s, each product's exact error and each addition's exact
+// error (TwoProduct, TwoSum) gathered in c, and s + c normalised once at the
+// end -- as accurate as double-float arithmetic per term, with one float
+// addition on the dependent chain per term instead of a full double-float add.
+template <typename R> struct Acc;
+template <> struct Acc<double> {
+    double v;
+    __device__ __forceinline__ explicit Acc(double x) : v(x) {}
+    __device__ __forceinline__ void add(float a, double x) { v = __fma_rn((double)a, x, v); }
+    __device__ __forceinline__ double get() const { return v; }
+};
+template <> struct Acc<ddf> {
+    float s, c;
+    __device__ __forceinline__ explicit Acc(ddf x) : s(x.hi), c(x.lo) {}
+    __device__ __forceinline__ void add(float a, ddf x) {
+        const float p = __fmul_rn(a, x.hi);
+        const float e = __fmaf_rn(a, x.lo, __fmaf_rn(a, x.hi, -p));
+        const ddf t = dd::dd_two_sum(s, p);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
+    __device__ __forceinline__ ddf get() const {
+        if (!isfinite(s)) return ddf(s, 0.0f);
+        const ddf r = dd::dd_fast_sum(s, c);
+        return isfinite(r.hi) ? r : ddf(r.hi, 0.0f);
+    }
+};
+
+template <typename R, int NSC, int NDC, bool MC = false>
+__global__ void __launch_bounds__(SIM_BLOCK) k_sim_ext(const Run run, const __grid_constant__ Plant P,
+                                                       const float* __restrict__ gains, double* __restrict__ ywin,
+                                                       double* __restrict__ summ) {
     const int tid = threadIdx.x;
     const int64_t c = (int64_t)blockIdx.x * SIM_BLOCK + tid;
     if (c >= run.n) return;
     const F64Plant<NDC, MC> pv(run, P, c);
     const int ns = run.ns;
     const float* row = gains + c * run.cuda_w;
-    double K[NSC], L[NSC];
+    float K[NSC], L[NSC];
 #pragma unroll
     for (int i = 0; i < NSC; ++i) {
-        K[i] = i < ns ? (double)row[i] : 0.0;
-        L[i] = i < ns ? (double)row[ns + i] : 0.0;
+        K[i] = i < ns ? row[i] : 0.0f;
+        L[i] = i < ns ? row[ns + i] : 0.0f;
     }
-    const double N = row[2 * ns];
-    double xh[NSC], xp[NDC];
+    const R N = R(row[2 * ns]);
+    R xh[NSC], xp[NDC];
 #pragma unroll
-    for (int i = 0; i < NSC; ++i) xh[i] = 0.0;
+    for (int i = 0; i < NSC; ++i) xh[i] = R(0);
 #pragma unroll
-    for (int i = 0; i < NDC; ++i) xp[i] = 0.0;
-    double ysum = 0.0, ymax = -CUDART_INF, ymin = CUDART_INF;
+    for (int i = 0; i < NDC; ++i) xp[i] = R(0);
+    R ysum = R(0), ymax = rneg(rinf<R>()), ymin = rinf<R>();
     double* wrow = ywin + c * (int64_t)run.fit_pitch;
     const int T = run.time;
     for (int t = 0; t < T; ++t) {
-        const double y = run_chain<double, NDC, MAX_DC, false, MC>(P.dc, P.n_dc, xp, -1, 0.0, 0.0, pv.k(0), pv.cs);
+        const R y = run_chain<R, NDC, MAX_DC, false, MC>(P.dc, P.n_dc, xp, -1, R(0), R(0), pv.k(0), pv.cs);
         const int w = t - run.fit_start_id;
-        if (w >= 0 && w < run.fit_steps) wrow[w] = y;
-        if (t >= run.steady_start_id) ysum = __dadd_rn(ysum, y);
+        if (w >= 0 && w < run.fit_steps) wrow[w] = as_double(y);
+        if (t >= run.steady_start_id) ysum = radd(ysum, y);
         ymax = fmax(ymax, y);
         ymin = fmin(ymin, y);
-        double kx = 0.0;
+        Acc<R> kx(R(0));
 #pragma unroll
-        for (int i = 0; i < NSC; ++i) kx = __fma_rn(K[i], xh[i], kx);
-        const double ref = t < run.ref_step_id ? 0.0 : (double)run.ref_amp;
-        const double u = run_chain<double, NSC, MAX_U, true, MC>(P.u, P.n_u, xh, -1, 0.0, __fma_rn(N, ref, -kx),
-                                                                  pv.k(MAX_DC), pv.cs);
-        double yh = 0.0;
+        for (int i = 0; i < NSC; ++i) kx.add(K[i], xh[i]);
+        const R ref = t < run.ref_step_id ? R(0) : R(run.ref_amp);
+        const R u = run_chain<R, NSC, MAX_U, true, MC>(P.u, P.n_u, xh, -1, R(0), rfma(N, ref, rneg(kx.get())),
+                                                        pv.k(MAX_DC), pv.cs);
+        Acc<R> yh(R(0));
 #pragma unroll
-        for (int i = 0; i < NSC; ++i) yh = __fma_rn((double)P.ss_c[i], xh[i], yh);
-        yh = __fma_rn((double)P.ss_d, u, yh);
-        const double yerr = __dsub_rn(y, yh);
-        double dh[NSC];
+        for (int i = 0; i < NSC; ++i) yh.add(P.ss_c[i], xh[i]);
+        yh.add(P.ss_d, u);
+        const R yerr = rsub(y, yh.get());
+        R dh[NSC];
 #pragma unroll
         for (int i = 0; i < NSC; ++i) {
-            double h = __fma_rn(L[i], yerr, __dmul_rn((double)P.ss_b[i], u));
+            Acc<R> h(rmul(P.ss_b[i], u));
+            h.add(L[i], yerr);
 #pragma unroll
-            for (int j = 0; j < NSC; ++j) h = __fma_rn((double)P.ss_ai[i * MAXS + j], xh[j], h);
-            dh[i] = h;
+            for (int j = 0; j < NSC; ++j) h.add(P.ss_ai[i * MAXS + j], xh[j]);
+            dh[i] = h.get();
         }
 #pragma unroll
-        for (int i = 0; i < NSC; ++i) xh[i] = __dadd_rn(xh[i], dh[i]);
-        double W[MAXW];
+        for (int i = 0; i < NSC; ++i) xh[i] = radd(xh[i], dh[i]);
+        R W[MAXW];
 #pragma unroll
         for (int k = 0; k < MAXW; ++k)
-            W[k] = run_chain<double, NDC, MAX_NL, false, MC>(P.nl[k], P.n_nl[k], xp, MAXD, y, 0.0,
-                                                             pv.k(MAX_DC + MAX_U + k * MAX_NL), pv.cs);
-        double ph[NDC];
+            W[k] = run_chain<R, NDC, MAX_NL, false, MC>(P.nl[k], P.n_nl[k], xp, MAXD, y, R(0),
+                                                        pv.k(MAX_DC + MAX_U + k * MAX_NL), pv.cs);
+        R ph[NDC];
 #pragma unroll
         for (int i = 0; i < NDC; ++i) {
-            double h = __dmul_rn(pv.bu(i), u);
+            Acc<R> h(rmul(pv.bu(i), u));
 #pragma unroll
-            for (int k = 0; k < MAXW; ++k) h = __fma_rn(pv.bw(i, k), W[k], h);
+            for (int k = 0; k < MAXW; ++k) h.add(pv.bw(i, k), W[k]);
 #pragma unroll
-            for (int j = 0; j < NDC; ++j) h = __fma_rn(pv.ai(i, j), xp[j], h);
-            ph[i] = h;
+            for (int j = 0; j < NDC; ++j) h.add(pv.ai(i, j), xp[j]);
+            ph[i] = h.get();
         }
 #pragma unroll
-        for (int i = 0; i < NDC; ++i) xp[i] = __dadd_rn(xp[i], ph[i]);
+        for (int i = 0; i < NDC; ++i) xp[i] = radd(xp[i], ph[i]);
     }
-    summ[4 * c + 0] = ysum;
-    summ[4 * c + 1] = ymax;
-    summ[4 * c + 2] = ymin;
+    summ[4 * c + 0] = as_double(ysum);
+    summ[4 * c + 1] = as_double(ymax);
+    summ[4 * c + 2] = as_double(ymin);
     summ[4 * c + 3] = 0.0;
 }
 
@@ -613,17 +655,23 @@ template <int NSC, int NDC, int KMODE = SIM_LUENBERGER>
 static void sim_launch(const Run& run, const Plant& P, int precision, const float* gains, void* ywin, void* summ,
                        float* traj, cudaStream_t st) {
     const int grid = sim_grid(run);
-    if (precision == CE_PRECISION_FP64) {
+    if (precision == CE_PRECISION_FP64 || precision == CE_PRECISION_COMPENSATED_DF) {
         if (KMODE != SIM_LUENBERGER) throw std::runtime_error("the Kalman observer runs in mixed precision only");
-        if (run.mc.tab) {
-            // per-candidate plants: each thread's plant matrices in its shared-memory column
-            const size_t cols = (size_t)F64Plant<NDC, true>::FIELDS * SIM_BLOCK * sizeof(float);
-            prefer_shared((const void*)k_sim_fp64<NSC, NDC, true>);
-            k_sim_fp64<NSC, NDC, true><<<grid, SIM_BLOCK, cols, st>>>(run, P, gains, (double*)ywin, (double*)summ);
-            return;
-        }
-        prefer_shared((const void*)k_sim_fp64<NSC, NDC>);
-        k_sim_fp64<NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
+        auto go = [&](auto r) {
+            using R = decltype(r);
+            if (run.mc.tab) {
+                // per-candidate plants: each thread's plant matrices in its shared-memory column
+                const size_t cols = (size_t)F64Plant<NDC, true>::FIELDS * SIM_BLOCK * sizeof(float);
+                prefer_shared((const void*)k_sim_ext<R, NSC, NDC, true>);
+                k_sim_ext<R, NSC, NDC, true><<<grid, SIM_BLOCK, cols, st>>>(run, P, gains, (double*)ywin,
+                                                                            (double*)summ);
+                return;
+            }
+            prefer_shared((const void*)k_sim_ext<R, NSC, NDC>);
+            k_sim_ext<R, NSC, NDC><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (double*)ywin, (double*)summ);
+        };
+        if (precision == CE_PRECISION_FP64) go(0.0);
+        else go(ddf(0.0f));
     } else {
         prefer_shared((const void*)k_sim_mixed<NSC, NDC, KMODE>);
         k_sim_mixed<NSC, NDC, KMODE><<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, (float*)ywin, (SimSummary*)summ, traj);
@@ -636,7 +684,7 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
     if (run.rg.runs) {
         // a ragged batch: every instance's plant and program from the table; the
         // wide form runs each warp at the dimension class of its candidates
-        if (precision == CE_PRECISION_FP64 || run.kalman)
+        if (precision != CE_PRECISION_MIXED || run.kalman)
             throw std::runtime_error("a ragged batch runs the Luenberger loop in mixed precision");
         if (run.rg.lanes == SW_LANES && !traj) {
             prefer_shared((const void*)k_sim_ragged_wide);

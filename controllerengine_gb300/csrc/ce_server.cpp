@@ -113,7 +113,7 @@ int64_t bytes_per_candidate(const ce_config& c, int precision) {
     const int64_t groups = (c.freq + SWEEP_FG - 1) / SWEEP_FG;
     // 4-byte words per real of each buffer: the simulation's (fit window, summary)
     // and the rest's (LIN_A, eigenvalues, normal equations, sweep scratch)
-    const int64_t sim = precision == CE_PRECISION_FP64 ? 2 : 1;
+    const int64_t sim = precision == CE_PRECISION_FP64 || precision == CE_PRECISION_COMPENSATED_DF ? 2 : 1;
     const int64_t real = precision == CE_PRECISION_MIXED ? 1 : 2;
     int64_t f = 0;
     f += 2 * (int64_t)c.cuda_mx_width + 2 * (int64_t)c.info_mx_width;  // gains + INFO, session and lane
@@ -343,7 +343,8 @@ void create_server(const ce_config* cfg, const ce_plant* plant, const int32_t* n
     if (opt) o = *opt;
     const int lanes = o.lanes > 0 ? o.lanes : 2;
     if (lanes > 8) fail("ce_server_create: at most 8 lanes, got {}", lanes);
-    if (o.precision != CE_PRECISION_MIXED && o.precision != CE_PRECISION_FP64 && o.precision != CE_PRECISION_COMPENSATED)
+    if (o.precision != CE_PRECISION_MIXED && o.precision != CE_PRECISION_FP64 && o.precision != CE_PRECISION_COMPENSATED &&
+        o.precision != CE_PRECISION_COMPENSATED_DF)
         fail("ce_server_create: unknown precision {}", o.precision);
     int64_t cap = o.max_batch > 0 ? o.max_batch : 65536;
     // every lane may hold a full batch's scratch for every model

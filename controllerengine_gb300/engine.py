@@ -291,7 +291,8 @@ class Session:
     def set_precision(self, precision: str):
         code = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
                 "compensated": _ffi.PRECISION_COMPENSATED,
-                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64}[precision]
+                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64,
+                "compensated_df": _ffi.PRECISION_COMPENSATED_DF}[precision]
         _check(_lib().ce_session_set_precision(self._h, code))
         self.precision = precision
 
@@ -474,7 +475,8 @@ class Server:
         self._h = C.c_void_p()
         prec = {"mixed": _ffi.PRECISION_MIXED, "fp64": _ffi.PRECISION_FP64,
                 "compensated": _ffi.PRECISION_COMPENSATED,
-                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64}[precision]
+                "compensated_traj64": _ffi.PRECISION_COMPENSATED_TRAJ64,
+                "compensated_df": _ffi.PRECISION_COMPENSATED_DF}[precision]
         opt = _ffi.ce_server_options(max_batch, lanes, hbm_budget_bytes, max_wait_us, prec, max_batch_work)
         k = len(models)
         cfgs = (_ffi.ce_config * k)(*[m[0].raw for m in models])

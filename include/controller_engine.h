@@ -64,6 +64,10 @@ extern "C" {
  * trajectory.  Against the FP64 form it isolates how much of the compensated form's difference
  * is the FP32 trajectory's own. */
 #define CE_PRECISION_COMPENSATED_TRAJ64 3
+/* The compensated form with the simulation in double-float arithmetic (pairs of FP32 values, about
+ * 48 significant bits, on the FP32 pipe) instead of the FP32 recurrence: the trajectory then agrees
+ * with the FP64 form's to ~1e-12 rather than ~1e-7, and the rest is the compensated form's. */
+#define CE_PRECISION_COMPENSATED_DF 4
 
 /*
  * Parsed ControllerEngine.config plus the sizes derived from it.
@@ -419,7 +423,7 @@ typedef struct ce_server_options {
     int32_t lanes;            /* concurrent batches (0: 2, at most 8) */
     int64_t hbm_budget_bytes; /* device memory for all lanes (0: no limit); capacity shrinks to fit */
     int32_t max_wait_us;      /* a partial batch waits up to this long for more requests (0: none) */
-    int32_t precision;        /* CE_PRECISION_MIXED (0, the default), _FP64 or _COMPENSATED for every lane */
+    int32_t precision;        /* CE_PRECISION_MIXED (0, the default), _FP64, _COMPENSATED or _COMPENSATED_DF for every lane */
     int64_t max_batch_work;   /* candidate-steps (candidates x horizon) per batch (0: no cap); a request
                                  above it is served in pieces on several lanes at once */
 } ce_server_options;
