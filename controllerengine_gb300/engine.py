@@ -484,22 +484,33 @@ class Server:
         nps = (C.c_int32 * k)(*[m[2] for m in models])
         _check(_lib().ce_server_create_models(cfgs, pls, nps, k, C.byref(opt), C.byref(self._h)))
 
+    @staticmethod
+    def _out(out, i):
+        """The result buffer: the caller's (C-contiguous float32, the INFO rows' shape), or a new one.
+        A caller serving many requests passes buffers it reuses, so the result copy does not fault
+        in fresh pages."""
+        if out is None:
+            return np.empty_like(i)
+        if out.dtype != F32 or out.shape != i.shape or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 array shaped like the INFO rows")
+        return out
+
     def submit(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, plant_index: int = 0,
-               model: int = 0) -> Request:
+               model: int = 0, out: np.ndarray | None = None) -> Request:
         c = self.configs[model]
         g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
         n = g.shape[0]
         if info_in is None:
             info_in = np.zeros((n, c.info_mx_width), F32)
         i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
-        out = np.empty_like(i)
+        out = self._out(out, i)
         rid = C.c_int64()
         _check(_lib().ce_server_submit_model(self._h, model, plant_index, n, _fptr(g), _fptr(i), _fptr(out),
                                              C.byref(rid)))
         return Request(self, rid.value, g, i, out)
 
     def submit_plants(self, cuda_mx: np.ndarray, info_in: np.ndarray | None = None, first_plant: int = 0,
-                      model: int = 0) -> Request:
+                      model: int = 0, out: np.ndarray | None = None) -> Request:
         """A Monte Carlo request: row k on plant first_plant + k (ce_server_submit_plants)."""
         c = self.configs[model]
         g = np.ascontiguousarray(cuda_mx, dtype=F32).reshape(-1, c.cuda_mx_width)
@@ -507,7 +518,7 @@ class Server:
         if info_in is None:
             info_in = np.zeros((n, c.info_mx_width), F32)
         i = np.ascontiguousarray(info_in, dtype=F32).reshape(n, c.info_mx_width)
-        out = np.empty_like(i)
+        out = self._out(out, i)
         rid = C.c_int64()
         _check(_lib().ce_server_submit_plants(self._h, model, first_plant, n, _fptr(g), _fptr(i), _fptr(out),
                                               C.byref(rid)))

@@ -162,6 +162,18 @@ def test_fp64_server_equals_fp64_session(mass_spring):
     assert not np.array_equal(_bits(got), _bits(mixed))
 
 
+@pytest.mark.parametrize("precision", ["compensated", "compensated_df"])
+def test_compensated_servers_equal_their_sessions(mass_spring, precision):
+    """A server created with a compensated form runs it in every lane; rows equal a session's."""
+    p = mass_spring
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant, precision=precision) as s:
+        ref = s.evaluate(p.cuda_mx, p.info_mx)
+    with ce.Server(cfg, p.plant, max_batch=700, lanes=2, precision=precision) as srv:
+        got = np.vstack([srv.submit(p.cuda_mx[a:a + 512], p.info_mx[a:a + 512]).wait() for a in range(0, 1536, 512)])
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
 def test_monte_carlo_requests_batch_with_each_other():
     """Monte Carlo requests (row k on plant first + k) of assorted plant ranges are packed into
     the same batches, between ordinary requests on one plant; every row equals ce_evaluate_plants
