@@ -65,7 +65,8 @@ struct Buffers {
         for (void* p : {(void*)gains, (void*)info, (void*)lina, eig, ywin, summ, ata, atb, (void*)nominal,
                         (void*)fit_counts, (void*)fit_order, (void*)nominal_list, (void*)nominal_count,
                         (void*)sweep_list, (void*)sweep_count, sweep.mag, sweep.arg, sweep.bpc, (void*)sweep.fail,
-                        (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order, (void*)plant_idx})
+                        (void*)traj, (void*)kal.bucket, (void*)kal.cnt, (void*)kal.order, (void*)kal.sched,
+                        (void*)kal.meta, (void*)kal.lists, (void*)plant_idx})
             if (p) cudaFree(p);
         gains = info = traj = nullptr;
         lina = eig = ywin = summ = ata = atb = nullptr;
@@ -111,11 +112,13 @@ struct ce_session {
     // priority); side: the FP64 eigensolves (highest priority)
     cudaStream_t stream = nullptr, fast = nullptr, side = nullptr;
     cudaStream_t side2 = nullptr;  // the nominal eigensolve of a small batch, beside LIN_A's
+    cudaStream_t side3 = nullptr;  // Kalman: the quad form's stragglers, beside the scheduled form
     // the latency forms of a small batch (wide simulation, more lanes per matrix in the FP64
     // eigensolves, the nominal eigensolve beside LIN_A's); a server's sessions run without them
     bool small_forms = true;
     int eig_arith = CE_EIG_ARITH_FUSED;  // arithmetic of the FP64 eigensolves
     cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_kal = nullptr, ev_kal_quad = nullptr;  // Kalman: schedules ready; quad form done
     cudaEvent_t ev_eig[ce::MAX_CHUNKS] = {}, ev_nom[ce::MAX_CHUNKS] = {};
     int64_t launches = 0;
     int device = 0;
@@ -266,12 +269,15 @@ void ensure_buffers(ce_session* s, int64_t n, bool traj) {
         if (c.observer == CE_OBSERVER_KALMAN) {
             // one block: cnt | fill | totals (cleared together) | hoff | poff
             dev_alloc(b.kal.bucket, (size_t)cap);
-            dev_alloc(b.kal.cnt, (size_t)4 * KAL_BUCKETS + 4);
+            dev_alloc(b.kal.cnt, (size_t)4 * KAL_BUCKETS + KAL_TOTALS);
             b.kal.fill = b.kal.cnt + KAL_BUCKETS;
             b.kal.totals = b.kal.fill + KAL_BUCKETS;
-            b.kal.hoff = b.kal.totals + 4;
+            b.kal.hoff = b.kal.totals + KAL_TOTALS;
             b.kal.poff = b.kal.hoff + KAL_BUCKETS;
             dev_alloc(b.kal.order, (size_t)kal_order_size(cap));
+            dev_alloc(b.kal.sched, (size_t)KAL_SCHED_STEPS * MAXS * cap);
+            dev_alloc(b.kal.meta, (size_t)cap);
+            dev_alloc(b.kal.lists, (size_t)2 * cap);
         }
         b.cap = cap;
         b.nt = nt;
@@ -526,16 +532,33 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
             rh.kal_order = b.kal.order;
             rh.kal_totals = b.kal.totals;
             rh.kal_defer = kal_shared_slots(n) + n;
+            rh.kal_sched = b.kal.sched;
+            rh.kal_meta = b.kal.meta;
+            rh.kal_lists = b.kal.lists;
+            rh.kal_sched_n = b.cap;
             rh.kal_list = 1;
-            Run rp = rh;
+            // the per-candidate list: gain schedules, then the scheduled form over the
+            // positions whose schedule turned periodic and, on a third stream beside
+            // it, the quad form over the rest (the two lists are disjoint)
+            Run rp = rh, ra = rh, rb = rh;
             rp.kal_list = 2;
+            ra.kal_list = 3;
+            rb.kal_list = 4;
+            cudaStream_t qs = s->side3;
+            if (sk) launch_sim_specialised(sk.shared, rh, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+            else launch_sim(rh, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
+            launch_kalman_schedule(rp, P, d_gains, b.kal, fs);
+            CE_CUDA(cudaEventRecord(s->ev_kal, fs));
+            CE_CUDA(cudaStreamWaitEvent(qs, s->ev_kal, 0));
             if (sk) {
-                launch_sim_specialised(sk.shared, rh, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
-                launch_sim_specialised(sk.main, rp, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
+                launch_sim_specialised(sk.quad, rb, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, qs);
+                launch_sim_specialised(sk.sched, ra, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
             } else {
-                launch_sim(rh, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
-                launch_sim(rp, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
+                launch_sim(rb, P, sprec, d_gains, b.ywin, b.summ, tr, qs);
+                launch_sim(ra, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
             }
+            CE_CUDA(cudaEventRecord(s->ev_kal_quad, qs));
+            CE_CUDA(cudaStreamWaitEvent(fs, s->ev_kal_quad, 0));
         } else if (sk) {
             // a batch too small to fill the GPU runs four lanes per candidate
             const bool wide = s->small_forms && sk.wide &&
@@ -579,7 +602,8 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
     }
     CE_CUDA(cudaEventRecord(s->ev_done, fs));
     CE_CUDA(cudaStreamWaitEvent(st, s->ev_done, 0));
-    s->launches += 1 + 8 * nch + (r.kalman ? 4 : 0);  // Kalman: three grouping kernels and a second simulation form
+    // Kalman: three grouping kernels, the gain schedules and two more simulation forms
+    s->launches += 1 + 8 * nch + (r.kalman ? 6 : 0);
 }
 
 std::vector<Instr> compact(const std::vector<ce_instruction>& rows) {
@@ -789,8 +813,11 @@ void init_streams(ce_session* s) {
     CE_CUDA(cudaStreamCreateWithPriority(&s->fast, cudaStreamNonBlocking, prio_least));
     CE_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_greatest));
     CE_CUDA(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, prio_greatest));
+    CE_CUDA(cudaStreamCreateWithPriority(&s->side3, cudaStreamNonBlocking, prio_least));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_kal, cudaEventDisableTiming));
+    CE_CUDA(cudaEventCreateWithFlags(&s->ev_kal_quad, cudaEventDisableTiming));
     for (int k = 0; k < MAX_CHUNKS; ++k) {
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_eig[k], cudaEventDisableTiming));
         CE_CUDA(cudaEventCreateWithFlags(&s->ev_nom[k], cudaEventDisableTiming));
@@ -855,6 +882,8 @@ void destroy_session(ce_session* s) {
     if (s->d_alpha64) cudaFree(s->d_alpha64);
     if (s->d_mc_tab) cudaFree(s->d_mc_tab);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_kal) cudaEventDestroy(s->ev_kal);
+    if (s->ev_kal_quad) cudaEventDestroy(s->ev_kal_quad);
     for (int k = 0; k < MAX_CHUNKS; ++k) {
         if (s->ev_eig[k]) cudaEventDestroy(s->ev_eig[k]);
         if (s->ev_nom[k]) cudaEventDestroy(s->ev_nom[k]);
@@ -862,6 +891,7 @@ void destroy_session(ce_session* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->side2) cudaStreamDestroy(s->side2);
+    if (s->side3) cudaStreamDestroy(s->side3);
     if (s->fast) cudaStreamDestroy(s->fast);
     if (s->ev_done) cudaEventDestroy(s->ev_done);
     delete s;

@@ -102,6 +102,8 @@ double measure_fma_rate(bool fp64);
 struct SimKernels {
     const void* main = nullptr;
     const void* shared = nullptr;
+    const void* sched = nullptr;  // Kalman: the gains from the candidate's schedule
+    const void* quad = nullptr;   // Kalman: the covariance split over four lanes
     const void* wide = nullptr;  // four lanes per candidate (Luenberger, one plant)
     explicit operator bool() const { return main != nullptr; }
 };
@@ -144,11 +146,30 @@ struct KalGroups {
     int* fill = nullptr;         // KAL_BUCKETS: scatter counters
     int* hoff = nullptr;         // KAL_BUCKETS: offset in the shared list
     int* poff = nullptr;         // KAL_BUCKETS: offset in the per-candidate list
-    int* totals = nullptr;       // 4: shared slots, per-candidate count, deferred count
+    int* totals = nullptr;       // KAL_TOTALS: shared slots, per-candidate count, deferred count,
+                                 // scheduled count, straggler count
     int* order = nullptr;        // kal_order_size(n)
+    // the per-candidate list's gain schedules (k_kal_schedule): the gains of the
+    // first KAL_SCHED_STEPS steps, [step][gain][list position]; per position
+    // (t0, p) -- the gains repeat with period p from step t0, or t0 = -1; and the
+    // positions whose schedule is periodic, then those whose is not
+    float* sched = nullptr;      // KAL_SCHED_STEPS * MAXS * n
+    int2* meta = nullptr;        // n
+    int* lists = nullptr;        // 2n: scheduled positions at [0, n), stragglers at [n, 2n)
 };
+constexpr int KAL_TOTALS = 8;
+// Steps of covariance recursion a candidate of the per-candidate list gets to
+// turn periodic (bit for bit); 87% of the distinct-noise eight-state batch do
+// within 2,048 steps (79% within 1,024), the rest run the recursion in full.
+constexpr int KAL_SCHED_STEPS = 2048;
 // Fills g.order / g.totals for the n candidates of `run` (4 launches incl. a memset).
 void launch_kalman_groups(const Run& run, const float* gains, const KalGroups& g, cudaStream_t st);
+// The gain schedules of the per-candidate list (`run` with kal_list = 2; one launch): each
+// position's recursion for up to min(time, KAL_SCHED_STEPS) steps, stopping once periodic; the
+// periodic positions go to g.lists[0, ...) (count totals[3]), the others to g.lists[n, ...)
+// (count totals[4]).
+void launch_kalman_schedule(const Run& run, const Plant& P, const float* gains, const KalGroups& g,
+                            cudaStream_t st);
 
 const Plant* session_plant(const ce_session* s, int plant);
 const ce_config* session_config(const ce_session* s);

@@ -129,11 +129,17 @@ struct Run {
     // Kalman candidate lists (kal_list 0: thread i simulates candidate i).  1: the
     // shared-noise list kal_order[0, kal_totals[0]) in whole warps (-1: padding);
     // 2: the per-candidate list kal_order[kal_totals[0], + kal_totals[1]), then
-    // the kal_totals[2] candidates deferred by the shared form at kal_order[kal_defer]
+    // the kal_totals[2] candidates deferred by the shared form at kal_order[kal_defer];
+    // 3: the positions of list 2 whose gain schedule turned periodic,
+    // kal_lists[0, kal_totals[3]); 4: the others, kal_lists[n, + kal_totals[4])
     int kal_list;
     int* kal_order;
     int* kal_totals;
     int64_t kal_defer;
+    const float* kal_sched;  // the gain schedules ([step][gain][position], stride kal_sched_n)
+    const int2* kal_meta;    // per position: (t0, p), the gains repeat with period p from step t0
+    const int* kal_lists;
+    int64_t kal_sched_n;     // positions per schedule row (the buffers' capacity)
     McPlants mc;     // per-candidate plants (mc.tab == null: the Plant for all)
     int eig_lanes;   // FP64 eigensolves: lanes per matrix (1, 2, 4, 8 or 16; 0: by batch size)
     int eig_blocks;  // FP64 eigensolves: one-warp blocks per SM (0: the default)

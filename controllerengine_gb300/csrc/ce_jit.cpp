@@ -115,6 +115,8 @@ std::string jit_source(const Plant& P, int ns, int nd, bool mc, bool kalman) {
     if (kalman) {
         kernel("ce_sim_specialised", MAXS, "ce::SIM_KALMAN_LANE");
         kernel("ce_sim_kalman_shared", MAXS, "ce::SIM_KALMAN_SHARED");
+        kernel("ce_sim_kalman_sched", MAXS, "ce::SIM_KALMAN_SCHED");
+        kernel("ce_sim_kalman_quad", MAXS, "ce::SIM_KALMAN_QUAD");
     } else {
         kernel("ce_sim_specialised", ns, "ce::SIM_LUENBERGER");
         if (!mc) {
@@ -165,7 +167,11 @@ SimKernels compile(const std::string& src, std::string& log, bool kalman) {
     }
     SimKernels out;
     std::vector<std::pair<const char*, const void**>> wanted{{"ce_sim_specialised", &out.main}};
-    if (kalman) wanted.push_back({"ce_sim_kalman_shared", &out.shared});
+    if (kalman) {
+        wanted.push_back({"ce_sim_kalman_shared", &out.shared});
+        wanted.push_back({"ce_sim_kalman_sched", &out.sched});
+        wanted.push_back({"ce_sim_kalman_quad", &out.quad});
+    }
     if (src.find("ce_sim_wide(") != std::string::npos) wanted.push_back({"ce_sim_wide", &out.wide});
     for (const auto& [name, slot] : wanted) {
         cudaKernel_t k;

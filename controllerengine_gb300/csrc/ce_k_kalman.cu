@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(256) k_kal_scatter(const Run run, const unsign
 
 void launch_kalman_groups(const Run& run, const float* gains, const KalGroups& g, cudaStream_t st) {
     // cnt, fill and totals are one contiguous block
-    CE_CUDA(cudaMemsetAsync(g.cnt, 0, (2 * (size_t)KAL_BUCKETS + 4) * sizeof(int), st));
+    CE_CUDA(cudaMemsetAsync(g.cnt, 0, (2 * (size_t)KAL_BUCKETS + KAL_TOTALS) * sizeof(int), st));
     CE_CUDA(cudaMemsetAsync(g.order, 0xff, (size_t)kal_shared_slots(run.n) * sizeof(int), st));
     const int blocks = (int)((run.n + 255) / 256);
     k_kal_hist<<<blocks, 256, 0, st>>>(run, gains, g.bucket, g.cnt);
@@ -117,7 +117,8 @@ void launch_kalman_groups(const Run& run, const float* gains, const KalGroups& g
 }
 
 int sim_grid(const Run& run) {
-    const int64_t slots = run.kal_list == 1 ? kal_shared_slots(run.n) : run.n;
+    // the shared list's slots; the stragglers' quad form: four lanes per candidate
+    const int64_t slots = run.kal_list == 1 ? kal_shared_slots(run.n) : run.kal_list == 4 ? 4 * run.n : run.n;
     return (int)((slots + SIM_BLOCK - 1) / SIM_BLOCK);
 }
 

@@ -638,6 +638,68 @@ __global__ void __launch_bounds__(SIM_BLOCK) k_sim_ext(const Run run, const __gr
     summ[4 * c + 3] = 0.0;
 }
 
+// The gain schedules of the Kalman per-candidate list.  The covariance
+// recursion reads only the observer model, R and diag(Q), so a candidate's
+// gains can be computed ahead of its trajectory: one thread per list position
+// runs the per-candidate form's recursion (kalman_cov_lane, the same
+// operations) for up to KAL_SCHED_STEPS steps and stores each step's gain.  A
+// snapshot of P every KAL_SCHED_SNAP steps is compared bit for bit with
+// P_{t+1}; once equal, the recursion is periodic -- P_{t+1} = P_{t0} makes
+// every later gain the one p = t + 1 - t0 steps earlier -- and the thread
+// stops.  Periodic positions are listed for the scheduled simulation form;
+// the others (no period within the schedule) for the quad form, which runs
+// their recursion in full.
+
+__global__ void __launch_bounds__(SIM_BLOCK) k_kal_schedule(const Run run, const __grid_constant__ Plant P,
+                                                            const float* __restrict__ gains, float* __restrict__ sched,
+                                                            int2* __restrict__ meta, int* __restrict__ lists,
+                                                            int* __restrict__ totals) {
+    __shared__ float snap[MAXS * MAXS][SIM_BLOCK];
+    const int tid = threadIdx.x;
+    const int64_t lp = (int64_t)blockIdx.x * SIM_BLOCK + tid;
+    if (lp >= (int64_t)run.kal_totals[1] + run.kal_totals[2]) return;
+    const int64_t c = kal_list_candidate(run, lp);
+    const int ns = run.ns;
+    const float* row = gains + c * run.cuda_w;
+    const float Rn = row[2 * ns + 1];
+    float Qd[MAXS], Pm[MAXS * MAXS], KG[MAXS];
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) Qd[i] = i < ns ? row[2 * ns + 2 + i] : 0.0f;
+#pragma unroll
+    for (int e = 0; e < MAXS * MAXS; ++e) Pm[e] = 0.0f;
+    const int64_t S = run.kal_sched_n;
+    const int steps = min(run.time, KAL_SCHED_STEPS);
+    int t_snap = 0;
+    int2 m = make_int2(-1, 0);
+    for (int t = 0; t < steps; ++t) {
+        if (t - t_snap == KAL_SCHED_SNAP || t == 0) {
+#pragma unroll
+            for (int e = 0; e < MAXS * MAXS; ++e) snap[e][tid] = Pm[e];
+            t_snap = t;
+        }
+        kalman_cov_lane(P, Pm, Qd, Rn, KG);
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) sched[((int64_t)t * MAXS + k) * S + lp] = KG[k];
+        bool same = true;
+#pragma unroll
+        for (int e = 0; e < MAXS * MAXS; ++e) same = same && __float_as_uint(Pm[e]) == __float_as_uint(snap[e][tid]);
+        if (same) {
+            m = make_int2(t_snap, t + 1 - t_snap);
+            break;
+        }
+    }
+    meta[lp] = m;
+    if (m.x >= 0) lists[atomicAdd(&totals[3], 1)] = (int)lp;
+    else lists[S + atomicAdd(&totals[4], 1)] = (int)lp;
+}
+
+void launch_kalman_schedule(const Run& run, const Plant& P, const float* gains, const KalGroups& g,
+                            cudaStream_t st) {
+    const int grid = (int)((run.n + SIM_BLOCK - 1) / SIM_BLOCK);
+    k_kal_schedule<<<grid, SIM_BLOCK, 0, st>>>(run, P, gains, g.sched, g.meta, g.lists, g.totals);
+    CE_CUDA(cudaGetLastError());
+}
+
 static int dim_class(int d) { return d <= 4 ? 4 : 8; }
 
 // Lanes per candidate of a ragged batch's simulation: 4 (the wide form,
@@ -702,6 +764,14 @@ void launch_sim(const Run& run, const Plant& P, int precision, const float* gain
         // the shared-noise form; the Kalman loop always runs the full padded observer width
         if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);
         else sim_launch<8, 8, SIM_KALMAN_SHARED>(run, P, precision, gains, ywin, summ, traj, st);
+    } else if (run.kalman && run.kal_list == 3) {
+        // the per-candidate list's positions whose gain schedule turned periodic
+        if (cd == 4) sim_launch<8, 4, SIM_KALMAN_SCHED>(run, P, precision, gains, ywin, summ, traj, st);
+        else sim_launch<8, 8, SIM_KALMAN_SCHED>(run, P, precision, gains, ywin, summ, traj, st);
+    } else if (run.kalman && run.kal_list == 4) {
+        // the positions whose schedule did not turn periodic: the quad form
+        if (cd == 4) sim_launch<8, 4, SIM_KALMAN_QUAD>(run, P, precision, gains, ywin, summ, traj, st);
+        else sim_launch<8, 8, SIM_KALMAN_QUAD>(run, P, precision, gains, ywin, summ, traj, st);
     } else if (run.kalman) {
         if (cd == 4) sim_launch<8, 4, SIM_KALMAN_LANE>(run, P, precision, gains, ywin, summ, traj, st);
         else sim_launch<8, 8, SIM_KALMAN_LANE>(run, P, precision, gains, ywin, summ, traj, st);

@@ -122,6 +122,7 @@ int64_t bytes_per_candidate(const ce_config& c, int precision) {
     f += real * (4 * nt * nt + 2 * nt);                                // AtA, Atb
     f += 1 + (MAXT + 1) + 1 + 1;                                       // nominal, fit order, lists
     f += real * (2 * (int64_t)c.freq + groups) + groups;               // sweep scratch
+    if (c.observer == CE_OBSERVER_KALMAN) f += (int64_t)KAL_SCHED_STEPS * MAXS + 4;  // gain schedules
     return 4 * f;
 }
 

@@ -385,7 +385,168 @@ __device__ __forceinline__ void kalman_gain_shared(const Plant& P, KalShared& S,
 // Simulation forms: KMODE 0 the Luenberger observer; 1 the Kalman observer
 // with each candidate's covariance in its own registers; 2 the Kalman observer
 // with the covariance shared by the warp (all 32 lanes hold the same R and Q).
-constexpr int SIM_LUENBERGER = 0, SIM_KALMAN_LANE = 1, SIM_KALMAN_SHARED = 2;
+// 3: the Kalman observer with the candidate's gains read from its gain
+// schedule (k_kal_schedule), no covariance recursion in the loop; 4: the
+// per-candidate covariance split over a quad of lanes (kalman_cov_quad).
+constexpr int SIM_LUENBERGER = 0, SIM_KALMAN_LANE = 1, SIM_KALMAN_SHARED = 2, SIM_KALMAN_SCHED = 3,
+              SIM_KALMAN_QUAD = 4;
+
+// The quad form: four lanes share a candidate.  Each lane runs the whole
+// trajectory (every value the same in the four; lane 0 writes the outputs) and
+// owns rows 2q and 2q+1 of every covariance product; P, the rows of P C^T and
+// the columns of C P meet in the candidate's slot of shared memory.  Every
+// element is formed by one lane with the per-candidate form's fma chain, so
+// the gains are bit-identical to it, at a quarter of the dependent chain per
+// step -- for the candidates whose recursion never turns periodic, which run
+// it for the whole horizon.
+struct KalQuadSlot {
+    float P[MAXS * MAXS];
+    float v[2 * MAXS];  // (P C^T)_i, then (C P)_j
+};
+struct KalQuadSmem {
+    KalQuadSlot s[SIM_BLOCK / SW_LANES];
+};
+struct KalQuadRef {
+    KalQuadSlot& s;
+    int q;
+    unsigned qm;
+};
+__device__ __forceinline__ void kalman_cov_quad(const Plant& P, const KalQuadRef& Q, const float (&Qd)[MAXS],
+                                                float Rn, float (&KG)[MAXS]) {
+    KalQuadSlot& S = Q.s;
+    const int i0 = 2 * Q.q;
+    float t[2][MAXS], p[2][MAXS];
+    // P <- A P A^T + diag(Q), own rows: row i of A P from all of P, then of (A P) A^T
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(P.ss_a[(i0 + r) * MAXS + k], S.P[k * MAXS + j], a);
+            t[r][j] = a;
+        }
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(t[r][k], P.ss_a[j * MAXS + k], a);
+            p[r][j] = j == i0 + r ? __fadd_rn(a, Qd[i0 + r]) : a;
+        }
+    __syncwarp(Q.qm);  // every read of the old P is done
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) S.P[(i0 + r) * MAXS + j] = p[r][j];
+    __syncwarp(Q.qm);
+    // gain: own rows of P C^T, own columns of C P
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        float a = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(p[r][k], P.ss_c[k], a);
+        S.v[i0 + r] = a;
+        float b = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXS; ++k) b = __fmaf_rn(P.ss_c[k], S.P[k * MAXS + i0 + r], b);
+        S.v[MAXS + i0 + r] = b;
+    }
+    __syncwarp(Q.qm);
+    float hphr = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) hphr = __fmaf_rn(S.v[MAXS + k], P.ss_c[k], hphr);
+    hphr = __fdiv_rn(1.0f, __fadd_rn(hphr, Rn));
+#pragma unroll
+    for (int i = 0; i < MAXS; ++i) KG[i] = __fmul_rn(S.v[i], hphr);
+    // P <- (I - KG C) P (I - KG C)^T + KG R KG^T, own rows
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(ikh(KG[i0 + r], P.ss_c[k], i0 + r == k), S.P[k * MAXS + j], a);
+            t[r][j] = a;
+        }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const float kr = __fmaf_rn(KG[i0 + r], Rn, 0.0f);
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) a = __fmaf_rn(t[r][k], ikh(KG[j], P.ss_c[k], j == k), a);
+            p[r][j] = __fadd_rn(a, __fmaf_rn(kr, KG[j], 0.0f));
+        }
+    }
+    __syncwarp(Q.qm);  // every read of P and of v is done
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) S.P[(i0 + r) * MAXS + j] = p[r][j];
+    __syncwarp(Q.qm);
+}
+
+template <bool Q> struct QuadSmemOf { using type = KalQuadSmem; };
+template <> struct QuadSmemOf<false> { struct type {}; };
+
+// The per-candidate list position of the Kalman list `pos` of a scheduled (3)
+// or straggler (4) launch, or pos itself for the per-candidate list (2); -1
+// past the list's end.
+__device__ __forceinline__ int64_t kal_list_position(const Run& run, int64_t pos) {
+    if (run.kal_list == 2) return pos < (int64_t)run.kal_totals[1] + run.kal_totals[2] ? pos : -1;
+    const int64_t cnt = run.kal_totals[run.kal_list == 3 ? 3 : 4];
+    return pos < cnt ? run.kal_lists[(run.kal_list == 3 ? 0 : run.kal_sched_n) + pos] : -1;
+}
+// The candidate at position lp of the per-candidate list: the list proper, then
+// the candidates deferred by the shared form.
+__device__ __forceinline__ int64_t kal_list_candidate(const Run& run, int64_t lp) {
+    const int64_t np = run.kal_totals[1];
+    return lp < np ? run.kal_order[run.kal_totals[0] + lp] : run.kal_order[run.kal_defer + lp - np];
+}
+
+// Snapshots of P every KAL_SCHED_SNAP steps in the gain schedules: periods of
+// up to this many steps are found.
+constexpr int KAL_SCHED_SNAP = 8;
+
+// The gain of step t from a candidate's schedule: KG_t for t below t0 + p, then
+// the period [t0, t0 + p) again and again (a running index, no division).  The
+// schedule is read in step with the warp's other candidates (one coalesced row
+// per gain); the period, which each candidate enters at its own step, is kept
+// in the thread's column of shared memory once reached.
+struct KalSchedSmem {
+    float g[KAL_SCHED_SNAP * MAXS][SIM_BLOCK];
+};
+struct KalSched {
+    const float* g;   // the candidate's column: gain k of schedule step s at g[(s * MAXS + k) * stride]
+    int64_t stride;
+    int idx, t0, end;  // index of the current step's gain; the period's first step and end
+    float* ring;       // the period's gains, gain k of period step s at ring[(s * MAXS + k) * SIM_BLOCK]
+    bool cyc;          // the period has been reached (gains from the ring)
+    __device__ __forceinline__ void next(float (&KG)[MAXS]) {
+        if (cyc) {
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) KG[k] = ring[((idx - t0) * MAXS + k) * SIM_BLOCK];
+        } else {
+#pragma unroll
+            for (int k = 0; k < MAXS; ++k) KG[k] = g[((int64_t)idx * MAXS + k) * stride];
+        }
+        if (++idx == end) {
+            if (!cyc) {
+                for (int s = t0; s < end; ++s)
+#pragma unroll
+                    for (int k = 0; k < MAXS; ++k)
+                        ring[((s - t0) * MAXS + k) * SIM_BLOCK] = g[((int64_t)s * MAXS + k) * stride];
+                cyc = true;
+            }
+            idx = t0;
+        }
+    }
+};
+template <bool S> struct SchedSmemOf { using type = KalSchedSmem; };
+template <> struct SchedSmemOf<false> { struct type {}; };
 
 template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
 __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run, const Plant& P, int64_t c,
@@ -406,11 +567,15 @@ __device__ __forceinline__ void sim_run(const Run& run_in, const Plant& P_in, co
     __shared__ float srcP[Chains::kSmem ? MAXD + 1 : 1][SIM_BLOCK];
     __shared__ float srcH[Chains::kSmem ? MAXS : 1][SIM_BLOCK];
     __shared__ KalWarp kw[SHARED ? SIM_BLOCK / 32 : 1];
+    __shared__ typename QuadSmemOf<KMODE == SIM_KALMAN_QUAD>::type kq;
+    __shared__ typename SchedSmemOf<KMODE == SIM_KALMAN_SCHED>::type ksr;
     const int tid = threadIdx.x;
-    // each thread only touches its own column of the shared rows
-    const int64_t pos = (int64_t)blockIdx.x * SIM_BLOCK + tid;
+    // each thread only touches its own column of the shared rows; the quad form
+    // gives a candidate to four consecutive threads
+    constexpr bool QUAD = KMODE == SIM_KALMAN_QUAD;
+    const int64_t pos = ((int64_t)blockIdx.x * SIM_BLOCK + tid) / (QUAD ? SW_LANES : 1);
     int64_t c = pos;
-    bool writer = true;
+    bool writer = !QUAD || (tid & 3) == 0;
     if constexpr (SHARED) {
         // the shared-noise list: whole warps of one group; a padding slot (-1)
         // shadows the warp's first candidate and writes nothing
@@ -419,17 +584,35 @@ __device__ __forceinline__ void sim_run(const Run& run_in, const Plant& P_in, co
         const int own = run.kal_order[pos];
         writer = own >= 0;
         c = writer ? own : run.kal_order[wbase];
-    } else if (KAL && run.kal_list == 2) {
-        // the per-candidate list, then the candidates of warps deferred by the shared form
-        const int64_t np = run.kal_totals[1], nd = run.kal_totals[2];
-        if (pos < np) c = run.kal_order[run.kal_totals[0] + pos];
-        else if (pos < np + nd) c = run.kal_order[run.kal_defer + pos - np];
-        else return;
+    } else if (KAL && run.kal_list >= 2) {
+        // the per-candidate list (then the candidates of warps deferred by the
+        // shared form), or its scheduled or straggling positions
+        const int64_t lp = kal_list_position(run, pos);
+        if (lp < 0) return;
+        c = kal_list_candidate(run, lp);
+        if constexpr (KMODE == SIM_KALMAN_SCHED) {
+            const int2 m = run.kal_meta[lp];
+            KalSched ks{run.kal_sched + lp, run.kal_sched_n, 0, m.x, m.x + m.y, &ksr.g[0][tid], false};
+            return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_in, run_of<RG>(run_in, c),
+                                                               plant_of<RG>(run_in, P_in, c), c, writer, gains, ywin,
+                                                               summ, traj, stage, srcP, srcH, ks);
+        }
+        if constexpr (QUAD) {
+            KalQuadRef kr{kq.s[tid >> 2], tid & 3, 0xFu << (tid & 28)};
+            return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_in, run_of<RG>(run_in, c),
+                                                               plant_of<RG>(run_in, P_in, c), c, writer, gains, ywin,
+                                                               summ, traj, stage, srcP, srcH, kr);
+        }
     } else {
         if (c >= run.n) return;
     }
-    return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_in, run_of<RG>(run_in, c), plant_of<RG>(run_in, P_in, c),
-                                                       c, writer, gains, ywin, summ, traj, stage, srcP, srcH, kw);
+    if constexpr (KMODE == SIM_KALMAN_SCHED || QUAD) {
+        return;  // the scheduled and quad forms run only over their lists (kal_list 3, 4)
+    } else {
+        return sim_candidate<NSC, NDC, Chains, KMODE, RG>(run_in, run_of<RG>(run_in, c),
+                                                           plant_of<RG>(run_in, P_in, c), c, writer, gains, ywin,
+                                                           summ, traj, stage, srcP, srcH, kw);
+    }
 }
 
 template <int NSC, int NDC, class Chains, int KMODE, bool RG, class Stage, class SrcP, class SrcH, class KW>
@@ -454,11 +637,20 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
     static_assert(!KAL || NSC == MAXS, "the Kalman observer runs the full padded width");
     // Kalman: noise weights and covariance (ref: src/discrete_solves.cu:88-101,
     // at the row offsets of [K, L, N, R, Q])
-    float Qd[KMODE == SIM_KALMAN_LANE ? MAXS : 1], Pm[KMODE == SIM_KALMAN_LANE ? MAXS * MAXS : 1];
+    float Qd[KMODE == SIM_KALMAN_LANE || KMODE == SIM_KALMAN_QUAD ? MAXS : 1],
+        Pm[KMODE == SIM_KALMAN_LANE ? MAXS * MAXS : 1];
     float KG[KAL ? MAXS : 1];
     float Rn = 0.0f;
     KalShared S;
     const int lane = tid & 31;
+    if constexpr (KMODE == SIM_KALMAN_QUAD) {
+        Rn = row[2 * ns + 1];
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) Qd[i] = i < ns ? row[2 * ns + 2 + i] : 0.0f;
+#pragma unroll
+        for (int j = 0; j < 2 * MAXS; ++j) kw.s.P[2 * kw.q * MAXS + j] = 0.0f;  // own rows of P
+        __syncwarp(kw.qm);
+    }
     if constexpr (KMODE == SIM_KALMAN_LANE) {
         Rn = row[2 * ns + 1];
 #pragma unroll
@@ -560,6 +752,10 @@ __device__ __forceinline__ void sim_candidate(const Run& launch, const Run& run,
             kalman_predict(P, xh_hi, xh_lo, u);
             if constexpr (SHARED) {
                 kalman_gain_shared(P, S, kw[tid >> 5], lane, KG);
+            } else if constexpr (KMODE == SIM_KALMAN_SCHED) {
+                kw.next(KG);
+            } else if constexpr (KMODE == SIM_KALMAN_QUAD) {
+                kalman_cov_quad(P, kw, Qd, Rn, KG);
             } else {
                 kalman_cov_lane(P, Pm, Qd, Rn, KG);
             }

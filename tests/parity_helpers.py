@@ -46,8 +46,9 @@ def _stagewise(problem, oracle_mod, score_atol=1e-6, eig_arith=None):
         info, d = s.evaluate_diagnostics(problem.cuda_mx, problem.info_mx)
         launches = s.kernel_launches
     # lina+eig, sim, fit classes, fit, modal, nominal, sweep selection, LU pass, scan; the
-    # Kalman observer adds three grouping kernels and its second simulation form
-    assert launches == (13 if cfg.observer else 9)
+    # Kalman observer adds three grouping kernels, the per-candidate list's gain schedules and
+    # two more simulation forms
+    assert launches == (15 if cfg.observer else 9)
     orc = oracle_mod.Oracle(problem.config_text, problem.plant, eig_fused=arith == "fused")
     g = problem.cuda_mx
 

@@ -41,6 +41,25 @@ def test_kalman_trajectories_bit_exact(oracle_mod, eight_kalman, mass_kalman, ke
     assert np.isfinite(d["yplant"]).mean() > 0.9
 
 
+@pytest.mark.parametrize("kernel", ["table", "specialised"])
+@pytest.mark.parametrize("time", [800, 3000])
+def test_kalman_distinct_noise_schedules_bit_exact(oracle_mod, kernel, time):
+    """Every candidate with its own noise weights (R scaled by 1 + U[0, 1e-3]): the per-candidate
+    list's gain schedules (periodic within 1,024 steps: the scheduled form; the rest: the full
+    per-candidate recursion; with T = 800 the schedule covers the whole horizon) give the oracle's
+    trajectories bit for bit."""
+    p = synth.eight_state(n=384, time=time, freq=80, observer="kalman")
+    g = p.cuda_mx.copy()
+    g[:, 17] *= (1.0 + 1e-3 * np.random.default_rng(17).random(g.shape[0])).astype(np.float32)
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        s.set_sim_kernel(kernel)
+        _, d = s.evaluate_diagnostics(g, p.info_mx)
+    y_o = oracle_mod.Oracle(p.config_text, p.plant).sim(g)
+    assert _eq(d["yplant"], y_o), f"trajectory mismatches: {_mismatch(d['yplant'], y_o)}"
+    assert np.isfinite(d["yplant"]).mean() > 0.9
+
+
 @pytest.mark.parametrize("which", ["eight", "mass"])
 def test_kalman_stagewise(oracle_mod, eight_kalman, mass_kalman, which):
     # one mass-spring row has a score of -2.0e-3 that the oracle's glibc-recomputed modes
@@ -107,7 +126,9 @@ def test_kalman_shared_noise_groups(oracle_mod):
     with ce.Session(cfg, p.plant) as s:
         _, d = s.evaluate_diagnostics(p.cuda_mx, p.info_mx, want=("yplant",))
         launches = s.kernel_launches
-    assert launches == 13  # the nine of the Luenberger pipeline, three grouping kernels, a second simulation form
+    # the nine of the Luenberger pipeline, three grouping kernels, the gain schedules and two more
+    # simulation forms
+    assert launches == 15
     y_o = oracle_mod.Oracle(p.config_text, p.plant).sim(p.cuda_mx)
     assert _eq(d["yplant"], y_o), f"trajectory mismatches: {_mismatch(d['yplant'], y_o)}"
 
