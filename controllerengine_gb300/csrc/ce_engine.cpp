@@ -547,9 +547,13 @@ void run_pipeline(ce_session* s, int plant, int64_t n, const float* d_gains, flo
             cudaStream_t qs = s->side3;
             if (sk) launch_sim_specialised(sk.shared, rh, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
             else launch_sim(rh, P, sprec, d_gains, b.ywin, b.summ, tr, fs);
-            launch_kalman_schedule(rp, P, d_gains, b.kal, fs);
+            // the schedules and the quad form on the high-priority stream: with
+            // per-candidate noise they are the step's critical path
             CE_CUDA(cudaEventRecord(s->ev_kal, fs));
             CE_CUDA(cudaStreamWaitEvent(qs, s->ev_kal, 0));
+            launch_kalman_schedule(rp, P, d_gains, b.kal, qs);
+            CE_CUDA(cudaEventRecord(s->ev_kal, qs));
+            CE_CUDA(cudaStreamWaitEvent(fs, s->ev_kal, 0));
             if (sk) {
                 launch_sim_specialised(sk.quad, rb, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, qs);
                 launch_sim_specialised(sk.sched, ra, P, d_gains, (float*)b.ywin, (SimSummary*)b.summ, tr, fs);
@@ -813,7 +817,7 @@ void init_streams(ce_session* s) {
     CE_CUDA(cudaStreamCreateWithPriority(&s->fast, cudaStreamNonBlocking, prio_least));
     CE_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_greatest));
     CE_CUDA(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, prio_greatest));
-    CE_CUDA(cudaStreamCreateWithPriority(&s->side3, cudaStreamNonBlocking, prio_least));
+    CE_CUDA(cudaStreamCreateWithPriority(&s->side3, cudaStreamNonBlocking, prio_greatest));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     CE_CUDA(cudaEventCreateWithFlags(&s->ev_kal, cudaEventDisableTiming));
