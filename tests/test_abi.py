@@ -53,3 +53,17 @@ def test_ragged_rejects_before_any_device_work(lib):
         ce.Ragged([(cfgs[0], p.plant), (cfgs[1], k.plant)])
     with pytest.raises(ce.ControllerEngineError, match="n_inst must be >= 1"):
         ce.Ragged([])
+
+
+def test_server_result_buffer_validation():
+    """A caller's result buffer for a served request must be a C-contiguous float32 array shaped like
+    the request's INFO rows; anything else is refused before the request reaches the library."""
+    import numpy as np
+    import pytest
+    i = np.zeros((5, 7), np.float32)
+    assert ce.Server._out(None, i).shape == (5, 7)
+    buf = np.empty((5, 7), np.float32)
+    assert ce.Server._out(buf, i) is buf
+    for bad in (np.empty((5, 7), np.float64), np.empty((4, 7), np.float32), np.empty((7, 5), np.float32).T):
+        with pytest.raises(ValueError):
+            ce.Server._out(bad, i)
