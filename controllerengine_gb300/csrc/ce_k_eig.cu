@@ -39,8 +39,12 @@
 // matrices resident per SM (about 100) and with them the warps that keep the
 // FP64 pipe fed: EQ = 1 issues the fewest FP64 instructions per matrix but
 // leaves 3 warps per SM; EQ = 2 or 4 gives 6 or 12 warps at the price of
-// computing the scalar steps (Householder vectors, shifts, deflation tests)
-// redundantly in every lane of the group.
+// computing the scalar steps (Householder vectors, shifts) redundantly in
+// every lane of the group.  The scans that only read T -- the deflation test
+// of every subdiagonal and the search for the row where a Francis step starts
+// -- are split over the group's lanes (the first hit from the top is taken,
+// which is the sequential scan's answer), and so are the independent divisions
+// of a Householder vector.
 #include <cfloat>
 #include <algorithm>
 #include <cstdlib>
@@ -78,6 +82,12 @@ struct Quad {
     unsigned mask;                // the group's lanes
     __device__ __forceinline__ void sync() const { __syncwarp(mask); }
     __device__ __forceinline__ bool lead() const { return q == 0; }
+    // A predicate of every lane of the group: bit k for the group's lane k.
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        return (__ballot_sync(mask, p) & mask) >> (__ffs(mask) - 1);
+    }
+    // v of the group's lane k, in every lane of the group.
+    __device__ __forceinline__ double bcast(double v, int k) const { return __shfl_sync(mask, v, k, EQ); }
 };
 
 // The eigensolver's arithmetic: F = false rounds every product and every sum
@@ -135,6 +145,115 @@ __device__ __forceinline__ void house_vec(const double* v, int m, double* ess, d
         ess[0] = __ddiv_rn(v[1], d);
         ess[1] = m == 3 ? __ddiv_rn(v[2], d) : 0.0;
         tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+    }
+}
+
+// house_vec computed by a group of lanes: the three quotients (v1 / d, v2 / d,
+// (beta - c0) / beta) are independent, so the group's lanes divide different
+// operands in one division and exchange the results -- the same quotients in
+// fewer FP64 instructions per warp (one division of a 2-lane group's three is
+// done by both lanes).
+template <bool F, class Qd>
+__device__ __forceinline__ void house_vec_g(const Qd& Q, const double* v, int m, double* ess, double& tau,
+                                            double& beta) {
+    if constexpr (Qd::N == 1) {
+        house_vec<F>(v, m, ess, tau, beta);
+    } else {
+        const double c0 = v[0];
+        const double v2 = m == 3 ? v[2] : 0.0;
+        double tail = __dmul_rn(v[1], v[1]);
+        if (m == 3) tail = mac<F>(tail, v2, v2);
+        if (tail <= DMIN_) {
+            tau = 0.0;
+            beta = c0;
+            ess[0] = 0.0;
+            ess[1] = 0.0;
+            return;
+        }
+        beta = sqrt(mac<F>(tail, c0, c0));
+        if (c0 >= 0.0) beta = -beta;
+        const double d = __dsub_rn(c0, beta);
+        const double nb = __dsub_rn(beta, c0);
+        if constexpr (Qd::N == 2) {
+            const double x = __ddiv_rn(Q.q == 0 ? v[1] : nb, Q.q == 0 ? d : beta);
+            ess[0] = Q.bcast(x, 0);
+            tau = Q.bcast(x, 1);
+            ess[1] = m == 3 ? __ddiv_rn(v2, d) : 0.0;
+        } else {
+            // lane 0: v1 / d, lane 1: v2 / d, lanes 2..: (beta - c0) / beta
+            const double x = __ddiv_rn(Q.q == 0 ? v[1] : Q.q == 1 ? v2 : nb, Q.q >= 2 ? beta : d);
+            ess[0] = Q.bcast(x, 0);
+            const double e1 = Q.bcast(x, 1);
+            ess[1] = m == 3 ? e1 : 0.0;
+            tau = Q.bcast(x, 2);
+        }
+    }
+}
+
+// The deflation point of the Francis iteration: the largest il <= iu with
+// il == 0 or |T(il, il-1)| <= max(eps (|T(il-1, il-1)| + |T(il, il)|), zero_tol).
+// The tests read T only, so the group's lanes take every N-th row each and
+// the first hit from the top is the sequential scan's answer.
+template <class Qd>
+__device__ __forceinline__ int deflation_row(const SMat& T, const Qd& Q, int iu, double zero_tol) {
+    auto small_sub = [&](int il) {
+        double s = __dadd_rn(fabs(T(il - 1, il - 1)), fabs(T(il, il)));
+        s = fmax(__dmul_rn(s, DEPS), zero_tol);
+        return fabs(T(il, il - 1)) <= s;
+    };
+    if constexpr (Qd::N == 1) {
+        int il = iu;
+        while (il > 0 && !small_sub(il)) il--;
+        return il;
+    } else {
+        for (int top = iu;; top -= Qd::N) {
+            const int il = top - Q.q;
+            const bool hit = il == 0 || (il > 0 && small_sub(il));
+            const unsigned b = Q.ballot(hit);
+            if (b) return top - (__ffs(b) - 1);
+        }
+    }
+}
+
+// The row im in [il, iu-2] where the Francis step starts, and the first
+// Householder vector v there: the largest im at which the bulge would not
+// disturb a negligible subdiagonal (or il).  Each candidate row's test reads
+// T only, so the group's lanes take every N-th row and the first hit from the
+// top is the sequential search's row, with v from the lane that found it.
+template <bool F, class Qd>
+__device__ __forceinline__ int francis_start(const SMat& T, const Qd& Q, int il, int iu, double sh0, double sh1,
+                                             double sh2, double* v) {
+    auto first_vec = [&](int im, double* w) {
+        const double Tmm = T(im, im);
+        const double r = __dsub_rn(sh0, Tmm);
+        const double s = __dsub_rn(sh1, Tmm);
+        w[0] = __dadd_rn(__ddiv_rn(__dsub_rn(__dmul_rn(r, s), sh2), T(im + 1, im)), T(im, im + 1));
+        w[1] = __dsub_rn(__dsub_rn(__dsub_rn(T(im + 1, im + 1), Tmm), r), s);
+        w[2] = T(im + 2, im + 1);
+        if (im == il) return true;
+        const double lhs = __dmul_rn(T(im, im - 1), __dadd_rn(fabs(w[1]), fabs(w[2])));
+        const double rhs =
+            __dmul_rn(w[0], __dadd_rn(__dadd_rn(fabs(T(im - 1, im - 1)), fabs(Tmm)), fabs(T(im + 1, im + 1))));
+        return fabs(lhs) < __dmul_rn(DEPS, rhs);
+    };
+    if constexpr (Qd::N == 1) {
+        int im = iu - 2;
+        while (!first_vec(im, v)) --im;
+        return im;
+    } else {
+        for (int top = iu - 2;; top -= Qd::N) {
+            const int im = top - Q.q;
+            double w[3] = {0.0, 0.0, 0.0};
+            const bool hit = im >= il && first_vec(im, w);
+            const unsigned b = Q.ballot(hit);
+            if (b) {
+                const int k = __ffs(b) - 1;
+                v[0] = Q.bcast(w[0], k);
+                v[1] = Q.bcast(w[1], k);
+                v[2] = Q.bcast(w[2], k);
+                return top - k;
+            }
+        }
     }
 }
 
@@ -457,13 +576,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
         double exshift = 0.0;
         if (norm != 0.0) {
             while (iu >= 0) {
-                int il = iu;
-                while (il > 0) {
-                    double s = __dadd_rn(fabs(T(il - 1, il - 1)), fabs(T(il, il)));
-                    s = fmax(__dmul_rn(s, DEPS), zero_tol);
-                    if (fabs(T(il, il - 1)) <= s) break;
-                    il--;
-                }
+                const int il = deflation_row(T, Q, iu, zero_tol);
                 Q.sync();
                 if (il == iu) {
                     if (Q.lead()) {
@@ -540,20 +653,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                     if (total > max_iter) break;
                     // first Householder vector
                     double v[3] = {0.0, 0.0, 0.0};
-                    int im;
-                    for (im = iu - 2; im >= il; --im) {
-                        const double Tmm = T(im, im);
-                        const double r = __dsub_rn(sh0, Tmm);
-                        const double s = __dsub_rn(sh1, Tmm);
-                        v[0] = __dadd_rn(__ddiv_rn(__dsub_rn(__dmul_rn(r, s), sh2), T(im + 1, im)), T(im, im + 1));
-                        v[1] = __dsub_rn(__dsub_rn(__dsub_rn(T(im + 1, im + 1), Tmm), r), s);
-                        v[2] = T(im + 2, im + 1);
-                        if (im == il) break;
-                        const double lhs = __dmul_rn(T(im, im - 1), __dadd_rn(fabs(v[1]), fabs(v[2])));
-                        const double rhs = __dmul_rn(
-                            v[0], __dadd_rn(__dadd_rn(fabs(T(im - 1, im - 1)), fabs(Tmm)), fabs(T(im + 1, im + 1))));
-                        if (fabs(lhs) < __dmul_rn(DEPS, rhs)) break;
-                    }
+                    const int im = francis_start<F>(T, Q, il, iu, sh0, sh1, sh2, v);
                     // the QR step
                     for (int k = im; k <= iu - 2; ++k) {
                         const bool first = (k == im);
@@ -564,7 +664,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                             w[0] = T(k, k - 1); w[1] = T(k + 1, k - 1); w[2] = T(k + 2, k - 1);
                         }
                         double ess[2], tau, beta;
-                        house_vec<F>(w, 3, ess, tau, beta);
+                        house_vec_g<F>(Q, w, 3, ess, tau, beta);
                         Q.sync();
                         if (beta != 0.0) {
                             if (Q.lead()) {
@@ -580,7 +680,7 @@ __device__ bool eig_real(const SMat& T, const Qd& Q, int n, Emit emit) {
                     {
                         double w[2] = {T(iu - 1, iu - 2), T(iu, iu - 2)};
                         double ess[2], tau, beta;
-                        house_vec<F>(w, 2, ess, tau, beta);
+                        house_vec_g<F>(Q, w, 2, ess, tau, beta);
                         Q.sync();
                         if (beta != 0.0) {
                             if (Q.lead()) T(iu - 1, iu - 2) = beta;
