@@ -54,12 +54,16 @@
 
 namespace ce {
 
-// One warp per block; EQ lanes per matrix, so 32 / EQ matrices per block,
-// interleaved in shared memory with a stride of 32 / EQ + 1 doubles.
+// One warp per block; EQ lanes per matrix, so M = 32 / EQ matrices per block,
+// interleaved in shared memory element by element: element e of matrix m at
+// double e * M + m.  Matrix m is owned by lanes m, m + M, m + 2M, ..: the lanes
+// of a half-warp belong to different matrices and, when they access the same
+// element of their matrices (the lanes of a warp run the same loop with the
+// same indices), hit 16 different bank pairs -- no conflict and no padding.
 constexpr int EIG_LANES_DEFAULT = 2;
 constexpr int EIG_BLOCKS_PER_SM_DEFAULT = 5;
 template <int EQ> constexpr int eig_mats() { return 32 / EQ; }
-template <int EQ> constexpr int eig_stride() { return 32 / EQ + 1; }
+template <int EQ> constexpr int eig_stride() { return 32 / EQ; }
 constexpr double DEPS = 2.220446049250313080847e-16;
 constexpr double DMIN_ = 2.2250738585072013831e-308;
 
@@ -69,25 +73,28 @@ struct SMat {
     __device__ __forceinline__ double& operator()(int i, int j) const { return p[(i * n + j) * B]; }
 };
 
-// A quad of lanes owns one matrix: loops over rows / columns are split by 4,
-// scalar decisions are computed redundantly by all four lanes (they read the
-// same values after each __syncwarp), and single-element writes are made by
-// lane 0 of the quad.  Every element is updated by exactly one lane with the
-// same operation sequence as a sequential code, so the results do not depend
-// on the split.
+// A group of EQ lanes owns one matrix: loops over rows / columns are split
+// over the group, scalar decisions are computed redundantly by all its lanes
+// (they read the same values after each __syncwarp), and single-element writes
+// are made by the group's lane 0.  Every element is updated by exactly one
+// lane with the same operation sequence as a sequential code, so the results
+// do not depend on the split.
 template <int EQ>
 struct Quad {
-    static constexpr int N = EQ;  // lanes per matrix
-    int q;                        // 0..EQ-1
-    unsigned mask;                // the group's lanes
+    static constexpr int N = EQ;       // lanes per matrix
+    static constexpr int M = 32 / EQ;  // matrices per warp
+    int q;                             // 0..EQ-1, the lane's place in its group
+    int m;                             // the matrix slot; the group is lanes m, m + M, ..
+    unsigned mask;                     // the group's lanes
     __device__ __forceinline__ void sync() const { __syncwarp(mask); }
     __device__ __forceinline__ bool lead() const { return q == 0; }
-    // A predicate of every lane of the group: bit k for the group's lane k.
-    __device__ __forceinline__ unsigned ballot(bool p) const {
-        return (__ballot_sync(mask, p) & mask) >> (__ffs(mask) - 1);
+    // The first k (in the group's lane order) for which p holds, or -1.
+    __device__ __forceinline__ int first(bool p) const {
+        const unsigned b = __ballot_sync(mask, p) & mask;
+        return b ? (__ffs(b) - 1 - m) / M : -1;
     }
     // v of the group's lane k, in every lane of the group.
-    __device__ __forceinline__ double bcast(double v, int k) const { return __shfl_sync(mask, v, k, EQ); }
+    __device__ __forceinline__ double bcast(double v, int k) const { return __shfl_sync(mask, v, m + k * M); }
 };
 
 // The eigensolver's arithmetic: F = false rounds every product and every sum
@@ -208,9 +215,8 @@ __device__ __forceinline__ int deflation_row(const SMat& T, const Qd& Q, int iu,
     } else {
         for (int top = iu;; top -= Qd::N) {
             const int il = top - Q.q;
-            const bool hit = il == 0 || (il > 0 && small_sub(il));
-            const unsigned b = Q.ballot(hit);
-            if (b) return top - (__ffs(b) - 1);
+            const int k = Q.first(il == 0 || (il > 0 && small_sub(il)));
+            if (k >= 0) return top - k;
         }
     }
 }
@@ -244,10 +250,8 @@ __device__ __forceinline__ int francis_start(const SMat& T, const Qd& Q, int il,
         for (int top = iu - 2;; top -= Qd::N) {
             const int im = top - Q.q;
             double w[3] = {0.0, 0.0, 0.0};
-            const bool hit = im >= il && first_vec(im, w);
-            const unsigned b = Q.ballot(hit);
-            if (b) {
-                const int k = __ffs(b) - 1;
+            const int k = Q.first(im >= il && first_vec(im, w));
+            if (k >= 0) {
                 v[0] = Q.bcast(w[0], k);
                 v[1] = Q.bcast(w[1], k);
                 v[2] = Q.bcast(w[2], k);
@@ -786,9 +790,12 @@ __device__ __forceinline__ float lina_entry(const Plant& P, const PV& pv, const 
 
 template <int EQ>
 __device__ __forceinline__ Quad<EQ> make_quad() {
+    constexpr int M = 32 / EQ;
+    unsigned rep = 0;  // bits 0, M, 2M, ..
+#pragma unroll
+    for (int k = 0; k < EQ; ++k) rep |= 1u << (k * M);
     const int lane = threadIdx.x & 31;
-    const int q = lane % EQ;
-    return Quad<EQ>{q, ((EQ == 32) ? 0xFFFFFFFFu : ((1u << EQ) - 1u)) << (lane - q)};
+    return Quad<EQ>{lane / M, lane % M, rep << (lane % M)};
 }
 // First index of the next 32 / EQ matrices for the calling warp (one-warp
 // blocks); called by all 32 lanes together, so the loop around it decides to
@@ -818,8 +825,8 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_
                                                         int* __restrict__ list, int* __restrict__ count,
                                                         int* __restrict__ next) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
+    const int m = Q.m;
     // persistent: the grid covers a fixed number of blocks per SM; each warp
     // takes the next 32 / EQ matrices from a counter when it is done (the
     // iteration count varies a lot between matrices, a static split would
@@ -882,8 +889,8 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
                                                           int* __restrict__ list, int* __restrict__ count,
                                                           int* __restrict__ next) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
+    const int m = Q.m;
     for (;;) {
         const int64_t base = take_work<EQ>(next);
         if (base >= run.n) break;
@@ -942,8 +949,8 @@ __global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_c
                                                        const int* __restrict__ list, const int* __restrict__ count,
                                                        int* __restrict__ nominal, int fp64_form, int* __restrict__ next) {
     extern __shared__ double smem[];
-    const int m = threadIdx.x / EQ;
     const auto Q = make_quad<EQ>();
+    const int m = Q.m;
     const int64_t listed = list ? (int64_t)*count : run.n;
     for (;;) {
         const int64_t base = take_work<EQ>(next);
