@@ -62,6 +62,13 @@ namespace ce {
 // same indices), hit 16 different bank pairs -- no conflict and no padding.
 constexpr int EIG_LANES_DEFAULT = 2;
 constexpr int EIG_BLOCKS_PER_SM_DEFAULT = 5;
+// The persistent eigensolve blocks share their SMs with the FP32 stages of the
+// other stream, so their registers come out of the fit's and the simulation's
+// share.  Bounding them as if 20 one-warp blocks were resident caps them at
+// 80-94 registers (no spills), which leaves room for a fifth fit block beside
+// the five eigensolve blocks: left unbounded (104 registers) the eigensolve
+// itself is ~2% faster but the fit loses a block and the step gets slower.
+constexpr int EIG_REG_BLOCKS = 20;
 template <int EQ> constexpr int eig_mats() { return 32 / EQ; }
 template <int EQ> constexpr int eig_stride() { return 32 / EQ; }
 constexpr double DEPS = 2.220446049250313080847e-16;
@@ -819,7 +826,7 @@ __device__ __forceinline__ void list_if_stable(bool unstable, int64_t c, int* no
 }
 
 template <int EQ, bool RG = false, bool F = false>
-__global__ void __launch_bounds__(32, 1) k_lina_eig(const Run run, const __grid_constant__ Plant P,
+__global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, int* __restrict__ nominal,
                                                         int* __restrict__ list, int* __restrict__ count,
@@ -883,7 +890,7 @@ __device__ __forceinline__ double lina_entry64(const Plant& P, double Kj, double
 }
 
 template <int EQ, bool F = false>
-__global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
+__global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_lina_eig64(const Run run, const __grid_constant__ Plant P,
                                                           const float* __restrict__ gains, double* __restrict__ lina,
                                                           double* __restrict__ eig64, int* __restrict__ nominal,
                                                           int* __restrict__ list, int* __restrict__ count,
@@ -944,7 +951,7 @@ __global__ void __launch_bounds__(32, 1) k_lina_eig64(const Run run, const __gri
 // kernel runs concurrently with k_lina_eig (which then lists nothing): the
 // flags of the candidates the modal stage flags are computed but never read.
 template <int EQ, bool RG = false, bool F = false>
-__global__ void __launch_bounds__(32, 1) k_nominal(const Run run, const __grid_constant__ Plant P,
+__global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const void* __restrict__ lina,
                                                        const int* __restrict__ list, const int* __restrict__ count,
                                                        int* __restrict__ nominal, int fp64_form, int* __restrict__ next) {
