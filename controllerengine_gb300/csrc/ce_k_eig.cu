@@ -68,7 +68,13 @@ constexpr int EIG_BLOCKS_PER_SM_DEFAULT = 5;
 // 80-94 registers (no spills), which leaves room for a fifth fit block beside
 // the five eigensolve blocks: left unbounded (104 registers) the eigensolve
 // itself is ~2% faster but the fit loses a block and the step gets slower.
+// With the Kalman observer the other stream runs the register-heavy
+// covariance forms instead, and there the unbounded kernels make the step
+// shorter (per-candidate noise weights: 93 against 103 ms per 65,536
+// candidates), so Kalman sessions launch unbounded instantiations of the
+// default form (two lanes per matrix, fused arithmetic).
 constexpr int EIG_REG_BLOCKS = 20;
+constexpr int EIG_REG_UNBOUNDED = 1;
 template <int EQ> constexpr int eig_mats() { return 32 / EQ; }
 template <int EQ> constexpr int eig_stride() { return 32 / EQ; }
 constexpr double DEPS = 2.220446049250313080847e-16;
@@ -825,8 +831,8 @@ __device__ __forceinline__ void list_if_stable(bool unstable, int64_t c, int* no
     }
 }
 
-template <int EQ, bool RG = false, bool F = false>
-__global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_lina_eig(const Run run, const __grid_constant__ Plant P,
+template <int EQ, bool RG = false, bool F = false, int RB = EIG_REG_BLOCKS>
+__global__ void __launch_bounds__(32, RB) k_lina_eig(const Run run, const __grid_constant__ Plant P,
                                                         const float* __restrict__ gains, float* __restrict__ lina,
                                                         float* __restrict__ eig32, int* __restrict__ nominal,
                                                         int* __restrict__ list, int* __restrict__ count,
@@ -950,8 +956,8 @@ __global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_lina_eig64(const Run run
 // solved, OPEN_A is formed here with LIN_A's own float operations, and the
 // kernel runs concurrently with k_lina_eig (which then lists nothing): the
 // flags of the candidates the modal stage flags are computed but never read.
-template <int EQ, bool RG = false, bool F = false>
-__global__ void __launch_bounds__(32, EIG_REG_BLOCKS) k_nominal(const Run run, const __grid_constant__ Plant P,
+template <int EQ, bool RG = false, bool F = false, int RB = EIG_REG_BLOCKS>
+__global__ void __launch_bounds__(32, RB) k_nominal(const Run run, const __grid_constant__ Plant P,
                                                        const float* __restrict__ gains, const void* __restrict__ lina,
                                                        const int* __restrict__ list, const int* __restrict__ count,
                                                        int* __restrict__ nominal, int fp64_form, int* __restrict__ next) {
@@ -1081,6 +1087,14 @@ static void lina_eig_qf(const Run& run, const Plant& P, int precision, const flo
         k_lina_eig<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, (float*)lina, (float*)eig, nominal, list,
                                                          count, count + 1);
     } else {
+        if constexpr (EQ == 2 && F) {
+            if (run.kalman) {
+                auto* k = k_lina_eig<EQ, false, F, EIG_REG_UNBOUNDED>;
+                set_smem((const void*)k, smem);
+                k<<<grid, 32, smem, st>>>(run, P, gains, (float*)lina, (float*)eig, nominal, list, count, count + 1);
+                return;
+            }
+        }
         set_smem((const void*)k_lina_eig<EQ, false, F>, smem);
         k_lina_eig<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, (float*)lina, (float*)eig, nominal, list,
                                                           count, count + 1);
@@ -1104,6 +1118,15 @@ static void nominal_qf(const Run& run, const Plant& P, int precision, const floa
         k_nominal<EQ, true, F><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, 0,
                                                        const_cast<int*>(count) + 2);
     } else {
+        if constexpr (EQ == 2 && F) {
+            if (run.kalman) {
+                auto* k = k_nominal<EQ, false, F, EIG_REG_UNBOUNDED>;
+                set_smem((const void*)k, smem);
+                k<<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal, precision == CE_PRECISION_FP64,
+                                          const_cast<int*>(count) + 2);
+                return;
+            }
+        }
         set_smem((const void*)k_nominal<EQ, false, F>, smem);
         k_nominal<EQ, false, F><<<grid, 32, smem, st>>>(run, P, gains, lina, list, count, nominal,
                                                         precision == CE_PRECISION_FP64, const_cast<int*>(count) + 2);

@@ -44,3 +44,18 @@ def test_small_batch_lanes_do_not_change_results():
             s.set_tuning(lanes, 0, 0)
             out = s.evaluate(p.cuda_mx, p.info_mx)
             assert np.array_equal(out.view(np.uint32), auto.view(np.uint32)), lanes
+
+
+def test_kalman_session_lanes_do_not_change_results():
+    """Kalman-observer sessions launch their own instantiations of the default eigensolve form
+    (two lanes per matrix, fused arithmetic, no register bound); its rows equal those of the other
+    lane counts."""
+    p = synth.eight_state(n=700, time=1500, freq=80, pool=4, observer="kalman")
+    cfg = ce.EngineConfig.parse(p.config_text)
+    with ce.Session(cfg, p.plant) as s:
+        s.set_tuning(2, 0, 0)
+        two = s.evaluate(p.cuda_mx, p.info_mx)
+        for lanes in (1, 4, 16):
+            s.set_tuning(lanes, 0, 0)
+            out = s.evaluate(p.cuda_mx, p.info_mx)
+            assert np.array_equal(out.view(np.uint32), two.view(np.uint32)), lanes
