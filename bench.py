@@ -742,7 +742,7 @@ def small_bench(steps: int, warmup: int, cpu: bool):
     return res
 
 
-def _kalman_time(p, n: int, steps: int, warmup: int):
+def _kalman_time(p, n: int, steps: int, warmup: int, autotune: bool = True):
     import torch
     import controllerengine_gb300 as ce
     cfg = ce.EngineConfig.parse(p.config_text)
@@ -753,6 +753,9 @@ def _kalman_time(p, n: int, steps: int, warmup: int):
     out = torch.empty_like(info)
     st = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    # the session autotuner picks the launch settings on this batch, as for the headline (untimed)
+    tuning = (sess.autotune(n, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream) if autotune
+              else None)
     for _ in range(warmup):
         sess.evaluate_device(n, g.data_ptr(), info.data_ptr(), out.data_ptr(), stream=st.cuda_stream)
     torch.cuda.synchronize()
@@ -773,12 +776,13 @@ def _kalman_time(p, n: int, steps: int, warmup: int):
     keys, counts = np.unique(p.cuda_mx[:, 2 * cfg.statespace_dim + 1:], axis=0, return_counts=True)
     return {"candidates_per_s": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps,
             "launches_per_step": launches, "stages_ms_per_step": stages, "noise_weight_sets": len(keys),
-            "shared_noise_fraction": float(counts[counts >= 8].sum() / n)}
+            "shared_noise_fraction": float(counts[counts >= 8].sum() / n), "tuning": tuning}
 
 
-def kalman_bench(n: int, steps: int, warmup: int, cpu_seconds: float):
+def kalman_bench(n: int, steps: int, warmup: int, cpu_seconds: float, autotune: bool = True):
     """The eight-state workload with the time-varying Kalman observer (rows [K, L, N, R, Q]):
-    candidates/s of ce_evaluate_device, inputs resident, CUDA events, L2 flushed between steps,
+    candidates/s of ce_evaluate_device at the session autotuner's launch settings (chosen untimed
+    on the batch, as for the headline), inputs resident, CUDA events, L2 flushed between steps,
     with the simulation stage's share.  Twice: noise weights from the 64-set pool the gains were
     designed with (candidates share covariance recursions: the shared-noise form), and with R
     perturbed per candidate by a factor 1 + U[0, 1e-3] (every recursion distinct: the
@@ -786,11 +790,11 @@ def kalman_bench(n: int, steps: int, warmup: int, cpu_seconds: float):
     from controllerengine_gb300 import synth
     p = synth.eight_state(n=n, observer="kalman")
     res = {"workload": f"eight_state with observer = kalman: {n} candidates, T = 10000, F = 400",
-           "pooled_noise": _kalman_time(p, n, steps, warmup)}
+           "pooled_noise": _kalman_time(p, n, steps, warmup, autotune)}
     q = synth.Problem(p.name, p.config_text, p.plant, p.cuda_mx.copy(), p.info_mx)
     rng = np.random.default_rng(17)
     q.cuda_mx[:, 17] *= (1.0 + 1e-3 * rng.random(n)).astype(np.float32)
-    res["distinct_noise"] = _kalman_time(q, n, max(1, steps - 1), 1)
+    res["distinct_noise"] = _kalman_time(q, n, max(1, steps - 1), 1, autotune)
     res["candidates_per_s"] = res["pooled_noise"]["candidates_per_s"]
     if cpu_seconds > 0:
         res["cpu_baseline"] = cpu_baseline(p, cpu_seconds, os.cpu_count() or 1)[0]
@@ -1104,7 +1108,7 @@ def main():
     if rank == 0 and a.uneven_instances > 0:
         line["uneven"] = uneven_bench(a.uneven_instances, 3, 2)
     if rank == 0 and a.kalman_candidates > 0:
-        line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0)
+        line["kalman"] = kalman_bench(a.kalman_candidates, 3, 3, 0.0 if a.no_cpu else 5.0, not a.no_autotune)
     if rank == 0 and a.serve_seconds > 0:
         models = serving_models()
         line["serving"] = serving_bench(models, a.serve_seconds, lanes=a.serve_lanes, max_wait_us=a.serve_max_wait_us,
