@@ -263,12 +263,25 @@ __global__ void __launch_bounds__(FIT_BLOCK) k_fit(const Run run_in, const R* __
         for (int r = 0; r < FIT_ROUNDS; ++r)
 #pragma unroll
             for (int k = 0; k < 16; ++k) acc[r][k] = R(0);
-        for (int w0 = 0; w0 < steps; w0 += CH) {
-            for (int k = lane; k < CH; k += 16) {
-                const int idx = w0 + k;
-                const R yw = (idx < steps && idx < wlimit) ? wrow[idx] : R(0);
-                cb[g][k][nc] = rsub(yw, yss);
+        // the window samples of a chunk are loaded one chunk ahead, so that their
+        // global-memory latency passes under the previous chunk's work
+        constexpr int YL = (CH + 15) / 16;  // samples per lane and chunk
+        auto window = [&](int w0, R (&y)[YL]) {
+#pragma unroll
+            for (int u = 0; u < YL; ++u) {
+                const int k = lane + 16 * u, idx = w0 + k;
+                y[u] = (k < CH && idx < steps && idx < wlimit) ? wrow[idx] : R(0);
             }
+        };
+        R ynext[YL];
+        window(0, ynext);
+        for (int w0 = 0; w0 < steps; w0 += CH) {
+#pragma unroll
+            for (int u = 0; u < YL; ++u) {
+                const int k = lane + 16 * u;
+                if (k < CH) cb[g][k][nc] = rsub(ynext[u], yss);
+            }
+            window(w0 + CH, ynext);
             int s = s0, md = m0;
             for (int k = lane; k < items; k += 16) {
                 const int w = w0 + s;
